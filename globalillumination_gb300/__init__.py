@@ -1,0 +1,20 @@
+"""GB300-native shadow-visibility engine (sm_103a CUDA behind a C ABI).
+
+Covers the shadow-visibility path of MarcioCerqueira/GlobalIllumination:
+light-view depth maps, the G-buffer, per-pixel visibility (hard test, PCF,
+PCSS, RBSM family) and shadow-volume stencil counts.  See shadow.py for the
+technique interface and include/gi_shadow.h for the C ABI.
+"""
+from . import _capi
+from ._capi import GIError
+from .shadow import (Context, Frame, FrameBuffers, MapParams, Scene, ShadowParams, TECHNIQUES, ViewSpec,
+                     allocate_frame, compute_hard_shadows, compute_visibility, frame_setup, poisson_table,
+                     render_frame, render_gbuffer, render_shadow_map, render_soft_shadows,
+                     shadow_volume_counts)
+
+__all__ = [
+    "Context", "Frame", "FrameBuffers", "GIError", "MapParams", "Scene", "ShadowParams", "TECHNIQUES",
+    "ViewSpec", "allocate_frame", "compute_hard_shadows", "compute_visibility", "frame_setup",
+    "poisson_table", "render_frame", "render_gbuffer", "render_shadow_map", "render_soft_shadows",
+    "shadow_volume_counts", "_capi",
+]

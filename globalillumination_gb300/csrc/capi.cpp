@@ -1,0 +1,400 @@
+// capi.cpp -- the C ABI of libgishadow.so: error reporting, contexts,
+// device copies of scenes, frame matrices and the pass entry points.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "host_math.h"
+#include "internal.h"
+#include "raster.h"
+
+namespace {
+thread_local std::string g_last_error;
+
+const int kMaxImage = 16384;  // guard-band fixed point stays in int32 below this
+
+gi_status check_device(gi_context* ctx) {
+    int cur = -1;
+    cudaError_t e = cudaGetDevice(&cur);
+    if (e != cudaSuccess) return gi::fail_cuda(e, "cudaGetDevice");
+    if (cur != ctx->device) {
+        e = cudaSetDevice(ctx->device);
+        if (e != cudaSuccess) return gi::fail_cuda(e, "cudaSetDevice");
+    }
+    return GI_OK;
+}
+}  // namespace
+
+namespace gi {
+
+gi_status fail(gi_status st, const std::string& msg) {
+    g_last_error = msg;
+    return st;
+}
+
+gi_status fail_cuda(int err, const char* what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString((cudaError_t)err);
+    return GI_ERR_CUDA;
+}
+
+gi_status ensure_buffer(void** ptr, size_t* cap, size_t bytes) {
+    if (*cap >= bytes && *ptr) return GI_OK;
+    if (*ptr) {
+        cudaFree(*ptr);
+        *ptr = nullptr;
+        *cap = 0;
+    }
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(GI_ERR_OOM, std::string("cudaMalloc of ") + std::to_string(bytes) +
+                                    " bytes failed: " + cudaGetErrorString(e));
+    }
+    *ptr = p;
+    *cap = bytes;
+    return GI_OK;
+}
+
+}  // namespace gi
+
+using gi::fail;
+
+extern "C" const char* gi_last_error_string(void) { return g_last_error.c_str(); }
+
+extern "C" const char* gi_version(void) { return "gi_shadow 0.1.0 (sm_103a)"; }
+
+extern "C" gi_status gi_context_create(int device, gi_context** out) {
+    if (!out) return fail(GI_ERR_INVALID_ARG, "gi_context_create: out is NULL");
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(GI_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    }
+    if (device < 0 || device >= n) return fail(GI_ERR_INVALID_ARG, "gi_context_create: bad device");
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) return gi::fail_cuda(e, "cudaSetDevice");
+    gi_context* c = new gi_context();
+    c->device = device;
+    e = cudaMalloc(&c->d_status, 16 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, 16 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_status, 16 * sizeof(unsigned));
+    if (e != cudaSuccess) {
+        gi_context_destroy(c);
+        return gi::fail_cuda(e, "gi_context_create allocation");
+    }
+    std::memset(c->h_status, 0, 16 * sizeof(unsigned));
+    *out = c;
+    return GI_OK;
+}
+
+extern "C" void gi_context_destroy(gi_context* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    cudaDeviceSynchronize();
+    cudaFree(c->d_tri_records);
+    cudaFree(c->d_tile_items);
+    cudaFree(c->d_vkeys);
+    cudaFree(c->d_depth_tmp);
+    cudaFree(c->d_counts);
+    cudaFree(c->d_status);
+    if (c->h_status) cudaFreeHost(c->h_status);
+    delete c;
+}
+
+extern "C" uint64_t gi_context_launch_count(const gi_context* c) { return c ? c->launches : 0; }
+
+extern "C" void gi_scene_destroy(gi_scene* s) {
+    if (!s) return;
+    if (s->device >= 0) {
+        cudaSetDevice(s->device);
+        cudaFree(s->d_points);
+        cudaFree(s->d_normals);
+        cudaFree(s->d_indices);
+    }
+    delete s;
+}
+
+extern "C" gi_status gi_scene_upload(gi_scene* s, gi_context* ctx, void* stream) {
+    if (!s || !ctx) return fail(GI_ERR_INVALID_ARG, "gi_scene_upload: NULL argument");
+    gi_status st = check_device(ctx);
+    if (st != GI_OK) return st;
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    const size_t nv = (size_t)s->mesh.num_vertices(), nt = (size_t)s->mesh.num_triangles();
+    if (s->device >= 0 && s->device != ctx->device) {
+        cudaFree(s->d_points);
+        cudaFree(s->d_normals);
+        cudaFree(s->d_indices);
+        s->d_points = s->d_normals = nullptr;
+        s->d_indices = nullptr;
+        s->cap_vertices = s->cap_triangles = 0;
+    }
+    s->device = ctx->device;
+    size_t capv = s->cap_vertices * 3 * sizeof(float), capn = capv;
+    size_t capi = s->cap_triangles * 3 * sizeof(int);
+    st = gi::ensure_buffer(reinterpret_cast<void**>(&s->d_points), &capv, nv * 3 * sizeof(float));
+    if (st == GI_OK)
+        st = gi::ensure_buffer(reinterpret_cast<void**>(&s->d_normals), &capn, nv * 3 * sizeof(float));
+    if (st == GI_OK)
+        st = gi::ensure_buffer(reinterpret_cast<void**>(&s->d_indices), &capi, nt * 3 * sizeof(int));
+    if (st != GI_OK) return st;
+    s->cap_vertices = capv / (3 * sizeof(float));
+    s->cap_triangles = capi / (3 * sizeof(int));
+    cudaError_t e = cudaSuccess;
+    if (nv) {
+        e = cudaMemcpyAsync(s->d_points, s->mesh.points.data(), nv * 3 * sizeof(float),
+                            cudaMemcpyHostToDevice, cs);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s->d_normals, s->mesh.normals.data(), nv * 3 * sizeof(float),
+                                cudaMemcpyHostToDevice, cs);
+    }
+    if (e == cudaSuccess && nt)
+        e = cudaMemcpyAsync(s->d_indices, s->mesh.indices.data(), nt * 3 * sizeof(int),
+                            cudaMemcpyHostToDevice, cs);
+    if (e != cudaSuccess) return gi::fail_cuda(e, "gi_scene_upload copy");
+    s->dev_vertices = (int)nv;
+    s->dev_triangles = (int)nt;
+    return GI_OK;
+}
+
+extern "C" gi_status gi_scene_device_arrays(const gi_scene* s, const float** p, const float** n,
+                                            const int** i) {
+    if (!s) return fail(GI_ERR_INVALID_ARG, "gi_scene_device_arrays: NULL scene");
+    if (p) *p = s->d_points;
+    if (n) *n = s->d_normals;
+    if (i) *i = s->d_indices;
+    return GI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Matrices
+// ---------------------------------------------------------------------------
+static gi_status check_view(const gi_view* v) {
+    if (!v) return fail(GI_ERR_INVALID_ARG, "gi_view is NULL");
+    if (v->width <= 0 || v->height <= 0)
+        return fail(GI_ERR_INVALID_ARG, "gi_view: width/height must be positive");
+    if (!(v->znear > 0.0f) || !(v->zfar > v->znear))
+        return fail(GI_ERR_INVALID_ARG, "gi_view: need 0 < znear < zfar");
+    if (!(v->fovy_deg > 0.0f && v->fovy_deg < 180.0f))
+        return fail(GI_ERR_INVALID_ARG, "gi_view: fovy must be in (0, 180)");
+    return GI_OK;
+}
+
+// MyGLGeometryViewer::configureAmbient (MyGLGeometryViewer.cpp:14-26):
+// perspective(fov, (GLfloat)w / h, zNear, zFar) and lookAt(eye, look, up).
+static void view_mats(const gi_view* v, gi::M4& P, gi::M4& V) {
+    float aspect = (float)v->width / (float)v->height;
+    P = gi::perspective(v->fovy_deg, aspect, v->znear, v->zfar);
+    V = gi::look_at(gi::v3(v->eye[0], v->eye[1], v->eye[2]), gi::v3(v->at[0], v->at[1], v->at[2]),
+                    gi::v3(v->up[0], v->up[1], v->up[2]));
+}
+
+extern "C" gi_status gi_view_matrices(const gi_view* v, float proj[16], float view_m[16]) {
+    gi_status st = check_view(v);
+    if (st != GI_OK) return st;
+    gi::M4 P, V;
+    view_mats(v, P, V);
+    if (proj) gi::store4(P, proj);
+    if (view_m) gi::store4(V, view_m);
+    return GI_OK;
+}
+
+extern "C" gi_status gi_frame_setup(const gi_view* light, const gi_view* camera,
+                                    gi_frame_matrices* out) {
+    gi_status st = check_view(light);
+    if (st == GI_OK) st = check_view(camera);
+    if (st != GI_OK) return st;
+    if (!out) return fail(GI_ERR_INVALID_ARG, "gi_frame_setup: out is NULL");
+    // The model matrix of every pass: identity * translate(0) * rotate(0, x)
+    // * rotate(0, y) * rotate(0, z) (ShadowMapping/src/main.cpp:255-260).
+    gi::M4 model = gi::identity4();
+    model = gi::translate(model, gi::v3(0.0f, 0.0f, 0.0f));
+    model = gi::rotate(model, 0.0f, gi::v3(1, 0, 0));
+    model = gi::rotate(model, 0.0f, gi::v3(0, 1, 0));
+    model = gi::rotate(model, 0.0f, gi::v3(0, 0, 1));
+    gi::M4 LP, LV, CP, CV;
+    view_mats(light, LP, LV);
+    view_mats(camera, CP, CV);
+    // lightMVP = projection * view * model (main.cpp:264).
+    gi::M4 light_mvp = gi::mul(gi::mul(LP, LV), model);
+    // bias matrix (MyGLGeometryViewer.cpp:139-145), lightMVP = bias * lightMVP.
+    gi::M4 bias;
+    std::memset(&bias, 0, sizeof(bias));
+    bias.m[0][0] = 0.5f;
+    bias.m[1][1] = 0.5f;
+    bias.m[2][2] = 0.5f;
+    bias.m[3][0] = 0.5f;
+    bias.m[3][1] = 0.5f;
+    bias.m[3][2] = 0.5f;
+    bias.m[3][3] = 1.0f;
+    gi::M4 biased = gi::mul(bias, light_mvp);
+    // configurePhong (MyGLGeometryViewer.cpp:108-134): mvp, mv, and the
+    // normal matrix latched on the first camera-view call.
+    gi::M4 cam_mvp = gi::mul(gi::mul(CP, CV), model);
+    gi::M4 cam_mv = gi::mul(CV, model);
+    gi::M3 nm = gi::inverse_transpose3(gi::upper3(cam_mv));
+    // lightEye = mat3(rotate(180, (0, 1, 0))) * lightEye (main.cpp:283, 309).
+    gi::M3 r180 = gi::upper3(gi::rotate(gi::identity4(), 180.0f, gi::v3(0, 1, 0)));
+    gi::V3 lp = gi::mul3(r180, gi::v3(light->eye[0], light->eye[1], light->eye[2]));
+    gi::store4(light_mvp, out->light_mvp);
+    gi::store4(biased, out->light_mvp_biased);
+    gi::store4(cam_mvp, out->camera_mvp);
+    gi::store4(cam_mv, out->camera_mv);
+    gi::store3(nm, out->normal_matrix);
+    out->light_position[0] = lp.x;
+    out->light_position[1] = lp.y;
+    out->light_position[2] = lp.z;
+    return GI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Passes
+// ---------------------------------------------------------------------------
+static gi_status check_pass(gi_context* ctx, const gi_scene* s) {
+    if (!ctx) return fail(GI_ERR_INVALID_ARG, "context is NULL");
+    if (!s) return fail(GI_ERR_INVALID_ARG, "scene is NULL");
+    if (s->dev_triangles > 0 && (s->device != ctx->device || !s->d_points))
+        return fail(GI_ERR_INVALID_ARG, "scene is not uploaded to the context's device");
+    if (s->dev_triangles == 0 && s->mesh.num_triangles() > 0)
+        return fail(GI_ERR_INVALID_ARG, "scene has not been uploaded (gi_scene_upload)");
+    return check_device(ctx);
+}
+
+static gi_status check_image(int w, int h, const char* who) {
+    if (w <= 0 || h <= 0 || w > kMaxImage || h > kMaxImage)
+        return fail(GI_ERR_INVALID_ARG, std::string(who) + ": image size must be in [1, 16384]");
+    return GI_OK;
+}
+
+static int small_px_default() { return 128; }
+
+extern "C" gi_status gi_shadow_map(gi_context* ctx, const gi_scene* s, const gi_map_params* mp,
+                                   const float light_mvp[16], float* d_depth, void* stream) {
+    gi_status st = check_pass(ctx, s);
+    if (st != GI_OK) return st;
+    if (!mp || !light_mvp || !d_depth) return fail(GI_ERR_INVALID_ARG, "gi_shadow_map: NULL argument");
+    st = check_image(mp->width, mp->height, "gi_shadow_map");
+    if (st != GI_OK) return st;
+    if (mp->bias_mode < GI_BIAS_NONE || mp->bias_mode > GI_BIAS_POLYGON_OFFSET)
+        return fail(GI_ERR_INVALID_ARG, "gi_shadow_map: bad bias_mode");
+    return gi::raster_depth_map(ctx, s, light_mvp, mp->width, mp->height, mp->bias_mode,
+                                mp->constant_bias, mp->offset_factor, mp->offset_units, d_depth,
+                                small_px_default(), static_cast<cudaStream_t>(stream));
+}
+
+extern "C" gi_status gi_gbuffer(gi_context* ctx, const gi_scene* s, const float camera_mvp[16],
+                                int W, int H, float* d_pos, float* d_nrm, void* stream) {
+    gi_status st = check_pass(ctx, s);
+    if (st != GI_OK) return st;
+    if (!camera_mvp || !d_pos || !d_nrm) return fail(GI_ERR_INVALID_ARG, "gi_gbuffer: NULL argument");
+    st = check_image(W, H, "gi_gbuffer");
+    if (st != GI_OK) return st;
+    if ((size_t)s->dev_triangles >= ((size_t)1 << 29))
+        return fail(GI_ERR_CAPACITY, "gi_gbuffer: more than 2^29 triangles");
+    return gi::raster_gbuffer(ctx, s, camera_mvp, W, H, d_pos, d_nrm, small_px_default(),
+                              static_cast<cudaStream_t>(stream));
+}
+
+extern "C" gi_status gi_vis_params_default(int technique, gi_vis_params* p) {
+    if (!p) return fail(GI_ERR_INVALID_ARG, "gi_vis_params_default: NULL");
+    if (technique < 0 || technique >= GI_TECH_COUNT)
+        return fail(GI_ERR_INVALID_ARG, "gi_vis_params_default: unknown technique");
+    std::memset(p, 0, sizeof(*p));
+    p->technique = technique;
+    p->pretest = GI_PRETEST_REFERENCE;
+    p->shadow_intensity = 0.25f;          // ShadowMapping/src/main.cpp:877
+    p->kernel_order = 7;                  // gaussianFilter->buildGaussianKernel(7), main.cpp:859
+    p->penumbra_size = 1;                 // main.cpp:871
+    p->max_search = 16;                   // main.cpp:872
+    p->depth_threshold = 0.0f;            // Configs key "d"
+    p->blocker_search_size = 7;           // SoftShadowMapping/src/main.cpp:1612
+    p->kernel_size = 15;                  // SoftShadowMapping/src/main.cpp:1613
+    p->light_radius = 8.0f;               // lightSource->getSize()/2 with size 16 (:1614)
+    p->znear = 1.0f;                      // MyGLGeometryViewer.cpp:7
+    p->pcss_min_blocker_depth = 0.99f;    // PlausibleSoftShadow.frag:368
+    p->poisson_blocker_taps = 16;
+    p->poisson_filter_taps = 32;
+    for (int i = 0; i < 4; ++i) {
+        p->light_mvp_biased[i * 5] = 1.0f;
+        p->camera_mv[i * 5] = 1.0f;
+    }
+    for (int i = 0; i < 3; ++i) p->normal_matrix[i * 4] = 1.0f;
+    return GI_OK;
+}
+
+static gi_status check_vis_params(const gi_vis_params* p) {
+    if (p->technique < 0 || p->technique >= GI_TECH_COUNT)
+        return fail(GI_ERR_INVALID_ARG, "gi_visibility: unknown technique");
+    if (p->pretest != GI_PRETEST_REFERENCE && p->pretest != GI_PRETEST_OFF)
+        return fail(GI_ERR_INVALID_ARG, "gi_visibility: bad pretest mode");
+    const int t = p->technique;
+    const bool pcf_loop = t == GI_TECH_PCF || t == GI_TECH_PCF_TRICUBIC || t == GI_TECH_RPCF_SMSR ||
+                          t == GI_TECH_RPCF_CONSERVATIVE || t == GI_TECH_RSMSS;
+    if (pcf_loop) {
+        // The reference's FP32 loops run about (2 * penumbra / step + 1)^2
+        // taps; bound them so a kernel cannot spin for long.
+        if (p->kernel_order < 1 || p->kernel_order > 64 || p->penumbra_size < 1 ||
+            p->penumbra_size > 64)
+            return fail(GI_ERR_INVALID_ARG,
+                        "gi_visibility: kernel_order and penumbra_size must be in [1, 64]");
+    }
+    if (t >= GI_TECH_SMSR_CONSERVATIVE && t <= GI_TECH_RSMSS) {
+        if (p->max_search < 0 || p->max_search > 4096)
+            return fail(GI_ERR_INVALID_ARG, "gi_visibility: max_search must be in [0, 4096]");
+    }
+    if (t == GI_TECH_PCSS_GRID || t == GI_TECH_PCSS_POISSON) {
+        if (p->kernel_size < 1 || p->kernel_size > 63)
+            return fail(GI_ERR_INVALID_ARG, "gi_visibility: kernel_size must be in [1, 63]");
+    }
+    if (t == GI_TECH_PCSS_GRID && (p->blocker_search_size < 1 || p->blocker_search_size > 63))
+        return fail(GI_ERR_INVALID_ARG, "gi_visibility: blocker_search_size must be in [1, 63]");
+    if (t == GI_TECH_PCSS_POISSON &&
+        (p->poisson_blocker_taps < 1 || p->poisson_blocker_taps > 64 ||
+         p->poisson_filter_taps < 1 || p->poisson_filter_taps > 64))
+        return fail(GI_ERR_INVALID_ARG, "gi_visibility: Poisson tap counts must be in [1, 64]");
+    return GI_OK;
+}
+
+extern "C" gi_status gi_visibility(gi_context* ctx, const gi_vis_params* p, const float* d_depth,
+                                   int map_w, int map_h, const float* d_pos, const float* d_nrm,
+                                   float* d_vis, int W, int H, void* stream) {
+    if (!ctx || !p || !d_depth || !d_pos || !d_nrm || !d_vis)
+        return fail(GI_ERR_INVALID_ARG, "gi_visibility: NULL argument");
+    gi_status st = check_image(map_w, map_h, "gi_visibility (map)");
+    if (st == GI_OK) st = check_image(W, H, "gi_visibility");
+    if (st == GI_OK) st = check_vis_params(p);
+    if (st == GI_OK) st = check_device(ctx);
+    if (st != GI_OK) return st;
+    return gi::launch_visibility(ctx, p, d_depth, map_w, map_h, d_pos, d_nrm, d_vis, W, H,
+                                 static_cast<cudaStream_t>(stream));
+}
+
+extern "C" gi_status gi_poisson_table(int n, float* xy) {
+    if (n < 1 || n > 64 || !xy) return fail(GI_ERR_INVALID_ARG, "gi_poisson_table: n in [1, 64]");
+    for (int i = 0; i < n; ++i) {
+        xy[2 * i] = gi::kPoissonDisk[i][0];
+        xy[2 * i + 1] = gi::kPoissonDisk[i][1];
+    }
+    return GI_OK;
+}
+
+extern "C" gi_status gi_shadow_volume_counts(gi_context* ctx, const gi_scene* s,
+                                             const float light_pos[3], float infinity,
+                                             const float camera_mvp[16], int W, int H,
+                                             int depth_func, uint8_t* d_stencil, float* d_depth,
+                                             void* stream) {
+    gi_status st = check_pass(ctx, s);
+    if (st != GI_OK) return st;
+    if (!light_pos || !camera_mvp || !d_stencil)
+        return fail(GI_ERR_INVALID_ARG, "gi_shadow_volume_counts: NULL argument");
+    st = check_image(W, H, "gi_shadow_volume_counts");
+    if (st != GI_OK) return st;
+    if (depth_func != GI_DEPTH_LESS && depth_func != GI_DEPTH_LEQUAL)
+        return fail(GI_ERR_INVALID_ARG, "gi_shadow_volume_counts: bad depth_func");
+    return gi::raster_shadow_volumes(ctx, s, light_pos, infinity, camera_mvp, W, H, depth_func,
+                                     d_stencil, d_depth, small_px_default(),
+                                     static_cast<cudaStream_t>(stream));
+}

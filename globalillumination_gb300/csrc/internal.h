@@ -1,0 +1,87 @@
+// Internal declarations shared by the host C++ and the CUDA translation
+// units of libgishadow.so.  Nothing here is part of the public C ABI.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/gi_shadow.h"
+
+namespace gi {
+
+// Records `msg` as the calling thread's last error and returns `st`.
+gi_status fail(gi_status st, const std::string& msg);
+gi_status fail_cuda(int cuda_err, const char* what);
+
+struct Mesh {
+    std::vector<float> points;   // float[3V]  (Mesh::pointCloud)
+    std::vector<float> normals;  // float[3V]  (Mesh::normalVector)
+    std::vector<int> indices;    // int[3T], 0-based (Mesh::indices)
+    int num_vertices() const { return (int)(points.size() / 3); }
+    int num_triangles() const { return (int)(indices.size() / 3); }
+};
+
+// Mesh::computeNormals (ShadowMapping/src/Mesh.cpp:195-234).
+void compute_normals(Mesh& m);
+// Mesh::scale / translate / rotate (Mesh.cpp:378-429).
+void mesh_scale(Mesh& m, float x, float y, float z);
+void mesh_translate(Mesh& m, float x, float y, float z);
+void mesh_rotate(Mesh& m, float x, float y, float z);
+// Mesh::addObject (Mesh.cpp:47-193).
+void mesh_append(Mesh& dst, const Mesh& src);
+// glmReadOBJ + Mesh::loadOBJFile.
+gi_status read_obj(const char* path, Mesh& out);
+
+}  // namespace gi
+
+struct gi_scene {
+    gi::Mesh mesh;             // committed objects
+    gi::Mesh pending;          // the reference's `temp` object
+    bool has_pending = false;
+    float camera_eye[3] = {0, 0, 0};
+    float camera_at[3] = {0, 0, 0};
+    float light_eye[3] = {0, 0, 0};
+    float light_at[3] = {0, 0, 0};
+    float depth_threshold = 0.0f;
+    float hsm_alpha = 0.0f;
+    float hsm_beta = 0.0f;
+    int num_objects = 0;
+    // device copy (owned)
+    int device = -1;
+    float* d_points = nullptr;
+    float* d_normals = nullptr;
+    int* d_indices = nullptr;
+    size_t cap_vertices = 0;
+    size_t cap_triangles = 0;
+    int dev_vertices = 0;
+    int dev_triangles = 0;
+};
+
+// Device scratch owned by a context.  Buffers only grow.
+struct gi_context {
+    int device = 0;
+    uint64_t launches = 0;
+    // raster work queue (large-triangle tiles) and triangle setup records
+    void* d_tri_records = nullptr;
+    size_t cap_tri_records = 0;
+    void* d_tile_items = nullptr;
+    size_t cap_tile_items = 0;
+    // visibility keys (64-bit depth|primitive) for the G-buffer
+    unsigned long long* d_vkeys = nullptr;
+    size_t cap_vkeys = 0;
+    // prepass depth / stencil counters for shadow volumes
+    float* d_depth_tmp = nullptr;
+    size_t cap_depth_tmp = 0;
+    int* d_counts = nullptr;
+    size_t cap_counts = 0;
+    // status words: [0] error flags, [1] tile-item count, [2] record count,
+    // [3] requested tile items (for diagnostics)
+    unsigned int* d_status = nullptr;
+    unsigned int* h_status = nullptr;  // pinned mirror
+};
+
+namespace gi {
+// Grows a device buffer to at least `bytes` (cudaMalloc). Returns GI_OK or an error.
+gi_status ensure_buffer(void** ptr, size_t* cap, size_t bytes);
+}

@@ -1,0 +1,32 @@
+// Host entry points of the raster and visibility kernels (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "internal.h"
+
+namespace gi {
+
+gi_status launch_fill_u32(gi_context* ctx, unsigned* p, size_t n, unsigned v, cudaStream_t st);
+
+gi_status raster_depth_map(gi_context* ctx, const gi_scene* scene, const float mvp[16], int W,
+                           int H, int bias_mode, float cbias, float factor, float units,
+                           float* d_depth, int small_px, cudaStream_t st);
+
+gi_status raster_gbuffer(gi_context* ctx, const gi_scene* scene, const float mvp[16], int W, int H,
+                         float* d_pos, float* d_nrm, int small_px, cudaStream_t st);
+
+gi_status raster_shadow_volumes(gi_context* ctx, const gi_scene* scene, const float L[3],
+                                float infinity, const float mvp[16], int W, int H, int depth_func,
+                                unsigned char* d_stencil, float* d_depth_out, int small_px,
+                                cudaStream_t st);
+
+gi_status launch_visibility(gi_context* ctx, const gi_vis_params* p, const float* d_depth,
+                            int map_w, int map_h, const float* d_pos, const float* d_nrm,
+                            float* d_vis, int W, int H, cudaStream_t st);
+
+// Progressive best-candidate Poisson-disk sequence in the unit disk
+// (poisson_table.inc); the n-tap table is its first n points.
+extern const float kPoissonDisk[64][2];
+
+}  // namespace gi

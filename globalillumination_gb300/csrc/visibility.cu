@@ -1,0 +1,648 @@
+// visibility.cu -- per-pixel shadow visibility kernels for sm_103a.
+//
+// One thread per camera pixel reads the G-buffer (object position and
+// normal+frontFacing, float4 each) and the light-view depth map, and writes
+// the r channel of the visibility target.  Each technique restates a
+// fragment shader of the reference (paths relative to the reference root):
+//   HARD            ShadowMapping/Shaders/Shadow.frag:240-272 (naive == 1)
+//   PCF             Shadow.frag:86-116 (bilinearPCF: NEAREST taps)
+//   PCF_TRICUBIC    Shadow.frag:41-116 (textureBicubic over NEAREST taps)
+//   PCSS_GRID       SoftShadowMapping/Shaders/SoftShadow/PlausibleSoftShadow.frag
+//                   :166-194, 365-398, 556-563, 605-633
+//   PCSS_POISSON    the same blocker / penumbra / filter structure with
+//                   Poisson-disk taps (no reference counterpart)
+//   SMSR_*, RPCF_*, RSMSS
+//                   ShadowMapping/Shaders/RBSM/{Conservative,NonConservative}SMSR.frag,
+//                   FilteredRBSM.frag
+//   HARD_SOFTAPP    SoftShadowMapping/Shaders/HardShadow/HardShadow.frag:35-58
+// plus the normal-orientation pre-test every one of them runs
+// (Shadow.frag:222-238).  The file is compiled with -fmad=false and IEEE
+// division / square root so each FP32 operation rounds once, in the order
+// written, exactly as the CPU oracle does.
+//
+// Texture fetches are GL_NEAREST with CLAMP_TO_BORDER and border depth 0
+// (MyGLTextureViewer.cpp:3-28): texel (floor(s W), floor(t H)), outside the
+// map (or NaN) reads 0.  Blocks are 32 x 4 pixels so a warp reads one
+// coalesced row segment of the G-buffer and its taps land on neighbouring
+// texels of the map (L1 / L2 hits: a 2048^2 map is 16 MiB and stays in L2).
+#include <cuda_runtime.h>
+
+#include "internal.h"
+#include "raster.h"
+
+namespace gi {
+
+const float kPoissonDisk[64][2] = {
+#include "poisson_table.inc"
+};
+
+namespace vis {
+
+__constant__ float2 c_poisson[64] = {
+#include "poisson_table.inc"
+};
+
+struct V4 {
+    float x, y, z, w;
+};
+struct V2 {
+    float x, y;
+};
+
+__device__ __forceinline__ float gmin(float x, float y) { return y < x ? y : x; }
+__device__ __forceinline__ float gmax(float x, float y) { return x < y ? y : x; }
+__device__ __forceinline__ float gclamp(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
+__device__ __forceinline__ float gmix(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+__device__ __forceinline__ float gfract(float x) { return x - floorf(x); }
+
+struct Ctx {
+    const float* __restrict__ map;
+    int W, H;
+    float fW, fH;
+    float sx, sy;
+    float I;
+};
+
+__device__ __forceinline__ float fetch(const Ctx& c, float s, float t) {
+    float fi = floorf(s * c.fW);
+    float fj = floorf(t * c.fH);
+    if (!(fi >= 0.0f && fi < c.fW && fj >= 0.0f && fj < c.fH)) return 0.0f;
+    return __ldg(c.map + (size_t)(int)fj * c.W + (int)fi);
+}
+
+__device__ __forceinline__ V4 mat4_mul(const float* m, V4 v) {
+    V4 r;
+    r.x = m[0] * v.x + m[4] * v.y + m[8] * v.z + m[12] * v.w;
+    r.y = m[1] * v.x + m[5] * v.y + m[9] * v.z + m[13] * v.w;
+    r.z = m[2] * v.x + m[6] * v.y + m[10] * v.z + m[14] * v.w;
+    r.w = m[3] * v.x + m[7] * v.y + m[11] * v.z + m[15] * v.w;
+    return r;
+}
+
+__device__ __forceinline__ float pretest(const gi_vis_params& p, const Ctx& c, V4 vertex, V4 normal) {
+    if (p.pretest == GI_PRETEST_OFF) return 1.0f;
+    V4 ev = mat4_mul(p.camera_mv, vertex);
+    const float* nm = p.normal_matrix;
+    float nx = nm[0] * normal.x + nm[3] * normal.y + nm[6] * normal.z;
+    float ny = nm[1] * normal.x + nm[4] * normal.y + nm[7] * normal.z;
+    float nz = nm[2] * normal.x + nm[5] * normal.y + nm[8] * normal.z;
+    float inv = 1.0f / sqrtf(nx * nx + ny * ny + nz * nz);
+    nx = nx * inv;
+    ny = ny * inv;
+    nz = nz * inv;
+    float lx = p.light_position[0] - ev.x;
+    float ly = p.light_position[1] - ev.y;
+    float lz = p.light_position[2] - ev.z;
+    float linv = 1.0f / sqrtf(lx * lx + ly * ly + lz * lz);
+    lx = lx * linv;
+    ly = ly * linv;
+    lz = lz * linv;
+    if (!(normal.w != 0.0f)) {
+        nx = nx * -1.0f;
+        ny = ny * -1.0f;
+        nz = nz * -1.0f;
+    }
+    float d = nx * lx + ny * ly + nz * lz;
+    if (gmax(d, 0.0f) == 0.0f) return c.I;
+    return 1.0f;
+}
+
+// ---- Shadow.frag -------------------------------------------------------------
+__device__ float pcf_bilinear(const gi_vis_params& p, const Ctx& c, V4 n) {
+    float incrW = 1.0f / c.fW, incrH = 1.0f / c.fH;
+    float illum = 0.0f;
+    float offset = (float)p.penumbra_size;
+    float step = 2.0f * offset / (float)p.kernel_order;
+    int count = 0;
+    for (float w = -offset; w < offset; w += step)
+        for (float h = -offset; h < offset; h += step) {
+            float d = fetch(c, n.x + w * incrW, n.y + h * incrH);
+            if (n.z <= d) illum = illum + 1.0f;
+            else illum += c.I;
+            count++;
+        }
+    return illum / (float)count;
+}
+
+__device__ __forceinline__ void cubic(float v, float out[4]) {
+    float nn[4] = {1.0f - v, 2.0f - v, 3.0f - v, 4.0f - v};
+    float s[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) s[i] = nn[i] * nn[i] * nn[i];
+    float x = s[0];
+    float y = s[1] - 4.0f * s[0];
+    float z = s[2] - 4.0f * s[1] + 6.0f * s[0];
+    float w = 6.0f - x - y - z;
+    const float k = 1.0f / 6.0f;
+    out[0] = x * k;
+    out[1] = y * k;
+    out[2] = z * k;
+    out[3] = w * k;
+}
+
+__device__ float texture_bicubic(const Ctx& c, float u, float v) {
+    float tsx = c.fW, tsy = c.fH;
+    float itx = 1.0f / tsx, ity = 1.0f / tsy;
+    float tx = u * tsx - 0.5f, ty = v * tsy - 0.5f;
+    float fx = gfract(tx), fy = gfract(ty);
+    tx -= fx;
+    ty -= fy;
+    float xc[4], yc[4];
+    cubic(fx, xc);
+    cubic(fy, yc);
+    float cc[4] = {tx + -0.5f, tx + 1.5f, ty + -0.5f, ty + 1.5f};
+    float s[4] = {xc[0] + xc[1], xc[2] + xc[3], yc[0] + yc[1], yc[2] + yc[3]};
+    float num[4] = {xc[1], xc[3], yc[1], yc[3]};
+    float off[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) off[i] = cc[i] + num[i] / s[i];
+    off[0] *= itx;
+    off[1] *= itx;
+    off[2] *= ity;
+    off[3] *= ity;
+    float s0 = fetch(c, off[0], off[2]);
+    float s1 = fetch(c, off[1], off[2]);
+    float s2 = fetch(c, off[0], off[3]);
+    float s3 = fetch(c, off[1], off[3]);
+    float sx = s[0] / (s[0] + s[1]);
+    float sy = s[2] / (s[2] + s[3]);
+    return gmix(gmix(s3, s2, sx), gmix(s1, s0, sx), sy);
+}
+
+__device__ float pcf_tricubic(const gi_vis_params& p, const Ctx& c, V4 n) {
+    float incrW = 1.0f / c.fW, incrH = 1.0f / c.fH;
+    float illum = 0.0f;
+    float offset = (float)p.penumbra_size;
+    float step = 2.0f * offset / (float)p.kernel_order;
+    int count = 0;
+    for (float w = -offset; w < offset; w += step)
+        for (float h = -offset; h < offset; h += step) {
+            float d = texture_bicubic(c, n.x + w * incrW, n.y + h * incrH);
+            if (n.z <= d) illum = illum + 1.0f;
+            else illum += c.I;
+            count++;
+        }
+    return illum / (float)count;
+}
+
+// ---- PlausibleSoftShadow.frag --------------------------------------------------
+__device__ __forceinline__ float blocker_search_width(const gi_vis_params& p, const Ctx& c) {
+    float R = p.light_radius;
+    if (c.fW <= 1024.0f) return R / c.fW;
+    return R / 1024.0f;
+}
+
+__device__ float avg_blocker_grid(const gi_vis_params& p, const Ctx& c, V4 n) {
+    float avg = 0.0f;
+    int nb = 0;
+    float bsw = blocker_search_width(p, c);
+    float fw = ((float)p.blocker_search_size - 1.0f) * 0.5f;
+    for (int h = (int)(-fw); (float)h <= fw; h++)
+        for (int w = (int)(-fw); (float)w <= fw; w++) {
+            float d = fetch(c, n.x + ((float)w * bsw) / fw, n.y + ((float)h * bsw) / fw);
+            if (n.z > d) {
+                avg += d;
+                nb++;
+            }
+        }
+    return nb == 0 ? 1.0f : avg / (float)nb;
+}
+
+__device__ float avg_blocker_poisson(const gi_vis_params& p, const Ctx& c, V4 n) {
+    float avg = 0.0f;
+    int nb = 0;
+    float bsw = blocker_search_width(p, c);
+    for (int i = 0; i < p.poisson_blocker_taps; ++i) {
+        float2 o = c_poisson[i];
+        float d = fetch(c, n.x + o.x * bsw, n.y + o.y * bsw);
+        if (n.z > d) {
+            avg += d;
+            nb++;
+        }
+    }
+    return nb == 0 ? 1.0f : avg / (float)nb;
+}
+
+__device__ __forceinline__ float penumbra_width(const gi_vis_params& p, float avg, float z) {
+    if (avg < p.pcss_min_blocker_depth) return 0.0f;
+    float pw = ((z - avg) / avg) * p.light_radius;
+    return (p.znear * pw) / z;
+}
+
+__device__ float pcss_filter_grid(const gi_vis_params& p, const Ctx& c, float pw, V4 n) {
+    float illum = 0.0f;
+    int K = p.kernel_size;
+    float step = 2.0f * pw / (float)K;
+    float fw = ((float)K - 1.0f) * 0.5f;
+    if (step <= 0.0f || step >= 1.0f) return 1.0f;
+    for (int h = (int)(-fw); (float)h <= fw; h++)
+        for (int w = (int)(-fw); (float)w <= fw; w++) {
+            float d = fetch(c, n.x + ((float)w * pw) / fw, n.y + ((float)h * pw) / fw);
+            if (n.z <= d) illum = illum + 1.0f;
+            else illum += c.I;
+        }
+    return illum / (float)(K * K);
+}
+
+__device__ float pcss_filter_poisson(const gi_vis_params& p, const Ctx& c, float pw, V4 n) {
+    float illum = 0.0f;
+    int K = p.kernel_size;
+    float step = 2.0f * pw / (float)K;
+    if (step <= 0.0f || step >= 1.0f) return 1.0f;
+    const int nf = p.poisson_filter_taps;
+    for (int j = 0; j < nf; ++j) {
+        float2 o = c_poisson[j];
+        float d = fetch(c, n.x + o.x * pw, n.y + o.y * pw);
+        if (n.z <= d) illum = illum + 1.0f;
+        else illum += c.I;
+    }
+    return illum / (float)nf;
+}
+
+// ---- RBSM/NonConservativeSMSR.frag and FilteredRBSM.frag -----------------------
+__device__ V4 nc_get_disc_all(const Ctx& c, V4 n) {
+    V4 dir = {0, 0, 0, 0};
+    n.x -= c.sx;
+    dir.x = (n.z <= fetch(c, n.x, n.y)) ? 1.0f : 0.0f;
+    n.x += 2.0f * c.sx;
+    dir.y = (n.z <= fetch(c, n.x, n.y)) ? 1.0f : 0.0f;
+    n.x -= c.sx;
+    n.y += c.sy;
+    dir.z = (n.z <= fetch(c, n.x, n.y)) ? 1.0f : 0.0f;
+    n.y -= 2.0f * c.sy;
+    dir.w = (n.z <= fetch(c, n.x, n.y)) ? 1.0f : 0.0f;
+    return dir;
+}
+
+__device__ bool nc_get_disc_type(const Ctx& c, V4 n, V2 dir, float disc_type) {
+    if (dir.x == 0.0f) {
+        n.x -= c.sx;
+        float left = (n.z <= fetch(c, n.x, n.y)) ? 1.0f : 0.0f;
+        if (fabsf(left - disc_type) == 0.0f) return true;
+        n.x += 2.0f * c.sx;
+        float right = (n.z <= fetch(c, n.x, n.y)) ? 1.0f : 0.0f;
+        if (fabsf(right - disc_type) == 0.0f) return true;
+        n.x -= c.sx;
+    }
+    if (dir.y == 0.0f) {
+        n.y += c.sy;
+        float bottom = (n.z <= fetch(c, n.x, n.y)) ? 1.0f : 0.0f;
+        if (fabsf(bottom - disc_type) == 0.0f) return true;
+        n.y -= 2.0f * c.sy;
+        float top = (n.z <= fetch(c, n.x, n.y)) ? 1.0f : 0.0f;
+        if (fabsf(top - disc_type) == 0.0f) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ bool nc_probe(const Ctx& c, float thr, V4& n, V4 dt, float& new_depth,
+                                         float s, float t) {
+    float d = fetch(c, s, t);
+    if (dt.z == 1.0f) {
+        if (fabsf(n.z - d) < thr) {
+            n.z -= thr;
+            new_depth = n.z;
+        }
+    }
+    float v = (n.z <= d) ? 1.0f : 0.0f;
+    return fabsf(v - dt.z) == 0.0f;
+}
+
+__device__ bool nc_get_disc_vec(const Ctx& c, float thr, V4 n, V2 dir, V4 dt, float& new_depth) {
+    V4 rel = n;
+    new_depth = n.z;
+    if (dir.x == 0.0f) {
+        if (dt.x == 0.5f || dt.x == 0.75f) {
+            rel.x = n.x - c.sx;
+            if (nc_probe(c, thr, n, dt, new_depth, rel.x, rel.y)) return true;
+        }
+        if (dt.x == 0.75f || dt.x == 0.25f) {
+            rel.x = n.x + c.sx;
+            if (nc_probe(c, thr, n, dt, new_depth, rel.x, rel.y)) return true;
+        }
+    }
+    if (dir.y == 0.0f) {
+        if (dt.y == 0.5f || dt.y == 0.75f) {
+            rel.y = n.y + c.sy;
+            if (nc_probe(c, thr, n, dt, new_depth, rel.x, rel.y)) return true;
+        }
+        if (dt.y == 0.75f || dt.y == 0.25f) {
+            rel.y = n.y - c.sy;
+            if (nc_probe(c, thr, n, dt, new_depth, rel.x, rel.y)) return true;
+        }
+    }
+    return false;
+}
+
+__device__ float nc_disc_length(const gi_vis_params& p, const Ctx& c, V4 in_disc, V4 lc, V2 dir,
+                                float sub) {
+    V4 cc = lc;
+    float found = 0.0f;
+    float dist = 0.0f;
+    float new_depth = 0.0f;
+    V2 st = {dir.x * c.sx, dir.y * c.sy};
+    cc.x += st.x;
+    cc.y += st.y;
+    const float thr = p.depth_threshold;
+    for (int it = 0; it < p.max_search; it++) {
+        float d = fetch(c, cc.x, cc.y);
+        if (in_disc.z == 0.0f)
+            if (fabsf(cc.z - d) < thr) cc.z -= thr;
+        float center = (cc.z <= d) ? 1.0f : 0.0f;
+        if (fabsf(center - in_disc.z) == 0.0f) {
+            bool has = nc_get_disc_type(c, cc, V2{0.0f, 0.0f}, in_disc.z);
+            found = has ? 1.0f : 0.0f;
+            break;
+        } else {
+            bool has = nc_get_disc_vec(c, thr, cc, dir, in_disc, new_depth);
+            if (!has) break;
+        }
+        dist = dist + 1.0f;
+        cc.x += st.x;
+        cc.y += st.y;
+        if (in_disc.z == 1.0f) cc.z = new_depth;
+    }
+    float a = dist + (1.0f - sub);
+    return gmix(-a, a, found);
+}
+
+__device__ __forceinline__ float nc_rel_pos(const gi_vis_params& p, V2 dir, float shadow,
+                                            bool filtered) {
+    float T = 1.0f;
+    if (dir.x < 0.0f && dir.y < 0.0f) T = 0.0f;
+    if (dir.x > 0.0f && dir.y > 0.0f) T = -2.0f;
+    float edge_len = gmin(fabsf(dir.x) + fabsf(dir.y), (float)p.max_search);
+    if (filtered) return (T * fabsf(gmax(T * dir.x, T * dir.y))) / edge_len;
+    return (gmax(T, 2.0f * shadow - 1.0f) * fabsf(gmax(T * dir.x, T * dir.y))) / edge_len;
+}
+
+__device__ __forceinline__ float nc_revectorize(V2 r, float shadow, bool filtered) {
+    if (filtered) {
+        if (r.x * r.y < 0.0f) return (1.0f - shadow) + (2.0f * shadow - 1.0f) * gmax(r.x, r.y);
+        else if (r.x * r.y == 0.0f) return shadow;
+        return gclamp((1.0f - shadow) + (2.0f * shadow - 1.0f) * (r.x + r.y), 0.0f, 1.0f);
+    }
+    if ((r.x * r.y == 2.0f * shadow) ||
+        ((fabsf(r.x) * fabsf(r.y) > 0.0f) &&
+         ((1.0f - shadow) + (2.0f * shadow - 1.0f) * (fabsf(r.x) + fabsf(r.y)) < 0.5f)))
+        return 0.0f;
+    return 1.0f;
+}
+
+__device__ __forceinline__ V4 nc_compute_disc(const Ctx& c, V4 n, float dist) {
+    float center = (n.z <= dist) ? 1.0f : 0.0f;
+    float disc_type = 1.0f - center;
+    V4 dir = nc_get_disc_all(c, n);
+    float dx = fabsf(dir.x - center), dy = fabsf(dir.y - center);
+    float dz = fabsf(dir.z - center), dw = fabsf(dir.w - center);
+    return V4{(2.0f * dx + dy) / 4.0f, (2.0f * dz + dw) / 4.0f, disc_type, 1.0f};
+}
+
+__device__ float nc_revectorized_tap(const gi_vis_params& p, const Ctx& c, V4 n, V4 disc,
+                                     float shadow, bool filtered) {
+    V2 sub = {gfract(n.x * c.fW), gfract(n.y * c.fH)};
+    float l = nc_disc_length(p, c, disc, n, V2{-1.0f, 0.0f}, 1.0f - sub.x);
+    float r = nc_disc_length(p, c, disc, n, V2{1.0f, 0.0f}, sub.x);
+    float d = nc_disc_length(p, c, disc, n, V2{0.0f, -1.0f}, 1.0f - sub.y);
+    float u = nc_disc_length(p, c, disc, n, V2{0.0f, 1.0f}, sub.y);
+    V2 rr = {nc_rel_pos(p, V2{l, r}, shadow, filtered), nc_rel_pos(p, V2{d, u}, shadow, filtered)};
+    return gmix(nc_revectorize(rr, shadow, filtered), 1.0f, c.I);
+}
+
+__device__ float nc_smsr(const gi_vis_params& p, const Ctx& c, V4 n) {
+    float dist = fetch(c, n.x, n.y);
+    V4 disc = nc_compute_disc(c, n, dist);
+    float shadow = (n.z <= dist) ? 1.0f : 0.0f;
+    if (disc.x > 0.0f || disc.y > 0.0f) {
+        if (disc.x == 0.75f && disc.y == 0.75f) return gmix(1.0f - shadow, 1.0f, c.I);
+        return nc_revectorized_tap(p, c, n, disc, shadow, false);
+    }
+    return gmix(shadow, 1.0f, c.I);
+}
+
+__device__ float nc_rpcf(const gi_vis_params& p, const Ctx& c, V4 n, bool filtered) {
+    float incrW = 1.0f / c.fW, incrH = 1.0f / c.fH;
+    float illum = 0.0f;
+    float offset = (float)p.penumbra_size;
+    float step = 2.0f * offset / (float)p.kernel_order;
+    int count = 0;
+    for (float w = -offset; w <= offset; w += step)
+        for (float h = -offset; h <= offset; h += step) {
+            V4 s = {n.x + w * incrW, n.y + h * incrH, n.z, n.w};
+            float d = fetch(c, s.x, s.y);
+            float shadow = (s.z <= d) ? 1.0f : 0.0f;
+            V4 disc = nc_compute_disc(c, s, d);
+            if (disc.x > 0.0f || disc.y > 0.0f) {
+                illum += nc_revectorized_tap(p, c, s, disc, shadow, filtered);
+            } else {
+                shadow = gmix(shadow, 1.0f, c.I);
+                illum += shadow;
+            }
+            count++;
+        }
+    return illum / (float)count;
+}
+
+// ---- RBSM/ConservativeSMSR.frag ---------------------------------------------------
+__device__ __forceinline__ V4 cs_compute_disc(const Ctx& c, V4 s) {
+    V4 dir = {0, 0, 0, 0};
+    s.x -= c.sx;
+    dir.x = (s.z <= fetch(c, s.x, s.y)) ? 1.0f : 0.0f;
+    s.x += 2.0f * c.sx;
+    dir.y = (s.z <= fetch(c, s.x, s.y)) ? 1.0f : 0.0f;
+    s.x -= c.sx;
+    s.y += c.sy;
+    dir.z = (s.z <= fetch(c, s.x, s.y)) ? 1.0f : 0.0f;
+    s.y -= 2.0f * c.sy;
+    dir.w = (s.z <= fetch(c, s.x, s.y)) ? 1.0f : 0.0f;
+    return V4{fabsf(dir.x - 1.0f), fabsf(dir.y - 1.0f), fabsf(dir.z - 1.0f), fabsf(dir.w - 1.0f)};
+}
+
+__device__ float cs_rel_dist(const gi_vis_params& p, const Ctx& c, V4 s, V2 dir, float cc) {
+    V4 t = s;
+    float found = 0.0f, distance = 0.0f;
+    V2 st = {dir.x * c.sx, dir.y * c.sy};
+    t.x += st.x;
+    t.y += st.y;
+    const float thr = p.depth_threshold;
+    for (int it = 0; it < p.max_search; it++) {
+        float d = fetch(c, t.x, t.y);
+        if (fabsf(t.z - d) < thr) t.z -= thr;
+        float center = (t.z <= d) ? 1.0f : 0.0f;
+        bool umbra = !(center != 0.0f);
+        if (umbra) {
+            found = 1.0f;
+            break;
+        } else {
+            V4 dd = cs_compute_disc(c, t);
+            if ((dd.x + dd.y + dd.z + dd.w) == 0.0f) break;
+        }
+        distance = distance + 1.0f;
+        t.x += st.x;
+        t.y += st.y;
+    }
+    distance = distance + (1.0f - cc);
+    return gmix(-distance, distance, found);
+}
+
+__device__ __forceinline__ float cs_normalize(const gi_vis_params& p, V2 d) {
+    float T = 1.0f;
+    if (d.x < 0.0f && d.y < 0.0f) T = 0.0f;
+    if (d.x > 0.0f && d.y > 0.0f) T = -2.0f;
+    float len = gmin(fabsf(d.x) + fabsf(d.y), (float)p.max_search);
+    return fabsf(gmax(T * d.x, T * d.y)) / len;
+}
+
+__device__ float cs_revectorized(const gi_vis_params& p, const Ctx& c, V4 s) {
+    V2 sub = {gfract(s.x * c.fW), gfract(s.y * c.fH)};
+    float dl = cs_rel_dist(p, c, s, V2{-1.0f, 0.0f}, 1.0f - sub.x);
+    float dr = cs_rel_dist(p, c, s, V2{1.0f, 0.0f}, sub.x);
+    float db = cs_rel_dist(p, c, s, V2{0.0f, -1.0f}, 1.0f - sub.y);
+    float dt = cs_rel_dist(p, c, s, V2{0.0f, 1.0f}, sub.y);
+    V2 r = {cs_normalize(p, V2{dl, dr}), cs_normalize(p, V2{db, dt})};
+    if ((r.x * r.y > 0.0f) && (1.0f - r.x > r.y)) return c.I;
+    return 1.0f;
+}
+
+__device__ float cs_smsr(const gi_vis_params& p, const Ctx& c, V4 s) {
+    float d = fetch(c, s.x, s.y);
+    float shadow = (s.z <= d) ? 1.0f : 0.0f;
+    if (shadow == 0.0f) return c.I;
+    V4 dd = cs_compute_disc(c, s);
+    if ((dd.x + dd.y + dd.z + dd.w) == 0.0f) return 1.0f;
+    else if ((dd.x + dd.y) == 2.0f || (dd.z + dd.w) == 2.0f) return c.I;
+    return cs_revectorized(p, c, s);
+}
+
+__device__ float cs_rpcf(const gi_vis_params& p, const Ctx& c, V4 n) {
+    float incrW = 1.0f / c.fW, incrH = 1.0f / c.fH;
+    float illum = 0.0f;
+    float offset = (float)p.penumbra_size;
+    float step = 2.0f * offset / (float)p.kernel_order;
+    int count = 0;
+    for (float w = -offset; w <= offset; w += step)
+        for (float h = -offset; h <= offset; h += step) {
+            float d = fetch(c, n.x + w * incrW, n.y + h * incrH);
+            float shadow = (n.z <= d) ? 1.0f : c.I;
+            if (shadow == 1.0f) {
+                V4 s = {n.x + w * incrW, n.y + h * incrH, n.z, n.w};
+                V4 dd = cs_compute_disc(c, s);
+                if (dd.x == 0.0f && dd.y == 0.0f) illum = illum + 1.0f;
+                else illum += cs_revectorized(p, c, s);
+            } else {
+                illum += c.I;
+            }
+            count++;
+        }
+    return illum / (float)count;
+}
+
+template <int TECH>
+__device__ __forceinline__ float shade(const gi_vis_params& p, const Ctx& c, V4 vertex, V4 normal) {
+    if (vertex.x == 0.0f) return 0.0f;
+    V4 sc = mat4_mul(p.light_mvp_biased, vertex);
+    V4 n = {sc.x / sc.w, sc.y / sc.w, sc.z / sc.w, sc.w / sc.w};
+    float shadow = pretest(p, c, vertex, normal);
+    if (TECH == GI_TECH_HARD) {
+        if (sc.w > 0.0f && shadow == 1.0f) {
+            float d = fetch(c, n.x, n.y);
+            shadow = (n.z <= d) ? 1.0f : c.I;
+        }
+    } else if (TECH == GI_TECH_PCF) {
+        if (sc.w > 0.0f && shadow == 1.0f) shadow = pcf_bilinear(p, c, n);
+    } else if (TECH == GI_TECH_PCF_TRICUBIC) {
+        if (sc.w > 0.0f && shadow == 1.0f) shadow = pcf_tricubic(p, c, n);
+    } else if (TECH == GI_TECH_PCSS_GRID) {
+        if (sc.w > 0.0f && shadow == 1.0f) {
+            float avg = avg_blocker_grid(p, c, n);
+            float pw = penumbra_width(p, avg, n.z);
+            shadow = pcss_filter_grid(p, c, pw, n);
+        }
+    } else if (TECH == GI_TECH_PCSS_POISSON) {
+        if (sc.w > 0.0f && shadow == 1.0f) {
+            float avg = avg_blocker_poisson(p, c, n);
+            float pw = penumbra_width(p, avg, n.z);
+            shadow = pcss_filter_poisson(p, c, pw, n);
+        }
+    } else if (TECH == GI_TECH_SMSR_NONCONSERVATIVE) {
+        if (shadow == 1.0f) shadow = nc_smsr(p, c, n);
+    } else if (TECH == GI_TECH_RPCF_SMSR) {
+        if (shadow == 1.0f) shadow = nc_rpcf(p, c, n, false);
+    } else if (TECH == GI_TECH_RSMSS) {
+        if (shadow == 1.0f) shadow = nc_rpcf(p, c, n, true);
+    } else if (TECH == GI_TECH_SMSR_CONSERVATIVE) {
+        if (shadow == 1.0f) shadow = cs_smsr(p, c, n);
+    } else if (TECH == GI_TECH_RPCF_CONSERVATIVE) {
+        if (shadow == 1.0f) shadow = cs_rpcf(p, c, n);
+    } else if (TECH == GI_TECH_HARD_SOFTAPP) {
+        float r = shadow;
+        if (sc.w > 0.0f && r == 1.0f) {
+            float d = fetch(c, n.x, n.y);
+            r = (n.z <= d) ? 1.0f : c.I;
+        }
+        if (pretest(p, c, vertex, normal) == c.I) r = 0.0f;
+        shadow = r;
+    }
+    return shadow;
+}
+
+template <int TECH>
+__global__ void __launch_bounds__(128) k_visibility(const gi_vis_params p,
+                                                    const float* __restrict__ map, int map_w,
+                                                    int map_h, const float4* __restrict__ pos,
+                                                    const float4* __restrict__ nrm,
+                                                    float* __restrict__ out, int W, int H) {
+    int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    int y = blockIdx.y * 4 + (threadIdx.x >> 5);
+    if (x >= W || y >= H) return;
+    Ctx c;
+    c.map = map;
+    c.W = map_w;
+    c.H = map_h;
+    c.fW = (float)map_w;
+    c.fH = (float)map_h;
+    c.sx = (float)(1.0 / (double)map_w);
+    c.sy = (float)(1.0 / (double)map_h);
+    c.I = p.shadow_intensity;
+    size_t i = (size_t)y * W + x;
+    float4 pv = __ldcs(pos + i);
+    float4 nv = __ldcs(nrm + i);
+    V4 vertex = {pv.x, pv.y, pv.z, pv.w};
+    V4 normal = {nv.x, nv.y, nv.z, nv.w};
+    __stcs(out + i, shade<TECH>(p, c, vertex, normal));
+}
+
+}  // namespace vis
+
+gi_status launch_visibility(gi_context* ctx, const gi_vis_params* p, const float* d_depth,
+                            int map_w, int map_h, const float* d_pos, const float* d_nrm,
+                            float* d_vis, int W, int H, cudaStream_t st) {
+    dim3 grid((W + 31) / 32, (H + 3) / 4);
+    const float4* pos = reinterpret_cast<const float4*>(d_pos);
+    const float4* nrm = reinterpret_cast<const float4*>(d_nrm);
+#define GI_VIS_CASE(T)                                                                     \
+    case T:                                                                                \
+        vis::k_visibility<T><<<grid, 128, 0, st>>>(*p, d_depth, map_w, map_h, pos, nrm, d_vis, W, H); \
+        break;
+    switch (p->technique) {
+        GI_VIS_CASE(GI_TECH_HARD)
+        GI_VIS_CASE(GI_TECH_PCF)
+        GI_VIS_CASE(GI_TECH_PCF_TRICUBIC)
+        GI_VIS_CASE(GI_TECH_PCSS_GRID)
+        GI_VIS_CASE(GI_TECH_PCSS_POISSON)
+        GI_VIS_CASE(GI_TECH_SMSR_CONSERVATIVE)
+        GI_VIS_CASE(GI_TECH_SMSR_NONCONSERVATIVE)
+        GI_VIS_CASE(GI_TECH_RPCF_CONSERVATIVE)
+        GI_VIS_CASE(GI_TECH_RPCF_SMSR)
+        GI_VIS_CASE(GI_TECH_RSMSS)
+        GI_VIS_CASE(GI_TECH_HARD_SOFTAPP)
+        default:
+            return fail(GI_ERR_INVALID_ARG, "gi_visibility: unknown technique");
+    }
+#undef GI_VIS_CASE
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "visibility kernel launch");
+}
+
+}  // namespace gi

@@ -1,0 +1,386 @@
+"""Host-side mirror of the reference's shadow technique interface.
+
+The reference drives its passes from GLUT callbacks
+(ShadowMapping/src/main.cpp:459-472 display(), SoftShadowMapping/src/main.cpp
+:925-1022 renderSoftShadows(), ShadowVolumes/src/main.cpp:120-206) and keeps
+the technique choice in a ShadowParams struct
+(ShadowMapping/include/Viewers/ShadowParams.h:6-37,
+SoftShadowMapping/include/Viewers/ShadowParams.h:6-69) set from menus.  This
+module keeps those names and meanings on top of the C ABI of libgishadow.so:
+
+  Scene                 SceneLoader + Mesh (Configs/<name>.txt and OBJ files)
+  ShadowParams          the parameter block, with the technique as an enum
+  render_shadow_map     renderShadowMap / displaySceneFromLightPOV
+  render_gbuffer        renderGBuffer
+  compute_hard_shadows  computeHardShadows (visibility into a float buffer)
+  render_soft_shadows   renderSoftShadows (G-buffer, light map, PCSS)
+  shadow_volume_counts  the ShadowVolumes stencil passes
+
+Device buffers are torch CUDA tensors (torch provides memory and streams
+only; all the work runs in the library's own kernels).  Every call raises
+GIError on failure; nothing falls back to a CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _capi as api
+from ._capi import check
+
+
+def _lib():
+    return api.load()
+
+
+def _f3(v) -> api.F3:
+    return api.F3(*[float(x) for x in v])
+
+
+def _f16(m) -> api.F16:
+    a = np.asarray(m, dtype=np.float32).reshape(-1)
+    return api.F16(*[float(x) for x in a])
+
+
+def _stream_ptr(stream) -> C.c_void_p:
+    if stream is None:
+        import torch
+        stream = torch.cuda.current_stream()
+    return C.c_void_p(int(stream.cuda_stream) if hasattr(stream, "cuda_stream") else int(stream))
+
+
+def _ptr(t) -> C.c_void_p:
+    return C.c_void_p(int(t.data_ptr()))
+
+
+class Context:
+    """Owns the scratch memory of the passes on one CUDA device."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        check(_lib().gi_context_create(int(device), C.byref(h)), "gi_context_create")
+        self.handle = h
+        self.device = int(device)
+
+    @property
+    def launch_count(self) -> int:
+        return int(_lib().gi_context_launch_count(self.handle))
+
+    def close(self) -> None:
+        if self.handle:
+            _lib().gi_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Scene:
+    """Scene geometry with the SceneLoader / Mesh semantics of the reference."""
+
+    def __init__(self, handle: C.c_void_p | None = None):
+        if handle is None:
+            handle = C.c_void_p()
+            check(_lib().gi_scene_create(C.byref(handle)), "gi_scene_create")
+        self.handle = handle
+
+    @classmethod
+    def from_config(cls, cfg_path: str, base_dir: str | None = None) -> "Scene":
+        h = C.c_void_p()
+        check(_lib().gi_scene_load_config(cfg_path.encode(), base_dir.encode() if base_dir else None,
+                                          C.byref(h)), "gi_scene_load_config")
+        return cls(h)
+
+    # config keys o / s / t / r / +
+    def load_obj(self, path: str) -> "Scene":
+        check(_lib().gi_scene_object_load_obj(self.handle, path.encode()), "load_obj")
+        return self
+
+    def object_from_arrays(self, points, indices) -> "Scene":
+        p = np.ascontiguousarray(points, dtype=np.float32).reshape(-1)
+        i = np.ascontiguousarray(indices, dtype=np.int32).reshape(-1)
+        check(_lib().gi_scene_object_from_arrays(self.handle, p.ctypes.data, p.size // 3, i.ctypes.data,
+                                                 i.size // 3), "object_from_arrays")
+        return self
+
+    def scale(self, x, y, z) -> "Scene":
+        check(_lib().gi_scene_object_scale(self.handle, x, y, z), "scale")
+        return self
+
+    def translate(self, x, y, z) -> "Scene":
+        check(_lib().gi_scene_object_translate(self.handle, x, y, z), "translate")
+        return self
+
+    def rotate(self, x, y, z) -> "Scene":
+        check(_lib().gi_scene_object_rotate(self.handle, x, y, z), "rotate")
+        return self
+
+    def commit(self) -> "Scene":
+        check(_lib().gi_scene_object_commit(self.handle), "commit")
+        return self
+
+    # procedural objects
+    def ground(self, half_size: float, y: float = 0.0) -> "Scene":
+        check(_lib().gi_gen_ground(self.handle, half_size, y), "gi_gen_ground")
+        return self.commit()
+
+    def uv_sphere(self, slices: int, stacks: int, radius: float, centre) -> "Scene":
+        check(_lib().gi_gen_uv_sphere(self.handle, slices, stacks, radius, _f3(centre)), "gi_gen_uv_sphere")
+        return self.commit()
+
+    def icosphere(self, level: int, radius: float, centre) -> "Scene":
+        check(_lib().gi_gen_icosphere(self.handle, level, radius, _f3(centre)), "gi_gen_icosphere")
+        return self.commit()
+
+    def displaced_sphere(self, slices: int, stacks: int, radius: float, amplitude: float, centre,
+                         seed: int) -> "Scene":
+        check(_lib().gi_gen_displaced_sphere(self.handle, slices, stacks, radius, amplitude, _f3(centre),
+                                             int(seed)), "gi_gen_displaced_sphere")
+        return self.commit()
+
+    def icosphere_field(self, count: int, level: int, lo, hi, rmin: float, rmax: float,
+                        seed: int) -> "Scene":
+        check(_lib().gi_gen_icosphere_field(self.handle, count, level, _f3(lo), _f3(hi), rmin, rmax,
+                                            int(seed)), "gi_gen_icosphere_field")
+        return self
+
+    def set_views(self, camera_eye, camera_at, light_eye, light_at, depth_threshold=0.0) -> "Scene":
+        check(_lib().gi_scene_set_views(self.handle, _f3(camera_eye), _f3(camera_at), _f3(light_eye),
+                                        _f3(light_at), float(depth_threshold)), "gi_scene_set_views")
+        return self
+
+    def info(self) -> api.SceneInfo:
+        out = api.SceneInfo()
+        check(_lib().gi_scene_get_info(self.handle, C.byref(out)), "gi_scene_get_info")
+        return out
+
+    def arrays(self):
+        """(points float32[V,3], normals float32[V,3], indices int32[T,3])."""
+        inf = self.info()
+        p = np.empty((inf.num_vertices, 3), np.float32)
+        n = np.empty((inf.num_vertices, 3), np.float32)
+        i = np.empty((inf.num_triangles, 3), np.int32)
+        check(_lib().gi_scene_get_arrays(self.handle, p.ctypes.data, n.ctypes.data, i.ctypes.data),
+              "gi_scene_get_arrays")
+        return p, n, i
+
+    def upload(self, ctx: Context, stream=None) -> "Scene":
+        check(_lib().gi_scene_upload(self.handle, ctx.handle, _stream_ptr(stream)), "gi_scene_upload")
+        return self
+
+    def close(self) -> None:
+        if self.handle:
+            _lib().gi_scene_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class ViewSpec:
+    """Eye / look / up plus the projection configureAmbient builds."""
+    eye: tuple
+    at: tuple
+    width: int
+    height: int
+    fovy_deg: float = 45.0
+    znear: float = 1.0
+    zfar: float = 1000.0
+    up: tuple = (0.0, 0.0, 1.0)
+
+    def to_c(self) -> api.View:
+        return api.View(_f3(self.eye), _f3(self.at), _f3(self.up), self.fovy_deg, self.znear, self.zfar,
+                        int(self.width), int(self.height))
+
+
+@dataclass
+class Frame:
+    light_mvp: np.ndarray
+    light_mvp_biased: np.ndarray
+    camera_mvp: np.ndarray
+    camera_mv: np.ndarray
+    normal_matrix: np.ndarray
+    light_position: np.ndarray
+
+
+def frame_setup(light: ViewSpec, camera: ViewSpec) -> Frame:
+    out = api.FrameMatrices()
+    lv, cv = light.to_c(), camera.to_c()
+    check(_lib().gi_frame_setup(C.byref(lv), C.byref(cv), C.byref(out)), "gi_frame_setup")
+    f = lambda a, n: np.frombuffer(bytes(a), dtype=np.float32, count=n).copy()
+    return Frame(f(out.light_mvp, 16), f(out.light_mvp_biased, 16), f(out.camera_mvp, 16),
+                 f(out.camera_mv, 16), f(out.normal_matrix, 9), f(out.light_position, 3))
+
+
+@dataclass
+class MapParams:
+    width: int
+    height: int
+    bias_mode: int = api.GI_BIAS_POLYGON_OFFSET
+    constant_bias: float = 0.0
+    offset_factor: float = 4.0
+    offset_units: float = 20.0
+
+    def to_c(self) -> api.MapParams:
+        return api.MapParams(self.width, self.height, self.bias_mode, self.constant_bias,
+                             self.offset_factor, self.offset_units)
+
+
+TECHNIQUES = {
+    "hard": api.GI_TECH_HARD,
+    "pcf": api.GI_TECH_PCF,
+    "pcf_tricubic": api.GI_TECH_PCF_TRICUBIC,
+    "pcss_grid": api.GI_TECH_PCSS_GRID,
+    "pcss_poisson": api.GI_TECH_PCSS_POISSON,
+    "smsr_conservative": api.GI_TECH_SMSR_CONSERVATIVE,
+    "smsr_nonconservative": api.GI_TECH_SMSR_NONCONSERVATIVE,
+    "rpcf_conservative": api.GI_TECH_RPCF_CONSERVATIVE,
+    "rpcf_smsr": api.GI_TECH_RPCF_SMSR,
+    "rsmss": api.GI_TECH_RSMSS,
+    "hard_softapp": api.GI_TECH_HARD_SOFTAPP,
+}
+
+
+@dataclass
+class ShadowParams:
+    """ShadowParams of the reference with the technique as one enum value."""
+    technique: int = api.GI_TECH_HARD
+    shadow_intensity: float = 0.25
+    kernel_order: int = 7
+    penumbra_size: int = 1
+    max_search: int = 16
+    depth_threshold: float = 0.0
+    blocker_search_size: int = 7
+    kernel_size: int = 15
+    light_radius: float = 8.0
+    znear: float = 1.0
+    pcss_min_blocker_depth: float = 0.99
+    poisson_blocker_taps: int = 16
+    poisson_filter_taps: int = 32
+    pretest: int = api.GI_PRETEST_REFERENCE
+
+    @classmethod
+    def defaults(cls, technique: int) -> "ShadowParams":
+        p = api.VisParams()
+        check(_lib().gi_vis_params_default(int(technique), C.byref(p)), "gi_vis_params_default")
+        return cls(technique=p.technique, shadow_intensity=p.shadow_intensity, kernel_order=p.kernel_order,
+                   penumbra_size=p.penumbra_size, max_search=p.max_search, depth_threshold=p.depth_threshold,
+                   blocker_search_size=p.blocker_search_size, kernel_size=p.kernel_size,
+                   light_radius=p.light_radius, znear=p.znear, pcss_min_blocker_depth=p.pcss_min_blocker_depth,
+                   poisson_blocker_taps=p.poisson_blocker_taps, poisson_filter_taps=p.poisson_filter_taps,
+                   pretest=p.pretest)
+
+    def to_c(self, frame: Frame) -> api.VisParams:
+        p = api.VisParams()
+        p.technique = int(self.technique)
+        p.pretest = int(self.pretest)
+        p.shadow_intensity = self.shadow_intensity
+        p.kernel_order = self.kernel_order
+        p.penumbra_size = self.penumbra_size
+        p.max_search = self.max_search
+        p.depth_threshold = self.depth_threshold
+        p.blocker_search_size = self.blocker_search_size
+        p.kernel_size = self.kernel_size
+        p.light_radius = self.light_radius
+        p.znear = self.znear
+        p.pcss_min_blocker_depth = self.pcss_min_blocker_depth
+        p.poisson_blocker_taps = self.poisson_blocker_taps
+        p.poisson_filter_taps = self.poisson_filter_taps
+        C.memmove(p.light_mvp_biased, frame.light_mvp_biased.astype(np.float32).tobytes(), 64)
+        C.memmove(p.camera_mv, frame.camera_mv.astype(np.float32).tobytes(), 64)
+        C.memmove(p.normal_matrix, frame.normal_matrix.astype(np.float32).tobytes(), 36)
+        C.memmove(p.light_position, frame.light_position.astype(np.float32).tobytes(), 12)
+        return p
+
+
+def poisson_table(n: int) -> np.ndarray:
+    out = np.empty((n, 2), np.float32)
+    check(_lib().gi_poisson_table(int(n), out.ctypes.data), "gi_poisson_table")
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Passes (device tensors in, device tensors out; stream-ordered)
+# ---------------------------------------------------------------------------
+def render_shadow_map(ctx: Context, scene: Scene, mp: MapParams, light_mvp, depth, stream=None):
+    """renderShadowMap: depth is a float32 CUDA tensor of mp.height * mp.width."""
+    assert depth.is_cuda and depth.dtype.itemsize == 4 and depth.numel() >= mp.width * mp.height
+    c = mp.to_c()
+    check(_lib().gi_shadow_map(ctx.handle, scene.handle, C.byref(c), _f16(light_mvp), _ptr(depth),
+                               _stream_ptr(stream)), "gi_shadow_map")
+    return depth
+
+
+def render_gbuffer(ctx: Context, scene: Scene, camera_mvp, width: int, height: int, pos, nrm, stream=None):
+    """renderGBuffer: pos / nrm are float32 CUDA tensors of height * width * 4."""
+    n = width * height * 4
+    assert pos.is_cuda and nrm.is_cuda and pos.numel() >= n and nrm.numel() >= n
+    check(_lib().gi_gbuffer(ctx.handle, scene.handle, _f16(camera_mvp), width, height, _ptr(pos), _ptr(nrm),
+                            _stream_ptr(stream)), "gi_gbuffer")
+    return pos, nrm
+
+
+def compute_visibility(ctx: Context, params: ShadowParams, frame: Frame, depth, map_w: int, map_h: int,
+                       pos, nrm, vis, width: int, height: int, stream=None):
+    """computeHardShadows / the soft visibility pass: vis is float32[height * width]."""
+    assert vis.is_cuda and vis.numel() >= width * height
+    p = params.to_c(frame)
+    check(_lib().gi_visibility(ctx.handle, C.byref(p), _ptr(depth), map_w, map_h, _ptr(pos), _ptr(nrm),
+                               _ptr(vis), width, height, _stream_ptr(stream)), "gi_visibility")
+    return vis
+
+
+compute_hard_shadows = compute_visibility
+
+
+def shadow_volume_counts(ctx: Context, scene: Scene, light_pos, camera_mvp, width: int, height: int,
+                         stencil, depth=None, depth_func: int = api.GI_DEPTH_LEQUAL, infinity: float = 100.0,
+                         stream=None):
+    """The ShadowVolumes stencil passes: stencil is a uint8 CUDA tensor of height * width."""
+    assert stencil.is_cuda and stencil.numel() >= width * height
+    check(_lib().gi_shadow_volume_counts(ctx.handle, scene.handle, _f3(light_pos), float(infinity),
+                                         _f16(camera_mvp), width, height, int(depth_func), _ptr(stencil),
+                                         _ptr(depth) if depth is not None else None, _stream_ptr(stream)),
+          "gi_shadow_volume_counts")
+    return stencil
+
+
+@dataclass
+class FrameBuffers:
+    depth: object
+    pos: object
+    nrm: object
+    vis: object
+
+
+def allocate_frame(map_w: int, map_h: int, width: int, height: int, device: int = 0) -> FrameBuffers:
+    import torch
+    dev = torch.device("cuda", device)
+    return FrameBuffers(
+        depth=torch.empty(map_h * map_w, dtype=torch.float32, device=dev),
+        pos=torch.empty(height * width * 4, dtype=torch.float32, device=dev),
+        nrm=torch.empty(height * width * 4, dtype=torch.float32, device=dev),
+        vis=torch.empty(height * width, dtype=torch.float32, device=dev),
+    )
+
+
+def render_frame(ctx: Context, scene: Scene, frame: Frame, mp: MapParams, params: ShadowParams, width: int,
+                 height: int, bufs: FrameBuffers, stream=None):
+    """One shadowed frame: light map, G-buffer, visibility (display() up to shading)."""
+    render_shadow_map(ctx, scene, mp, frame.light_mvp, bufs.depth, stream)
+    render_gbuffer(ctx, scene, frame.camera_mvp, width, height, bufs.pos, bufs.nrm, stream)
+    compute_visibility(ctx, params, frame, bufs.depth, mp.width, mp.height, bufs.pos, bufs.nrm, bufs.vis,
+                       width, height, stream)
+    return bufs.vis
+
+
+render_soft_shadows = render_frame

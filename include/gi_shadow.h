@@ -1,0 +1,320 @@
+/*
+ * gi_shadow.h -- C ABI of the GB300 shadow-visibility engine.
+ *
+ * This is the drop-in boundary for the shadow passes of
+ * MarcioCerqueira/GlobalIllumination.  The reference has no library API:
+ * its passes are free functions called from the GLUT display callback and
+ * its outputs are OpenGL textures.  Each entry point below names the
+ * reference function (file:line) whose work it replaces.  Paths are relative
+ * to the reference project root.
+ *
+ * Conventions
+ *   - Every call returns gi_status; gi_last_error_string() gives the text of
+ *     the last failure on the calling thread.
+ *   - Device buffers (d_*) are owned by the caller and must be allocated on
+ *     the device that the gi_context was created for.  Images are row-major
+ *     with row 0 at the BOTTOM (OpenGL window/texture convention): pixel
+ *     (x, y) of a W x H image lives at index y * W + x.
+ *   - Matrices are 4x4 FP32, column-major (m[col * 4 + row]), as glm and
+ *     glUniformMatrix4fv(..., GL_FALSE, ...) use them.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default).
+ *     Every pass is stream-ordered and asynchronous; results are valid once
+ *     the stream has been synchronised.
+ *   - A gi_context owns the scratch memory of the passes (triangle work
+ *     queues, visibility keys, an error word).  Use one context per host
+ *     thread / stream.
+ */
+#ifndef GI_SHADOW_H
+#define GI_SHADOW_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* Status                                                              */
+/* ------------------------------------------------------------------ */
+typedef enum gi_status {
+    GI_OK = 0,
+    GI_ERR_INVALID_ARG = 1,  /* bad pointer, size or enum value            */
+    GI_ERR_IO = 2,           /* a file could not be opened (the reference   */
+                             /* calls exit(1): Mesh.cpp:336-340,            */
+                             /* OBJLoader.cpp:1315-1319)                    */
+    GI_ERR_PARSE = 3,        /* malformed OBJ / config content              */
+    GI_ERR_CUDA = 4,         /* a CUDA runtime call failed                  */
+    GI_ERR_CAPACITY = 5,     /* a device work queue overflowed              */
+    GI_ERR_OOM = 6,          /* host or device allocation failed            */
+    GI_ERR_DEVICE = 7,       /* a kernel reported an error in its status    */
+    GI_ERR_UNSUPPORTED = 8
+} gi_status;
+
+/* Text of the last error raised on this thread ("" if none). */
+const char* gi_last_error_string(void);
+/* Library version string. */
+const char* gi_version(void);
+
+/* ------------------------------------------------------------------ */
+/* Context (scratch memory owner)                                      */
+/* ------------------------------------------------------------------ */
+typedef struct gi_context gi_context;
+
+/* Creates a context bound to CUDA device `device`.  Scratch buffers grow on
+ * demand with cudaMalloc and are released by gi_context_destroy. */
+gi_status gi_context_create(int device, gi_context** out);
+void gi_context_destroy(gi_context* ctx);
+/* Number of kernel launches issued through this context since creation. */
+uint64_t gi_context_launch_count(const gi_context* ctx);
+
+/* ------------------------------------------------------------------ */
+/* Scene (host geometry + optional device copy)                        */
+/* ------------------------------------------------------------------ */
+typedef struct gi_scene gi_scene;
+
+typedef struct gi_scene_info {
+    int num_vertices;
+    int num_triangles;
+    float camera_eye[3];     /* config key "ve"                            */
+    float camera_at[3];      /* config key "va" (any 2nd char but 'e')     */
+    float light_eye[3];      /* config key "le"                            */
+    float light_at[3];       /* config key "la"                            */
+    float depth_threshold;   /* config key "d" (RBSM, A10-A12)             */
+    float hsm_alpha;         /* config key "ha" (soft app only)            */
+    float hsm_beta;          /* config key "hb"                            */
+    int num_objects;         /* number of "+" commits                      */
+} gi_scene_info;
+
+/* Parses a Configs/<name>.txt scene file with the grammar of
+ * SceneLoader::load (ShadowMapping/src/IO/SceneLoader.cpp:11-94, soft keys
+ * ha/hb SoftShadowMapping/src/IO/SceneLoader.cpp:93-97).  Relative OBJ
+ * paths are resolved against `base_dir` (NULL = the current directory),
+ * which plays the role of the reference's working directory. */
+gi_status gi_scene_load_config(const char* cfg_path, const char* base_dir,
+                               gi_scene** out);
+
+/* Creates an empty scene. */
+gi_status gi_scene_create(gi_scene** out);
+void gi_scene_destroy(gi_scene* scene);
+
+/* Reads one Wavefront OBJ (glmReadOBJ, ShadowMapping/src/IO/OBJLoader.cpp:
+ * 1309-1387 + Mesh::loadOBJFile, ShadowMapping/src/Mesh.cpp:251-313) into
+ * the scene's pending object and computes its normals
+ * (Mesh::computeNormals, Mesh.cpp:195-234). */
+gi_status gi_scene_object_load_obj(gi_scene* scene, const char* obj_path);
+/* Sets the pending object from host arrays (points float[3V], indices
+ * int[3T], 0-based) and computes its normals like Mesh::computeNormals. */
+gi_status gi_scene_object_from_arrays(gi_scene* scene, const float* points,
+                                      int num_vertices, const int* indices,
+                                      int num_triangles);
+/* Config keys s / t / r on the pending object (Mesh::scale, translate,
+ * rotate, Mesh.cpp:378-429; rotate angles are in degrees, p' = Rx Ry Rz p,
+ * normals are rotated, scale/translate leave normals untouched). */
+gi_status gi_scene_object_scale(gi_scene* scene, float x, float y, float z);
+gi_status gi_scene_object_translate(gi_scene* scene, float x, float y, float z);
+gi_status gi_scene_object_rotate(gi_scene* scene, float x, float y, float z);
+/* Config key "+": appends the pending object (Mesh::addObject,
+ * Mesh.cpp:47-193). */
+gi_status gi_scene_object_commit(gi_scene* scene);
+/* Sets camera / light eye and at, and the RBSM depth threshold. */
+gi_status gi_scene_set_views(gi_scene* scene, const float camera_eye[3],
+                             const float camera_at[3], const float light_eye[3],
+                             const float light_at[3], float depth_threshold);
+
+gi_status gi_scene_get_info(const gi_scene* scene, gi_scene_info* out);
+/* Copies the committed geometry out (any pointer may be NULL). */
+gi_status gi_scene_get_arrays(const gi_scene* scene, float* points,
+                              float* normals, int* indices);
+
+/* Procedural generators for the synthetic benchmark scenes.  Each one
+ * replaces the pending object (call gi_scene_object_commit afterwards). */
+/* Axis-aligned quad at height y spanning [-h, h] in x and z, face normal +y. */
+gi_status gi_gen_ground(gi_scene* scene, float half_size, float y);
+/* UV sphere with `slices` x `stacks` segments and single pole vertices. */
+gi_status gi_gen_uv_sphere(gi_scene* scene, int slices, int stacks,
+                           float radius, const float centre[3]);
+/* Icosphere: icosahedron subdivided `level` times (20 * 4^level tris). */
+gi_status gi_gen_icosphere(gi_scene* scene, int level, float radius,
+                           const float centre[3]);
+/* UV-grid sphere (slices x stacks) whose radius is displaced by seeded
+ * FP32 Perlin noise of amplitude `amplitude`. */
+gi_status gi_gen_displaced_sphere(gi_scene* scene, int slices, int stacks,
+                                  float radius, float amplitude,
+                                  const float centre[3], uint64_t seed);
+/* Batch of `count` icospheres with PCG32(seed) centres uniform in
+ * [lo, hi] per axis and radii uniform in [rmin, rmax], each committed. */
+gi_status gi_gen_icosphere_field(gi_scene* scene, int count, int level,
+                                 const float lo[3], const float hi[3],
+                                 float rmin, float rmax, uint64_t seed);
+
+/* Uploads (or re-uploads) the committed geometry to device memory owned by
+ * the scene, on `stream` (the reference re-uploads its VBOs every draw:
+ * MyGLGeometryViewer::loadVBOs, MyGLGeometryViewer.cpp:383-405). */
+gi_status gi_scene_upload(gi_scene* scene, gi_context* ctx, void* stream);
+/* Device pointers of the uploaded geometry (NULL before upload). */
+gi_status gi_scene_device_arrays(const gi_scene* scene, const float** d_points,
+                                 const float** d_normals, const int** d_indices);
+
+/* ------------------------------------------------------------------ */
+/* Matrices (MyGLGeometryViewer::configureAmbient / configureShadow /   */
+/* configurePhong, ShadowMapping/src/Viewers/MyGLGeometryViewer.cpp)    */
+/* ------------------------------------------------------------------ */
+typedef struct gi_view {
+    float eye[3];
+    float at[3];
+    float up[3];      /* the reference uses (0, 0, 1) for light and camera */
+    float fovy_deg;   /* reference: 45                                     */
+    float znear;      /* reference: 1                                      */
+    float zfar;       /* reference: 1000                                   */
+    int width;        /* viewport                                          */
+    int height;
+} gi_view;
+
+typedef struct gi_frame_matrices {
+    float light_mvp[16];        /* P V M of the light (main.cpp:255-266)        */
+    float light_mvp_biased[16]; /* bias * light_mvp (MyGLGeometryViewer.cpp:139-145) */
+    float camera_mvp[16];       /* P V M of the camera                          */
+    float camera_mv[16];        /* V M of the camera                            */
+    float normal_matrix[9];     /* inverseTranspose(mat3(camera MV)), col-major */
+    float light_position[3];    /* lightEye rotated 180 deg about +y
+                                   (ShadowMapping/src/main.cpp:283,309)          */
+} gi_frame_matrices;
+
+/* glm::perspective(fovy, w/h, n, f) * glm::lookAt(eye, at, up). */
+gi_status gi_view_matrices(const gi_view* view, float proj[16], float view_m[16]);
+/* Everything the light-view pass and the per-pixel passes need. */
+gi_status gi_frame_setup(const gi_view* light, const gi_view* camera,
+                         gi_frame_matrices* out);
+
+/* ------------------------------------------------------------------ */
+/* A4: light-view depth map                                            */
+/* ------------------------------------------------------------------ */
+typedef enum gi_bias_mode {
+    GI_BIAS_NONE = 0,
+    GI_BIAS_CONSTANT = 1,        /* depth += constant_bias                  */
+    GI_BIAS_POLYGON_OFFSET = 2   /* glPolygonOffset(factor, units), float   */
+                                 /* depth buffer (main.cpp:246-247)         */
+} gi_bias_mode;
+
+typedef struct gi_map_params {
+    int width;                   /* reference: 2048 (SM), 1024 (Soft)       */
+    int height;
+    int bias_mode;               /* gi_bias_mode                            */
+    float constant_bias;
+    float offset_factor;         /* reference: 4                            */
+    float offset_units;          /* reference: 20                           */
+} gi_map_params;
+
+/* renderShadowMap + displaySceneFromLightPOV (ShadowMapping/src/main.cpp:
+ * 221-274, 350-361; soft copy SoftShadowMapping/src/main.cpp:274-318):
+ * clears d_depth (float[width*height]) to 1 and rasterises every triangle
+ * of the uploaded scene through `light_mvp` with depth test LESS and no
+ * culling.  Window depth = 0.5 z_ndc + 0.5; the bias is applied per
+ * fragment and the result clamped to [0, 1]. */
+gi_status gi_shadow_map(gi_context* ctx, const gi_scene* scene,
+                        const gi_map_params* params, const float light_mvp[16],
+                        float* d_depth, void* stream);
+
+/* ------------------------------------------------------------------ */
+/* A5: G-buffer                                                        */
+/* ------------------------------------------------------------------ */
+/* renderGBuffer (ShadowMapping/src/main.cpp:363-372, GBuffer.vert:12-23,
+ * GBuffer.frag:32-38): d_pos / d_nrm are float4[width*height].  Covered
+ * pixels get (object-space position, 1) and (interpolated vertex normal,
+ * gl_FrontFacing); background pixels get (0, 0, 0, 1).  Depth test LESS,
+ * first-drawn triangle wins depth ties. */
+gi_status gi_gbuffer(gi_context* ctx, const gi_scene* scene,
+                     const float camera_mvp[16], int width, int height,
+                     float* d_pos, float* d_nrm, void* stream);
+
+/* ------------------------------------------------------------------ */
+/* A6-A12, A15: per-pixel visibility                                   */
+/* ------------------------------------------------------------------ */
+typedef enum gi_technique {
+    GI_TECH_HARD = 0,           /* Shadow.frag:253-256 ("naive")            */
+    GI_TECH_PCF = 1,            /* Shadow.frag:86-116, bilinearPCF flag     */
+    GI_TECH_PCF_TRICUBIC = 2,   /* Shadow.frag:54-116, tricubicPCF flag     */
+    GI_TECH_PCSS_GRID = 3,      /* PlausibleSoftShadow.frag:166-194,365-398,556-563 */
+    GI_TECH_PCSS_POISSON = 4,   /* PCSS with Poisson-disk taps (no ref counterpart) */
+    GI_TECH_SMSR_CONSERVATIVE = 5,    /* RBSM/ConservativeSMSR.frag:128-144   */
+    GI_TECH_SMSR_NONCONSERVATIVE = 6, /* RBSM/NonConservativeSMSR.frag:288-304 */
+    GI_TECH_RPCF_CONSERVATIVE = 7,    /* ConservativeSMSR.frag:146-198 (RPCF v.1, conservative) */
+    GI_TECH_RPCF_SMSR = 8,            /* NonConservativeSMSR.frag:306-350 (RPCF v.1) */
+    GI_TECH_RSMSS = 9,                /* FilteredRBSM.frag (RSMSS / RPCF v.2) */
+    GI_TECH_HARD_SOFTAPP = 10,        /* SoftShadow HardShadow.frag:35-58     */
+    GI_TECH_COUNT = 11
+} gi_technique;
+
+typedef enum gi_pretest_mode {
+    GI_PRETEST_REFERENCE = 0,  /* as the reference: world-space light rotated
+                                  180 deg vs eye-space vertex (Shadow.frag:222-238) */
+    GI_PRETEST_OFF = 1
+} gi_pretest_mode;
+
+/* Mirrors ShadowParams (ShadowMapping/include/Viewers/ShadowParams.h:6-37,
+ * SoftShadowMapping/include/Viewers/ShadowParams.h:6-69) plus the uniforms
+ * the passes receive. */
+typedef struct gi_vis_params {
+    int technique;              /* gi_technique                             */
+    int pretest;                /* gi_pretest_mode                          */
+    float shadow_intensity;     /* reference: 0.25                          */
+    int kernel_order;           /* PCF k (reference Gaussian order 7)       */
+    int penumbra_size;          /* PCF offset in texels (reference 1)       */
+    int max_search;             /* RBSM (reference 16)                      */
+    float depth_threshold;      /* RBSM, config key "d"                     */
+    int blocker_search_size;    /* PCSS grid B (reference 7)                */
+    int kernel_size;            /* PCSS grid K (reference 15)               */
+    float light_radius;         /* PCSS lightSourceRadius (float here)      */
+    float znear;                /* PCSS zNear uniform (reference 1)         */
+    float pcss_min_blocker_depth; /* PlausibleSoftShadow.frag:368 (0.99)    */
+    int poisson_blocker_taps;   /* PCSS_POISSON: 16                         */
+    int poisson_filter_taps;    /* PCSS_POISSON: 32                         */
+    float light_mvp_biased[16];
+    float camera_mv[16];
+    float normal_matrix[9];
+    float light_position[3];
+} gi_vis_params;
+
+/* Fills *p with the reference defaults for `technique`. */
+gi_status gi_vis_params_default(int technique, gi_vis_params* p);
+
+/* computeHardShadows / renderSoftShadows (ShadowMapping/src/main.cpp:
+ * 400-414, SoftShadowMapping/src/main.cpp:1010-1017): writes the r channel
+ * of the visibility target, d_vis float[width*height] (background 0). */
+gi_status gi_visibility(gi_context* ctx, const gi_vis_params* params,
+                        const float* d_depth, int map_width, int map_height,
+                        const float* d_pos, const float* d_nrm,
+                        float* d_vis, int width, int height, void* stream);
+
+/* Poisson-disk sample table used by GI_TECH_PCSS_POISSON (n <= 64 points in
+ * the unit disk, interleaved x,y).  Shared with the CPU oracle. */
+gi_status gi_poisson_table(int n, float* xy_out);
+
+/* ------------------------------------------------------------------ */
+/* A13/A14: shadow volumes with stencil counts                         */
+/* ------------------------------------------------------------------ */
+typedef enum gi_depth_func {
+    GI_DEPTH_LESS = 0,    /* first frame                                    */
+    GI_DEPTH_LEQUAL = 1   /* every later frame (ShadowVolumes/src/main.cpp:174) */
+} gi_depth_func;
+
+/* One frame of ShadowVolumes display() (ShadowVolumes/src/main.cpp:120-206)
+ * up to the stencil buffer: depth prepass of the scene through
+ * `camera_mvp`, then the extruded volume of every triangle
+ * (ShadowVolume::update, ShadowVolume.cpp:116-194, far vertices
+ * (v - L) * infinity) with depth writes off, front faces INCR_WRAP, back
+ * faces DECR_WRAP on depth pass.  d_stencil is uint8[width*height]; a pixel
+ * is lit iff its count is 0.  d_depth (float[width*height], may be NULL)
+ * receives the prepass depth. */
+gi_status gi_shadow_volume_counts(gi_context* ctx, const gi_scene* scene,
+                                  const float light_pos[3], float infinity,
+                                  const float camera_mvp[16], int width,
+                                  int height, int depth_func,
+                                  uint8_t* d_stencil, float* d_depth,
+                                  void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GI_SHADOW_H */

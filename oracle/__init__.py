@@ -1,0 +1,77 @@
+"""Python wrapper of the CPU oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and the CPU-baseline leg of bench.py
+import this package, to check or time the CUDA path; the product never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .build_oracle import ORACLE_LIB, build_oracle
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_LIB):
+            build_oracle()
+        lib = C.CDLL(ORACLE_LIB)
+        vp, i, f = C.c_void_p, C.c_int, C.c_float
+        lib.or_shadow_map.argtypes = [vp, i, vp, i, vp, i, i, i, f, f, f, vp, i]
+        lib.or_gbuffer.argtypes = [vp, vp, i, vp, i, vp, i, i, vp, vp, i]
+        lib.or_visibility.argtypes = [vp, vp, i, i, vp, vp, vp, i, i, vp, i]
+        lib.or_shadow_volume_counts.argtypes = [vp, vp, i, vp, i, vp, f, vp, i, i, i, vp, vp, i]
+        for fn in (lib.or_shadow_map, lib.or_gbuffer, lib.or_visibility, lib.or_shadow_volume_counts):
+            fn.restype = None
+        _lib = lib
+    return _lib
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def shadow_map(points, indices, mvp, width, height, bias_mode=0, constant_bias=0.0, factor=0.0, units=0.0,
+               threads=0):
+    p, ix, m = _f32(points), np.ascontiguousarray(indices, dtype=np.int32), _f32(mvp).reshape(16)
+    out = np.empty(height * width, np.float32)
+    load().or_shadow_map(p.ctypes.data, p.size // 3, ix.ctypes.data, ix.size // 3, m.ctypes.data, width, height,
+                         bias_mode, constant_bias, factor, units, out.ctypes.data, threads)
+    return out
+
+
+def gbuffer(points, normals, indices, mvp, width, height, threads=0):
+    p, n = _f32(points), _f32(normals)
+    ix, m = np.ascontiguousarray(indices, dtype=np.int32), _f32(mvp).reshape(16)
+    pos = np.empty(height * width * 4, np.float32)
+    nrm = np.empty(height * width * 4, np.float32)
+    load().or_gbuffer(p.ctypes.data, n.ctypes.data, p.size // 3, ix.ctypes.data, ix.size // 3, m.ctypes.data,
+                      width, height, pos.ctypes.data, nrm.ctypes.data, threads)
+    return pos, nrm
+
+
+def visibility(vis_params, depth, map_w, map_h, pos, nrm, width, height, poisson_xy=None, threads=0):
+    """vis_params is a globalillumination_gb300._capi.VisParams (same layout as gi_vis_params)."""
+    d, ps, ns = _f32(depth), _f32(pos), _f32(nrm)
+    out = np.empty(height * width, np.float32)
+    tab = _f32(poisson_xy) if poisson_xy is not None else None
+    load().or_visibility(C.addressof(vis_params), d.ctypes.data, map_w, map_h, ps.ctypes.data, ns.ctypes.data,
+                         out.ctypes.data, width, height, tab.ctypes.data if tab is not None else None, threads)
+    return out
+
+
+def shadow_volume_counts(points, normals, indices, light_pos, infinity, mvp, width, height, depth_func,
+                         threads=0):
+    p, n = _f32(points), _f32(normals)
+    ix, m, L = np.ascontiguousarray(indices, dtype=np.int32), _f32(mvp).reshape(16), _f32(light_pos)
+    st = np.empty(height * width, np.uint8)
+    dp = np.empty(height * width, np.float32)
+    load().or_shadow_volume_counts(p.ctypes.data, n.ctypes.data, p.size // 3, ix.ctypes.data, ix.size // 3,
+                                   L.ctypes.data, infinity, m.ctypes.data, width, height, depth_func,
+                                   st.ctypes.data, dp.ctypes.data, threads)
+    return st, dp

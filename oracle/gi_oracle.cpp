@@ -1,0 +1,1056 @@
+// gi_oracle.cpp -- CPU oracle (test infrastructure; see gi_oracle.h).
+//
+// Scalar restatement of the reference's shadow passes.  Build with
+// -O2 -ffp-contract=off and without -ffast-math: every FP32 operation below
+// is meant to round exactly once, in the order written.
+//
+// Rasterisation rules (OpenGL 4.6 core spec, sections 13.6 / 14.6 / 14.9;
+// the choices the spec leaves open are fixed here):
+//   * clip coordinates c = MVP * (x, y, z, 1), glm's operation order;
+//   * triangles are clipped against the near (z >= -w) and far (z <= w)
+//     planes and against a guard band |x|, |y| <= 16 w (Sutherland-Hodgman,
+//     intersection computed from the inside vertex); the clipped polygon is
+//     fanned from its first vertex;
+//   * window coordinates x_w = x_ndc * W/2 + W/2 (same for y),
+//     z_w = z_ndc * 0.5 + 0.5, snapped to 8 sub-pixel bits (round to nearest
+//     even);
+//   * integer edge functions; pixel centres at (x + 1/2, y + 1/2); a centre
+//     on an edge belongs to the triangle iff the edge is a top or left edge
+//     of the counter-clockwise-ordered triangle (y up);
+//   * gl_FrontFacing = counter-clockwise window-space area > 0, no culling;
+//   * depth is interpolated linearly in window space from the barycentrics
+//     l_i = E_i * (1 / area); attributes perspective-correctly;
+//   * polygon offset o = m * factor + r * units, m = max(|dz/dx|, |dz/dy|),
+//     r = 2^(e - 23) with e the exponent of the primitive's largest z_w;
+//   * depth is clamped to [0, 1] after the offset; the depth buffer is
+//     cleared to 1 and the test is LESS, so a buffer texel ends as the
+//     minimum fragment depth below 1;
+//   * for the G-buffer the surviving fragment is the first one in draw
+//     order among those with the minimum depth (LESS keeps the earlier).
+// Texture fetches: GL_NEAREST, i = floor(s * width), CLAMP_TO_BORDER with
+// border depth 0 (ShadowMapping/src/Viewers/MyGLTextureViewer.cpp:3-28).
+#include "gi_oracle.h"
+
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+const float kGuard = 16.0f;
+const int kSubBits = 8;
+const int64_t kSub = 1 << kSubBits;
+
+// ---------------------------------------------------------------------------
+// Clipping
+// ---------------------------------------------------------------------------
+struct CV {
+    float c[4];  // clip x, y, z, w
+    float b[3];  // barycentric weights with respect to the source triangle
+};
+
+float plane_dist(const CV& v, int k) {
+    const float x = v.c[0], y = v.c[1], z = v.c[2], w = v.c[3];
+    switch (k) {
+        case 0: return z + w;
+        case 1: return w - z;
+        case 2: return x + kGuard * w;
+        case 3: return kGuard * w - x;
+        case 4: return y + kGuard * w;
+        default: return kGuard * w - y;
+    }
+}
+
+CV intersect(const CV& in, const CV& out, float din, float dout) {
+    float t = din / (din - dout);
+    CV r;
+    for (int k = 0; k < 4; ++k) r.c[k] = in.c[k] + t * (out.c[k] - in.c[k]);
+    for (int k = 0; k < 3; ++k) r.b[k] = in.b[k] + t * (out.b[k] - in.b[k]);
+    return r;
+}
+
+// Returns the clipped polygon size (0 if culled); poly holds <= 9 vertices.
+int clip_polygon(const float c0[4], const float c1[4], const float c2[4], CV poly[9]) {
+    CV a[9], b[9];
+    for (int k = 0; k < 4; ++k) {
+        a[0].c[k] = c0[k];
+        a[1].c[k] = c1[k];
+        a[2].c[k] = c2[k];
+    }
+    for (int i = 0; i < 3; ++i)
+        for (int k = 0; k < 3; ++k) a[i].b[k] = (i == k) ? 1.0f : 0.0f;
+    int n = 3;
+    CV* src = a;
+    CV* dst = b;
+    for (int plane = 0; plane < 6; ++plane) {
+        bool any_out = false, all_out = true;
+        for (int i = 0; i < n; ++i) {
+            bool out = !(plane_dist(src[i], plane) >= 0.0f);
+            any_out |= out;
+            all_out &= out;
+        }
+        if (all_out) return 0;
+        if (!any_out) continue;
+        int m = 0;
+        for (int i = 0; i < n; ++i) {
+            const CV& cur = src[i];
+            const CV& nxt = src[(i + 1) % n];
+            float dc = plane_dist(cur, plane), dn = plane_dist(nxt, plane);
+            bool cin = dc >= 0.0f, nin = dn >= 0.0f;
+            if (cin) dst[m++] = cur;
+            if (cin != nin) {
+                if (cin) dst[m++] = intersect(cur, nxt, dc, dn);
+                else dst[m++] = intersect(nxt, cur, dn, dc);
+            }
+        }
+        n = m;
+        CV* t = src;
+        src = dst;
+        dst = t;
+        if (n < 3) return 0;
+    }
+    for (int i = 0; i < n; ++i) poly[i] = src[i];
+    return n;
+}
+
+// ---------------------------------------------------------------------------
+// Triangle setup for one (sub-)triangle
+// ---------------------------------------------------------------------------
+struct Setup {
+    int64_t X[3], Y[3];
+    float z[3];
+    float iw[3];     // 1 / clip w
+    float b[3][3];   // source barycentric rows of the three vertices
+    int64_t area;    // > 0 after reordering
+    bool front;
+    bool topleft[3];
+    float inv_area;
+};
+
+float f_of_ll(int64_t v) { return (float)v; }
+
+bool setup_triangle(const CV& v0, const CV& v1, const CV& v2, int W, int H, Setup& s) {
+    const CV* v[3] = {&v0, &v1, &v2};
+    const float hw = 0.5f * (float)W, hh = 0.5f * (float)H;
+    float wv[3];
+    for (int i = 0; i < 3; ++i) {
+        float w = v[i]->c[3];
+        if (!(w > 0.0f)) return false;
+        float xd = v[i]->c[0] / w, yd = v[i]->c[1] / w, zd = v[i]->c[2] / w;
+        float xw = xd * hw + hw;
+        float yw = yd * hh + hh;
+        float zw = zd * 0.5f + 0.5f;
+        s.X[i] = (int64_t)std::nearbyint(xw * (float)kSub);
+        s.Y[i] = (int64_t)std::nearbyint(yw * (float)kSub);
+        s.z[i] = zw;
+        wv[i] = w;
+        for (int k = 0; k < 3; ++k) s.b[i][k] = v[i]->b[k];
+    }
+    int64_t area = (s.X[1] - s.X[0]) * (s.Y[2] - s.Y[0]) - (s.X[2] - s.X[0]) * (s.Y[1] - s.Y[0]);
+    if (area == 0) return false;
+    s.front = area > 0;
+    if (area < 0) {
+        std::swap(s.X[1], s.X[2]);
+        std::swap(s.Y[1], s.Y[2]);
+        std::swap(s.z[1], s.z[2]);
+        std::swap(wv[1], wv[2]);
+        for (int k = 0; k < 3; ++k) std::swap(s.b[1][k], s.b[2][k]);
+        area = -area;
+    }
+    s.area = area;
+    for (int i = 0; i < 3; ++i) s.iw[i] = 1.0f / wv[i];
+    // Edge i is the edge opposite vertex i: (1,2), (2,0), (0,1).
+    for (int i = 0; i < 3; ++i) {
+        int a = (i + 1) % 3, bb = (i + 2) % 3;
+        int64_t dy = s.Y[bb] - s.Y[a], dx = s.X[bb] - s.X[a];
+        s.topleft[i] = (dy < 0) || (dy == 0 && dx < 0);
+    }
+    s.inv_area = 1.0f / f_of_ll(area);
+    return true;
+}
+
+int64_t edge(const Setup& s, int i, int64_t px, int64_t py) {
+    int a = (i + 1) % 3, b = (i + 2) % 3;
+    return (s.X[b] - s.X[a]) * (py - s.Y[a]) - (s.Y[b] - s.Y[a]) * (px - s.X[a]);
+}
+
+int64_t floor_div(int64_t a, int64_t b) {
+    int64_t q = a / b;
+    if ((a % b != 0) && ((a < 0) != (b < 0))) --q;
+    return q;
+}
+
+float pow2i(int k) {
+    // exact 2^k for k in [-149, 127]
+    uint32_t bits;
+    if (k >= -126) bits = (uint32_t)(k + 127) << 23;
+    else bits = 1u << (k + 149);
+    float f;
+    std::memcpy(&f, &bits, 4);
+    return f;
+}
+
+float polygon_offset(const Setup& s, float factor, float units) {
+    float fx1 = f_of_ll(s.X[1] - s.X[0]), fy1 = f_of_ll(s.Y[1] - s.Y[0]);
+    float fx2 = f_of_ll(s.X[2] - s.X[0]), fy2 = f_of_ll(s.Y[2] - s.Y[0]);
+    float dz1 = s.z[1] - s.z[0], dz2 = s.z[2] - s.z[0];
+    float area_f = f_of_ll(s.area);
+    float dzdx = ((dz1 * fy2 - dz2 * fy1) / area_f) * (float)kSub;
+    float dzdy = ((dz2 * fx1 - dz1 * fx2) / area_f) * (float)kSub;
+    float ax = std::fabs(dzdx), ay = std::fabs(dzdy);
+    float m = ax > ay ? ax : ay;
+    float zmax = s.z[0];
+    if (s.z[1] > zmax) zmax = s.z[1];
+    if (s.z[2] > zmax) zmax = s.z[2];
+    int e = -126;
+    if (zmax > 0.0f) {
+        uint32_t bits;
+        std::memcpy(&bits, &zmax, 4);
+        int be = (int)((bits >> 23) & 0xFF);
+        e = be == 0 ? -126 : be - 127;
+    }
+    float r = pow2i(e - 23);
+    return m * factor + r * units;
+}
+
+float clamp01(float z) {
+    if (!(z > 0.0f)) return 0.0f;
+    if (z > 1.0f) return 1.0f;
+    return z;
+}
+
+uint32_t fbits(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+}
+
+void transform(const float m[16], const float* p, float out[4]) {
+    const float x = p[0], y = p[1], z = p[2];
+    for (int r = 0; r < 4; ++r)
+        out[r] = m[0 * 4 + r] * x + m[1 * 4 + r] * y + m[2 * 4 + r] * z + m[3 * 4 + r];
+}
+
+// Visits every covered pixel of every sub-triangle of one clipped triangle:
+// fn(sub_index, setup, x, y, E0, E1, E2).
+template <class Fn>
+void raster_clipped(const float c0[4], const float c1[4], const float c2[4], int W, int H, Fn fn) {
+    CV poly[9];
+    int n = clip_polygon(c0, c1, c2, poly);
+    for (int i = 1; i + 1 < n; ++i) {
+        Setup s;
+        if (!setup_triangle(poly[0], poly[i], poly[i + 1], W, H, s)) continue;
+        int64_t minX = std::min(s.X[0], std::min(s.X[1], s.X[2]));
+        int64_t maxX = std::max(s.X[0], std::max(s.X[1], s.X[2]));
+        int64_t minY = std::min(s.Y[0], std::min(s.Y[1], s.Y[2]));
+        int64_t maxY = std::max(s.Y[0], std::max(s.Y[1], s.Y[2]));
+        int64_t x0 = std::max<int64_t>(0, -floor_div(-(minX - kSub / 2), kSub));
+        int64_t x1 = std::min<int64_t>(W - 1, floor_div(maxX - kSub / 2, kSub));
+        int64_t y0 = std::max<int64_t>(0, -floor_div(-(minY - kSub / 2), kSub));
+        int64_t y1 = std::min<int64_t>(H - 1, floor_div(maxY - kSub / 2, kSub));
+        for (int64_t y = y0; y <= y1; ++y)
+            for (int64_t x = x0; x <= x1; ++x) {
+                int64_t px = x * kSub + kSub / 2, py = y * kSub + kSub / 2;
+                int64_t e[3];
+                bool inside = true;
+                for (int k = 0; k < 3 && inside; ++k) {
+                    e[k] = edge(s, k, px, py);
+                    inside = e[k] > 0 || (e[k] == 0 && s.topleft[k]);
+                }
+                if (inside) fn(i - 1, s, (int)x, (int)y, e);
+            }
+    }
+}
+
+float depth_at(const Setup& s, const int64_t e[3]) {
+    float l1 = f_of_ll(e[1]) * s.inv_area;
+    float l2 = f_of_ll(e[2]) * s.inv_area;
+    return s.z[0] + (l1 * (s.z[1] - s.z[0]) + l2 * (s.z[2] - s.z[0]));
+}
+
+template <class T>
+void atomic_min(std::atomic<T>& a, T v) {
+    T cur = a.load(std::memory_order_relaxed);
+    while (v < cur && !a.compare_exchange_weak(cur, v, std::memory_order_relaxed)) {
+    }
+}
+
+int nthreads(int t) {
+#ifdef _OPENMP
+    return t > 0 ? t : omp_get_max_threads();
+#else
+    (void)t;
+    return 1;
+#endif
+}
+
+// Depth-only rasterisation of a whole mesh into `buf` (uint32 depth bits,
+// pre-cleared), with the given bias; used by the light map and the
+// shadow-volume prepass.
+void raster_depth(const float* points, const int* indices, int nt, const float mvp[16], int W,
+                  int H, int bias_mode, float cbias, float factor, float units,
+                  std::atomic<uint32_t>* buf, int threads) {
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads(threads))
+    for (int t = 0; t < nt; ++t) {
+        float c[3][4];
+        for (int k = 0; k < 3; ++k) transform(mvp, points + 3 * (size_t)indices[3 * (size_t)t + k], c[k]);
+        float offset = 0.0f;
+        bool offset_done = false;
+        int last_sub = -1;
+        raster_clipped(c[0], c[1], c[2], W, H,
+                       [&](int sub, const Setup& s, int x, int y, const int64_t e[3]) {
+                           if (bias_mode == GI_BIAS_POLYGON_OFFSET && (!offset_done || sub != last_sub)) {
+                               offset = polygon_offset(s, factor, units);
+                               offset_done = true;
+                               last_sub = sub;
+                           }
+                           float z = depth_at(s, e);
+                           if (bias_mode == GI_BIAS_CONSTANT) z = z + cbias;
+                           else if (bias_mode == GI_BIAS_POLYGON_OFFSET) z = z + offset;
+                           z = clamp01(z);
+                           if (z < 1.0f) atomic_min(buf[(size_t)y * W + x], fbits(z));
+                       });
+    }
+}
+
+}  // namespace
+
+extern "C" void or_shadow_map(const float* points, int nv, const int* indices, int nt,
+                              const float mvp[16], int W, int H, int bias_mode, float cbias,
+                              float factor, float units, float* out_depth, int threads) {
+    (void)nv;
+    std::vector<std::atomic<uint32_t>> buf((size_t)W * H);
+    for (auto& b : buf) b.store(fbits(1.0f), std::memory_order_relaxed);
+    raster_depth(points, indices, nt, mvp, W, H, bias_mode, cbias, factor, units, buf.data(),
+                 threads);
+    for (size_t i = 0; i < buf.size(); ++i) {
+        uint32_t u = buf[i].load(std::memory_order_relaxed);
+        std::memcpy(&out_depth[i], &u, 4);
+    }
+}
+
+extern "C" void or_gbuffer(const float* points, const float* normals, int nv, const int* indices,
+                           int nt, const float mvp[16], int W, int H, float* out_pos,
+                           float* out_nrm, int threads) {
+    (void)nv;
+    const uint64_t clear = ((uint64_t)fbits(1.0f) << 32) | 0xFFFFFFFFull;
+    std::vector<std::atomic<uint64_t>> key((size_t)W * H);
+    for (auto& k : key) k.store(clear, std::memory_order_relaxed);
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads(threads))
+    for (int t = 0; t < nt; ++t) {
+        float c[3][4];
+        for (int k = 0; k < 3; ++k) transform(mvp, points + 3 * (size_t)indices[3 * (size_t)t + k], c[k]);
+        raster_clipped(c[0], c[1], c[2], W, H,
+                       [&](int sub, const Setup& s, int x, int y, const int64_t e[3]) {
+                           float z = clamp01(depth_at(s, e));
+                           if (!(z < 1.0f)) return;
+                           uint64_t k = ((uint64_t)fbits(z) << 32) | (uint32_t)(t * 8 + sub);
+                           atomic_min(key[(size_t)y * W + x], k);
+                       });
+    }
+    // Resolve: re-derive the winning sub-triangle and interpolate.
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads(threads))
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            size_t p = (size_t)y * W + x;
+            uint64_t k = key[p].load(std::memory_order_relaxed);
+            float* op = out_pos + 4 * p;
+            float* on = out_nrm + 4 * p;
+            if (k == clear) {
+                op[0] = op[1] = op[2] = 0.0f;
+                op[3] = 1.0f;
+                on[0] = on[1] = on[2] = 0.0f;
+                on[3] = 1.0f;
+                continue;
+            }
+            uint32_t prim = (uint32_t)(k & 0xFFFFFFFFull);
+            int t = (int)(prim >> 3), sub = (int)(prim & 7);
+            const int* tri = indices + 3 * (size_t)t;
+            float c[3][4];
+            for (int j = 0; j < 3; ++j) transform(mvp, points + 3 * (size_t)tri[j], c[j]);
+            CV poly[9];
+            int n = clip_polygon(c[0], c[1], c[2], poly);
+            Setup s;
+            bool ok = (sub + 2 < n) && setup_triangle(poly[0], poly[sub + 1], poly[sub + 2], W, H, s);
+            if (!ok) continue;  // unreachable for keys the raster wrote
+            int64_t px = (int64_t)x * kSub + kSub / 2, py = (int64_t)y * kSub + kSub / 2;
+            int64_t e[3];
+            for (int j = 0; j < 3; ++j) e[j] = edge(s, j, px, py);
+            float l[3], q[3];
+            for (int j = 0; j < 3; ++j) {
+                l[j] = f_of_ll(e[j]) * s.inv_area;
+                q[j] = l[j] * s.iw[j];
+            }
+            float sum = (q[0] + q[1]) + q[2];
+            float pc[3] = {q[0] / sum, q[1] / sum, q[2] / sum};
+            float B[3];
+            for (int j = 0; j < 3; ++j) B[j] = (pc[0] * s.b[0][j] + pc[1] * s.b[1][j]) + pc[2] * s.b[2][j];
+            const float* P0 = points + 3 * (size_t)tri[0];
+            const float* P1 = points + 3 * (size_t)tri[1];
+            const float* P2 = points + 3 * (size_t)tri[2];
+            const float* N0 = normals + 3 * (size_t)tri[0];
+            const float* N1 = normals + 3 * (size_t)tri[1];
+            const float* N2 = normals + 3 * (size_t)tri[2];
+            for (int j = 0; j < 3; ++j) {
+                op[j] = (B[0] * P0[j] + B[1] * P1[j]) + B[2] * P2[j];
+                on[j] = (B[0] * N0[j] + B[1] * N1[j]) + B[2] * N2[j];
+            }
+            op[3] = 1.0f;
+            on[3] = s.front ? 1.0f : 0.0f;
+        }
+}
+
+extern "C" void or_shadow_volume_counts(const float* points, const float* normals, int nv,
+                                        const int* indices, int nt, const float L[3],
+                                        float infinity, const float mvp[16], int W, int H,
+                                        int depth_func, uint8_t* out_stencil, float* out_depth,
+                                        int threads) {
+    (void)nv;
+    const size_t npx = (size_t)W * H;
+    std::vector<std::atomic<uint32_t>> depth(npx);
+    for (auto& d : depth) d.store(fbits(1.0f), std::memory_order_relaxed);
+    raster_depth(points, indices, nt, mvp, W, H, GI_BIAS_NONE, 0, 0, 0, depth.data(), threads);
+    std::vector<std::atomic<int>> count(npx);
+    for (auto& c : count) c.store(0, std::memory_order_relaxed);
+    // ShadowVolume::build/update (ShadowVolumes/src/ShadowVolume.cpp:15-194).
+    static const int kPatA[6][3] = {{1, 0, 3}, {1, 3, 4}, {2, 1, 4}, {2, 4, 5}, {0, 2, 5}, {0, 5, 3}};
+    static const int kPatB[6][3] = {{4, 3, 0}, {4, 0, 1}, {5, 4, 1}, {5, 1, 2}, {3, 5, 2}, {3, 2, 0}};
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads(threads))
+    for (int t = 0; t < nt; ++t) {
+        const int* tri = indices + 3 * (size_t)t;
+        float q[6][3];
+        for (int k = 0; k < 3; ++k)
+            for (int a = 0; a < 3; ++a) {
+                q[k][a] = points[3 * (size_t)tri[k] + a];
+                q[k + 3][a] = (points[3 * (size_t)tri[k] + a] - L[a]) * infinity;
+            }
+        const float* n0 = normals + 3 * (size_t)tri[0];
+        const float* n1 = normals + 3 * (size_t)tri[1];
+        const float* n2 = normals + 3 * (size_t)tri[2];
+        float n[3];
+        for (int a = 0; a < 3; ++a) n[a] = ((n0[a] + n1[a]) + n2[a]) / 3.0f;
+        float d = n[0] * L[0] + n[1] * L[1] + n[2] * L[2];
+        const int(*pat)[3] = d >= 0.0f ? kPatA : kPatB;
+        for (int k = 0; k < 6; ++k) {
+            float c[3][4];
+            for (int j = 0; j < 3; ++j) transform(mvp, q[pat[k][j]], c[j]);
+            raster_clipped(c[0], c[1], c[2], W, H,
+                           [&](int, const Setup& s, int x, int y, const int64_t e[3]) {
+                               float z = clamp01(depth_at(s, e));
+                               size_t p = (size_t)y * W + x;
+                               uint32_t db = depth[p].load(std::memory_order_relaxed);
+                               float dv;
+                               std::memcpy(&dv, &db, 4);
+                               bool pass = depth_func == GI_DEPTH_LEQUAL ? (z <= dv) : (z < dv);
+                               if (pass) count[p].fetch_add(s.front ? 1 : -1, std::memory_order_relaxed);
+                           });
+        }
+    }
+    for (size_t p = 0; p < npx; ++p) {
+        out_stencil[p] = (uint8_t)((uint32_t)count[p].load(std::memory_order_relaxed) & 0xFFu);
+        if (out_depth) {
+            uint32_t u = depth[p].load(std::memory_order_relaxed);
+            std::memcpy(&out_depth[p], &u, 4);
+        }
+    }
+}
+
+// ===========================================================================
+// Per-pixel visibility: restatement of the fragment shaders.
+// ===========================================================================
+namespace {
+
+struct V4 {
+    float x, y, z, w;
+};
+struct V2 {
+    float x, y;
+};
+
+// GLSL built-ins as the GLSL 1.20 spec defines them.
+float gmin(float x, float y) { return y < x ? y : x; }
+float gmax(float x, float y) { return x < y ? y : x; }
+float gclamp(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
+float gmix(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+float gfract(float x) { return x - std::floor(x); }
+float gabs(float x) { return std::fabs(x); }
+
+struct Ctx {
+    const gi_vis_params* p;
+    const float* map;
+    int W, H;
+    float sx, sy;  // shadowMapStep = (1/W, 1/H)
+    float I;       // shadowIntensity
+};
+
+float fetch(const Ctx& c, float s, float t) {
+    float fi = std::floor(s * (float)c.W);
+    float fj = std::floor(t * (float)c.H);
+    if (!(fi >= 0.0f && fi < (float)c.W && fj >= 0.0f && fj < (float)c.H)) return 0.0f;
+    return c.map[(size_t)(int)fj * c.W + (int)fi];
+}
+
+V4 mat4_mul(const float m[16], V4 v) {
+    V4 r;
+    float* o = &r.x;
+    for (int row = 0; row < 4; ++row)
+        o[row] = m[0 * 4 + row] * v.x + m[1 * 4 + row] * v.y + m[2 * 4 + row] * v.z +
+                 m[3 * 4 + row] * v.w;
+    return r;
+}
+
+// computePreEvaluationBasedOnNormalOrientation (Shadow.frag:222-238 and its
+// copies in every visibility shader).
+float pretest(const Ctx& c, V4 vertex, V4 normal) {
+    if (c.p->pretest == GI_PRETEST_OFF) return 1.0f;
+    V4 ev = mat4_mul(c.p->camera_mv, vertex);
+    const float* nm = c.p->normal_matrix;
+    float nx = nm[0] * normal.x + nm[3] * normal.y + nm[6] * normal.z;
+    float ny = nm[1] * normal.x + nm[4] * normal.y + nm[7] * normal.z;
+    float nz = nm[2] * normal.x + nm[5] * normal.y + nm[8] * normal.z;
+    float inv = 1.0f / std::sqrt(nx * nx + ny * ny + nz * nz);
+    nx = nx * inv;
+    ny = ny * inv;
+    nz = nz * inv;
+    float lx = c.p->light_position[0] - ev.x;
+    float ly = c.p->light_position[1] - ev.y;
+    float lz = c.p->light_position[2] - ev.z;
+    float linv = 1.0f / std::sqrt(lx * lx + ly * ly + lz * lz);
+    lx = lx * linv;
+    ly = ly * linv;
+    lz = lz * linv;
+    if (!(normal.w != 0.0f)) {
+        nx = nx * -1.0f;
+        ny = ny * -1.0f;
+        nz = nz * -1.0f;
+    }
+    float d = nx * lx + ny * ly + nz * lz;
+    if (gmax(d, 0.0f) == 0.0f) return c.I;
+    return 1.0f;
+}
+
+// ---- Shadow.frag ----------------------------------------------------------
+float pcf_bilinear(const Ctx& c, V4 n) {
+    float incrW = 1.0f / (float)c.W, incrH = 1.0f / (float)c.H;
+    float illum = 0.0f;
+    float offset = (float)c.p->penumbra_size;
+    float step = 2.0f * offset / (float)c.p->kernel_order;
+    int count = 0;
+    for (float w = -offset; w < offset; w += step)
+        for (float h = -offset; h < offset; h += step) {
+            float d = fetch(c, n.x + w * incrW, n.y + h * incrH);
+            if (n.z <= d) illum = illum + 1.0f;
+            else illum += c.I;
+            count++;
+        }
+    return illum / (float)count;
+}
+
+void cubic(float v, float out[4]) {
+    float n[4] = {1.0f - v, 2.0f - v, 3.0f - v, 4.0f - v};
+    float s[4];
+    for (int i = 0; i < 4; ++i) s[i] = n[i] * n[i] * n[i];
+    float x = s[0];
+    float y = s[1] - 4.0f * s[0];
+    float z = s[2] - 4.0f * s[1] + 6.0f * s[0];
+    float w = 6.0f - x - y - z;
+    const float k = 1.0f / 6.0f;
+    out[0] = x * k;
+    out[1] = y * k;
+    out[2] = z * k;
+    out[3] = w * k;
+}
+
+// textureBicubic (Shadow.frag:54-84) over a NEAREST depth texture.
+float texture_bicubic(const Ctx& c, float u, float v) {
+    float tsx = (float)c.W, tsy = (float)c.H;
+    float itx = 1.0f / tsx, ity = 1.0f / tsy;
+    float tx = u * tsx - 0.5f, ty = v * tsy - 0.5f;
+    float fx = gfract(tx), fy = gfract(ty);
+    tx -= fx;
+    ty -= fy;
+    float xc[4], yc[4];
+    cubic(fx, xc);
+    cubic(fy, yc);
+    float cc[4] = {tx + -0.5f, tx + 1.5f, ty + -0.5f, ty + 1.5f};
+    float s[4] = {xc[0] + xc[1], xc[2] + xc[3], yc[0] + yc[1], yc[2] + yc[3]};
+    float num[4] = {xc[1], xc[3], yc[1], yc[3]};
+    float off[4];
+    for (int i = 0; i < 4; ++i) off[i] = cc[i] + num[i] / s[i];
+    off[0] *= itx;
+    off[1] *= itx;
+    off[2] *= ity;
+    off[3] *= ity;
+    float s0 = fetch(c, off[0], off[2]);
+    float s1 = fetch(c, off[1], off[2]);
+    float s2 = fetch(c, off[0], off[3]);
+    float s3 = fetch(c, off[1], off[3]);
+    float sx = s[0] / (s[0] + s[1]);
+    float sy = s[2] / (s[2] + s[3]);
+    return gmix(gmix(s3, s2, sx), gmix(s1, s0, sx), sy);
+}
+
+float pcf_tricubic(const Ctx& c, V4 n) {
+    float incrW = 1.0f / (float)c.W, incrH = 1.0f / (float)c.H;
+    float illum = 0.0f;
+    float offset = (float)c.p->penumbra_size;
+    float step = 2.0f * offset / (float)c.p->kernel_order;
+    int count = 0;
+    for (float w = -offset; w < offset; w += step)
+        for (float h = -offset; h < offset; h += step) {
+            float d = texture_bicubic(c, n.x + w * incrW, n.y + h * incrH);
+            if (n.z <= d) illum = illum + 1.0f;
+            else illum += c.I;
+            count++;
+        }
+    return illum / (float)count;
+}
+
+// ---- PlausibleSoftShadow.frag ----------------------------------------------
+float blocker_search_width(const Ctx& c) {
+    float R = c.p->light_radius;
+    if ((float)c.W <= 1024.0f) return R / (float)c.W;
+    return R / 1024.0f;
+}
+
+float avg_blocker_grid(const Ctx& c, V4 n) {
+    float avg = 0.0f;
+    int nb = 0;
+    float bsw = blocker_search_width(c);
+    float fw = ((float)c.p->blocker_search_size - 1.0f) * 0.5f;
+    for (int h = (int)(-fw); (float)h <= fw; h++)
+        for (int w = (int)(-fw); (float)w <= fw; w++) {
+            float d = fetch(c, n.x + ((float)w * bsw) / fw, n.y + ((float)h * bsw) / fw);
+            if (n.z > d) {
+                avg += d;
+                nb++;
+            }
+        }
+    return nb == 0 ? 1.0f : avg / (float)nb;
+}
+
+float avg_blocker_poisson(const Ctx& c, V4 n, const float* tab) {
+    float avg = 0.0f;
+    int nb = 0;
+    float bsw = blocker_search_width(c);
+    for (int i = 0; i < c.p->poisson_blocker_taps; ++i) {
+        float d = fetch(c, n.x + tab[2 * i] * bsw, n.y + tab[2 * i + 1] * bsw);
+        if (n.z > d) {
+            avg += d;
+            nb++;
+        }
+    }
+    return nb == 0 ? 1.0f : avg / (float)nb;
+}
+
+float penumbra_width(const Ctx& c, float avg, float z) {
+    if (avg < c.p->pcss_min_blocker_depth) return 0.0f;
+    float pw = ((z - avg) / avg) * c.p->light_radius;
+    return (c.p->znear * pw) / z;
+}
+
+float pcss_filter_grid(const Ctx& c, float pw, V4 n) {
+    float illum = 0.0f;
+    int K = c.p->kernel_size;
+    float step = 2.0f * pw / (float)K;
+    float fw = ((float)K - 1.0f) * 0.5f;
+    if (step <= 0.0f || step >= 1.0f) return 1.0f;
+    for (int h = (int)(-fw); (float)h <= fw; h++)
+        for (int w = (int)(-fw); (float)w <= fw; w++) {
+            float d = fetch(c, n.x + ((float)w * pw) / fw, n.y + ((float)h * pw) / fw);
+            if (n.z <= d) illum = illum + 1.0f;
+            else illum += c.I;
+        }
+    return illum / (float)(K * K);
+}
+
+float pcss_filter_poisson(const Ctx& c, float pw, V4 n, const float* tab) {
+    float illum = 0.0f;
+    int K = c.p->kernel_size;
+    float step = 2.0f * pw / (float)K;
+    if (step <= 0.0f || step >= 1.0f) return 1.0f;
+    const int nf = c.p->poisson_filter_taps;
+    for (int j = 0; j < nf; ++j) {
+        float d = fetch(c, n.x + tab[2 * j] * pw, n.y + tab[2 * j + 1] * pw);
+        if (n.z <= d) illum = illum + 1.0f;
+        else illum += c.I;
+    }
+    return illum / (float)nf;
+}
+
+// ---- RBSM/NonConservativeSMSR.frag and FilteredRBSM.frag ---------------------
+V4 nc_get_disc_all(const Ctx& c, V4 n) {  // getDisc(vec4, ..., false, false)
+    V4 dir = {0, 0, 0, 0};
+    n.x -= c.sx;
+    dir.x = (n.z <= fetch(c, n.x, n.y)) ? 1.0f : 0.0f;
+    n.x += 2.0f * c.sx;
+    dir.y = (n.z <= fetch(c, n.x, n.y)) ? 1.0f : 0.0f;
+    n.x -= c.sx;
+    n.y += c.sy;
+    dir.z = (n.z <= fetch(c, n.x, n.y)) ? 1.0f : 0.0f;
+    n.y -= 2.0f * c.sy;
+    dir.w = (n.z <= fetch(c, n.x, n.y)) ? 1.0f : 0.0f;
+    return dir;
+}
+
+bool nc_get_disc_type(const Ctx& c, V4 n, V2 dir, float disc_type) {  // getDisc(vec4, vec2, float)
+    if (dir.x == 0.0f) {
+        n.x -= c.sx;
+        float left = (n.z <= fetch(c, n.x, n.y)) ? 1.0f : 0.0f;
+        if (gabs(left - disc_type) == 0.0f) return true;
+        n.x += 2.0f * c.sx;
+        float right = (n.z <= fetch(c, n.x, n.y)) ? 1.0f : 0.0f;
+        if (gabs(right - disc_type) == 0.0f) return true;
+        n.x -= c.sx;
+    }
+    if (dir.y == 0.0f) {
+        n.y += c.sy;
+        float bottom = (n.z <= fetch(c, n.x, n.y)) ? 1.0f : 0.0f;
+        if (gabs(bottom - disc_type) == 0.0f) return true;
+        n.y -= 2.0f * c.sy;
+        float top = (n.z <= fetch(c, n.x, n.y)) ? 1.0f : 0.0f;
+        if (gabs(top - disc_type) == 0.0f) return true;
+    }
+    return false;
+}
+
+// getDisc(vec4, vec2, vec4) with its write to the global newDepth.
+bool nc_get_disc_vec(const Ctx& c, V4 n, V2 dir, V4 dt, float& new_depth) {
+    V4 rel = n;
+    new_depth = n.z;
+    const float thr = c.p->depth_threshold;
+    auto probe = [&](float s, float t) -> bool {
+        float d = fetch(c, s, t);
+        if (dt.z == 1.0f) {
+            if (gabs(n.z - d) < thr) {
+                n.z -= thr;
+                new_depth = n.z;
+            }
+        }
+        float v = (n.z <= d) ? 1.0f : 0.0f;
+        return gabs(v - dt.z) == 0.0f;
+    };
+    if (dir.x == 0.0f) {
+        if (dt.x == 0.5f || dt.x == 0.75f) {
+            rel.x = n.x - c.sx;
+            if (probe(rel.x, rel.y)) return true;
+        }
+        if (dt.x == 0.75f || dt.x == 0.25f) {
+            rel.x = n.x + c.sx;
+            if (probe(rel.x, rel.y)) return true;
+        }
+    }
+    if (dir.y == 0.0f) {
+        if (dt.y == 0.5f || dt.y == 0.75f) {
+            rel.y = n.y + c.sy;
+            if (probe(rel.x, rel.y)) return true;
+        }
+        if (dt.y == 0.75f || dt.y == 0.25f) {
+            rel.y = n.y - c.sy;
+            if (probe(rel.x, rel.y)) return true;
+        }
+    }
+    return false;
+}
+
+float nc_disc_length(const Ctx& c, V4 in_disc, V4 lc, V2 dir, float sub) {
+    V4 cc = lc;
+    float found = 0.0f;
+    float dist = 0.0f;
+    float new_depth = 0.0f;
+    V2 st = {dir.x * c.sx, dir.y * c.sy};
+    cc.x += st.x;
+    cc.y += st.y;
+    const float thr = c.p->depth_threshold;
+    for (int it = 0; it < c.p->max_search; it++) {
+        float d = fetch(c, cc.x, cc.y);
+        if (in_disc.z == 0.0f)
+            if (gabs(cc.z - d) < thr) cc.z -= thr;
+        float center = (cc.z <= d) ? 1.0f : 0.0f;
+        if (gabs(center - in_disc.z) == 0.0f) {
+            bool has = nc_get_disc_type(c, cc, V2{0.0f, 0.0f}, in_disc.z);
+            found = has ? 1.0f : 0.0f;
+            break;
+        } else {
+            bool has = nc_get_disc_vec(c, cc, dir, in_disc, new_depth);
+            if (!has) break;
+        }
+        dist = dist + 1.0f;
+        cc.x += st.x;
+        cc.y += st.y;
+        if (in_disc.z == 1.0f) cc.z = new_depth;
+    }
+    float a = dist + (1.0f - sub);
+    return gmix(-a, a, found);
+}
+
+V4 nc_orientate(const Ctx& c, V4 lc, V4 disc, V2 sub) {
+    V4 r;
+    r.x = nc_disc_length(c, disc, lc, V2{-1.0f, 0.0f}, 1.0f - sub.x);
+    r.y = nc_disc_length(c, disc, lc, V2{1.0f, 0.0f}, sub.x);
+    r.z = nc_disc_length(c, disc, lc, V2{0.0f, -1.0f}, 1.0f - sub.y);
+    r.w = nc_disc_length(c, disc, lc, V2{0.0f, 1.0f}, sub.y);
+    return r;
+}
+
+float nc_rel_pos(const Ctx& c, V2 dir, float shadow, bool filtered) {
+    float T = 1.0f;
+    if (dir.x < 0.0f && dir.y < 0.0f) T = 0.0f;
+    if (dir.x > 0.0f && dir.y > 0.0f) T = -2.0f;
+    float edge_len = gmin(gabs(dir.x) + gabs(dir.y), (float)c.p->max_search);
+    if (filtered) return (T * gabs(gmax(T * dir.x, T * dir.y))) / edge_len;
+    return (gmax(T, 2.0f * shadow - 1.0f) * gabs(gmax(T * dir.x, T * dir.y))) / edge_len;
+}
+
+float nc_revectorize(V2 r, float shadow, bool filtered) {
+    if (filtered) {
+        if (r.x * r.y < 0.0f) return (1.0f - shadow) + (2.0f * shadow - 1.0f) * gmax(r.x, r.y);
+        else if (r.x * r.y == 0.0f) return shadow;
+        return gclamp((1.0f - shadow) + (2.0f * shadow - 1.0f) * (r.x + r.y), 0.0f, 1.0f);
+    }
+    if ((r.x * r.y == 2.0f * shadow) ||
+        ((gabs(r.x) * gabs(r.y) > 0.0f) &&
+         ((1.0f - shadow) + (2.0f * shadow - 1.0f) * (gabs(r.x) + gabs(r.y)) < 0.5f)))
+        return 0.0f;
+    return 1.0f;
+}
+
+V4 nc_compute_disc(const Ctx& c, V4 n, float dist) {
+    float center = (n.z <= dist) ? 1.0f : 0.0f;
+    float disc_type = 1.0f - center;
+    V4 dir = nc_get_disc_all(c, n);
+    float dx = gabs(dir.x - center), dy = gabs(dir.y - center);
+    float dz = gabs(dir.z - center), dw = gabs(dir.w - center);
+    return V4{(2.0f * dx + dy) / 4.0f, (2.0f * dz + dw) / 4.0f, disc_type, 1.0f};
+}
+
+float nc_revectorized_tap(const Ctx& c, V4 n, V4 disc, float shadow, bool filtered) {
+    V2 sub = {gfract(n.x * (float)c.W), gfract(n.y * (float)c.H)};
+    V4 ds = nc_orientate(c, n, disc, sub);
+    V2 r = {nc_rel_pos(c, V2{ds.x, ds.y}, shadow, filtered),
+            nc_rel_pos(c, V2{ds.z, ds.w}, shadow, filtered)};
+    return gmix(nc_revectorize(r, shadow, filtered), 1.0f, c.I);
+}
+
+float nc_smsr(const Ctx& c, V4 n) {  // computeShadowFromSMSR
+    float dist = fetch(c, n.x, n.y);
+    V4 disc = nc_compute_disc(c, n, dist);
+    float shadow = (n.z <= dist) ? 1.0f : 0.0f;
+    if (disc.x > 0.0f || disc.y > 0.0f) {
+        if (disc.x == 0.75f && disc.y == 0.75f) return gmix(1.0f - shadow, 1.0f, c.I);
+        return nc_revectorized_tap(c, n, disc, shadow, false);
+    }
+    return gmix(shadow, 1.0f, c.I);
+}
+
+float nc_rpcf(const Ctx& c, V4 n, bool filtered) {  // computeShadowFromAccurateRPCF
+    float incrW = 1.0f / (float)c.W, incrH = 1.0f / (float)c.H;
+    float illum = 0.0f;
+    float offset = (float)c.p->penumbra_size;
+    float step = 2.0f * offset / (float)c.p->kernel_order;
+    int count = 0;
+    for (float w = -offset; w <= offset; w += step)
+        for (float h = -offset; h <= offset; h += step) {
+            V4 s = {n.x + w * incrW, n.y + h * incrH, n.z, n.w};
+            float d = fetch(c, s.x, s.y);
+            float shadow = (s.z <= d) ? 1.0f : 0.0f;
+            V4 disc = nc_compute_disc(c, s, d);
+            if (disc.x > 0.0f || disc.y > 0.0f) {
+                illum += nc_revectorized_tap(c, s, disc, shadow, filtered);
+            } else {
+                shadow = gmix(shadow, 1.0f, c.I);
+                illum += shadow;
+            }
+            count++;
+        }
+    return illum / (float)count;
+}
+
+// ---- RBSM/ConservativeSMSR.frag ---------------------------------------------
+V4 cs_compute_disc(const Ctx& c, V4 s) {
+    V4 dir = {0, 0, 0, 0};
+    s.x -= c.sx;
+    dir.x = (s.z <= fetch(c, s.x, s.y)) ? 1.0f : 0.0f;
+    s.x += 2.0f * c.sx;
+    dir.y = (s.z <= fetch(c, s.x, s.y)) ? 1.0f : 0.0f;
+    s.x -= c.sx;
+    s.y += c.sy;
+    dir.z = (s.z <= fetch(c, s.x, s.y)) ? 1.0f : 0.0f;
+    s.y -= 2.0f * c.sy;
+    dir.w = (s.z <= fetch(c, s.x, s.y)) ? 1.0f : 0.0f;
+    return V4{gabs(dir.x - 1.0f), gabs(dir.y - 1.0f), gabs(dir.z - 1.0f), gabs(dir.w - 1.0f)};
+}
+
+float cs_rel_dist(const Ctx& c, V4 s, V2 dir, float cc) {
+    V4 t = s;
+    float found = 0.0f, distance = 0.0f;
+    V2 st = {dir.x * c.sx, dir.y * c.sy};
+    t.x += st.x;
+    t.y += st.y;
+    const float thr = c.p->depth_threshold;
+    for (int it = 0; it < c.p->max_search; it++) {
+        float d = fetch(c, t.x, t.y);
+        if (gabs(t.z - d) < thr) t.z -= thr;
+        float center = (t.z <= d) ? 1.0f : 0.0f;
+        bool umbra = !(center != 0.0f);
+        if (umbra) {
+            found = 1.0f;
+            break;
+        } else {
+            V4 dd = cs_compute_disc(c, t);
+            if ((dd.x + dd.y + dd.z + dd.w) == 0.0f) break;
+        }
+        distance = distance + 1.0f;
+        t.x += st.x;
+        t.y += st.y;
+    }
+    distance = distance + (1.0f - cc);
+    return gmix(-distance, distance, found);
+}
+
+float cs_normalize(const Ctx& c, V2 d) {
+    float T = 1.0f;
+    if (d.x < 0.0f && d.y < 0.0f) T = 0.0f;
+    if (d.x > 0.0f && d.y > 0.0f) T = -2.0f;
+    float len = gmin(gabs(d.x) + gabs(d.y), (float)c.p->max_search);
+    return gabs(gmax(T * d.x, T * d.y)) / len;
+}
+
+float cs_revectorize(const Ctx& c, V2 r) {
+    if ((r.x * r.y > 0.0f) && (1.0f - r.x > r.y)) return c.I;
+    return 1.0f;
+}
+
+float cs_revectorized(const Ctx& c, V4 s) {
+    V2 sub = {gfract(s.x * (float)c.W), gfract(s.y * (float)c.H)};
+    float dl = cs_rel_dist(c, s, V2{-1.0f, 0.0f}, 1.0f - sub.x);
+    float dr = cs_rel_dist(c, s, V2{1.0f, 0.0f}, sub.x);
+    float db = cs_rel_dist(c, s, V2{0.0f, -1.0f}, 1.0f - sub.y);
+    float dt = cs_rel_dist(c, s, V2{0.0f, 1.0f}, sub.y);
+    V2 r = {cs_normalize(c, V2{dl, dr}), cs_normalize(c, V2{db, dt})};
+    return cs_revectorize(c, r);
+}
+
+float cs_smsr(const Ctx& c, V4 s) {  // computeShadowFromSMSR (conservative)
+    float d = fetch(c, s.x, s.y);
+    float shadow = (s.z <= d) ? 1.0f : 0.0f;
+    if (shadow == 0.0f) return c.I;
+    V4 dd = cs_compute_disc(c, s);
+    if ((dd.x + dd.y + dd.z + dd.w) == 0.0f) return 1.0f;
+    else if ((dd.x + dd.y) == 2.0f || (dd.z + dd.w) == 2.0f) return c.I;
+    return cs_revectorized(c, s);
+}
+
+float cs_rpcf(const Ctx& c, V4 n) {  // computeShadowFromRPCF (conservative)
+    float incrW = 1.0f / (float)c.W, incrH = 1.0f / (float)c.H;
+    float illum = 0.0f;
+    float offset = (float)c.p->penumbra_size;
+    float step = 2.0f * offset / (float)c.p->kernel_order;
+    int count = 0;
+    for (float w = -offset; w <= offset; w += step)
+        for (float h = -offset; h <= offset; h += step) {
+            float d = fetch(c, n.x + w * incrW, n.y + h * incrH);
+            float shadow = (n.z <= d) ? 1.0f : c.I;
+            if (shadow == 1.0f) {
+                V4 s = {n.x + w * incrW, n.y + h * incrH, n.z, n.w};
+                V4 dd = cs_compute_disc(c, s);
+                if (dd.x == 0.0f && dd.y == 0.0f) illum = illum + 1.0f;
+                else illum += cs_revectorized(c, s);
+            } else {
+                illum += c.I;
+            }
+            count++;
+        }
+    return illum / (float)count;
+}
+
+float shade_pixel(const Ctx& c, V4 vertex, V4 normal, const float* poisson) {
+    if (vertex.x == 0.0f) return 0.0f;  // discard: the target keeps its clear value 0
+    const gi_vis_params* p = c.p;
+    V4 sc = mat4_mul(p->light_mvp_biased, vertex);
+    V4 n = {sc.x / sc.w, sc.y / sc.w, sc.z / sc.w, sc.w / sc.w};
+    float shadow = pretest(c, vertex, normal);
+    switch (p->technique) {
+        case GI_TECH_HARD:
+            if (sc.w > 0.0f && shadow == 1.0f) {
+                float d = fetch(c, n.x, n.y);
+                shadow = (n.z <= d) ? 1.0f : c.I;
+            }
+            return shadow;
+        case GI_TECH_PCF:
+            if (sc.w > 0.0f && shadow == 1.0f) shadow = pcf_bilinear(c, n);
+            return shadow;
+        case GI_TECH_PCF_TRICUBIC:
+            if (sc.w > 0.0f && shadow == 1.0f) shadow = pcf_tricubic(c, n);
+            return shadow;
+        case GI_TECH_PCSS_GRID:
+            if (sc.w > 0.0f && shadow == 1.0f) {
+                float avg = avg_blocker_grid(c, n);
+                float pw = penumbra_width(c, avg, n.z);
+                shadow = pcss_filter_grid(c, pw, n);
+            }
+            return shadow;
+        case GI_TECH_PCSS_POISSON:
+            if (sc.w > 0.0f && shadow == 1.0f) {
+                float avg = avg_blocker_poisson(c, n, poisson);
+                float pw = penumbra_width(c, avg, n.z);
+                shadow = pcss_filter_poisson(c, pw, n, poisson + 2 * p->poisson_blocker_taps);
+            }
+            return shadow;
+        case GI_TECH_SMSR_NONCONSERVATIVE:
+            if (shadow == 1.0f) shadow = nc_smsr(c, n);
+            return shadow;
+        case GI_TECH_RPCF_SMSR:
+            if (shadow == 1.0f) shadow = nc_rpcf(c, n, false);
+            return shadow;
+        case GI_TECH_RSMSS:
+            if (shadow == 1.0f) shadow = nc_rpcf(c, n, true);
+            return shadow;
+        case GI_TECH_SMSR_CONSERVATIVE:
+            if (shadow == 1.0f) shadow = cs_smsr(c, n);
+            return shadow;
+        case GI_TECH_RPCF_CONSERVATIVE:
+            if (shadow == 1.0f) shadow = cs_rpcf(c, n);
+            return shadow;
+        case GI_TECH_HARD_SOFTAPP: {
+            float r = shadow;
+            if (sc.w > 0.0f && r == 1.0f) {
+                float d = fetch(c, n.x, n.y);
+                r = (n.z <= d) ? 1.0f : c.I;
+            }
+            if (pretest(c, vertex, normal) == c.I) r = 0.0f;
+            return r;
+        }
+        default:
+            return 0.0f;
+    }
+}
+
+}  // namespace
+
+extern "C" void or_visibility(const gi_vis_params* p, const float* depth, int map_w, int map_h,
+                              const float* pos, const float* nrm, float* out, int W, int H,
+                              const float* poisson_xy, int threads) {
+    Ctx c;
+    c.p = p;
+    c.map = depth;
+    c.W = map_w;
+    c.H = map_h;
+    c.sx = (float)(1.0 / map_w);  // glUniform2f(1.0/w, 1.0/h): double then float
+    c.sy = (float)(1.0 / map_h);
+    c.I = p->shadow_intensity;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads(threads))
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            size_t i = (size_t)y * W + x;
+            V4 v = {pos[4 * i], pos[4 * i + 1], pos[4 * i + 2], pos[4 * i + 3]};
+            V4 nn = {nrm[4 * i], nrm[4 * i + 1], nrm[4 * i + 2], nrm[4 * i + 3]};
+            out[i] = shade_pixel(c, v, nn, poisson_xy);
+        }
+}

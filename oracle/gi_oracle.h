@@ -1,0 +1,63 @@
+/*
+ * gi_oracle.h -- CPU oracle for the shadow-visibility path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library restates, in plain scalar C++,
+ * the reference's GLSL passes and the OpenGL fixed-function rules they rely
+ * on (rasterisation, depth test, polygon offset, clipping, NEAREST texture
+ * fetch with CLAMP_TO_BORDER, stencil INCR_WRAP/DECR_WRAP).  It is the
+ * checker of the CUDA path: only the tests, the smoke check and the CPU
+ * baseline leg of the benchmark may load it.  The product never calls it.
+ *
+ * Parity status: the reference's passes run only through OpenGL, which is
+ * not available here, so these functions are pinned by hand-derived
+ * known-answer tests; the matrix helpers of the product are pinned against
+ * the reference's vendored glm.  The GL rules are the ones written in the
+ * OpenGL 4.x specification; where the spec leaves a choice (sub-pixel
+ * precision, fill convention, polygon-offset r), the choice is stated in
+ * gi_oracle.cpp.
+ *
+ * All images are row-major with row 0 at the bottom; matrices column-major.
+ */
+#ifndef GI_ORACLE_H
+#define GI_ORACLE_H
+
+#include <stdint.h>
+
+#include "../include/gi_shadow.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Light-view depth map: clear to 1, rasterise, LESS, bias, clamp. */
+void or_shadow_map(const float* points, int nv, const int* indices, int nt,
+                   const float mvp[16], int width, int height, int bias_mode,
+                   float constant_bias, float offset_factor, float offset_units,
+                   float* out_depth, int threads);
+
+/* G-buffer: (object position, 1) and (normal, frontFacing); background
+ * (0,0,0,1) in both. */
+void or_gbuffer(const float* points, const float* normals, int nv,
+                const int* indices, int nt, const float mvp[16], int width,
+                int height, float* out_pos, float* out_nrm, int threads);
+
+/* Per-pixel visibility (r channel).  poisson_xy holds the PCSS Poisson
+ * tables: poisson_blocker_taps (x, y) pairs for the blocker search followed
+ * by poisson_filter_taps pairs for the filter (NULL for other techniques). */
+void or_visibility(const gi_vis_params* p, const float* depth, int map_w,
+                   int map_h, const float* pos, const float* nrm, float* out,
+                   int width, int height, const float* poisson_xy,
+                   int threads);
+
+/* Shadow-volume stencil counts (uint8, wrapping). out_depth may be NULL. */
+void or_shadow_volume_counts(const float* points, const float* normals,
+                             int nv, const int* indices, int nt,
+                             const float light_pos[3], float infinity,
+                             const float mvp[16], int width, int height,
+                             int depth_func, uint8_t* out_stencil,
+                             float* out_depth, int threads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,37 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+REFERENCE = "/root/reference"
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA device (runs on the GB300 box)")
+    # Build (incrementally) the library and the oracle before any test imports them.
+    from globalillumination_gb300.build import build_library
+    from oracle.build_oracle import build_oracle
+
+    build_library()
+    build_oracle()
+
+
+def has_reference() -> bool:
+    return os.path.isdir(os.path.join(REFERENCE, "Configs"))
+
+
+@pytest.fixture(scope="session")
+def cuda_ctx():
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import globalillumination_gb300 as gi
+
+    ctx = gi.Context(0)
+    yield ctx
+    ctx.close()

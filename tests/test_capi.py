@@ -1,0 +1,97 @@
+"""The C ABI library loads, exports every symbol the header declares, and
+reports argument errors through gi_status without touching a GPU."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from globalillumination_gb300 import _capi as api
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "gi_shadow.h")
+
+
+def header_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gi_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_entry_points():
+    fns = header_functions()
+    for name in ("gi_shadow_map", "gi_gbuffer", "gi_visibility", "gi_shadow_volume_counts",
+                 "gi_scene_load_config", "gi_frame_setup", "gi_context_create"):
+        assert name in fns
+
+
+def test_library_exports_every_declared_symbol():
+    lib = api.load()
+    missing = [f for f in header_functions() if not hasattr(lib, f)]
+    assert not missing, missing
+
+
+def test_bindings_cover_header():
+    assert set(header_functions()) == set(api.exported_symbols())
+
+
+def test_struct_layouts():
+    # the ctypes mirrors must match the C layout (checked through sizes)
+    assert C.sizeof(api.VisParams) == 14 * 4 + 16 * 4 * 2 + 9 * 4 + 3 * 4
+    assert C.sizeof(api.View) == 12 * 4 + 2 * 4
+    assert C.sizeof(api.MapParams) == 6 * 4
+
+
+def test_version_and_error_string():
+    lib = api.load()
+    assert lib.gi_version().startswith(b"gi_shadow")
+    st = lib.gi_frame_setup(None, None, None)
+    assert st == api.GI_ERR_INVALID_ARG
+    assert b"NULL" in lib.gi_last_error_string()
+
+
+def test_invalid_views_rejected():
+    lib = api.load()
+    bad = api.View(api.F3(0, 0, 0), api.F3(0, 0, 1), api.F3(0, 1, 0), 45.0, 0.0, 1000.0, 64, 64)
+    P, V = api.F16(), api.F16()
+    assert lib.gi_view_matrices(C.byref(bad), P, V) == api.GI_ERR_INVALID_ARG
+    bad.znear, bad.width = 1.0, 0
+    assert lib.gi_view_matrices(C.byref(bad), P, V) == api.GI_ERR_INVALID_ARG
+    bad.width, bad.fovy_deg = 64, 180.0
+    assert lib.gi_view_matrices(C.byref(bad), P, V) == api.GI_ERR_INVALID_ARG
+
+
+def test_pass_argument_checks_before_device_work():
+    lib = api.load()
+    p = api.VisParams()
+    assert lib.gi_vis_params_default(api.GI_TECH_PCF, C.byref(p)) == api.GI_OK
+    assert lib.gi_vis_params_default(99, C.byref(p)) == api.GI_ERR_INVALID_ARG
+    # NULL context / buffers
+    assert lib.gi_visibility(None, C.byref(p), None, 4, 4, None, None, None, 4, 4, None) == api.GI_ERR_INVALID_ARG
+    assert lib.gi_shadow_map(None, None, None, api.F16(), None, None) == api.GI_ERR_INVALID_ARG
+    assert lib.gi_gbuffer(None, None, api.F16(), 4, 4, None, None, None) == api.GI_ERR_INVALID_ARG
+
+
+def test_poisson_table():
+    lib = api.load()
+    import numpy as np
+
+    t = np.empty(128, np.float32)
+    assert lib.gi_poisson_table(64, t.ctypes.data) == api.GI_OK
+    xy = t.reshape(64, 2)
+    r = np.hypot(xy[:, 0], xy[:, 1])
+    assert (r <= 1.0).all()
+    d = np.hypot(xy[:, None, 0] - xy[None, :, 0], xy[:, None, 1] - xy[None, :, 1]) + np.eye(64) * 9
+    assert d[:16, :16].min() > 0.3  # the 16-tap prefix is well spread
+    assert lib.gi_poisson_table(65, t.ctypes.data) == api.GI_ERR_INVALID_ARG
+    assert lib.gi_poisson_table(0, t.ctypes.data) == api.GI_ERR_INVALID_ARG
+
+
+def test_context_without_device_fails_cleanly():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    lib = api.load()
+    h = C.c_void_p()
+    assert lib.gi_context_create(0, C.byref(h)) == api.GI_ERR_CUDA
+    assert lib.gi_last_error_string()
