@@ -1,0 +1,414 @@
+#!/usr/bin/env python
+"""Shadowed frames per second on the pcss_1080p workload.
+
+Workload (the 1080p PCSS scene): ground + 64 seeded icospheres (81,922
+triangles), 2048^2 FP32 light map with polygon offset (4, 20), 1920 x 1080
+camera, PCSS with 16 Poisson blocker taps and 32 filter taps.  One step is
+one shadowed frame: light-view depth map, G-buffer, visibility.
+
+  value   frames/s with the scene resident in HBM, timed per step with CUDA
+          events on the launching stream; L2 is flushed (256 MiB write)
+          before every timed step, outside the step's events
+  e2e     frames/s through the C ABI with host buffers: every step uploads
+          the scene from pinned host memory (gi_scene_upload_from), renders,
+          and reads the visibility buffer back to pinned host memory
+  roofline  the visibility kernel (the frame's largest): algorithmic bytes
+          36 P + 4 S^2 per launch over its event-timed duration, against the
+          measured HBM copy bandwidth
+  cpu_baseline  the CPU oracle (restatement of the reference's passes) on
+          the host cores for a bounded sample of whole frames
+
+--impl reference times that CPU implementation alone (the reference's own
+passes need OpenGL, which this machine does not have).  For N > 1 every rank
+renders its own frames (replicas; no collective on the data path) and the
+slowest rank's time is used.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("shadowed frames/sec @1080p, batched+surrogate vs plain GPU pass at ≤1% vis error; "
+          "HBM GB/s")
+UNIT = "frames/s"
+L2_FLUSH_BYTES = 256 << 20
+CPU_SAMPLE_SECONDS = 10.0
+THROTTLE_BAD = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="render --warmup frames and exit (the command profiled with ncu)")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+def workload_config(w, tris):
+    return {
+        "workload": "pcss_1080p",
+        "triangles": int(tris),
+        "light_map": f"{w.map_params.width}x{w.map_params.height} fp32, polygon offset (4, 20)",
+        "camera": f"{w.camera.width}x{w.camera.height}",
+        "technique": "PCSS, 16 Poisson blocker taps + 32 filter taps, light radius 0.25",
+        "step": "light map + G-buffer + visibility (one shadowed frame)",
+        "l2": "flushed (256 MiB write) before each timed step, outside the step's events",
+        "scene_seed": "0x5EED0001",
+    }
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else ".",
+                                 f".clocks_{os.getpid()}.csv")
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 8:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        smax = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        power = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in rows:
+            for name, v in zip(names, r[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(smax) if smax else None,
+            "power_w_max": max(power) if power else None,
+            "samples": len(rows),
+            "reasons": sorted(reasons),
+        }
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle frames (cpu_baseline and the reference arm)
+# ---------------------------------------------------------------------------
+def oracle_frame(arrays, fr, w, tab, threads):
+    import oracle
+
+    p, n, i = arrays
+    mp = w.map_params
+    S, W, H = mp.width, w.camera.width, w.camera.height
+    d = oracle.shadow_map(p, i, fr.light_mvp, S, S, mp.bias_mode, mp.constant_bias, mp.offset_factor,
+                          mp.offset_units, threads=threads)
+    pos, nrm = oracle.gbuffer(p, n, i, fr.camera_mvp, W, H, threads=threads)
+    return oracle.visibility(w.params.to_c(fr), d, S, S, pos, nrm, W, H, tab, threads=threads)
+
+
+def cpu_frames(min_seconds: float, max_frames: int, setup):
+    arrays, fr, w, tab, threads = setup
+    times = []
+    t_all = time.perf_counter()
+    while len(times) < max_frames and (time.perf_counter() - t_all) < min_seconds:
+        t0 = time.perf_counter()
+        oracle_frame(arrays, fr, w, tab, threads)
+        times.append(time.perf_counter() - t0)
+    return times
+
+
+def cpu_setup():
+    import numpy as np
+
+    from oracle.build_oracle import build_oracle
+    import globalillumination_gb300 as gi
+    from globalillumination_gb300 import scenes
+
+    build_oracle()
+    w = scenes.pcss_1080p()
+    fr = gi.frame_setup(w.light, w.camera)
+    tab = np.concatenate([gi.poisson_table(w.params.poisson_blocker_taps).reshape(-1),
+                          gi.poisson_table(w.params.poisson_filter_taps).reshape(-1)])
+    threads = os.cpu_count() or 1
+    return (w.scene.arrays(), fr, w, tab, threads)
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    setup = cpu_setup()
+    w = setup[2]
+    threads = setup[4]
+    for _ in range(args.warmup):
+        oracle_frame(*setup[:4], threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle_frame(*setup[:4], threads)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = len(times) / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": workload_config(w, setup[0][2].shape[0]),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{len(times)} whole frames (light map, G-buffer, PCSS visibility) of "
+                                   "the CPU restatement of the reference's passes, OpenMP on all host threads; "
+                                   "the reference's own passes run only through OpenGL, unavailable on this box"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def traffic_from_profiles():
+    path = os.path.join(ROOT, "profiles", "visibility_pcss_1080p.md")
+    if not os.path.exists(path):
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
+    return float(m.group(1)) if m else None
+
+
+def measured_hbm_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from globalillumination_gb300.build import LIB, build_library
+
+    if not os.path.exists(LIB):
+        build_library()
+    import globalillumination_gb300 as gi
+    from globalillumination_gb300 import scenes
+
+    w = scenes.pcss_1080p()
+    fr = gi.frame_setup(w.light, w.camera)
+    S, W, H = w.map_params.width, w.camera.width, w.camera.height
+    P = W * H
+    ctx = gi.Context(local)
+    stream = torch.cuda.current_stream()
+    w.scene.upload(ctx, stream)
+    pts, nrm, idx = w.scene.arrays()
+    tris = idx.shape[0]
+    bufs = gi.allocate_frame(S, S, W, H, local)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def frame():
+        gi.render_frame(ctx, w.scene, fr, w.map_params, w.params, W, H, bufs, stream)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    if args.profile:
+        for _ in range(max(args.warmup, 1)):
+            frame()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_frames": max(args.warmup, 1), "launches": ctx.launch_count}), flush=True)
+        ctx.close()
+        return 0
+    for _ in range(max(args.warmup, 3)):
+        frame()
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    # soak: bring clocks to their loaded state (about a second of frames)
+    t_soak = time.perf_counter()
+    while time.perf_counter() - t_soak < 1.5:
+        for _ in range(50):
+            frame()
+        torch.cuda.synchronize()
+
+    # ---- timed region -------------------------------------------------------
+    K = args.steps
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    launches0 = ctx.launch_count
+    barrier()
+    wall0 = time.perf_counter()
+    for k in range(K):
+        flush.fill_(float(k))
+        starts[k].record(stream)
+        frame()
+        ends[k].record(stream)
+    barrier()
+    wall = time.perf_counter() - wall0
+    launches = ctx.launch_count - launches0
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    if dist is not None:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * K / (total_ms / 1000.0)
+
+    # ---- per-pass breakdown (same frames, events between passes) -------------
+    R = max(20, min(K, 100))
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(R)]
+    for r in range(R):
+        flush.fill_(float(r))
+        ev[r][0].record(stream)
+        gi.render_shadow_map(ctx, w.scene, w.map_params, fr.light_mvp, bufs.depth, stream)
+        ev[r][1].record(stream)
+        gi.render_gbuffer(ctx, w.scene, fr.camera_mvp, W, H, bufs.pos, bufs.nrm, stream)
+        ev[r][2].record(stream)
+        gi.compute_visibility(ctx, w.params, fr, bufs.depth, S, S, bufs.pos, bufs.nrm, bufs.vis, W, H, stream)
+        ev[r][3].record(stream)
+    torch.cuda.synchronize()
+    pass_ms = {
+        "shadow_map": statistics.mean(e[0].elapsed_time(e[1]) for e in ev),
+        "gbuffer": statistics.mean(e[1].elapsed_time(e[2]) for e in ev),
+        "visibility": statistics.mean(e[2].elapsed_time(e[3]) for e in ev),
+    }
+
+    # ---- end to end through the C ABI with host buffers ---------------------
+    h_pts = torch.from_numpy(pts.reshape(-1).copy()).pin_memory()
+    h_nrm = torch.from_numpy(nrm.reshape(-1).copy()).pin_memory()
+    h_idx = torch.from_numpy(idx.reshape(-1).copy()).pin_memory()
+    h_vis = torch.empty(P, dtype=torch.float32).pin_memory()
+    e2e_scene = gi.Scene()
+
+    def e2e_step():
+        e2e_scene.upload_from(ctx, h_pts.data_ptr(), h_nrm.data_ptr(), pts.shape[0], h_idx.data_ptr(), tris, stream)
+        gi.render_frame(ctx, e2e_scene, fr, w.map_params, w.params, W, H, bufs, stream)
+        h_vis.copy_(bufs.vis, non_blocking=True)
+
+    for _ in range(3):
+        e2e_step()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(K):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * K / (e2e_ms / 1000.0)
+    h2d = pts.nbytes + nrm.nbytes + idx.nbytes
+    d2h = P * 4
+    clk = clocks.stop()
+
+    # sanity: the frame produced soft shadows
+    vis_host = bufs.vis.cpu().numpy()
+    frac_soft = float(((vis_host > 0.25) & (vis_host < 1.0)).mean())
+
+    if rank == 0:
+        peak, peak_kind = measured_hbm_peak()
+        alg_bytes = 36 * P + 4 * S * S
+        vis_s = pass_ms["visibility"] / 1000.0
+        achieved = alg_bytes / vis_s / 1e9
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+            "warmup": args.warmup, "ms_per_step": total_ms / K, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(w, tris),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches),
+            "roofline": {"kernel": "k_visibility<PCSS_POISSON>", "bound": "hbm", "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": peak_kind, "traffic": traffic_from_profiles(),
+                         "algorithmic_bytes_per_launch": alg_bytes},
+            "pass_ms": pass_ms,
+            "step_ms_median": statistics.median(step_ms),
+            "wall_s_timed_region": wall,
+            "clocks": clk,
+            "soft_pixel_fraction": frac_soft,
+        }
+        if clk and any(r in clk["reasons"] for r in THROTTLE_BAD):
+            line["clocks_warning"] = "throttled during the timed region"
+        if world == 1 and not args.no_cpu_baseline:
+            setup = cpu_setup()
+            times = cpu_frames(CPU_SAMPLE_SECONDS, 50, setup)
+            line["cpu_baseline"] = {
+                "value": len(times) / sum(times), "unit": UNIT, "cores": setup[4], "kind": "port",
+                "sample": f"{len(times)} whole pcss_1080p frames (light map, G-buffer, visibility) of the CPU "
+                          "oracle, OpenMP on all host threads"}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    ctx.close()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -158,6 +158,7 @@ _PROTOS = {
     "gi_gen_displaced_sphere": (C.c_int, [_VP, C.c_int, C.c_int, C.c_float, C.c_float, F3, C.c_uint64]),
     "gi_gen_icosphere_field": (C.c_int, [_VP, C.c_int, C.c_int, F3, F3, C.c_float, C.c_float, C.c_uint64]),
     "gi_scene_upload": (C.c_int, [_VP, _VP, _VP]),
+    "gi_scene_upload_from": (C.c_int, [_VP, _VP, _VP, _VP, C.c_int, _VP, C.c_int, _VP]),
     "gi_scene_device_arrays": (C.c_int, [_VP, C.POINTER(_VP), C.POINTER(_VP), C.POINTER(_VP)]),
     "gi_view_matrices": (C.c_int, [C.POINTER(View), F16, F16]),
     "gi_frame_setup": (C.c_int, [C.POINTER(View), C.POINTER(View), C.POINTER(FrameMatrices)]),

@@ -160,6 +160,48 @@ extern "C" gi_status gi_scene_upload(gi_scene* s, gi_context* ctx, void* stream)
     return GI_OK;
 }
 
+extern "C" gi_status gi_scene_upload_from(gi_scene* s, gi_context* ctx, const float* hp,
+                                          const float* hn, int nv, const int* hi, int nt,
+                                          void* stream) {
+    if (!s || !ctx || nv < 0 || nt < 0 || (nv > 0 && (!hp || !hn)) || (nt > 0 && !hi))
+        return fail(GI_ERR_INVALID_ARG, "gi_scene_upload_from: bad arguments");
+    if ((size_t)nt >= ((size_t)1 << 29)) return fail(GI_ERR_CAPACITY, "more than 2^29 triangles");
+    gi_status st = check_device(ctx);
+    if (st != GI_OK) return st;
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    if (s->device >= 0 && s->device != ctx->device) {
+        cudaFree(s->d_points);
+        cudaFree(s->d_normals);
+        cudaFree(s->d_indices);
+        s->d_points = s->d_normals = nullptr;
+        s->d_indices = nullptr;
+        s->cap_vertices = s->cap_triangles = 0;
+    }
+    s->device = ctx->device;
+    size_t capv = s->cap_vertices * 3 * sizeof(float), capn = capv;
+    size_t capi = s->cap_triangles * 3 * sizeof(int);
+    const size_t vb = (size_t)nv * 3 * sizeof(float), ib = (size_t)nt * 3 * sizeof(int);
+    if (capv < vb || capi < ib) {
+        // growing frees the old buffers: let queued work that reads them finish
+        cudaError_t e = cudaStreamSynchronize(cs);
+        if (e != cudaSuccess) return gi::fail_cuda(e, "gi_scene_upload_from sync");
+    }
+    st = gi::ensure_buffer(reinterpret_cast<void**>(&s->d_points), &capv, vb);
+    if (st == GI_OK) st = gi::ensure_buffer(reinterpret_cast<void**>(&s->d_normals), &capn, vb);
+    if (st == GI_OK) st = gi::ensure_buffer(reinterpret_cast<void**>(&s->d_indices), &capi, ib);
+    if (st != GI_OK) return st;
+    s->cap_vertices = capv / (3 * sizeof(float));
+    s->cap_triangles = capi / (3 * sizeof(int));
+    cudaError_t e = cudaSuccess;
+    if (vb) e = cudaMemcpyAsync(s->d_points, hp, vb, cudaMemcpyHostToDevice, cs);
+    if (e == cudaSuccess && vb) e = cudaMemcpyAsync(s->d_normals, hn, vb, cudaMemcpyHostToDevice, cs);
+    if (e == cudaSuccess && ib) e = cudaMemcpyAsync(s->d_indices, hi, ib, cudaMemcpyHostToDevice, cs);
+    if (e != cudaSuccess) return gi::fail_cuda(e, "gi_scene_upload_from copy");
+    s->dev_vertices = nv;
+    s->dev_triangles = nt;
+    return GI_OK;
+}
+
 extern "C" gi_status gi_scene_device_arrays(const gi_scene* s, const float** p, const float** n,
                                             const int** i) {
     if (!s) return fail(GI_ERR_INVALID_ARG, "gi_scene_device_arrays: NULL scene");

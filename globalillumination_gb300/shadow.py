@@ -173,6 +173,14 @@ class Scene:
         check(_lib().gi_scene_upload(self.handle, ctx.handle, _stream_ptr(stream)), "gi_scene_upload")
         return self
 
+    def upload_from(self, ctx: Context, points_ptr: int, normals_ptr: int, num_vertices: int,
+                    indices_ptr: int, num_triangles: int, stream=None) -> "Scene":
+        """Replaces the device geometry with caller-owned host arrays (pinned for async copies)."""
+        check(_lib().gi_scene_upload_from(self.handle, ctx.handle, C.c_void_p(points_ptr), C.c_void_p(normals_ptr),
+                                          int(num_vertices), C.c_void_p(indices_ptr), int(num_triangles),
+                                          _stream_ptr(stream)), "gi_scene_upload_from")
+        return self
+
     def close(self) -> None:
         if self.handle:
             _lib().gi_scene_destroy(self.handle)

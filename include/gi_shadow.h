@@ -152,6 +152,16 @@ gi_status gi_gen_icosphere_field(gi_scene* scene, int count, int level,
  * the scene, on `stream` (the reference re-uploads its VBOs every draw:
  * MyGLGeometryViewer::loadVBOs, MyGLGeometryViewer.cpp:383-405). */
 gi_status gi_scene_upload(gi_scene* scene, gi_context* ctx, void* stream);
+/* Replaces the scene's device geometry with caller-owned host arrays
+ * (points/normals float[3V], indices int[3T]) on `stream`; pinned host
+ * memory makes the copies asynchronous.  This is the per-draw VBO upload of
+ * MyGLGeometryViewer::loadVBOs (MyGLGeometryViewer.cpp:383-405) without the
+ * host mesh; the host copy inside the scene is left unchanged.  Index
+ * values are trusted: they must lie in [0, V). */
+gi_status gi_scene_upload_from(gi_scene* scene, gi_context* ctx,
+                               const float* h_points, const float* h_normals,
+                               int num_vertices, const int* h_indices,
+                               int num_triangles, void* stream);
 /* Device pointers of the uploaded geometry (NULL before upload). */
 gi_status gi_scene_device_arrays(const gi_scene* scene, const float** d_points,
                                  const float** d_normals, const int** d_indices);

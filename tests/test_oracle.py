@@ -1,0 +1,215 @@
+"""Known-answer tests of the CPU oracle (no GPU).
+
+The reference has no tests or golden images, so the oracle is pinned here
+by answers derived by hand from the rules it restates: the GL raster rules
+(coverage, window-space depth, polygon offset, top-left ownership of shared
+edges), the fragment-shader quirks (PCF's float loop, PCSS cut-offs,
+CLAMP_TO_BORDER, background discard) and the shadow-volume counts.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from globalillumination_gb300 import _capi as api
+import globalillumination_gb300 as gi
+
+IDENTITY = np.eye(4, dtype=np.float32).reshape(-1)
+
+
+def ndc(xw, yw, W, H):
+    return xw / (W / 2.0) - 1.0, yw / (H / 2.0) - 1.0
+
+
+def test_single_triangle_depth_is_the_window_plane():
+    W = H = 64
+    win = [(8.25, 10.5, 0.25), (50.0, 12.75, 0.625), (20.5, 55.25, 0.875)]  # (x_w, y_w, z_w)
+    pts = []
+    for xw, yw, zw in win:
+        x, y = ndc(xw, yw, W, H)
+        pts.append((x, y, 2.0 * zw - 1.0))
+    pts = np.array(pts, np.float32)
+    d = oracle.shadow_map(pts, np.array([[0, 1, 2]]), IDENTITY, W, H).reshape(H, W)
+    A = np.array([[w[0], w[1], 1.0] for w in win])
+    coef = np.linalg.solve(A, np.array([w[2] for w in win]))
+    ys, xs = np.mgrid[0:H, 0:W] + 0.5
+    # barycentrics of pixel centres
+    P = np.stack([xs, ys], -1)
+    v = np.array([w[:2] for w in win])
+
+    def e(a, b):
+        return (v[b, 0] - v[a, 0]) * (P[..., 1] - v[a, 1]) - (v[b, 1] - v[a, 1]) * (P[..., 0] - v[a, 0])
+
+    E = np.stack([e(1, 2), e(2, 0), e(0, 1)], -1)
+    inside = (E > 1e-9).all(-1)
+    boundary = (np.abs(E) <= 1e-9).any(-1)
+    plane = coef[0] * xs + coef[1] * ys + coef[2]
+    assert (d[inside] < 1.0).all()
+    assert (d[~inside & ~boundary] == 1.0).all()
+    assert np.abs(d[inside] - plane[inside]).max() < 3e-7
+    assert inside.sum() > 600
+
+
+def test_shared_diagonal_owned_by_one_triangle():
+    # square [8, 40]^2 split along y = x, which runs through pixel centres;
+    # A (below) has the diagonal as a left edge and owns it, B does not.
+    W = H = 64
+    corner = {k: ndc(*k, W, H) for k in [(8, 8), (40, 8), (40, 40), (8, 40)]}
+    za, zb = 0.2, 0.4
+    pts = np.array([[*corner[(8, 8)], za], [*corner[(40, 8)], za], [*corner[(40, 40)], za],
+                    [*corner[(8, 8)], zb], [*corner[(40, 40)], zb], [*corner[(8, 40)], zb]], np.float32)
+    d = oracle.shadow_map(pts, np.array([[0, 1, 2], [3, 4, 5]]), IDENTITY, W, H).reshape(H, W)
+    wa, wb = np.float32(0.5 * za + 0.5), np.float32(0.5 * zb + 0.5)
+    for y in range(H):
+        for x in range(W):
+            if 8 <= x < 40 and 8 <= y < 40:
+                assert d[y, x] == (wa if x >= y else wb), (x, y)
+            else:
+                assert d[y, x] == 1.0, (x, y)
+
+
+def test_polygon_offset_value():
+    W = H = 64
+    # z_w rises by 0.25 over 64 pixels in x, flat in y: m = 2^-8; max z_w = 0.5
+    # (exponent -1) gives r = 2^-24; offset = 4 m + 20 r.
+    win = [(0.0, 0.0, 0.25), (64.0, 0.0, 0.5), (0.0, 64.0, 0.25)]
+    pts = np.array([[*ndc(x, y, W, H), 2 * z - 1] for x, y, z in win], np.float32)
+    d = oracle.shadow_map(pts, np.array([[0, 1, 2]]), IDENTITY, W, H, api.GI_BIAS_POLYGON_OFFSET,
+                          0.0, 4.0, 20.0).reshape(H, W)
+    offset = 4.0 * 2.0 ** -8 + 20.0 * 2.0 ** -24
+    x, y = 10, 20
+    expect = 0.25 + 0.25 * (x + 0.5) / 64.0 + offset
+    assert abs(d[y, x] - expect) < 2e-7
+    dc = oracle.shadow_map(pts, np.array([[0, 1, 2]]), IDENTITY, W, H, api.GI_BIAS_CONSTANT, 1e-3).reshape(H, W)
+    assert abs(dc[y, x] - (0.25 + 0.25 * (x + 0.5) / 64.0 + 1e-3)) < 2e-7
+
+
+def _probe(tech, depth_map, S, s, t, z, **kw):
+    """Visibility of one synthetic G-buffer pixel whose light-space coordinate is (s, t, z)."""
+    p = gi.ShadowParams.defaults(tech)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    p.pretest = api.GI_PRETEST_OFF
+    fr = gi.Frame(IDENTITY, IDENTITY, IDENTITY, IDENTITY, np.eye(3, dtype=np.float32).reshape(-1),
+                  np.zeros(3, np.float32))
+    pos = np.array([s, t, z, 1.0], np.float32)
+    nrm = np.array([0, 0, 1, 1], np.float32)
+    tab = np.concatenate([gi.poisson_table(p.poisson_blocker_taps).reshape(-1),
+                          gi.poisson_table(p.poisson_filter_taps).reshape(-1)])
+    return float(oracle.visibility(p.to_c(fr), depth_map, S, S, pos, nrm, 1, 1, tab)[0])
+
+
+def test_pcf_float_loop_is_asymmetric():
+    # k = 3: offsets w, h in {-1, -1/3, +1/3} texels -> columns {7, 8, 8}
+    S = 16
+    s = t = 8.5 / S
+    left = np.ones(S * S, np.float32)
+    left[8 * S + 7] = 0.1
+    right = np.ones(S * S, np.float32)
+    right[8 * S + 9] = 0.1
+    kw = dict(kernel_order=3, penumbra_size=1)
+    assert _probe(api.GI_TECH_PCF, left, S, s, t, 0.5, **kw) == pytest.approx((7 + 2 * 0.25) / 9, abs=1e-7)
+    assert _probe(api.GI_TECH_PCF, right, S, s, t, 0.5, **kw) == 1.0
+
+
+def test_hard_border_is_shadowed_and_background_is_zero():
+    S = 8
+    m = np.ones(S * S, np.float32)
+    assert _probe(api.GI_TECH_HARD, m, S, 0.5, 0.5, 0.5) == 1.0
+    assert _probe(api.GI_TECH_HARD, m, S, 1.0, 0.5, 0.5) == 0.25  # s = 1 -> texel S -> border 0
+    assert _probe(api.GI_TECH_HARD, m, S, 0.5, -0.01, 0.5) == 0.25
+    assert _probe(api.GI_TECH_HARD, m, S, 0.0, 0.5, 0.5) == 0.0  # vertex.x == 0: background
+
+
+def test_pcss_cutoffs():
+    S = 64
+    m = np.full(S * S, 0.9, np.float32)  # every blocker at window depth 0.9
+    kw = dict(light_radius=2.0, kernel_size=15, blocker_search_size=7)
+    # reference cut-off 0.99: average blocker 0.9 < 0.99 -> penumbra 0 -> lit
+    assert _probe(api.GI_TECH_PCSS_GRID, m, S, 0.5, 0.5, 0.95, **kw) == 1.0
+    assert _probe(api.GI_TECH_PCSS_POISSON, m, S, 0.5, 0.5, 0.95, **kw) == 1.0
+    # without the cut-off the receiver is in umbra: every filter tap shadowed
+    kw["pcss_min_blocker_depth"] = 0.0
+    assert _probe(api.GI_TECH_PCSS_GRID, m, S, 0.5, 0.5, 0.95, **kw) == pytest.approx(0.25)
+    assert _probe(api.GI_TECH_PCSS_POISSON, m, S, 0.5, 0.5, 0.95, **kw) == pytest.approx(0.25)
+    # no blocker at all -> average 1 -> (z - 1) < 0 -> step <= 0 -> lit
+    assert _probe(api.GI_TECH_PCSS_GRID, np.ones(S * S, np.float32), S, 0.5, 0.5, 0.95, **kw) == 1.0
+
+
+def test_pcss_penumbra_is_fractional_at_an_edge():
+    S = 256
+    m = np.ones((S, S), np.float32)
+    m[:, : S // 2] = 0.5  # blockers on the left half
+    kw = dict(light_radius=8.0, kernel_size=15, blocker_search_size=7, pcss_min_blocker_depth=0.0)
+    v = _probe(api.GI_TECH_PCSS_GRID, m.reshape(-1), S, 0.5 + 0.5 / S, 0.5, 0.9, **kw)
+    assert 0.25 < v < 1.0
+
+
+def test_rbsm_variants_on_a_straight_edge():
+    # a vertical shadow edge: texels x < 8 block (depth 0.1), receiver z 0.5
+    S = 16
+    m = np.ones((S, S), np.float32)
+    m[:, :8] = 0.1
+    m = m.reshape(-1)
+    kw = dict(max_search=16, kernel_order=3, penumbra_size=1)
+    for tech in (api.GI_TECH_SMSR_CONSERVATIVE, api.GI_TECH_SMSR_NONCONSERVATIVE, api.GI_TECH_RPCF_CONSERVATIVE,
+                 api.GI_TECH_RPCF_SMSR, api.GI_TECH_RSMSS):
+        lit = _probe(tech, m, S, 12.5 / S, 8.5 / S, 0.5, **kw)
+        dark = _probe(tech, m, S, 3.5 / S, 8.5 / S, 0.5, **kw)
+        assert lit == 1.0, tech
+        assert dark == 0.25, tech
+        edge = _probe(tech, m, S, 8.5 / S, 8.5 / S, 0.5, **kw)
+        assert 0.25 <= edge <= 1.0, tech
+
+
+def test_pretest_reference_mode_shadows_back_facing_normals():
+    S = 8
+    m = np.ones(S * S, np.float32)
+    p = gi.ShadowParams.defaults(api.GI_TECH_HARD)
+    fr = gi.Frame(IDENTITY, IDENTITY, IDENTITY, IDENTITY, np.eye(3, dtype=np.float32).reshape(-1),
+                  np.array([0.0, 0.0, 10.0], np.float32))
+    pos = np.array([0.5, 0.5, 0.5, 1.0, 0.5, 0.5, 0.5, 1.0, 0.5, 0.5, 0.5, 1.0], np.float32)
+    # normal towards the light, away from it, and away but back-facing (flipped)
+    nrm = np.array([0, 0, 1, 1, 0, 0, -1, 1, 0, 0, -1, 0], np.float32)
+    out = oracle.visibility(p.to_c(fr), m, S, S, pos, nrm, 3, 1)
+    assert out.tolist() == [1.0, 0.25, 1.0]
+
+
+def test_shadow_volume_counts_match_a_ray_test():
+    # one occluder triangle above a ground quad; pixels far from the shadow
+    # boundary must count non-zero exactly when the ground point's segment to
+    # the light crosses the triangle (the reference's extrusion (v - L) * 100
+    # bends the volume slightly, hence the margin).
+    W, H = 96, 72
+    s = gi.Scene()
+    s.ground(10.0, 0.0)
+    s.object_from_arrays(np.array([[-1.5, 2.0, -1.0], [1.5, 2.0, -1.0], [0.0, 2.0, 2.0]], np.float32),
+                         [[0, 2, 1]]).commit()
+    L = np.array([0.5, 9.0, 0.5], np.float32)
+    cam = gi.ViewSpec(eye=(0.0, 12.0, -6.0), at=(0.0, 0.0, 0.0), width=W, height=H)
+    fr = gi.frame_setup(gi.ViewSpec(eye=tuple(L), at=(0, 0, 0), width=8, height=8), cam)
+    p, n, i = s.arrays()
+    st, _ = oracle.shadow_volume_counts(p, n, i, L, 100.0, fr.camera_mvp, W, H, api.GI_DEPTH_LEQUAL)
+    pos, _ = oracle.gbuffer(p, n, i, fr.camera_mvp, W, H)
+    pos = pos.reshape(H, W, 4)
+    st = st.reshape(H, W)
+    tri = p[4:7].astype(np.float64)
+    checked = 0
+    for y in range(H):
+        for x in range(W):
+            g = pos[y, x, :3].astype(np.float64)
+            if pos[y, x, 0] == 0.0 or abs(g[1]) > 1e-4:
+                continue  # background or the occluder itself
+            # segment g -> L against the plane y = 2 of the triangle
+            t = (2.0 - g[1]) / (L[1] - g[1])
+            q = g + t * (L - g)
+            a, b, c = tri
+            d = [np.cross(b - a, q - a)[1], np.cross(c - b, q - b)[1], np.cross(a - c, q - c)[1]]
+            margin = 0.15
+            dist = min(abs(v) / np.linalg.norm(e) for v, e in zip(d, (b - a, c - b, a - c)))
+            if dist < margin:
+                continue
+            inside = all(v > 0 for v in d) or all(v < 0 for v in d)
+            assert (st[y, x] != 0) == inside, (x, y, st[y, x])
+            checked += 1
+    assert checked > 2000
+    assert (st != 0).sum() > 100
