@@ -164,6 +164,7 @@ _PROTOS = {
     "gi_frame_setup": (C.c_int, [C.POINTER(View), C.POINTER(View), C.POINTER(FrameMatrices)]),
     "gi_shadow_map": (C.c_int, [_VP, _VP, C.POINTER(MapParams), F16, _VP, _VP]),
     "gi_gbuffer": (C.c_int, [_VP, _VP, F16, C.c_int, C.c_int, _VP, _VP, _VP]),
+    "gi_gbuffer_noalloc": (C.c_int, [_VP, _VP, C.c_int, _VP, C.c_int, F16, C.c_int, C.c_int, _VP, _VP, _VP]),
     "gi_vis_params_default": (C.c_int, [C.c_int, C.POINTER(VisParams)]),
     "gi_visibility": (C.c_int, [_VP, C.POINTER(VisParams), _VP, C.c_int, C.c_int, _VP, _VP, _VP,
                                 C.c_int, C.c_int, _VP]),

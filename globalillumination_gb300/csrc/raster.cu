@@ -40,6 +40,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 #include <string>
 
 #include "internal.h"
@@ -656,4 +657,115 @@ gi_status raster_shadow_volumes(gi_context* ctx, const gi_scene* scene, const fl
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "stencil wrap launch");
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free G-buffer (gi_gbuffer_noalloc)
+//
+// Some callers cannot allocate device memory: a real-time frame loop where
+// cudaMalloc's implicit device synchronisation would stall the frame, or a
+// host application whose device memory is all owned by its own pool.  This
+// variant of the G-buffer pass takes every input and output from the caller
+// and keeps its scratch (the per-pixel visibility keys, the large-triangle
+// records and the pass counters) in the file-scope array below instead of
+// in a gi_context.  The array is reserved on every GPU that loads the
+// library, for the life of the process.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoallocMaxPixels = 1024 * 1024;  // width * height limit
+constexpr unsigned kNoallocRecords = 16384;         // large triangles before spilling
+constexpr size_t kNoallocKeysBytes = kNoallocMaxPixels * sizeof(unsigned long long);
+constexpr size_t kNoallocRecsBytes = (size_t)kNoallocRecords * sizeof(dev::TriRec);
+constexpr size_t kNoallocStatusBytes = 256;
+constexpr size_t kNoallocBytes = kNoallocKeysBytes + kNoallocRecsBytes + kNoallocStatusBytes;
+static_assert(kNoallocKeysBytes % 256 == 0 && kNoallocRecsBytes % 8 == 0, "scratch carving");
+
+// keys | records | status words (counters[2], tile total)
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[kNoallocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device, resolved once
+// per device.  The array's name in host code is only a host-side handle.
+gi_status noalloc_scratch(unsigned char** out) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail_cuda(e, "gi_gbuffer_noalloc: cudaGetDevice");
+    if (dev < 0 || dev >= kNoallocMaxDevices)
+        return fail(GI_ERR_UNSUPPORTED, "gi_gbuffer_noalloc: device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail_cuda(e == cudaSuccess ? cudaErrorInvalidSymbol : e,
+                             "gi_gbuffer_noalloc: cudaGetSymbolAddress");
+        g_noalloc_addr[dev] = p;
+    }
+    *out = static_cast<unsigned char*>(g_noalloc_addr[dev]);
+    return GI_OK;
+}
+
+}  // namespace
 }  // namespace gi
+
+extern "C" gi_status gi_gbuffer_noalloc(const float* d_points, const float* d_normals,
+                                        int num_vertices, const int* d_indices, int num_triangles,
+                                        const float camera_mvp[16], int width, int height,
+                                        float* d_pos, float* d_nrm, void* stream) {
+    using namespace gi;
+    if (num_vertices < 0 || num_triangles < 0 || !camera_mvp || !d_pos || !d_nrm ||
+        (num_vertices > 0 && (!d_points || !d_normals)) || (num_triangles > 0 && !d_indices))
+        return fail(GI_ERR_INVALID_ARG, "gi_gbuffer_noalloc: bad arguments");
+    if (width <= 0 || height <= 0 || width > 16384 || height > 16384)
+        return fail(GI_ERR_INVALID_ARG, "gi_gbuffer_noalloc: image size must be in [1, 16384]");
+    const size_t npx = (size_t)width * height;
+    if (npx > kNoallocMaxPixels)
+        return fail(GI_ERR_CAPACITY,
+                    "gi_gbuffer_noalloc: " + std::to_string(npx) +
+                        " pixels exceed the allocation-free scratch (at most 1048576 = 1024 x 1024)");
+    if ((size_t)num_triangles >= ((size_t)1 << 29))
+        return fail(GI_ERR_CAPACITY, "gi_gbuffer_noalloc: more than 2^29 triangles");
+    unsigned char* base = nullptr;
+    gi_status st = noalloc_scratch(&base);
+    if (st != GI_OK) return st;
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    unsigned long long* keys = reinterpret_cast<unsigned long long*>(base);
+    dev::TriRec* recs = reinterpret_cast<dev::TriRec*>(base + kNoallocKeysBytes);
+    unsigned* status = reinterpret_cast<unsigned*>(base + kNoallocKeysBytes + kNoallocRecsBytes);
+    // The array keeps the previous call's contents: reset the counters and
+    // the keys before use.
+    cudaError_t e = cudaMemsetAsync(status, 0, kNoallocStatusBytes, cs);
+    if (e != cudaSuccess) return fail_cuda(e, "gi_gbuffer_noalloc: cudaMemsetAsync");
+    int device = 0;
+    cudaGetDevice(&device);
+    const unsigned fill_blocks = std::min<unsigned>(grid_for(npx, 256), (unsigned)sm_count(device) * 8);
+    const unsigned long long clear = ((unsigned long long)0x3f800000u << 32) | 0xFFFFFFFFull;
+    dev::k_fill_u64<<<fill_blocks, 256, 0, cs>>>(keys, npx, clear);
+    dev::RasterArgs a = {};
+    a.points = d_points;
+    a.normals = d_normals;
+    a.indices = d_indices;
+    a.num_prims = num_triangles;
+    a.mvp = mat_of(camera_mvp);
+    a.W = width;
+    a.H = height;
+    a.keys = keys;
+    a.recs = recs;
+    a.rec_cap = kNoallocRecords;
+    a.counters = status;
+    a.tile_total = reinterpret_cast<unsigned long long*>(status + 4);
+    a.small_px = 128;
+    if (num_triangles > 0) {
+        dev::k_setup<dev::MODE_VKEY><<<grid_for((size_t)num_triangles, 128), 128, 0, cs>>>(a);
+        dev::k_scan<<<1, 1024, 0, cs>>>(a.recs, a.counters, a.rec_cap, a.tile_total);
+        dev::k_tiles<dev::MODE_VKEY><<<sm_count(device) * 8, 256, 0, cs>>>(a);
+    }
+    dim3 grid((width + 31) / 32, (height + 3) / 4);
+    dev::k_gbuffer_resolve<<<grid, 128, 0, cs>>>(keys, d_points, d_normals, d_indices, a.mvp, width,
+                                                 height, reinterpret_cast<float4*>(d_pos),
+                                                 reinterpret_cast<float4*>(d_nrm));
+    e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_gbuffer_noalloc: kernel launch");
+}

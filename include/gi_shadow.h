@@ -238,6 +238,27 @@ gi_status gi_gbuffer(gi_context* ctx, const gi_scene* scene,
                      const float camera_mvp[16], int width, int height,
                      float* d_pos, float* d_nrm, void* stream);
 
+/* Allocation-free G-buffer.  No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory (a real-time frame loop where
+ * cudaMalloc's implicit device synchronisation would stall the frame, or an
+ * application whose device memory is all owned by its own pool).  Same
+ * result as gi_gbuffer, with the geometry passed as caller-owned device
+ * arrays and no gi_context: the pass's scratch (per-pixel keys, large-
+ * triangle records, counters) lives in one static device array of
+ * 9,568,512 bytes that every GPU loading the library reserves until the
+ * process exits.  Limit: width * height <= 1,048,576 (1024 x 1024); larger
+ * images return GI_ERR_CAPACITY.  Runs on the calling thread's current
+ * device; the first call on each device looks up the array's device
+ * address, so make that first call before any stream capture.  Every call
+ * reuses the same array: calls that overlap on the GPU (other streams,
+ * other threads) race and must be serialised by the caller.  Allocates
+ * nothing (no cudaMalloc / cudaFree). */
+gi_status gi_gbuffer_noalloc(const float* d_points, const float* d_normals,
+                             int num_vertices, const int* d_indices,
+                             int num_triangles, const float camera_mvp[16],
+                             int width, int height, float* d_pos, float* d_nrm,
+                             void* stream);
+
 /* ------------------------------------------------------------------ */
 /* A6-A12, A15: per-pixel visibility                                   */
 /* ------------------------------------------------------------------ */
