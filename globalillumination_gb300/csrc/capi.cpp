@@ -79,14 +79,14 @@ extern "C" gi_status gi_context_create(int device, gi_context** out) {
     if (e != cudaSuccess) return gi::fail_cuda(e, "cudaSetDevice");
     gi_context* c = new gi_context();
     c->device = device;
-    e = cudaMalloc(&c->d_status, 16 * sizeof(unsigned));
-    if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, 16 * sizeof(unsigned));
-    if (e == cudaSuccess) e = cudaMallocHost(&c->h_status, 16 * sizeof(unsigned));
+    e = cudaMalloc(&c->d_status, 64 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, 64 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_status, 64 * sizeof(unsigned));
     if (e != cudaSuccess) {
         gi_context_destroy(c);
         return gi::fail_cuda(e, "gi_context_create allocation");
     }
-    std::memset(c->h_status, 0, 16 * sizeof(unsigned));
+    std::memset(c->h_status, 0, 64 * sizeof(unsigned));
     *out = c;
     return GI_OK;
 }
@@ -100,6 +100,8 @@ extern "C" void gi_context_destroy(gi_context* c) {
     cudaFree(c->d_vkeys);
     cudaFree(c->d_depth_tmp);
     cudaFree(c->d_counts);
+    for (int i = 0; i < 8; ++i) cudaFree(c->bin_buf[i]);
+    for (int i = 0; i < 6; ++i) cudaFree(c->tier_buf[i]);
     cudaFree(c->d_status);
     if (c->h_status) cudaFreeHost(c->h_status);
     delete c;

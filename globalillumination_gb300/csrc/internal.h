@@ -75,8 +75,17 @@ struct gi_context {
     size_t cap_depth_tmp = 0;
     int* d_counts = nullptr;
     size_t cap_counts = 0;
-    // status words: [0] error flags, [1] tile-item count, [2] record count,
-    // [3] requested tile items (for diagnostics)
+    // binned rasteriser: records, big-record list, big-record bases, spill
+    // list, bin counters (small | big | offset | cursor), bin lists, ranks,
+    // bin work items
+    void* bin_buf[8] = {};
+    size_t bin_cap[8] = {};
+    // tiered rasteriser: records, tiny / warp / large lists, large bases, spill
+    void* tier_buf[6] = {};
+    size_t tier_cap[6] = {};
+    // status words (64): [4..11] counters of the binned raster (records, big
+    // records, spills, error bits, admitted big pairs as u64, work items),
+    // [32..55] counters of the tiered raster
     unsigned int* d_status = nullptr;
     unsigned int* h_status = nullptr;  // pinned mirror
 };

@@ -462,6 +462,1017 @@ __global__ void k_wrap_stencil(const int* counts, unsigned char* out, size_t n) 
     if (i < n) out[i] = (unsigned char)((unsigned)counts[i] & 0xFFu);
 }
 
+
+// ===========================================================================
+// Binned (sort-middle) rasteriser
+//
+// The image is cut into 32 x 32-pixel bins.  k_bin_setup turns every
+// primitive into sub-triangle records (transform, clip, set up) and counts
+// them into the bins their bounding box touches; records spanning more than
+// four bins go through a second, exact bin-overlap expansion (k_big_scan /
+// k_big_pairs).  After an exclusive scan of the bin counts, the record ids
+// are scattered into per-bin lists, and k_bin_raster runs one CTA per bin:
+// warp w owns rows 4w..4w+3 of the bin, lane l owns column l, so every
+// pixel has a single owner thread that keeps its depth (or key, or stencil
+// count) in registers while it walks the bin's list, and writes it once at
+// the end: no global atomics, no clear pass.  Records that do not fit the
+// scratch capacities are "spilled" and rasterised afterwards with the
+// global-atomic path (k_spill), so every capacity overflow stays exact.
+// ===========================================================================
+constexpr int kBin = 32;
+constexpr int kBinShift = 5;
+constexpr int kDirectBins = 4;
+constexpr unsigned kSeg = 256;        // records per bin work item
+constexpr unsigned kItemBinBits = 18; // work item = bin | segment << 18
+constexpr unsigned kFlagFront = 1u, kFlagBig = 2u;
+
+struct __align__(16) BRec {
+    int X[3];
+    int Y[3];
+    float z0, dz1, dz2, inv_area;
+    float zoff;
+    unsigned prim;     // key / stencil primitive id
+    unsigned short x0, x1, y0, y1;
+    unsigned flags;
+    unsigned spill_id; // (primitive << 3) | sub-triangle
+};
+static_assert(sizeof(BRec) == 64, "BRec is four 16-byte words");
+
+struct BinArgs {
+    RasterArgs r;
+    BRec* recs;
+    unsigned rec_cap;
+    unsigned* big_list;
+    unsigned long long* big_base;
+    unsigned big_cap;
+    unsigned* spill;
+    unsigned spill_cap;
+    unsigned* bin_count;   // small-record entries per bin (setup)
+    unsigned* big_count;   // big-record entries per bin (expansion)
+    unsigned* bin_offset;  // nbins + 1
+    unsigned* bin_cursor;  // big-record scatter cursors
+    unsigned* ranks;       // per small record: its slot within each of its <= 4 bins
+    unsigned* items;       // bin work items (bin | segment << 18)
+    unsigned item_cap;
+    unsigned* bin_list;
+    unsigned long long list_cap;
+    unsigned long long big_pair_cap;
+    unsigned* ctr;  // [0] records [1] big records [2] spills [3] error bits [4,5] admitted big pairs
+                    // [6] work items
+    int nbx, nby;
+};
+
+__device__ __forceinline__ void spill_push(const BinArgs& a, unsigned id) {
+    unsigned s = atomicAdd(a.ctr + 2, 1u);
+    if (s < a.spill_cap) a.spill[s] = id;
+    else atomicOr(a.ctr + 3, 1u);  // spill list full: results incomplete
+}
+
+template <int MODE>
+__device__ void bin_sub(const BinArgs& a, const float* c0, const float* c1, const float* c2,
+                        const float* b0, const float* b1, const float* b2, unsigned prim,
+                        unsigned sub) {
+    Setup s;
+    if (!setup_triangle(c0, c1, c2, b0, b1, b2, a.r.W, a.r.H, s)) return;
+    int64_t minX = min(s.X[0], min(s.X[1], s.X[2])), maxX = max(s.X[0], max(s.X[1], s.X[2]));
+    int64_t minY = min(s.Y[0], min(s.Y[1], s.Y[2])), maxY = max(s.Y[0], max(s.Y[1], s.Y[2]));
+    int64_t bx0 = -((-(minX - kSub / 2)) >> kSubBits);
+    int64_t bx1 = (maxX - kSub / 2) >> kSubBits;
+    int64_t by0 = -((-(minY - kSub / 2)) >> kSubBits);
+    int64_t by1 = (maxY - kSub / 2) >> kSubBits;
+    int x0 = (int)max((int64_t)0, bx0), x1 = (int)min((int64_t)a.r.W - 1, bx1);
+    int y0 = (int)max((int64_t)0, by0), y1 = (int)min((int64_t)a.r.H - 1, by1);
+    if (x0 > x1 || y0 > y1) return;
+    const unsigned spill_id = (prim << 3) | sub;
+    unsigned slot = atomicAdd(a.ctr + 0, 1u);
+    if (slot >= a.rec_cap) {
+        spill_push(a, spill_id);
+        return;
+    }
+    float zoff = 0.0f;
+    if (MODE == MODE_DEPTH) {
+        if (a.r.bias_mode == GI_BIAS_POLYGON_OFFSET) zoff = polygon_offset(s, a.r.factor, a.r.units);
+        else if (a.r.bias_mode == GI_BIAS_CONSTANT) zoff = a.r.cbias;
+    }
+    const int cx0 = x0 >> kBinShift, cx1 = x1 >> kBinShift, cy0 = y0 >> kBinShift, cy1 = y1 >> kBinShift;
+    const int nb = (cx1 - cx0 + 1) * (cy1 - cy0 + 1);
+    BRec r;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        r.X[i] = (int)s.X[i];
+        r.Y[i] = (int)s.Y[i];
+    }
+    r.z0 = s.z[0];
+    r.dz1 = s.z[1] - s.z[0];
+    r.dz2 = s.z[2] - s.z[0];
+    r.inv_area = s.inv_area;
+    r.zoff = zoff;
+    r.prim = MODE == MODE_VKEY ? spill_id : prim;
+    r.x0 = (unsigned short)x0;
+    r.x1 = (unsigned short)x1;
+    r.y0 = (unsigned short)y0;
+    r.y1 = (unsigned short)y1;
+    r.flags = (s.front ? kFlagFront : 0u) | (nb > kDirectBins ? kFlagBig : 0u);
+    r.spill_id = spill_id;
+    a.recs[slot] = r;
+    if (nb <= kDirectBins) {
+        int k = 0;
+        for (int by = cy0; by <= cy1; ++by)
+            for (int bx = cx0; bx <= cx1; ++bx, ++k)
+                a.ranks[4 * (size_t)slot + k] = atomicAdd(a.bin_count + by * a.nbx + bx, 1u);
+    } else {
+        unsigned bi = atomicAdd(a.ctr + 1, 1u);
+        if (bi < a.big_cap) a.big_list[bi] = slot;
+        else spill_push(a, spill_id);  // the record stays unreferenced
+    }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(128) k_bin_setup(BinArgs a) {
+    int prim = blockIdx.x * blockDim.x + threadIdx.x;
+    if (prim >= a.r.num_prims) return;
+    float v[3][3];
+    prim_vertices<MODE>(a.r, prim, v);
+    float c[3][4];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) transform(a.r.mvp, v[j][0], v[j][1], v[j][2], c[j]);
+    const float id[3][3] = {{1.0f, 0.0f, 0.0f}, {0.0f, 1.0f, 0.0f}, {0.0f, 0.0f, 1.0f}};
+    if (all_inside(c[0], c[1], c[2])) {
+        bin_sub<MODE>(a, c[0], c[1], c[2], id[0], id[1], id[2], (unsigned)prim, 0u);
+        return;
+    }
+    CV poly[9];
+    int n = clip_polygon(c[0], c[1], c[2], poly);
+    for (int i = 1; i + 1 < n; ++i)
+        bin_sub<MODE>(a, poly[0].c, poly[i].c, poly[i + 1].c, poly[0].b, poly[i].b, poly[i + 1].b,
+                      (unsigned)prim, (unsigned)(i - 1));
+}
+
+__device__ __forceinline__ int rec_bins(const BRec& r) {
+    return ((r.x1 >> kBinShift) - (r.x0 >> kBinShift) + 1) * ((r.y1 >> kBinShift) - (r.y0 >> kBinShift) + 1);
+}
+
+// Block-wide exclusive scan helper (1024 threads); returns the exclusive
+// prefix of v and writes the block total to *total.
+__device__ __forceinline__ unsigned long long block_scan_1024(unsigned long long v,
+                                                             unsigned long long* warp_sums,
+                                                             unsigned long long* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long x = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        unsigned long long y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long w = warp_sums[lane];
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            unsigned long long y = __shfl_up_sync(0xffffffffu, w, off);
+            if (lane >= off) w += y;
+        }
+        warp_sums[lane] = w;
+    }
+    __syncthreads();
+    unsigned long long r = (warp == 0 ? 0ull : warp_sums[warp - 1]) + x - v;
+    *total = warp_sums[31];
+    __syncthreads();
+    return r;
+}
+
+// Offsets of the big records' bin ranges.  Admission is a prefix (bases
+// grow): records whose range ends past the pair capacity are spilled.
+__global__ void __launch_bounds__(1024) k_big_scan(BinArgs a) {
+    __shared__ unsigned long long warp_sums[32];
+    __shared__ unsigned long long admitted;
+    const unsigned n = min(a.ctr[1], a.big_cap);
+    if (threadIdx.x == 0) admitted = 0;
+    unsigned long long carry = 0;
+    for (unsigned start = 0; start < n; start += 1024) {
+        unsigned i = start + threadIdx.x;
+        unsigned long long v = 0;
+        if (i < n) v = (unsigned long long)rec_bins(a.recs[a.big_list[i]]);
+        unsigned long long tot;
+        unsigned long long ex = block_scan_1024(v, warp_sums, &tot);
+        if (i < n) {
+            unsigned long long base = carry + ex;
+            if (base + v <= a.big_pair_cap) {
+                a.big_base[i] = base;
+                atomicMax(&admitted, base + v);
+            } else {
+                a.big_base[i] = ~0ull;
+                spill_push(a, a.recs[a.big_list[i]].spill_id);
+            }
+        }
+        carry += tot;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *reinterpret_cast<unsigned long long*>(a.ctr + 4) = admitted;
+}
+
+// Smallest edge-function upper bound test: true if the record may cover a
+// pixel centre of the rectangle [px0, px1] x [py0, py1].
+__device__ __forceinline__ bool rect_may_cover(const BRec& r, int px0, int px1, int py0, int py1) {
+    int64_t cx0 = (int64_t)px0 * kSub + kSub / 2, cx1 = (int64_t)px1 * kSub + kSub / 2;
+    int64_t cy0 = (int64_t)py0 * kSub + kSub / 2, cy1 = (int64_t)py1 * kSub + kSub / 2;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        int a = (i + 1) % 3, b = (i + 2) % 3;
+        int64_t A = (int64_t)r.X[b] - r.X[a], B = (int64_t)r.Y[b] - r.Y[a];
+        int64_t ymax = A > 0 ? cy1 : cy0;
+        int64_t xmin = B > 0 ? cx0 : cx1;
+        if (A * (ymax - r.Y[a]) - B * (xmin - r.X[a]) < 0) return false;
+    }
+    return true;
+}
+
+// Expansion of the admitted big records into (bin, record) pairs: counts
+// (FILL = false) or list entries (FILL = true).  Warps take contiguous pair
+// ranges and walk the record list.
+template <bool FILL>
+__global__ void __launch_bounds__(256) k_big_pairs(BinArgs a) {
+    const unsigned n = min(a.ctr[1], a.big_cap);
+    const unsigned long long total = *reinterpret_cast<const unsigned long long*>(a.ctr + 4);
+    if (n == 0 || total == 0) return;
+    const unsigned long long nthreads = (unsigned long long)gridDim.x * blockDim.x;
+    const unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long begin = total * t / nthreads, end = total * (t + 1) / nthreads;
+    if (begin >= end) return;
+    unsigned lo = 0, hi = n - 1;
+    while (lo < hi) {
+        unsigned mid = (lo + hi + 1) >> 1;
+        unsigned long long b = a.big_base[mid];
+        if (b != ~0ull && b <= begin) lo = mid;
+        else hi = mid - 1;
+    }
+    unsigned ri = lo;
+    unsigned rec_id = a.big_list[ri];
+    BRec r = a.recs[rec_id];
+    unsigned long long base = a.big_base[ri];
+    int cx0 = r.x0 >> kBinShift, cy0 = r.y0 >> kBinShift;
+    int ncx = (r.x1 >> kBinShift) - cx0 + 1;
+    unsigned long long nb = (unsigned long long)rec_bins(r);
+    for (unsigned long long p = begin; p < end; ++p) {
+        while (p >= base + nb) {
+            ++ri;
+            rec_id = a.big_list[ri];
+            r = a.recs[rec_id];
+            base = a.big_base[ri];
+            cx0 = r.x0 >> kBinShift;
+            cy0 = r.y0 >> kBinShift;
+            ncx = (r.x1 >> kBinShift) - cx0 + 1;
+            nb = (unsigned long long)rec_bins(r);
+        }
+        unsigned local = (unsigned)(p - base);
+        int bx = cx0 + (int)(local % (unsigned)ncx), by = cy0 + (int)(local / (unsigned)ncx);
+        int px0 = max(bx * kBin, (int)r.x0), px1 = min(bx * kBin + kBin - 1, (int)r.x1);
+        int py0 = max(by * kBin, (int)r.y0), py1 = min(by * kBin + kBin - 1, (int)r.y1);
+        if (!rect_may_cover(r, px0, px1, py0, py1)) continue;
+        unsigned bin = (unsigned)(by * a.nbx + bx);
+        if (!FILL) {
+            atomicAdd(a.big_count + bin, 1u);
+        } else {
+            unsigned slot = atomicAdd(a.bin_cursor + bin, 1u);
+            a.bin_list[slot] = rec_id;
+        }
+    }
+}
+
+// Exclusive scan of the bin counts into offsets and cursors, and of the
+// bins' segment counts into the work-item list (one block).  Empty bins get
+// no work item: the target was cleared before the raster.
+__global__ void __launch_bounds__(1024) k_bin_scan(BinArgs a) {
+    __shared__ unsigned long long warp_sums[32];
+    const unsigned nbins = (unsigned)(a.nbx * a.nby);
+    unsigned long long carry = 0, icarry = 0;
+    for (unsigned start = 0; start < nbins; start += 1024) {
+        unsigned i = start + threadIdx.x;
+        unsigned small = i < nbins ? a.bin_count[i] : 0u;
+        unsigned long long v = i < nbins ? (unsigned long long)small + a.big_count[i] : 0u;
+        unsigned long long tot;
+        unsigned long long ex = block_scan_1024(v, warp_sums, &tot);
+        if (i < nbins) {
+            a.bin_offset[i] = (unsigned)(carry + ex);
+            a.bin_cursor[i] = (unsigned)(carry + ex) + small;
+        }
+        carry += tot;
+        const unsigned long long nseg = (v + kSeg - 1) / kSeg;
+        unsigned long long itot;
+        unsigned long long iex = block_scan_1024(nseg, warp_sums, &itot);
+        for (unsigned long long k = 0; k < nseg; ++k) {
+            unsigned long long slot = icarry + iex + k;
+            if (slot < a.item_cap) a.items[slot] = i | ((unsigned)k << kItemBinBits);
+        }
+        icarry += itot;
+    }
+    if (threadIdx.x == 0) {
+        a.bin_offset[nbins] = (unsigned)carry;
+        a.ctr[6] = (unsigned)min(icarry, (unsigned long long)a.item_cap);
+        if (icarry > a.item_cap) atomicOr(a.ctr + 3, 2u);
+    }
+}
+
+// Scatter of the small records into their (at most four) bins, at the
+// ranks the setup kernel drew from the bin counters (no atomics here).
+__global__ void __launch_bounds__(256) k_bin_fill_small(BinArgs a) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned n = min(a.ctr[0], a.rec_cap);
+    if (i >= n) return;
+    // the last 16 bytes of the record hold the bounding box and the flags
+    const uint4 tail = __ldg(reinterpret_cast<const uint4*>(a.recs + i) + 3);
+    const unsigned flags = tail.z;
+    if (flags & kFlagBig) return;
+    const int x0 = (int)(tail.x & 0xFFFFu), x1 = (int)(tail.x >> 16);
+    const int y0 = (int)(tail.y & 0xFFFFu), y1 = (int)(tail.y >> 16);
+    const int cx0 = x0 >> kBinShift, cx1 = x1 >> kBinShift;
+    const int cy0 = y0 >> kBinShift, cy1 = y1 >> kBinShift;
+    int k = 0;
+    for (int by = cy0; by <= cy1; ++by)
+        for (int bx = cx0; bx <= cx1; ++bx, ++k) {
+            const unsigned bin = (unsigned)(by * a.nbx + bx);
+            a.bin_list[a.bin_offset[bin] + a.ranks[4 * (size_t)i + k]] = i;
+        }
+}
+
+template <int MODE>
+struct BinVal;
+template <>
+struct BinVal<MODE_DEPTH> {
+    typedef unsigned T;
+};
+template <>
+struct BinVal<MODE_VKEY> {
+    typedef unsigned long long T;
+};
+template <>
+struct BinVal<MODE_STENCIL> {
+    typedef int T;
+};
+
+// Fragment update of one bin pixel (index t in the 32 x 32 tile).
+template <int MODE, typename V>
+__device__ __forceinline__ void bin_frag(const BinArgs& a, V* tile, const float* dtile, int t,
+                                         const BRec& r, float fe1, float fe2) {
+    const float l1 = fe1 * r.inv_area;
+    const float l2 = fe2 * r.inv_area;
+    float z = r.z0 + (l1 * r.dz1 + l2 * r.dz2);
+    if (MODE == MODE_DEPTH) {
+        z = clamp01(z + r.zoff);
+        if (z < 1.0f) atomicMin(reinterpret_cast<unsigned*>(&tile[t]), __float_as_uint(z));
+    } else if (MODE == MODE_VKEY) {
+        z = clamp01(z);
+        if (z < 1.0f)
+            atomicMin(reinterpret_cast<unsigned long long*>(&tile[t]),
+                      ((unsigned long long)__float_as_uint(z) << 32) | r.prim);
+    } else {
+        z = clamp01(z);
+        const float d = dtile[t];
+        const bool pass = a.r.depth_func == GI_DEPTH_LEQUAL ? (z <= d) : (z < d);
+        if (pass) atomicAdd(reinterpret_cast<int*>(&tile[t]), (r.flags & kFlagFront) ? 1 : -1);
+    }
+}
+
+// One CTA per work item (a bin, or a 256-record segment of a heavy bin).
+// The bin's 32 x 32 values live in shared memory.  Records are staged and
+// sorted by their coverage of the bin: those covering more than 256 pixels
+// are swept by the whole CTA (thread = column, 4 rows apart by 8,
+// incremental edge values), the others one record per warp with the lanes
+// over the record's bounding box clipped to the bin.  Shared-memory
+// atomicMin / atomicAdd merge overlaps, so the order does not matter.  A
+// single-segment bin stores its tile; the segments of a heavy bin merge
+// theirs into the cleared target with global atomics.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_bin_raster(BinArgs a) {
+    typedef typename BinVal<MODE>::T V;
+    __shared__ BRec srec[kSeg];
+    __shared__ V tile[kBin * kBin];
+    __shared__ float dtile[MODE == MODE_STENCIL ? kBin * kBin : 1];
+    __shared__ float recip[kBin + 1];
+    __shared__ unsigned short s_small[kSeg], s_big[kSeg];
+    __shared__ int n_small, n_big;
+    if (blockIdx.x >= a.ctr[6]) return;
+    const unsigned item = a.items[blockIdx.x];
+    const int bin = (int)(item & ((1u << kItemBinBits) - 1));
+    const unsigned seg = item >> kItemBinBits;
+    const int bx = bin % a.nbx, by = bin / a.nbx;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ox = bx * kBin, oy = by * kBin;
+    const unsigned bbegin = a.bin_offset[bin], bend = a.bin_offset[bin + 1];
+    const bool multi = bend - bbegin > kSeg;
+    const unsigned begin = bbegin + seg * kSeg, end = min(bend, begin + kSeg);
+    if (threadIdx.x <= kBin) recip[threadIdx.x] = threadIdx.x ? 1.0f / (float)threadIdx.x : 0.0f;
+    if (threadIdx.x == 0) {
+        n_small = 0;
+        n_big = 0;
+    }
+    const V clearv = MODE == MODE_DEPTH ? (V)0x3f800000u
+                     : MODE == MODE_VKEY ? (V)(((unsigned long long)0x3f800000u << 32) | 0xFFFFFFFFull)
+                                         : (V)0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int i = threadIdx.x + 256 * k;
+        tile[i] = clearv;
+        if (MODE == MODE_STENCIL) {
+            const int x = ox + (i & (kBin - 1)), y = oy + (i >> kBinShift);
+            dtile[i] = (x < a.r.W && y < a.r.H) ? __uint_as_float(__ldg(a.r.depth + (size_t)y * a.r.W + x))
+                                                 : 1.0f;
+        }
+    }
+    __syncthreads();
+    const unsigned cnt = end - begin;
+    if (threadIdx.x < cnt) {
+        const uint4* src = reinterpret_cast<const uint4*>(a.recs + a.bin_list[begin + threadIdx.x]);
+        uint4* dst = reinterpret_cast<uint4*>(srec + threadIdx.x);
+        uint4 q3 = __ldg(src + 3);
+        dst[0] = __ldg(src + 0);
+        dst[1] = __ldg(src + 1);
+        dst[2] = __ldg(src + 2);
+        dst[3] = q3;
+        const int x0 = max((int)(q3.x & 0xFFFFu), ox), x1 = min((int)(q3.x >> 16), ox + kBin - 1);
+        const int y0 = max((int)(q3.y & 0xFFFFu), oy), y1 = min((int)(q3.y >> 16), oy + kBin - 1);
+        if (x0 <= x1 && y0 <= y1) {
+            const int n = (x1 - x0 + 1) * (y1 - y0 + 1);
+            if (n > 256) s_big[atomicAdd(&n_big, 1)] = (unsigned short)threadIdx.x;
+            else s_small[atomicAdd(&n_small, 1)] = (unsigned short)threadIdx.x;
+        }
+    }
+    __syncthreads();
+    // -- records covering most of the bin: the whole CTA, one column each
+    const int col = threadIdx.x & (kBin - 1), row0 = threadIdx.x >> kBinShift;  // rows row0 + 8k
+    const int x = ox + col;
+    const int64_t px = (int64_t)x * kSub + kSub / 2;
+    for (int b = 0; b < n_big; ++b) {
+        const BRec& r = srec[s_big[b]];
+        int64_t A[3], E[3];
+        bool tl[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const int ia = (i + 1) % 3, ib = (i + 2) % 3;
+            A[i] = (int64_t)r.X[ib] - r.X[ia];
+            const int64_t B = (int64_t)r.Y[ib] - r.Y[ia];
+            tl[i] = (B < 0) || (B == 0 && A[i] < 0);
+            const int64_t py = (int64_t)(oy + row0) * kSub + kSub / 2;
+            E[i] = A[i] * (py - r.Y[ia]) - B * (px - r.X[ia]);
+        }
+        const bool colin = x >= (int)r.x0 && x <= (int)r.x1;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int y = oy + row0 + 8 * k;
+            const bool in = colin && y >= (int)r.y0 && y <= (int)r.y1 &&
+                            (E[0] > 0 || (E[0] == 0 && tl[0])) && (E[1] > 0 || (E[1] == 0 && tl[1])) &&
+                            (E[2] > 0 || (E[2] == 0 && tl[2]));
+            if (in) bin_frag<MODE>(a, tile, dtile, (row0 + 8 * k) * kBin + col, r, (float)E[1], (float)E[2]);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) E[i] += A[i] * (8 * kSub);
+        }
+    }
+    // -- the other records: one per warp
+    for (int j = warp; j < n_small; j += 8) {
+        const BRec& r = srec[s_small[j]];
+        const int x0 = max((int)r.x0, ox), x1 = min((int)r.x1, ox + kBin - 1);
+        const int y0 = max((int)r.y0, oy), y1 = min((int)r.y1, oy + kBin - 1);
+        const int w = x1 - x0 + 1, n = w * (y1 - y0 + 1);
+        const float inv_w = recip[w];
+        const int64_t cx = (int64_t)x0 * kSub + kSub / 2, cy = (int64_t)y0 * kSub + kSub / 2;
+        int64_t A[3], B[3], E0[3];
+        bool tl[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const int ia = (i + 1) % 3, ib = (i + 2) % 3;
+            A[i] = (int64_t)r.X[ib] - r.X[ia];
+            B[i] = (int64_t)r.Y[ib] - r.Y[ia];
+            tl[i] = (B[i] < 0) || (B[i] == 0 && A[i] < 0);
+            E0[i] = A[i] * (cy - r.Y[ia]) - B[i] * (cx - r.X[ia]);
+        }
+        // Small triangles: every edge value over the bin fits in 32 bits
+        // (|A|, |B| <= 2^13 and the bin spans 2^13 sub-pixels), so the same
+        // integers are formed with 32-bit arithmetic.
+        const bool small = max(max(abs(A[0]), abs(A[1])), abs(A[2])) <= 8192 &&
+                           max(max(abs(B[0]), abs(B[1])), abs(B[2])) <= 8192 &&
+                           abs(E0[0]) < (1LL << 28) && abs(E0[1]) < (1LL << 28) && abs(E0[2]) < (1LL << 28);
+        for (int p = lane; p < n; p += 32) {
+            // p / w by a reciprocal: exact because (p + 1/2) / w is never
+            // within 2^-11 of an integer for p < 1024, w <= 32.
+            const int dy = (int)(((float)p + 0.5f) * inv_w);
+            const int dx = p - dy * w;
+            bool in;
+            float fe1, fe2;
+            if (small) {
+                int e[3];
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+                    e[i] = (int)E0[i] + (int)A[i] * (dy << kSubBits) - (int)B[i] * (dx << kSubBits);
+                in = (e[0] > 0 || (e[0] == 0 && tl[0])) && (e[1] > 0 || (e[1] == 0 && tl[1])) &&
+                     (e[2] > 0 || (e[2] == 0 && tl[2]));
+                fe1 = (float)e[1];
+                fe2 = (float)e[2];
+            } else {
+                int64_t E[3];
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+                    E[i] = E0[i] + A[i] * (int64_t)(dy << kSubBits) - B[i] * (int64_t)(dx << kSubBits);
+                in = (E[0] > 0 || (E[0] == 0 && tl[0])) && (E[1] > 0 || (E[1] == 0 && tl[1])) &&
+                     (E[2] > 0 || (E[2] == 0 && tl[2]));
+                fe1 = (float)E[1];
+                fe2 = (float)E[2];
+            }
+            if (in) bin_frag<MODE>(a, tile, dtile, (y0 + dy - oy) * kBin + (x0 + dx - ox), r, fe1, fe2);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int i = threadIdx.x + 256 * k;
+        const int xx = ox + (i & (kBin - 1)), y = oy + (i >> kBinShift);
+        if (xx >= a.r.W || y >= a.r.H) continue;
+        const size_t idx = (size_t)y * a.r.W + xx;
+        const V v = tile[i];
+        if (!multi) {
+            if (MODE == MODE_DEPTH) a.r.depth[idx] = (unsigned)v;
+            else if (MODE == MODE_VKEY) a.r.keys[idx] = (unsigned long long)v;
+            else a.r.counts[idx] = (int)v;
+        } else if (v != clearv) {
+            if (MODE == MODE_DEPTH) atomicMin(a.r.depth + idx, (unsigned)v);
+            else if (MODE == MODE_VKEY) atomicMin(a.r.keys + idx, (unsigned long long)v);
+            else atomicAdd(a.r.counts + idx, (int)v);
+        }
+    }
+}
+
+// Spilled sub-triangles: re-derived from (primitive, sub) and rasterised by
+// one thread each with global atomics after k_bin_raster.
+template <int MODE>
+__global__ void __launch_bounds__(128) k_spill(BinArgs a) {
+    const unsigned n = min(a.ctr[2], a.spill_cap);
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned id = a.spill[i];
+        const int prim = (int)(id >> 3), sub = (int)(id & 7);
+        float v[3][3];
+        prim_vertices<MODE>(a.r, prim, v);
+        float c[3][4];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) transform(a.r.mvp, v[j][0], v[j][1], v[j][2], c[j]);
+        const float idm[3][3] = {{1.0f, 0.0f, 0.0f}, {0.0f, 1.0f, 0.0f}, {0.0f, 0.0f, 1.0f}};
+        Setup s;
+        bool ok;
+        if (all_inside(c[0], c[1], c[2])) {
+            ok = sub == 0 && setup_triangle(c[0], c[1], c[2], idm[0], idm[1], idm[2], a.r.W, a.r.H, s);
+        } else {
+            CV poly[9];
+            int np = clip_polygon(c[0], c[1], c[2], poly);
+            ok = (sub + 2 < np) && setup_triangle(poly[0].c, poly[sub + 1].c, poly[sub + 2].c, poly[0].b,
+                                                  poly[sub + 1].b, poly[sub + 2].b, a.r.W, a.r.H, s);
+        }
+        if (!ok) continue;
+        int64_t minX = min(s.X[0], min(s.X[1], s.X[2])), maxX = max(s.X[0], max(s.X[1], s.X[2]));
+        int64_t minY = min(s.Y[0], min(s.Y[1], s.Y[2])), maxY = max(s.Y[0], max(s.Y[1], s.Y[2]));
+        int x0 = (int)max((int64_t)0, -((-(minX - kSub / 2)) >> kSubBits));
+        int x1 = (int)min((int64_t)a.r.W - 1, (maxX - kSub / 2) >> kSubBits);
+        int y0 = (int)max((int64_t)0, -((-(minY - kSub / 2)) >> kSubBits));
+        int y1 = (int)min((int64_t)a.r.H - 1, (maxY - kSub / 2) >> kSubBits);
+        if (x0 > x1 || y0 > y1) continue;
+        float zoff = 0.0f;
+        if (MODE == MODE_DEPTH) {
+            if (a.r.bias_mode == GI_BIAS_POLYGON_OFFSET) zoff = polygon_offset(s, a.r.factor, a.r.units);
+            else if (a.r.bias_mode == GI_BIAS_CONSTANT) zoff = a.r.cbias;
+        }
+        Edges e;
+        make_edges(s, e);
+        raster_small<MODE>(a.r, s, e, x0, x1, y0, y1, zoff, MODE == MODE_VKEY ? id : (unsigned)prim);
+    }
+}
+
+
+// ===========================================================================
+// Tiered rasteriser (light map and G-buffer)
+//
+// k_tier_setup turns every primitive into sub-triangle records and sorts
+// them by pixel bounding box: tiny (<= 16 pixels), warp-sized (<= 1024) and
+// large.  k_large_scan picks up to eight "huge" records (bounding box of at
+// least an eighth of the image, e.g. a ground plane) and scans the 16 x 16
+// tile counts of the other large ones.  k_base then evaluates the huge
+// records at every pixel and writes the target with plain stores (this is
+// also the clear).  Last, tiny records (one thread each), warp-sized records
+// (one warp each, lanes over the bounding box) and large records (one warp
+// per 16 x 16 tile) merge into the target with global atomicMin; the result
+// is the same in any order.
+// ===========================================================================
+constexpr int kTinyPx = 16;
+constexpr int kCoopPx = 1024;
+constexpr int kHugeMax = 8;
+
+struct TierArgs {
+    RasterArgs r;
+    BRec* recs;
+    unsigned rec_cap;
+    unsigned* tiny;
+    unsigned* coop;
+    unsigned* large;
+    unsigned long long* large_base;
+    unsigned* spill;
+    unsigned spill_cap;
+    unsigned long long huge_px;  // bounding-box pixels that make a record huge
+    unsigned* ctr;  // [0] records [1] tiny [2] coop [3] large [4] spills [5] error bits
+                    // [6] huge count [8,9] tile total (u64) [16..23] huge record ids
+};
+
+__device__ __forceinline__ void tier_spill(const TierArgs& a, unsigned id) {
+    unsigned s = atomicAdd(a.ctr + 4, 1u);
+    if (s < a.spill_cap) a.spill[s] = id;
+    else atomicOr(a.ctr + 5, 1u);
+}
+
+template <int MODE>
+__device__ void tier_sub(const TierArgs& a, const float* c0, const float* c1, const float* c2,
+                         const float* b0, const float* b1, const float* b2, unsigned prim,
+                         unsigned sub) {
+    Setup s;
+    if (!setup_triangle(c0, c1, c2, b0, b1, b2, a.r.W, a.r.H, s)) return;
+    int64_t minX = min(s.X[0], min(s.X[1], s.X[2])), maxX = max(s.X[0], max(s.X[1], s.X[2]));
+    int64_t minY = min(s.Y[0], min(s.Y[1], s.Y[2])), maxY = max(s.Y[0], max(s.Y[1], s.Y[2]));
+    int x0 = (int)max((int64_t)0, -((-(minX - kSub / 2)) >> kSubBits));
+    int x1 = (int)min((int64_t)a.r.W - 1, (maxX - kSub / 2) >> kSubBits);
+    int y0 = (int)max((int64_t)0, -((-(minY - kSub / 2)) >> kSubBits));
+    int y1 = (int)min((int64_t)a.r.H - 1, (maxY - kSub / 2) >> kSubBits);
+    if (x0 > x1 || y0 > y1) return;
+    const unsigned spill_id = (prim << 3) | sub;
+    unsigned slot = atomicAdd(a.ctr + 0, 1u);
+    if (slot >= a.rec_cap) {
+        tier_spill(a, spill_id);
+        return;
+    }
+    float zoff = 0.0f;
+    if (MODE == MODE_DEPTH) {
+        if (a.r.bias_mode == GI_BIAS_POLYGON_OFFSET) zoff = polygon_offset(s, a.r.factor, a.r.units);
+        else if (a.r.bias_mode == GI_BIAS_CONSTANT) zoff = a.r.cbias;
+    }
+    BRec r;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        r.X[i] = (int)s.X[i];
+        r.Y[i] = (int)s.Y[i];
+    }
+    r.z0 = s.z[0];
+    r.dz1 = s.z[1] - s.z[0];
+    r.dz2 = s.z[2] - s.z[0];
+    r.inv_area = s.inv_area;
+    r.zoff = zoff;
+    r.prim = MODE == MODE_VKEY ? spill_id : prim;
+    r.x0 = (unsigned short)x0;
+    r.x1 = (unsigned short)x1;
+    r.y0 = (unsigned short)y0;
+    r.y1 = (unsigned short)y1;
+    r.flags = s.front ? kFlagFront : 0u;
+    r.spill_id = spill_id;
+    a.recs[slot] = r;
+    const long long npx = (long long)(x1 - x0 + 1) * (y1 - y0 + 1);
+    if (npx <= kTinyPx) a.tiny[atomicAdd(a.ctr + 1, 1u)] = slot;
+    else if (npx <= kCoopPx) a.coop[atomicAdd(a.ctr + 2, 1u)] = slot;
+    else a.large[atomicAdd(a.ctr + 3, 1u)] = slot;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(128) k_tier_setup(TierArgs a) {
+    int prim = blockIdx.x * blockDim.x + threadIdx.x;
+    if (prim >= a.r.num_prims) return;
+    float v[3][3];
+    prim_vertices<MODE>(a.r, prim, v);
+    float c[3][4];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) transform(a.r.mvp, v[j][0], v[j][1], v[j][2], c[j]);
+    const float id[3][3] = {{1.0f, 0.0f, 0.0f}, {0.0f, 1.0f, 0.0f}, {0.0f, 0.0f, 1.0f}};
+    if (all_inside(c[0], c[1], c[2])) {
+        tier_sub<MODE>(a, c[0], c[1], c[2], id[0], id[1], id[2], (unsigned)prim, 0u);
+        return;
+    }
+    CV poly[9];
+    int n = clip_polygon(c[0], c[1], c[2], poly);
+    for (int i = 1; i + 1 < n; ++i)
+        tier_sub<MODE>(a, poly[0].c, poly[i].c, poly[i + 1].c, poly[0].b, poly[i].b, poly[i + 1].b,
+                       (unsigned)prim, (unsigned)(i - 1));
+}
+
+constexpr unsigned kFlagHuge = 4u;
+
+// 16 x 16 tiles of a large record's bounding box (0 for the huge ones,
+// which k_base draws).
+__device__ __forceinline__ unsigned long long rec_tiles(const BRec& r) {
+    if (r.flags & kFlagHuge) return 0;
+    return (unsigned long long)((r.x1 / kTile) - (r.x0 / kTile) + 1) * ((r.y1 / kTile) - (r.y0 / kTile) + 1);
+}
+
+// Picks the huge records and scans the 16 x 16 tile counts of the others
+// (bases are non-decreasing; huge records get an empty range).
+__global__ void __launch_bounds__(1024) k_large_scan(TierArgs a) {
+    __shared__ unsigned long long warp_sums[32];
+    __shared__ int nhuge;
+    const unsigned n = a.ctr[3];
+    if (threadIdx.x == 0) nhuge = 0;
+    __syncthreads();
+    unsigned long long carry = 0;
+    for (unsigned start = 0; start < n; start += 1024) {
+        unsigned i = start + threadIdx.x;
+        unsigned long long v = 0;
+        if (i < n) {
+            BRec* rp = a.recs + a.large[i];
+            const BRec r = *rp;
+            const unsigned long long npx = (unsigned long long)(r.x1 - r.x0 + 1) * (r.y1 - r.y0 + 1);
+            bool huge = false;
+            if (npx >= a.huge_px) {
+                const int h = atomicAdd(&nhuge, 1);
+                if (h < kHugeMax) {
+                    a.ctr[16 + h] = a.large[i];
+                    rp->flags = r.flags | kFlagHuge;
+                    huge = true;
+                }
+            }
+            if (!huge) v = (unsigned long long)((r.x1 / kTile) - (r.x0 / kTile) + 1) * ((r.y1 / kTile) - (r.y0 / kTile) + 1);
+        }
+        unsigned long long tot;
+        unsigned long long ex = block_scan_1024(v, warp_sums, &tot);
+        if (i < n) a.large_base[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) {
+        a.ctr[6] = (unsigned)min(nhuge, kHugeMax);
+        *reinterpret_cast<unsigned long long*>(a.ctr + 8) = carry;
+    }
+}
+
+// Huge records at every pixel; writes the target (and so clears it).
+template <int MODE>
+__global__ void __launch_bounds__(256) k_base(TierArgs a) {
+    typedef typename BinVal<MODE>::T V;
+    __shared__ BRec hr[kHugeMax];
+    const int nh = (int)a.ctr[6];
+    if (threadIdx.x < nh) hr[threadIdx.x] = a.recs[a.ctr[16 + threadIdx.x]];
+    __syncthreads();
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int yb = blockIdx.y * 32 + (threadIdx.x >> 5) * 4;  // 4 rows per thread
+    if (x >= a.r.W) return;
+    const V clearv = MODE == MODE_DEPTH ? (V)0x3f800000u
+                                        : (V)(((unsigned long long)0x3f800000u << 32) | 0xFFFFFFFFull);
+    V val[4] = {clearv, clearv, clearv, clearv};
+    const int64_t px = (int64_t)x * kSub + kSub / 2;
+    for (int h = 0; h < nh; ++h) {
+        const BRec& r = hr[h];
+        if (x < (int)r.x0 || x > (int)r.x1) continue;
+        int64_t A[3], E[3];
+        bool tl[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const int ia = (i + 1) % 3, ib = (i + 2) % 3;
+            A[i] = (int64_t)r.X[ib] - r.X[ia];
+            const int64_t B = (int64_t)r.Y[ib] - r.Y[ia];
+            tl[i] = (B < 0) || (B == 0 && A[i] < 0);
+            E[i] = A[i] * ((int64_t)yb * kSub + kSub / 2 - r.Y[ia]) - B * (px - r.X[ia]);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int y = yb + k;
+            const bool in = y >= (int)r.y0 && y <= (int)r.y1 && (E[0] > 0 || (E[0] == 0 && tl[0])) &&
+                            (E[1] > 0 || (E[1] == 0 && tl[1])) && (E[2] > 0 || (E[2] == 0 && tl[2]));
+            if (in) {
+                const float l1 = (float)E[1] * r.inv_area, l2 = (float)E[2] * r.inv_area;
+                float z = r.z0 + (l1 * r.dz1 + l2 * r.dz2);
+                if (MODE == MODE_DEPTH) {
+                    z = clamp01(z + r.zoff);
+                    if (z < 1.0f && __float_as_uint(z) < (unsigned)val[k]) val[k] = __float_as_uint(z);
+                } else {
+                    z = clamp01(z);
+                    if (z < 1.0f) {
+                        const unsigned long long key = ((unsigned long long)__float_as_uint(z) << 32) | r.prim;
+                        if (key < (unsigned long long)val[k]) val[k] = key;
+                    }
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 3; ++i) E[i] += A[i] * kSub;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int y = yb + k;
+        if (y >= a.r.H) break;
+        const size_t idx = (size_t)y * a.r.W + x;
+        if (MODE == MODE_DEPTH) a.r.depth[idx] = (unsigned)val[k];
+        else a.r.keys[idx] = (unsigned long long)val[k];
+    }
+}
+
+__device__ __forceinline__ void rec_edges(const BRec& r, int64_t A[3], int64_t B[3], bool tl[3]) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const int ia = (i + 1) % 3, ib = (i + 2) % 3;
+        A[i] = (int64_t)r.X[ib] - r.X[ia];
+        B[i] = (int64_t)r.Y[ib] - r.Y[ia];
+        tl[i] = (B[i] < 0) || (B[i] == 0 && A[i] < 0);
+    }
+}
+
+template <int MODE>
+__device__ __forceinline__ void rec_emit(const TierArgs& a, const BRec& r, int x, int y, float fe1, float fe2) {
+    const float l1 = fe1 * r.inv_area, l2 = fe2 * r.inv_area;
+    const float z = r.z0 + (l1 * r.dz1 + l2 * r.dz2);
+    emit<MODE>(a.r, x, y, z, r.zoff, r.prim, (r.flags & kFlagFront) != 0);
+}
+
+// Tiny records: one thread each over the bounding box.
+template <int MODE>
+__global__ void __launch_bounds__(128) k_tiny(TierArgs a) {
+    const unsigned n = a.ctr[1];
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const BRec r = a.recs[a.tiny[i]];
+        int64_t A[3], B[3];
+        bool tl[3];
+        rec_edges(r, A, B, tl);
+        for (int y = r.y0; y <= (int)r.y1; ++y) {
+            const int64_t py = (int64_t)y * kSub + kSub / 2;
+            for (int x = r.x0; x <= (int)r.x1; ++x) {
+                const int64_t px = (int64_t)x * kSub + kSub / 2;
+                int64_t E[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const int ia = (k + 1) % 3;
+                    E[k] = A[k] * (py - r.Y[ia]) - B[k] * (px - r.X[ia]);
+                }
+                const bool in = (E[0] > 0 || (E[0] == 0 && tl[0])) && (E[1] > 0 || (E[1] == 0 && tl[1])) &&
+                                (E[2] > 0 || (E[2] == 0 && tl[2]));
+                if (in) rec_emit<MODE>(a, r, x, y, (float)E[1], (float)E[2]);
+            }
+        }
+    }
+}
+
+// Warp-sized records: one warp per record, lanes over the bounding box.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_coop(TierArgs a) {
+    const unsigned n = a.ctr[2];
+    const int lane = threadIdx.x & 31;
+    const unsigned nwarps = gridDim.x * (blockDim.x >> 5);
+    for (unsigned i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += nwarps) {
+        const BRec r = a.recs[a.coop[i]];
+        const int w = r.x1 - r.x0 + 1, h = r.y1 - r.y0 + 1, npx = w * h;
+        // p / w by a reciprocal: (p + 1/2) / w stays at least 1/(2w) >= 2^-11
+        // from an integer and the product errs by under 2^-13 for p < 1024.
+        const float inv_w = 1.0f / (float)w;
+        int64_t A[3], B[3], E0[3];
+        bool tl[3];
+        rec_edges(r, A, B, tl);
+        const int64_t cx = (int64_t)r.x0 * kSub + kSub / 2, cy = (int64_t)r.y0 * kSub + kSub / 2;
+        bool fits32 = true;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int ia = (k + 1) % 3;
+            E0[k] = A[k] * (cy - r.Y[ia]) - B[k] * (cx - r.X[ia]);
+            const int64_t bound = abs(E0[k]) + abs(A[k]) * (int64_t)(h - 1) * kSub + abs(B[k]) * (int64_t)(w - 1) * kSub;
+            fits32 &= bound < (1LL << 31);
+        }
+        for (int p = lane; p < npx; p += 32) {
+            const int dy = (int)(((float)p + 0.5f) * inv_w);
+            const int dx = p - dy * w;
+            bool in;
+            float fe1, fe2;
+            if (fits32) {
+                int e[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+                    e[k] = (int)E0[k] + (int)A[k] * (dy << kSubBits) - (int)B[k] * (dx << kSubBits);
+                in = (e[0] > 0 || (e[0] == 0 && tl[0])) && (e[1] > 0 || (e[1] == 0 && tl[1])) &&
+                     (e[2] > 0 || (e[2] == 0 && tl[2]));
+                fe1 = (float)e[1];
+                fe2 = (float)e[2];
+            } else {
+                int64_t E[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+                    E[k] = E0[k] + A[k] * (int64_t)(dy << kSubBits) - B[k] * (int64_t)(dx << kSubBits);
+                in = (E[0] > 0 || (E[0] == 0 && tl[0])) && (E[1] > 0 || (E[1] == 0 && tl[1])) &&
+                     (E[2] > 0 || (E[2] == 0 && tl[2]));
+                fe1 = (float)E[1];
+                fe2 = (float)E[2];
+            }
+            if (in) rec_emit<MODE>(a, r, r.x0 + dx, r.y0 + dy, fe1, fe2);
+        }
+    }
+}
+
+// Large (non-huge) records: warps take contiguous ranges of the implied
+// 16 x 16 tile list, reject tiles the triangle misses, 8 pixels per lane.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_large_tiles(TierArgs a) {
+    const unsigned n = a.ctr[3];
+    const unsigned long long total = *reinterpret_cast<const unsigned long long*>(a.ctr + 8);
+    if (n == 0 || total == 0) return;
+    const int lane = threadIdx.x & 31;
+    const unsigned long long nwarps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+    const unsigned long long w = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const unsigned long long begin = total * w / nwarps, end = total * (w + 1) / nwarps;
+    if (begin >= end) return;
+    // last record whose base is <= begin
+    unsigned lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const unsigned mid = (lo + hi + 1) >> 1;
+        if (a.large_base[mid] <= begin) lo = mid;
+        else hi = mid - 1;
+    }
+    unsigned ri = lo;
+    BRec r = a.recs[a.large[ri]];
+    unsigned long long base = a.large_base[ri], nt = rec_tiles(r);
+    int64_t A[3], B[3];
+    bool tl[3];
+    rec_edges(r, A, B, tl);
+    for (unsigned long long item = begin; item < end; ++item) {
+        while (item >= base + nt) {
+            ++ri;
+            r = a.recs[a.large[ri]];
+            base = a.large_base[ri];
+            nt = rec_tiles(r);
+            rec_edges(r, A, B, tl);
+        }
+        const unsigned local = (unsigned)(item - base);
+        const int ntx = (r.x1 / kTile) - (r.x0 / kTile) + 1;
+        const int ty = (r.y0 / kTile) + (int)(local / (unsigned)ntx);
+        const int tx = (r.x0 / kTile) + (int)(local % (unsigned)ntx);
+        const int px0 = max(tx * kTile, (int)r.x0), px1 = min(tx * kTile + kTile - 1, (int)r.x1);
+        const int py0 = max(ty * kTile, (int)r.y0), py1 = min(ty * kTile + kTile - 1, (int)r.y1);
+        bool miss = false;
+        {
+            const int64_t cx0 = (int64_t)px0 * kSub + kSub / 2, cx1 = (int64_t)px1 * kSub + kSub / 2;
+            const int64_t cy0 = (int64_t)py0 * kSub + kSub / 2, cy1 = (int64_t)py1 * kSub + kSub / 2;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const int ia = (i + 1) % 3;
+                const int64_t ymax = A[i] > 0 ? cy1 : cy0, xmin = B[i] > 0 ? cx0 : cx1;
+                miss |= A[i] * (ymax - r.Y[ia]) - B[i] * (xmin - r.X[ia]) < 0;
+            }
+        }
+        if (miss) continue;
+        const int x = tx * kTile + (lane & 15);
+        int y = ty * kTile + (lane >> 4);
+        if (x < px0 || x > px1) continue;
+        const int64_t px = (int64_t)x * kSub + kSub / 2, py = (int64_t)y * kSub + kSub / 2;
+        int64_t E[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const int ia = (i + 1) % 3;
+            E[i] = A[i] * (py - r.Y[ia]) - B[i] * (px - r.X[ia]);
+        }
+#pragma unroll 2
+        for (int k = 0; k < kTile / 2; ++k, y += 2) {
+            const bool in = y >= py0 && y <= py1 && (E[0] > 0 || (E[0] == 0 && tl[0])) &&
+                            (E[1] > 0 || (E[1] == 0 && tl[1])) && (E[2] > 0 || (E[2] == 0 && tl[2]));
+            if (in) rec_emit<MODE>(a, r, x, y, (float)E[1], (float)E[2]);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) E[i] += A[i] * (2 * kSub);
+        }
+    }
+}
+
+// Spilled sub-triangles of the tiered passes (one thread each, atomics).
+template <int MODE>
+__global__ void __launch_bounds__(128) k_tier_spill(TierArgs a) {
+    const unsigned n = min(a.ctr[4], a.spill_cap);
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned id = a.spill[i];
+        const int prim = (int)(id >> 3), sub = (int)(id & 7);
+        float v[3][3];
+        prim_vertices<MODE>(a.r, prim, v);
+        float c[3][4];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) transform(a.r.mvp, v[j][0], v[j][1], v[j][2], c[j]);
+        const float idm[3][3] = {{1.0f, 0.0f, 0.0f}, {0.0f, 1.0f, 0.0f}, {0.0f, 0.0f, 1.0f}};
+        Setup s;
+        bool ok;
+        if (all_inside(c[0], c[1], c[2])) {
+            ok = sub == 0 && setup_triangle(c[0], c[1], c[2], idm[0], idm[1], idm[2], a.r.W, a.r.H, s);
+        } else {
+            CV poly[9];
+            int np = clip_polygon(c[0], c[1], c[2], poly);
+            ok = (sub + 2 < np) && setup_triangle(poly[0].c, poly[sub + 1].c, poly[sub + 2].c, poly[0].b,
+                                                  poly[sub + 1].b, poly[sub + 2].b, a.r.W, a.r.H, s);
+        }
+        if (!ok) continue;
+        int64_t minX = min(s.X[0], min(s.X[1], s.X[2])), maxX = max(s.X[0], max(s.X[1], s.X[2]));
+        int64_t minY = min(s.Y[0], min(s.Y[1], s.Y[2])), maxY = max(s.Y[0], max(s.Y[1], s.Y[2]));
+        int x0 = (int)max((int64_t)0, -((-(minX - kSub / 2)) >> kSubBits));
+        int x1 = (int)min((int64_t)a.r.W - 1, (maxX - kSub / 2) >> kSubBits);
+        int y0 = (int)max((int64_t)0, -((-(minY - kSub / 2)) >> kSubBits));
+        int y1 = (int)min((int64_t)a.r.H - 1, (maxY - kSub / 2) >> kSubBits);
+        if (x0 > x1 || y0 > y1) continue;
+        float zoff = 0.0f;
+        if (MODE == MODE_DEPTH) {
+            if (a.r.bias_mode == GI_BIAS_POLYGON_OFFSET) zoff = polygon_offset(s, a.r.factor, a.r.units);
+            else if (a.r.bias_mode == GI_BIAS_CONSTANT) zoff = a.r.cbias;
+        }
+        Edges e;
+        make_edges(s, e);
+        raster_small<MODE>(a.r, s, e, x0, x1, y0, y1, zoff, MODE == MODE_VKEY ? id : (unsigned)prim);
+    }
+}
+
 }  // namespace dev
 
 // ---------------------------------------------------------------------------
@@ -497,59 +1508,7 @@ gi_status launch_fill_u32(gi_context* ctx, unsigned* p, size_t n, unsigned v, cu
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "fill kernel launch");
 }
 
-static gi_status ensure_records(gi_context* ctx) {
-    // Start with room for 256K large triangles; grow 4x after a pass that
-    // spilled (the spilled triangles were still rasterised, only slower).
-    size_t want = ctx->cap_tri_records ? ctx->cap_tri_records / sizeof(dev::TriRec) : 0;
-    if (want == 0) want = 256 * 1024;
-    if (ctx->h_status && ctx->h_status[1] > 0 && ctx->h_status[0] > want) {
-        while (want < ctx->h_status[0] && want < (size_t)1 << 26) want *= 4;
-        ctx->h_status[1] = 0;
-    }
-    return ensure_buffer(&ctx->d_tri_records, &ctx->cap_tri_records, want * sizeof(dev::TriRec));
-}
 
-// One raster pass: setup, scan and tile kernels (the target is cleared by
-// the caller).  `mode` selects the fragment operation.
-static gi_status run_raster(gi_context* ctx, dev::RasterArgs& a, int mode, cudaStream_t st) {
-    if (a.num_prims <= 0) return GI_OK;
-    gi_status s = ensure_records(ctx);
-    if (s != GI_OK) return s;
-    a.recs = static_cast<dev::TriRec*>(ctx->d_tri_records);
-    a.rec_cap = (unsigned)(ctx->cap_tri_records / sizeof(dev::TriRec));
-    a.counters = ctx->d_status + 4;
-    a.tile_total = reinterpret_cast<unsigned long long*>(ctx->d_status + 8);
-    if (a.small_px <= 0) a.small_px = 128;
-    cudaError_t e = cudaMemsetAsync(ctx->d_status + 4, 0, 8 * sizeof(unsigned), st);
-    if (e != cudaSuccess) return fail_cuda(e, "cudaMemsetAsync(counters)");
-    unsigned g = grid_for((size_t)a.num_prims, 128);
-    const int blocks_tiles = sm_count(ctx->device) * 8;
-    switch (mode) {
-        case dev::MODE_DEPTH:
-            dev::k_setup<dev::MODE_DEPTH><<<g, 128, 0, st>>>(a);
-            dev::k_scan<<<1, 1024, 0, st>>>(a.recs, a.counters, a.rec_cap, a.tile_total);
-            dev::k_tiles<dev::MODE_DEPTH><<<blocks_tiles, 256, 0, st>>>(a);
-            break;
-        case dev::MODE_VKEY:
-            dev::k_setup<dev::MODE_VKEY><<<g, 128, 0, st>>>(a);
-            dev::k_scan<<<1, 1024, 0, st>>>(a.recs, a.counters, a.rec_cap, a.tile_total);
-            dev::k_tiles<dev::MODE_VKEY><<<blocks_tiles, 256, 0, st>>>(a);
-            break;
-        default:
-            dev::k_setup<dev::MODE_STENCIL><<<g, 128, 0, st>>>(a);
-            dev::k_scan<<<1, 1024, 0, st>>>(a.recs, a.counters, a.rec_cap, a.tile_total);
-            dev::k_tiles<dev::MODE_STENCIL><<<blocks_tiles, 256, 0, st>>>(a);
-            break;
-    }
-    ctx->launches += 3;
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return fail_cuda(e, "raster kernel launch");
-    // Mirror the counters for the capacity heuristic (read on a later call).
-    e = cudaMemcpyAsync(ctx->h_status, ctx->d_status + 4, 2 * sizeof(unsigned),
-                        cudaMemcpyDeviceToHost, st);
-    if (e != cudaSuccess) return fail_cuda(e, "cudaMemcpyAsync(counters)");
-    return GI_OK;
-}
 
 static dev::Mat4 mat_of(const float m[16]) {
     dev::Mat4 r;
@@ -557,12 +1516,158 @@ static dev::Mat4 mat_of(const float m[16]) {
     return r;
 }
 
+// Binned pass: setup, big-record expansion, bin scan, scatter, per-bin
+// raster and the spill pass (8 launches + 2 memsets, stream-ordered).
+static gi_status run_binned(gi_context* ctx, dev::RasterArgs& r, int mode, cudaStream_t st) {
+    const int nbx = (r.W + dev::kBin - 1) / dev::kBin, nby = (r.H + dev::kBin - 1) / dev::kBin;
+    const size_t nbins = (size_t)nbx * nby;
+    const size_t prims = (size_t)std::max(r.num_prims, 0);
+    const size_t rec_cap = 2 * prims + 4096;
+    const size_t big_pair_cap = 16 * nbins + 4 * rec_cap;
+    const size_t list_cap = 4 * rec_cap + big_pair_cap;
+    const size_t item_cap = nbins + list_cap / dev::kSeg + 1;
+    const size_t need[8] = {rec_cap * sizeof(dev::BRec), rec_cap * sizeof(unsigned),
+                            rec_cap * sizeof(unsigned long long), rec_cap * sizeof(unsigned),
+                            4 * (nbins + 1) * sizeof(unsigned), list_cap * sizeof(unsigned),
+                            4 * rec_cap * sizeof(unsigned), item_cap * sizeof(unsigned)};
+    for (int i = 0; i < 8; ++i) {
+        gi_status s = ensure_buffer(&ctx->bin_buf[i], &ctx->bin_cap[i], need[i]);
+        if (s != GI_OK) return s;
+    }
+    dev::BinArgs a;
+    a.r = r;
+    a.recs = static_cast<dev::BRec*>(ctx->bin_buf[0]);
+    a.rec_cap = (unsigned)rec_cap;
+    a.big_list = static_cast<unsigned*>(ctx->bin_buf[1]);
+    a.big_base = static_cast<unsigned long long*>(ctx->bin_buf[2]);
+    a.big_cap = (unsigned)rec_cap;
+    a.spill = static_cast<unsigned*>(ctx->bin_buf[3]);
+    a.spill_cap = (unsigned)rec_cap;
+    unsigned* bins = static_cast<unsigned*>(ctx->bin_buf[4]);
+    a.bin_count = bins;
+    a.big_count = bins + (nbins + 1);
+    a.bin_offset = bins + 2 * (nbins + 1);
+    a.bin_cursor = bins + 3 * (nbins + 1);
+    a.bin_list = static_cast<unsigned*>(ctx->bin_buf[5]);
+    a.ranks = static_cast<unsigned*>(ctx->bin_buf[6]);
+    a.items = static_cast<unsigned*>(ctx->bin_buf[7]);
+    a.item_cap = (unsigned)item_cap;
+    a.list_cap = list_cap;
+    a.big_pair_cap = big_pair_cap;
+    a.ctr = ctx->d_status + 4;  // [0..3] counters, [4..5] admitted pairs (u64)
+    a.nbx = nbx;
+    a.nby = nby;
+    cudaError_t e = cudaMemsetAsync(a.bin_count, 0, 2 * (nbins + 1) * sizeof(unsigned), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.ctr, 0, 8 * sizeof(unsigned), st);
+    if (e != cudaSuccess) return fail_cuda(e, "binned raster memset");
+    const unsigned sms = (unsigned)sm_count(ctx->device);
+    const unsigned gsetup = grid_for(prims ? prims : 1, 128);
+    const unsigned gfill = grid_for(rec_cap, 256);
+    switch (mode) {
+        case dev::MODE_DEPTH:
+            if (prims) dev::k_bin_setup<dev::MODE_DEPTH><<<gsetup, 128, 0, st>>>(a);
+            break;
+        case dev::MODE_VKEY:
+            if (prims) dev::k_bin_setup<dev::MODE_VKEY><<<gsetup, 128, 0, st>>>(a);
+            break;
+        default:
+            if (prims) dev::k_bin_setup<dev::MODE_STENCIL><<<gsetup, 128, 0, st>>>(a);
+            break;
+    }
+    dev::k_big_scan<<<1, 1024, 0, st>>>(a);
+    dev::k_big_pairs<false><<<sms * 4, 256, 0, st>>>(a);
+    dev::k_bin_scan<<<1, 1024, 0, st>>>(a);
+    dev::k_bin_fill_small<<<gfill, 256, 0, st>>>(a);
+    dev::k_big_pairs<true><<<sms * 4, 256, 0, st>>>(a);
+    // the raster leaves empty bins alone: clear the target first
+    const size_t npx = (size_t)r.W * r.H;
+    const unsigned gclear = std::min<unsigned>(grid_for(npx / 4 + 1, 256), sms * 8);
+    if (mode == dev::MODE_DEPTH) {
+        dev::k_fill_u32<<<gclear, 256, 0, st>>>(r.depth, npx, 0x3f800000u);
+    } else if (mode == dev::MODE_VKEY) {
+        dev::k_fill_u64<<<std::min<unsigned>(grid_for(npx, 256), sms * 8), 256, 0, st>>>(
+            r.keys, npx, ((unsigned long long)0x3f800000u << 32) | 0xFFFFFFFFull);
+    } else {
+        e = cudaMemsetAsync(r.counts, 0, npx * sizeof(int), st);
+        if (e != cudaSuccess) return fail_cuda(e, "binned raster memset(counts)");
+    }
+    const unsigned graster = (unsigned)item_cap;
+    switch (mode) {
+        case dev::MODE_DEPTH:
+            dev::k_bin_raster<dev::MODE_DEPTH><<<graster, 256, 0, st>>>(a);
+            dev::k_spill<dev::MODE_DEPTH><<<sms * 2, 128, 0, st>>>(a);
+            break;
+        case dev::MODE_VKEY:
+            dev::k_bin_raster<dev::MODE_VKEY><<<graster, 256, 0, st>>>(a);
+            dev::k_spill<dev::MODE_VKEY><<<sms * 2, 128, 0, st>>>(a);
+            break;
+        default:
+            dev::k_bin_raster<dev::MODE_STENCIL><<<graster, 256, 0, st>>>(a);
+            dev::k_spill<dev::MODE_STENCIL><<<sms * 2, 128, 0, st>>>(a);
+            break;
+    }
+    ctx->launches += (prims ? 8 : 7) + (mode == dev::MODE_STENCIL ? 0 : 1);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail_cuda(e, "binned raster launch");
+    return GI_OK;
+}
+
+// Tiered pass (light map, G-buffer keys): setup, large-record scan, base
+// layer (huge records + clear), tiny / warp / tile rasterisation with
+// atomics, spill (7 launches + 1 memset, stream-ordered).
+static gi_status run_tiered(gi_context* ctx, dev::RasterArgs& r, int mode, cudaStream_t st) {
+    const size_t prims = (size_t)std::max(r.num_prims, 0);
+    const size_t rec_cap = 2 * prims + 4096;
+    const size_t need[6] = {rec_cap * sizeof(dev::BRec), rec_cap * sizeof(unsigned),
+                            rec_cap * sizeof(unsigned), rec_cap * sizeof(unsigned),
+                            rec_cap * sizeof(unsigned long long), rec_cap * sizeof(unsigned)};
+    for (int i = 0; i < 6; ++i) {
+        gi_status s = ensure_buffer(&ctx->tier_buf[i], &ctx->tier_cap[i], need[i]);
+        if (s != GI_OK) return s;
+    }
+    dev::TierArgs a;
+    a.r = r;
+    a.recs = static_cast<dev::BRec*>(ctx->tier_buf[0]);
+    a.rec_cap = (unsigned)rec_cap;
+    a.tiny = static_cast<unsigned*>(ctx->tier_buf[1]);
+    a.coop = static_cast<unsigned*>(ctx->tier_buf[2]);
+    a.large = static_cast<unsigned*>(ctx->tier_buf[3]);
+    a.large_base = static_cast<unsigned long long*>(ctx->tier_buf[4]);
+    a.spill = static_cast<unsigned*>(ctx->tier_buf[5]);
+    a.spill_cap = (unsigned)rec_cap;
+    a.huge_px = std::max<unsigned long long>(65536ull, (unsigned long long)r.W * r.H / 8);
+    a.ctr = ctx->d_status + 32;  // 24 words
+    cudaError_t e = cudaMemsetAsync(a.ctr, 0, 24 * sizeof(unsigned), st);
+    if (e != cudaSuccess) return fail_cuda(e, "tiered raster memset");
+    const unsigned sms = (unsigned)sm_count(ctx->device);
+    const unsigned gsetup = grid_for(prims ? prims : 1, 128);
+    const dim3 gbase((r.W + 31) / 32, (r.H + 31) / 32);
+    if (mode == dev::MODE_DEPTH) {
+        if (prims) dev::k_tier_setup<dev::MODE_DEPTH><<<gsetup, 128, 0, st>>>(a);
+        dev::k_large_scan<<<1, 1024, 0, st>>>(a);
+        dev::k_base<dev::MODE_DEPTH><<<gbase, 256, 0, st>>>(a);
+        dev::k_tiny<dev::MODE_DEPTH><<<sms * 8, 128, 0, st>>>(a);
+        dev::k_coop<dev::MODE_DEPTH><<<sms * 8, 256, 0, st>>>(a);
+        dev::k_large_tiles<dev::MODE_DEPTH><<<sms * 8, 256, 0, st>>>(a);
+        dev::k_tier_spill<dev::MODE_DEPTH><<<sms * 2, 128, 0, st>>>(a);
+    } else {
+        if (prims) dev::k_tier_setup<dev::MODE_VKEY><<<gsetup, 128, 0, st>>>(a);
+        dev::k_large_scan<<<1, 1024, 0, st>>>(a);
+        dev::k_base<dev::MODE_VKEY><<<gbase, 256, 0, st>>>(a);
+        dev::k_tiny<dev::MODE_VKEY><<<sms * 8, 128, 0, st>>>(a);
+        dev::k_coop<dev::MODE_VKEY><<<sms * 8, 256, 0, st>>>(a);
+        dev::k_large_tiles<dev::MODE_VKEY><<<sms * 8, 256, 0, st>>>(a);
+        dev::k_tier_spill<dev::MODE_VKEY><<<sms * 2, 128, 0, st>>>(a);
+    }
+    ctx->launches += prims ? 7 : 6;
+    e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "tiered raster launch");
+}
+
 gi_status raster_depth_map(gi_context* ctx, const gi_scene* scene, const float mvp[16], int W,
                            int H, int bias_mode, float cbias, float factor, float units,
                            float* d_depth, int small_px, cudaStream_t st) {
-    gi_status s = launch_fill_u32(ctx, reinterpret_cast<unsigned*>(d_depth), (size_t)W * H,
-                                  0x3f800000u, st);
-    if (s != GI_OK) return s;
+    (void)small_px;
     dev::RasterArgs a = {};
     a.points = scene->d_points;
     a.normals = scene->d_normals;
@@ -576,20 +1681,16 @@ gi_status raster_depth_map(gi_context* ctx, const gi_scene* scene, const float m
     a.factor = factor;
     a.units = units;
     a.depth = reinterpret_cast<unsigned*>(d_depth);
-    a.small_px = small_px;
-    return run_raster(ctx, a, dev::MODE_DEPTH, st);
+    return run_tiered(ctx, a, dev::MODE_DEPTH, st);
 }
 
 gi_status raster_gbuffer(gi_context* ctx, const gi_scene* scene, const float mvp[16], int W, int H,
                          float* d_pos, float* d_nrm, int small_px, cudaStream_t st) {
+    (void)small_px;
     const size_t npx = (size_t)W * H;
     gi_status s = ensure_buffer(reinterpret_cast<void**>(&ctx->d_vkeys), &ctx->cap_vkeys,
                                 npx * sizeof(unsigned long long));
     if (s != GI_OK) return s;
-    const unsigned long long clear = ((unsigned long long)0x3f800000u << 32) | 0xFFFFFFFFull;
-    dev::k_fill_u64<<<std::min<unsigned>(grid_for(npx, 256), (unsigned)sm_count(ctx->device) * 8),
-                      256, 0, st>>>(ctx->d_vkeys, npx, clear);
-    ctx->launches++;
     dev::RasterArgs a = {};
     a.points = scene->d_points;
     a.normals = scene->d_normals;
@@ -599,8 +1700,7 @@ gi_status raster_gbuffer(gi_context* ctx, const gi_scene* scene, const float mvp
     a.W = W;
     a.H = H;
     a.keys = ctx->d_vkeys;
-    a.small_px = small_px;
-    s = run_raster(ctx, a, dev::MODE_VKEY, st);
+    s = run_tiered(ctx, a, dev::MODE_VKEY, st);
     if (s != GI_OK) return s;
     dim3 grid((W + 31) / 32, (H + 3) / 4);
     dev::k_gbuffer_resolve<<<grid, 128, 0, st>>>(ctx->d_vkeys, scene->d_points, scene->d_normals,
@@ -629,14 +1729,12 @@ gi_status raster_shadow_volumes(gi_context* ctx, const gi_scene* scene, const fl
     if (s != GI_OK) return s;
     s = raster_depth_map(ctx, scene, mvp, W, H, GI_BIAS_NONE, 0.0f, 0.0f, 0.0f, depth, small_px, st);
     if (s != GI_OK) return s;
-    cudaError_t e = cudaMemsetAsync(ctx->d_counts, 0, npx * sizeof(int), st);
-    if (e != cudaSuccess) return fail_cuda(e, "cudaMemsetAsync(counts)");
     dev::RasterArgs a = {};
     a.points = scene->d_points;
     a.normals = scene->d_normals;
     a.indices = scene->d_indices;
-    if ((long long)scene->dev_triangles * 6 > 0x7fffffffLL)
-        return fail(GI_ERR_CAPACITY, "too many volume triangles");
+    if ((long long)scene->dev_triangles * 6 >= (1LL << 29))
+        return fail(GI_ERR_CAPACITY, "too many volume triangles (6 T must stay below 2^29)");
     a.num_prims = scene->dev_triangles * 6;
     a.mvp = mat_of(mvp);
     a.W = W;
@@ -648,12 +1746,11 @@ gi_status raster_shadow_volumes(gi_context* ctx, const gi_scene* scene, const fl
     a.infinity = infinity;
     a.depth = reinterpret_cast<unsigned*>(depth);
     a.counts = ctx->d_counts;
-    a.small_px = small_px;
-    s = run_raster(ctx, a, dev::MODE_STENCIL, st);
+    s = run_binned(ctx, a, dev::MODE_STENCIL, st);
     if (s != GI_OK) return s;
     dev::k_wrap_stencil<<<grid_for(npx, 256), 256, 0, st>>>(ctx->d_counts, d_stencil, npx);
     ctx->launches++;
-    e = cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "stencil wrap launch");
 }
 
