@@ -12,9 +12,9 @@ one shadowed frame: light-view depth map, G-buffer, visibility.
   e2e     frames/s through the C ABI with host buffers: every step uploads
           the scene from pinned host memory (gi_scene_upload_from), renders,
           and reads the visibility buffer back to pinned host memory
-  roofline  the visibility kernel (the frame's largest): algorithmic bytes
-          36 P + 4 S^2 per launch over its event-timed duration, against the
-          measured HBM copy bandwidth
+  roofline  the fused G-buffer-resolve + visibility kernel: algorithmic
+          bytes 12 P + 4 S^2 + scene per launch over its event-timed
+          duration, against the measured HBM copy bandwidth
   cpu_baseline  the CPU oracle (restatement of the reference's passes) on
           the host cores for a bounded sample of whole frames
 
@@ -71,7 +71,7 @@ def workload_config(w, tris):
         "light_map": f"{w.map_params.width}x{w.map_params.height} fp32, polygon offset (4, 20)",
         "camera": f"{w.camera.width}x{w.camera.height}",
         "technique": "PCSS, 16 Poisson blocker taps + 32 filter taps, light radius 0.25",
-        "step": "light map + G-buffer + visibility (one shadowed frame)",
+        "step": "gi_render_frame: light map + G-buffer + visibility (one shadowed frame)",
         "l2": "flushed (256 MiB write) before each timed step, outside the step's events",
         "scene_seed": "0x5EED0001",
     }
@@ -210,7 +210,7 @@ def run_reference(args):
 # GPU arm
 # ---------------------------------------------------------------------------
 def traffic_from_profiles():
-    path = os.path.join(ROOT, "profiles", "visibility_pcss_1080p.md")
+    path = os.path.join(ROOT, "profiles", "frame_visibility_pcss_1080p.md")
     if not os.path.exists(path):
         return None
     m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
@@ -308,23 +308,19 @@ def run_ours(args):
         total_ms = float(t.item())
     value = world * K / (total_ms / 1000.0)
 
-    # ---- per-pass breakdown (same frames, events between passes) -------------
+    # ---- phase breakdown (same frames, events recorded by the library) -------
     R = max(20, min(K, 100))
-    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(R)]
+    ctx.set_profiling(True)
+    phases = []
     for r in range(R):
         flush.fill_(float(r))
-        ev[r][0].record(stream)
-        gi.render_shadow_map(ctx, w.scene, w.map_params, fr.light_mvp, bufs.depth, stream)
-        ev[r][1].record(stream)
-        gi.render_gbuffer(ctx, w.scene, fr.camera_mvp, W, H, bufs.pos, bufs.nrm, stream)
-        ev[r][2].record(stream)
-        gi.compute_visibility(ctx, w.params, fr, bufs.depth, S, S, bufs.pos, bufs.nrm, bufs.vis, W, H, stream)
-        ev[r][3].record(stream)
-    torch.cuda.synchronize()
+        frame()
+        phases.append(ctx.phase_ms())
+    ctx.set_profiling(False)
     pass_ms = {
-        "shadow_map": statistics.mean(e[0].elapsed_time(e[1]) for e in ev),
-        "gbuffer": statistics.mean(e[1].elapsed_time(e[2]) for e in ev),
-        "visibility": statistics.mean(e[2].elapsed_time(e[3]) for e in ev),
+        "light_map": statistics.mean(p[0] for p in phases),
+        "visibility_keys": statistics.mean(p[1] for p in phases),
+        "resolve_and_visibility": statistics.mean(p[2] for p in phases),
     }
 
     # ---- end to end through the C ABI with host buffers ---------------------
@@ -365,8 +361,11 @@ def run_ours(args):
 
     if rank == 0:
         peak, peak_kind = measured_hbm_peak()
-        alg_bytes = 36 * P + 4 * S * S
-        vis_s = pass_ms["visibility"] / 1000.0
+        # k_frame_visibility: 8 B key read + 4 B visibility write per pixel,
+        # one read of the light map, and the scene's vertices / indices.
+        geom = pts.nbytes + nrm.nbytes + idx.nbytes
+        alg_bytes = 12 * P + 4 * S * S + geom
+        vis_s = pass_ms["resolve_and_visibility"] / 1000.0
         achieved = alg_bytes / vis_s / 1e9
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
@@ -376,10 +375,10 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),
-            "roofline": {"kernel": "k_visibility<PCSS_POISSON>", "bound": "hbm", "achieved": achieved,
-                         "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "peak_source": peak_kind, "traffic": traffic_from_profiles(),
-                         "algorithmic_bytes_per_launch": alg_bytes},
+            "roofline": {"kernel": "k_frame_visibility<PCSS_POISSON> (G-buffer resolve + visibility)",
+                         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic_from_profiles(),
+                         "algorithmic_bytes_per_launch": int(alg_bytes)},
             "pass_ms": pass_ms,
             "step_ms_median": statistics.median(step_ms),
             "wall_s_timed_region": wall,

@@ -9,12 +9,12 @@ from . import _capi
 from ._capi import GIError
 from .shadow import (Context, Frame, FrameBuffers, MapParams, Scene, ShadowParams, TECHNIQUES, ViewSpec,
                      allocate_frame, compute_hard_shadows, compute_visibility, frame_setup, poisson_table,
-                     render_frame, render_gbuffer, render_shadow_map, render_soft_shadows,
+                     render_frame, render_frame_passes, render_gbuffer, render_shadow_map, render_soft_shadows,
                      shadow_volume_counts)
 
 __all__ = [
     "Context", "Frame", "FrameBuffers", "GIError", "MapParams", "Scene", "ShadowParams", "TECHNIQUES",
     "ViewSpec", "allocate_frame", "compute_hard_shadows", "compute_visibility", "frame_setup",
-    "poisson_table", "render_frame", "render_gbuffer", "render_shadow_map", "render_soft_shadows",
+    "poisson_table", "render_frame", "render_frame_passes", "render_gbuffer", "render_shadow_map", "render_soft_shadows",
     "shadow_volume_counts", "_capi",
 ]

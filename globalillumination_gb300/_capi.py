@@ -140,6 +140,8 @@ _PROTOS = {
     "gi_context_create": (C.c_int, [C.c_int, C.POINTER(_VP)]),
     "gi_context_destroy": (None, [_VP]),
     "gi_context_launch_count": (C.c_uint64, [_VP]),
+    "gi_context_set_profiling": (C.c_int, [_VP, C.c_int]),
+    "gi_context_phase_ms": (C.c_int, [_VP, C.c_float * 3]),
     "gi_scene_load_config": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(_VP)]),
     "gi_scene_create": (C.c_int, [C.POINTER(_VP)]),
     "gi_scene_destroy": (None, [_VP]),
@@ -168,6 +170,8 @@ _PROTOS = {
     "gi_vis_params_default": (C.c_int, [C.c_int, C.POINTER(VisParams)]),
     "gi_visibility": (C.c_int, [_VP, C.POINTER(VisParams), _VP, C.c_int, C.c_int, _VP, _VP, _VP,
                                 C.c_int, C.c_int, _VP]),
+    "gi_render_frame": (C.c_int, [_VP, _VP, C.POINTER(MapParams), F16, F16, C.POINTER(VisParams), C.c_int,
+                                  C.c_int, _VP, _VP, _VP, _VP, _VP]),
     "gi_poisson_table": (C.c_int, [C.c_int, _VP]),
     "gi_shadow_volume_counts": (C.c_int, [_VP, _VP, F3, C.c_float, F16, C.c_int, C.c_int, C.c_int,
                                           _VP, _VP, _VP]),

@@ -101,13 +101,41 @@ extern "C" void gi_context_destroy(gi_context* c) {
     cudaFree(c->d_depth_tmp);
     cudaFree(c->d_counts);
     for (int i = 0; i < 8; ++i) cudaFree(c->bin_buf[i]);
-    for (int i = 0; i < 6; ++i) cudaFree(c->tier_buf[i]);
+    for (int i = 0; i < 8; ++i) cudaFree(c->tier_buf[i]);
+    for (int i = 0; i < 4; ++i)
+        if (c->phase_ev[i]) cudaEventDestroy(static_cast<cudaEvent_t>(c->phase_ev[i]));
     cudaFree(c->d_status);
     if (c->h_status) cudaFreeHost(c->h_status);
     delete c;
 }
 
 extern "C" uint64_t gi_context_launch_count(const gi_context* c) { return c ? c->launches : 0; }
+
+extern "C" gi_status gi_context_set_profiling(gi_context* c, int enable) {
+    if (!c) return fail(GI_ERR_INVALID_ARG, "gi_context_set_profiling: NULL context");
+    if (enable && !c->phase_ev[0]) {
+        gi_status st = check_device(c);
+        if (st != GI_OK) return st;
+        for (int i = 0; i < 4; ++i) {
+            cudaEvent_t ev;
+            cudaError_t e = cudaEventCreate(&ev);
+            if (e != cudaSuccess) return gi::fail_cuda(e, "cudaEventCreate");
+            c->phase_ev[i] = ev;
+        }
+    }
+    c->profiling = enable != 0;
+    return GI_OK;
+}
+
+extern "C" gi_status gi_context_phase_ms(gi_context* c, float ms[3]) {
+    if (!c || !ms) return fail(GI_ERR_INVALID_ARG, "gi_context_phase_ms: NULL argument");
+    if (!c->phase_ev[0]) return fail(GI_ERR_INVALID_ARG, "gi_context_phase_ms: profiling never enabled");
+    cudaError_t e = cudaEventSynchronize(static_cast<cudaEvent_t>(c->phase_ev[3]));
+    for (int i = 0; i < 3 && e == cudaSuccess; ++i)
+        e = cudaEventElapsedTime(&ms[i], static_cast<cudaEvent_t>(c->phase_ev[i]),
+                                 static_cast<cudaEvent_t>(c->phase_ev[i + 1]));
+    return e == cudaSuccess ? GI_OK : gi::fail_cuda(e, "gi_context_phase_ms");
+}
 
 extern "C" void gi_scene_destroy(gi_scene* s) {
     if (!s) return;
@@ -414,6 +442,40 @@ extern "C" gi_status gi_visibility(gi_context* ctx, const gi_vis_params* p, cons
     if (st != GI_OK) return st;
     return gi::launch_visibility(ctx, p, d_depth, map_w, map_h, d_pos, d_nrm, d_vis, W, H,
                                  static_cast<cudaStream_t>(stream));
+}
+
+extern "C" gi_status gi_render_frame(gi_context* ctx, const gi_scene* s, const gi_map_params* mp,
+                                     const float light_mvp[16], const float camera_mvp[16],
+                                     const gi_vis_params* vp, int W, int H, float* d_depth,
+                                     float* d_vis, float* d_pos, float* d_nrm, void* stream) {
+    gi_status st = check_pass(ctx, s);
+    if (st != GI_OK) return st;
+    if (!mp || !light_mvp || !camera_mvp || !vp || !d_depth || !d_vis || (!d_pos != !d_nrm))
+        return fail(GI_ERR_INVALID_ARG, "gi_render_frame: bad arguments");
+    st = check_image(mp->width, mp->height, "gi_render_frame (map)");
+    if (st == GI_OK) st = check_image(W, H, "gi_render_frame");
+    if (st == GI_OK) st = check_vis_params(vp);
+    if (st != GI_OK) return st;
+    if (mp->bias_mode < GI_BIAS_NONE || mp->bias_mode > GI_BIAS_POLYGON_OFFSET)
+        return fail(GI_ERR_INVALID_ARG, "gi_render_frame: bad bias_mode");
+    if ((size_t)s->dev_triangles >= ((size_t)1 << 29))
+        return fail(GI_ERR_CAPACITY, "gi_render_frame: more than 2^29 triangles");
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    auto mark = [&](int i) {
+        if (ctx->profiling) cudaEventRecord(static_cast<cudaEvent_t>(ctx->phase_ev[i]), cs);
+    };
+    mark(0);
+    st = gi::raster_depth_map(ctx, s, light_mvp, mp->width, mp->height, mp->bias_mode,
+                              mp->constant_bias, mp->offset_factor, mp->offset_units, d_depth,
+                              small_px_default(), cs);
+    mark(1);
+    if (st == GI_OK) st = gi::raster_gbuffer_keys(ctx, s, camera_mvp, W, H, cs);
+    mark(2);
+    if (st == GI_OK)
+        st = gi::launch_frame_visibility(ctx, vp, d_depth, mp->width, mp->height, s, camera_mvp, d_vis,
+                                         W, H, d_pos, d_nrm, cs);
+    mark(3);
+    return st;
 }
 
 extern "C" gi_status gi_poisson_table(int n, float* xy) {

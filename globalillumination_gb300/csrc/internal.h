@@ -80,14 +80,18 @@ struct gi_context {
     // bin work items
     void* bin_buf[8] = {};
     size_t bin_cap[8] = {};
-    // tiered rasteriser: records, tiny / warp / large lists, large bases, spill
-    void* tier_buf[6] = {};
-    size_t tier_cap[6] = {};
+    // tiered rasteriser: records, tiny / warp / large lists, large bases,
+    // spill, G-buffer triangle -> record map, per-record resolve data
+    void* tier_buf[8] = {};
+    size_t tier_cap[8] = {};
     // status words (64): [4..11] counters of the binned raster (records, big
     // records, spills, error bits, admitted big pairs as u64, work items),
     // [32..55] counters of the tiered raster
     unsigned int* d_status = nullptr;
     unsigned int* h_status = nullptr;  // pinned mirror
+    // phase timing (cudaEvent_t handles) for gi_render_frame
+    bool profiling = false;
+    void* phase_ev[4] = {};
 };
 
 namespace gi {

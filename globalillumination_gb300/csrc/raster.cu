@@ -388,73 +388,17 @@ __global__ void k_fill_u64(unsigned long long* p, size_t n, unsigned long long v
 __global__ void __launch_bounds__(128) k_gbuffer_resolve(const unsigned long long* keys,
                                                          const float* points, const float* normals,
                                                          const int* indices, Mat4 mvp, int W,
-                                                         int H, float4* pos, float4* nrm) {
+                                                         int H, float4* pos, float4* nrm,
+                                                         const unsigned* rec_of, const BRec* recs,
+                                                         const uint4* rres) {
     int x = blockIdx.x * 32 + (threadIdx.x & 31);
     int y = blockIdx.y * 4 + (threadIdx.x >> 5);
     if (x >= W || y >= H) return;
     size_t p = (size_t)y * W + x;
-    const unsigned long long clear = ((unsigned long long)__float_as_uint(1.0f) << 32) | 0xFFFFFFFFull;
-    unsigned long long k = __ldg(keys + p);
-    float4 bg = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
-    if (k == clear) {
-        pos[p] = bg;
-        nrm[p] = bg;
-        return;
-    }
-    unsigned prim = (unsigned)(k & 0xFFFFFFFFull);
-    int t = (int)(prim >> 3), sub = (int)(prim & 7);
-    const int* tri = indices + 3 * (size_t)t;
-    int ids[3] = {__ldg(tri), __ldg(tri + 1), __ldg(tri + 2)};
-    float c[3][4];
-    for (int j = 0; j < 3; ++j) {
-        float v[3];
-        load_vertex(points, ids[j], v);
-        transform(mvp, v[0], v[1], v[2], c[j]);
-    }
-    const float id[3][3] = {{1.0f, 0.0f, 0.0f}, {0.0f, 1.0f, 0.0f}, {0.0f, 0.0f, 1.0f}};
-    Setup s;
-    bool ok;
-    if (all_inside(c[0], c[1], c[2])) {
-        ok = sub == 0 && setup_triangle(c[0], c[1], c[2], id[0], id[1], id[2], W, H, s);
-    } else {
-        CV poly[9];
-        int n = clip_polygon(c[0], c[1], c[2], poly);
-        ok = (sub + 2 < n) && setup_triangle(poly[0].c, poly[sub + 1].c, poly[sub + 2].c, poly[0].b,
-                                             poly[sub + 1].b, poly[sub + 2].b, W, H, s);
-    }
-    if (!ok) {
-        pos[p] = bg;
-        nrm[p] = bg;
-        return;
-    }
-    Edges e;
-    make_edges(s, e);
-    int64_t px = (int64_t)x * kSub + kSub / 2, py = (int64_t)y * kSub + kSub / 2;
-    float q[3];
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-        float l = (float)edge_at(e, j, px, py) * s.inv_area;
-        q[j] = l * s.iw[j];
-    }
-    float sum = (q[0] + q[1]) + q[2];
-    float pc[3] = {q[0] / sum, q[1] / sum, q[2] / sum};
-    float B[3];
-#pragma unroll
-    for (int j = 0; j < 3; ++j) B[j] = (pc[0] * s.b[0][j] + pc[1] * s.b[1][j]) + pc[2] * s.b[2][j];
-    float P[3][3], N[3][3];
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-        load_vertex(points, ids[j], P[j]);
-        load_vertex(normals, ids[j], N[j]);
-    }
-    float o[3], on[3];
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-        o[j] = (B[0] * P[0][j] + B[1] * P[1][j]) + B[2] * P[2][j];
-        on[j] = (B[0] * N[0][j] + B[1] * N[1][j]) + B[2] * N[2][j];
-    }
-    pos[p] = make_float4(o[0], o[1], o[2], 1.0f);
-    nrm[p] = make_float4(on[0], on[1], on[2], s.front ? 1.0f : 0.0f);
+    float4 o, on;
+    resolve_pixel(__ldg(keys + p), points, normals, indices, mvp, W, H, x, y, rec_of, recs, rres, o, on);
+    pos[p] = o;
+    nrm[p] = on;
 }
 
 __global__ void k_wrap_stencil(const int* counts, unsigned char* out, size_t n) {
@@ -484,19 +428,8 @@ constexpr int kBinShift = 5;
 constexpr int kDirectBins = 4;
 constexpr unsigned kSeg = 256;        // records per bin work item
 constexpr unsigned kItemBinBits = 18; // work item = bin | segment << 18
-constexpr unsigned kFlagFront = 1u, kFlagBig = 2u;
+constexpr unsigned kFlagBig = 2u;
 
-struct __align__(16) BRec {
-    int X[3];
-    int Y[3];
-    float z0, dz1, dz2, inv_area;
-    float zoff;
-    unsigned prim;     // key / stencil primitive id
-    unsigned short x0, x1, y0, y1;
-    unsigned flags;
-    unsigned spill_id; // (primitive << 3) | sub-triangle
-};
-static_assert(sizeof(BRec) == 64, "BRec is four 16-byte words");
 
 struct BinArgs {
     RasterArgs r;
@@ -1074,6 +1007,8 @@ struct TierArgs {
     unsigned* spill;
     unsigned spill_cap;
     unsigned long long huge_px;  // bounding-box pixels that make a record huge
+    unsigned* rec_of;            // G-buffer: triangle -> record of its unclipped triangle (~0: none)
+    uint4* rres;                 // G-buffer: per record (1/w0, 1/w1, 1/w2 bits, swapped)
     unsigned* ctr;  // [0] records [1] tiny [2] coop [3] large [4] spills [5] error bits
                     // [6] huge count [8,9] tile total (u64) [16..23] huge record ids
 };
@@ -1087,7 +1022,7 @@ __device__ __forceinline__ void tier_spill(const TierArgs& a, unsigned id) {
 template <int MODE>
 __device__ void tier_sub(const TierArgs& a, const float* c0, const float* c1, const float* c2,
                          const float* b0, const float* b1, const float* b2, unsigned prim,
-                         unsigned sub) {
+                         unsigned sub, bool unclipped) {
     Setup s;
     if (!setup_triangle(c0, c1, c2, b0, b1, b2, a.r.W, a.r.H, s)) return;
     int64_t minX = min(s.X[0], min(s.X[1], s.X[2])), maxX = max(s.X[0], max(s.X[1], s.X[2]));
@@ -1127,6 +1062,11 @@ __device__ void tier_sub(const TierArgs& a, const float* c0, const float* c1, co
     r.flags = s.front ? kFlagFront : 0u;
     r.spill_id = spill_id;
     a.recs[slot] = r;
+    if (MODE == MODE_VKEY && a.rec_of) {
+        a.rres[slot] = make_uint4(__float_as_uint(s.iw[0]), __float_as_uint(s.iw[1]),
+                                  __float_as_uint(s.iw[2]), s.swapped ? 1u : 0u);
+        if (unclipped) a.rec_of[prim] = slot;
+    }
     const long long npx = (long long)(x1 - x0 + 1) * (y1 - y0 + 1);
     if (npx <= kTinyPx) a.tiny[atomicAdd(a.ctr + 1, 1u)] = slot;
     else if (npx <= kCoopPx) a.coop[atomicAdd(a.ctr + 2, 1u)] = slot;
@@ -1143,15 +1083,18 @@ __global__ void __launch_bounds__(128) k_tier_setup(TierArgs a) {
 #pragma unroll
     for (int j = 0; j < 3; ++j) transform(a.r.mvp, v[j][0], v[j][1], v[j][2], c[j]);
     const float id[3][3] = {{1.0f, 0.0f, 0.0f}, {0.0f, 1.0f, 0.0f}, {0.0f, 0.0f, 1.0f}};
+    // The G-buffer resolve reads an unclipped triangle's record through
+    // rec_of; every other triangle is marked and resolved from scratch.
+    if (MODE == MODE_VKEY && a.rec_of) a.rec_of[prim] = ~0u;
     if (all_inside(c[0], c[1], c[2])) {
-        tier_sub<MODE>(a, c[0], c[1], c[2], id[0], id[1], id[2], (unsigned)prim, 0u);
+        tier_sub<MODE>(a, c[0], c[1], c[2], id[0], id[1], id[2], (unsigned)prim, 0u, true);
         return;
     }
     CV poly[9];
     int n = clip_polygon(c[0], c[1], c[2], poly);
     for (int i = 1; i + 1 < n; ++i)
         tier_sub<MODE>(a, poly[0].c, poly[i].c, poly[i + 1].c, poly[0].b, poly[i].b, poly[i + 1].b,
-                       (unsigned)prim, (unsigned)(i - 1));
+                       (unsigned)prim, (unsigned)(i - 1), false);
 }
 
 constexpr unsigned kFlagHuge = 4u;
@@ -1618,10 +1561,14 @@ static gi_status run_binned(gi_context* ctx, dev::RasterArgs& r, int mode, cudaS
 static gi_status run_tiered(gi_context* ctx, dev::RasterArgs& r, int mode, cudaStream_t st) {
     const size_t prims = (size_t)std::max(r.num_prims, 0);
     const size_t rec_cap = 2 * prims + 4096;
-    const size_t need[6] = {rec_cap * sizeof(dev::BRec), rec_cap * sizeof(unsigned),
+    const bool keys = mode == dev::MODE_VKEY;
+    const size_t need[8] = {rec_cap * sizeof(dev::BRec), rec_cap * sizeof(unsigned),
                             rec_cap * sizeof(unsigned), rec_cap * sizeof(unsigned),
-                            rec_cap * sizeof(unsigned long long), rec_cap * sizeof(unsigned)};
-    for (int i = 0; i < 6; ++i) {
+                            rec_cap * sizeof(unsigned long long), rec_cap * sizeof(unsigned),
+                            keys ? std::max<size_t>(prims, 1) * sizeof(unsigned) : 0,
+                            keys ? rec_cap * sizeof(uint4) : 0};
+    for (int i = 0; i < 8; ++i) {
+        if (!need[i]) continue;
         gi_status s = ensure_buffer(&ctx->tier_buf[i], &ctx->tier_cap[i], need[i]);
         if (s != GI_OK) return s;
     }
@@ -1636,6 +1583,8 @@ static gi_status run_tiered(gi_context* ctx, dev::RasterArgs& r, int mode, cudaS
     a.spill = static_cast<unsigned*>(ctx->tier_buf[5]);
     a.spill_cap = (unsigned)rec_cap;
     a.huge_px = std::max<unsigned long long>(65536ull, (unsigned long long)r.W * r.H / 8);
+    a.rec_of = keys ? static_cast<unsigned*>(ctx->tier_buf[6]) : nullptr;
+    a.rres = keys ? static_cast<uint4*>(ctx->tier_buf[7]) : nullptr;
     a.ctr = ctx->d_status + 32;  // 24 words
     cudaError_t e = cudaMemsetAsync(a.ctr, 0, 24 * sizeof(unsigned), st);
     if (e != cudaSuccess) return fail_cuda(e, "tiered raster memset");
@@ -1703,13 +1652,32 @@ gi_status raster_gbuffer(gi_context* ctx, const gi_scene* scene, const float mvp
     s = run_tiered(ctx, a, dev::MODE_VKEY, st);
     if (s != GI_OK) return s;
     dim3 grid((W + 31) / 32, (H + 3) / 4);
-    dev::k_gbuffer_resolve<<<grid, 128, 0, st>>>(ctx->d_vkeys, scene->d_points, scene->d_normals,
-                                                 scene->d_indices, a.mvp, W, H,
-                                                 reinterpret_cast<float4*>(d_pos),
-                                                 reinterpret_cast<float4*>(d_nrm));
+    dev::k_gbuffer_resolve<<<grid, 128, 0, st>>>(
+        ctx->d_vkeys, scene->d_points, scene->d_normals, scene->d_indices, a.mvp, W, H,
+        reinterpret_cast<float4*>(d_pos), reinterpret_cast<float4*>(d_nrm),
+        static_cast<const unsigned*>(ctx->tier_buf[6]), static_cast<const dev::BRec*>(ctx->tier_buf[0]),
+        static_cast<const uint4*>(ctx->tier_buf[7]));
     ctx->launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "gbuffer resolve launch");
+}
+
+gi_status raster_gbuffer_keys(gi_context* ctx, const gi_scene* scene, const float mvp[16], int W,
+                              int H, cudaStream_t st) {
+    const size_t npx = (size_t)W * H;
+    gi_status s = ensure_buffer(reinterpret_cast<void**>(&ctx->d_vkeys), &ctx->cap_vkeys,
+                                npx * sizeof(unsigned long long));
+    if (s != GI_OK) return s;
+    dev::RasterArgs a = {};
+    a.points = scene->d_points;
+    a.normals = scene->d_normals;
+    a.indices = scene->d_indices;
+    a.num_prims = scene->dev_triangles;
+    a.mvp = mat_of(mvp);
+    a.W = W;
+    a.H = H;
+    a.keys = ctx->d_vkeys;
+    return run_tiered(ctx, a, dev::MODE_VKEY, st);
 }
 
 gi_status raster_shadow_volumes(gi_context* ctx, const gi_scene* scene, const float L[3],
@@ -1862,7 +1830,7 @@ extern "C" gi_status gi_gbuffer_noalloc(const float* d_points, const float* d_no
     dim3 grid((width + 31) / 32, (height + 3) / 4);
     dev::k_gbuffer_resolve<<<grid, 128, 0, cs>>>(keys, d_points, d_normals, d_indices, a.mvp, width,
                                                  height, reinterpret_cast<float4*>(d_pos),
-                                                 reinterpret_cast<float4*>(d_nrm));
+                                                 reinterpret_cast<float4*>(d_nrm), nullptr, nullptr, nullptr);
     e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_gbuffer_noalloc: kernel launch");
 }

@@ -21,6 +21,17 @@ gi_status raster_shadow_volumes(gi_context* ctx, const gi_scene* scene, const fl
                                 unsigned char* d_stencil, float* d_depth_out, int small_px,
                                 cudaStream_t st);
 
+// G-buffer visibility keys only (into ctx->d_vkeys), no resolve.
+gi_status raster_gbuffer_keys(gi_context* ctx, const gi_scene* scene, const float mvp[16], int W,
+                              int H, cudaStream_t st);
+
+// Resolve + visibility in one kernel from ctx->d_vkeys; d_pos / d_nrm may
+// be NULL (no G-buffer output).
+gi_status launch_frame_visibility(gi_context* ctx, const gi_vis_params* p, const float* d_depth,
+                                  int map_w, int map_h, const gi_scene* scene, const float camera_mvp[16],
+                                  float* d_vis, int W, int H, float* d_pos, float* d_nrm,
+                                  cudaStream_t st);
+
 gi_status launch_visibility(gi_context* ctx, const gi_vis_params* p, const float* d_depth,
                             int map_w, int map_h, const float* d_pos, const float* d_nrm,
                             float* d_vis, int W, int H, cudaStream_t st);

@@ -66,7 +66,7 @@ __device__ __forceinline__ CV intersect(const CV& in, const CV& out, float din, 
 
 // Sutherland-Hodgman against the planes some vertex violates, in the fixed
 // plane order; returns the polygon size (0 = culled).
-__device__ __noinline__ int clip_polygon(const float c0[4], const float c1[4], const float c2[4],
+static __device__ __noinline__ int clip_polygon(const float c0[4], const float c1[4], const float c2[4],
                                          CV poly[9]) {
     CV a[9], b[9];
 #pragma unroll
@@ -121,6 +121,7 @@ struct Setup {
     int64_t area;
     float inv_area;
     bool front;
+    bool swapped;  // vertices 1 and 2 exchanged to make the triangle CCW
 };
 
 // Window transform, snapping and orientation of one (sub-)triangle whose
@@ -150,6 +151,7 @@ __device__ __forceinline__ bool setup_triangle(const float* c0, const float* c1,
     int64_t area = (s.X[1] - s.X[0]) * (s.Y[2] - s.Y[0]) - (s.X[2] - s.X[0]) * (s.Y[1] - s.Y[0]);
     if (area == 0) return false;
     s.front = area > 0;
+    s.swapped = area < 0;
     if (area < 0) {
         int64_t t;
         t = s.X[1]; s.X[1] = s.X[2]; s.X[2] = t;
@@ -242,6 +244,174 @@ __device__ __forceinline__ float clamp01(float z) {
 __device__ __forceinline__ int64_t floor_div256(int64_t a) {
     // floor(a / 256) for signed a (arithmetic shift rounds toward -inf)
     return a >> 8;
+}
+
+
+// Set-up record of one (sub-)triangle, 64 bytes: snapped CCW window
+// vertices, window depth plane (z0 + l1 dz1 + l2 dz2 with l = E / area),
+// bias, key / stencil primitive id, pixel bounding box, flags.
+constexpr unsigned kFlagFront = 1u;
+struct __align__(16) BRec {
+    int X[3];
+    int Y[3];
+    float z0, dz1, dz2, inv_area;
+    float zoff;
+    unsigned prim;     // key / stencil primitive id
+    unsigned short x0, x1, y0, y1;
+    unsigned flags;
+    unsigned spill_id; // (primitive << 3) | sub-triangle
+};
+static_assert(sizeof(BRec) == 64, "BRec is four 16-byte words");
+
+__device__ __forceinline__ void ldg3(const float* p, int idx, float out[3]) {
+    out[0] = __ldg(p + 3 * (size_t)idx + 0);
+    out[1] = __ldg(p + 3 * (size_t)idx + 1);
+    out[2] = __ldg(p + 3 * (size_t)idx + 2);
+}
+
+// Resolve from a stored record of an unclipped triangle: X / Y are the
+// snapped (CCW-ordered) window vertices, inv_area = 1 / area, iw = 1 / clip w
+// of the CCW-ordered vertices, swapped = vertices 1 and 2 were exchanged.
+// Performs the same operations as resolve_key's interpolation.
+__device__ __forceinline__ void resolve_record(const int X[3], const int Y[3], float inv_area,
+                                               const float iw[3], bool swapped, bool front, int t,
+                                               const float* points, const float* normals,
+                                               const int* indices, int x, int y, float4& pos,
+                                               float4& nrm) {
+    const int64_t px = (int64_t)x * kSub + kSub / 2, py = (int64_t)y * kSub + kSub / 2;
+    float q[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        const int a = (j + 1) % 3, b = (j + 2) % 3;
+        const int64_t e = ((int64_t)X[b] - X[a]) * (py - Y[a]) - ((int64_t)Y[b] - Y[a]) * (px - X[a]);
+        const float l = (float)e * inv_area;
+        q[j] = l * iw[j];
+    }
+    const float sum = (q[0] + q[1]) + q[2];
+    const float pc[3] = {q[0] / sum, q[1] / sum, q[2] / sum};
+    // identity source rows (exchanged for a swapped triangle): B = pc permuted
+    const float B[3] = {pc[0], swapped ? pc[2] : pc[1], swapped ? pc[1] : pc[2]};
+    const int* tri = indices + 3 * (size_t)t;
+    const int ids[3] = {__ldg(tri), __ldg(tri + 1), __ldg(tri + 2)};
+    float P[3][3], N[3][3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        ldg3(points, ids[j], P[j]);
+        ldg3(normals, ids[j], N[j]);
+    }
+    float o[3], on[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        o[j] = (B[0] * P[0][j] + B[1] * P[1][j]) + B[2] * P[2][j];
+        on[j] = (B[0] * N[0][j] + B[1] * N[1][j]) + B[2] * N[2][j];
+    }
+    pos = make_float4(o[0], o[1], o[2], 1.0f);
+    nrm = make_float4(on[0], on[1], on[2], front ? 1.0f : 0.0f);
+}
+
+// The G-buffer texel of pixel (x, y) from its 64-bit visibility key
+// (depth bits << 32 | triangle * 8 + sub-triangle): the winning
+// sub-triangle is re-derived (transform, clip, set up) and the object
+// position and vertex normal are interpolated perspective-correctly
+// (GBuffer.frag:32-38: (position, 1), (normal, gl_FrontFacing)).
+// Background keys give (0, 0, 0, 1) for both, the G-buffer's clear colour.
+// Returns false for background.
+__device__ __forceinline__ bool resolve_key(unsigned long long k, const float* points,
+                                            const float* normals, const int* indices,
+                                            const Mat4& mvp, int W, int H, int x, int y,
+                                            float4& pos, float4& nrm) {
+    const unsigned long long clear = ((unsigned long long)__float_as_uint(1.0f) << 32) | 0xFFFFFFFFull;
+    const float4 bg = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+    if (k == clear) {
+        pos = bg;
+        nrm = bg;
+        return false;
+    }
+    const unsigned prim = (unsigned)(k & 0xFFFFFFFFull);
+    const int t = (int)(prim >> 3), sub = (int)(prim & 7);
+    const int* tri = indices + 3 * (size_t)t;
+    const int ids[3] = {__ldg(tri), __ldg(tri + 1), __ldg(tri + 2)};
+    float P[3][3];
+    float c[3][4];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        ldg3(points, ids[j], P[j]);
+        transform(mvp, P[j][0], P[j][1], P[j][2], c[j]);
+    }
+    const float id[3][3] = {{1.0f, 0.0f, 0.0f}, {0.0f, 1.0f, 0.0f}, {0.0f, 0.0f, 1.0f}};
+    Setup s;
+    bool ok;
+    if (all_inside(c[0], c[1], c[2])) {
+        ok = sub == 0 && setup_triangle(c[0], c[1], c[2], id[0], id[1], id[2], W, H, s);
+    } else {
+        CV poly[9];
+        const int n = clip_polygon(c[0], c[1], c[2], poly);
+        ok = (sub + 2 < n) && setup_triangle(poly[0].c, poly[sub + 1].c, poly[sub + 2].c, poly[0].b,
+                                             poly[sub + 1].b, poly[sub + 2].b, W, H, s);
+    }
+    if (!ok) {
+        pos = bg;
+        nrm = bg;
+        return false;
+    }
+    Edges e;
+    make_edges(s, e);
+    const int64_t px = (int64_t)x * kSub + kSub / 2, py = (int64_t)y * kSub + kSub / 2;
+    float q[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        const float l = (float)edge_at(e, j, px, py) * s.inv_area;
+        q[j] = l * s.iw[j];
+    }
+    const float sum = (q[0] + q[1]) + q[2];
+    const float pc[3] = {q[0] / sum, q[1] / sum, q[2] / sum};
+    float B[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) B[j] = (pc[0] * s.b[0][j] + pc[1] * s.b[1][j]) + pc[2] * s.b[2][j];
+    float N[3][3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) ldg3(normals, ids[j], N[j]);
+    float o[3], on[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        o[j] = (B[0] * P[0][j] + B[1] * P[1][j]) + B[2] * P[2][j];
+        on[j] = (B[0] * N[0][j] + B[1] * N[1][j]) + B[2] * N[2][j];
+    }
+    pos = make_float4(o[0], o[1], o[2], 1.0f);
+    nrm = make_float4(on[0], on[1], on[2], s.front ? 1.0f : 0.0f);
+    return true;
+}
+
+// resolve_key with a shortcut: when the key names the unclipped triangle t
+// and rec_of[t] holds its record (written by the light-map / G-buffer
+// set-up), the interpolation starts from the stored set-up instead of
+// re-deriving it.  Same values either way.
+__device__ __forceinline__ bool resolve_pixel(unsigned long long k, const float* points,
+                                              const float* normals, const int* indices,
+                                              const Mat4& mvp, int W, int H, int x, int y,
+                                              const unsigned* rec_of, const BRec* recs,
+                                              const uint4* rres, float4& pos, float4& nrm) {
+    const unsigned long long clear = ((unsigned long long)__float_as_uint(1.0f) << 32) | 0xFFFFFFFFull;
+    if (k != clear && rec_of) {
+        const unsigned prim = (unsigned)(k & 0xFFFFFFFFull);
+        const int t = (int)(prim >> 3);
+        if ((prim & 7) == 0) {
+            const unsigned ri = __ldg(rec_of + t);
+            if (ri != ~0u) {
+                const uint4* rp = reinterpret_cast<const uint4*>(recs + ri);
+                const uint4 q0 = __ldg(rp), q1 = __ldg(rp + 1), q2 = __ldg(rp + 2), q3 = __ldg(rp + 3);
+                const int X[3] = {(int)q0.x, (int)q0.y, (int)q0.z};
+                const int Y[3] = {(int)q0.w, (int)q1.x, (int)q1.y};
+                const float inv_area = __uint_as_float(q2.y);
+                const uint4 rr = __ldg(rres + ri);
+                const float iw[3] = {__uint_as_float(rr.x), __uint_as_float(rr.y), __uint_as_float(rr.z)};
+                resolve_record(X, Y, inv_area, iw, rr.w != 0u, (q3.z & kFlagFront) != 0, t, points, normals,
+                               indices, x, y, pos, nrm);
+                return true;
+            }
+        }
+    }
+    return resolve_key(k, points, normals, indices, mvp, W, H, x, y, pos, nrm);
 }
 
 }  // namespace dev

@@ -29,6 +29,7 @@
 
 #include "internal.h"
 #include "raster.h"
+#include "raster_common.cuh"
 
 namespace gi {
 
@@ -589,7 +590,8 @@ __device__ __forceinline__ float shade(const gi_vis_params& p, const Ctx& c, V4 
 template <int TECH>
 __global__ void __launch_bounds__(128) k_visibility(const gi_vis_params p,
                                                     const float* __restrict__ map, int map_w,
-                                                    int map_h, const float4* __restrict__ pos,
+                                                    int map_h, float sx, float sy,
+                                                    const float4* __restrict__ pos,
                                                     const float4* __restrict__ nrm,
                                                     float* __restrict__ out, int W, int H) {
     int x = blockIdx.x * 32 + (threadIdx.x & 31);
@@ -601,12 +603,48 @@ __global__ void __launch_bounds__(128) k_visibility(const gi_vis_params p,
     c.H = map_h;
     c.fW = (float)map_w;
     c.fH = (float)map_h;
-    c.sx = (float)(1.0 / (double)map_w);
-    c.sy = (float)(1.0 / (double)map_h);
+    c.sx = sx;
+    c.sy = sy;
     c.I = p.shadow_intensity;
     size_t i = (size_t)y * W + x;
     float4 pv = __ldcs(pos + i);
     float4 nv = __ldcs(nrm + i);
+    V4 vertex = {pv.x, pv.y, pv.z, pv.w};
+    V4 normal = {nv.x, nv.y, nv.z, nv.w};
+    __stcs(out + i, shade<TECH>(p, c, vertex, normal));
+}
+
+// Fused G-buffer resolve and visibility: the G-buffer texel of each pixel
+// is interpolated from the visibility key in registers and shaded at once,
+// so the frame never writes / reads the 32-byte-per-pixel G-buffer (it is
+// stored only when the caller asks for it).  Same values as
+// k_gbuffer_resolve followed by k_visibility.
+template <int TECH>
+__global__ void __launch_bounds__(128) k_frame_visibility(
+    const gi_vis_params p, const float* __restrict__ map, int map_w, int map_h, float sx, float sy,
+    const unsigned long long* __restrict__ keys, const float* __restrict__ points,
+    const float* __restrict__ normals, const int* __restrict__ indices, const dev::Mat4 mvp,
+    const unsigned* __restrict__ rec_of, const dev::BRec* __restrict__ recs, const uint4* __restrict__ rres,
+    float* __restrict__ out, int W, int H, float4* __restrict__ pos_out, float4* __restrict__ nrm_out) {
+    int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    int y = blockIdx.y * 4 + (threadIdx.x >> 5);
+    if (x >= W || y >= H) return;
+    Ctx c;
+    c.map = map;
+    c.W = map_w;
+    c.H = map_h;
+    c.fW = (float)map_w;
+    c.fH = (float)map_h;
+    c.sx = sx;
+    c.sy = sy;
+    c.I = p.shadow_intensity;
+    const size_t i = (size_t)y * W + x;
+    float4 pv, nv;
+    dev::resolve_pixel(__ldcs(keys + i), points, normals, indices, mvp, W, H, x, y, rec_of, recs, rres, pv, nv);
+    if (pos_out) {
+        pos_out[i] = pv;
+        nrm_out[i] = nv;
+    }
     V4 vertex = {pv.x, pv.y, pv.z, pv.w};
     V4 normal = {nv.x, nv.y, nv.z, nv.w};
     __stcs(out + i, shade<TECH>(p, c, vertex, normal));
@@ -618,11 +656,14 @@ gi_status launch_visibility(gi_context* ctx, const gi_vis_params* p, const float
                             int map_w, int map_h, const float* d_pos, const float* d_nrm,
                             float* d_vis, int W, int H, cudaStream_t st) {
     dim3 grid((W + 31) / 32, (H + 3) / 4);
+    // shadowMapStep = (1.0 / w, 1.0 / h) in double, stored as float
+    // (glUniform2f at MyGLGeometryViewer.cpp:237-238)
+    const float sx = (float)(1.0 / (double)map_w), sy = (float)(1.0 / (double)map_h);
     const float4* pos = reinterpret_cast<const float4*>(d_pos);
     const float4* nrm = reinterpret_cast<const float4*>(d_nrm);
 #define GI_VIS_CASE(T)                                                                     \
     case T:                                                                                \
-        vis::k_visibility<T><<<grid, 128, 0, st>>>(*p, d_depth, map_w, map_h, pos, nrm, d_vis, W, H); \
+        vis::k_visibility<T><<<grid, 128, 0, st>>>(*p, d_depth, map_w, map_h, sx, sy, pos, nrm, d_vis, W, H); \
         break;
     switch (p->technique) {
         GI_VIS_CASE(GI_TECH_HARD)
@@ -643,6 +684,47 @@ gi_status launch_visibility(gi_context* ctx, const gi_vis_params* p, const float
     ctx->launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "visibility kernel launch");
+}
+
+gi_status launch_frame_visibility(gi_context* ctx, const gi_vis_params* p, const float* d_depth,
+                                  int map_w, int map_h, const gi_scene* scene, const float camera_mvp[16],
+                                  float* d_vis, int W, int H, float* d_pos, float* d_nrm,
+                                  cudaStream_t st) {
+    dim3 grid((W + 31) / 32, (H + 3) / 4);
+    const float sx = (float)(1.0 / (double)map_w), sy = (float)(1.0 / (double)map_h);
+    const unsigned* rec_of = static_cast<const unsigned*>(ctx->tier_buf[6]);
+    const dev::BRec* recs = static_cast<const dev::BRec*>(ctx->tier_buf[0]);
+    const uint4* rres = static_cast<const uint4*>(ctx->tier_buf[7]);
+    dev::Mat4 m;
+    for (int k = 0; k < 16; ++k) m.m[k] = camera_mvp[k];
+    float4* po = reinterpret_cast<float4*>(d_pos);
+    float4* no = reinterpret_cast<float4*>(d_nrm);
+#define GI_FRAME_CASE(T)                                                                          \
+    case T:                                                                                       \
+        vis::k_frame_visibility<T><<<grid, 128, 0, st>>>(*p, d_depth, map_w, map_h, sx, sy,         \
+                                                          ctx->d_vkeys, scene->d_points,          \
+                                                          scene->d_normals, scene->d_indices, m,  \
+                                                          rec_of, recs, rres, d_vis, W, H, po, no); \
+        break;
+    switch (p->technique) {
+        GI_FRAME_CASE(GI_TECH_HARD)
+        GI_FRAME_CASE(GI_TECH_PCF)
+        GI_FRAME_CASE(GI_TECH_PCF_TRICUBIC)
+        GI_FRAME_CASE(GI_TECH_PCSS_GRID)
+        GI_FRAME_CASE(GI_TECH_PCSS_POISSON)
+        GI_FRAME_CASE(GI_TECH_SMSR_CONSERVATIVE)
+        GI_FRAME_CASE(GI_TECH_SMSR_NONCONSERVATIVE)
+        GI_FRAME_CASE(GI_TECH_RPCF_CONSERVATIVE)
+        GI_FRAME_CASE(GI_TECH_RPCF_SMSR)
+        GI_FRAME_CASE(GI_TECH_RSMSS)
+        GI_FRAME_CASE(GI_TECH_HARD_SOFTAPP)
+        default:
+            return fail(GI_ERR_INVALID_ARG, "gi_render_frame: unknown technique");
+    }
+#undef GI_FRAME_CASE
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "frame visibility kernel launch");
 }
 
 }  // namespace gi

@@ -68,6 +68,15 @@ class Context:
     def launch_count(self) -> int:
         return int(_lib().gi_context_launch_count(self.handle))
 
+    def set_profiling(self, enable: bool) -> None:
+        check(_lib().gi_context_set_profiling(self.handle, int(bool(enable))), "gi_context_set_profiling")
+
+    def phase_ms(self):
+        """(light map, visibility keys, resolve + visibility) of the last render_frame, in ms."""
+        out = (C.c_float * 3)()
+        check(_lib().gi_context_phase_ms(self.handle, out), "gi_context_phase_ms")
+        return tuple(float(v) for v in out)
+
     def close(self) -> None:
         if self.handle:
             _lib().gi_context_destroy(self.handle)
@@ -382,8 +391,25 @@ def allocate_frame(map_w: int, map_h: int, width: int, height: int, device: int 
 
 
 def render_frame(ctx: Context, scene: Scene, frame: Frame, mp: MapParams, params: ShadowParams, width: int,
-                 height: int, bufs: FrameBuffers, stream=None):
-    """One shadowed frame: light map, G-buffer, visibility (display() up to shading)."""
+                 height: int, bufs: FrameBuffers, stream=None, store_gbuffer: bool = False):
+    """One shadowed frame (display() up to the visibility target) through gi_render_frame.
+
+    The G-buffer is resolved and shaded in one kernel; it is written to
+    bufs.pos / bufs.nrm only when store_gbuffer is true.
+    """
+    c = mp.to_c()
+    p = params.to_c(frame)
+    pos = _ptr(bufs.pos) if store_gbuffer else None
+    nrm = _ptr(bufs.nrm) if store_gbuffer else None
+    check(_lib().gi_render_frame(ctx.handle, scene.handle, C.byref(c), _f16(frame.light_mvp), _f16(frame.camera_mvp),
+                                 C.byref(p), width, height, _ptr(bufs.depth), _ptr(bufs.vis), pos, nrm,
+                                 _stream_ptr(stream)), "gi_render_frame")
+    return bufs.vis
+
+
+def render_frame_passes(ctx: Context, scene: Scene, frame: Frame, mp: MapParams, params: ShadowParams,
+                        width: int, height: int, bufs: FrameBuffers, stream=None):
+    """The same frame as three separate passes (light map, G-buffer, visibility)."""
     render_shadow_map(ctx, scene, mp, frame.light_mvp, bufs.depth, stream)
     render_gbuffer(ctx, scene, frame.camera_mvp, width, height, bufs.pos, bufs.nrm, stream)
     compute_visibility(ctx, params, frame, bufs.depth, mp.width, mp.height, bufs.pos, bufs.nrm, bufs.vis,

@@ -67,6 +67,12 @@ gi_status gi_context_create(int device, gi_context** out);
 void gi_context_destroy(gi_context* ctx);
 /* Number of kernel launches issued through this context since creation. */
 uint64_t gi_context_launch_count(const gi_context* ctx);
+/* Phase timing for benchmarks: while enabled, gi_render_frame records CUDA
+ * events on its stream around its three phases (light map, visibility keys,
+ * resolve + visibility); gi_context_phase_ms waits for the last call's
+ * events and returns the three durations in milliseconds. */
+gi_status gi_context_set_profiling(gi_context* ctx, int enable);
+gi_status gi_context_phase_ms(gi_context* ctx, float ms[3]);
 
 /* ------------------------------------------------------------------ */
 /* Scene (host geometry + optional device copy)                        */
@@ -317,6 +323,20 @@ gi_status gi_visibility(gi_context* ctx, const gi_vis_params* params,
                         const float* d_depth, int map_width, int map_height,
                         const float* d_pos, const float* d_nrm,
                         float* d_vis, int width, int height, void* stream);
+
+/* One shadowed frame: display() of the reference up to the visibility
+ * target (ShadowMapping/src/main.cpp:459-472 renderShadowMap, renderGBuffer,
+ * computeHardShadows; SoftShadowMapping/src/main.cpp:925-1017
+ * renderSoftShadows).  Renders the light map into d_depth, then the camera
+ * visibility keys, then resolves the G-buffer and shades in one kernel, so
+ * the G-buffer is never stored unless d_pos / d_nrm are given (float4
+ * [width*height] each, may be NULL).  Results equal gi_shadow_map +
+ * gi_gbuffer + gi_visibility. */
+gi_status gi_render_frame(gi_context* ctx, const gi_scene* scene,
+                          const gi_map_params* map, const float light_mvp[16],
+                          const float camera_mvp[16], const gi_vis_params* vis,
+                          int width, int height, float* d_depth, float* d_vis,
+                          float* d_pos, float* d_nrm, void* stream);
 
 /* Poisson-disk sample table used by GI_TECH_PCSS_POISSON (n <= 64 points in
  * the unit disk, interleaved x,y).  Shared with the CPU oracle. */

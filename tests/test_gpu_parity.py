@@ -180,6 +180,33 @@ def test_shadow_volume_counts_bit_exact(cuda_ctx, depth_func, dims):
     assert (st_ref != 0).sum() > 0 and (st_ref == 0).sum() > 0
 
 
+@pytest.mark.parametrize("tech", [api.GI_TECH_PCF, api.GI_TECH_PCSS_POISSON, api.GI_TECH_SMSR_NONCONSERVATIVE,
+                                  api.GI_TECH_RSMSS])
+@pytest.mark.parametrize("store", [False, True])
+def test_fused_frame_equals_passes(cuda_ctx, tech, store):
+    """gi_render_frame (resolve + visibility in one kernel) == the three passes."""
+    torch = _torch()
+    w = _small_c2(W=333, H=190, S=512)
+    W, H, S = w.camera.width, w.camera.height, w.map_params.width
+    params = _vis_params(w, tech)
+    fr = gi.frame_setup(w.light, w.camera)
+    w.scene.upload(cuda_ctx)
+    a = gi.allocate_frame(S, S, W, H)
+    b = gi.allocate_frame(S, S, W, H)
+    gi.render_frame_passes(cuda_ctx, w.scene, fr, w.map_params, params, W, H, a)
+    b.pos.fill_(-3.0)
+    b.nrm.fill_(-3.0)
+    gi.render_frame(cuda_ctx, w.scene, fr, w.map_params, params, W, H, b, store_gbuffer=store)
+    torch.cuda.synchronize()
+    assert torch.equal(a.depth.view(torch.int32), b.depth.view(torch.int32))
+    assert torch.equal(a.vis.view(torch.int32), b.vis.view(torch.int32))
+    if store:
+        assert torch.equal(a.pos.view(torch.int32), b.pos.view(torch.int32))
+        assert torch.equal(a.nrm.view(torch.int32), b.nrm.view(torch.int32))
+    else:
+        assert bool((b.pos == -3.0).all())
+
+
 def test_empty_scene(cuda_ctx):
     torch = _torch()
     s = gi.Scene()
@@ -188,7 +215,8 @@ def test_empty_scene(cuda_ctx):
     cam = gi.ViewSpec(eye=(0, 5, -5), at=(0, 0, 0), width=48, height=32)
     fr = gi.frame_setup(light, cam)
     bufs = gi.allocate_frame(64, 64, 48, 32)
-    gi.render_frame(cuda_ctx, s, fr, gi.MapParams(64, 64), gi.ShadowParams.defaults(api.GI_TECH_PCF), 48, 32, bufs)
+    gi.render_frame(cuda_ctx, s, fr, gi.MapParams(64, 64), gi.ShadowParams.defaults(api.GI_TECH_PCF), 48, 32, bufs,
+                    store_gbuffer=True)
     torch.cuda.synchronize()
     assert (bufs.depth.cpu().numpy() == 1.0).all()
     assert (bufs.vis.cpu().numpy() == 0.0).all()
