@@ -52,6 +52,8 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 256-scene batched leg")
+    ap.add_argument("--batched-scenes", type=int, default=256)
     ap.add_argument("--profile", action="store_true",
                     help="render --warmup frames and exit (the command profiled with ncu)")
     return ap.parse_args()
@@ -226,6 +228,72 @@ def measured_hbm_peak():
         return 6800.0, "fallback"
 
 
+def run_batched(args, ctx, stream, local):
+    """The batched workload (256 seeded scenes, 1-8 lights each, 1280 x 720,
+    5 x 5 PCF) replayed as one CUDA graph after autotuning; also the same
+    light-frames through gi_render_frame one at a time for comparison."""
+    import torch
+
+    import globalillumination_gb300 as gi
+    from globalillumination_gb300 import scenes
+
+    t0 = time.perf_counter()
+    frames = scenes.batched_720p(scenes=args.batched_scenes)
+    for f in frames:
+        f.scene.upload(ctx, stream)
+    outs = [torch.empty((len(f.lights), f.camera.height, f.camera.width), device="cuda") for f in frames]
+    b = gi.Batch(local)
+    for f, o in zip(frames, outs):
+        b.add_frame(f.scene, f.camera, f.lights, f.maps, f.params, o)
+    tune = b.autotune(stream, repeats=2)
+    setup_s = time.perf_counter() - t0
+    light_frames = sum(len(f.lights) for f in frames)
+    for _ in range(3):
+        b.run(stream)
+    torch.cuda.synchronize()
+    R = 5
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(R):
+        b.run(stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batch_ms = e0.elapsed_time(e1) / R
+    # the same light-frames, one gi_render_frame call each, on one stream
+    S_max = max(m.width for f in frames for m in f.maps)
+    bufs = gi.allocate_frame(S_max, S_max, frames[0].camera.width, frames[0].camera.height, local)
+    mats = [[gi.frame_setup(l, f.camera) for l in f.lights] for f in frames]
+
+    def singles():
+        for f, fm in zip(frames, mats):
+            for l, fr in enumerate(fm):
+                gi.render_frame(ctx, f.scene, fr, f.maps[l], f.params, f.camera.width, f.camera.height, bufs, stream)
+
+    singles()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    singles()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    single_ms = e0.elapsed_time(e1)
+    info = b.info()
+    b.close()
+    del outs
+    return {
+        "workload": "batched_720p", "scenes": len(frames), "light_frames": light_frames,
+        "triangles": int(sum(f.triangles for f in frames)),
+        "light_frames_per_s": light_frames / (batch_ms / 1000.0),
+        "scenes_per_s": len(frames) / (batch_ms / 1000.0),
+        "ms_per_batch": batch_ms, "replays_timed": R,
+        "tuning": {k: tune[k] for k in ("tiny_px", "coop_px", "streams")},
+        "kernel_launches_per_batch": info["kernel_launches"],
+        "single_frame_calls_light_frames_per_s": light_frames / (single_ms / 1000.0),
+        "setup_and_autotune_s": setup_s,
+        "l2": "working set (4+ GB of outputs, up to 64 MiB maps) larger than L2",
+    }
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -355,6 +423,10 @@ def run_ours(args):
     d2h = P * 4
     clk = clocks.stop()
 
+    batched = None
+    if not args.no_batched:
+        batched = run_batched(args, ctx, stream, local)
+
     # sanity: the frame produced soft shadows
     vis_host = bufs.vis.cpu().numpy()
     frac_soft = float(((vis_host > 0.25) & (vis_host < 1.0)).mean())
@@ -385,6 +457,8 @@ def run_ours(args):
             "clocks": clk,
             "soft_pixel_fraction": frac_soft,
         }
+        if batched is not None:
+            line["batched"] = batched
         if clk and any(r in clk["reasons"] for r in THROTTLE_BAD):
             line["clocks_warning"] = "throttled during the timed region"
         if world == 1 and not args.no_cpu_baseline:

@@ -132,6 +132,17 @@ class VisParams(C.Structure):
     ]
 
 
+class BatchTuning(C.Structure):
+    _fields_ = [
+        ("tiny_px", C.c_int),
+        ("coop_px", C.c_int),
+        ("streams", C.c_int),
+        ("frames", C.c_int),
+        ("kernel_launches", C.c_uint64),
+        ("best_ms", C.c_float),
+    ]
+
+
 # Every function the header declares, with its ctypes prototype.
 _VP = C.c_void_p
 _PROTOS = {
@@ -175,6 +186,14 @@ _PROTOS = {
     "gi_poisson_table": (C.c_int, [C.c_int, _VP]),
     "gi_shadow_volume_counts": (C.c_int, [_VP, _VP, F3, C.c_float, F16, C.c_int, C.c_int, C.c_int,
                                           _VP, _VP, _VP]),
+    "gi_batch_create": (C.c_int, [C.c_int, C.POINTER(_VP)]),
+    "gi_batch_destroy": (None, [_VP]),
+    "gi_batch_add_frame": (C.c_int, [_VP, _VP, C.POINTER(View), C.POINTER(View), C.POINTER(MapParams), C.c_int,
+                                     C.POINTER(VisParams), _VP]),
+    "gi_batch_build": (C.c_int, [_VP, C.c_int]),
+    "gi_batch_run": (C.c_int, [_VP, _VP]),
+    "gi_batch_autotune": (C.c_int, [_VP, _VP, C.c_int, C.POINTER(BatchTuning)]),
+    "gi_batch_info": (C.c_int, [_VP, C.POINTER(BatchTuning)]),
 }
 
 _lib = None

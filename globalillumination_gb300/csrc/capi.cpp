@@ -101,7 +101,8 @@ extern "C" void gi_context_destroy(gi_context* c) {
     cudaFree(c->d_depth_tmp);
     cudaFree(c->d_counts);
     for (int i = 0; i < 8; ++i) cudaFree(c->bin_buf[i]);
-    for (int i = 0; i < 8; ++i) cudaFree(c->tier_buf[i]);
+    for (int k = 0; k < 2; ++k)
+        for (int i = 0; i < 8; ++i) cudaFree(c->tier_buf[k][i]);
     for (int i = 0; i < 4; ++i)
         if (c->phase_ev[i]) cudaEventDestroy(static_cast<cudaEvent_t>(c->phase_ev[i]));
     cudaFree(c->d_status);

@@ -81,9 +81,14 @@ struct gi_context {
     void* bin_buf[8] = {};
     size_t bin_cap[8] = {};
     // tiered rasteriser: records, tiny / warp / large lists, large bases,
-    // spill, G-buffer triangle -> record map, per-record resolve data
-    void* tier_buf[8] = {};
-    size_t tier_cap[8] = {};
+    // spill, G-buffer triangle -> record map, per-record resolve data.
+    // Set 0 serves light maps, set 1 the G-buffer keys (the resolve reads
+    // set 1 after any number of light maps).
+    void* tier_buf[2][8] = {};
+    size_t tier_cap[2][8] = {};
+    // tier thresholds (bounding-box pixels): tiny <= tiny_px < warp <= coop_px
+    int tiny_px = 16;
+    int coop_px = 1024;
     // status words (64): [4..11] counters of the binned raster (records, big
     // records, spills, error bits, admitted big pairs as u64, work items),
     // [32..55] counters of the tiered raster

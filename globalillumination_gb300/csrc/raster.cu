@@ -992,8 +992,6 @@ __global__ void __launch_bounds__(128) k_spill(BinArgs a) {
 // per 16 x 16 tile) merge into the target with global atomicMin; the result
 // is the same in any order.
 // ===========================================================================
-constexpr int kTinyPx = 16;
-constexpr int kCoopPx = 1024;
 constexpr int kHugeMax = 8;
 
 struct TierArgs {
@@ -1007,6 +1005,7 @@ struct TierArgs {
     unsigned* spill;
     unsigned spill_cap;
     unsigned long long huge_px;  // bounding-box pixels that make a record huge
+    int tiny_px, coop_px;        // tier thresholds (bounding-box pixels; coop_px <= 1024)
     unsigned* rec_of;            // G-buffer: triangle -> record of its unclipped triangle (~0: none)
     uint4* rres;                 // G-buffer: per record (1/w0, 1/w1, 1/w2 bits, swapped)
     unsigned* ctr;  // [0] records [1] tiny [2] coop [3] large [4] spills [5] error bits
@@ -1068,8 +1067,8 @@ __device__ void tier_sub(const TierArgs& a, const float* c0, const float* c1, co
         if (unclipped) a.rec_of[prim] = slot;
     }
     const long long npx = (long long)(x1 - x0 + 1) * (y1 - y0 + 1);
-    if (npx <= kTinyPx) a.tiny[atomicAdd(a.ctr + 1, 1u)] = slot;
-    else if (npx <= kCoopPx) a.coop[atomicAdd(a.ctr + 2, 1u)] = slot;
+    if (npx <= a.tiny_px) a.tiny[atomicAdd(a.ctr + 1, 1u)] = slot;
+    else if (npx <= a.coop_px) a.coop[atomicAdd(a.ctr + 2, 1u)] = slot;
     else a.large[atomicAdd(a.ctr + 3, 1u)] = slot;
 }
 
@@ -1567,24 +1566,28 @@ static gi_status run_tiered(gi_context* ctx, dev::RasterArgs& r, int mode, cudaS
                             rec_cap * sizeof(unsigned long long), rec_cap * sizeof(unsigned),
                             keys ? std::max<size_t>(prims, 1) * sizeof(unsigned) : 0,
                             keys ? rec_cap * sizeof(uint4) : 0};
+    void** buf = ctx->tier_buf[keys ? 1 : 0];
+    size_t* cap = ctx->tier_cap[keys ? 1 : 0];
     for (int i = 0; i < 8; ++i) {
         if (!need[i]) continue;
-        gi_status s = ensure_buffer(&ctx->tier_buf[i], &ctx->tier_cap[i], need[i]);
+        gi_status s = ensure_buffer(&buf[i], &cap[i], need[i]);
         if (s != GI_OK) return s;
     }
     dev::TierArgs a;
     a.r = r;
-    a.recs = static_cast<dev::BRec*>(ctx->tier_buf[0]);
+    a.recs = static_cast<dev::BRec*>(buf[0]);
     a.rec_cap = (unsigned)rec_cap;
-    a.tiny = static_cast<unsigned*>(ctx->tier_buf[1]);
-    a.coop = static_cast<unsigned*>(ctx->tier_buf[2]);
-    a.large = static_cast<unsigned*>(ctx->tier_buf[3]);
-    a.large_base = static_cast<unsigned long long*>(ctx->tier_buf[4]);
-    a.spill = static_cast<unsigned*>(ctx->tier_buf[5]);
+    a.tiny = static_cast<unsigned*>(buf[1]);
+    a.coop = static_cast<unsigned*>(buf[2]);
+    a.large = static_cast<unsigned*>(buf[3]);
+    a.large_base = static_cast<unsigned long long*>(buf[4]);
+    a.spill = static_cast<unsigned*>(buf[5]);
     a.spill_cap = (unsigned)rec_cap;
     a.huge_px = std::max<unsigned long long>(65536ull, (unsigned long long)r.W * r.H / 8);
-    a.rec_of = keys ? static_cast<unsigned*>(ctx->tier_buf[6]) : nullptr;
-    a.rres = keys ? static_cast<uint4*>(ctx->tier_buf[7]) : nullptr;
+    a.tiny_px = ctx->tiny_px;
+    a.coop_px = ctx->coop_px;
+    a.rec_of = keys ? static_cast<unsigned*>(buf[6]) : nullptr;
+    a.rres = keys ? static_cast<uint4*>(buf[7]) : nullptr;
     a.ctr = ctx->d_status + 32;  // 24 words
     cudaError_t e = cudaMemsetAsync(a.ctr, 0, 24 * sizeof(unsigned), st);
     if (e != cudaSuccess) return fail_cuda(e, "tiered raster memset");
@@ -1655,8 +1658,8 @@ gi_status raster_gbuffer(gi_context* ctx, const gi_scene* scene, const float mvp
     dev::k_gbuffer_resolve<<<grid, 128, 0, st>>>(
         ctx->d_vkeys, scene->d_points, scene->d_normals, scene->d_indices, a.mvp, W, H,
         reinterpret_cast<float4*>(d_pos), reinterpret_cast<float4*>(d_nrm),
-        static_cast<const unsigned*>(ctx->tier_buf[6]), static_cast<const dev::BRec*>(ctx->tier_buf[0]),
-        static_cast<const uint4*>(ctx->tier_buf[7]));
+        static_cast<const unsigned*>(ctx->tier_buf[1][6]), static_cast<const dev::BRec*>(ctx->tier_buf[1][0]),
+        static_cast<const uint4*>(ctx->tier_buf[1][7]));
     ctx->launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "gbuffer resolve launch");

@@ -692,9 +692,9 @@ gi_status launch_frame_visibility(gi_context* ctx, const gi_vis_params* p, const
                                   cudaStream_t st) {
     dim3 grid((W + 31) / 32, (H + 3) / 4);
     const float sx = (float)(1.0 / (double)map_w), sy = (float)(1.0 / (double)map_h);
-    const unsigned* rec_of = static_cast<const unsigned*>(ctx->tier_buf[6]);
-    const dev::BRec* recs = static_cast<const dev::BRec*>(ctx->tier_buf[0]);
-    const uint4* rres = static_cast<const uint4*>(ctx->tier_buf[7]);
+    const unsigned* rec_of = static_cast<const unsigned*>(ctx->tier_buf[1][6]);
+    const dev::BRec* recs = static_cast<const dev::BRec*>(ctx->tier_buf[1][0]);
+    const uint4* rres = static_cast<const uint4*>(ctx->tier_buf[1][7]);
     dev::Mat4 m;
     for (int k = 0; k < 16; ++k) m.m[k] = camera_mvp[k];
     float4* po = reinterpret_cast<float4*>(d_pos);

@@ -17,6 +17,13 @@ visibility parameters.
                     ground is inside the map); 2048^2 map with the
                     reference's polygon offset (4, 20); camera 1920 x 1080;
                     PCSS with 16 Poisson blocker taps and 32 filter taps.
+  batched_720p      256 scenes (seed base + 2): ground + an icosphere field
+                    whose triangle count is log-uniform in [1k, 500k]; 1-8
+                    spot lights (60 deg) at uniform points of the upper
+                    hemisphere of radius 10 (elevation >= 15 deg) aimed at
+                    the origin, each with a map side drawn from {512, 1024,
+                    2048, 4096}; camera 1280 x 720 on a circle of radius 15,
+                    height 8; 5 x 5 PCF, polygon offset (4, 20).
   heavy_2160p       1024 x 1024 UV-grid sphere (r 2) displaced by Perlin
                     noise of amplitude 0.3 + ground; 8 spot lights, 4096^2
                     maps, camera 3840 x 2160.
@@ -24,7 +31,9 @@ visibility parameters.
 from __future__ import annotations
 
 import math
-from dataclasses import dataclass
+from dataclasses import dataclass, field
+
+import numpy as np
 
 from . import _capi as api
 from .shadow import MapParams, Scene, ShadowParams, ViewSpec
@@ -89,3 +98,47 @@ def heavy_2160p(width: int = 3840, height: int = 2160, map_size: int = 4096, gri
     p.light_radius = 0.25
     p.pcss_min_blocker_depth = 0.0
     return Workload("heavy_2160p", s, light, camera, mp, p, lights=eyes)
+
+
+@dataclass
+class BatchFrame:
+    scene: Scene
+    camera: ViewSpec
+    lights: list = field(default_factory=list)
+    maps: list = field(default_factory=list)
+    params: ShadowParams | None = None
+    triangles: int = 0
+
+
+def batched_720p(scenes: int = 256, width: int = 1280, height: int = 720, tri_min: int = 1000,
+                 tri_max: int = 500_000, map_sides=(512, 1024, 2048, 4096), max_lights: int = 8,
+                 seed: int = SEED_BASE + 2) -> list[BatchFrame]:
+    """The batched workload: `scenes` seeded scenes of varied size and light count."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(scenes):
+        target = math.exp(rng.uniform(math.log(tri_min), math.log(tri_max)))
+        level = int(min(6, max(0, round(math.log(target / (20 * 24), 4)))))
+        count = max(1, int(round(target / (20 * 4 ** level))))
+        s = Scene()
+        s.ground(10.0, 0.0)
+        s.icosphere_field(count, level, (-6.0, 0.2, -6.0), (6.0, 2.5, 6.0), 0.2, 0.8, seed * 1000 + k)
+        az = rng.uniform(0.0, 2.0 * math.pi)
+        camera = ViewSpec(eye=(15.0 * math.cos(az), 8.0, 15.0 * math.sin(az)), at=(0.0, 0.5, 0.0),
+                          width=width, height=height, up=(0.0, 1.0, 0.0))
+        lights, maps = [], []
+        for _ in range(int(rng.integers(1, max_lights + 1))):
+            phi = rng.uniform(0.0, 2.0 * math.pi)
+            # uniform over the area of the hemisphere cap above 15 deg elevation
+            cos_p = rng.uniform(math.sin(math.radians(15.0)), 1.0)
+            y = 10.0 * cos_p
+            r = 10.0 * math.sqrt(1.0 - cos_p * cos_p)
+            side = int(rng.choice(map_sides))
+            lights.append(ViewSpec(eye=(r * math.cos(phi), y, r * math.sin(phi)), at=(0.0, 0.0, 0.0),
+                                   width=side, height=side, fovy_deg=60.0, up=(0.0, 1.0, 0.0)))
+            maps.append(MapParams(side, side, bias_mode=api.GI_BIAS_POLYGON_OFFSET, offset_factor=4.0,
+                                  offset_units=20.0))
+        p = ShadowParams.defaults(api.GI_TECH_PCF)
+        p.kernel_order = 5
+        out.append(BatchFrame(s, camera, lights, maps, p, int(s.info().num_triangles)))
+    return out

@@ -418,3 +418,66 @@ def render_frame_passes(ctx: Context, scene: Scene, frame: Frame, mp: MapParams,
 
 
 render_soft_shadows = render_frame
+
+
+class Batch:
+    """Many frames (scene, camera, lights) replayed as one CUDA graph (gi_batch_*).
+
+    Every light of a frame writes its visibility image into its own slice of
+    the frame's output tensor (lights x height x width); the result of each
+    light equals render_frame for that light.  Scenes and output tensors
+    must outlive the batch.
+    """
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        check(_lib().gi_batch_create(device, C.byref(h)), "gi_batch_create")
+        self.handle = h
+        self._keep = []
+
+    def add_frame(self, scene: Scene, camera: ViewSpec, lights, maps, params: ShadowParams, out) -> None:
+        lights, maps = list(lights), list(maps)
+        if len(lights) != len(maps) or not lights:
+            raise ValueError("one map per light, at least one light")
+        import torch
+        if out.dtype != torch.float32 or not out.is_cuda or out.numel() < len(lights) * camera.width * camera.height:
+            raise ValueError("out must be a CUDA float32 tensor of lights x height x width")
+        lv = (api.View * len(lights))(*[l.to_c() for l in lights])
+        mv = (api.MapParams * len(maps))(*[m.to_c() for m in maps])
+        cv = camera.to_c()
+        p = params.to_c(frame_setup(lights[0], camera))
+        check(_lib().gi_batch_add_frame(self.handle, scene.handle, C.byref(cv), lv, mv, len(lights), C.byref(p),
+                                        _ptr(out)), "gi_batch_add_frame")
+        self._keep.append((scene, out))
+
+    def build(self, streams: int = 8) -> None:
+        check(_lib().gi_batch_build(self.handle, streams), "gi_batch_build")
+
+    def run(self, stream=None) -> None:
+        check(_lib().gi_batch_run(self.handle, _stream_ptr(stream)), "gi_batch_run")
+
+    def autotune(self, stream=None, repeats: int = 3) -> dict:
+        t = api.BatchTuning()
+        check(_lib().gi_batch_autotune(self.handle, _stream_ptr(stream), repeats, C.byref(t)), "gi_batch_autotune")
+        return self._tuning(t)
+
+    def info(self) -> dict:
+        t = api.BatchTuning()
+        check(_lib().gi_batch_info(self.handle, C.byref(t)), "gi_batch_info")
+        return self._tuning(t)
+
+    @staticmethod
+    def _tuning(t) -> dict:
+        return {"tiny_px": t.tiny_px, "coop_px": t.coop_px, "streams": t.streams, "frames": t.frames,
+                "kernel_launches": int(t.kernel_launches), "best_ms": float(t.best_ms)}
+
+    def close(self) -> None:
+        if self.handle:
+            _lib().gi_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

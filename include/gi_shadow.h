@@ -365,6 +365,48 @@ gi_status gi_shadow_volume_counts(gi_context* ctx, const gi_scene* scene,
                                   uint8_t* d_stencil, float* d_depth,
                                   void* stream);
 
+/* ------------------------------------------------------------------ */
+/* Batched frames under one CUDA graph                                 */
+/* ------------------------------------------------------------------ */
+/* The reference renders one scene from one light per display() call
+ * (ShadowMapping/src/main.cpp:459-472).  A gi_batch holds many frames
+ * (scene, camera, one or more lights) and replays them as one captured CUDA
+ * graph over several streams; per frame the camera's visibility keys are
+ * rasterised once and shared by all of its lights.  Each light's result
+ * equals gi_render_frame for that light. */
+typedef struct gi_batch gi_batch;
+
+typedef struct gi_batch_tuning {
+    int tiny_px;              /* bounding-box pixels drawn by one thread    */
+    int coop_px;              /* bounding-box pixels drawn by one warp      */
+    int streams;              /* streams the frames are dealt over          */
+    int frames;
+    uint64_t kernel_launches; /* kernel nodes in one gi_batch_run           */
+    float best_ms;            /* autotune: time of the chosen setting       */
+} gi_batch_tuning;
+
+gi_status gi_batch_create(int device, gi_batch** out);
+void gi_batch_destroy(gi_batch* batch);
+/* Adds a frame: `lights`, `maps` have num_lights entries; the camera view
+ * gives the image size.  d_vis is float[num_lights * width * height]: light
+ * l's visibility image at offset l * width * height.  Scenes must stay
+ * uploaded and unchanged while the batch exists.  Invalidates the graph. */
+gi_status gi_batch_add_frame(gi_batch* batch, const gi_scene* scene,
+                             const gi_view* camera, const gi_view* lights,
+                             const gi_map_params* maps, int num_lights,
+                             const gi_vis_params* vis, float* d_vis);
+/* Sizes the scratch by running every frame once (synchronising the device),
+ * then captures the batch over `streams` streams (1..64). */
+gi_status gi_batch_build(gi_batch* batch, int streams);
+/* Launches the captured graph on `stream`. */
+gi_status gi_batch_run(gi_batch* batch, void* stream);
+/* Times tier thresholds and stream counts on this batch (each candidate
+ * rebuilt and replayed `repeats` times on `stream`), keeps the fastest
+ * and rebuilds with it.  *out (may be NULL) receives the choice. */
+gi_status gi_batch_autotune(gi_batch* batch, void* stream, int repeats,
+                            gi_batch_tuning* out);
+gi_status gi_batch_info(const gi_batch* batch, gi_batch_tuning* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -95,3 +95,13 @@ def test_context_without_device_fails_cleanly():
     h = C.c_void_p()
     assert lib.gi_context_create(0, C.byref(h)) == api.GI_ERR_CUDA
     assert lib.gi_last_error_string()
+
+
+def test_batch_argument_checks():
+    lib = api.load()
+    assert lib.gi_batch_create(0, None) == api.GI_ERR_INVALID_ARG
+    assert lib.gi_batch_build(None, 4) == api.GI_ERR_INVALID_ARG
+    assert lib.gi_batch_run(None, None) == api.GI_ERR_INVALID_ARG
+    assert lib.gi_batch_add_frame(None, None, None, None, None, 1, None, None) == api.GI_ERR_INVALID_ARG
+    assert lib.gi_batch_info(None, None) == api.GI_ERR_INVALID_ARG
+    assert C.sizeof(api.BatchTuning) == 4 * 4 + 8 + 8
