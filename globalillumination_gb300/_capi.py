@@ -44,7 +44,8 @@ GI_TECH_RPCF_CONSERVATIVE = 7
 GI_TECH_RPCF_SMSR = 8
 GI_TECH_RSMSS = 9
 GI_TECH_HARD_SOFTAPP = 10
-GI_TECH_COUNT = 11
+GI_TECH_RBSSM = 11
+GI_TECH_COUNT = 12
 
 # gi_pretest_mode
 GI_PRETEST_REFERENCE = 0

@@ -390,6 +390,7 @@ extern "C" gi_status gi_vis_params_default(int technique, gi_vis_params* p) {
     p->pcss_min_blocker_depth = 0.99f;    // PlausibleSoftShadow.frag:368
     p->poisson_blocker_taps = 16;
     p->poisson_filter_taps = 32;
+    if (technique == GI_TECH_RBSSM) p->kernel_size = 7;  // SoftShadowMapping/src/main.cpp:1450-1455
     for (int i = 0; i < 4; ++i) {
         p->light_mvp_biased[i * 5] = 1.0f;
         p->camera_mv[i * 5] = 1.0f;
@@ -414,15 +415,15 @@ static gi_status check_vis_params(const gi_vis_params* p) {
             return fail(GI_ERR_INVALID_ARG,
                         "gi_visibility: kernel_order and penumbra_size must be in [1, 64]");
     }
-    if (t >= GI_TECH_SMSR_CONSERVATIVE && t <= GI_TECH_RSMSS) {
+    if ((t >= GI_TECH_SMSR_CONSERVATIVE && t <= GI_TECH_RSMSS) || t == GI_TECH_RBSSM) {
         if (p->max_search < 0 || p->max_search > 4096)
             return fail(GI_ERR_INVALID_ARG, "gi_visibility: max_search must be in [0, 4096]");
     }
-    if (t == GI_TECH_PCSS_GRID || t == GI_TECH_PCSS_POISSON) {
+    if (t == GI_TECH_PCSS_GRID || t == GI_TECH_PCSS_POISSON || t == GI_TECH_RBSSM) {
         if (p->kernel_size < 1 || p->kernel_size > 63)
             return fail(GI_ERR_INVALID_ARG, "gi_visibility: kernel_size must be in [1, 63]");
     }
-    if (t == GI_TECH_PCSS_GRID && (p->blocker_search_size < 1 || p->blocker_search_size > 63))
+    if ((t == GI_TECH_PCSS_GRID || t == GI_TECH_RBSSM) && (p->blocker_search_size < 1 || p->blocker_search_size > 63))
         return fail(GI_ERR_INVALID_ARG, "gi_visibility: blocker_search_size must be in [1, 63]");
     if (t == GI_TECH_PCSS_POISSON &&
         (p->poisson_blocker_taps < 1 || p->poisson_blocker_taps > 64 ||

@@ -264,6 +264,7 @@ TECHNIQUES = {
     "rpcf_smsr": api.GI_TECH_RPCF_SMSR,
     "rsmss": api.GI_TECH_RSMSS,
     "hard_softapp": api.GI_TECH_HARD_SOFTAPP,
+    "rbssm": api.GI_TECH_RBSSM,
 }
 
 

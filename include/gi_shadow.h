@@ -280,7 +280,8 @@ typedef enum gi_technique {
     GI_TECH_RPCF_SMSR = 8,            /* NonConservativeSMSR.frag:306-350 (RPCF v.1) */
     GI_TECH_RSMSS = 9,                /* FilteredRBSM.frag (RSMSS / RPCF v.2) */
     GI_TECH_HARD_SOFTAPP = 10,        /* SoftShadow HardShadow.frag:35-58     */
-    GI_TECH_COUNT = 11
+    GI_TECH_RBSSM = 11,               /* SoftShadow/RBSSM.frag:1202-1376      */
+    GI_TECH_COUNT = 12
 } gi_technique;
 
 typedef enum gi_pretest_mode {

@@ -26,6 +26,7 @@ def load():
         lib.or_gbuffer.argtypes = [vp, vp, i, vp, i, vp, i, i, vp, vp, i]
         lib.or_visibility.argtypes = [vp, vp, i, i, vp, vp, vp, i, i, vp, i]
         lib.or_shadow_volume_counts.argtypes = [vp, vp, i, vp, i, vp, f, vp, i, i, i, vp, vp, i]
+        lib.or_rbssm_hits.argtypes = [vp, i]
         for fn in (lib.or_shadow_map, lib.or_gbuffer, lib.or_visibility, lib.or_shadow_volume_counts):
             fn.restype = None
         _lib = lib
@@ -75,3 +76,20 @@ def shadow_volume_counts(points, normals, indices, light_pos, infinity, mvp, wid
                                    L.ctypes.data, infinity, m.ctypes.data, width, height, depth_func,
                                    st.ctypes.data, dp.ctypes.data, threads)
     return st, dp
+
+
+def rbssm_hits(reset=False):
+    """Hit counts of the RBSSM smoothONDS return sites: {source line: hits}."""
+    out = np.zeros(4096, np.uint64)
+    load().or_rbssm_hits(out.ctypes.data, 1 if reset else 0)
+    return {int(k): int(out[k]) for k in np.nonzero(out)[0]}
+
+
+def rbssm_return_sites():
+    """Source lines of the RBSSM smoothONDS return sites in gi_oracle.cpp."""
+    import os
+
+    src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "gi_oracle.cpp")
+    with open(src) as f:
+        lines = f.read().split("\n")
+    return [i + 1 for i, l in enumerate(lines) if "RB_RET(" in l and "#define" not in l]

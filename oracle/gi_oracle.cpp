@@ -872,6 +872,521 @@ float nc_rpcf(const Ctx& c, V4 n, bool filtered) {  // computeShadowFromAccurate
     return illum / (float)count;
 }
 
+// ---- SoftShadow/RBSSM.frag -----------------------------------------------------
+// Revectorization-based soft shadow mapping.  getDisc(vec4, vec2, float) and
+// getDisc(vec4, vec2, vec4) are the same functions as in
+// NonConservativeSMSR.frag (nc_get_disc_type / nc_get_disc_vec above); the
+// four-neighbour getDisc(vec4, float) (RBSSM.frag:37-61) is nc_get_disc_all
+// without early exits.
+float gstep(float edge, float x) { return x < edge ? 0.0f : 1.0f; }
+
+// compressPositiveDiscontinuity / decompressPositiveDiscontinuity
+// (RBSSM.frag:25-35).
+float rb_compress(float nd) { return -2.0f - ((0.5f - nd) * 2.0f); }
+float rb_decompress(float nd) { return 0.5f - ((nd + 2.0f) * -1.0f) / 2.0f; }
+
+bool rb_disc_t(const Ctx& c, V4 n, float dx, float dy, float type) {
+    return nc_get_disc_type(c, n, V2{dx, dy}, type);
+}
+bool rb_disc_v(const Ctx& c, V4 n, float dx, float dy, V4 type) {
+    float unused = 0.0f;
+    return nc_get_disc_vec(c, n, V2{dx, dy}, type, unused);
+}
+
+// computeDiscontinuityLength (RBSSM.frag:193-253).
+float rb_disc_length(const Ctx& c, V4 in_disc, V4 lc, V2 dir) {
+    V4 cc = lc;
+    float found = 0.0f;
+    if (dir.x == 0.0f && in_disc.x == 0.0f && in_disc.y != 0.0f) return -1.0f;
+    if (dir.y == 0.0f && in_disc.x != 0.0f && in_disc.y == 0.0f) return -1.0f;
+    if (((0.5f - in_disc.x) * 8.0f - 1.0f) == dir.x) return 1.0f;
+    if (((in_disc.y - 0.5f) * 8.0f + 1.0f) == dir.y) return 1.0f;
+    float dist = 1.0f;
+    float new_depth = 0.0f;
+    V2 st = {dir.x * c.sx, dir.y * c.sy};
+    cc.x += st.x;
+    cc.y += st.y;
+    const float thr = c.p->depth_threshold;
+    for (int it = 0; it < c.p->max_search; it++) {
+        float d = fetch(c, cc.x, cc.y);
+        if (in_disc.z == 0.0f)
+            if (gabs(cc.z - d) < thr) cc.z -= thr;
+        float center = (cc.z <= d) ? 1.0f : 0.0f;
+        if (gabs(center - in_disc.z) == 0.0f) {
+            bool has = nc_get_disc_type(c, cc, V2{0.0f, 0.0f}, in_disc.z);
+            found = has ? 1.0f : 0.0f;
+            break;
+        } else {
+            bool has = nc_get_disc_vec(c, cc, dir, in_disc, new_depth);
+            if (!has) break;
+        }
+        dist = dist + 1.0f;
+        cc.x += st.x;
+        cc.y += st.y;
+        if (in_disc.z == 1.0f) cc.z = new_depth;
+    }
+    return gmix(-dist, dist, found);
+}
+
+// normalizeDiscontinuitySpace (RBSSM.frag:255-280).
+float rb_normalize_space(const Ctx& c, V2 dir, float sub) {
+    if (dir.x < 0.0f && dir.y < 0.0f) return -1.0f;
+    float edge = gmin(gabs(dir.x) + gabs(dir.y) - 1.0f, (float)c.p->max_search);
+    float nd = 1.0f - gmax(dir.x, dir.y) / edge;
+    if (dir.x == dir.y) nd += gmix(sub / edge, (1.0f - sub) / edge, gstep(0.5f, sub));
+    else if (dir.x == gmax(dir.x, dir.y)) nd += (1.0f - sub) / edge;
+    else nd += sub / edge;
+    if (dir.x > 0.0f && dir.y > 0.0f) return rb_compress(nd);
+    return nd;
+}
+
+// Branch coverage of smoothONDS for the tests: every return site counts
+// its hits (indexed by source line).
+std::atomic<unsigned long long> g_rb_hits[4096];
+#define RB_RET(v)                                                    \
+    do {                                                             \
+        g_rb_hits[__LINE__ & 4095].fetch_add(1, std::memory_order_relaxed); \
+        return (v);                                                  \
+    } while (0)
+
+// smoothONDS (RBSSM.frag:311-1117): the fill of one discontinuity tap.
+// lc, nd and disc are by-value copies that the cases modify in place, as
+// the shader does; a case that does not return leaves its changes for the
+// cases below it.
+float rb_smooth_onds(const Ctx& c, V4 lc, V4 nd, V4 disc, V2 sub) {
+    const float sx = c.sx, sy = c.sy;
+    if (disc.z == 0.0f) {
+        // entering discontinuity: positive on both axes, both sides of one axis
+        if (nd.x <= -2.0f && nd.y <= -2.0f && (disc.x == 0.75f || disc.y == 0.75f)) {
+            bool left = true, right = true, bottom = true, top = true;
+            if (disc.x == 0.75f) {
+                if (disc.y == 0.0f) {
+                    lc.y += sy;
+                    top = rb_disc_t(c, lc, 0.0f, 1.0f, disc.z);
+                    lc.y -= 2.0f * sy;
+                    bottom = rb_disc_t(c, lc, 0.0f, 1.0f, disc.z);
+                    lc.y += sy;
+                    if (top && bottom) RB_RET(0.0f);
+                    lc.y += gmix(-sy, sy, gstep(1.0f, top ? 1.0f : 0.0f));
+                    left = rb_disc_v(c, lc, 0.0f, 1.0f, V4{0.5f, 0.0f, 0.0f, 0.0f});
+                    right = !left;
+                } else {
+                    if (disc.y == 0.5f) top = false;
+                    else if (disc.y == 0.25f) bottom = false;
+                    lc.y += ((0.5f - disc.y) * 8.0f - 1.0f) * sy;
+                    left = rb_disc_v(c, lc, 0.0f, 1.0f, V4{0.5f, 0.0f, 0.0f, disc.z});
+                    right = rb_disc_v(c, lc, 0.0f, 1.0f, V4{0.25f, 0.0f, 0.0f, disc.z});
+                    if (left && right) {
+                        if (nd.y <= -2.0f) nd.y = rb_decompress(nd.y) + 0.5f;
+                        float a = gclamp(sub.x - (nd.y - 1.0f), 0.0f, 1.0f);
+                        float b = gclamp((1.0f - sub.x) - (nd.y - 1.0f), 0.0f, 1.0f);
+                        float cc = gmix(1.0f - sub.y, sub.y, gstep(disc.y, 1.0f));
+                        RB_RET(gmin(gmin(a, b), cc));
+                    }
+                }
+            }
+            if (disc.y == 0.75f) {
+                if (disc.x == 0.0f) {
+                    lc.x -= sx;
+                    left = rb_disc_t(c, lc, 1.0f, 0.0f, disc.z);
+                    lc.x += 2.0f * sx;
+                    right = rb_disc_t(c, lc, 1.0f, 0.0f, disc.z);
+                    lc.x -= sx;
+                    if (left && right) RB_RET(0.0f);
+                    lc.x += gmix(sx, -sx, gstep(1.0f, left ? 1.0f : 0.0f));
+                    bottom = rb_disc_v(c, lc, 0.0f, 0.25f, V4{0.5f, 0.0f, 0.0f, disc.z});
+                    top = !bottom;
+                } else {
+                    if (disc.x == 0.5f) right = false;
+                    else if (disc.x == 0.25f) left = false;
+                    lc.x -= ((0.5f - disc.x) * 8.0f - 1.0f) * sx;
+                    bottom = rb_disc_v(c, lc, 1.0f, 0.0f, V4{0.0f, 0.5f, 0.0f, disc.z});
+                    top = rb_disc_v(c, lc, 1.0f, 0.0f, V4{0.0f, 0.25f, 0.0f, disc.z});
+                    if (bottom && top) {
+                        if (nd.x <= -2.0f) nd.x = rb_decompress(nd.x) + 0.5f;
+                        float a = gclamp(sub.y - (nd.x - 1.0f), 0.0f, 1.0f);
+                        float b = gclamp((1.0f - sub.y) - (nd.x - 1.0f), 0.0f, 1.0f);
+                        float cc = gmix(1.0f - sub.x, sub.x, gstep(disc.x, 1.0f));
+                        RB_RET(gmin(gmin(a, b), cc));
+                    }
+                }
+            }
+            if (!left && !bottom) RB_RET(gclamp((1.0f - sub.x) - (1.0f - sub.y), 0.0f, 1.0f));
+            else if (!right && !bottom) RB_RET(gclamp(sub.x - (1.0f - sub.y), 0.0f, 1.0f));
+            else if (!left && !top) RB_RET(gclamp((1.0f - sub.y) - sub.x, 0.0f, 1.0f));
+            else if (!right && !top) RB_RET(gclamp((1.0f - sub.y) - (1.0f - sub.x), 0.0f, 1.0f));
+        }
+        if (disc.x == 0.75f || disc.y == 0.75f) {
+            // entering left and right, plus top or bottom
+            if (disc.x == 0.75f && disc.y != 0.0f) {
+                lc.y += ((disc.y - 0.75f) * 4.0f) * sy;
+                bool left = rb_disc_v(c, lc, 0.0f, 1.0f, V4{0.5f, 0.0f, 0.0f, disc.z});
+                bool right = rb_disc_v(c, lc, 0.0f, 1.0f, V4{0.25f, 0.0f, 0.0f, disc.z});
+                if (!left && !right) RB_RET(gclamp(1.0f - nd.y, 0.0f, 1.0f));
+                float s = gmix(1.0f - sub.y, sub.y, gstep(1.0f, disc.y));
+                float a = gmix(s, gclamp((1.0f - sub.x) - (nd.y - 1.0f), 0.0f, 1.0f),
+                               gstep(1.0f, right ? 1.0f : 0.0f));
+                float b = gmix(s, gclamp(sub.x - (nd.y - 1.0f), 0.0f, 1.0f),
+                               gstep(1.0f, left ? 1.0f : 0.0f));
+                RB_RET(gmin(a, b));
+            }
+            // entering left and right only
+            if (disc.x == 0.75f && disc.y == 0.0f) {
+                bool topLeft = true, topRight = true, bottomLeft = true, bottomRight = true;
+                bool topCenter = false, bottomCenter = false;
+                V4 tlc = lc, blc = lc;
+                if (!topCenter) {
+                    tlc.y += sy;
+                    float center = (tlc.z <= fetch(c, tlc.x, tlc.y)) ? 1.0f : 0.0f;
+                    topCenter = !(center != 0.0f);
+                    topLeft = rb_disc_v(c, tlc, 0.0f, 1.0f, V4{0.5f, 0.0f, 0.0f, disc.z});
+                    topRight = rb_disc_v(c, tlc, 0.0f, 1.0f, V4{0.25f, 0.0f, 0.0f, disc.z});
+                }
+                if (!bottomCenter) {
+                    blc.y -= sy;
+                    float center = (blc.z <= fetch(c, blc.x, blc.y)) ? 1.0f : 0.0f;
+                    bottomCenter = !(center != 0.0f);
+                    bottomLeft = rb_disc_v(c, blc, 0.0f, 1.0f, V4{0.5f, 0.0f, 0.0f, disc.z});
+                    bottomRight = rb_disc_v(c, blc, 0.0f, 1.0f, V4{0.25f, 0.0f, 0.0f, disc.z});
+                }
+                if (topCenter) {
+                    topLeft = true;
+                    topRight = true;
+                }
+                if (bottomCenter) {
+                    bottomLeft = true;
+                    bottomRight = true;
+                }
+                if (nd.y <= -2.0f) {
+                    nd.y = rb_decompress(nd.y) + 0.5f;
+                    float a = gclamp(sub.x - (nd.y - 1.0f), 0.0f, 1.0f);
+                    float b = gclamp((1.0f - sub.x) - (nd.y - 1.0f), 0.0f, 1.0f);
+                    if (!bottomRight || !topRight) RB_RET(a);
+                    else if (!bottomLeft || !topLeft) RB_RET(b);
+                    else RB_RET(gmin(a, b));
+                }
+                if ((!bottomRight && !bottomLeft) || (!topRight && !topLeft))
+                    RB_RET(gclamp(1.0f - nd.y, 0.0f, 1.0f));
+                else if (!bottomRight || !topRight)
+                    RB_RET(gclamp(sub.x - (nd.y - 1.0f), 0.0f, 1.0f));
+                else
+                    RB_RET(gclamp((1.0f - sub.x) - (nd.y - 1.0f), 0.0f, 1.0f));
+            }
+            // entering top and bottom, plus left or right
+            if (disc.x != 0.0f && disc.y == 0.75f) {
+                lc.x -= ((0.5f - disc.x) * 8.0f - 1.0f) * sx;
+                bool bottom = rb_disc_v(c, lc, 1.0f, 0.0f, V4{0.0f, 0.5f, 0.0f, disc.z});
+                bool top = rb_disc_v(c, lc, 1.0f, 0.0f, V4{0.0f, 0.25f, 0.0f, disc.z});
+                if (!bottom && !top) RB_RET(gclamp(1.0f - nd.x, 0.0f, 1.0f));
+                float s = gmix(sub.x, 1.0f - sub.x, gstep(disc.x, 0.25f));
+                float a = gmix(s, gclamp(sub.y - (nd.x - 1.0f), 0.0f, 1.0f), gstep(1.0f, top ? 1.0f : 0.0f));
+                float b = gmix(s, gclamp((1.0f - sub.y) - (nd.x - 1.0f), 0.0f, 1.0f),
+                               gstep(1.0f, bottom ? 1.0f : 0.0f));
+                RB_RET(gmin(a, b));
+            }
+            // entering top and bottom only
+            if (disc.x == 0.0f && disc.y == 0.75f) {
+                bool topLeft = true, topRight = true, bottomLeft = true, bottomRight = true;
+                bool leftCenter = false, rightCenter = false;
+                V4 llc = lc, rlc = lc;
+                if (!rightCenter) {
+                    rlc.x += sx;
+                    float center = (rlc.z <= fetch(c, rlc.x, rlc.y)) ? 1.0f : 0.0f;
+                    rightCenter = !(center != 0.0f);
+                    bottomRight = rb_disc_v(c, rlc, 1.0f, 0.0f, V4{0.0f, 0.5f, 0.0f, disc.z});
+                    topRight = rb_disc_v(c, rlc, 1.0f, 0.0f, V4{0.0f, 0.25f, 0.0f, disc.z});
+                }
+                if (!leftCenter) {
+                    llc.x -= sx;
+                    float center = (llc.z <= fetch(c, llc.x, llc.y)) ? 1.0f : 0.0f;
+                    leftCenter = !(center != 0.0f);
+                    bottomLeft = rb_disc_v(c, llc, 1.0f, 0.0f, V4{0.0f, 0.5f, 0.0f, disc.z});
+                    topLeft = rb_disc_v(c, llc, 1.0f, 0.0f, V4{0.0f, 0.25f, 0.0f, disc.z});
+                }
+                if (rightCenter) {
+                    bottomRight = true;
+                    topRight = true;
+                }
+                if (leftCenter) {
+                    topLeft = true;
+                    bottomLeft = true;
+                }
+                if (nd.x <= -2.0f) {
+                    nd.x = rb_decompress(nd.x) + 0.5f;
+                    float a = gclamp(sub.y - (nd.x - 1.0f), 0.0f, 1.0f);
+                    float b = gclamp((1.0f - sub.y) - (nd.x - 1.0f), 0.0f, 1.0f);
+                    if (!bottomRight || !bottomLeft) RB_RET(a);
+                    else if (!topRight || !topLeft) RB_RET(b);
+                    else RB_RET(gmin(a, b));
+                }
+                if ((!bottomRight && !topRight) || (!bottomLeft && !topLeft))
+                    RB_RET(gclamp(1.0f - nd.x, 0.0f, 1.0f));
+                else if (!bottomRight || !bottomLeft)
+                    RB_RET(gclamp(sub.y - (nd.x - 1.0f), 0.0f, 1.0f));
+                else
+                    RB_RET(gclamp((1.0f - sub.y) - (nd.x - 1.0f), 0.0f, 1.0f));
+            }
+        }
+        // corner: discontinuity on both axes
+        if (disc.x > 0.0f && disc.y > 0.0f) {
+            lc.x -= ((0.5f - disc.x) * 8.0f - 1.0f) * sx;
+            bool horizontal = rb_disc_t(c, lc, 1.0f, 0.0f, 0.0f);
+            lc.x += ((0.5f - disc.x) * 8.0f - 1.0f) * sx;
+            lc.y += ((0.5f - disc.y) * 8.0f - 1.0f) * sy;
+            bool vertical = rb_disc_t(c, lc, 0.0f, 1.0f, 0.0f);
+            if (horizontal && !vertical) {
+                disc.x = 0.0f;
+            } else if (!horizontal && vertical) {
+                disc.y = 0.0f;
+            } else if (!horizontal && !vertical) {
+                if (disc.y == 0.5f) RB_RET(gclamp((1.0f - nd.x) - (sub.y - 1.0f), 0.0f, 1.0f));
+                else if (disc.y == 0.25f) RB_RET(gclamp((1.0f - nd.x) + sub.y, 0.0f, 1.0f));
+            } else {
+                float a, b;
+                if (disc.x == 0.5f && disc.y == 0.5f) {
+                    a = gmix(1.0f - sub.y, gclamp(1.0f - (nd.x - (1.0f - sub.y)), 0.0f, 1.0f), gstep(-2.0f, nd.x));
+                    b = gmix(sub.x, gclamp(1.0f - (nd.y - sub.x), 0.0f, 1.0f), gstep(-2.0f, nd.y));
+                    RB_RET(gmin(a, b));
+                } else if (disc.x == 0.5f && disc.y == 0.25f) {
+                    a = gmix(sub.y, gclamp(1.0f - (nd.x - sub.y), 0.0f, 1.0f), gstep(-2.0f, nd.x));
+                    b = gmix(sub.x, gclamp(1.0f - (nd.y - sub.x), 0.0f, 1.0f), gstep(-2.0f, nd.y));
+                    RB_RET(gmin(a, b));
+                } else if (disc.x == 0.25f && disc.y == 0.5f) {
+                    a = gmix(1.0f - sub.y, gclamp(1.0f - (nd.x - (1.0f - sub.y)), 0.0f, 1.0f), gstep(-2.0f, nd.x));
+                    b = gmix(1.0f - sub.x, gclamp(1.0f - (nd.y - (1.0f - sub.x)), 0.0f, 1.0f), gstep(-2.0f, nd.y));
+                    RB_RET(gmin(a, b));
+                } else if (disc.x == 0.25f && disc.y == 0.25f) {
+                    a = gmix(sub.y, gclamp(1.0f - (nd.x - sub.y), 0.0f, 1.0f), gstep(-2.0f, nd.x));
+                    b = gmix(1.0f - sub.x, gclamp(1.0f - (nd.y - (1.0f - sub.x)), 0.0f, 1.0f), gstep(-2.0f, nd.y));
+                    RB_RET(gmin(a, b));
+                }
+            }
+        }
+        if (nd.x <= -2.0f) RB_RET(gmix(1.0f - sub.y, sub.y, gstep(disc.y, 0.25f)));
+        if (nd.y <= -2.0f) RB_RET(gmix(sub.x, 1.0f - sub.x, gstep(disc.x, 0.25f)));
+        if (disc.y > 0.0f) {
+            if (disc.y == 0.5f) RB_RET(gclamp((1.0f - sub.y) - (nd.x - 1.0f), 0.0f, 1.0f));
+            else RB_RET(gclamp(sub.y - (nd.x - 1.0f), 0.0f, 1.0f));
+        }
+        if (disc.x > 0.0f) {
+            if (disc.x == 0.5f) RB_RET(gclamp(sub.x - (nd.y - 1.0f), 0.0f, 1.0f));
+            else RB_RET(gclamp((1.0f - sub.x) - (nd.y - 1.0f), 0.0f, 1.0f));
+        }
+    } else {
+        // exiting discontinuity
+        if (disc.x == 0.75f || disc.y == 0.75f) {
+            // exiting left and right only
+            if (disc.x == 0.75f && disc.y == 0.0f) {
+                V4 ref = lc;
+                ref.x = lc.x - sx;
+                bool left = rb_disc_v(c, ref, 0.0f, 1.0f, V4{0.5f, 0.0f, 0.0f, disc.z});
+                ref.x = lc.x + sx;
+                bool right = rb_disc_v(c, ref, 0.0f, 1.0f, V4{0.25f, 0.0f, 0.0f, disc.z});
+                if (left && right) {
+                    RB_RET(gclamp(nd.y, 0.0f, 1.0f));
+                } else if (left || right) {
+                    if (!left) RB_RET(gmix(1.0f - sub.x, gclamp(nd.y - sub.x, 0.0f, 1.0f), gstep(-2.0f, nd.y)));
+                    else RB_RET(gmix(sub.x, gclamp(nd.y - (1.0f - sub.x), 0.0f, 1.0f), gstep(-2.0f, nd.y)));
+                } else {
+                    // one pass of the commented-out while loop: count = 0, mult = 1
+                    const int count = 0;
+                    const int mult = (count / 2) + 1;
+                    if (std::fmod((float)count, 2.0f) == 0.0f) ref.y = lc.y + (float)mult * sy;
+                    else ref.y = lc.y - (float)mult * sy;
+                    ref.x = lc.x - sx;
+                    left = rb_disc_t(c, ref, 1.0f, 0.0f, 0.0f);
+                    ref.x = lc.x + sx;
+                    right = rb_disc_t(c, ref, 1.0f, 0.0f, 0.0f);
+                    if (left && right) {
+                        RB_RET(gclamp(nd.y, 0.0f, 1.0f));
+                    } else {
+                        if (!left) RB_RET(gmix(1.0f - sub.x, gclamp(nd.y - sub.x, 0.0f, 1.0f), gstep(-2.0f, nd.y)));
+                        else RB_RET(gmix(sub.x, gclamp(nd.y - (1.0f - sub.x), 0.0f, 1.0f), gstep(-2.0f, nd.y)));
+                    }
+                }
+            }
+            // exiting left and right, plus top or bottom
+            if (disc.x == 0.75f && disc.y != 0.0f) {
+                lc.y += ((0.5f - disc.y) * 8.0f - 1.0f) * sy;
+                bool left = rb_disc_v(c, lc, 0.0f, 1.0f, V4{0.5f, 0.0f, 0.0f, disc.z});
+                bool right = rb_disc_v(c, lc, 0.0f, 1.0f, V4{0.25f, 0.0f, 0.0f, disc.z});
+                float a = 0.0f, b = 0.0f;
+                if (left && right) {
+                    RB_RET(gclamp(nd.y, 0.0f, 1.0f));
+                } else if (left || right) {
+                    if (left) a = gmix(sub.y, 1.0f - sub.y, gstep(disc.y, 0.25f));
+                    else a = gmix(1.0f - sub.x, gclamp(nd.y - sub.x, 0.0f, 1.0f), gstep(-2.0f, nd.y));
+                    if (right) b = gmix(sub.y, 1.0f - sub.y, gstep(disc.y, 0.25f));
+                    else b = gmix(sub.x, gclamp(nd.y - (1.0f - sub.x), 0.0f, 1.0f), gstep(-2.0f, nd.y));
+                    RB_RET(gmax(a, b));
+                } else {
+                    if (disc.y == 0.75f) RB_RET(0.0f);
+                    V4 ref = lc;
+                    ref.x = lc.x - sx;
+                    left = rb_disc_t(c, ref, 1.0f, 0.0f, 0.0f);
+                    ref.x = lc.x + sx;
+                    right = rb_disc_t(c, ref, 1.0f, 0.0f, 0.0f);
+                    lc.y += ((0.5f - disc.y) * 8.0f - 1.0f) * sy;
+                    if (left && right) {
+                        RB_RET(gclamp(nd.y, 0.0f, 1.0f));
+                    } else {
+                        a = gmix(1.0f - sub.x, sub.x, gstep(1.0f, left ? 1.0f : 0.0f));
+                        b = gmix(sub.y, 1.0f - sub.y, gstep(disc.y, 0.25f));
+                        RB_RET(gmax(a, b));
+                    }
+                }
+            }
+            // exiting top and bottom only
+            if (disc.x == 0.0f && disc.y == 0.75f) {
+                V4 ref = lc;
+                ref.y = lc.y - sy;
+                bool top = rb_disc_t(c, ref, 0.0f, 1.0f, 0.0f);
+                ref.y = lc.y + sy;
+                bool bottom = rb_disc_t(c, ref, 0.0f, 1.0f, 0.0f);
+                if (bottom && top) {
+                    RB_RET(gclamp(nd.x, 0.0f, 1.0f));
+                } else if (bottom || top) {
+                    if (!top) RB_RET(gmix(1.0f - sub.y, gclamp(nd.x - sub.y, 0.0f, 1.0f), gstep(-2.0f, nd.x)));
+                    else RB_RET(gmix(sub.y, gclamp(nd.x - (1.0f - sub.y), 0.0f, 1.0f), gstep(-2.0f, nd.x)));
+                } else {
+                    const int count = 0;
+                    const int mult = (count / 2) + 1;
+                    if (std::fmod((float)count, 2.0f) == 0.0f) ref.x = lc.x + (float)mult * sx;
+                    else ref.x = lc.x - (float)mult * sx;
+                    ref.y = lc.y - sy;
+                    top = rb_disc_t(c, ref, 0.0f, 1.0f, 0.0f);
+                    ref.y = lc.y + sy;
+                    bottom = rb_disc_t(c, ref, 0.0f, 1.0f, 0.0f);
+                    if (top && bottom) {
+                        RB_RET(gclamp(nd.x, 0.0f, 1.0f));
+                    } else {
+                        if (!top) RB_RET(gmix(1.0f - sub.y, gclamp(nd.x - sub.y, 0.0f, 1.0f), gstep(-2.0f, nd.x)));
+                        else RB_RET(gmix(sub.y, gclamp(nd.x - (1.0f - sub.y), 0.0f, 1.0f), gstep(-2.0f, nd.x)));
+                    }
+                }
+            }
+            // exiting top and bottom, plus left or right
+            if (disc.x != 0.0f && disc.y == 0.75f) {
+                lc.x -= ((0.5f - disc.x) * 8.0f - 1.0f) * sx;
+                bool bottom = rb_disc_v(c, lc, 1.0f, 0.0f, V4{0.0f, 0.5f, 0.0f, disc.z});
+                bool top = rb_disc_v(c, lc, 1.0f, 0.0f, V4{0.0f, 0.25f, 0.0f, disc.z});
+                float a = 0.0f, b = 0.0f;
+                if (bottom && top) {
+                    RB_RET(gclamp(nd.x, 0.0f, 1.0f));
+                } else if (bottom || top) {
+                    if (top) a = gmix(1.0f - sub.x, sub.x, gstep(disc.x, 0.25f));
+                    else a = gmix(1.0f - sub.y, gclamp(nd.x - sub.y, 0.0f, 1.0f), gstep(-2.0f, nd.x));
+                    if (bottom) b = gmix(1.0f - sub.x, sub.x, gstep(disc.x, 0.25f));
+                    else b = gmix(sub.y, gclamp(nd.x - (1.0f - sub.y), 0.0f, 1.0f), gstep(-2.0f, nd.x));
+                    RB_RET(gmax(a, b));
+                } else {
+                    if (disc.x == 0.75f) RB_RET(0.0f);
+                    V4 ref = lc;
+                    ref.y = lc.y - sy;
+                    top = rb_disc_t(c, ref, 0.0f, 1.0f, 0.0f);
+                    ref.y = lc.y + sy;
+                    bottom = rb_disc_t(c, ref, 0.0f, 1.0f, 0.0f);
+                    lc.x -= ((0.5f - disc.x) * 8.0f - 1.0f) * sx;
+                    if (top && bottom) {
+                        RB_RET(gclamp(nd.x, 0.0f, 1.0f));
+                    } else {
+                        a = gmix(1.0f - sub.y, sub.y, gstep(1.0f, top ? 1.0f : 0.0f));
+                        b = gmix(1.0f - sub.x, sub.x, gstep(disc.x, 0.25f));
+                        RB_RET(gmax(a, b));
+                    }
+                }
+            }
+        }
+        // corner: discontinuity on both axes (the x step is added twice, as
+        // in the shader)
+        if (disc.x > 0.0f && disc.y > 0.0f) {
+            lc.x += ((0.5f - disc.x) * 8.0f - 1.0f) * sx;
+            bool horizontal = rb_disc_t(c, lc, 1.0f, 0.0f, disc.z);
+            lc.x += ((0.5f - disc.x) * 8.0f - 1.0f) * sx;
+            lc.y += ((0.5f - disc.y) * 8.0f - 1.0f) * sy;
+            bool vertical = rb_disc_t(c, lc, 0.0f, 1.0f, disc.z);
+            if (horizontal && !vertical) {
+                disc.x = 0.0f;
+            } else if (!horizontal && vertical) {
+                disc.y = 0.0f;
+            } else if (!horizontal && !vertical) {
+                if (disc.y == 0.5f) RB_RET(gclamp(sub.y - (1.0f - nd.x), 0.0f, 1.0f));
+                else if (disc.y == 0.25f) RB_RET(gclamp((1.0f - sub.y) - (1.0f - nd.x), 0.0f, 1.0f));
+            } else {
+                float a, b;
+                if (disc.x == 0.5f && disc.y == 0.5f) {
+                    a = gmix(sub.y, gclamp(nd.x - (1.0f - sub.y), 0.0f, 1.0f), gstep(-2.0f, nd.x));
+                    b = gmix(1.0f - sub.x, gclamp(nd.y - sub.x, 0.0f, 1.0f), gstep(-2.0f, nd.y));
+                    RB_RET(gmax(a, b));
+                } else if (disc.x == 0.5f && disc.y == 0.25f) {
+                    a = gmix(1.0f - sub.y, gclamp(nd.x - sub.y, 0.0f, 1.0f), gstep(-2.0f, nd.x));
+                    b = gmix(1.0f - sub.x, gclamp(nd.y - sub.x, 0.0f, 1.0f), gstep(-2.0f, nd.y));
+                    RB_RET(gmax(a, b));
+                } else if (disc.x == 0.25f && disc.y == 0.5f) {
+                    a = gmix(sub.y, gclamp(nd.x - (1.0f - sub.y), 0.0f, 1.0f), gstep(-2.0f, nd.x));
+                    b = gmix(sub.x, gclamp(nd.y - (1.0f - sub.x), 0.0f, 1.0f), gstep(-2.0f, nd.y));
+                    RB_RET(gmax(a, b));
+                } else if (disc.x == 0.25f && disc.y == 0.25f) {
+                    a = gmix(1.0f - sub.y, gclamp(nd.x - sub.y, 0.0f, 1.0f), gstep(-2.0f, nd.x));
+                    b = gmix(sub.x, gclamp(nd.y - (1.0f - sub.x), 0.0f, 1.0f), gstep(-2.0f, nd.y));
+                    RB_RET(gmax(a, b));
+                }
+            }
+        }
+        if (nd.x <= -2.0f) RB_RET(gmix(sub.y, 1.0f - sub.y, gstep(disc.y, 0.25f)));
+        if (nd.y <= -2.0f) RB_RET(gmix(1.0f - sub.x, sub.x, gstep(disc.x, 0.25f)));
+        if (disc.y > 0.0f) {
+            if (disc.y == 0.5f) RB_RET(gclamp(nd.x - (1.0f - sub.y), 0.0f, 1.0f));
+            else RB_RET(gclamp(nd.x - sub.y, 0.0f, 1.0f));
+        }
+        if (disc.x > 0.0f) {
+            if (disc.x == 0.5f) RB_RET(gclamp(nd.y - sub.x, 0.0f, 1.0f));
+            else RB_RET(gclamp(nd.y - (1.0f - sub.x), 0.0f, 1.0f));
+        }
+    }
+    RB_RET(1.0f - disc.z);
+}
+
+// RBSSM (RBSSM.frag:1202-1339, the commented-out branches left out): K x K
+// taps over the penumbra; a discontinuity tap is filled by smoothONDS.
+float rb_filter(const Ctx& c, float pw, V4 n) {
+    float illum = 0.0f;
+    const int K = c.p->kernel_size;
+    float fw = ((float)K - 1.0f) * 0.5f;
+    for (int h = (int)(-fw); (float)h <= fw; h++)
+        for (int w = (int)(-fw); (float)w <= fw; w++) {
+            V4 lc = {n.x + ((float)w * pw) / fw, n.y + ((float)h * pw) / fw, n.z, n.w};
+            V2 sub = {gfract(lc.x * (float)c.W), gfract(lc.y * (float)c.H)};
+            float d = fetch(c, lc.x, lc.y);
+            V4 disc = nc_compute_disc(c, lc, d);
+            if (disc.x > 0.0f || disc.y > 0.0f) {
+                V4 ds;
+                ds.x = rb_disc_length(c, disc, lc, V2{-1.0f, 0.0f});
+                ds.y = rb_disc_length(c, disc, lc, V2{1.0f, 0.0f});
+                ds.z = rb_disc_length(c, disc, lc, V2{0.0f, -1.0f});
+                ds.w = rb_disc_length(c, disc, lc, V2{0.0f, 1.0f});
+                V4 nd = {rb_normalize_space(c, V2{ds.x, ds.y}, sub.x),
+                         rb_normalize_space(c, V2{ds.z, ds.w}, sub.y), 0.0f, 0.0f};
+                float fill = rb_smooth_onds(c, lc, nd, disc, sub);
+                fill = gmix(fill, 1.0f, c.I);
+                illum += fill;
+            } else {
+                float shadow = (lc.z <= d) ? 1.0f : c.I;
+                illum += shadow;
+            }
+        }
+    return illum / (float)(K * K);
+}
+
+// revectorizationBasedShadowMappingSmoothing (RBSSM.frag:1341-1360).
+float rb_rbssm(const Ctx& c, V4 n) {
+    float avg = avg_blocker_grid(c, n);
+    float pw = penumbra_width(c, avg, n.z);
+    float step = 2.0f * pw / (float)c.p->kernel_size;
+    if (step <= 0.0f || step >= 1.0f) return 1.0f;
+    return rb_filter(c, pw, n);
+}
+
 // ---- RBSM/ConservativeSMSR.frag ---------------------------------------------
 V4 cs_compute_disc(const Ctx& c, V4 s) {
     V4 dir = {0, 0, 0, 0};
@@ -1018,6 +1533,9 @@ float shade_pixel(const Ctx& c, V4 vertex, V4 normal, const float* poisson) {
         case GI_TECH_RPCF_CONSERVATIVE:
             if (shadow == 1.0f) shadow = cs_rpcf(c, n);
             return shadow;
+        case GI_TECH_RBSSM:  // RBSSM.frag:1362-1376
+            if (sc.w > 0.0f && shadow == 1.0f) shadow = rb_rbssm(c, n);
+            return shadow;
         case GI_TECH_HARD_SOFTAPP: {
             float r = shadow;
             if (sc.w > 0.0f && r == 1.0f) {
@@ -1053,4 +1571,11 @@ extern "C" void or_visibility(const gi_vis_params* p, const float* depth, int ma
             V4 nn = {nrm[4 * i], nrm[4 * i + 1], nrm[4 * i + 2], nrm[4 * i + 3]};
             out[i] = shade_pixel(c, v, nn, poisson_xy);
         }
+}
+
+extern "C" void or_rbssm_hits(unsigned long long* out4096, int reset) {
+    for (int i = 0; i < 4096; ++i) {
+        if (out4096) out4096[i] = g_rb_hits[i].load();
+        if (reset) g_rb_hits[i].store(0);
+    }
 }

@@ -57,6 +57,10 @@ void or_shadow_volume_counts(const float* points, const float* normals,
                              int depth_func, uint8_t* out_stencil,
                              float* out_depth, int threads);
 
+/* Hit counts of the return sites of the RBSSM smoothONDS restatement,
+ * indexed by source line modulo 4096 (test coverage only). */
+void or_rbssm_hits(unsigned long long* out4096, int reset);
+
 #ifdef __cplusplus
 }
 #endif

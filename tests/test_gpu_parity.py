@@ -82,7 +82,8 @@ def test_gbuffer_bit_exact(cuda_ctx, dims):
 
 TECHS = [api.GI_TECH_HARD, api.GI_TECH_PCF, api.GI_TECH_PCF_TRICUBIC, api.GI_TECH_PCSS_GRID,
          api.GI_TECH_PCSS_POISSON, api.GI_TECH_SMSR_CONSERVATIVE, api.GI_TECH_SMSR_NONCONSERVATIVE,
-         api.GI_TECH_RPCF_CONSERVATIVE, api.GI_TECH_RPCF_SMSR, api.GI_TECH_RSMSS, api.GI_TECH_HARD_SOFTAPP]
+         api.GI_TECH_RPCF_CONSERVATIVE, api.GI_TECH_RPCF_SMSR, api.GI_TECH_RSMSS, api.GI_TECH_HARD_SOFTAPP,
+         api.GI_TECH_RBSSM]
 
 
 def _vis_params(w, tech):

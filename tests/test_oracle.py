@@ -213,3 +213,81 @@ def test_shadow_volume_counts_match_a_ray_test():
             checked += 1
     assert checked > 2000
     assert (st != 0).sum() > 100
+
+
+def _rbssm_kw(**extra):
+    kw = dict(light_radius=8.0, kernel_size=7, blocker_search_size=7, max_search=16, depth_threshold=0.0,
+              pcss_min_blocker_depth=0.0)
+    kw.update(extra)
+    return kw
+
+
+def test_rbssm_lit_and_umbra():
+    S = 64
+    # no blocker anywhere: average depth 1, negative penumbra, lit
+    assert _probe(api.GI_TECH_RBSSM, np.ones(S * S, np.float32), S, 0.5, 0.5, 0.9995, **_rbssm_kw()) == 1.0
+    # a uniform blocker plane: every tap is shadowed and none is a discontinuity
+    m = np.full(S * S, 0.995, np.float32)
+    assert _probe(api.GI_TECH_RBSSM, m, S, 0.5, 0.5, 0.9995, **_rbssm_kw()) == 0.25
+    # the reference's 0.99 cut-off on the average blocker depth returns 0 -> lit
+    m = np.full(S * S, 0.5, np.float32)
+    assert _probe(api.GI_TECH_RBSSM, m, S, 0.5, 0.5, 0.9, **_rbssm_kw(pcss_min_blocker_depth=0.99)) == 1.0
+
+
+def test_rbssm_straight_edge_known_answer():
+    # Vertical edge: texels x < 32 hold blockers at 0.995, the rest is lit.
+    # On an axis-aligned edge every discontinuity tap is filled binary:
+    # an entering tap (lit, shadowed left neighbour) gets 1, an exiting tap
+    # (shadowed, lit right neighbour) gets 0, so the result is the count of
+    # lit taps over K^2 with shadowed taps weighted by the intensity 0.25.
+    S, z = 64, np.float32(0.999)
+    m = np.ones((S, S), np.float32)
+    m[:, :32] = 0.995
+    s = t = np.float32(32.5 / S)
+    kw = _rbssm_kw()
+    got = _probe(api.GI_TECH_RBSSM, m.reshape(-1), S, float(s), float(t), float(z), **kw)
+    # replay the blocker search and the tap positions in FP32
+    f = np.float32
+    bsw = f(8.0) / f(S)
+    fw = f(3.0)
+    total, nb = f(0.0), 0
+    for h in range(-3, 4):
+        for w in range(-3, 4):
+            x = int(np.floor((s + (f(w) * bsw) / fw) * f(S)))
+            if x < 32:
+                total = f(total + f(0.995))
+                nb += 1
+    avg = f(total / f(nb))
+    pw = f(f(f(z - avg) / avg) * f(8.0))
+    pw = f(f(f(1.0) * pw) / z)
+    lit = sum(1 for w in range(-3, 4) if int(np.floor((s + (f(w) * pw) / fw) * f(S))) >= 32)
+    expect = f(f(7 * (lit * 1.0 + (7 - lit) * 0.25)) / f(49))
+    assert 0 < lit < 7
+    assert got == float(expect)
+
+
+def test_rbssm_corner_is_fractional():
+    S = 64
+    m = np.ones((S, S), np.float32)
+    m[:32, :32] = 0.995  # blocker quadrant
+    v = _probe(api.GI_TECH_RBSSM, m.reshape(-1), S, 32.5 / S, 32.5 / S, 0.999, **_rbssm_kw())
+    assert 0.25 < v < 1.0
+
+
+def test_rbssm_fuzz_reaches_every_reachable_case():
+    # 71 return sites; four cannot be reached: the two "fill all" returns of
+    # the both-positive case need nd <= -2 on the axis whose lengths are the
+    # early -1 returns, the r == 0.75 exit of the top/bottom case is taken by
+    # an earlier case, and the final return needs r == g == 0.
+    from rbssm_fuzz import CASES, case
+
+    sites = oracle.rbssm_return_sites()
+    assert len(sites) == 71
+    oracle.rbssm_hits(reset=True)
+    for k in range(len(CASES)):
+        p, fr, depth, pos, nrm, S, W, H = case(k)
+        v = oracle.visibility(p.to_c(fr), depth, S, S, pos, nrm, W, H)
+        assert ((v > 0.25) & (v < 1.0)).mean() > 0.3
+    hits = oracle.rbssm_hits()
+    covered = [s for s in sites if (s & 4095) in hits]
+    assert len(covered) >= len(sites) - 4, sorted(set(sites) - set(covered))
