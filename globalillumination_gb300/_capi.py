@@ -46,6 +46,8 @@ GI_TECH_RSMSS = 9
 GI_TECH_HARD_SOFTAPP = 10
 GI_TECH_RBSSM = 11
 GI_TECH_COUNT = 12
+GI_ACT_NONE = 0
+GI_ACT_RELU = 1
 
 # gi_pretest_mode
 GI_PRETEST_REFERENCE = 0
@@ -195,6 +197,22 @@ _PROTOS = {
     "gi_batch_run": (C.c_int, [_VP, _VP]),
     "gi_batch_autotune": (C.c_int, [_VP, _VP, C.c_int, C.POINTER(BatchTuning)]),
     "gi_batch_info": (C.c_int, [_VP, C.POINTER(BatchTuning)]),
+    # gi_surrogate.h
+    "gi_conv2d_bf16": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP, C.c_int, C.c_int, C.c_int, _VP,
+                                 _VP, C.c_int, C.c_int, _VP, _VP, _VP]),
+    "gi_conv2d_wgrad_scratch_floats": (C.c_size_t, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "gi_conv2d_wgrad_bf16": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP,
+                                       _VP, _VP, _VP]),
+    "gi_pack_conv_weights": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP]),
+    "gi_unpack_conv_grad": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP]),
+    "gi_maxpool2_bf16": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP]),
+    "gi_maxpool2_bwd_bf16": (C.c_int, [_VP, _VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP]),
+    "gi_upsample2_bf16": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, _VP, C.c_int, C.c_int, _VP]),
+    "gi_upsample2_bwd_bf16": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP]),
+    "gi_channel_slice_bf16": (C.c_int, [_VP, C.c_size_t, C.c_int, C.c_int, C.c_int, _VP, _VP]),
+    "gi_channel_slice_add_bf16": (C.c_int, [_VP, C.c_size_t, C.c_int, _VP, C.c_int, C.c_int, _VP]),
+    "gi_adam_f32": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
+                              C.c_float, _VP]),
 }
 
 _lib = None

@@ -37,7 +37,7 @@ def _cuda_include(nvcc: str) -> str:
 
 
 def _headers() -> list[str]:
-    hs = [os.path.join(INCLUDE, "gi_shadow.h")]
+    hs = [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
     for f in os.listdir(CSRC):
         if f.endswith((".h", ".cuh", ".inc")):
             hs.append(os.path.join(CSRC, f))

@@ -1,0 +1,864 @@
+// surrogate.cu -- tcgen05 (5th-generation tensor core) kernels of the
+// learned soft-shadow surrogate: implicit-GEMM convolution forward / data
+// gradient / weight gradient on NHWC BF16 tensors with FP32 accumulation in
+// tensor memory, plus the memory-bound pieces of the U-Net (pooling,
+// upsampling, channel slices, Adam).
+//
+// Convolution as GEMM: D[pixel, co] = sum_k A[pixel, k] * B[co, k] with
+// k = (tap, ci) in K-blocks of 8 channels.  One CTA of 128 threads owns 128
+// output pixels (M = 128) and all cout columns (N = cout <= 256).  Each
+// pipeline stage holds 4 K-blocks (32 K elements) of A (gathered with
+// zero padding by cp.async) and of B (packed weights) in shared memory, in
+// the canonical no-swizzle K-major layout: 8 x 16-byte core matrices, the
+// K-adjacent ones 128 B apart (LBO), the 8-row groups 512 B apart (SBO).
+// Thread 0 issues tcgen05.mma (kind::f16, BF16 x BF16 -> FP32) into a TMEM
+// accumulator and commits each stage to an mbarrier, which the loaders
+// wait on before refilling that stage.  The epilogue reads the
+// accumulator with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31, i.e.
+// pixels), applies bias / ReLU / ReLU-derivative mask and stores BF16
+// (and optionally FP32).
+//
+// Every wait on an mbarrier is bounded; on timeout the kernel sets bit 0 of
+// the caller's error word, still frees its tensor memory and returns.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "../../include/gi_surrogate.h"
+#include "internal.h"
+
+namespace gi {
+namespace tc {
+
+constexpr int kThreads = 128;
+constexpr int kNS = 4;          // pipeline stages
+constexpr int kBKB = 4;         // K-blocks (8 elements) per stage
+constexpr int kCore = 128;      // bytes per core matrix (8 rows x 16 B)
+constexpr int kSBO = kBKB * kCore;
+constexpr int kStageA = 16 * kSBO;  // 128 rows
+constexpr unsigned kSpinLimit = 1u << 20;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// tcgen05 shared-memory matrix descriptor: start address, leading (K)
+// and stride (M/N) byte offsets, descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B,
+// both K-major, shape M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+    const uint32_t a = smem_u32(bar);
+    for (unsigned it = 0; it < kSpinLimit; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(bar))
+                 : "memory");
+}
+
+// 16 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, int bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ uint32_t tmem_cols(int n) { return n <= 32 ? 32u : n <= 64 ? 64u : n <= 128 ? 128u : 256u; }
+
+__device__ __forceinline__ float bf16_to_f(uint16_t v) { return __uint_as_float((uint32_t)v << 16); }
+__device__ __forceinline__ uint16_t f_to_bf16(float f) { return __bfloat16_as_ushort(__float2bfloat16_rn(f)); }
+
+struct ConvArgs {
+    const uint16_t* x;
+    int n, h, w, cin;
+    const uint16_t* wt;
+    int cout, nkb, nkb_pad, ksize;
+    const float* bias;
+    int act;
+    const uint16_t* mask;
+    uint16_t* y;
+    int y_c, y_off;
+    float* y32;
+    uint32_t* err;
+    long long P;
+};
+
+__global__ void __launch_bounds__(kThreads) k_conv_fwd(ConvArgs a) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t bars[kNS];
+    __shared__ uint32_t tmem_slot;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int N = a.cout;
+    const int stage_bytes = kStageA + (N / 8) * kSBO;
+    const uint32_t ncols = tmem_cols(N);
+    if (warp == 0) tmem_alloc(&tmem_slot, ncols);
+    if (tid == 0) {
+        for (int s = 0; s < kNS; ++s) mbar_init(&bars[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_slot;
+    const long long tile0 = (long long)blockIdx.x * 128;
+    const int nk = a.nkb_pad / kBKB;
+    const int cg = a.cin / 8;
+    bool ok = true;
+
+    auto load_stage = [&](int chunk, int s) {
+        uint8_t* sa = smem + s * stage_bytes;
+        uint8_t* sb = sa + kStageA;
+        const int kb0 = chunk * kBKB;
+        for (int c = tid; c < 128 * kBKB; c += kThreads) {
+            const int m = c & 127, kl = c >> 7, kb = kb0 + kl;
+            const long long p = tile0 + m;
+            const uint16_t* src = a.x;
+            int bytes = 0;
+            if (p < a.P && kb < a.nkb) {
+                const int tap = kb / cg, g = kb - tap * cg;
+                const int dy = a.ksize == 3 ? tap / 3 - 1 : 0, dx = a.ksize == 3 ? tap % 3 - 1 : 0;
+                const int xx = (int)(p % a.w);
+                const long long t = p / a.w;
+                const int yy = (int)(t % a.h);
+                const long long img = t / a.h;
+                const int x2 = xx + dx, y2 = yy + dy;
+                if (x2 >= 0 && x2 < a.w && y2 >= 0 && y2 < a.h) {
+                    src = a.x + ((img * a.h + y2) * a.w + x2) * a.cin + g * 8;
+                    bytes = 16;
+                }
+            }
+            cp_async16(smem_u32(sa + kl * kCore + (m >> 3) * kSBO + (m & 7) * 16), src, bytes);
+        }
+        for (int c = tid; c < N * kBKB; c += kThreads) {
+            const int r = c % N, kl = c / N;
+            const uint16_t* src = a.wt + ((long long)r * a.nkb_pad + kb0 + kl) * 8;
+            cp_async16(smem_u32(sb + kl * kCore + (r >> 3) * kSBO + (r & 7) * 16), src, 16);
+        }
+    };
+
+    const uint32_t idesc = idesc_bf16(128, N);
+    for (int s = 0; s < kNS - 1; ++s) {
+        if (s < nk) load_stage(s, s);
+        cp_async_commit();
+    }
+    // Iteration i: wait for chunk i's copies, issue its MMAs, then refill
+    // the stage chunk i - 1 used (its MMAs overlap with those just issued).
+    for (int i = 0; i < nk; ++i) {
+        const int s = i % kNS;
+        cp_async_wait<kNS - 2>();
+        fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+            fence_after();
+            const uint8_t* sa = smem + s * stage_bytes;
+            const uint8_t* sb = sa + kStageA;
+#pragma unroll
+            for (int kk = 0; kk < kBKB / 2; ++kk) {
+                const uint64_t ad = smem_desc(smem_u32(sa + kk * 2 * kCore), kCore, kSBO);
+                const uint64_t bd = smem_desc(smem_u32(sb + kk * 2 * kCore), kCore, kSBO);
+                mma_bf16(tmem, ad, bd, idesc, (i > 0 || kk > 0) ? 1u : 0u);
+            }
+            mma_commit(&bars[s]);
+        }
+        const int j = i + kNS - 1;
+        if (j < nk) {
+            const int sj = j % kNS;
+            if (i >= 1) ok &= mbar_wait(&bars[sj], (unsigned)((i - 1) / kNS) & 1u);
+            load_stage(j, sj);
+        }
+        cp_async_commit();
+    }
+    const int last = nk - 1;
+    ok &= mbar_wait(&bars[last % kNS], (unsigned)(last / kNS) & 1u);
+    fence_after();
+
+    const long long p = tile0 + warp * 32 + lane;
+    const bool live = p < a.P;
+    for (int c0 = 0; c0 < N; c0 += 16) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+        if (!live) continue;
+        if (a.bias) {
+#pragma unroll
+            for (int q = 0; q < 16; ++q) v[q] += __ldg(a.bias + c0 + q);
+        }
+        if (a.act == GI_ACT_RELU) {
+#pragma unroll
+            for (int q = 0; q < 16; ++q) v[q] = fmaxf(v[q], 0.0f);
+        }
+        const long long o = p * a.y_c + a.y_off + c0;
+        if (a.mask) {
+            const uint4* mp = reinterpret_cast<const uint4*>(a.mask + o);
+            uint4 m0 = __ldg(mp), m1 = __ldg(mp + 1);
+            const uint32_t mw[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const uint16_t mv = (uint16_t)(mw[q >> 1] >> ((q & 1) * 16));
+                if (!(bf16_to_f(mv) > 0.0f)) v[q] = 0.0f;
+            }
+        }
+        if (a.y32) {
+            float4* yp = reinterpret_cast<float4*>(a.y32 + p * N + c0);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) yp[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        }
+        if (a.y) {
+            uint32_t pk[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                pk[q] = (uint32_t)f_to_bf16(v[2 * q]) | ((uint32_t)f_to_bf16(v[2 * q + 1]) << 16);
+            uint4* yp = reinterpret_cast<uint4*>(a.y + o);
+            yp[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            yp[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, ncols);
+    if (!ok && tid == 0 && a.err) atomicOr(a.err, 1u);
+}
+
+// ---- weight gradient ---------------------------------------------------------
+// D[r, co] = sum_p A[r, p] * B[co, p] with r = (K-block, channel) of the
+// forward K and p the pixels of this CTA's split.  Both operands are
+// staged transposed (pixels along K): a thread loads 8 pixels x 8 channels
+// (8 x 16 B) and writes the 8 x 8 block back as one core matrix.
+struct WgradArgs {
+    const uint16_t* x;
+    const uint16_t* dy;
+    int n, h, w, cin, cout, ksize, nkb, m_tiles;
+    long long P, px_per_split;
+    float* scratch;
+    uint32_t* err;
+};
+
+__device__ __forceinline__ void transpose8(const uint4 (&in)[8], uint4 (&out)[8]) {
+    const uint32_t* w = reinterpret_cast<const uint32_t*>(in);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const uint32_t sel = (j & 1) ? 0x7632u : 0x5410u;
+        uint32_t o[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) o[k] = __byte_perm(w[(2 * k) * 4 + (j >> 1)], w[(2 * k + 1) * 4 + (j >> 1)], sel);
+        out[j] = make_uint4(o[0], o[1], o[2], o[3]);
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_conv_wgrad(WgradArgs a) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t bars[kNS];
+    __shared__ uint32_t tmem_slot;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int N = a.cout;
+    const int stage_bytes = kStageA + (N / 8) * kSBO;
+    const uint32_t ncols = tmem_cols(N);
+    const int mt = blockIdx.x;
+    const long long p_begin = (long long)blockIdx.y * a.px_per_split;
+    const long long p_end = min(a.P, p_begin + a.px_per_split);
+    if (warp == 0) tmem_alloc(&tmem_slot, ncols);
+    if (tid == 0) {
+        for (int s = 0; s < kNS; ++s) mbar_init(&bars[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_slot;
+    const int cg = a.cin / 8;
+    const long long span = p_end > p_begin ? p_end - p_begin : 0;
+    const int nk = (int)((span + 8 * kBKB - 1) / (8 * kBKB));
+    bool ok = true;
+
+    auto load_stage = [&](int chunk, int s) {
+        uint8_t* sa = smem + s * stage_bytes;
+        uint8_t* sb = sa + kStageA;
+        const long long pc = p_begin + (long long)chunk * 8 * kBKB;
+        const int na = 16 * kBKB, nb = (N / 8) * kBKB;
+        for (int task = tid; task < na + nb; task += kThreads) {
+            uint4 in[8], out[8];
+            const bool is_a = task < na;
+            const int t = is_a ? task : task - na;
+            const int rg = t / kBKB, q = t % kBKB;
+            const long long p0 = pc + q * 8;
+            if (is_a) {
+                const int kb = mt * 16 + rg;
+                int tap = 0, g = 0, dy = 0, dx = 0;
+                const bool kb_ok = kb < a.nkb;
+                if (kb_ok) {
+                    tap = kb / cg;
+                    g = kb - tap * cg;
+                    if (a.ksize == 3) {
+                        dy = tap / 3 - 1;
+                        dx = tap % 3 - 1;
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    in[i] = make_uint4(0, 0, 0, 0);
+                    const long long p = p0 + i;
+                    if (kb_ok && p < p_end) {
+                        const int xx = (int)(p % a.w);
+                        const long long tt = p / a.w;
+                        const int yy = (int)(tt % a.h);
+                        const long long img = tt / a.h;
+                        const int x2 = xx + dx, y2 = yy + dy;
+                        if (x2 >= 0 && x2 < a.w && y2 >= 0 && y2 < a.h)
+                            in[i] = __ldg(reinterpret_cast<const uint4*>(a.x + ((img * a.h + y2) * a.w + x2) * a.cin + g * 8));
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    in[i] = make_uint4(0, 0, 0, 0);
+                    const long long p = p0 + i;
+                    if (p < p_end) in[i] = __ldg(reinterpret_cast<const uint4*>(a.dy + p * a.cout + rg * 8));
+                }
+            }
+            transpose8(in, out);
+            uint8_t* dst = (is_a ? sa : sb) + q * kCore + rg * kSBO;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) *reinterpret_cast<uint4*>(dst + j * 16) = out[j];
+        }
+    };
+
+    const uint32_t idesc = idesc_bf16(128, N);
+    for (int s = 0; s < kNS - 1; ++s)
+        if (s < nk) load_stage(s, s);
+    for (int i = 0; i < nk; ++i) {
+        const int s = i % kNS;
+        fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+            fence_after();
+            const uint8_t* sa = smem + s * stage_bytes;
+            const uint8_t* sb = sa + kStageA;
+#pragma unroll
+            for (int kk = 0; kk < kBKB / 2; ++kk) {
+                const uint64_t ad = smem_desc(smem_u32(sa + kk * 2 * kCore), kCore, kSBO);
+                const uint64_t bd = smem_desc(smem_u32(sb + kk * 2 * kCore), kCore, kSBO);
+                mma_bf16(tmem, ad, bd, idesc, (i > 0 || kk > 0) ? 1u : 0u);
+            }
+            mma_commit(&bars[s]);
+        }
+        const int j = i + kNS - 1;
+        if (j < nk) {
+            const int sj = j % kNS;
+            if (i >= 1) ok &= mbar_wait(&bars[sj], (unsigned)((i - 1) / kNS) & 1u);
+            load_stage(j, sj);
+        }
+    }
+    if (nk > 0) {
+        const int last = nk - 1;
+        ok &= mbar_wait(&bars[last % kNS], (unsigned)(last / kNS) & 1u);
+    }
+    fence_after();
+    const long long row = ((long long)blockIdx.y * a.m_tiles + mt) * 128 + warp * 32 + lane;
+    for (int c0 = 0; c0 < N; c0 += 16) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+        if (nk == 0) {
+#pragma unroll
+            for (int q = 0; q < 16; ++q) v[q] = 0.0f;
+        }
+        float4* o = reinterpret_cast<float4*>(a.scratch + row * N + c0);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, ncols);
+    if (!ok && tid == 0 && a.err) atomicOr(a.err, 1u);
+}
+
+// dw[co][r] += sum over splits of scratch[split][r][co], r < 8 * nkb.
+__global__ void k_wgrad_reduce(const float* __restrict__ scratch, int splits, int m_tiles, int cout, int nkb,
+                               int nkb_pad, float* __restrict__ dw) {
+    const long long total = (long long)8 * nkb * cout;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int co = (int)(i % cout);
+        const long long r = i / cout;
+        float s = 0.0f;
+        for (int k = 0; k < splits; ++k) s += scratch[((long long)k * m_tiles * 128 + r) * cout + co];
+        dw[(long long)co * nkb_pad * 8 + r] += s;
+    }
+}
+
+// db[co] += sum_p dy[p][co]
+__global__ void k_bias_grad(const uint16_t* __restrict__ dy, long long P, int cout, float* __restrict__ db) {
+    __shared__ float acc[256];
+    for (int c = threadIdx.x; c < cout; c += blockDim.x) acc[c] = 0.0f;
+    __syncthreads();
+    const int c = threadIdx.x % cout;
+    const int rows = blockDim.x / cout;
+    const int r0 = threadIdx.x / cout;
+    float s = 0.0f;
+    if (r0 < rows)
+        for (long long p = blockIdx.x * (long long)rows + r0; p < P; p += (long long)gridDim.x * rows)
+            s += bf16_to_f(dy[p * cout + c]);
+    if (r0 < rows) atomicAdd(&acc[c], s);
+    __syncthreads();
+    for (int k = threadIdx.x; k < cout; k += blockDim.x) atomicAdd(db + k, acc[k]);
+}
+
+__global__ void k_pack_weights(const float* __restrict__ w, int cout, int cin_real, int cin, int ks, int flip,
+                               int nkb_pad, uint16_t* __restrict__ out) {
+    // out rows: the packed conv's output channels (cout, or cin when flipped)
+    const int rows = flip ? cin : cout;
+    const int kin = flip ? cout : cin;  // packed conv's input channels
+    const long long total = (long long)rows * nkb_pad * 8;
+    const int cgk = kin / 8;
+    const int taps = ks * ks;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(i % 8);
+        const long long t = i / 8;
+        const int kb = (int)(t % nkb_pad);
+        const int r = (int)(t / nkb_pad);
+        float v = 0.0f;
+        if (kb < taps * cgk) {
+            const int tap = kb / cgk, g = kb % cgk;
+            const int k = g * 8 + j;  // packed conv's input channel
+            if (!flip) {
+                if (k < cin_real) v = w[(((long long)r * cin_real + k) * ks + tap / ks) * ks + tap % ks];
+            } else {
+                // dX[ci] = sum_co W[co][ci][taps-1-tap] dY[co]: row r = ci, k = co
+                const int src_tap = taps - 1 - tap;
+                if (r < cin_real) v = w[(((long long)k * cin_real + r) * ks + src_tap / ks) * ks + src_tap % ks];
+            }
+        }
+        out[i] = f_to_bf16(v);
+    }
+}
+
+__global__ void k_unpack_grad(const float* __restrict__ dwp, int cout, int cin_real, int cin, int ks, int nkb_pad,
+                              float* __restrict__ out) {
+    const long long total = (long long)cout * cin_real * ks * ks;
+    const int cg = cin / 8;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int kx = (int)(i % ks);
+        const int ky = (int)((i / ks) % ks);
+        const int ci = (int)((i / (ks * ks)) % cin_real);
+        const int co = (int)(i / ((long long)ks * ks * cin_real));
+        const int tap = ky * ks + kx;
+        const int kb = tap * cg + ci / 8;
+        out[i] = dwp[((long long)co * nkb_pad + kb) * 8 + ci % 8];
+    }
+}
+
+__global__ void k_maxpool2(const uint16_t* __restrict__ x, int n, int h, int w, int c, uint16_t* __restrict__ y) {
+    const int ho = h / 2, wo = w / 2;
+    const long long total = (long long)n * ho * wo * c;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int ch = (int)(i % c);
+        const long long pix = i / c;
+        const int xo = (int)(pix % wo);
+        const int yo = (int)((pix / wo) % ho);
+        const long long img = pix / ((long long)wo * ho);
+        const long long b = ((img * h + 2 * yo) * w + 2 * xo) * c + ch;
+        float m = bf16_to_f(x[b]);
+        m = fmaxf(m, bf16_to_f(x[b + c]));
+        m = fmaxf(m, bf16_to_f(x[b + (long long)w * c]));
+        m = fmaxf(m, bf16_to_f(x[b + (long long)w * c + c]));
+        y[i] = f_to_bf16(m);
+    }
+}
+
+__global__ void k_maxpool2_bwd(const uint16_t* __restrict__ x, const uint16_t* __restrict__ y,
+                               const uint16_t* __restrict__ dy, int n, int h, int w, int c, uint16_t* __restrict__ dx) {
+    const int ho = h / 2, wo = w / 2;
+    const long long total = (long long)n * ho * wo * c;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int ch = (int)(i % c);
+        const long long pix = i / c;
+        const int xo = (int)(pix % wo);
+        const int yo = (int)((pix / wo) % ho);
+        const long long img = pix / ((long long)wo * ho);
+        const long long b = ((img * h + 2 * yo) * w + 2 * xo) * c + ch;
+        const long long off[4] = {0, c, (long long)w * c, (long long)w * c + c};
+        const uint16_t ym = y[i], g = dy[i];
+        bool taken = false;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const bool hit = !taken && x[b + off[k]] == ym;
+            dx[b + off[k]] = hit ? g : (uint16_t)0;
+            taken |= hit;
+        }
+    }
+}
+
+__global__ void k_upsample2(const uint16_t* __restrict__ x, int n, int h, int w, int c, uint16_t* __restrict__ y,
+                            int ys, int yoff) {
+    const int H = 2 * h, W = 2 * w;
+    const long long total = (long long)n * H * W * (c / 8);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int g = (int)(i % (c / 8));
+        const long long pix = i / (c / 8);
+        const int X = (int)(pix % W);
+        const int Y = (int)((pix / W) % H);
+        const long long img = pix / ((long long)W * H);
+        const uint4 v = *reinterpret_cast<const uint4*>(x + ((img * h + Y / 2) * w + X / 2) * c + g * 8);
+        *reinterpret_cast<uint4*>(y + pix * ys + yoff + g * 8) = v;
+    }
+}
+
+__global__ void k_upsample2_bwd(const uint16_t* __restrict__ dy, int n, int h, int w, int c, int ds, int doff,
+                                uint16_t* __restrict__ dx) {
+    const int W = 2 * w;
+    const long long total = (long long)n * h * w * c;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int ch = (int)(i % c);
+        const long long pix = i / c;
+        const int xx = (int)(pix % w);
+        const int yy = (int)((pix / w) % h);
+        const long long img = pix / ((long long)w * h);
+        const long long b = ((img * 2 * h + 2 * yy) * W + 2 * xx);
+        float s = bf16_to_f(dy[b * ds + doff + ch]) + bf16_to_f(dy[(b + 1) * ds + doff + ch]) +
+                  bf16_to_f(dy[(b + W) * ds + doff + ch]) + bf16_to_f(dy[(b + W + 1) * ds + doff + ch]);
+        dx[i] = f_to_bf16(s);
+    }
+}
+
+__global__ void k_slice(const uint16_t* __restrict__ x, long long pixels, int stride, int off, int c,
+                        uint16_t* __restrict__ y) {
+    const long long total = pixels * (c / 8);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int g = (int)(i % (c / 8));
+        const long long p = i / (c / 8);
+        *reinterpret_cast<uint4*>(y + p * c + g * 8) = *reinterpret_cast<const uint4*>(x + p * stride + off + g * 8);
+    }
+}
+
+__global__ void k_slice_add(const uint16_t* __restrict__ x, long long pixels, int c, uint16_t* __restrict__ y,
+                            int stride, int off) {
+    const long long total = pixels * c;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int ch = (int)(i % c);
+        const long long p = i / c;
+        uint16_t* d = y + p * stride + off + ch;
+        *d = f_to_bf16(bf16_to_f(*d) + bf16_to_f(x[i]));
+    }
+}
+
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, long long n, float lr, float b1, float b2, float eps, float c1,
+                       float c2, float gs) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float gi = g[i] * gs;
+        const float mi = b1 * m[i] + (1.0f - b1) * gi;
+        const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    }
+}
+
+unsigned grid1d(long long n, int threads) {
+    long long b = (n + threads - 1) / threads;
+    return (unsigned)std::max<long long>(1, std::min<long long>(b, 152LL * 16));
+}
+
+int nkb_of(int cin, int ks) { return ks * ks * cin / 8; }
+int nkb_pad_of(int cin, int ks) { return (nkb_of(cin, ks) + kBKB - 1) / kBKB * kBKB; }
+
+}  // namespace tc
+}  // namespace gi
+
+using gi::fail;
+using gi::fail_cuda;
+namespace tc = gi::tc;
+
+extern "C" gi_status gi_conv2d_bf16(const gi_bf16* x, int n, int h, int w, int cin, const gi_bf16* wt,
+                                    const float* bias, int cout, int ksize, int act, const gi_bf16* mask,
+                                    gi_bf16* y, int y_stride, int y_off, float* y32, uint32_t* err,
+                                    void* stream) {
+    if (!x || !wt || (!y && !y32)) return fail(GI_ERR_INVALID_ARG, "gi_conv2d_bf16: NULL argument");
+    if (n < 1 || h < 1 || w < 1 || cin < 8 || cin % 8 || cout < 16 || cout > 256 || cout % 16 ||
+        (ksize != 1 && ksize != 3) || (act != GI_ACT_NONE && act != GI_ACT_RELU))
+        return fail(GI_ERR_INVALID_ARG, "gi_conv2d_bf16: bad shape (cin % 8, cout % 16 in [16, 256], ksize 1|3)");
+    if (y && (y_stride % 8 || y_off % 8 || y_off + cout > y_stride))
+        return fail(GI_ERR_INVALID_ARG, "gi_conv2d_bf16: y_stride / y_off must be multiples of 8 and fit cout");
+    if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(wt) | reinterpret_cast<uintptr_t>(y) |
+         reinterpret_cast<uintptr_t>(mask) | reinterpret_cast<uintptr_t>(y32)) % 16)
+        return fail(GI_ERR_INVALID_ARG, "gi_conv2d_bf16: tensors must be 16-byte aligned");
+    tc::ConvArgs a;
+    a.x = x;
+    a.n = n;
+    a.h = h;
+    a.w = w;
+    a.cin = cin;
+    a.wt = wt;
+    a.cout = cout;
+    a.nkb = tc::nkb_of(cin, ksize);
+    a.nkb_pad = tc::nkb_pad_of(cin, ksize);
+    a.ksize = ksize;
+    a.bias = bias;
+    a.act = act;
+    a.mask = mask;
+    a.y = y;
+    a.y_c = y ? y_stride : cout;
+    a.y_off = y ? y_off : 0;
+    a.y32 = y32;
+    a.err = err;
+    a.P = (long long)n * h * w;
+    const int smem = tc::kNS * (tc::kStageA + (cout / 8) * tc::kSBO);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(tc::k_conv_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * (8192 + 16384));
+        attr_set = true;
+    }
+    const long long tiles = (a.P + 127) / 128;
+    if (tiles > 0x7FFFFFFFLL) return fail(GI_ERR_INVALID_ARG, "gi_conv2d_bf16: too many pixels");
+    tc::k_conv_fwd<<<(unsigned)tiles, tc::kThreads, smem, static_cast<cudaStream_t>(stream)>>>(a);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_conv2d_bf16 launch");
+}
+
+namespace {
+struct WgradPlan {
+    int m_tiles, splits;
+    long long px_per_split;
+};
+WgradPlan wgrad_plan(long long P, int cin, int ks) {
+    WgradPlan pl;
+    pl.m_tiles = (tc::nkb_of(cin, ks) * 8 + 127) / 128;
+    const long long target = 2LL * 152;
+    long long splits = std::max<long long>(1, (target + pl.m_tiles - 1) / pl.m_tiles);
+    splits = std::min<long long>(splits, std::max<long long>(1, (P + 1023) / 1024));
+    long long per = (P + splits - 1) / splits;
+    per = (per + 31) / 32 * 32;
+    pl.px_per_split = std::max<long long>(per, 32);
+    pl.splits = (int)((P + pl.px_per_split - 1) / pl.px_per_split);
+    if (pl.splits < 1) pl.splits = 1;
+    return pl;
+}
+}  // namespace
+
+extern "C" size_t gi_conv2d_wgrad_scratch_floats(int n, int h, int w, int cin, int cout, int ksize) {
+    if (n < 1 || h < 1 || w < 1 || cin < 8 || cout < 16) return 0;
+    WgradPlan pl = wgrad_plan((long long)n * h * w, cin, ksize);
+    return (size_t)pl.splits * pl.m_tiles * 128 * cout;
+}
+
+extern "C" gi_status gi_conv2d_wgrad_bf16(const gi_bf16* x, const gi_bf16* dy, int n, int h, int w, int cin,
+                                          int cout, int ksize, float* dw, float* db, float* scratch,
+                                          uint32_t* err, void* stream) {
+    if (!x || !dy || !dw || !scratch) return fail(GI_ERR_INVALID_ARG, "gi_conv2d_wgrad_bf16: NULL argument");
+    if (n < 1 || h < 1 || w < 1 || cin < 8 || cin % 8 || cout < 16 || cout > 256 || cout % 16 ||
+        (ksize != 1 && ksize != 3))
+        return fail(GI_ERR_INVALID_ARG, "gi_conv2d_wgrad_bf16: bad shape");
+    if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(dy) | reinterpret_cast<uintptr_t>(scratch)) % 16)
+        return fail(GI_ERR_INVALID_ARG, "gi_conv2d_wgrad_bf16: tensors must be 16-byte aligned");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const long long P = (long long)n * h * w;
+    WgradPlan pl = wgrad_plan(P, cin, ksize);
+    tc::WgradArgs a;
+    a.x = x;
+    a.dy = dy;
+    a.n = n;
+    a.h = h;
+    a.w = w;
+    a.cin = cin;
+    a.cout = cout;
+    a.ksize = ksize;
+    a.nkb = tc::nkb_of(cin, ksize);
+    a.m_tiles = pl.m_tiles;
+    a.P = P;
+    a.px_per_split = pl.px_per_split;
+    a.scratch = scratch;
+    a.err = err;
+    const int smem = tc::kNS * (tc::kStageA + (cout / 8) * tc::kSBO);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(tc::k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * (8192 + 16384));
+        attr_set = true;
+    }
+    tc::k_conv_wgrad<<<dim3(pl.m_tiles, pl.splits), tc::kThreads, smem, st>>>(a);
+    const long long red = (long long)8 * a.nkb * cout;
+    tc::k_wgrad_reduce<<<tc::grid1d(red, 256), 256, 0, st>>>(scratch, pl.splits, pl.m_tiles, cout, a.nkb,
+                                                            tc::nkb_pad_of(cin, ksize), dw);
+    if (db) tc::k_bias_grad<<<std::min<long long>(1216, (P + 63) / 64), 256, 0, st>>>(dy, P, cout, db);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_conv2d_wgrad_bf16 launch");
+}
+
+extern "C" gi_status gi_pack_conv_weights(const float* w, int cout, int cin_real, int cin, int ksize, int flip,
+                                          gi_bf16* out, void* stream) {
+    if (!w || !out || cout < 1 || cin_real < 1 || cin_real > cin || cin % 8 || (ksize != 1 && ksize != 3))
+        return fail(GI_ERR_INVALID_ARG, "gi_pack_conv_weights: bad arguments");
+    if (flip && cout % 8) return fail(GI_ERR_INVALID_ARG, "gi_pack_conv_weights: flip needs cout % 8 == 0");
+    const int kin = flip ? cout : cin;
+    const int rows = flip ? cin : cout;
+    const int nkb_pad = tc::nkb_pad_of(kin, ksize);
+    const long long total = (long long)rows * nkb_pad * 8;
+    tc::k_pack_weights<<<tc::grid1d(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        w, cout, cin_real, cin, ksize, flip, nkb_pad, out);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_pack_conv_weights launch");
+}
+
+extern "C" gi_status gi_unpack_conv_grad(const float* dw_packed, int cout, int cin_real, int cin, int ksize,
+                                         float* out, void* stream) {
+    if (!dw_packed || !out || cin % 8 || cin_real > cin || (ksize != 1 && ksize != 3))
+        return fail(GI_ERR_INVALID_ARG, "gi_unpack_conv_grad: bad arguments");
+    const long long total = (long long)cout * cin_real * ksize * ksize;
+    tc::k_unpack_grad<<<tc::grid1d(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        dw_packed, cout, cin_real, cin, ksize, tc::nkb_pad_of(cin, ksize), out);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_unpack_conv_grad launch");
+}
+
+extern "C" gi_status gi_maxpool2_bf16(const gi_bf16* x, int n, int h, int w, int c, gi_bf16* y, void* stream) {
+    if (!x || !y || h % 2 || w % 2 || c < 1) return fail(GI_ERR_INVALID_ARG, "gi_maxpool2_bf16: bad arguments");
+    const long long total = (long long)n * (h / 2) * (w / 2) * c;
+    tc::k_maxpool2<<<tc::grid1d(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, n, h, w, c, y);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_maxpool2_bf16 launch");
+}
+
+extern "C" gi_status gi_maxpool2_bwd_bf16(const gi_bf16* x, const gi_bf16* y, const gi_bf16* dy, int n, int h,
+                                          int w, int c, gi_bf16* dx, void* stream) {
+    if (!x || !y || !dy || !dx || h % 2 || w % 2) return fail(GI_ERR_INVALID_ARG, "gi_maxpool2_bwd_bf16: bad arguments");
+    const long long total = (long long)n * (h / 2) * (w / 2) * c;
+    tc::k_maxpool2_bwd<<<tc::grid1d(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, y, dy, n, h, w, c,
+                                                                                            dx);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_maxpool2_bwd_bf16 launch");
+}
+
+extern "C" gi_status gi_upsample2_bf16(const gi_bf16* x, int n, int h, int w, int c, gi_bf16* y, int y_stride,
+                                       int y_off, void* stream) {
+    if (!x || !y || c % 8 || y_stride % 8 || y_off % 8 || y_off + c > y_stride)
+        return fail(GI_ERR_INVALID_ARG, "gi_upsample2_bf16: bad arguments");
+    const long long total = (long long)n * 4 * h * w * (c / 8);
+    tc::k_upsample2<<<tc::grid1d(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, n, h, w, c, y,
+                                                                                         y_stride, y_off);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_upsample2_bf16 launch");
+}
+
+extern "C" gi_status gi_upsample2_bwd_bf16(const gi_bf16* dy, int n, int h, int w, int c, int dy_stride,
+                                           int dy_off, gi_bf16* dx, void* stream) {
+    if (!dy || !dx || dy_off + c > dy_stride) return fail(GI_ERR_INVALID_ARG, "gi_upsample2_bwd_bf16: bad arguments");
+    const long long total = (long long)n * h * w * c;
+    tc::k_upsample2_bwd<<<tc::grid1d(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(dy, n, h, w, c,
+                                                                                             dy_stride, dy_off, dx);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_upsample2_bwd_bf16 launch");
+}
+
+extern "C" gi_status gi_channel_slice_bf16(const gi_bf16* x, size_t pixels, int stride, int off, int c, gi_bf16* y,
+                                           void* stream) {
+    if (!x || !y || c % 8 || stride % 8 || off % 8 || off + c > stride)
+        return fail(GI_ERR_INVALID_ARG, "gi_channel_slice_bf16: bad arguments");
+    const long long total = (long long)pixels * (c / 8);
+    tc::k_slice<<<tc::grid1d(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, (long long)pixels, stride,
+                                                                                     off, c, y);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_channel_slice_bf16 launch");
+}
+
+extern "C" gi_status gi_channel_slice_add_bf16(const gi_bf16* x, size_t pixels, int c, gi_bf16* y, int stride,
+                                               int off, void* stream) {
+    if (!x || !y || off + c > stride) return fail(GI_ERR_INVALID_ARG, "gi_channel_slice_add_bf16: bad arguments");
+    const long long total = (long long)pixels * c;
+    tc::k_slice_add<<<tc::grid1d(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, (long long)pixels, c,
+                                                                                          y, stride, off);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_channel_slice_add_bf16 launch");
+}
+
+extern "C" gi_status gi_adam_f32(float* p, const float* g, float* m, float* v, size_t n, float lr, float beta1,
+                                 float beta2, float eps, int step, float grad_scale, void* stream) {
+    if (!p || !g || !m || !v || step < 1) return fail(GI_ERR_INVALID_ARG, "gi_adam_f32: bad arguments");
+    const float c1 = 1.0f - powf(beta1, (float)step);
+    const float c2 = 1.0f - powf(beta2, (float)step);
+    tc::k_adam<<<tc::grid1d((long long)n, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        p, g, m, v, (long long)n, lr, beta1, beta2, eps, c1, c2, grad_scale);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_adam_f32 launch");
+}

@@ -1,0 +1,123 @@
+"""Thin torch wrappers over the tcgen05 convolution kernels (gi_surrogate.h).
+
+Tensors are NHWC CUDA tensors; BF16 tensors are torch.bfloat16 (same bits
+as the C ABI's uint16 BF16).  Nothing here computes on its own: every
+function is one C ABI call on the current stream, so the CUDA extension
+must be loaded (there is no fallback).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _capi as api
+from ._capi import check
+
+
+def _lib():
+    return api.load()
+
+
+def _p(t) -> C.c_void_p:
+    return C.c_void_p(int(t.data_ptr())) if t is not None else None
+
+
+def _s() -> C.c_void_p:
+    return C.c_void_p(int(torch.cuda.current_stream().cuda_stream))
+
+
+def nkb_pad(cin: int, ksize: int) -> int:
+    nkb = ksize * ksize * cin // 8
+    return (nkb + 3) // 4 * 4
+
+
+def pack_weights(w: torch.Tensor, cin: int, flip: bool = False) -> torch.Tensor:
+    """FP32 [cout, cin_real, k, k] -> packed BF16 ([cout or cin] x kblocks x 8)."""
+    cout, cin_real, k, _ = w.shape
+    kin = cout if flip else cin
+    rows = cin if flip else cout
+    out = torch.empty((rows, nkb_pad(kin, k), 8), dtype=torch.bfloat16, device=w.device)
+    check(_lib().gi_pack_conv_weights(_p(w.contiguous()), cout, cin_real, cin, k, 1 if flip else 0, _p(out), _s()),
+          "gi_pack_conv_weights")
+    return out
+
+
+def unpack_grad(dw_packed: torch.Tensor, cout: int, cin_real: int, cin: int, k: int) -> torch.Tensor:
+    out = torch.empty((cout, cin_real, k, k), dtype=torch.float32, device=dw_packed.device)
+    check(_lib().gi_unpack_conv_grad(_p(dw_packed), cout, cin_real, cin, k, _p(out), _s()), "gi_unpack_conv_grad")
+    return out
+
+
+def conv2d(x: torch.Tensor, wp: torch.Tensor, cout: int, ksize: int, bias: torch.Tensor | None = None,
+           relu: bool = False, mask: torch.Tensor | None = None, out: torch.Tensor | None = None, out_off: int = 0,
+           out32: torch.Tensor | None = None, err: torch.Tensor | None = None) -> torch.Tensor:
+    """NHWC BF16 convolution (stride 1, zero padding) on the tensor cores."""
+    n, h, w, cin = x.shape
+    if out is None and out32 is None:
+        out = torch.empty((n, h, w, cout), dtype=torch.bfloat16, device=x.device)
+    stride = out.shape[-1] if out is not None else cout
+    check(_lib().gi_conv2d_bf16(_p(x), n, h, w, cin, _p(wp), _p(bias), cout, ksize,
+                                api.GI_ACT_RELU if relu else api.GI_ACT_NONE, _p(mask), _p(out), stride, out_off,
+                                _p(out32), _p(err), _s()), "gi_conv2d_bf16")
+    return out if out is not None else out32
+
+
+def conv2d_wgrad(x: torch.Tensor, dy: torch.Tensor, cout: int, ksize: int, dw: torch.Tensor,
+                 db: torch.Tensor | None = None, scratch: torch.Tensor | None = None,
+                 err: torch.Tensor | None = None) -> torch.Tensor:
+    """dw (FP32, packed layout) += weight gradient; db += bias gradient."""
+    n, h, w, cin = x.shape
+    need = int(_lib().gi_conv2d_wgrad_scratch_floats(n, h, w, cin, cout, ksize))
+    if scratch is None or scratch.numel() < need:
+        scratch = torch.empty(need, dtype=torch.float32, device=x.device)
+    check(_lib().gi_conv2d_wgrad_bf16(_p(x), _p(dy), n, h, w, cin, cout, ksize, _p(dw), _p(db), _p(scratch), _p(err),
+                                      _s()), "gi_conv2d_wgrad_bf16")
+    return scratch
+
+
+def maxpool2(x: torch.Tensor) -> torch.Tensor:
+    n, h, w, c = x.shape
+    y = torch.empty((n, h // 2, w // 2, c), dtype=x.dtype, device=x.device)
+    check(_lib().gi_maxpool2_bf16(_p(x), n, h, w, c, _p(y), _s()), "gi_maxpool2_bf16")
+    return y
+
+
+def maxpool2_bwd(x: torch.Tensor, y: torch.Tensor, dy: torch.Tensor) -> torch.Tensor:
+    n, h, w, c = x.shape
+    dx = torch.empty_like(x)
+    check(_lib().gi_maxpool2_bwd_bf16(_p(x), _p(y), _p(dy), n, h, w, c, _p(dx), _s()), "gi_maxpool2_bwd_bf16")
+    return dx
+
+
+def upsample2(x: torch.Tensor, out: torch.Tensor, out_off: int = 0) -> torch.Tensor:
+    n, h, w, c = x.shape
+    check(_lib().gi_upsample2_bf16(_p(x), n, h, w, c, _p(out), out.shape[-1], out_off, _s()), "gi_upsample2_bf16")
+    return out
+
+
+def upsample2_bwd(dy: torch.Tensor, c: int, off: int = 0) -> torch.Tensor:
+    n, H, W, cs = dy.shape
+    dx = torch.empty((n, H // 2, W // 2, c), dtype=dy.dtype, device=dy.device)
+    check(_lib().gi_upsample2_bwd_bf16(_p(dy), n, H // 2, W // 2, c, cs, off, _p(dx), _s()), "gi_upsample2_bwd_bf16")
+    return dx
+
+
+def channel_slice(x: torch.Tensor, off: int, c: int) -> torch.Tensor:
+    pixels = x.numel() // x.shape[-1]
+    y = torch.empty(x.shape[:-1] + (c,), dtype=x.dtype, device=x.device)
+    check(_lib().gi_channel_slice_bf16(_p(x), pixels, x.shape[-1], off, c, _p(y), _s()), "gi_channel_slice_bf16")
+    return y
+
+
+def channel_slice_add(x: torch.Tensor, y: torch.Tensor, off: int) -> torch.Tensor:
+    pixels = x.numel() // x.shape[-1]
+    check(_lib().gi_channel_slice_add_bf16(_p(x), pixels, x.shape[-1], _p(y), y.shape[-1], off, _s()),
+          "gi_channel_slice_add_bf16")
+    return y
+
+
+def adam(p: torch.Tensor, g: torch.Tensor, m: torch.Tensor, v: torch.Tensor, lr: float, step: int,
+         beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8, grad_scale: float = 1.0) -> None:
+    check(_lib().gi_adam_f32(_p(p), _p(g), _p(m), _p(v), p.numel(), lr, beta1, beta2, eps, step, grad_scale, _s()),
+          "gi_adam_f32")
