@@ -211,6 +211,11 @@ _PROTOS = {
     "gi_upsample2_bwd_bf16": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP]),
     "gi_channel_slice_bf16": (C.c_int, [_VP, C.c_size_t, C.c_int, C.c_int, C.c_int, _VP, _VP]),
     "gi_channel_slice_add_bf16": (C.c_int, [_VP, C.c_size_t, C.c_int, _VP, C.c_int, C.c_int, _VP]),
+    "gi_surrogate_features": (C.c_int, [_VP, _VP, C.POINTER(MapParams), F16, F16, C.POINTER(VisParams), C.c_int,
+                                        C.c_int, _VP, _VP, _VP]),
+    "gi_surrogate_finish": (C.c_int, [_VP, _VP, C.c_int, C.c_int, _VP, F16, C.POINTER(VisParams), C.c_int, C.c_int,
+                                      _VP, _VP, C.c_float, _VP, _VP, _VP]),
+    "gi_surrogate_loss": (C.c_int, [_VP, _VP, _VP, C.c_size_t, C.c_float, _VP, _VP, _VP]),
     "gi_adam_f32": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
                               C.c_float, _VP]),
 }

@@ -8,6 +8,7 @@
 
 #include "host_math.h"
 #include "internal.h"
+#include "../../include/gi_surrogate.h"
 #include "raster.h"
 
 namespace {
@@ -478,6 +479,51 @@ extern "C" gi_status gi_render_frame(gi_context* ctx, const gi_scene* s, const g
                                          W, H, d_pos, d_nrm, cs);
     mark(3);
     return st;
+}
+
+extern "C" gi_status gi_surrogate_features(gi_context* ctx, const gi_scene* s, const gi_map_params* mp,
+                                           const float light_mvp[16], const float camera_mvp[16],
+                                           const gi_vis_params* vp, int W, int H, float* d_depth, void* d_feat,
+                                           void* stream) {
+    gi_status st = check_pass(ctx, s);
+    if (st != GI_OK) return st;
+    if (!mp || !light_mvp || !camera_mvp || !vp || !d_depth || !d_feat)
+        return fail(GI_ERR_INVALID_ARG, "gi_surrogate_features: bad arguments");
+    if (vp->technique != GI_TECH_PCSS_POISSON)
+        return fail(GI_ERR_INVALID_ARG, "gi_surrogate_features: the surrogate models GI_TECH_PCSS_POISSON");
+    st = check_image(mp->width, mp->height, "gi_surrogate_features (map)");
+    if (st == GI_OK) st = check_image(W, H, "gi_surrogate_features");
+    if (st == GI_OK) st = check_vis_params(vp);
+    if (st != GI_OK) return st;
+    if ((size_t)s->dev_triangles >= ((size_t)1 << 29))
+        return fail(GI_ERR_CAPACITY, "gi_surrogate_features: more than 2^29 triangles");
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    st = gi::raster_depth_map(ctx, s, light_mvp, mp->width, mp->height, mp->bias_mode, mp->constant_bias,
+                              mp->offset_factor, mp->offset_units, d_depth, small_px_default(), cs);
+    if (st == GI_OK) st = gi::raster_gbuffer_keys(ctx, s, camera_mvp, W, H, cs);
+    if (st == GI_OK)
+        st = gi::launch_surrogate_features(ctx, vp, d_depth, mp->width, mp->height, s, camera_mvp, W, H, d_feat, cs);
+    return st;
+}
+
+extern "C" gi_status gi_surrogate_finish(gi_context* ctx, const gi_scene* s, int map_w, int map_h,
+                                         const float* d_depth, const float camera_mvp[16], const gi_vis_params* vp,
+                                         int W, int H, const float* d_head, const void* d_feat, float err_threshold,
+                                         float* d_vis, uint32_t* d_fallback, void* stream) {
+    gi_status st = check_pass(ctx, s);
+    if (st != GI_OK) return st;
+    if (!camera_mvp || !vp || !d_depth || !d_head || !d_feat || !d_vis)
+        return fail(GI_ERR_INVALID_ARG, "gi_surrogate_finish: bad arguments");
+    if (vp->technique != GI_TECH_PCSS_POISSON)
+        return fail(GI_ERR_INVALID_ARG, "gi_surrogate_finish: the surrogate models GI_TECH_PCSS_POISSON");
+    st = check_image(map_w, map_h, "gi_surrogate_finish (map)");
+    if (st == GI_OK) st = check_image(W, H, "gi_surrogate_finish");
+    if (st == GI_OK) st = check_vis_params(vp);
+    if (st != GI_OK) return st;
+    if (ctx->cap_vkeys < (size_t)W * H * sizeof(unsigned long long))
+        return fail(GI_ERR_INVALID_ARG, "gi_surrogate_finish: call gi_surrogate_features for this frame first");
+    return gi::launch_surrogate_finish(ctx, vp, d_depth, map_w, map_h, s, camera_mvp, W, H, d_head, d_feat,
+                                       err_threshold, d_vis, d_fallback, static_cast<cudaStream_t>(stream));
 }
 
 extern "C" gi_status gi_poisson_table(int n, float* xy) {

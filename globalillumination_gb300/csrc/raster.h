@@ -36,6 +36,17 @@ gi_status launch_visibility(gi_context* ctx, const gi_vis_params* p, const float
                             int map_w, int map_h, const float* d_pos, const float* d_nrm,
                             float* d_vis, int W, int H, cudaStream_t st);
 
+// Learned surrogate: per-pixel features (BF16 x 8) from ctx->d_vkeys and the
+// light map, and the final visibility from the network head with exact
+// PCSS fallback.
+gi_status launch_surrogate_features(gi_context* ctx, const gi_vis_params* p, const float* d_depth, int map_w,
+                                    int map_h, const gi_scene* scene, const float camera_mvp[16], int W, int H,
+                                    void* d_feat, cudaStream_t st);
+gi_status launch_surrogate_finish(gi_context* ctx, const gi_vis_params* p, const float* d_depth, int map_w,
+                                  int map_h, const gi_scene* scene, const float camera_mvp[16], int W, int H,
+                                  const float* d_head, const void* d_feat, float thr, float* d_vis,
+                                  unsigned* d_fallback, cudaStream_t st);
+
 // Progressive best-candidate Poisson-disk sequence in the unit disk
 // (poisson_table.inc); the n-tap table is its first n points.
 extern const float kPoissonDisk[64][2];

@@ -637,6 +637,41 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
     }
 }
 
+__global__ void k_surrogate_loss(const float* __restrict__ head, const float* __restrict__ target,
+                                 const uint4* __restrict__ feat, long long P, float inv, float ew,
+                                 uint16_t* __restrict__ dhead, float* __restrict__ sums) {
+    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < P; i += (long long)gridDim.x * blockDim.x) {
+        const float f3 = __uint_as_float(feat[i].y & 0xFFFF0000u);
+        float g0 = 0.0f, g1 = 0.0f;
+        if (f3 == 1.0f) {
+            const float v = head[i * 16], e = head[i * 16 + 1];
+            const float d = v - target[i];
+            const float ad = fabsf(d);
+            g0 = (d > 0.0f ? 1.0f : d < 0.0f ? -1.0f : 0.0f) * inv;
+            const float de = e - ad;
+            g1 = (de > 0.0f ? ew : de < 0.0f ? -ew : 0.0f) * inv;
+            s0 += ad;
+            s1 += 1.0f;
+            s2 += fabsf(de);
+        }
+        uint4* o = reinterpret_cast<uint4*>(dhead + i * 16);
+        o[0] = make_uint4((uint32_t)f_to_bf16(g0) | ((uint32_t)f_to_bf16(g1) << 16), 0u, 0u, 0u);
+        o[1] = make_uint4(0u, 0u, 0u, 0u);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(sums, s0);
+        atomicAdd(sums + 1, s1);
+        atomicAdd(sums + 2, s2);
+    }
+}
+
 unsigned grid1d(long long n, int threads) {
     long long b = (n + threads - 1) / threads;
     return (unsigned)std::max<long long>(1, std::min<long long>(b, 152LL * 16));
@@ -861,4 +896,15 @@ extern "C" gi_status gi_adam_f32(float* p, const float* g, float* m, float* v, s
         p, g, m, v, (long long)n, lr, beta1, beta2, eps, c1, c2, grad_scale);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_adam_f32 launch");
+}
+
+extern "C" gi_status gi_surrogate_loss(const float* d_head, const float* d_target, const void* d_feat, size_t pixels,
+                                       float err_weight, gi_bf16* d_dhead, float* d_sums, void* stream) {
+    if (!d_head || !d_target || !d_feat || !d_dhead || !d_sums || pixels == 0)
+        return fail(GI_ERR_INVALID_ARG, "gi_surrogate_loss: bad arguments");
+    tc::k_surrogate_loss<<<tc::grid1d((long long)pixels, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        d_head, d_target, static_cast<const uint4*>(d_feat), (long long)pixels, 1.0f / (float)pixels, err_weight,
+        d_dhead, d_sums);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_surrogate_loss launch");
 }

@@ -28,6 +28,7 @@
 // map (or NaN) reads 0.  Blocks are 32 x 4 pixels so a warp reads one
 // coalesced row segment of the G-buffer and its taps land on neighbouring
 // texels of the map (L1 / L2 hits: a 2048^2 map is 16 MiB and stays in L2).
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "internal.h"
@@ -1162,7 +1163,155 @@ __global__ void __launch_bounds__(128) k_frame_visibility(
     __stcs(out + i, shade<TECH>(p, c, vertex, normal));
 }
 
+// ---- learned surrogate: per-pixel features and the final visibility -----------
+// Features (BF16, 8 channels per pixel, 4 used):
+//   0  hard visibility with the pre-test (shade<HARD>): 1, intensity or 0
+//   1  (z - d) * 64 clamped to [-1, 4]: receiver depth minus the map depth
+//      at the pixel's texel (window units)
+//   2  penumbra estimate in map texels / 8 (<= 4) from four diagonal
+//      blocker taps at the PCSS blocker-search radius
+//   3  1 if the pre-test passed, 0.5 if it failed, 0 for background
+__device__ __forceinline__ uint16_t f2bf(float f) { return __bfloat16_as_ushort(__float2bfloat16_rn(f)); }
+
+__global__ void __launch_bounds__(128) k_surrogate_features(
+    const gi_vis_params p, const float* __restrict__ map, int map_w, int map_h, float sx, float sy,
+    const unsigned long long* __restrict__ keys, const float* __restrict__ points,
+    const float* __restrict__ normals, const int* __restrict__ indices, const dev::Mat4 mvp,
+    const unsigned* __restrict__ rec_of, const dev::BRec* __restrict__ recs, const uint4* __restrict__ rres,
+    int W, int H, uint4* __restrict__ feat) {
+    int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    int y = blockIdx.y * 4 + (threadIdx.x >> 5);
+    if (x >= W || y >= H) return;
+    Ctx c;
+    c.map = map;
+    c.W = map_w;
+    c.H = map_h;
+    c.fW = (float)map_w;
+    c.fH = (float)map_h;
+    c.sx = sx;
+    c.sy = sy;
+    c.I = p.shadow_intensity;
+    const size_t i = (size_t)y * W + x;
+    float4 pv, nv;
+    dev::resolve_pixel(__ldcs(keys + i), points, normals, indices, mvp, W, H, x, y, rec_of, recs, rres, pv, nv);
+    float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, f3 = 0.0f;
+    V4 vertex = {pv.x, pv.y, pv.z, pv.w};
+    if (vertex.x != 0.0f) {
+        V4 normal = {nv.x, nv.y, nv.z, nv.w};
+        V4 sc = mat4_mul(p.light_mvp_biased, vertex);
+        V4 n = {sc.x / sc.w, sc.y / sc.w, sc.z / sc.w, 1.0f};
+        const float pre = pretest(p, c, vertex, normal);
+        f3 = pre == 1.0f ? 1.0f : 0.5f;
+        f0 = pre;
+        const float d = fetch(c, n.x, n.y);
+        if (sc.w > 0.0f && pre == 1.0f) f0 = (n.z <= d) ? 1.0f : c.I;
+        f1 = fminf(fmaxf((n.z - d) * 64.0f, -1.0f), 4.0f);
+        const float r = blocker_search_width(p, c) * 0.70710678f;
+        float avg = 0.0f;
+        int nb = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float dd = fetch(c, n.x + ((k & 1) ? r : -r), n.y + ((k & 2) ? r : -r));
+            if (n.z > dd) {
+                avg += dd;
+                nb++;
+            }
+        }
+        if (nb > 0) {
+            avg /= (float)nb;
+            const float pw = penumbra_width(p, avg, n.z);
+            f2 = fminf(fmaxf(pw * c.fW * 0.125f, 0.0f), 4.0f);
+        }
+    }
+    const uint32_t w0 = (uint32_t)f2bf(f0) | ((uint32_t)f2bf(f1) << 16);
+    const uint32_t w1 = (uint32_t)f2bf(f2) | ((uint32_t)f2bf(f3) << 16);
+    feat[i] = make_uint4(w0, w1, 0u, 0u);
+}
+
+// Visibility from the network head (FP32, 16 channels per pixel: 0 the
+// visibility, 1 the predicted absolute error): background 0, failed
+// pre-test the intensity, otherwise the prediction clamped to
+// [intensity, 1], or the exact PCSS (Poisson) value where the predicted
+// error exceeds `thr`.
+__global__ void __launch_bounds__(128) k_surrogate_finish(
+    const gi_vis_params p, const float* __restrict__ map, int map_w, int map_h, float sx, float sy,
+    const unsigned long long* __restrict__ keys, const float* __restrict__ points,
+    const float* __restrict__ normals, const int* __restrict__ indices, const dev::Mat4 mvp,
+    const unsigned* __restrict__ rec_of, const dev::BRec* __restrict__ recs, const uint4* __restrict__ rres,
+    const float* __restrict__ head, const uint4* __restrict__ feat, float thr, float* __restrict__ out, int W,
+    int H, unsigned* __restrict__ n_fallback) {
+    int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    int y = blockIdx.y * 4 + (threadIdx.x >> 5);
+    if (x >= W || y >= H) return;
+    const size_t i = (size_t)y * W + x;
+    const uint4 f = __ldg(feat + i);
+    const float f3 = __uint_as_float(f.y & 0xFFFF0000u);
+    const float I = p.shadow_intensity;
+    float v;
+    if (f3 == 0.0f) {
+        v = 0.0f;
+    } else if (f3 != 1.0f) {
+        v = I;
+    } else {
+        const float2 h = *reinterpret_cast<const float2*>(head + i * 16);
+        if (h.y > thr) {
+            Ctx c;
+            c.map = map;
+            c.W = map_w;
+            c.H = map_h;
+            c.fW = (float)map_w;
+            c.fH = (float)map_h;
+            c.sx = sx;
+            c.sy = sy;
+            c.I = I;
+            float4 pv, nv;
+            dev::resolve_pixel(keys[i], points, normals, indices, mvp, W, H, x, y, rec_of, recs, rres, pv, nv);
+            V4 vertex = {pv.x, pv.y, pv.z, pv.w};
+            V4 normal = {nv.x, nv.y, nv.z, nv.w};
+            v = shade<GI_TECH_PCSS_POISSON>(p, c, vertex, normal);
+            if (n_fallback) atomicAdd(n_fallback, 1u);
+        } else {
+            v = fminf(fmaxf(h.x, I), 1.0f);
+        }
+    }
+    __stcs(out + i, v);
+}
+
 }  // namespace vis
+
+gi_status launch_surrogate_features(gi_context* ctx, const gi_vis_params* p, const float* d_depth, int map_w,
+                                    int map_h, const gi_scene* scene, const float camera_mvp[16], int W, int H,
+                                    void* d_feat, cudaStream_t st) {
+    dim3 grid((W + 31) / 32, (H + 3) / 4);
+    const float sx = (float)(1.0 / (double)map_w), sy = (float)(1.0 / (double)map_h);
+    dev::Mat4 m;
+    for (int k = 0; k < 16; ++k) m.m[k] = camera_mvp[k];
+    vis::k_surrogate_features<<<grid, 128, 0, st>>>(
+        *p, d_depth, map_w, map_h, sx, sy, ctx->d_vkeys, scene->d_points, scene->d_normals, scene->d_indices, m,
+        static_cast<const unsigned*>(ctx->tier_buf[1][6]), static_cast<const dev::BRec*>(ctx->tier_buf[1][0]),
+        static_cast<const uint4*>(ctx->tier_buf[1][7]), W, H, static_cast<uint4*>(d_feat));
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "surrogate features launch");
+}
+
+gi_status launch_surrogate_finish(gi_context* ctx, const gi_vis_params* p, const float* d_depth, int map_w,
+                                  int map_h, const gi_scene* scene, const float camera_mvp[16], int W, int H,
+                                  const float* d_head, const void* d_feat, float thr, float* d_vis,
+                                  unsigned* d_fallback, cudaStream_t st) {
+    dim3 grid((W + 31) / 32, (H + 3) / 4);
+    const float sx = (float)(1.0 / (double)map_w), sy = (float)(1.0 / (double)map_h);
+    dev::Mat4 m;
+    for (int k = 0; k < 16; ++k) m.m[k] = camera_mvp[k];
+    vis::k_surrogate_finish<<<grid, 128, 0, st>>>(
+        *p, d_depth, map_w, map_h, sx, sy, ctx->d_vkeys, scene->d_points, scene->d_normals, scene->d_indices, m,
+        static_cast<const unsigned*>(ctx->tier_buf[1][6]), static_cast<const dev::BRec*>(ctx->tier_buf[1][0]),
+        static_cast<const uint4*>(ctx->tier_buf[1][7]), d_head, static_cast<const uint4*>(d_feat), thr, d_vis, W,
+        H, d_fallback);
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "surrogate finish launch");
+}
 
 gi_status launch_visibility(gi_context* ctx, const gi_vis_params* p, const float* d_depth,
                             int map_w, int map_h, const float* d_pos, const float* d_nrm,

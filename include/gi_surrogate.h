@@ -94,6 +94,36 @@ gi_status gi_channel_slice_bf16(const gi_bf16* x, size_t pixels, int stride, int
 gi_status gi_channel_slice_add_bf16(const gi_bf16* x, size_t pixels, int c, gi_bf16* y,
                                     int stride, int off, void* stream);
 
+/* Surrogate frame, step 1 (replaces the light map + G-buffer part of
+ * gi_render_frame for GI_TECH_PCSS_POISSON): renders the light map into
+ * d_depth and the camera visibility keys into the context, then writes
+ * the network input d_feat (BF16 [height][width][8]; channels 0-3 used:
+ * hard visibility with the pre-test, clamped (z - map depth) * 64,
+ * penumbra estimate in map texels / 8 from four blocker taps, and 1 /
+ * 0.5 / 0 for pre-test passed / failed / background). */
+gi_status gi_surrogate_features(gi_context* ctx, const gi_scene* scene, const gi_map_params* map,
+                                const float light_mvp[16], const float camera_mvp[16],
+                                const gi_vis_params* vis, int width, int height, float* d_depth,
+                                void* d_feat, void* stream);
+/* Surrogate frame, step 3 (after the U-Net wrote d_head, FP32
+ * [height][width][16]: channel 0 the visibility, 1 the predicted absolute
+ * error): background 0, failed pre-test the intensity, else the clamped
+ * prediction, or the exact PCSS value where the predicted error exceeds
+ * err_threshold (counted into *d_fallback when not NULL).  Uses the keys
+ * that gi_surrogate_features left in ctx. */
+gi_status gi_surrogate_finish(gi_context* ctx, const gi_scene* scene, int map_width, int map_height,
+                              const float* d_depth, const float camera_mvp[16], const gi_vis_params* vis,
+                              int width, int height, const float* d_head, const void* d_feat,
+                              float err_threshold, float* d_vis, uint32_t* d_fallback, void* stream);
+/* Training loss of the surrogate over `pixels` pixels: L1 of the
+ * visibility (channel 0 of head) against target on pixels whose feature 3
+ * is 1, plus L1 of the error head (channel 1) against the current
+ * |visibility - target|.  Writes dhead (BF16 [pixels][16], gradient of
+ * the mean loss, other channels 0) and adds {sum |v - t|, pixel count,
+ * sum error-head loss} to sums[0..2]. */
+gi_status gi_surrogate_loss(const float* d_head, const float* d_target, const void* d_feat, size_t pixels,
+                            float err_weight, gi_bf16* d_dhead, float* d_sums, void* stream);
+
 /* Adam step on FP32 master weights p with gradient g (both n floats), then
  * the BF16 copy is refreshed by the caller with gi_pack_conv_weights. */
 gi_status gi_adam_f32(float* p, const float* g, float* m, float* v, size_t n, float lr,
