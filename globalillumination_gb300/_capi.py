@@ -214,7 +214,9 @@ _PROTOS = {
     "gi_surrogate_features": (C.c_int, [_VP, _VP, C.POINTER(MapParams), F16, F16, C.POINTER(VisParams), C.c_int,
                                         C.c_int, _VP, _VP, _VP]),
     "gi_surrogate_finish": (C.c_int, [_VP, _VP, C.c_int, C.c_int, _VP, F16, C.POINTER(VisParams), C.c_int, C.c_int,
-                                      _VP, _VP, C.c_float, _VP, _VP, _VP]),
+                                      _VP, C.c_int, _VP, C.c_float, _VP, _VP, _VP]),
+    "gi_conv2d_head_bf16": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP, C.c_int, C.c_int, _VP, _VP,
+                                      _VP, _VP, _VP]),
     "gi_surrogate_loss": (C.c_int, [_VP, _VP, _VP, C.c_size_t, C.c_float, _VP, _VP, _VP]),
     "gi_adam_f32": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
                               C.c_float, _VP]),

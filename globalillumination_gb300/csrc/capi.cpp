@@ -508,11 +508,11 @@ extern "C" gi_status gi_surrogate_features(gi_context* ctx, const gi_scene* s, c
 
 extern "C" gi_status gi_surrogate_finish(gi_context* ctx, const gi_scene* s, int map_w, int map_h,
                                          const float* d_depth, const float camera_mvp[16], const gi_vis_params* vp,
-                                         int W, int H, const float* d_head, const void* d_feat, float err_threshold,
-                                         float* d_vis, uint32_t* d_fallback, void* stream) {
+                                         int W, int H, const float* d_head, int head_stride, const void* d_feat,
+                                         float err_threshold, float* d_vis, uint32_t* d_fallback, void* stream) {
     gi_status st = check_pass(ctx, s);
     if (st != GI_OK) return st;
-    if (!camera_mvp || !vp || !d_depth || !d_head || !d_feat || !d_vis)
+    if (!camera_mvp || !vp || !d_depth || !d_head || !d_feat || !d_vis || head_stride < 2 || head_stride % 2)
         return fail(GI_ERR_INVALID_ARG, "gi_surrogate_finish: bad arguments");
     if (vp->technique != GI_TECH_PCSS_POISSON)
         return fail(GI_ERR_INVALID_ARG, "gi_surrogate_finish: the surrogate models GI_TECH_PCSS_POISSON");
@@ -522,8 +522,8 @@ extern "C" gi_status gi_surrogate_finish(gi_context* ctx, const gi_scene* s, int
     if (st != GI_OK) return st;
     if (ctx->cap_vkeys < (size_t)W * H * sizeof(unsigned long long))
         return fail(GI_ERR_INVALID_ARG, "gi_surrogate_finish: call gi_surrogate_features for this frame first");
-    return gi::launch_surrogate_finish(ctx, vp, d_depth, map_w, map_h, s, camera_mvp, W, H, d_head, d_feat,
-                                       err_threshold, d_vis, d_fallback, static_cast<cudaStream_t>(stream));
+    return gi::launch_surrogate_finish(ctx, vp, d_depth, map_w, map_h, s, camera_mvp, W, H, d_head, head_stride,
+                                       d_feat, err_threshold, d_vis, d_fallback, static_cast<cudaStream_t>(stream));
 }
 
 extern "C" gi_status gi_poisson_table(int n, float* xy) {

@@ -44,8 +44,8 @@ gi_status launch_surrogate_features(gi_context* ctx, const gi_vis_params* p, con
                                     void* d_feat, cudaStream_t st);
 gi_status launch_surrogate_finish(gi_context* ctx, const gi_vis_params* p, const float* d_depth, int map_w,
                                   int map_h, const gi_scene* scene, const float camera_mvp[16], int W, int H,
-                                  const float* d_head, const void* d_feat, float thr, float* d_vis,
-                                  unsigned* d_fallback, cudaStream_t st);
+                                  const float* d_head, int head_stride, const void* d_feat, float thr,
+                                  float* d_vis, unsigned* d_fallback, cudaStream_t st);
 
 // Progressive best-candidate Poisson-disk sequence in the unit disk
 // (poisson_table.inc); the n-tap table is its first n points.

@@ -158,6 +158,11 @@ struct ConvArgs {
     float* y32;
     uint32_t* err;
     long long P;
+    // optional fused 1x1 head on the activated BF16-rounded output:
+    // hout[p][j] = hb[j] + sum_c hw[j][c] * bf16(v[c]), j < 2
+    const float* hw;
+    const float* hb;
+    float* hout;
 };
 
 __global__ void __launch_bounds__(kThreads) k_conv_fwd(ConvArgs a) {
@@ -292,6 +297,189 @@ __global__ void __launch_bounds__(kThreads) k_conv_fwd(ConvArgs a) {
     fence_before();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, ncols);
+    if (!ok && tid == 0 && a.err) atomicOr(a.err, 1u);
+}
+
+// ---- 3x3 convolution from halo slabs (cin % 16 == 0) ---------------------------
+// A CTA computes R output rows x 128 pixels (R accumulators of 128 x N in
+// TMEM).  A stage holds two channel groups (16 channels) of the R + 2 input
+// rows y0-1 .. y0+R over x0-1 .. x0+128 ("slab": 130 pixels x 16 B per
+// row and group) and the weights of all 9 taps for those channels.  The
+// MMA of tap (dy, dx) for output row r reads A at slab row r + dy, shifted
+// by dx pixels (16 B): the 8-pixel core matrices stay contiguous (SBO 128 B)
+// and the second channel group is one slab further (LBO).  Each input
+// pixel is loaded (R + 2) / R times instead of 9.
+constexpr int kSlabPx = 130;
+constexpr int kSlabRow = kSlabPx * 16;  // 2080 B
+
+struct SlabGeom {
+    int R, NS, ncols, a_bytes, b_bytes, stage_bytes;
+};
+
+// Rows per CTA R and stage count NS: 32-wide outputs keep R = 4 so that
+// two or three CTAs fit an SM; 64-wide ones use R = 8 (weights reused over
+// more pixels, TMEM full); layers with at most two K-stages use two stages.
+__host__ __device__ inline SlabGeom slab_geom(int N, int nk) {
+    SlabGeom g;
+    g.ncols = N <= 32 ? 32 : N <= 64 ? 64 : N <= 128 ? 128 : 256;
+    g.R = N <= 32 ? 4 : N <= 64 ? 8 : N <= 128 ? 4 : 2;
+    g.a_bytes = 2 * (g.R + 2) * kSlabRow;
+    g.b_bytes = 9 * 2 * N * 16;
+    g.stage_bytes = g.a_bytes + g.b_bytes;
+    g.NS = (nk > 2 && 3 * g.stage_bytes <= 200 * 1024) ? 3 : 2;
+    return g;
+}
+
+__global__ void __launch_bounds__(kThreads) k_conv3_slab(ConvArgs a, int tiles_x, int tiles_y) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t bars[3];
+    __shared__ uint32_t tmem_slot;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int N = a.cout;
+    const SlabGeom G = slab_geom(N, a.cin / 16);
+    const int R = G.R, NS = G.NS;
+    const uint32_t tcols = (uint32_t)(R * G.ncols);
+    if (warp == 0) tmem_alloc(&tmem_slot, tcols);
+    if (tid == 0) {
+        for (int s = 0; s < NS; ++s) mbar_init(&bars[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_slot;
+    const int bx = blockIdx.x % tiles_x;
+    const int by = (blockIdx.x / tiles_x) % tiles_y;
+    const long long img = blockIdx.x / ((long long)tiles_x * tiles_y);
+    const int x0 = bx * 128, y0 = by * R;
+    const int cg = a.cin / 8;
+    const int nk = cg / 2;
+    const int rows = R + 2;
+    bool ok = true;
+
+    auto load_stage = [&](int chunk, int s) {
+        uint8_t* sa = smem + s * G.stage_bytes;
+        uint8_t* sb = sa + G.a_bytes;
+        const int g0 = chunk * 2;
+        const int na = 2 * rows * kSlabPx;
+        for (int c = tid; c < na; c += kThreads) {
+            const int gl = c / (rows * kSlabPx);
+            const int rem = c - gl * rows * kSlabPx;
+            const int r = rem / kSlabPx, px = rem - r * kSlabPx;
+            const int yy = y0 + r - 1, xx = x0 + px - 1;
+            const uint16_t* src = a.x;
+            int bytes = 0;
+            if (yy >= 0 && yy < a.h && xx >= 0 && xx < a.w) {
+                src = a.x + ((img * a.h + yy) * a.w + xx) * a.cin + (g0 + gl) * 8;
+                bytes = 16;
+            }
+            cp_async16(smem_u32(sa + (gl * rows + r) * kSlabRow + px * 16), src, bytes);
+        }
+        const int nb = 9 * 2 * N;
+        for (int c = tid; c < nb; c += kThreads) {
+            const int co = c % N;
+            const int rest = c / N;
+            const int gl = rest & 1, t = rest >> 1;
+            const uint16_t* src = a.wt + ((long long)co * a.nkb_pad + t * cg + g0 + gl) * 8;
+            cp_async16(smem_u32(sb + ((t * 2 + gl) * N + co) * 16), src, 16);
+        }
+    };
+
+    const uint32_t idesc = idesc_bf16(128, N);
+    for (int s = 0; s < NS - 1; ++s) {
+        if (s < nk) load_stage(s, s);
+        cp_async_commit();
+    }
+    for (int i = 0; i < nk; ++i) {
+        const int s = i % NS;
+        if (NS == 3) cp_async_wait<1>();
+        else cp_async_wait<0>();
+        fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+            fence_after();
+            const uint8_t* sa = smem + s * G.stage_bytes;
+            const uint8_t* sb = sa + G.a_bytes;
+            for (int t = 0; t < 9; ++t) {
+                const int dy = t / 3, dx = t % 3;
+                const uint64_t bd = smem_desc(smem_u32(sb + t * 2 * N * 16), (uint32_t)N * 16u, 128u);
+                for (int r = 0; r < R; ++r) {
+                    const uint64_t ad =
+                        smem_desc(smem_u32(sa + (r + dy) * kSlabRow + dx * 16), (uint32_t)(rows * kSlabRow), 128u);
+                    mma_bf16(tmem + (uint32_t)(r * G.ncols), ad, bd, idesc, (i > 0 || t > 0) ? 1u : 0u);
+                }
+            }
+            mma_commit(&bars[s]);
+        }
+        const int j = i + NS - 1;
+        if (j < nk) {
+            const int sj = j % NS;
+            if (i >= 1) ok &= mbar_wait(&bars[sj], (unsigned)((i - 1) / NS) & 1u);
+            load_stage(j, sj);
+        }
+        cp_async_commit();
+    }
+    const int last = nk - 1;
+    ok &= mbar_wait(&bars[last % NS], (unsigned)(last / NS) & 1u);
+    fence_after();
+
+    const int xo = x0 + warp * 32 + lane;
+    for (int r = 0; r < R; ++r) {
+        const int yo = y0 + r;
+        const bool live = xo < a.w && yo < a.h;
+        const long long p = (img * a.h + yo) * a.w + xo;
+        float h0 = a.hw ? __ldg(a.hb) : 0.0f, h1 = a.hw ? __ldg(a.hb + 1) : 0.0f;
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(r * G.ncols + c0), v);
+            if (!live) continue;
+            if (a.bias) {
+#pragma unroll
+                for (int q = 0; q < 16; ++q) v[q] += __ldg(a.bias + c0 + q);
+            }
+            if (a.act == GI_ACT_RELU) {
+#pragma unroll
+                for (int q = 0; q < 16; ++q) v[q] = fmaxf(v[q], 0.0f);
+            }
+            const long long o = p * a.y_c + a.y_off + c0;
+            if (a.mask) {
+                const uint4* mp = reinterpret_cast<const uint4*>(a.mask + o);
+                uint4 m0 = __ldg(mp), m1 = __ldg(mp + 1);
+                const uint32_t mw[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    const uint16_t mv = (uint16_t)(mw[q >> 1] >> ((q & 1) * 16));
+                    if (!(bf16_to_f(mv) > 0.0f)) v[q] = 0.0f;
+                }
+            }
+            if (a.y32) {
+                float4* yp = reinterpret_cast<float4*>(a.y32 + p * N + c0);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) yp[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            }
+            if (a.hw) {
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    const float vb = bf16_to_f(f_to_bf16(v[q]));
+                    h0 += __ldg(a.hw + c0 + q) * vb;
+                    h1 += __ldg(a.hw + N + c0 + q) * vb;
+                }
+            }
+            if (a.y) {
+                uint32_t pk[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    pk[q] = (uint32_t)f_to_bf16(v[2 * q]) | ((uint32_t)f_to_bf16(v[2 * q + 1]) << 16);
+                uint4* yp = reinterpret_cast<uint4*>(a.y + o);
+                yp[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                yp[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+            }
+        }
+        if (a.hout && live) *reinterpret_cast<float2*>(a.hout + p * 2) = make_float2(h0, h1);
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, tcols);
     if (!ok && tid == 0 && a.err) atomicOr(a.err, 1u);
 }
 
@@ -642,7 +830,7 @@ __global__ void k_surrogate_loss(const float* __restrict__ head, const float* __
                                  uint16_t* __restrict__ dhead, float* __restrict__ sums) {
     float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < P; i += (long long)gridDim.x * blockDim.x) {
-        const float f3 = __uint_as_float(feat[i].y & 0xFFFF0000u);
+        const float f3 = __uint_as_float(feat[2 * i].y & 0xFFFF0000u);
         float g0 = 0.0f, g1 = 0.0f;
         if (f3 == 1.0f) {
             const float v = head[i * 16], e = head[i * 16 + 1];
@@ -720,6 +908,24 @@ extern "C" gi_status gi_conv2d_bf16(const gi_bf16* x, int n, int h, int w, int c
     a.y32 = y32;
     a.err = err;
     a.P = (long long)n * h * w;
+    a.hw = nullptr;
+    a.hb = nullptr;
+    a.hout = nullptr;
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    if (ksize == 3 && cin % 16 == 0) {
+        const tc::SlabGeom G = tc::slab_geom(cout, cin / 16);
+        static bool slab_attr = false;
+        if (!slab_attr) {
+            cudaFuncSetAttribute(tc::k_conv3_slab, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+            slab_attr = true;
+        }
+        const int tx = (w + 127) / 128, ty = (h + G.R - 1) / G.R;
+        const long long blocks = (long long)tx * ty * n;
+        if (blocks > 0x7FFFFFFFLL) return fail(GI_ERR_INVALID_ARG, "gi_conv2d_bf16: too many tiles");
+        tc::k_conv3_slab<<<(unsigned)blocks, tc::kThreads, G.NS * G.stage_bytes, cs>>>(a, tx, ty);
+        cudaError_t e = cudaGetLastError();
+        return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_conv2d_bf16 launch");
+    }
     const int smem = tc::kNS * (tc::kStageA + (cout / 8) * tc::kSBO);
     static bool attr_set = false;
     if (!attr_set) {
@@ -728,7 +934,7 @@ extern "C" gi_status gi_conv2d_bf16(const gi_bf16* x, int n, int h, int w, int c
     }
     const long long tiles = (a.P + 127) / 128;
     if (tiles > 0x7FFFFFFFLL) return fail(GI_ERR_INVALID_ARG, "gi_conv2d_bf16: too many pixels");
-    tc::k_conv_fwd<<<(unsigned)tiles, tc::kThreads, smem, static_cast<cudaStream_t>(stream)>>>(a);
+    tc::k_conv_fwd<<<(unsigned)tiles, tc::kThreads, smem, cs>>>(a);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_conv2d_bf16 launch");
 }
@@ -907,4 +1113,42 @@ extern "C" gi_status gi_surrogate_loss(const float* d_head, const float* d_targe
         d_dhead, d_sums);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_surrogate_loss launch");
+}
+
+extern "C" gi_status gi_conv2d_head_bf16(const gi_bf16* x, int n, int h, int w, int cin, const gi_bf16* wt,
+                                         const float* bias, int cout, int act, const float* head_w,
+                                         const float* head_b, float* head_out, uint32_t* err, void* stream) {
+    if (!x || !wt || !head_w || !head_b || !head_out) return fail(GI_ERR_INVALID_ARG, "gi_conv2d_head_bf16: NULL argument");
+    if (n < 1 || h < 1 || w < 1 || cin < 16 || cin % 16 || cout < 16 || cout > 256 || cout % 16 ||
+        (act != GI_ACT_NONE && act != GI_ACT_RELU))
+        return fail(GI_ERR_INVALID_ARG, "gi_conv2d_head_bf16: bad shape (cin % 16, cout % 16 in [16, 256])");
+    if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(wt) | reinterpret_cast<uintptr_t>(head_out)) % 16)
+        return fail(GI_ERR_INVALID_ARG, "gi_conv2d_head_bf16: tensors must be 16-byte aligned");
+    tc::ConvArgs a = {};
+    a.x = x;
+    a.n = n;
+    a.h = h;
+    a.w = w;
+    a.cin = cin;
+    a.wt = wt;
+    a.cout = cout;
+    a.nkb = tc::nkb_of(cin, 3);
+    a.nkb_pad = tc::nkb_pad_of(cin, 3);
+    a.ksize = 3;
+    a.bias = bias;
+    a.act = act;
+    a.y_c = cout;
+    a.err = err;
+    a.P = (long long)n * h * w;
+    a.hw = head_w;
+    a.hb = head_b;
+    a.hout = head_out;
+    const tc::SlabGeom G = tc::slab_geom(cout, cin / 16);
+    cudaFuncSetAttribute(tc::k_conv3_slab, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    const int tx = (w + 127) / 128, ty = (h + G.R - 1) / G.R;
+    const long long blocks = (long long)tx * ty * n;
+    tc::k_conv3_slab<<<(unsigned)blocks, tc::kThreads, G.NS * G.stage_bytes, static_cast<cudaStream_t>(stream)>>>(
+        a, tx, ty);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_conv2d_head_bf16 launch");
 }

@@ -1164,7 +1164,7 @@ __global__ void __launch_bounds__(128) k_frame_visibility(
 }
 
 // ---- learned surrogate: per-pixel features and the final visibility -----------
-// Features (BF16, 8 channels per pixel, 4 used):
+// Features (BF16, 16 channels per pixel, 4 used):
 //   0  hard visibility with the pre-test (shade<HARD>): 1, intensity or 0
 //   1  (z - d) * 64 clamped to [-1, 4]: receiver depth minus the map depth
 //      at the pixel's texel (window units)
@@ -1225,11 +1225,12 @@ __global__ void __launch_bounds__(128) k_surrogate_features(
     }
     const uint32_t w0 = (uint32_t)f2bf(f0) | ((uint32_t)f2bf(f1) << 16);
     const uint32_t w1 = (uint32_t)f2bf(f2) | ((uint32_t)f2bf(f3) << 16);
-    feat[i] = make_uint4(w0, w1, 0u, 0u);
+    feat[2 * i] = make_uint4(w0, w1, 0u, 0u);
+    feat[2 * i + 1] = make_uint4(0u, 0u, 0u, 0u);
 }
 
-// Visibility from the network head (FP32, 16 channels per pixel: 0 the
-// visibility, 1 the predicted absolute error): background 0, failed
+// Visibility from the network head (FP32, head_stride channels per pixel: 0
+// the visibility, 1 the predicted absolute error): background 0, failed
 // pre-test the intensity, otherwise the prediction clamped to
 // [intensity, 1], or the exact PCSS (Poisson) value where the predicted
 // error exceeds `thr`.
@@ -1238,13 +1239,13 @@ __global__ void __launch_bounds__(128) k_surrogate_finish(
     const unsigned long long* __restrict__ keys, const float* __restrict__ points,
     const float* __restrict__ normals, const int* __restrict__ indices, const dev::Mat4 mvp,
     const unsigned* __restrict__ rec_of, const dev::BRec* __restrict__ recs, const uint4* __restrict__ rres,
-    const float* __restrict__ head, const uint4* __restrict__ feat, float thr, float* __restrict__ out, int W,
-    int H, unsigned* __restrict__ n_fallback) {
+    const float* __restrict__ head, int head_stride, const uint4* __restrict__ feat, float thr,
+    float* __restrict__ out, int W, int H, unsigned* __restrict__ n_fallback) {
     int x = blockIdx.x * 32 + (threadIdx.x & 31);
     int y = blockIdx.y * 4 + (threadIdx.x >> 5);
     if (x >= W || y >= H) return;
     const size_t i = (size_t)y * W + x;
-    const uint4 f = __ldg(feat + i);
+    const uint4 f = __ldg(feat + 2 * i);
     const float f3 = __uint_as_float(f.y & 0xFFFF0000u);
     const float I = p.shadow_intensity;
     float v;
@@ -1253,7 +1254,7 @@ __global__ void __launch_bounds__(128) k_surrogate_finish(
     } else if (f3 != 1.0f) {
         v = I;
     } else {
-        const float2 h = *reinterpret_cast<const float2*>(head + i * 16);
+        const float2 h = *reinterpret_cast<const float2*>(head + i * head_stride);
         if (h.y > thr) {
             Ctx c;
             c.map = map;
@@ -1297,8 +1298,8 @@ gi_status launch_surrogate_features(gi_context* ctx, const gi_vis_params* p, con
 
 gi_status launch_surrogate_finish(gi_context* ctx, const gi_vis_params* p, const float* d_depth, int map_w,
                                   int map_h, const gi_scene* scene, const float camera_mvp[16], int W, int H,
-                                  const float* d_head, const void* d_feat, float thr, float* d_vis,
-                                  unsigned* d_fallback, cudaStream_t st) {
+                                  const float* d_head, int head_stride, const void* d_feat, float thr,
+                                  float* d_vis, unsigned* d_fallback, cudaStream_t st) {
     dim3 grid((W + 31) / 32, (H + 3) / 4);
     const float sx = (float)(1.0 / (double)map_w), sy = (float)(1.0 / (double)map_h);
     dev::Mat4 m;
@@ -1306,8 +1307,8 @@ gi_status launch_surrogate_finish(gi_context* ctx, const gi_vis_params* p, const
     vis::k_surrogate_finish<<<grid, 128, 0, st>>>(
         *p, d_depth, map_w, map_h, sx, sy, ctx->d_vkeys, scene->d_points, scene->d_normals, scene->d_indices, m,
         static_cast<const unsigned*>(ctx->tier_buf[1][6]), static_cast<const dev::BRec*>(ctx->tier_buf[1][0]),
-        static_cast<const uint4*>(ctx->tier_buf[1][7]), d_head, static_cast<const uint4*>(d_feat), thr, d_vis, W,
-        H, d_fallback);
+        static_cast<const uint4*>(ctx->tier_buf[1][7]), d_head, head_stride, static_cast<const uint4*>(d_feat), thr,
+        d_vis, W, H, d_fallback);
     ctx->launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "surrogate finish launch");

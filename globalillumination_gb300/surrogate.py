@@ -31,7 +31,7 @@ from ._capi import check
 from .shadow import Context, Frame, MapParams, Scene, ShadowParams, ViewSpec, frame_setup, _f16, _ptr
 
 ERR_THRESHOLD = 0.02
-FEATURES = 8  # channels of the feature tensor (4 used)
+FEATURES = 16  # channels of the feature tensor (4 used)
 HEAD = 16     # channels of the head (0: visibility, 1: predicted error)
 
 
@@ -57,7 +57,7 @@ class Layer:
 
 # (name, cin_real, cin, cout, k)
 ARCH = [
-    ("e0a", 4, 8, 32, 3), ("e0b", 32, 32, 32, 3),
+    ("e0a", 4, FEATURES, 32, 3), ("e0b", 32, 32, 32, 3),
     ("e1a", 32, 32, 64, 3), ("e1b", 64, 64, 64, 3),
     ("e2a", 64, 64, 96, 3), ("e2b", 96, 96, 96, 3),
     ("e3a", 96, 96, 128, 3), ("e3b", 128, 128, 128, 3),
@@ -168,6 +168,42 @@ class UNet:
         self._acts = a if keep else None
         return out32
 
+    def forward_fused(self, feat: torch.Tensor, head2: torch.Tensor) -> torch.Tensor:
+        """Inference: forward with the 1x1 head fused into the last 3x3
+        convolution's epilogue; head2 (FP32, [n, H, W, 2]) receives the
+        visibility and the predicted error, the last activation is never
+        stored."""
+        n, H, W, _ = feat.shape
+        assert H % 8 == 0 and W % 8 == 0, "the U-Net needs height and width divisible by 8"
+        if getattr(self, "_hw_ver", -1) != self.step_count or not hasattr(self, "_hw"):
+            L = self.layers["head"]
+            self._hw = L.w[:2, :, 0, 0].to(torch.bfloat16).float().contiguous()
+            self._hb = L.b[:2].contiguous()
+            self._hw_ver = self.step_count
+        bf = dict(dtype=torch.bfloat16, device=feat.device)
+        t0 = self._conv("e0a", feat)
+        cat0 = torch.empty((n, H, W, 96), **bf)
+        self._conv("e0b", t0, out=cat0, out_off=0)
+        p0 = ops.maxpool2(ops.channel_slice(cat0, 0, 32))
+        t1 = self._conv("e1a", p0)
+        cat1 = torch.empty((n, H // 2, W // 2, 160), **bf)
+        self._conv("e1b", t1, out=cat1, out_off=0)
+        p1 = ops.maxpool2(ops.channel_slice(cat1, 0, 64))
+        t2 = self._conv("e2a", p1)
+        cat2 = torch.empty((n, H // 4, W // 4, 224), **bf)
+        self._conv("e2b", t2, out=cat2, out_off=0)
+        p2 = ops.maxpool2(ops.channel_slice(cat2, 0, 96))
+        b3 = self._conv("e3b", self._conv("e3a", p2))
+        ops.upsample2(b3, cat2, 96)
+        u2 = self._conv("d2b", self._conv("d2a", cat2))
+        ops.upsample2(u2, cat1, 64)
+        u1 = self._conv("d1b", self._conv("d1a", cat1))
+        ops.upsample2(u1, cat0, 32)
+        u0a = self._conv("d0a", cat0)
+        L = self.layers["d0b"]
+        ops.conv2d_head(u0a, L.wp, L.cout, L.b, self._hw, self._hb, head2, relu=True, err=self.err)
+        return head2
+
     def _wgrad(self, name, x, dy):
         L = self.layers[name]
         self._scratch = ops.conv2d_wgrad(x, dy, L.cout, L.k, L.dwp, L.db, self._scratch, err=self.err)
@@ -251,7 +287,8 @@ def finish(ctx: Context, scene: Scene, frame: Frame, mp: MapParams, params: Shad
     p = params.to_c(frame)
     s = C.c_void_p(int((stream or torch.cuda.current_stream()).cuda_stream))
     check(api.load().gi_surrogate_finish(ctx.handle, scene.handle, mp.width, mp.height, _ptr(depth),
-                                         _f16(frame.camera_mvp), C.byref(p), W, H, _ptr(head), _ptr(feat),
+                                         _f16(frame.camera_mvp), C.byref(p), W, H, _ptr(head), head.shape[-1],
+                                         _ptr(feat),
                                          float(threshold), _ptr(vis), _ptr(fallback) if fallback is not None else None,
                                          s), "gi_surrogate_finish")
     return vis
@@ -274,14 +311,14 @@ class SurrogateFrame:
         self.W, self.H = W, H
         self.depth = torch.empty(map_size * map_size, dtype=torch.float32, device=dev)
         self.feat = torch.empty((1, H, W, FEATURES), dtype=torch.bfloat16, device=dev)
-        self.head = torch.empty((1, H, W, HEAD), dtype=torch.float32, device=dev)
+        self.head = torch.empty((1, H, W, 2), dtype=torch.float32, device=dev)
         self.vis = torch.empty(W * H, dtype=torch.float32, device=dev)
         self.fallback = torch.zeros(1, dtype=torch.int32, device=dev)
 
     def render(self, ctx: Context, scene: Scene, frame: Frame, mp: MapParams, params: ShadowParams,
                threshold: float = ERR_THRESHOLD) -> torch.Tensor:
         features(ctx, scene, frame, mp, params, self.W, self.H, self.depth, self.feat)
-        self.net.forward(self.feat, out32=self.head)
+        self.net.forward_fused(self.feat, self.head)
         finish(ctx, scene, frame, mp, params, self.W, self.H, self.depth, self.head, self.feat, self.vis,
                self.fallback, threshold)
         return self.vis

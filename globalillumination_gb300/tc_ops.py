@@ -27,6 +27,13 @@ def _s() -> C.c_void_p:
     return C.c_void_p(int(torch.cuda.current_stream().cuda_stream))
 
 
+def _need(t: torch.Tensor, numel: int, dtype, what: str) -> None:
+    """Device tensors handed to the kernels must be CUDA, contiguous and large enough."""
+    if not t.is_cuda or t.dtype != dtype or not t.is_contiguous() or t.numel() < numel:
+        raise ValueError(f"{what}: need a contiguous CUDA {dtype} tensor of >= {numel} elements, "
+                         f"got {t.dtype} {tuple(t.shape)} on {t.device}")
+
+
 def nkb_pad(cin: int, ksize: int) -> int:
     nkb = ksize * ksize * cin // 8
     return (nkb + 3) // 4 * 4
@@ -57,10 +64,39 @@ def conv2d(x: torch.Tensor, wp: torch.Tensor, cout: int, ksize: int, bias: torch
     if out is None and out32 is None:
         out = torch.empty((n, h, w, cout), dtype=torch.bfloat16, device=x.device)
     stride = out.shape[-1] if out is not None else cout
+    _need(x, n * h * w * cin, torch.bfloat16, "x")
+    _need(wp, wp.shape[0] * nkb_pad(cin, ksize) * 8, torch.bfloat16, "packed weights")
+    if wp.shape[0] < cout:
+        raise ValueError("packed weights have fewer rows than cout")
+    if out is not None:
+        _need(out, n * h * w * stride, torch.bfloat16, "out")
+        if out_off + cout > stride:
+            raise ValueError("out_off + cout exceeds the channels of out")
+    if out32 is not None:
+        _need(out32, n * h * w * cout, torch.float32, "out32")
+    if mask is not None:
+        _need(mask, n * h * w * stride, torch.bfloat16, "mask")
+    if bias is not None:
+        _need(bias, cout, torch.float32, "bias")
     check(_lib().gi_conv2d_bf16(_p(x), n, h, w, cin, _p(wp), _p(bias), cout, ksize,
                                 api.GI_ACT_RELU if relu else api.GI_ACT_NONE, _p(mask), _p(out), stride, out_off,
                                 _p(out32), _p(err), _s()), "gi_conv2d_bf16")
     return out if out is not None else out32
+
+
+def conv2d_head(x: torch.Tensor, wp: torch.Tensor, cout: int, bias: torch.Tensor, head_w: torch.Tensor,
+                head_b: torch.Tensor, out: torch.Tensor, relu: bool = True, err: torch.Tensor | None = None):
+    """3x3 convolution with a fused two-output 1x1 head: out (FP32, [.., 2]) only."""
+    n, h, w, cin = x.shape
+    _need(x, n * h * w * cin, torch.bfloat16, "x")
+    _need(out, n * h * w * 2, torch.float32, "out")
+    _need(head_w, 2 * cout, torch.float32, "head_w")
+    _need(head_b, 2, torch.float32, "head_b")
+    _need(bias, cout, torch.float32, "bias")
+    check(_lib().gi_conv2d_head_bf16(_p(x), n, h, w, cin, _p(wp), _p(bias), cout,
+                                     api.GI_ACT_RELU if relu else api.GI_ACT_NONE, _p(head_w), _p(head_b), _p(out),
+                                     _p(err), _s()), "gi_conv2d_head_bf16")
+    return out
 
 
 def conv2d_wgrad(x: torch.Tensor, dy: torch.Tensor, cout: int, ksize: int, dw: torch.Tensor,
@@ -68,6 +104,11 @@ def conv2d_wgrad(x: torch.Tensor, dy: torch.Tensor, cout: int, ksize: int, dw: t
                  err: torch.Tensor | None = None) -> torch.Tensor:
     """dw (FP32, packed layout) += weight gradient; db += bias gradient."""
     n, h, w, cin = x.shape
+    _need(x, n * h * w * cin, torch.bfloat16, "x")
+    _need(dy, n * h * w * cout, torch.bfloat16, "dy")
+    _need(dw, cout * nkb_pad(cin, ksize) * 8, torch.float32, "dw")
+    if db is not None:
+        _need(db, cout, torch.float32, "db")
     need = int(_lib().gi_conv2d_wgrad_scratch_floats(n, h, w, cin, cout, ksize))
     if scratch is None or scratch.numel() < need:
         scratch = torch.empty(need, dtype=torch.float32, device=x.device)

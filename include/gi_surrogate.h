@@ -57,6 +57,15 @@ gi_status gi_conv2d_bf16(const gi_bf16* x, int n, int h, int w, int cin,
                          int act, const gi_bf16* mask, gi_bf16* y, int y_stride,
                          int y_off, float* y32, uint32_t* err, void* stream);
 
+/* 3x3 convolution (cin % 16 == 0) whose epilogue also applies a 1x1 head
+ * with two outputs to the activated, BF16-rounded result and writes only
+ * that: head_out[p][j] = head_b[j] + sum_c head_w[j][c] * y[p][c], j < 2
+ * (FP32, 2 per pixel); the convolution's own output is not stored. */
+gi_status gi_conv2d_head_bf16(const gi_bf16* x, int n, int h, int w, int cin,
+                              const gi_bf16* wt, const float* bias, int cout, int act,
+                              const float* head_w, const float* head_b, float* head_out,
+                              uint32_t* err, void* stream);
+
 /* dW[co, tap, ci] += sum over pixels of dy[p, co] * x[p + tap, ci] and
  * db[co] += sum dy[p, co] (db may be NULL); dw is FP32 in the packed
  * [cout][kblocks][8] layout.  scratch: FP32 workspace of at least
@@ -97,7 +106,7 @@ gi_status gi_channel_slice_add_bf16(const gi_bf16* x, size_t pixels, int c, gi_b
 /* Surrogate frame, step 1 (replaces the light map + G-buffer part of
  * gi_render_frame for GI_TECH_PCSS_POISSON): renders the light map into
  * d_depth and the camera visibility keys into the context, then writes
- * the network input d_feat (BF16 [height][width][8]; channels 0-3 used:
+ * the network input d_feat (BF16 [height][width][16]; channels 0-3 used:
  * hard visibility with the pre-test, clamped (z - map depth) * 64,
  * penumbra estimate in map texels / 8 from four blocker taps, and 1 /
  * 0.5 / 0 for pre-test passed / failed / background). */
@@ -106,15 +115,16 @@ gi_status gi_surrogate_features(gi_context* ctx, const gi_scene* scene, const gi
                                 const gi_vis_params* vis, int width, int height, float* d_depth,
                                 void* d_feat, void* stream);
 /* Surrogate frame, step 3 (after the U-Net wrote d_head, FP32
- * [height][width][16]: channel 0 the visibility, 1 the predicted absolute
- * error): background 0, failed pre-test the intensity, else the clamped
+ * [height][width][head_stride]: channel 0 the visibility, 1 the predicted
+ * absolute error): background 0, failed pre-test the intensity, else the clamped
  * prediction, or the exact PCSS value where the predicted error exceeds
  * err_threshold (counted into *d_fallback when not NULL).  Uses the keys
  * that gi_surrogate_features left in ctx. */
 gi_status gi_surrogate_finish(gi_context* ctx, const gi_scene* scene, int map_width, int map_height,
                               const float* d_depth, const float camera_mvp[16], const gi_vis_params* vis,
-                              int width, int height, const float* d_head, const void* d_feat,
-                              float err_threshold, float* d_vis, uint32_t* d_fallback, void* stream);
+                              int width, int height, const float* d_head, int head_stride,
+                              const void* d_feat, float err_threshold, float* d_vis,
+                              uint32_t* d_fallback, void* stream);
 /* Training loss of the surrogate over `pixels` pixels: L1 of the
  * visibility (channel 0 of head) against target on pixels whose feature 3
  * is 1, plus L1 of the error head (channel 1) against the current

@@ -40,7 +40,7 @@ def _torch_unet(net, f):
 
 def _feat(n, H, W, seed=0):
     g = torch.Generator().manual_seed(seed)
-    f = torch.zeros(n, H, W, 8)
+    f = torch.zeros(n, H, W, sg.FEATURES)
     f[..., 0] = (torch.rand(n, H, W, generator=g) > 0.5).float() * 0.75 + 0.25
     f[..., 1] = torch.rand(n, H, W, generator=g) * 2 - 0.5
     f[..., 2] = torch.rand(n, H, W, generator=g) * 2
@@ -105,6 +105,17 @@ def test_unet_gradients_match_torch():
     assert net.kernel_error() == 0
 
 
+def test_fused_head_matches_separate_head():
+    net = sg.UNet(0, seed=7)
+    f = _feat(1, 40, 64, seed=3).cuda()
+    full = net.forward(f)
+    h2 = torch.empty((1, 40, 64, 2), device="cuda")
+    net.forward_fused(f, h2)
+    torch.cuda.synchronize()
+    d = (full[..., :2] - h2).abs().max().item()
+    assert d < 1e-3 * (1.0 + full[..., :2].abs().max().item()), d
+
+
 def _pcss_frame(W=320, H=184, S=512):
     w = scenes.pcss_1080p(width=W, height=H, map_size=S, spheres=24)
     w.params.light_radius = 0.5
@@ -134,6 +145,7 @@ def test_surrogate_frame_fallback_is_exact(cuda_ctx):
     assert int(sf.fallback.item()) == 0
     I = w.params.shadow_intensity
     head = sf.head.cpu().numpy()[0]
+    assert head.shape[-1] == 2
     m = feat[..., 3]
     assert (v_net[m == 0] == 0).all()
     assert (v_net[m == 0.5] == np.float32(I)).all()
