@@ -18,6 +18,16 @@ one shadowed frame: light-view depth map, G-buffer, visibility.
   cpu_baseline  the CPU oracle (restatement of the reference's passes) on
           the host cores for a bounded sample of whole frames
 
+Extra legs in the same line (not the headline):
+  batched     the 256-scene 1280 x 720 workload (1-8 spot lights per
+              scene, maps 512^2-4096^2, 5 x 5 PCF) replayed as one CUDA
+              graph after autotuning, against the same light-frames
+              rendered one gi_render_frame call at a time
+  surrogate   the learned PCSS surrogate (BF16 U-Net on the tcgen05
+              convolution kernels) trained here on freshly rendered
+              frames, then its 1080p frame time, its error against the
+              exact PCSS frame, and the tensor roofline of the U-Net
+
 --impl reference times that CPU implementation alone (the reference's own
 passes need OpenGL, which this machine does not have).  For N > 1 every rank
 renders its own frames (replicas; no collective on the data path) and the
@@ -54,6 +64,9 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-scene batched leg")
     ap.add_argument("--batched-scenes", type=int, default=256)
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate leg")
+    ap.add_argument("--surrogate-frames", type=int, default=8000,
+                    help="training frames (one 256^2 crop each, batch 16) for the surrogate leg")
     ap.add_argument("--profile", action="store_true",
                     help="render --warmup frames and exit (the command profiled with ncu)")
     return ap.parse_args()
@@ -294,6 +307,75 @@ def run_batched(args, ctx, stream, local):
     }
 
 
+def run_surrogate(args, ctx, stream, local, w, fr, bufs):
+    """The learned PCSS surrogate on the same 1080p frame: trained here from
+    scratch on freshly rendered PCSS frames of varied scenes, then timed and
+    compared with the exact PCSS visibility of the benchmark frame."""
+    import torch
+
+    import globalillumination_gb300 as gi
+    from globalillumination_gb300 import surrogate as sg
+
+    S, W, H = w.map_params.width, w.camera.width, w.camera.height
+    net = sg.UNet(local, seed=1)
+    t0 = time.perf_counter()
+    tr = sg.train(ctx, net, frames=args.surrogate_frames, batch=16, crop=256, lr=1e-3, verbose=False,
+                  log_every=max(1, args.surrogate_frames // 16 // 4))
+    train_s = time.perf_counter() - t0
+    gi.render_frame(ctx, w.scene, fr, w.map_params, w.params, W, H, bufs, stream)
+    sf = sg.SurrogateFrame(net, S, W, H)
+    out = {}
+    for thr, key in ((float("inf"), "network_only"), (sg.ERR_THRESHOLD, "with_fallback")):
+        sf.fallback.zero_()
+        v = sf.render(ctx, w.scene, fr, w.map_params, w.params, threshold=thr)
+        torch.cuda.synchronize()
+        err = (v - bufs.vis).abs()
+        geo = sf.feat[0, ..., 3].reshape(-1).float() > 0
+        out[key] = {"mae_all_pixels": float(err.mean()), "mae_geometry_pixels": float(err[geo].mean()),
+                    "max_abs_error": float(err.max()), "fallback_fraction": int(sf.fallback.item()) / (W * H)}
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps=20):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(reps):
+            fn()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / reps
+
+    t_frame = timed(lambda: sf.render(ctx, w.scene, fr, w.map_params, w.params))
+    t_net = timed(lambda: net.forward_fused(sf.feat, sf.head))
+    t_plain = timed(lambda: gi.render_frame(ctx, w.scene, fr, w.map_params, w.params, W, H, bufs, stream))
+    flops = net.flops(H, W)
+    peak, kind = measured_bf16_peak()
+    if net.kernel_error():
+        raise RuntimeError("a tcgen05 kernel reported a timed-out wait")
+    return {
+        "workload": "pcss_1080p frame, PCSS (Poisson) visibility predicted by a BF16 U-Net (32/64/96/128 channels)",
+        "frames_per_s": 1000.0 / t_frame, "ms_per_frame": t_frame,
+        "plain_pcss_frames_per_s": 1000.0 / t_plain,
+        "accuracy_vs_plain_pcss": out, "error_threshold": sg.ERR_THRESHOLD,
+        "training": {"frames": tr["frames"], "batch": 16, "crop": 256, "steps": tr["steps"], "seconds": train_s,
+                     "optimizer": "Adam lr 1e-3", "final_crop_mae": tr["history"][-1]["mae"]},
+        "roofline": {"kernel": "U-Net forward (tcgen05 implicit-GEMM convolutions, fused head)", "bound": "tensor",
+                     "achieved": flops / (t_net / 1000.0) / 1e12, "peak": peak, "unit": "TFLOP/s",
+                     "frac": flops / (t_net / 1000.0) / 1e12 / peak, "peak_source": kind,
+                     "flops_per_frame": flops, "ms": t_net},
+    }
+
+
+def measured_bf16_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured (burst)"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback"
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -426,6 +508,9 @@ def run_ours(args):
     batched = None
     if not args.no_batched:
         batched = run_batched(args, ctx, stream, local)
+    surrogate = None
+    if not args.no_surrogate and rank == 0:
+        surrogate = run_surrogate(args, ctx, stream, local, w, fr, bufs)
 
     # sanity: the frame produced soft shadows
     vis_host = bufs.vis.cpu().numpy()
@@ -459,6 +544,8 @@ def run_ours(args):
         }
         if batched is not None:
             line["batched"] = batched
+        if surrogate is not None:
+            line["surrogate"] = surrogate
         if clk and any(r in clk["reasons"] for r in THROTTLE_BAD):
             line["clocks_warning"] = "throttled during the timed region"
         if world == 1 and not args.no_cpu_baseline:
