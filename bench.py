@@ -23,6 +23,10 @@ Extra legs in the same line (not the headline):
               scene, maps 512^2-4096^2, 5 x 5 PCF) replayed as one CUDA
               graph after autotuning, against the same light-frames
               rendered one gi_render_frame call at a time
+  heavy       the 3840 x 2160 scene (2.1M-triangle displaced sphere, 8
+              lights, 4096^2 maps): PCSS and RBSM frames of all 8 lights
+              as one CUDA graph, shadow-volume stencil counts, and the
+              surrogate's 4K frame
   surrogate   the learned PCSS surrogate (BF16 U-Net on the tcgen05
               convolution kernels) trained here on freshly rendered
               frames, then its 1080p frame time, its error against the
@@ -65,6 +69,7 @@ def parse_args():
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-scene batched leg")
     ap.add_argument("--batched-scenes", type=int, default=256)
     ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate leg")
+    ap.add_argument("--no-heavy", action="store_true", help="skip the heavy 2160p leg")
     ap.add_argument("--surrogate-frames", type=int, default=8000,
                     help="training frames (one 256^2 crop each, batch 16) for the surrogate leg")
     ap.add_argument("--profile", action="store_true",
@@ -354,7 +359,7 @@ def run_surrogate(args, ctx, stream, local, w, fr, bufs):
     peak, kind = measured_bf16_peak()
     if net.kernel_error():
         raise RuntimeError("a tcgen05 kernel reported a timed-out wait")
-    return {
+    summary = {
         "workload": "pcss_1080p frame, PCSS (Poisson) visibility predicted by a BF16 U-Net (32/64/96/128 channels)",
         "frames_per_s": 1000.0 / t_frame, "ms_per_frame": t_frame,
         "plain_pcss_frames_per_s": 1000.0 / t_plain,
@@ -366,6 +371,86 @@ def run_surrogate(args, ctx, stream, local, w, fr, bufs):
                      "frac": flops / (t_net / 1000.0) / 1e12 / peak, "peak_source": kind,
                      "flops_per_frame": flops, "ms": t_net},
     }
+    return summary, net
+
+
+def run_heavy(args, ctx, stream, local, net=None):
+    """The heavy 3840 x 2160 scene: a 1024 x 1024 UV-grid sphere displaced by
+    Perlin noise (2,097,152 triangles) over a ground quad, 8 spot lights with
+    4096^2 maps.  Per technique one frame = all 8 lights (camera keys once,
+    8 light maps, 8 visibility images) replayed as one CUDA graph; plus the
+    shadow-volume stencil counts of every light and, when a trained
+    surrogate is given, its 4K frame for the first light."""
+    import torch
+
+    import globalillumination_gb300 as gi
+    from globalillumination_gb300 import _capi as api
+    from globalillumination_gb300 import scenes
+
+    t0 = time.perf_counter()
+    w = scenes.heavy_2160p()
+    w.scene.upload(ctx, stream)
+    tris = int(w.scene.info().num_triangles)
+    W, H, S = w.camera.width, w.camera.height, w.map_params.width
+    lights = [gi.ViewSpec(eye=e, at=(0.0, 0.0, 0.0), width=S, height=S, fovy_deg=90.0) for e in w.lights]
+    maps = [w.map_params] * len(lights)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(reps):
+            fn()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / reps
+
+    out = {"workload": "heavy_2160p", "triangles": tris, "lights": len(lights), "map": f"{S}x{S}",
+           "camera": f"{W}x{H}"}
+    vis = torch.empty((len(lights), H, W), device="cuda")
+    for tech, key in ((api.GI_TECH_PCSS_POISSON, "pcss_poisson"), (api.GI_TECH_SMSR_NONCONSERVATIVE, "rbsm_smsr")):
+        p = gi.ShadowParams.defaults(tech)
+        p.light_radius = w.params.light_radius
+        p.pcss_min_blocker_depth = 0.0
+        b = gi.Batch(local)
+        b.add_frame(w.scene, w.camera, lights, maps, p, vis)
+        b.build(1)
+        ms = timed(lambda: b.run(stream), 5)
+        soft = float(((vis > 0.25) & (vis < 1.0)).float().mean())
+        out[key] = {"ms_per_frame_8_lights": ms, "light_frames_per_s": len(lights) * 1000.0 / ms,
+                    "soft_pixel_fraction": soft}
+        b.close()
+    stencil = torch.empty(W * H, dtype=torch.uint8, device="cuda")
+    fr0 = gi.frame_setup(lights[0], w.camera)
+
+    def volumes():
+        for l in lights:
+            gi.shadow_volume_counts(ctx, w.scene, l.eye, fr0.camera_mvp, W, H, stencil, stream=stream)
+
+    ms = timed(volumes, 2)
+    out["shadow_volumes"] = {"ms_per_frame_8_lights": ms, "volume_triangles_per_light": 6 * tris,
+                             "lit_fraction_last_light": float((stencil == 0).float().mean())}
+    if net is not None:
+        from globalillumination_gb300 import surrogate as sg
+
+        p = gi.ShadowParams.defaults(api.GI_TECH_PCSS_POISSON)
+        p.light_radius = w.params.light_radius
+        p.pcss_min_blocker_depth = 0.0
+        bufs = gi.allocate_frame(S, S, W, H, local)
+        sf = sg.SurrogateFrame(net, S, W, H)
+        ms_plain = timed(lambda: gi.render_frame(ctx, w.scene, fr0, w.map_params, p, W, H, bufs, stream), 3)
+        ms_sg = timed(lambda: sf.render(ctx, w.scene, fr0, w.map_params, p), 3)
+        sf.fallback.zero_()
+        v = sf.render(ctx, w.scene, fr0, w.map_params, p)
+        gi.render_frame(ctx, w.scene, fr0, w.map_params, p, W, H, bufs, stream)
+        torch.cuda.synchronize()
+        out["surrogate_one_light"] = {"ms_plain_pcss": ms_plain, "ms_surrogate": ms_sg,
+                                      "mae_all_pixels": float((v - bufs.vis).abs().mean()),
+                                      "fallback_fraction": int(sf.fallback.item()) / (W * H)}
+    out["setup_s"] = time.perf_counter() - t0
+    return out
 
 
 def measured_bf16_peak():
@@ -509,8 +594,12 @@ def run_ours(args):
     if not args.no_batched:
         batched = run_batched(args, ctx, stream, local)
     surrogate = None
+    net = None
     if not args.no_surrogate and rank == 0:
-        surrogate = run_surrogate(args, ctx, stream, local, w, fr, bufs)
+        surrogate, net = run_surrogate(args, ctx, stream, local, w, fr, bufs)
+    heavy = None
+    if not args.no_heavy and rank == 0:
+        heavy = run_heavy(args, ctx, stream, local, net)
 
     # sanity: the frame produced soft shadows
     vis_host = bufs.vis.cpu().numpy()
@@ -546,6 +635,8 @@ def run_ours(args):
             line["batched"] = batched
         if surrogate is not None:
             line["surrogate"] = surrogate
+        if heavy is not None:
+            line["heavy"] = heavy
         if clk and any(r in clk["reasons"] for r in THROTTLE_BAD):
             line["clocks_warning"] = "throttled during the timed region"
         if world == 1 and not args.no_cpu_baseline:

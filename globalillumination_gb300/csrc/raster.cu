@@ -934,6 +934,120 @@ __global__ void __launch_bounds__(256) k_bin_raster(BinArgs a) {
     }
 }
 
+// ---- stencil slivers ------------------------------------------------------
+// Extruded shadow-volume sides are long, thin triangles whose bounding boxes
+// cover most of the screen.  Every stencil record spanning more than four
+// bins is drawn here instead of through bin pairs: one warp per triangle,
+// lanes over rows.  On a row the covered pixel centres form one interval;
+// each edge bounds it by floor((K - c) / (B * 256)), tracked exactly from
+// row to row with an integer quotient / remainder step, so the interval is
+// the set of pixels the per-pixel inside test accepts (each pixel is still
+// tested before its update).  Counts are added with global atomics after
+// k_bin_raster (sums commute with its stores and atomics).
+struct FloorTrack {
+    int64_t q, rem, den, dq, dr;
+    __device__ __forceinline__ static int64_t fdiv(int64_t a, int64_t b) {  // b > 0
+        int64_t q = a / b;
+        if (a % b != 0 && a < 0) --q;
+        return q;
+    }
+    __device__ __forceinline__ void init(int64_t num, int64_t d, int64_t delta) {
+        den = d;
+        q = fdiv(num, d);
+        rem = num - q * d;
+        dq = fdiv(delta, d);
+        dr = delta - dq * d;
+    }
+    __device__ __forceinline__ void step() {
+        q += dq;
+        rem += dr;
+        if (rem >= den) {
+            rem -= den;
+            ++q;
+        }
+    }
+};
+
+__global__ void __launch_bounds__(256) k_sliver(BinArgs a) {
+    const unsigned n = min(a.ctr[1], a.big_cap);
+    const int lane = threadIdx.x & 31;
+    const unsigned nwarps = gridDim.x * (blockDim.x >> 5);
+    for (unsigned i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += nwarps) {
+        const BRec r = a.recs[a.big_list[i]];
+        int64_t A[3], B[3], XA[3], YA[3];
+        bool tl[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int ia = (k + 1) % 3, ib = (k + 2) % 3;
+            A[k] = (int64_t)r.X[ib] - r.X[ia];
+            B[k] = (int64_t)r.Y[ib] - r.Y[ia];
+            tl[k] = (B[k] < 0) || (B[k] == 0 && A[k] < 0);
+            XA[k] = r.X[ia];
+            YA[k] = r.Y[ia];
+        }
+        const int y_first = (int)r.y0 + lane;
+        if (y_first > (int)r.y1) continue;
+        // edge k at row y: E(x) = K - B * (x * 256 + 128), K = A * (py - Ya) + B * Xa
+        FloorTrack f[3];
+        int64_t K0[3];
+        const int64_t py0 = (int64_t)y_first * kSub + kSub / 2;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            K0[k] = A[k] * (py0 - YA[k]) + B[k] * XA[k];
+            const int64_t dK = A[k] * (int64_t)(32 * kSub);
+            if (B[k] > 0) {
+                // x <= floor((K - 128 B - (tl ? 0 : 1)) / (256 B))
+                f[k].init(K0[k] - B[k] * (kSub / 2) - (tl[k] ? 0 : 1), B[k] * kSub, dK);
+            } else if (B[k] < 0) {
+                const int64_t Bp = -B[k];
+                if (tl[k])  // x >= ceil((-K - 128 Bp) / (256 Bp)) = -floor((K + 128 Bp) / (256 Bp))
+                    f[k].init(K0[k] + Bp * (kSub / 2), Bp * kSub, dK);
+                else  // x >= floor((-K - 128 Bp) / (256 Bp)) + 1
+                    f[k].init(-K0[k] - Bp * (kSub / 2), Bp * kSub, -dK);
+            }
+        }
+        const float sgn_front = (r.flags & kFlagFront) ? 1.0f : -1.0f;
+        const int inc = sgn_front > 0.0f ? 1 : -1;
+        for (int y = y_first, it = 0; y <= (int)r.y1; y += 32, ++it) {
+            if (it > 0) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    K0[k] += A[k] * (int64_t)(32 * kSub);
+                    if (B[k] != 0) f[k].step();
+                }
+            }
+            int lo = r.x0, hi = r.x1;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                if (B[k] == 0) {
+                    if (!(K0[k] > 0 || (K0[k] == 0 && tl[k]))) hi = lo - 1;
+                } else if (B[k] > 0) {
+                    if (f[k].q < (int64_t)hi) hi = (int)max(f[k].q, (int64_t)lo - 1);
+                } else {
+                    const int64_t xm = tl[k] ? -f[k].q : f[k].q + 1;
+                    if (xm > (int64_t)lo) lo = (int)min(xm, (int64_t)hi + 1);
+                }
+            }
+            const int64_t py = (int64_t)y * kSub + kSub / 2;
+            for (int x = lo; x <= hi; ++x) {
+                const int64_t px = (int64_t)x * kSub + kSub / 2;
+                int64_t E[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) E[k] = A[k] * (py - YA[k]) - B[k] * (px - XA[k]);
+                const bool in = (E[0] > 0 || (E[0] == 0 && tl[0])) && (E[1] > 0 || (E[1] == 0 && tl[1])) &&
+                                (E[2] > 0 || (E[2] == 0 && tl[2]));
+                if (!in) continue;
+                const float l1 = (float)E[1] * r.inv_area, l2 = (float)E[2] * r.inv_area;
+                const float z = clamp01(r.z0 + (l1 * r.dz1 + l2 * r.dz2));
+                const size_t idx = (size_t)y * a.r.W + x;
+                const float d = __uint_as_float(__ldg(a.r.depth + idx));
+                const bool pass = a.r.depth_func == GI_DEPTH_LEQUAL ? (z <= d) : (z < d);
+                if (pass) atomicAdd(a.r.counts + idx, inc);
+            }
+        }
+    }
+}
+
 // Spilled sub-triangles: re-derived from (primitive, sub) and rasterised by
 // one thread each with global atomics after k_bin_raster.
 template <int MODE>
@@ -1516,11 +1630,16 @@ static gi_status run_binned(gi_context* ctx, dev::RasterArgs& r, int mode, cudaS
             if (prims) dev::k_bin_setup<dev::MODE_STENCIL><<<gsetup, 128, 0, st>>>(a);
             break;
     }
-    dev::k_big_scan<<<1, 1024, 0, st>>>(a);
-    dev::k_big_pairs<false><<<sms * 4, 256, 0, st>>>(a);
+    // stencil records spanning more than four bins go to k_sliver instead of
+    // the bin-pair expansion (big_count stays zero)
+    const bool pairs = mode != dev::MODE_STENCIL;
+    if (pairs) {
+        dev::k_big_scan<<<1, 1024, 0, st>>>(a);
+        dev::k_big_pairs<false><<<sms * 4, 256, 0, st>>>(a);
+    }
     dev::k_bin_scan<<<1, 1024, 0, st>>>(a);
     dev::k_bin_fill_small<<<gfill, 256, 0, st>>>(a);
-    dev::k_big_pairs<true><<<sms * 4, 256, 0, st>>>(a);
+    if (pairs) dev::k_big_pairs<true><<<sms * 4, 256, 0, st>>>(a);
     // the raster leaves empty bins alone: clear the target first
     const size_t npx = (size_t)r.W * r.H;
     const unsigned gclear = std::min<unsigned>(grid_for(npx / 4 + 1, 256), sms * 8);
@@ -1545,10 +1664,11 @@ static gi_status run_binned(gi_context* ctx, dev::RasterArgs& r, int mode, cudaS
             break;
         default:
             dev::k_bin_raster<dev::MODE_STENCIL><<<graster, 256, 0, st>>>(a);
+            dev::k_sliver<<<sms * 8, 256, 0, st>>>(a);
             dev::k_spill<dev::MODE_STENCIL><<<sms * 2, 128, 0, st>>>(a);
             break;
     }
-    ctx->launches += (prims ? 8 : 7) + (mode == dev::MODE_STENCIL ? 0 : 1);
+    ctx->launches += (prims ? 8 : 7) + (mode == dev::MODE_STENCIL ? -2 : 1);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail_cuda(e, "binned raster launch");
     return GI_OK;

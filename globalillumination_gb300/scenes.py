@@ -93,7 +93,8 @@ def heavy_2160p(width: int = 3840, height: int = 2160, map_size: int = 4096, gri
         eyes.append((10.0 * math.cos(a) * 0.7, 10.0 * 0.7, 10.0 * math.sin(a) * 0.7))
     light = ViewSpec(eye=eyes[0], at=(0.0, 0.0, 0.0), width=map_size, height=map_size, fovy_deg=90.0)
     camera = ViewSpec(eye=(0.0, 9.0, -14.0), at=(0.0, 1.5, 0.0), width=width, height=height)
-    mp = MapParams(map_size, map_size, bias_mode=api.GI_BIAS_POLYGON_OFFSET)
+    mp = MapParams(map_size, map_size, bias_mode=api.GI_BIAS_POLYGON_OFFSET, offset_factor=4.0,
+                   offset_units=20.0)
     p = ShadowParams.defaults(technique)
     p.light_radius = 0.25
     p.pcss_min_blocker_depth = 0.0

@@ -181,6 +181,29 @@ def test_shadow_volume_counts_bit_exact(cuda_ctx, depth_func, dims):
     assert (st_ref != 0).sum() > 0 and (st_ref == 0).sum() > 0
 
 
+@pytest.mark.parametrize("light_eye", [(4.9, 7.0, 0.0), (-2.0, 6.0, -5.0)])
+def test_shadow_volume_slivers_bit_exact(cuda_ctx, light_eye):
+    """A displaced sphere (the heavy scene's shape at a small size): its
+    extruded sides are long slivers, drawn by the row-span path."""
+    torch = _torch()
+    W, H = 320, 240
+    s = gi.Scene()
+    s.ground(10.0, 0.0)
+    s.displaced_sphere(40, 20, 2.0, 0.3, (0.0, 2.6, 0.0), 0x5EED0004)
+    cam = gi.ViewSpec(eye=(0.0, 9.0, -14.0), at=(0.0, 1.5, 0.0), width=W, height=H)
+    light = gi.ViewSpec(eye=light_eye, at=(0.0, 0.0, 0.0), width=64, height=64)
+    fr = gi.frame_setup(light, cam)
+    s.upload(cuda_ctx)
+    st = torch.empty(W * H, dtype=torch.uint8, device="cuda")
+    gi.shadow_volume_counts(cuda_ctx, s, light.eye, fr.camera_mvp, W, H, st)
+    torch.cuda.synchronize()
+    p, n, i = s.arrays()
+    st_ref, _ = oracle.shadow_volume_counts(p, n, i, light.eye, 100.0, fr.camera_mvp, W, H, api.GI_DEPTH_LEQUAL)
+    got = st.cpu().numpy()
+    assert np.array_equal(got, st_ref), f"{int((got != st_ref).sum())} stencil values differ"
+    assert (st_ref != 0).sum() > 1000
+
+
 @pytest.mark.parametrize("tech", [api.GI_TECH_PCF, api.GI_TECH_PCSS_POISSON, api.GI_TECH_SMSR_NONCONSERVATIVE,
                                   api.GI_TECH_RSMSS])
 @pytest.mark.parametrize("store", [False, True])
