@@ -156,6 +156,7 @@ _PROTOS = {
     "gi_context_launch_count": (C.c_uint64, [_VP]),
     "gi_context_set_profiling": (C.c_int, [_VP, C.c_int]),
     "gi_context_phase_ms": (C.c_int, [_VP, C.c_float * 3]),
+    "gi_context_set_tuning": (C.c_int, [_VP, C.c_int, C.c_int]),
     "gi_scene_load_config": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(_VP)]),
     "gi_scene_create": (C.c_int, [C.POINTER(_VP)]),
     "gi_scene_destroy": (None, [_VP]),

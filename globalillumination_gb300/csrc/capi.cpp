@@ -80,14 +80,22 @@ extern "C" gi_status gi_context_create(int device, gi_context** out) {
     if (e != cudaSuccess) return gi::fail_cuda(e, "cudaSetDevice");
     gi_context* c = new gi_context();
     c->device = device;
-    e = cudaMalloc(&c->d_status, 64 * sizeof(unsigned));
-    if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, 64 * sizeof(unsigned));
-    if (e == cudaSuccess) e = cudaMallocHost(&c->h_status, 64 * sizeof(unsigned));
+    e = cudaMalloc(&c->d_status, 128 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, 128 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_status, 128 * sizeof(unsigned));
+    cudaStream_t aux = nullptr;
+    cudaEvent_t fev = nullptr, jev = nullptr;
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking);
+    c->aux_stream = aux;
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fev, cudaEventDisableTiming);
+    c->fork_ev = fev;
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&jev, cudaEventDisableTiming);
+    c->join_ev = jev;
     if (e != cudaSuccess) {
         gi_context_destroy(c);
         return gi::fail_cuda(e, "gi_context_create allocation");
     }
-    std::memset(c->h_status, 0, 64 * sizeof(unsigned));
+    std::memset(c->h_status, 0, 128 * sizeof(unsigned));
     *out = c;
     return GI_OK;
 }
@@ -106,12 +114,24 @@ extern "C" void gi_context_destroy(gi_context* c) {
         for (int i = 0; i < 8; ++i) cudaFree(c->tier_buf[k][i]);
     for (int i = 0; i < 4; ++i)
         if (c->phase_ev[i]) cudaEventDestroy(static_cast<cudaEvent_t>(c->phase_ev[i]));
+    if (c->aux_stream) cudaStreamDestroy(static_cast<cudaStream_t>(c->aux_stream));
+    if (c->fork_ev) cudaEventDestroy(static_cast<cudaEvent_t>(c->fork_ev));
+    if (c->join_ev) cudaEventDestroy(static_cast<cudaEvent_t>(c->join_ev));
     cudaFree(c->d_status);
     if (c->h_status) cudaFreeHost(c->h_status);
     delete c;
 }
 
 extern "C" uint64_t gi_context_launch_count(const gi_context* c) { return c ? c->launches : 0; }
+
+extern "C" gi_status gi_context_set_tuning(gi_context* c, int tiny_px, int coop_px) {
+    if (!c) return fail(GI_ERR_INVALID_ARG, "gi_context_set_tuning: NULL context");
+    if (tiny_px < 1 || coop_px <= tiny_px || coop_px > 1024)
+        return fail(GI_ERR_INVALID_ARG, "gi_context_set_tuning: need 1 <= tiny_px < coop_px <= 1024");
+    c->tiny_px = tiny_px;
+    c->coop_px = coop_px;
+    return GI_OK;
+}
 
 extern "C" gi_status gi_context_set_profiling(gi_context* c, int enable) {
     if (!c) return fail(GI_ERR_INVALID_ARG, "gi_context_set_profiling: NULL context");
@@ -464,15 +484,25 @@ extern "C" gi_status gi_render_frame(gi_context* ctx, const gi_scene* s, const g
     if ((size_t)s->dev_triangles >= ((size_t)1 << 29))
         return fail(GI_ERR_CAPACITY, "gi_render_frame: more than 2^29 triangles");
     cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    cudaStream_t aux = static_cast<cudaStream_t>(ctx->aux_stream);
     auto mark = [&](int i) {
         if (ctx->profiling) cudaEventRecord(static_cast<cudaEvent_t>(ctx->phase_ev[i]), cs);
     };
+    // the camera-key pass runs on the context's second stream, concurrently
+    // with the light map; the visibility kernel waits for both
     mark(0);
-    st = gi::raster_depth_map(ctx, s, light_mvp, mp->width, mp->height, mp->bias_mode,
-                              mp->constant_bias, mp->offset_factor, mp->offset_units, d_depth,
-                              small_px_default(), cs);
+    cudaError_t e = cudaEventRecord(static_cast<cudaEvent_t>(ctx->fork_ev), cs);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, static_cast<cudaEvent_t>(ctx->fork_ev), 0);
+    if (e != cudaSuccess) return gi::fail_cuda(e, "gi_render_frame: fork");
+    st = gi::raster_gbuffer_keys(ctx, s, camera_mvp, W, H, aux);
+    e = cudaEventRecord(static_cast<cudaEvent_t>(ctx->join_ev), aux);
+    if (st == GI_OK)
+        st = gi::raster_depth_map(ctx, s, light_mvp, mp->width, mp->height, mp->bias_mode,
+                                  mp->constant_bias, mp->offset_factor, mp->offset_units, d_depth,
+                                  small_px_default(), cs);
     mark(1);
-    if (st == GI_OK) st = gi::raster_gbuffer_keys(ctx, s, camera_mvp, W, H, cs);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, static_cast<cudaEvent_t>(ctx->join_ev), 0);
+    if (e != cudaSuccess) return gi::fail_cuda(e, "gi_render_frame: join");
     mark(2);
     if (st == GI_OK)
         st = gi::launch_frame_visibility(ctx, vp, d_depth, mp->width, mp->height, s, camera_mvp, d_vis,

@@ -89,11 +89,17 @@ struct gi_context {
     // tier thresholds (bounding-box pixels): tiny <= tiny_px < warp <= coop_px
     int tiny_px = 16;
     int coop_px = 1024;
-    // status words (64): [4..11] counters of the binned raster (records, big
-    // records, spills, error bits, admitted big pairs as u64, work items),
-    // [32..55] counters of the tiered raster
+    // status words (128): [4..11] counters of the binned raster (records,
+    // big records, spills, error bits, admitted big pairs as u64, work
+    // items), [32..55] counters of the tiered light-map pass, [64..87] of
+    // the tiered camera-key pass (the two passes may run concurrently)
     unsigned int* d_status = nullptr;
     unsigned int* h_status = nullptr;  // pinned mirror
+    // second stream for the camera-key pass of gi_render_frame, and the
+    // fork / join events (cudaStream_t / cudaEvent_t)
+    void* aux_stream = nullptr;
+    void* fork_ev = nullptr;
+    void* join_ev = nullptr;
     // phase timing (cudaEvent_t handles) for gi_render_frame
     bool profiling = false;
     void* phase_ev[4] = {};

@@ -1708,7 +1708,7 @@ static gi_status run_tiered(gi_context* ctx, dev::RasterArgs& r, int mode, cudaS
     a.coop_px = ctx->coop_px;
     a.rec_of = keys ? static_cast<unsigned*>(buf[6]) : nullptr;
     a.rres = keys ? static_cast<uint4*>(buf[7]) : nullptr;
-    a.ctr = ctx->d_status + 32;  // 24 words
+    a.ctr = ctx->d_status + (keys ? 64 : 32);  // 24 words per set
     cudaError_t e = cudaMemsetAsync(a.ctr, 0, 24 * sizeof(unsigned), st);
     if (e != cudaSuccess) return fail_cuda(e, "tiered raster memset");
     const unsigned sms = (unsigned)sm_count(ctx->device);

@@ -68,6 +68,10 @@ class Context:
     def launch_count(self) -> int:
         return int(_lib().gi_context_launch_count(self.handle))
 
+    def set_tuning(self, tiny_px: int, coop_px: int) -> None:
+        """Rasteriser tier thresholds (results do not depend on them)."""
+        check(_lib().gi_context_set_tuning(self.handle, int(tiny_px), int(coop_px)), "gi_context_set_tuning")
+
     def set_profiling(self, enable: bool) -> None:
         check(_lib().gi_context_set_profiling(self.handle, int(bool(enable))), "gi_context_set_profiling")
 

@@ -68,10 +68,16 @@ void gi_context_destroy(gi_context* ctx);
 /* Number of kernel launches issued through this context since creation. */
 uint64_t gi_context_launch_count(const gi_context* ctx);
 /* Phase timing for benchmarks: while enabled, gi_render_frame records CUDA
- * events on its stream around its three phases (light map, visibility keys,
- * resolve + visibility); gi_context_phase_ms waits for the last call's
- * events and returns the three durations in milliseconds. */
+ * events on its stream around its three phases (light map — the camera
+ * visibility keys run concurrently on a second stream —, the wait for the
+ * keys after the map, resolve + visibility); gi_context_phase_ms waits for
+ * the last call's events and returns the three durations in milliseconds. */
 gi_status gi_context_set_profiling(gi_context* ctx, int enable);
+/* Rasteriser tier thresholds (bounding-box pixels): triangles up to
+ * tiny_px are drawn by one thread, up to coop_px by one warp, larger ones
+ * by tiles (defaults 16 / 1024; 1 <= tiny_px < coop_px <= 1024).  Results
+ * do not depend on them. */
+gi_status gi_context_set_tuning(gi_context* ctx, int tiny_px, int coop_px);
 gi_status gi_context_phase_ms(gi_context* ctx, float ms[3]);
 
 /* ------------------------------------------------------------------ */
