@@ -856,7 +856,7 @@ __global__ void __launch_bounds__(256) k_bin_raster(BinArgs a) {
             const bool in = colin && y >= (int)r.y0 && y <= (int)r.y1 &&
                             (E[0] > 0 || (E[0] == 0 && tl[0])) && (E[1] > 0 || (E[1] == 0 && tl[1])) &&
                             (E[2] > 0 || (E[2] == 0 && tl[2]));
-            if (in) bin_frag<MODE>(a, tile, dtile, (row0 + 8 * k) * kBin + col, r, (float)E[1], (float)E[2]);
+            if (in) bin_frag<MODE>(a, tile, dtile, (row0 + 8 * k) * kBin + col, r, i2f(E[1]), i2f(E[2]));
 #pragma unroll
             for (int i = 0; i < 3; ++i) E[i] += A[i] * (8 * kSub);
         }
@@ -908,8 +908,8 @@ __global__ void __launch_bounds__(256) k_bin_raster(BinArgs a) {
                     E[i] = E0[i] + A[i] * (int64_t)(dy << kSubBits) - B[i] * (int64_t)(dx << kSubBits);
                 in = (E[0] > 0 || (E[0] == 0 && tl[0])) && (E[1] > 0 || (E[1] == 0 && tl[1])) &&
                      (E[2] > 0 || (E[2] == 0 && tl[2]));
-                fe1 = (float)E[1];
-                fe2 = (float)E[2];
+                fe1 = i2f(E[1]);
+                fe2 = i2f(E[2]);
             }
             if (in) bin_frag<MODE>(a, tile, dtile, (y0 + dy - oy) * kBin + (x0 + dx - ox), r, fe1, fe2);
         }
@@ -1037,7 +1037,7 @@ __global__ void __launch_bounds__(256) k_sliver(BinArgs a) {
                 const bool in = (E[0] > 0 || (E[0] == 0 && tl[0])) && (E[1] > 0 || (E[1] == 0 && tl[1])) &&
                                 (E[2] > 0 || (E[2] == 0 && tl[2]));
                 if (!in) continue;
-                const float l1 = (float)E[1] * r.inv_area, l2 = (float)E[2] * r.inv_area;
+                const float l1 = i2f(E[1]) * r.inv_area, l2 = i2f(E[2]) * r.inv_area;
                 const float z = clamp01(r.z0 + (l1 * r.dz1 + l2 * r.dz2));
                 const size_t idx = (size_t)y * a.r.W + x;
                 const float d = __uint_as_float(__ldg(a.r.depth + idx));
@@ -1291,7 +1291,7 @@ __global__ void __launch_bounds__(256) k_base(TierArgs a) {
             const bool in = y >= (int)r.y0 && y <= (int)r.y1 && (E[0] > 0 || (E[0] == 0 && tl[0])) &&
                             (E[1] > 0 || (E[1] == 0 && tl[1])) && (E[2] > 0 || (E[2] == 0 && tl[2]));
             if (in) {
-                const float l1 = (float)E[1] * r.inv_area, l2 = (float)E[2] * r.inv_area;
+                const float l1 = i2f(E[1]) * r.inv_area, l2 = i2f(E[2]) * r.inv_area;
                 float z = r.z0 + (l1 * r.dz1 + l2 * r.dz2);
                 if (MODE == MODE_DEPTH) {
                     z = clamp01(z + r.zoff);
@@ -1356,7 +1356,7 @@ __global__ void __launch_bounds__(128) k_tiny(TierArgs a) {
                 }
                 const bool in = (E[0] > 0 || (E[0] == 0 && tl[0])) && (E[1] > 0 || (E[1] == 0 && tl[1])) &&
                                 (E[2] > 0 || (E[2] == 0 && tl[2]));
-                if (in) rec_emit<MODE>(a, r, x, y, (float)E[1], (float)E[2]);
+                if (in) rec_emit<MODE>(a, r, x, y, i2f(E[1]), i2f(E[2]));
             }
         }
     }
@@ -1407,8 +1407,8 @@ __global__ void __launch_bounds__(256) k_coop(TierArgs a) {
                     E[k] = E0[k] + A[k] * (int64_t)(dy << kSubBits) - B[k] * (int64_t)(dx << kSubBits);
                 in = (E[0] > 0 || (E[0] == 0 && tl[0])) && (E[1] > 0 || (E[1] == 0 && tl[1])) &&
                      (E[2] > 0 || (E[2] == 0 && tl[2]));
-                fe1 = (float)E[1];
-                fe2 = (float)E[2];
+                fe1 = i2f(E[1]);
+                fe2 = i2f(E[2]);
             }
             if (in) rec_emit<MODE>(a, r, r.x0 + dx, r.y0 + dy, fe1, fe2);
         }
@@ -1480,7 +1480,7 @@ __global__ void __launch_bounds__(256) k_large_tiles(TierArgs a) {
         for (int k = 0; k < kTile / 2; ++k, y += 2) {
             const bool in = y >= py0 && y <= py1 && (E[0] > 0 || (E[0] == 0 && tl[0])) &&
                             (E[1] > 0 || (E[1] == 0 && tl[1])) && (E[2] > 0 || (E[2] == 0 && tl[2]));
-            if (in) rec_emit<MODE>(a, r, x, y, (float)E[1], (float)E[2]);
+            if (in) rec_emit<MODE>(a, r, x, y, i2f(E[1]), i2f(E[2]));
 #pragma unroll
             for (int i = 0; i < 3; ++i) E[i] += A[i] * (2 * kSub);
         }

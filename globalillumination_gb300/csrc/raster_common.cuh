@@ -201,9 +201,23 @@ __device__ __forceinline__ bool inside3(const Edges& e, const int64_t E[3]) {
            (E[2] > 0 || (E[2] == 0 && e.topleft[2]));
 }
 
+// int64 -> float with round-to-nearest-even, off the FP64 pipe (a narrow
+// unit on this GPU): for |v| < 2^47, v = h * 2^24 + l with h = v >> 24
+// (|h| < 2^23) and 0 <= l < 2^24, both exact in FP32; h * 2^24 is exact and
+// the one addition rounds once, giving the correctly rounded v, the same
+// value as the (float) cast.
+__device__ __forceinline__ float i2f(int64_t v) {
+    if (v >= -(1LL << 47) && v < (1LL << 47)) {
+        const int h = (int)(v >> 24);
+        const int l = (int)(v & 0xFFFFFF);
+        return __int2float_rn(h) * 16777216.0f + __int2float_rn(l);
+    }
+    return (float)v;
+}
+
 __device__ __forceinline__ float depth_at(const Setup& s, const int64_t E[3]) {
-    float l1 = (float)E[1] * s.inv_area;
-    float l2 = (float)E[2] * s.inv_area;
+    float l1 = i2f(E[1]) * s.inv_area;
+    float l2 = i2f(E[2]) * s.inv_area;
     return s.z[0] + (l1 * (s.z[1] - s.z[0]) + l2 * (s.z[2] - s.z[0]));
 }
 
@@ -284,7 +298,7 @@ __device__ __forceinline__ void resolve_record(const int X[3], const int Y[3], f
     for (int j = 0; j < 3; ++j) {
         const int a = (j + 1) % 3, b = (j + 2) % 3;
         const int64_t e = ((int64_t)X[b] - X[a]) * (py - Y[a]) - ((int64_t)Y[b] - Y[a]) * (px - X[a]);
-        const float l = (float)e * inv_area;
+        const float l = i2f(e) * inv_area;
         q[j] = l * iw[j];
     }
     const float sum = (q[0] + q[1]) + q[2];
@@ -360,7 +374,7 @@ __device__ __forceinline__ bool resolve_key(unsigned long long k, const float* p
     float q[3];
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-        const float l = (float)edge_at(e, j, px, py) * s.inv_area;
+        const float l = i2f(edge_at(e, j, px, py)) * s.inv_area;
         q[j] = l * s.iw[j];
     }
     const float sum = (q[0] + q[1]) + q[2];

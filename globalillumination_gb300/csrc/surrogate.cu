@@ -20,6 +20,8 @@
 //
 // Every wait on an mbarrier is bounded; on timeout the kernel sets bit 0 of
 // the caller's error word, still frees its tensor memory and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -304,16 +306,21 @@ __global__ void __launch_bounds__(kThreads) k_conv_fwd(ConvArgs a) {
 // A CTA computes R output rows x 128 pixels (R accumulators of 128 x N in
 // TMEM).  A stage holds two channel groups (16 channels) of the R + 2 input
 // rows y0-1 .. y0+R over x0-1 .. x0+128 ("slab": 130 pixels x 16 B per
-// row and group) and the weights of all 9 taps for those channels.  The
-// MMA of tap (dy, dx) for output row r reads A at slab row r + dy, shifted
-// by dx pixels (16 B): the 8-pixel core matrices stay contiguous (SBO 128 B)
-// and the second channel group is one slab further (LBO).  Each input
-// pixel is loaded (R + 2) / R times instead of 9.
+// row and group), fetched by one 4-D TMA box load per group (the halo
+// outside the image is zero-filled by TMA), and the weights of all 9 taps
+// for those channels, fetched by one bulk copy from the stage-ordered
+// packing [chunk][tap][group][cout][8].  The MMA of tap (dy, dx) for output
+// row r reads A at slab row r + dy, shifted by dx pixels (16 B): the
+// 8-pixel core matrices stay contiguous (SBO 128 B) and the second channel
+// group is one slab further (LBO).  Each input pixel is loaded (R + 2) / R
+// times instead of 9.  Warp 0 runs the main loop (lane 0 issues the TMA
+// loads and the MMAs; full / empty mbarriers per stage); all four warps
+// then drain the accumulators.
 constexpr int kSlabPx = 130;
 constexpr int kSlabRow = kSlabPx * 16;  // 2080 B
 
 struct SlabGeom {
-    int R, NS, ncols, a_bytes, b_bytes, stage_bytes;
+    int R, NS, ncols, slab, a_box, a_bytes, b_bytes, stage_bytes;
 };
 
 // Rows per CTA R and stage count NS: 32-wide outputs keep R = 4 so that
@@ -323,25 +330,58 @@ __host__ __device__ inline SlabGeom slab_geom(int N, int nk) {
     SlabGeom g;
     g.ncols = N <= 32 ? 32 : N <= 64 ? 64 : N <= 128 ? 128 : 256;
     g.R = N <= 32 ? 4 : N <= 64 ? 8 : N <= 128 ? 4 : 2;
-    g.a_bytes = 2 * (g.R + 2) * kSlabRow;
+    g.a_box = (g.R + 2) * kSlabRow;
+    g.slab = (g.a_box + 127) / 128 * 128;  // TMA destinations are 128-byte aligned
+    g.a_bytes = 2 * g.slab;
     g.b_bytes = 9 * 2 * N * 16;
     g.stage_bytes = g.a_bytes + g.b_bytes;
     g.NS = (nk > 2 && 3 * g.stage_bytes <= 200 * 1024) ? 3 : 2;
     return g;
 }
 
-__global__ void __launch_bounds__(kThreads) k_conv3_slab(ConvArgs a, int tiles_x, int tiles_y) {
-    extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ uint64_t bars[3];
+__host__ __device__ inline bool slab_layout(int kin, int ks) { return ks == 3 && kin % 16 == 0; }
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__global__ void __launch_bounds__(kThreads) k_conv3_slab(ConvArgs a, const __grid_constant__ CUtensorMap xmap,
+                                                         int tiles_x, int tiles_y) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
+    __shared__ uint64_t full[3], empty[3], done;
     __shared__ uint32_t tmem_slot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int N = a.cout;
-    const SlabGeom G = slab_geom(N, a.cin / 16);
+    const int nk = a.cin / 16;
+    const SlabGeom G = slab_geom(N, nk);
     const int R = G.R, NS = G.NS;
     const uint32_t tcols = (uint32_t)(R * G.ncols);
     if (warp == 0) tmem_alloc(&tmem_slot, tcols);
     if (tid == 0) {
-        for (int s = 0; s < NS; ++s) mbar_init(&bars[s], 1);
+        for (int s = 0; s < NS; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(&done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     fence_before();
@@ -350,84 +390,60 @@ __global__ void __launch_bounds__(kThreads) k_conv3_slab(ConvArgs a, int tiles_x
     const uint32_t tmem = tmem_slot;
     const int bx = blockIdx.x % tiles_x;
     const int by = (blockIdx.x / tiles_x) % tiles_y;
-    const long long img = blockIdx.x / ((long long)tiles_x * tiles_y);
+    const int img = (int)(blockIdx.x / ((long long)tiles_x * tiles_y));
     const int x0 = bx * 128, y0 = by * R;
-    const int cg = a.cin / 8;
-    const int nk = cg / 2;
-    const int rows = R + 2;
     bool ok = true;
 
-    auto load_stage = [&](int chunk, int s) {
-        uint8_t* sa = smem + s * G.stage_bytes;
-        uint8_t* sb = sa + G.a_bytes;
-        const int g0 = chunk * 2;
-        const int na = 2 * rows * kSlabPx;
-        for (int c = tid; c < na; c += kThreads) {
-            const int gl = c / (rows * kSlabPx);
-            const int rem = c - gl * rows * kSlabPx;
-            const int r = rem / kSlabPx, px = rem - r * kSlabPx;
-            const int yy = y0 + r - 1, xx = x0 + px - 1;
-            const uint16_t* src = a.x;
-            int bytes = 0;
-            if (yy >= 0 && yy < a.h && xx >= 0 && xx < a.w) {
-                src = a.x + ((img * a.h + yy) * a.w + xx) * a.cin + (g0 + gl) * 8;
-                bytes = 16;
-            }
-            cp_async16(smem_u32(sa + (gl * rows + r) * kSlabRow + px * 16), src, bytes);
-        }
-        const int nb = 9 * 2 * N;
-        for (int c = tid; c < nb; c += kThreads) {
-            const int co = c % N;
-            const int rest = c / N;
-            const int gl = rest & 1, t = rest >> 1;
-            const uint16_t* src = a.wt + ((long long)co * a.nkb_pad + t * cg + g0 + gl) * 8;
-            cp_async16(smem_u32(sb + ((t * 2 + gl) * N + co) * 16), src, 16);
-        }
-    };
-
-    const uint32_t idesc = idesc_bf16(128, N);
-    for (int s = 0; s < NS - 1; ++s) {
-        if (s < nk) load_stage(s, s);
-        cp_async_commit();
-    }
-    for (int i = 0; i < nk; ++i) {
-        const int s = i % NS;
-        if (NS == 3) cp_async_wait<1>();
-        else cp_async_wait<0>();
-        fence_proxy_async();
-        __syncthreads();
-        if (tid == 0) {
-            fence_after();
-            const uint8_t* sa = smem + s * G.stage_bytes;
-            const uint8_t* sb = sa + G.a_bytes;
-            for (int t = 0; t < 9; ++t) {
-                const int dy = t / 3, dx = t % 3;
-                const uint64_t bd = smem_desc(smem_u32(sb + t * 2 * N * 16), (uint32_t)N * 16u, 128u);
-                for (int r = 0; r < R; ++r) {
-                    const uint64_t ad =
-                        smem_desc(smem_u32(sa + (r + dy) * kSlabRow + dx * 16), (uint32_t)(rows * kSlabRow), 128u);
-                    mma_bf16(tmem + (uint32_t)(r * G.ncols), ad, bd, idesc, (i > 0 || t > 0) ? 1u : 0u);
+    if (warp == 0) {
+        const uint32_t stage_tx = (uint32_t)(2 * G.a_box + G.b_bytes);
+        auto issue = [&](int chunk, int s) {
+            uint8_t* sa = smem + s * G.stage_bytes;
+            mbar_expect_tx(&full[s], stage_tx);
+            tma_load_4d(sa, &xmap, chunk * 16, x0 - 1, y0 - 1, img, &full[s]);
+            tma_load_4d(sa + G.slab, &xmap, chunk * 16 + 8, x0 - 1, y0 - 1, img, &full[s]);
+            bulk_load(sa + G.a_bytes, a.wt + (size_t)chunk * (G.b_bytes / 2), (uint32_t)G.b_bytes, &full[s]);
+        };
+        const uint32_t idesc = idesc_bf16(128, N);
+        if (lane == 0)
+            for (int s = 0; s < NS - 1 && s < nk; ++s) issue(s, s);
+        for (int i = 0; i < nk; ++i) {
+            const int s = i % NS;
+            ok &= mbar_wait(&full[s], (unsigned)(i / NS) & 1u);
+            if (lane == 0) {
+                fence_after();
+                const uint8_t* sa = smem + s * G.stage_bytes;
+                const uint8_t* sb = sa + G.a_bytes;
+                for (int t = 0; t < 9; ++t) {
+                    const int dy = t / 3, dx = t % 3;
+                    const uint64_t bd = smem_desc(smem_u32(sb + t * 2 * N * 16), (uint32_t)N * 16u, 128u);
+                    for (int r = 0; r < R; ++r) {
+                        const uint64_t ad =
+                            smem_desc(smem_u32(sa + (r + dy) * kSlabRow + dx * 16), (uint32_t)G.slab, 128u);
+                        mma_bf16(tmem + (uint32_t)(r * G.ncols), ad, bd, idesc, (i > 0 || t > 0) ? 1u : 0u);
+                    }
                 }
+                mma_commit(&empty[s]);
             }
-            mma_commit(&bars[s]);
+            __syncwarp();
+            const int j = i + NS - 1;
+            if (j < nk) {
+                const int sj = j % NS;
+                if (i >= 1) ok &= mbar_wait(&empty[sj], (unsigned)((i - 1) / NS) & 1u);
+                if (lane == 0) issue(j, sj);
+            }
+            __syncwarp();
         }
-        const int j = i + NS - 1;
-        if (j < nk) {
-            const int sj = j % NS;
-            if (i >= 1) ok &= mbar_wait(&bars[sj], (unsigned)((i - 1) / NS) & 1u);
-            load_stage(j, sj);
-        }
-        cp_async_commit();
+        if (lane == 0) mma_commit(&done);
+        __syncwarp();
     }
-    const int last = nk - 1;
-    ok &= mbar_wait(&bars[last % NS], (unsigned)(last / NS) & 1u);
+    ok &= mbar_wait(&done, 0u);
     fence_after();
 
     const int xo = x0 + warp * 32 + lane;
     for (int r = 0; r < R; ++r) {
         const int yo = y0 + r;
         const bool live = xo < a.w && yo < a.h;
-        const long long p = (img * a.h + yo) * a.w + xo;
+        const long long p = ((long long)img * a.h + yo) * a.w + xo;
         float h0 = a.hw ? __ldg(a.hb) : 0.0f, h1 = a.hw ? __ldg(a.hb + 1) : 0.0f;
         for (int c0 = 0; c0 < N; c0 += 16) {
             float v[16];
@@ -674,6 +690,8 @@ __global__ void k_pack_weights(const float* __restrict__ w, int cout, int cin_re
     const long long total = (long long)rows * nkb_pad * 8;
     const int cgk = kin / 8;
     const int taps = ks * ks;
+    // the slab kernel reads stage-ordered weights [kin/16][tap][2][rows][8]
+    const bool slab = slab_layout(kin, ks);
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
          i += (long long)gridDim.x * blockDim.x) {
         const int j = (int)(i % 8);
@@ -681,6 +699,7 @@ __global__ void k_pack_weights(const float* __restrict__ w, int cout, int cin_re
         const int kb = (int)(t % nkb_pad);
         const int r = (int)(t / nkb_pad);
         float v = 0.0f;
+        long long dst = i;
         if (kb < taps * cgk) {
             const int tap = kb / cgk, g = kb % cgk;
             const int k = g * 8 + j;  // packed conv's input channel
@@ -691,8 +710,11 @@ __global__ void k_pack_weights(const float* __restrict__ w, int cout, int cin_re
                 const int src_tap = taps - 1 - tap;
                 if (r < cin_real) v = w[(((long long)k * cin_real + r) * ks + src_tap / ks) * ks + src_tap % ks];
             }
+            if (slab) dst = ((((long long)(g >> 1) * 9 + tap) * 2 + (g & 1)) * rows + r) * 8 + j;
+        } else if (slab) {
+            continue;
         }
-        out[i] = f_to_bf16(v);
+        out[dst] = f_to_bf16(v);
     }
 }
 
@@ -875,6 +897,54 @@ using gi::fail;
 using gi::fail_cuda;
 namespace tc = gi::tc;
 
+namespace {
+PFN_cuTensorMapEncodeTiled_v12000 g_encode_tiled = nullptr;
+
+gi_status tensor_map_fn() {
+    if (g_encode_tiled) return GI_OK;
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+        return fail(GI_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    g_encode_tiled = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    return GI_OK;
+}
+
+// 4-D map (c, w, h, n) of an NHWC BF16 tensor with boxes of 8 channels x
+// 130 pixels x `rows` rows x 1 image (the halo slab of one channel group).
+gi_status slab_map(CUtensorMap* m, const uint16_t* x, int n, int h, int w, int c, int rows) {
+    gi_status st = tensor_map_fn();
+    if (st != GI_OK) return st;
+    const cuuint64_t dims[4] = {(cuuint64_t)c, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
+    const cuuint64_t strides[3] = {(cuuint64_t)c * 2, (cuuint64_t)w * c * 2, (cuuint64_t)h * w * c * 2};
+    const cuuint32_t box[4] = {8, (cuuint32_t)tc::kSlabPx, (cuuint32_t)rows, 1};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    CUresult r = g_encode_tiled(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<uint16_t*>(x), dims, strides,
+                                box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? GI_OK : fail(GI_ERR_CUDA, "cuTensorMapEncodeTiled rejected the activation map");
+}
+
+gi_status launch_slab(const tc::ConvArgs& a, cudaStream_t cs) {
+    const tc::SlabGeom G = tc::slab_geom(a.cout, a.cin / 16);
+    CUtensorMap m;
+    gi_status st = slab_map(&m, a.x, a.n, a.h, a.w, a.cin, G.R + 2);
+    if (st != GI_OK) return st;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(tc::k_conv3_slab, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+        attr = true;
+    }
+    const int tx = (a.w + 127) / 128, ty = (a.h + G.R - 1) / G.R;
+    const long long blocks = (long long)tx * ty * a.n;
+    if (blocks > 0x7FFFFFFFLL) return fail(GI_ERR_INVALID_ARG, "gi_conv2d_bf16: too many tiles");
+    tc::k_conv3_slab<<<(unsigned)blocks, tc::kThreads, G.NS * G.stage_bytes + 128, cs>>>(a, m, tx, ty);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_conv2d_bf16 launch");
+}
+}  // namespace
+
 extern "C" gi_status gi_conv2d_bf16(const gi_bf16* x, int n, int h, int w, int cin, const gi_bf16* wt,
                                     const float* bias, int cout, int ksize, int act, const gi_bf16* mask,
                                     gi_bf16* y, int y_stride, int y_off, float* y32, uint32_t* err,
@@ -912,20 +982,7 @@ extern "C" gi_status gi_conv2d_bf16(const gi_bf16* x, int n, int h, int w, int c
     a.hb = nullptr;
     a.hout = nullptr;
     cudaStream_t cs = static_cast<cudaStream_t>(stream);
-    if (ksize == 3 && cin % 16 == 0) {
-        const tc::SlabGeom G = tc::slab_geom(cout, cin / 16);
-        static bool slab_attr = false;
-        if (!slab_attr) {
-            cudaFuncSetAttribute(tc::k_conv3_slab, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-            slab_attr = true;
-        }
-        const int tx = (w + 127) / 128, ty = (h + G.R - 1) / G.R;
-        const long long blocks = (long long)tx * ty * n;
-        if (blocks > 0x7FFFFFFFLL) return fail(GI_ERR_INVALID_ARG, "gi_conv2d_bf16: too many tiles");
-        tc::k_conv3_slab<<<(unsigned)blocks, tc::kThreads, G.NS * G.stage_bytes, cs>>>(a, tx, ty);
-        cudaError_t e = cudaGetLastError();
-        return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_conv2d_bf16 launch");
-    }
+    if (tc::slab_layout(cin, ksize)) return launch_slab(a, cs);
     const int smem = tc::kNS * (tc::kStageA + (cout / 8) * tc::kSBO);
     static bool attr_set = false;
     if (!attr_set) {
@@ -1143,12 +1200,8 @@ extern "C" gi_status gi_conv2d_head_bf16(const gi_bf16* x, int n, int h, int w, 
     a.hw = head_w;
     a.hb = head_b;
     a.hout = head_out;
-    const tc::SlabGeom G = tc::slab_geom(cout, cin / 16);
-    cudaFuncSetAttribute(tc::k_conv3_slab, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    const int tx = (w + 127) / 128, ty = (h + G.R - 1) / G.R;
-    const long long blocks = (long long)tx * ty * n;
-    tc::k_conv3_slab<<<(unsigned)blocks, tc::kThreads, G.NS * G.stage_bytes, static_cast<cudaStream_t>(stream)>>>(
-        a, tx, ty);
+    gi_status st = launch_slab(a, static_cast<cudaStream_t>(stream));
+    if (st != GI_OK) return st;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_conv2d_head_bf16 launch");
 }
