@@ -29,6 +29,9 @@ Extra legs in the same line (not the headline):
               lights, 4096^2 maps): PCSS and RBSM frames of all 8 lights
               as one CUDA graph, shadow-volume stencil counts, and the
               surrogate's 4K frame
+  area_light_ground_truth  the reference's Monte-Carlo area light (17 x 17
+              point-light maps) for the 1080p frame, and the error of
+              PCSS and of the surrogate against it
   surrogate   the learned PCSS surrogate (BF16 U-Net on the tcgen05
               convolution kernels) trained here on freshly rendered
               frames, then its 1080p frame time, its error against the
@@ -72,6 +75,7 @@ def parse_args():
     ap.add_argument("--batched-scenes", type=int, default=256)
     ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate leg")
     ap.add_argument("--no-heavy", action="store_true", help="skip the heavy 2160p leg")
+    ap.add_argument("--no-area-light", action="store_true", help="skip the 289-sample area-light ground-truth leg")
     ap.add_argument("--surrogate-frames", type=int, default=8000,
                     help="training frames (one 256^2 crop each, batch 16) for the surrogate leg")
     ap.add_argument("--profile", action="store_true",
@@ -463,6 +467,46 @@ def run_heavy(args, ctx, stream, local, net=None):
     return out
 
 
+def run_area_light(args, ctx, stream, local, w, fr, bufs, net=None):
+    """Monte-Carlo ground truth of the pcss_1080p area light (the reference's
+    17 x 17 point-light grid over the light's side, 289 light maps of
+    2048^2) and the error of the PCSS frame (and the surrogate) against it."""
+    import torch
+
+    import globalillumination_gb300 as gi
+
+    S, W, H = w.map_params.width, w.camera.width, w.camera.height
+    views = gi.area_light_samples(w.light, 2.0 * w.params.light_radius, 17)
+    truth = torch.empty(W * H, device="cuda")
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    gi.area_light_visibility(ctx, w.scene, views, w.map_params, fr.camera_mvp, w.params.shadow_intensity, W, H, truth,
+                             stream)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    gi.area_light_visibility(ctx, w.scene, views, w.map_params, fr.camera_mvp, w.params.shadow_intensity, W, H, truth,
+                             stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    gi.render_frame(ctx, w.scene, fr, w.map_params, w.params, W, H, bufs, stream)
+    torch.cuda.synchronize()
+    geo = truth > 0
+    out = {"samples": len(views), "map": f"{S}x{S}", "ms": ms,
+           "light_maps_per_s": len(views) * 1000.0 / ms,
+           "soft_pixel_fraction": float(((truth > 0.25) & (truth < 1.0)).float().mean()),
+           "pcss_poisson_mae_all_pixels": float((bufs.vis - truth).abs().mean()),
+           "pcss_poisson_mae_geometry_pixels": float((bufs.vis - truth)[geo].abs().mean())}
+    if net is not None:
+        from globalillumination_gb300 import surrogate as sg
+
+        sf = sg.SurrogateFrame(net, S, W, H)
+        v = sf.render(ctx, w.scene, fr, w.map_params, w.params)
+        torch.cuda.synchronize()
+        out["surrogate_mae_all_pixels"] = float((v - truth).abs().mean())
+    return out
+
+
 def measured_bf16_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -632,6 +676,9 @@ def run_ours(args):
     net = None
     if not args.no_surrogate and rank == 0:
         surrogate, net = run_surrogate(args, ctx, stream, local, w, fr, bufs)
+    area = None
+    if not args.no_area_light and rank == 0:
+        area = run_area_light(args, ctx, stream, local, w, fr, bufs, net)
     heavy = None
     if not args.no_heavy and rank == 0:
         heavy = run_heavy(args, ctx, stream, local, net)
@@ -672,6 +719,8 @@ def run_ours(args):
             line["surrogate"] = surrogate
         if heavy is not None:
             line["heavy"] = heavy
+        if area is not None:
+            line["area_light_ground_truth"] = area
         if clk and any(r in clk["reasons"] for r in THROTTLE_BAD):
             line["clocks_warning"] = "throttled during the timed region"
         if world == 1 and not args.no_cpu_baseline:

@@ -2,8 +2,11 @@
 // device copies of scenes, frame matrices and the pass entry points.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <vector>
 #include <string>
 
 #include "host_math.h"
@@ -109,6 +112,8 @@ extern "C" void gi_context_destroy(gi_context* c) {
     cudaFree(c->d_vkeys);
     cudaFree(c->d_depth_tmp);
     cudaFree(c->d_counts);
+    cudaFree(c->d_area_maps);
+    cudaFree(c->d_area_acc);
     for (int i = 0; i < 8; ++i) cudaFree(c->bin_buf[i]);
     for (int k = 0; k < 2; ++k)
         for (int i = 0; i < 8; ++i) cudaFree(c->tier_buf[k][i]);
@@ -508,6 +513,90 @@ extern "C" gi_status gi_render_frame(gi_context* ctx, const gi_scene* s, const g
         st = gi::launch_frame_visibility(ctx, vp, d_depth, mp->width, mp->height, s, camera_mvp, d_vis,
                                          W, H, d_pos, d_nrm, cs);
     mark(3);
+    return st;
+}
+
+// UniformSampledLightSource::computeUniformSampling
+// (SoftShadowMapping/src/Scene/LightSource/UniformSampledLightSource.cpp:27-38):
+// sample i of an n_side x n_side grid shifts eye and at by
+// (((i % n_side) - c) / c * half, ((int)(i / n_side) - c) / c * half, 0) with
+// half = size / 2 and c = (n_side - 1) / 2, in the reference's float /
+// double operation order.
+extern "C" gi_status gi_area_light_samples(const gi_view* light, float size, int n_side, gi_view* out) {
+    gi_status st = check_view(light);
+    if (st != GI_OK) return st;
+    if (!out || n_side < 2 || n_side > 32 || !(size >= 0.0f))
+        return fail(GI_ERR_INVALID_ARG, "gi_area_light_samples: need out, 2 <= n_side <= 32, size >= 0");
+    const int n = n_side * n_side;
+    const float half = (float)((double)size / 2.0);
+    const float factor = sqrtf((float)n);
+    const float sample_size = (float)((double)(factor - 1.0f) / 2.0);
+    for (int i = 0; i < n; ++i) {
+        const float dx = ((float)(i % (int)factor) - sample_size) / sample_size * half;
+        const float dy = ((float)(int)((float)i / factor) - sample_size) / sample_size * half;
+        out[i] = *light;
+        out[i].eye[0] = light->eye[0] + dx;
+        out[i].eye[1] = light->eye[1] + dy;
+        out[i].at[0] = light->at[0] + dx;
+        out[i].at[1] = light->at[1] + dy;
+    }
+    return GI_OK;
+}
+
+// renderMonteCarlo (SoftShadowMapping/src/main.cpp:756-811) + the uniform
+// branch of AccurateSoftShadow.frag:52-133.  Sample maps are rendered in
+// waves into context scratch; each wave adds its hard tests to the
+// per-pixel sums in sample order.
+extern "C" gi_status gi_area_light_visibility(gi_context* ctx, const gi_scene* s, const gi_view* samples, int n,
+                                              const gi_map_params* mp, const float camera_mvp[16],
+                                              float shadow_intensity, int W, int H, float* d_vis, void* stream) {
+    gi_status st = check_pass(ctx, s);
+    if (st != GI_OK) return st;
+    if (!samples || n < 1 || n > 4096 || !mp || !camera_mvp || !d_vis)
+        return fail(GI_ERR_INVALID_ARG, "gi_area_light_visibility: bad arguments");
+    if (mp->width != mp->height) return fail(GI_ERR_INVALID_ARG, "gi_area_light_visibility: square maps only");
+    st = check_image(mp->width, mp->height, "gi_area_light_visibility (map)");
+    if (st == GI_OK) st = check_image(W, H, "gi_area_light_visibility");
+    if (st != GI_OK) return st;
+    if ((size_t)s->dev_triangles >= ((size_t)1 << 29))
+        return fail(GI_ERR_CAPACITY, "gi_area_light_visibility: more than 2^29 triangles");
+    // per-sample light MVP (projection * view * model) and biased MVP
+    std::vector<float> mvp((size_t)n * 16), biased((size_t)n * 16);
+    for (int i = 0; i < n; ++i) {
+        st = check_view(&samples[i]);
+        if (st != GI_OK) return st;
+        gi_frame_matrices fm;
+        st = gi_frame_setup(&samples[i], &samples[i], &fm);
+        if (st != GI_OK) return st;
+        std::memcpy(&mvp[(size_t)i * 16], fm.light_mvp, 64);
+        std::memcpy(&biased[(size_t)i * 16], fm.light_mvp_biased, 64);
+    }
+    const int S = mp->width;
+    const size_t map_bytes = (size_t)S * S * sizeof(float);
+    const int wave_max = (int)std::max<size_t>(1, std::min<size_t>(16, ((size_t)1 << 30) / map_bytes));
+    st = gi::ensure_buffer(reinterpret_cast<void**>(&ctx->d_area_maps), &ctx->cap_area_maps, wave_max * map_bytes);
+    if (st == GI_OK)
+        st = gi::ensure_buffer(reinterpret_cast<void**>(&ctx->d_area_acc), &ctx->cap_area_acc,
+                               (size_t)W * H * sizeof(float));
+    if (st != GI_OK) return st;
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    st = gi::raster_gbuffer_keys(ctx, s, camera_mvp, W, H, cs);
+    gi::AreaWave wave;
+    // the shader's lightMVP uniform is the last sample's (biased) MVP
+    std::memcpy(wave.common, &biased[(size_t)(n - 1) * 16], 12 * sizeof(float));
+    for (int w0 = 0; w0 < n && st == GI_OK; w0 += wave_max) {
+        const int nw = std::min(wave_max, n - w0);
+        for (int k = 0; k < nw && st == GI_OK; ++k) {
+            const int i = w0 + k;
+            st = gi::raster_depth_map(ctx, s, &mvp[(size_t)i * 16], S, S, mp->bias_mode, mp->constant_bias,
+                                      mp->offset_factor, mp->offset_units, ctx->d_area_maps + (size_t)k * S * S,
+                                      small_px_default(), cs);
+            for (int c = 0; c < 4; ++c) wave.trans[k][c] = biased[(size_t)i * 16 + 12 + c];
+        }
+        if (st == GI_OK)
+            st = gi::launch_area_accumulate(ctx, s, camera_mvp, W, H, ctx->d_area_maps, S, nw, wave,
+                                            shadow_intensity, w0 == 0, w0 + nw == n ? n : 0, d_vis, cs);
+    }
     return st;
 }
 

@@ -95,6 +95,11 @@ struct gi_context {
     // the tiered camera-key pass (the two passes may run concurrently)
     unsigned int* d_status = nullptr;
     unsigned int* h_status = nullptr;  // pinned mirror
+    // area-light ground truth: a wave of sample light maps, per-pixel sums
+    float* d_area_maps = nullptr;
+    size_t cap_area_maps = 0;
+    float* d_area_acc = nullptr;
+    size_t cap_area_acc = 0;
     // second stream for the camera-key pass of gi_render_frame, and the
     // fork / join events (cudaStream_t / cudaEvent_t)
     void* aux_stream = nullptr;

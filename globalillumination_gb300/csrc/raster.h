@@ -47,6 +47,18 @@ gi_status launch_surrogate_finish(gi_context* ctx, const gi_vis_params* p, const
                                   const float* d_head, int head_stride, const void* d_feat, float thr,
                                   float* d_vis, unsigned* d_fallback, cudaStream_t st);
 
+// Area-light ground truth: adds the hard tests of `nw` sample maps (one
+// wave, maps[k] of map_s^2 texels, biased translation columns trans[k]) to
+// every pixel's running sum; `first` starts the sums at 0, and a non-zero
+// `total` finishes them into d_vis (sum / total).
+struct AreaWave {
+    float trans[16][4];
+    float common[12];  // columns 0..2 of the last sample's biased light MVP
+};
+gi_status launch_area_accumulate(gi_context* ctx, const gi_scene* scene, const float camera_mvp[16], int W, int H,
+                                 const float* maps, int map_s, int nw, const AreaWave& wave, float intensity,
+                                 bool first, int total, float* d_vis, cudaStream_t st);
+
 // Progressive best-candidate Poisson-disk sequence in the unit disk
 // (poisson_table.inc); the n-tap table is its first n points.
 extern const float kPoissonDisk[64][2];

@@ -1278,6 +1278,50 @@ __global__ void __launch_bounds__(128) k_surrogate_finish(
     __stcs(out + i, v);
 }
 
+// ---- area-light ground truth (AccurateSoftShadow.frag:52-133, uniform samples) --
+// Per pixel: commonShadowCoord from columns 0-2 of the light MVP uniform,
+// then per sample shadowCoord = common + translation, divided by w, one
+// NEAREST fetch from that sample's map and accShadow += (z <= d ? 1 : I) *
+// accFactor (1); shadow = accShadow / count.  The pre-test is commented out
+// in the shader; background pixels are discarded (0).
+__global__ void __launch_bounds__(128) k_area_accumulate(
+    const float* __restrict__ maps, int map_s, int nw, const AreaWave wave, float I,
+    const unsigned long long* __restrict__ keys, const float* __restrict__ points,
+    const float* __restrict__ normals, const int* __restrict__ indices, const dev::Mat4 mvp,
+    const unsigned* __restrict__ rec_of, const dev::BRec* __restrict__ recs, const uint4* __restrict__ rres,
+    float* __restrict__ acc, int first, int total, float* __restrict__ out, int W, int H) {
+    int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    int y = blockIdx.y * 4 + (threadIdx.x >> 5);
+    if (x >= W || y >= H) return;
+    const size_t i = (size_t)y * W + x;
+    float4 pv, nv;
+    dev::resolve_pixel(__ldcs(keys + i), points, normals, indices, mvp, W, H, x, y, rec_of, recs, rres, pv, nv);
+    if (pv.x == 0.0f) {
+        if (total) out[i] = 0.0f;
+        return;
+    }
+    const float* m = wave.common;
+    const float cx = m[0] * pv.x + m[4] * pv.y + m[8] * pv.z;
+    const float cy = m[1] * pv.x + m[5] * pv.y + m[9] * pv.z;
+    const float cz = m[2] * pv.x + m[6] * pv.y + m[10] * pv.z;
+    const float cw = m[3] * pv.x + m[7] * pv.y + m[11] * pv.z;
+    Ctx c;
+    c.W = map_s;
+    c.H = map_s;
+    c.fW = (float)map_s;
+    c.fH = (float)map_s;
+    float a = first ? 0.0f : acc[i];
+    for (int k = 0; k < nw; ++k) {
+        const float sx = cx + wave.trans[k][0], sy = cy + wave.trans[k][1];
+        const float sz = cz + wave.trans[k][2], sw = cw + wave.trans[k][3];
+        c.map = maps + (size_t)k * map_s * map_s;
+        const float d = fetch(c, sx / sw, sy / sw);
+        a += ((sz / sw <= d) ? 1.0f : I) * 1.0f;
+    }
+    if (total) out[i] = a / (float)total;
+    else acc[i] = a;
+}
+
 }  // namespace vis
 
 gi_status launch_surrogate_features(gi_context* ctx, const gi_vis_params* p, const float* d_depth, int map_w,
@@ -1312,6 +1356,21 @@ gi_status launch_surrogate_finish(gi_context* ctx, const gi_vis_params* p, const
     ctx->launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "surrogate finish launch");
+}
+
+gi_status launch_area_accumulate(gi_context* ctx, const gi_scene* scene, const float camera_mvp[16], int W, int H,
+                                 const float* maps, int map_s, int nw, const AreaWave& wave, float intensity,
+                                 bool first, int total, float* d_vis, cudaStream_t st) {
+    dim3 grid((W + 31) / 32, (H + 3) / 4);
+    dev::Mat4 m;
+    for (int k = 0; k < 16; ++k) m.m[k] = camera_mvp[k];
+    vis::k_area_accumulate<<<grid, 128, 0, st>>>(
+        maps, map_s, nw, wave, intensity, ctx->d_vkeys, scene->d_points, scene->d_normals, scene->d_indices, m,
+        static_cast<const unsigned*>(ctx->tier_buf[1][6]), static_cast<const dev::BRec*>(ctx->tier_buf[1][0]),
+        static_cast<const uint4*>(ctx->tier_buf[1][7]), ctx->d_area_acc, first ? 1 : 0, total, d_vis, W, H);
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "area-light accumulate launch");
 }
 
 gi_status launch_visibility(gi_context* ctx, const gi_vis_params* p, const float* d_depth,

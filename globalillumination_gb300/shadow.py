@@ -425,6 +425,31 @@ def render_frame_passes(ctx: Context, scene: Scene, frame: Frame, mp: MapParams,
 render_soft_shadows = render_frame
 
 
+def area_light_samples(light: ViewSpec, size: float, n_side: int = 17) -> list:
+    """The reference's uniform point-light samples of an area light (n_side^2 views)."""
+    n = n_side * n_side
+    out = (api.View * n)()
+    lv = light.to_c()
+    check(_lib().gi_area_light_samples(C.byref(lv), float(size), int(n_side), out), "gi_area_light_samples")
+    views = []
+    for v in out:
+        views.append(ViewSpec(eye=tuple(v.eye), at=tuple(v.at), width=v.width, height=v.height, fovy_deg=v.fovy_deg,
+                              znear=v.znear, zfar=v.zfar, up=tuple(v.up)))
+    return views
+
+
+def area_light_visibility(ctx: Context, scene: Scene, samples, mp: MapParams, camera_mvp, intensity: float,
+                          width: int, height: int, vis, stream=None):
+    """Monte-Carlo area-light ground truth (renderMonteCarlo + AccurateSoftShadow.frag)."""
+    assert vis.is_cuda and vis.numel() >= width * height
+    arr = (api.View * len(samples))(*[v.to_c() for v in samples])
+    c = mp.to_c()
+    check(_lib().gi_area_light_visibility(ctx.handle, scene.handle, arr, len(samples), C.byref(c), _f16(camera_mvp),
+                                          float(intensity), width, height, _ptr(vis), _stream_ptr(stream)),
+          "gi_area_light_visibility")
+    return vis
+
+
 class Batch:
     """Many frames (scene, camera, lights) replayed as one CUDA graph (gi_batch_*).
 

@@ -350,6 +350,33 @@ gi_status gi_render_frame(gi_context* ctx, const gi_scene* scene,
 gi_status gi_poisson_table(int n, float* xy_out);
 
 /* ------------------------------------------------------------------ */
+/* Area-light ground truth (Monte-Carlo over point-light samples)       */
+/* ------------------------------------------------------------------ */
+/* UniformSampledLightSource::computeUniformSampling
+ * (SoftShadowMapping/src/Scene/LightSource/UniformSampledLightSource.cpp:
+ * 27-38): the n_side x n_side point lights of an area light of side
+ * `size` (the reference: 17 x 17 = 289, size 16).  Sample i shifts eye and
+ * at by ((i % n_side - c) / c * size / 2, ((int)(i / n_side) - c) / c *
+ * size / 2, 0), c = (n_side - 1) / 2 — in world x and y, as the reference
+ * does.  out receives n_side^2 views (the light's other fields copied). */
+gi_status gi_area_light_samples(const gi_view* light, float size, int n_side, gi_view* out);
+
+/* renderMonteCarlo (SoftShadowMapping/src/main.cpp:756-811) with
+ * AccurateSoftShadow.frag:52-133 (uniform sampling): one light map per
+ * sample view (map parameters as gi_shadow_map; square maps), then per
+ * camera pixel the average over samples of the hard test (1 or
+ * shadow_intensity), using columns 0-2 of the last sample's biased light
+ * MVP and each sample's own translation column, as the shader's uniforms
+ * do.  No pre-test (it is commented out in the shader); background 0.
+ * d_vis is float[width*height].  Maps are rendered in waves into context
+ * scratch (at most 1 GiB). */
+gi_status gi_area_light_visibility(gi_context* ctx, const gi_scene* scene,
+                                   const gi_view* samples, int num_samples,
+                                   const gi_map_params* map, const float camera_mvp[16],
+                                   float shadow_intensity, int width, int height,
+                                   float* d_vis, void* stream);
+
+/* ------------------------------------------------------------------ */
 /* A13/A14: shadow volumes with stencil counts                         */
 /* ------------------------------------------------------------------ */
 typedef enum gi_depth_func {

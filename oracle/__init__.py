@@ -27,6 +27,7 @@ def load():
         lib.or_visibility.argtypes = [vp, vp, i, i, vp, vp, vp, i, i, vp, i]
         lib.or_shadow_volume_counts.argtypes = [vp, vp, i, vp, i, vp, f, vp, i, i, i, vp, vp, i]
         lib.or_rbssm_hits.argtypes = [vp, i]
+        lib.or_area_light_visibility.argtypes = [vp, vp, i, vp, i, vp, vp, i, i, i, f, f, f, vp, f, i, i, vp, i]
         for fn in (lib.or_shadow_map, lib.or_gbuffer, lib.or_visibility, lib.or_shadow_volume_counts):
             fn.restype = None
         _lib = lib
@@ -93,3 +94,16 @@ def rbssm_return_sites():
     with open(src) as f:
         lines = f.read().split("\n")
     return [i + 1 for i, l in enumerate(lines) if "RB_RET(" in l and "#define" not in l]
+
+
+def area_light_visibility(points, normals, indices, mvps, biased, S, bias_mode, cbias, factor, units, camera_mvp,
+                          intensity, width, height, threads=0):
+    p, n = _f32(points), _f32(normals)
+    ix = np.ascontiguousarray(indices, dtype=np.int32)
+    mv, bs, cm = _f32(mvps).reshape(-1), _f32(biased).reshape(-1), _f32(camera_mvp).reshape(16)
+    out = np.empty(height * width, np.float32)
+    load().or_area_light_visibility(p.ctypes.data, n.ctypes.data, p.size // 3, ix.ctypes.data, ix.size // 3,
+                                    mv.ctypes.data,
+                                    bs.ctypes.data, mv.size // 16, S, bias_mode, cbias, factor, units, cm.ctypes.data,
+                                    intensity, width, height, out.ctypes.data, threads)
+    return out

@@ -1573,6 +1573,52 @@ extern "C" void or_visibility(const gi_vis_params* p, const float* depth, int ma
         }
 }
 
+// renderMonteCarlo (SoftShadowMapping/src/main.cpp:756-811) + the uniform
+// branch of AccurateSoftShadow.frag:52-133: one map per sample (mvps, the
+// unbiased light MVPs), then per pixel commonShadowCoord from columns 0-2 of
+// the last sample's biased MVP, shadowCoord = common + the sample's biased
+// translation column, / w, one NEAREST fetch, accShadow += (z <= d ? 1 : I)
+// * 1, shadow = accShadow / count.  No pre-test; background 0.
+extern "C" void or_area_light_visibility(const float* points, const float* normals, int nv, const int* indices,
+                                         int nt, const float* mvps, const float* biased, int n, int S,
+                                         int bias_mode, float cbias, float factor, float units,
+                                         const float camera_mvp[16], float I, int W, int H, float* out,
+                                         int threads) {
+    std::vector<float> pos((size_t)W * H * 4), nrm((size_t)W * H * 4), map((size_t)S * S);
+    or_gbuffer(points, normals, nv, indices, nt, camera_mvp, W, H, pos.data(), nrm.data(), threads);
+    std::vector<float> acc((size_t)W * H, 0.0f);
+    const float* m = biased + (size_t)(n - 1) * 16;
+    for (int i = 0; i < n; ++i) {
+        or_shadow_map(points, nv, indices, nt, mvps + (size_t)i * 16, S, S, bias_mode, cbias, factor, units,
+                      map.data(), threads);
+        const float* t = biased + (size_t)i * 16 + 12;
+        Ctx c;
+        c.p = nullptr;
+        c.map = map.data();
+        c.W = S;
+        c.H = S;
+        c.sx = c.sy = 0.0f;
+        c.I = I;
+#pragma omp parallel for schedule(static) num_threads(nthreads(threads))
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                const size_t q = (size_t)y * W + x;
+                const float* v = &pos[4 * q];
+                if (v[0] == 0.0f) continue;
+                const float cx = m[0] * v[0] + m[4] * v[1] + m[8] * v[2];
+                const float cy = m[1] * v[0] + m[5] * v[1] + m[9] * v[2];
+                const float cz = m[2] * v[0] + m[6] * v[1] + m[10] * v[2];
+                const float cw = m[3] * v[0] + m[7] * v[1] + m[11] * v[2];
+                const float sx = cx + t[0], sy = cy + t[1], sz = cz + t[2], sw = cw + t[3];
+                const float d = fetch(c, sx / sw, sy / sw);
+                acc[q] += ((sz / sw <= d) ? 1.0f : I) * 1.0f;
+            }
+    }
+    float count = 0.0f;
+    for (int i = 0; i < n; ++i) count += 1.0f;
+    for (size_t q = 0; q < (size_t)W * H; ++q) out[q] = pos[4 * q] == 0.0f ? 0.0f : acc[q] / count;
+}
+
 extern "C" void or_rbssm_hits(unsigned long long* out4096, int reset) {
     for (int i = 0; i < 4096; ++i) {
         if (out4096) out4096[i] = g_rb_hits[i].load();

@@ -57,6 +57,14 @@ void or_shadow_volume_counts(const float* points, const float* normals,
                              int depth_func, uint8_t* out_stencil,
                              float* out_depth, int threads);
 
+/* Area-light ground truth (renderMonteCarlo + AccurateSoftShadow.frag):
+ * mvps / biased are n x 16 light matrices of the sample lights. */
+void or_area_light_visibility(const float* points, const float* normals, int nv,
+                              const int* indices, int nt, const float* mvps,
+                              const float* biased, int n, int S, int bias_mode, float cbias,
+                              float factor, float units, const float camera_mvp[16], float I,
+                              int W, int H, float* out, int threads);
+
 /* Hit counts of the return sites of the RBSSM smoothONDS restatement,
  * indexed by source line modulo 4096 (test coverage only). */
 void or_rbssm_hits(unsigned long long* out4096, int reset);

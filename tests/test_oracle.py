@@ -291,3 +291,52 @@ def test_rbssm_fuzz_reaches_every_reachable_case():
     hits = oracle.rbssm_hits()
     covered = [s for s in sites if (s & 4095) in hits]
     assert len(covered) >= len(sites) - 4, sorted(set(sites) - set(covered))
+
+
+def test_area_light_samples_follow_the_reference_grid():
+    light = gi.ViewSpec(eye=(1.0, 12.0, -2.0), at=(0.5, 0.0, 0.25), width=64, height=64, fovy_deg=90.0)
+    views = gi.area_light_samples(light, 16.0, 17)
+    assert len(views) == 289
+    f32 = np.float32
+    half, factor = f32(8.0), f32(17.0)
+    c = f32((factor - f32(1.0)) / 2.0)
+    for i in (0, 1, 16, 17, 144, 288):
+        dx = f32(f32(f32(i % 17) - c) / c) * half
+        dy = f32(f32(f32(int(f32(i) / factor)) - c) / c) * half
+        assert views[i].eye == (float(f32(f32(1.0) + dx)), float(f32(f32(12.0) + dy)), -2.0)
+        assert views[i].at == (float(f32(f32(0.5) + dx)), float(f32(f32(0.0) + dy)), 0.25)
+    assert views[144].eye == light.eye  # centre sample
+
+
+def _area_scene(occluder: bool):
+    s = gi.Scene()
+    s.ground(4.0, 0.0)
+    if occluder:
+        s.object_from_arrays(np.array([[-1.5, 3.0, -1.5], [1.5, 3.0, -1.5], [1.5, 3.0, 1.5], [-1.5, 3.0, 1.5]],
+                                      np.float32), [[0, 2, 1], [0, 3, 2]]).commit()
+    return s
+
+
+def _area_truth(s, n_side=3, S=64, W=48, H=40):
+    light = gi.ViewSpec(eye=(0.0, 12.0, 0.0), at=(0.0, 0.0, 0.0), width=S, height=S, fovy_deg=90.0, up=(0, 0, 1))
+    cam = gi.ViewSpec(eye=(0.0, 10.0, -1.0), at=(0.0, 0.0, 0.0), width=W, height=H, fovy_deg=40.0)
+    views = gi.area_light_samples(light, 1.0, n_side)
+    frames = [gi.frame_setup(v, cam) for v in views]
+    mvps = np.stack([f.light_mvp for f in frames])
+    biased = np.stack([f.light_mvp_biased for f in frames])
+    p, n, i = s.arrays()
+    v = oracle.area_light_visibility(p, n, i, mvps, biased, S, api.GI_BIAS_POLYGON_OFFSET, 0.0, 4.0, 20.0,
+                                     frames[0].camera_mvp, 0.25, W, H)
+    pos, _ = oracle.gbuffer(p, n, i, frames[0].camera_mvp, W, H)
+    return v, pos.reshape(-1, 4)[:, 0] != 0
+
+
+def test_area_light_truth_lit_and_umbra():
+    v, geo = _area_truth(_area_scene(False))
+    assert geo.sum() > 500 and (v[geo] == 1.0).all() and (v[~geo] == 0.0).all()
+    v, geo = _area_truth(_area_scene(True))
+    # a plate at y = 3 over the ground: umbra below it, penumbra (fractions
+    # of the 9 samples) around it, lit ground and plate elsewhere
+    g = v[geo]
+    assert (g >= 0.25).all() and (g <= 1.0).all()
+    assert (g == 0.25).sum() > 10 and (g == 1.0).sum() > 500 and ((g > 0.25) & (g < 1.0)).sum() > 10
