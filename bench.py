@@ -80,6 +80,9 @@ def parse_args():
                     help="training frames (one 256^2 crop each, batch 16) for the surrogate leg")
     ap.add_argument("--profile", action="store_true",
                     help="render --warmup frames and exit (the command profiled with ncu)")
+    ap.add_argument("--profile-case", choices=["frame", "conv", "volumes"], default="frame",
+                    help="with --profile: the pcss_1080p frame, three U-Net convolutions at 1080p (d0a, d1a, "
+                         "d2a), or the heavy scene's shadow volumes of one light at 960x540")
     return ap.parse_args()
 
 
@@ -515,12 +518,50 @@ def measured_bf16_peak():
         return 1900.0, "fallback"
 
 
+def run_profile_case(args, local):
+    """Small, self-contained launches for ncu (no timing)."""
+    import torch
+
+    import globalillumination_gb300 as gi
+
+    if args.profile_case == "conv":
+        from globalillumination_gb300 import surrogate as sg, tc_ops
+
+        net = sg.UNet(local, seed=1)
+        for name in ("d0a", "d1a", "d2a"):
+            L = net.layers[name]
+            sc = sg.LEVEL_SCALE[name[:2]]
+            h, w = 1080 // sc, 1920 // sc
+            x = torch.randn((1, h, w, L.cin), device="cuda").to(torch.bfloat16)
+            y = torch.empty((1, h, w, L.cout), dtype=torch.bfloat16, device="cuda")
+            tc_ops.conv2d(x, L.wp, L.cout, 3, bias=L.b, relu=True, out=y, err=net.err)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "conv", "kernel_error": net.kernel_error()}), flush=True)
+        return 0
+    from globalillumination_gb300 import scenes
+
+    w = scenes.heavy_2160p()
+    ctx = gi.Context(local)
+    w.scene.upload(ctx)
+    cam = gi.ViewSpec(eye=w.camera.eye, at=w.camera.at, width=960, height=540)
+    light = gi.ViewSpec(eye=w.lights[0], at=(0.0, 0.0, 0.0), width=4096, height=4096, fovy_deg=90.0)
+    fr = gi.frame_setup(light, cam)
+    st = torch.empty(960 * 540, dtype=torch.uint8, device="cuda")
+    gi.shadow_volume_counts(ctx, w.scene, light.eye, fr.camera_mvp, 960, 540, st)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "volumes", "lit_fraction": float((st == 0).float().mean())}), flush=True)
+    ctx.close()
+    return 0
+
+
 def run_ours(args):
     import numpy as np
     import torch
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
+    if args.profile and args.profile_case != "frame":
+        return run_profile_case(args, local)
     dist = None
     if world > 1:
         import torch.distributed as dist

@@ -951,12 +951,14 @@ struct FloorTrack {
         if (a % b != 0 && a < 0) --q;
         return q;
     }
-    __device__ __forceinline__ void init(int64_t num, int64_t d, int64_t delta) {
-        den = d;
-        q = fdiv(num, d);
-        rem = num - q * d;
-        dq = fdiv(delta, d);
-        dr = delta - dq * d;
+    // floor(v / d) for 0 <= v < 64 d (a small quotient): float estimate,
+    // then exact integer correction
+    __device__ __forceinline__ static int64_t small_quot(int64_t v, int64_t d) {
+        int64_t c = (int64_t)((float)v / (float)d);
+        if (c < 0) c = 0;
+        for (int it = 0; it < 4 && c * d > v; ++it) --c;
+        for (int it = 0; it < 4 && (c + 1) * d <= v; ++it) ++c;
+        return c;
     }
     __device__ __forceinline__ void step() {
         q += dq;
@@ -985,26 +987,64 @@ __global__ void __launch_bounds__(256) k_sliver(BinArgs a) {
             XA[k] = r.X[ia];
             YA[k] = r.Y[ia];
         }
+        // every lane takes part in the shuffles below; lanes past the last
+        // row simply run no row iterations
         const int y_first = (int)r.y0 + lane;
-        if (y_first > (int)r.y1) continue;
-        // edge k at row y: E(x) = K - B * (x * 256 + 128), K = A * (py - Ya) + B * Xa
+        // edge k at row y: E(x) = K - B * (x * 256 + 128), K = A * (py - Ya) + B * Xa.
+        // The bound of edge k is floor(num / den) with num linear in the row;
+        // the warp computes the row-y0 quotients and the one-row steps with
+        // one 64-bit division per lane (lanes 0-5), shares them, and each
+        // lane derives its own first row (y0 + lane) and its 32-row step
+        // with small exact quotients.
         FloorTrack f[3];
         int64_t K0[3];
         const int64_t py0 = (int64_t)y_first * kSub + kSub / 2;
+        int64_t num_b[3], den[3], step1[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
+            const int64_t base_py = (int64_t)r.y0 * kSub + kSub / 2;
+            const int64_t Kb = A[k] * (base_py - YA[k]) + B[k] * XA[k];
+            const int64_t dK = A[k] * (int64_t)kSub;
             K0[k] = A[k] * (py0 - YA[k]) + B[k] * XA[k];
-            const int64_t dK = A[k] * (int64_t)(32 * kSub);
             if (B[k] > 0) {
-                // x <= floor((K - 128 B - (tl ? 0 : 1)) / (256 B))
-                f[k].init(K0[k] - B[k] * (kSub / 2) - (tl[k] ? 0 : 1), B[k] * kSub, dK);
+                num_b[k] = Kb - B[k] * (kSub / 2) - (tl[k] ? 0 : 1);
+                den[k] = B[k] * kSub;
+                step1[k] = dK;
             } else if (B[k] < 0) {
                 const int64_t Bp = -B[k];
-                if (tl[k])  // x >= ceil((-K - 128 Bp) / (256 Bp)) = -floor((K + 128 Bp) / (256 Bp))
-                    f[k].init(K0[k] + Bp * (kSub / 2), Bp * kSub, dK);
-                else  // x >= floor((-K - 128 Bp) / (256 Bp)) + 1
-                    f[k].init(-K0[k] - Bp * (kSub / 2), Bp * kSub, -dK);
+                den[k] = Bp * kSub;
+                num_b[k] = tl[k] ? Kb + Bp * (kSub / 2) : -Kb - Bp * (kSub / 2);
+                step1[k] = tl[k] ? dK : -dK;
+            } else {
+                num_b[k] = 0;
+                den[k] = 1;
+                step1[k] = 0;
             }
+        }
+        // lanes 0-2: floor(num_b / den); lanes 3-5: floor(step1 / den)
+        int64_t mine = 0;
+        if (lane < 6) {
+            const int k = lane % 3;
+            mine = FloorTrack::fdiv(lane < 3 ? num_b[k] : step1[k], den[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int64_t q0 = __shfl_sync(0xffffffffu, mine, k);
+            const int64_t dq1 = __shfl_sync(0xffffffffu, mine, 3 + k);
+            if (B[k] == 0) continue;
+            const int64_t rem0 = num_b[k] - q0 * den[k];
+            const int64_t dr1 = step1[k] - dq1 * den[k];
+            // row y0 + lane
+            const int64_t v = rem0 + (int64_t)lane * dr1;
+            const int64_t c = FloorTrack::small_quot(v, den[k]);
+            f[k].den = den[k];
+            f[k].q = q0 + (int64_t)lane * dq1 + c;
+            f[k].rem = v - c * den[k];
+            // 32-row step
+            const int64_t v32 = 32 * dr1;
+            const int64_t c32 = FloorTrack::small_quot(v32, den[k]);
+            f[k].dq = 32 * dq1 + c32;
+            f[k].dr = v32 - c32 * den[k];
         }
         const float sgn_front = (r.flags & kFlagFront) ? 1.0f : -1.0f;
         const int inc = sgn_front > 0.0f ? 1 : -1;
