@@ -190,6 +190,7 @@ _PROTOS = {
     "gi_poisson_table": (C.c_int, [C.c_int, _VP]),
     "gi_shadow_volume_counts": (C.c_int, [_VP, _VP, F3, C.c_float, F16, C.c_int, C.c_int, C.c_int,
                                           _VP, _VP, _VP]),
+    "gi_phong_shade": (C.c_int, [_VP, C.POINTER(VisParams), _VP, _VP, _VP, _VP, C.c_int, C.c_int, _VP, _VP]),
     "gi_area_light_samples": (C.c_int, [C.POINTER(View), C.c_float, C.c_int, _VP]),
     "gi_area_light_visibility": (C.c_int, [_VP, _VP, _VP, C.c_int, C.POINTER(MapParams), F16, C.c_float, C.c_int,
                                            C.c_int, _VP, _VP]),

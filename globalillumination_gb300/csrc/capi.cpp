@@ -600,6 +600,17 @@ extern "C" gi_status gi_area_light_visibility(gi_context* ctx, const gi_scene* s
     return st;
 }
 
+extern "C" gi_status gi_phong_shade(gi_context* ctx, const gi_vis_params* vp, const float* d_pos,
+                                    const float* d_nrm, const float* d_vis, const float* d_color, int W, int H,
+                                    float* d_out, void* stream) {
+    if (!ctx || !vp || !d_pos || !d_nrm || !d_vis || !d_out)
+        return fail(GI_ERR_INVALID_ARG, "gi_phong_shade: NULL argument");
+    gi_status st = check_device(ctx);
+    if (st == GI_OK) st = check_image(W, H, "gi_phong_shade");
+    if (st != GI_OK) return st;
+    return gi::launch_phong(ctx, vp, d_pos, d_nrm, d_vis, d_color, d_out, W, H, static_cast<cudaStream_t>(stream));
+}
+
 extern "C" gi_status gi_surrogate_features(gi_context* ctx, const gi_scene* s, const gi_map_params* mp,
                                            const float light_mvp[16], const float camera_mvp[16],
                                            const gi_vis_params* vp, int W, int H, float* d_depth, void* d_feat,

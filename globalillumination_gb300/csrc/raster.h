@@ -59,6 +59,11 @@ gi_status launch_area_accumulate(gi_context* ctx, const gi_scene* scene, const f
                                  const float* maps, int map_s, int nw, const AreaWave& wave, float intensity,
                                  bool first, int total, float* d_vis, cudaStream_t st);
 
+// Deferred Phong shading of the G-buffer with the visibility as shadow
+// term (d_color float4 per pixel or NULL for white); d_out float4.
+gi_status launch_phong(gi_context* ctx, const gi_vis_params* p, const float* d_pos, const float* d_nrm,
+                       const float* d_vis, const float* d_color, float* d_out, int W, int H, cudaStream_t st);
+
 // Progressive best-candidate Poisson-disk sequence in the unit disk
 // (poisson_table.inc); the n-tap table is its first n points.
 extern const float kPoissonDisk[64][2];

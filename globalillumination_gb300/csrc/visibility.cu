@@ -1322,6 +1322,69 @@ __global__ void __launch_bounds__(128) k_area_accumulate(
     else acc[i] = a;
 }
 
+// ---- deferred Phong shading (ShadowMapping/Shaders/GBuffer/PhongShading.frag:11-46)
+// color = shadow * fragmentColor * (Idiff + Ispec + Iamb) with the light
+// in eye space as the pre-test uses it; E = normalize(-vertex) normalises
+// the 4-component eye-space vertex (w = 1) before the vec3 truncation, as
+// the shader's implicit conversion does.  pow(x, 0.3 * 10) is evaluated as
+// x * x * x.  Background pixels keep the clear colour (0.63, 0.82, 0.96, 1).
+__global__ void __launch_bounds__(128) k_phong(const gi_vis_params p, const float4* __restrict__ pos,
+                                               const float4* __restrict__ nrm, const float* __restrict__ vis,
+                                               const float4* __restrict__ color, float4* __restrict__ out, int W,
+                                               int H) {
+    int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    int y = blockIdx.y * 4 + (threadIdx.x >> 5);
+    if (x >= W || y >= H) return;
+    const size_t i = (size_t)y * W + x;
+    const float4 pv = pos[i];
+    if (pv.x == 0.0f) {
+        out[i] = make_float4(0.63f, 0.82f, 0.96f, 1.0f);
+        return;
+    }
+    const float4 nv = nrm[i];
+    const float shadow = vis[i];
+    const float spec_shadow = shadow - p.shadow_intensity;
+    V4 v = mat4_mul(p.camera_mv, V4{pv.x, pv.y, pv.z, pv.w});
+    const float* nm = p.normal_matrix;
+    float nx = nm[0] * nv.x + nm[3] * nv.y + nm[6] * nv.z;
+    float ny = nm[1] * nv.x + nm[4] * nv.y + nm[7] * nv.z;
+    float nz = nm[2] * nv.x + nm[5] * nv.y + nm[8] * nv.z;
+    const float ninv = 1.0f / sqrtf(nx * nx + ny * ny + nz * nz);
+    nx = nx * ninv;
+    ny = ny * ninv;
+    nz = nz * ninv;
+    float lx = p.light_position[0] - v.x, ly = p.light_position[1] - v.y, lz = p.light_position[2] - v.z;
+    const float linv = 1.0f / sqrtf(lx * lx + ly * ly + lz * lz);
+    lx = lx * linv;
+    ly = ly * linv;
+    lz = lz * linv;
+    const float ex0 = -v.x, ey0 = -v.y, ez0 = -v.z, ew0 = -v.w;
+    const float einv = 1.0f / sqrtf(ex0 * ex0 + ey0 * ey0 + ez0 * ez0 + ew0 * ew0);
+    const float ex = ex0 * einv, ey = ey0 * einv, ez = ez0 * einv;
+    // reflect(L, N) = L - 2 * dot(N, L) * N; R = normalize(-reflect)
+    const float ndl = nx * lx + ny * ly + nz * lz;
+    float rx = -(lx - 2.0f * ndl * nx), ry = -(ly - 2.0f * ndl * ny), rz = -(lz - 2.0f * ndl * nz);
+    const float rinv = 1.0f / sqrtf(rx * rx + ry * ry + rz * rz);
+    rx = rx * rinv;
+    ry = ry * rinv;
+    rz = rz * rinv;
+    const float diff = gmax(ndl, 0.0f);
+    const float re = gmax(rx * ex + ry * ey + rz * ez, 0.0f);
+    const float spec = re * re * re;
+    const float4 c = color ? color[i] : make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+    const float amb[4] = {0.4f, 0.4f, 0.4f, 1.0f}, dif[4] = {0.5f, 0.5f, 0.5f, 1.0f};
+    const float spc[4] = {0.25f, 0.25f, 0.25f, 1.0f};
+    const float cc[4] = {c.x, c.y, c.z, c.w};
+    float o[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float idiff = dif[k] * diff;
+        const float ispec = (spec_shadow * spc[k]) * spec;
+        o[k] = (shadow * cc[k]) * ((idiff + ispec) + amb[k]);
+    }
+    out[i] = make_float4(o[0], o[1], o[2], o[3]);
+}
+
 }  // namespace vis
 
 gi_status launch_surrogate_features(gi_context* ctx, const gi_vis_params* p, const float* d_depth, int map_w,
@@ -1356,6 +1419,17 @@ gi_status launch_surrogate_finish(gi_context* ctx, const gi_vis_params* p, const
     ctx->launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "surrogate finish launch");
+}
+
+gi_status launch_phong(gi_context* ctx, const gi_vis_params* p, const float* d_pos, const float* d_nrm,
+                       const float* d_vis, const float* d_color, float* d_out, int W, int H, cudaStream_t st) {
+    dim3 grid((W + 31) / 32, (H + 3) / 4);
+    vis::k_phong<<<grid, 128, 0, st>>>(*p, reinterpret_cast<const float4*>(d_pos),
+                                      reinterpret_cast<const float4*>(d_nrm), d_vis,
+                                      reinterpret_cast<const float4*>(d_color), reinterpret_cast<float4*>(d_out), W, H);
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "phong launch");
 }
 
 gi_status launch_area_accumulate(gi_context* ctx, const gi_scene* scene, const float camera_mvp[16], int W, int H,

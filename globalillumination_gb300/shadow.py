@@ -425,6 +425,17 @@ def render_frame_passes(ctx: Context, scene: Scene, frame: Frame, mp: MapParams,
 render_soft_shadows = render_frame
 
 
+def phong_shade(ctx: Context, params: ShadowParams, frame: Frame, pos, nrm, vis, width: int, height: int, out,
+                color=None, stream=None):
+    """shadeScene: deferred Phong of the G-buffer with vis as shadow term; out is float4 per pixel."""
+    assert out.is_cuda and out.numel() >= 4 * width * height
+    p = params.to_c(frame)
+    check(_lib().gi_phong_shade(ctx.handle, C.byref(p), _ptr(pos), _ptr(nrm), _ptr(vis),
+                                _ptr(color) if color is not None else None, width, height, _ptr(out),
+                                _stream_ptr(stream)), "gi_phong_shade")
+    return out
+
+
 def area_light_samples(light: ViewSpec, size: float, n_side: int = 17) -> list:
     """The reference's uniform point-light samples of an area light (n_side^2 views)."""
     n = n_side * n_side

@@ -349,6 +349,18 @@ gi_status gi_render_frame(gi_context* ctx, const gi_scene* scene,
  * the unit disk, interleaved x,y).  Shared with the CPU oracle. */
 gi_status gi_poisson_table(int n, float* xy_out);
 
+/* shadeScene / PhongShading.frag (ShadowMapping/src/main.cpp:449-457,
+ * Shaders/GBuffer/PhongShading.frag:11-46): deferred Phong shading of the
+ * G-buffer (float4 position / normal per pixel) with d_vis as the shadow
+ * term: shadow * color * (diffuse 0.5 max(N.L, 0) + (shadow - intensity)
+ * 0.25 max(R.E, 0)^3 + ambient 0.4), eye-space light from vis
+ * (camera_mv, normal_matrix, light_position, shadow_intensity).  d_color
+ * is float4 per pixel (NULL = white); d_out float4 per pixel; background
+ * pixels get the clear colour (0.63, 0.82, 0.96, 1). */
+gi_status gi_phong_shade(gi_context* ctx, const gi_vis_params* vis, const float* d_pos,
+                         const float* d_nrm, const float* d_vis, const float* d_color,
+                         int width, int height, float* d_out, void* stream);
+
 /* ------------------------------------------------------------------ */
 /* Area-light ground truth (Monte-Carlo over point-light samples)       */
 /* ------------------------------------------------------------------ */

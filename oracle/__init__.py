@@ -27,6 +27,7 @@ def load():
         lib.or_visibility.argtypes = [vp, vp, i, i, vp, vp, vp, i, i, vp, i]
         lib.or_shadow_volume_counts.argtypes = [vp, vp, i, vp, i, vp, f, vp, i, i, i, vp, vp, i]
         lib.or_rbssm_hits.argtypes = [vp, i]
+        lib.or_phong_shade.argtypes = [vp, vp, vp, vp, vp, i, i, vp]
         lib.or_area_light_visibility.argtypes = [vp, vp, i, vp, i, vp, vp, i, i, i, f, f, f, vp, f, i, i, vp, i]
         for fn in (lib.or_shadow_map, lib.or_gbuffer, lib.or_visibility, lib.or_shadow_volume_counts):
             fn.restype = None
@@ -106,4 +107,13 @@ def area_light_visibility(points, normals, indices, mvps, biased, S, bias_mode, 
                                     mv.ctypes.data,
                                     bs.ctypes.data, mv.size // 16, S, bias_mode, cbias, factor, units, cm.ctypes.data,
                                     intensity, width, height, out.ctypes.data, threads)
+    return out
+
+
+def phong_shade(vis_params, pos, nrm, vis, width, height, color=None):
+    ps, ns, vs = _f32(pos), _f32(nrm), _f32(vis)
+    cs = _f32(color) if color is not None else None
+    out = np.empty(height * width * 4, np.float32)
+    load().or_phong_shade(C.byref(vis_params), ps.ctypes.data, ns.ctypes.data, vs.ctypes.data,
+                          cs.ctypes.data if cs is not None else None, width, height, out.ctypes.data)
     return out

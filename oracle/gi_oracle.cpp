@@ -1573,6 +1573,62 @@ extern "C" void or_visibility(const gi_vis_params* p, const float* depth, int ma
         }
 }
 
+// shadeScene / PhongShading.frag:11-46: shadow * fragmentColor *
+// (Idiff + Ispec + Iamb), normalize(x) = x * (1 / sqrt(dot(x, x))), E from
+// the 4-component eye-space vertex, pow(x, 3) as x * x * x.
+extern "C" void or_phong_shade(const gi_vis_params* p, const float* pos, const float* nrm, const float* vis,
+                               const float* color, int W, int H, float* out) {
+    for (size_t i = 0; i < (size_t)W * H; ++i) {
+        const float* pv = pos + 4 * i;
+        float* o = out + 4 * i;
+        if (pv[0] == 0.0f) {
+            o[0] = 0.63f;
+            o[1] = 0.82f;
+            o[2] = 0.96f;
+            o[3] = 1.0f;
+            continue;
+        }
+        const float* nv = nrm + 4 * i;
+        const float shadow = vis[i];
+        const float spec_shadow = shadow - p->shadow_intensity;
+        V4 v = mat4_mul(p->camera_mv, V4{pv[0], pv[1], pv[2], pv[3]});
+        const float* nm = p->normal_matrix;
+        float nx = nm[0] * nv[0] + nm[3] * nv[1] + nm[6] * nv[2];
+        float ny = nm[1] * nv[0] + nm[4] * nv[1] + nm[7] * nv[2];
+        float nz = nm[2] * nv[0] + nm[5] * nv[1] + nm[8] * nv[2];
+        const float ninv = 1.0f / std::sqrt(nx * nx + ny * ny + nz * nz);
+        nx = nx * ninv;
+        ny = ny * ninv;
+        nz = nz * ninv;
+        float lx = p->light_position[0] - v.x, ly = p->light_position[1] - v.y, lz = p->light_position[2] - v.z;
+        const float linv = 1.0f / std::sqrt(lx * lx + ly * ly + lz * lz);
+        lx = lx * linv;
+        ly = ly * linv;
+        lz = lz * linv;
+        const float ex0 = -v.x, ey0 = -v.y, ez0 = -v.z, ew0 = -v.w;
+        const float einv = 1.0f / std::sqrt(ex0 * ex0 + ey0 * ey0 + ez0 * ez0 + ew0 * ew0);
+        const float ex = ex0 * einv, ey = ey0 * einv, ez = ez0 * einv;
+        const float ndl = nx * lx + ny * ly + nz * lz;
+        float rx = -(lx - 2.0f * ndl * nx), ry = -(ly - 2.0f * ndl * ny), rz = -(lz - 2.0f * ndl * nz);
+        const float rinv = 1.0f / std::sqrt(rx * rx + ry * ry + rz * rz);
+        rx = rx * rinv;
+        ry = ry * rinv;
+        rz = rz * rinv;
+        const float diff = gmax(ndl, 0.0f);
+        const float re = gmax(rx * ex + ry * ey + rz * ez, 0.0f);
+        const float spec = re * re * re;
+        const float cc[4] = {color ? color[4 * i] : 1.0f, color ? color[4 * i + 1] : 1.0f,
+                             color ? color[4 * i + 2] : 1.0f, color ? color[4 * i + 3] : 1.0f};
+        const float amb[4] = {0.4f, 0.4f, 0.4f, 1.0f}, dif[4] = {0.5f, 0.5f, 0.5f, 1.0f};
+        const float spc[4] = {0.25f, 0.25f, 0.25f, 1.0f};
+        for (int k = 0; k < 4; ++k) {
+            const float idiff = dif[k] * diff;
+            const float ispec = (spec_shadow * spc[k]) * spec;
+            o[k] = (shadow * cc[k]) * ((idiff + ispec) + amb[k]);
+        }
+    }
+}
+
 // renderMonteCarlo (SoftShadowMapping/src/main.cpp:756-811) + the uniform
 // branch of AccurateSoftShadow.frag:52-133: one map per sample (mvps, the
 // unbiased light MVPs), then per pixel commonShadowCoord from columns 0-2 of

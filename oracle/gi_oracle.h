@@ -57,6 +57,10 @@ void or_shadow_volume_counts(const float* points, const float* normals,
                              int depth_func, uint8_t* out_stencil,
                              float* out_depth, int threads);
 
+/* Deferred Phong shading (PhongShading.frag); out is float4 per pixel. */
+void or_phong_shade(const gi_vis_params* p, const float* pos, const float* nrm, const float* vis,
+                    const float* color, int W, int H, float* out);
+
 /* Area-light ground truth (renderMonteCarlo + AccurateSoftShadow.frag):
  * mvps / biased are n x 16 light matrices of the sample lights. */
 void or_area_light_visibility(const float* points, const float* normals, int nv,

@@ -340,3 +340,21 @@ def test_area_light_truth_lit_and_umbra():
     g = v[geo]
     assert (g >= 0.25).all() and (g <= 1.0).all()
     assert (g == 0.25).sum() > 10 and (g == 1.0).sum() > 500 and ((g > 0.25) & (g < 1.0)).sum() > 10
+
+
+def test_phong_single_pixel_known_answer():
+    f = np.float32
+    p = gi.ShadowParams.defaults(api.GI_TECH_HARD)
+    fr = gi.Frame(IDENTITY, IDENTITY, IDENTITY, IDENTITY, np.eye(3, dtype=np.float32).reshape(-1),
+                  np.array([0.5, 0.0, 10.0], np.float32))
+    pos = np.array([0.5, 0.0, -5.0, 1.0, 0.0, 0.0, 0.0, 1.0], np.float32)  # one surface pixel, one background
+    nrm = np.array([0.0, 0.0, 1.0, 1.0, 0.0, 0.0, 0.0, 1.0], np.float32)
+    vis = np.array([1.0, 0.0], np.float32)
+    out = oracle.phong_shade(p.to_c(fr), pos, nrm, vis, 2, 1).reshape(2, 4)
+    # N = L = R = (0, 0, 1); E = (-0.5, 0, 5) / sqrt(26.25) from the 4-component normalise
+    e = f(f(5.0) * f(f(1.0) / np.sqrt(f(26.25), dtype=np.float32)))
+    spec = f(f(e * e) * e)
+    rgb = f(f(f(0.5) + f(f(f(0.75) * f(0.25)) * spec)) + f(0.4))
+    alpha = f(f(f(1.0) + f(f(0.75) * spec)) + f(1.0))  # diffuse and ambient alpha are 1
+    assert out[0].tolist() == [float(rgb)] * 3 + [float(alpha)]
+    assert out[1].tolist() == [float(f(0.63)), float(f(0.82)), float(f(0.96)), 1.0]
