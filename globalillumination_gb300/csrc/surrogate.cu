@@ -363,140 +363,193 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
         : "memory");
 }
 
-__global__ void __launch_bounds__(kThreads) k_conv3_slab(ConvArgs a, const __grid_constant__ CUtensorMap xmap,
-                                                         int tiles_x, int tiles_y) {
+// Persistent CTAs (one per SM) of six warps: warp 0 issues the TMA loads,
+// warp 1 the MMAs, warps 2-5 drain the accumulators (warp w reads TMEM
+// lanes 32 (w % 4) ..).  Two TMEM accumulator sets alternate between tiles,
+// so the epilogue of tile t overlaps the MMAs of tile t + 1.  Barriers:
+// full / empty per smem stage, acc_full / acc_empty per accumulator set.
+constexpr int kPersistThreads = 192;
+
+__host__ __device__ inline SlabGeom persist_geom(int N, int nk) {
+    SlabGeom g;
+    g.ncols = N <= 32 ? 32 : N <= 64 ? 64 : N <= 128 ? 128 : 256;
+    g.R = 256 / g.ncols;  // two accumulator sets of R x ncols columns
+    if (g.R > 8) g.R = 8;
+    g.a_box = (g.R + 2) * kSlabRow;
+    g.slab = (g.a_box + 127) / 128 * 128;
+    g.a_bytes = 2 * g.slab;
+    g.b_bytes = 9 * 2 * N * 16;
+    g.stage_bytes = g.a_bytes + g.b_bytes;
+    g.NS = 4;
+    while (g.NS > 2 && g.NS * g.stage_bytes > 200 * 1024) --g.NS;
+    (void)nk;
+    return g;
+}
+
+__global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, const __grid_constant__ CUtensorMap xmap,
+                                                                int tiles_x, int tiles_y, int tiles) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
-    __shared__ uint64_t full[3], empty[3], done;
+    __shared__ uint64_t full[4], empty[4], acc_full[2], acc_empty[2];
     __shared__ uint32_t tmem_slot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int N = a.cout;
     const int nk = a.cin / 16;
-    const SlabGeom G = slab_geom(N, nk);
+    const SlabGeom G = persist_geom(N, nk);
     const int R = G.R, NS = G.NS;
-    const uint32_t tcols = (uint32_t)(R * G.ncols);
+    const uint32_t set_cols = (uint32_t)(R * G.ncols);
+    const uint32_t tcols = 2 * set_cols;
     if (warp == 0) tmem_alloc(&tmem_slot, tcols);
     if (tid == 0) {
         for (int s = 0; s < NS; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(&done, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 128);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     fence_before();
     __syncthreads();
     fence_after();
     const uint32_t tmem = tmem_slot;
-    const int bx = blockIdx.x % tiles_x;
-    const int by = (blockIdx.x / tiles_x) % tiles_y;
-    const int img = (int)(blockIdx.x / ((long long)tiles_x * tiles_y));
-    const int x0 = bx * 128, y0 = by * R;
     bool ok = true;
+    const int ntiles_mine = tiles > (int)blockIdx.x ? (tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+
+    auto tile_coords = [&](int t, int& x0, int& y0, int& img) {
+        const int bx = t % tiles_x;
+        const int by = (t / tiles_x) % tiles_y;
+        img = t / (tiles_x * tiles_y);
+        x0 = bx * 128;
+        y0 = by * R;
+    };
 
     if (warp == 0) {
+        // TMA producer
         const uint32_t stage_tx = (uint32_t)(2 * G.a_box + G.b_bytes);
-        auto issue = [&](int chunk, int s) {
-            uint8_t* sa = smem + s * G.stage_bytes;
-            mbar_expect_tx(&full[s], stage_tx);
-            tma_load_4d(sa, &xmap, chunk * 16, x0 - 1, y0 - 1, img, &full[s]);
-            tma_load_4d(sa + G.slab, &xmap, chunk * 16 + 8, x0 - 1, y0 - 1, img, &full[s]);
-            bulk_load(sa + G.a_bytes, a.wt + (size_t)chunk * (G.b_bytes / 2), (uint32_t)G.b_bytes, &full[s]);
-        };
+        int g = 0;
+        for (int it = 0; it < ntiles_mine; ++it) {
+            int x0, y0, img;
+            tile_coords((int)blockIdx.x + it * (int)gridDim.x, x0, y0, img);
+            for (int c = 0; c < nk; ++c, ++g) {
+                const int s = g % NS;
+                if (g >= NS) ok &= mbar_wait(&empty[s], (unsigned)((g / NS) - 1) & 1u);
+                if (lane == 0) {
+                    uint8_t* sa = smem + s * G.stage_bytes;
+                    mbar_expect_tx(&full[s], stage_tx);
+                    tma_load_4d(sa, &xmap, c * 16, x0 - 1, y0 - 1, img, &full[s]);
+                    tma_load_4d(sa + G.slab, &xmap, c * 16 + 8, x0 - 1, y0 - 1, img, &full[s]);
+                    bulk_load(sa + G.a_bytes, a.wt + (size_t)c * (G.b_bytes / 2), (uint32_t)G.b_bytes, &full[s]);
+                }
+                __syncwarp();
+            }
+        }
+    } else if (warp == 1) {
+        // MMA issuer
         const uint32_t idesc = idesc_bf16(128, N);
-        if (lane == 0)
-            for (int s = 0; s < NS - 1 && s < nk; ++s) issue(s, s);
-        for (int i = 0; i < nk; ++i) {
-            const int s = i % NS;
-            ok &= mbar_wait(&full[s], (unsigned)(i / NS) & 1u);
-            if (lane == 0) {
-                fence_after();
-                const uint8_t* sa = smem + s * G.stage_bytes;
-                const uint8_t* sb = sa + G.a_bytes;
-                for (int t = 0; t < 9; ++t) {
-                    const int dy = t / 3, dx = t % 3;
-                    const uint64_t bd = smem_desc(smem_u32(sb + t * 2 * N * 16), (uint32_t)N * 16u, 128u);
-                    for (int r = 0; r < R; ++r) {
-                        const uint64_t ad =
-                            smem_desc(smem_u32(sa + (r + dy) * kSlabRow + dx * 16), (uint32_t)G.slab, 128u);
-                        mma_bf16(tmem + (uint32_t)(r * G.ncols), ad, bd, idesc, (i > 0 || t > 0) ? 1u : 0u);
+        int g = 0;
+        for (int it = 0; it < ntiles_mine; ++it) {
+            const int b = it & 1;
+            if (it >= 2) ok &= mbar_wait(&acc_empty[b], (unsigned)((it >> 1) - 1) & 1u);
+            fence_after();
+            const uint32_t acc = tmem + (uint32_t)b * set_cols;
+            for (int c = 0; c < nk; ++c, ++g) {
+                const int s = g % NS;
+                ok &= mbar_wait(&full[s], (unsigned)(g / NS) & 1u);
+                if (lane == 0) {
+                    fence_after();
+                    const uint8_t* sa = smem + s * G.stage_bytes;
+                    const uint8_t* sb = sa + G.a_bytes;
+                    for (int t = 0; t < 9; ++t) {
+                        const int dy = t / 3, dx = t % 3;
+                        const uint64_t bd = smem_desc(smem_u32(sb + t * 2 * N * 16), (uint32_t)N * 16u, 128u);
+                        for (int r = 0; r < R; ++r) {
+                            const uint64_t ad = smem_desc(smem_u32(sa + (r + dy) * kSlabRow + dx * 16),
+                                                          (uint32_t)G.slab, 128u);
+                            mma_bf16(acc + (uint32_t)(r * G.ncols), ad, bd, idesc, (c > 0 || t > 0) ? 1u : 0u);
+                        }
+                    }
+                    mma_commit(&empty[s]);
+                    if (c == nk - 1) mma_commit(&acc_full[b]);
+                }
+                __syncwarp();
+            }
+        }
+    } else {
+        // epilogue: warps 2..5 -> TMEM lane quarter warp % 4
+        const int q = warp & 3;
+        for (int it = 0; it < ntiles_mine; ++it) {
+            const int b = it & 1;
+            int x0, y0, img;
+            tile_coords((int)blockIdx.x + it * (int)gridDim.x, x0, y0, img);
+            ok &= mbar_wait(&acc_full[b], (unsigned)(it >> 1) & 1u);
+            fence_after();
+            const uint32_t acc = tmem + (uint32_t)b * set_cols;
+            const int xo = x0 + q * 32 + lane;
+            for (int r = 0; r < R; ++r) {
+                const int yo = y0 + r;
+                const bool live = xo < a.w && yo < a.h;
+                const long long p = ((long long)img * a.h + yo) * a.w + xo;
+                float h0 = a.hw ? __ldg(a.hb) : 0.0f, h1 = a.hw ? __ldg(a.hb + 1) : 0.0f;
+                for (int c0 = 0; c0 < N; c0 += 16) {
+                    float v[16];
+                    tmem_ld16(acc + ((uint32_t)(q * 32) << 16) + (uint32_t)(r * G.ncols + c0), v);
+                    if (!live) continue;
+                    if (a.bias) {
+#pragma unroll
+                        for (int k = 0; k < 16; ++k) v[k] += __ldg(a.bias + c0 + k);
+                    }
+                    if (a.act == GI_ACT_RELU) {
+#pragma unroll
+                        for (int k = 0; k < 16; ++k) v[k] = fmaxf(v[k], 0.0f);
+                    }
+                    const long long o = p * a.y_c + a.y_off + c0;
+                    if (a.mask) {
+                        const uint4* mp = reinterpret_cast<const uint4*>(a.mask + o);
+                        uint4 m0 = __ldg(mp), m1 = __ldg(mp + 1);
+                        const uint32_t mw[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
+#pragma unroll
+                        for (int k = 0; k < 16; ++k) {
+                            const uint16_t mv = (uint16_t)(mw[k >> 1] >> ((k & 1) * 16));
+                            if (!(bf16_to_f(mv) > 0.0f)) v[k] = 0.0f;
+                        }
+                    }
+                    if (a.y32) {
+                        float4* yp = reinterpret_cast<float4*>(a.y32 + p * N + c0);
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            yp[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+                    }
+                    if (a.hw) {
+#pragma unroll
+                        for (int k = 0; k < 16; ++k) {
+                            const float vb = bf16_to_f(f_to_bf16(v[k]));
+                            h0 += __ldg(a.hw + c0 + k) * vb;
+                            h1 += __ldg(a.hw + N + c0 + k) * vb;
+                        }
+                    }
+                    if (a.y) {
+                        uint32_t pk[8];
+#pragma unroll
+                        for (int k = 0; k < 8; ++k)
+                            pk[k] = (uint32_t)f_to_bf16(v[2 * k]) | ((uint32_t)f_to_bf16(v[2 * k + 1]) << 16);
+                        uint4* yp = reinterpret_cast<uint4*>(a.y + o);
+                        yp[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                        yp[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
                     }
                 }
-                mma_commit(&empty[s]);
+                if (a.hout && live) *reinterpret_cast<float2*>(a.hout + p * 2) = make_float2(h0, h1);
             }
-            __syncwarp();
-            const int j = i + NS - 1;
-            if (j < nk) {
-                const int sj = j % NS;
-                if (i >= 1) ok &= mbar_wait(&empty[sj], (unsigned)((i - 1) / NS) & 1u);
-                if (lane == 0) issue(j, sj);
-            }
-            __syncwarp();
+            fence_before();
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[b])) : "memory");
         }
-        if (lane == 0) mma_commit(&done);
-        __syncwarp();
-    }
-    ok &= mbar_wait(&done, 0u);
-    fence_after();
-
-    const int xo = x0 + warp * 32 + lane;
-    for (int r = 0; r < R; ++r) {
-        const int yo = y0 + r;
-        const bool live = xo < a.w && yo < a.h;
-        const long long p = ((long long)img * a.h + yo) * a.w + xo;
-        float h0 = a.hw ? __ldg(a.hb) : 0.0f, h1 = a.hw ? __ldg(a.hb + 1) : 0.0f;
-        for (int c0 = 0; c0 < N; c0 += 16) {
-            float v[16];
-            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(r * G.ncols + c0), v);
-            if (!live) continue;
-            if (a.bias) {
-#pragma unroll
-                for (int q = 0; q < 16; ++q) v[q] += __ldg(a.bias + c0 + q);
-            }
-            if (a.act == GI_ACT_RELU) {
-#pragma unroll
-                for (int q = 0; q < 16; ++q) v[q] = fmaxf(v[q], 0.0f);
-            }
-            const long long o = p * a.y_c + a.y_off + c0;
-            if (a.mask) {
-                const uint4* mp = reinterpret_cast<const uint4*>(a.mask + o);
-                uint4 m0 = __ldg(mp), m1 = __ldg(mp + 1);
-                const uint32_t mw[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
-#pragma unroll
-                for (int q = 0; q < 16; ++q) {
-                    const uint16_t mv = (uint16_t)(mw[q >> 1] >> ((q & 1) * 16));
-                    if (!(bf16_to_f(mv) > 0.0f)) v[q] = 0.0f;
-                }
-            }
-            if (a.y32) {
-                float4* yp = reinterpret_cast<float4*>(a.y32 + p * N + c0);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) yp[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-            }
-            if (a.hw) {
-#pragma unroll
-                for (int q = 0; q < 16; ++q) {
-                    const float vb = bf16_to_f(f_to_bf16(v[q]));
-                    h0 += __ldg(a.hw + c0 + q) * vb;
-                    h1 += __ldg(a.hw + N + c0 + q) * vb;
-                }
-            }
-            if (a.y) {
-                uint32_t pk[8];
-#pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    pk[q] = (uint32_t)f_to_bf16(v[2 * q]) | ((uint32_t)f_to_bf16(v[2 * q + 1]) << 16);
-                uint4* yp = reinterpret_cast<uint4*>(a.y + o);
-                yp[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-                yp[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
-            }
-        }
-        if (a.hout && live) *reinterpret_cast<float2*>(a.hout + p * 2) = make_float2(h0, h1);
     }
     fence_before();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, tcols);
-    if (!ok && tid == 0 && a.err) atomicOr(a.err, 1u);
+    if (!ok && a.err) atomicOr(a.err, 1u);
 }
 
 // ---- weight gradient ---------------------------------------------------------
@@ -927,7 +980,7 @@ gi_status slab_map(CUtensorMap* m, const uint16_t* x, int n, int h, int w, int c
 }
 
 gi_status launch_slab(const tc::ConvArgs& a, cudaStream_t cs) {
-    const tc::SlabGeom G = tc::slab_geom(a.cout, a.cin / 16);
+    const tc::SlabGeom G = tc::persist_geom(a.cout, a.cin / 16);
     CUtensorMap m;
     gi_status st = slab_map(&m, a.x, a.n, a.h, a.w, a.cin, G.R + 2);
     if (st != GI_OK) return st;
@@ -937,9 +990,13 @@ gi_status launch_slab(const tc::ConvArgs& a, cudaStream_t cs) {
         attr = true;
     }
     const int tx = (a.w + 127) / 128, ty = (a.h + G.R - 1) / G.R;
-    const long long blocks = (long long)tx * ty * a.n;
-    if (blocks > 0x7FFFFFFFLL) return fail(GI_ERR_INVALID_ARG, "gi_conv2d_bf16: too many tiles");
-    tc::k_conv3_slab<<<(unsigned)blocks, tc::kThreads, G.NS * G.stage_bytes + 128, cs>>>(a, m, tx, ty);
+    const long long tiles = (long long)tx * ty * a.n;
+    if (tiles > 0x7FFFFFFFLL) return fail(GI_ERR_INVALID_ARG, "gi_conv2d_bf16: too many tiles");
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int grid = (int)std::min<long long>(tiles, sms);
+    tc::k_conv3_slab<<<grid, tc::kPersistThreads, G.NS * G.stage_bytes + 128, cs>>>(a, m, tx, ty, (int)tiles);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_conv2d_bf16 launch");
 }
