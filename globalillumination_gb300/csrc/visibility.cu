@@ -213,19 +213,49 @@ __device__ float avg_blocker_grid(const gi_vis_params& p, const Ctx& c, V4 n) {
     return nb == 0 ? 1.0f : avg / (float)nb;
 }
 
-__device__ float avg_blocker_poisson(const gi_vis_params& p, const Ctx& c, V4 n) {
+// Same texel as fetch() when s * W and t * H are not NaN: floor-convert
+// (out-of-range values saturate and fail the unsigned range check, -0
+// becomes 0 as floorf(-0) >= 0 does).  Callers use it only when every
+// input of the tap coordinates is finite, so no coordinate can be NaN.
+__device__ __forceinline__ float fetch_finite(const Ctx& c, float s, float t) {
+    const int ix = __float2int_rd(s * c.fW);
+    const int iy = __float2int_rd(t * c.fH);
+    if ((unsigned)ix >= (unsigned)c.W || (unsigned)iy >= (unsigned)c.H) return 0.0f;
+    return __ldg(c.map + (iy * c.W + ix));
+}
+
+__device__ __forceinline__ bool finite3(float a, float b, float d) {
+    return isfinite(a) && isfinite(b) && isfinite(d);
+}
+
+template <bool FAST>
+__device__ float avg_blocker_poisson_t(const gi_vis_params& p, const Ctx& c, V4 n, float bsw) {
     float avg = 0.0f;
     int nb = 0;
-    float bsw = blocker_search_width(p, c);
     for (int i = 0; i < p.poisson_blocker_taps; ++i) {
         float2 o = c_poisson[i];
-        float d = fetch(c, n.x + o.x * bsw, n.y + o.y * bsw);
+        const float s = n.x + o.x * bsw, t = n.y + o.y * bsw;
+        float d = FAST ? fetch_finite(c, s, t) : fetch(c, s, t);
         if (n.z > d) {
             avg += d;
             nb++;
         }
     }
     return nb == 0 ? 1.0f : avg / (float)nb;
+}
+
+template <bool FAST>
+__device__ float pcss_filter_poisson_t(const gi_vis_params& p, const Ctx& c, float pw, V4 n) {
+    float illum = 0.0f;
+    const int nf = p.poisson_filter_taps;
+    for (int j = 0; j < nf; ++j) {
+        float2 o = c_poisson[j];
+        const float s = n.x + o.x * pw, t = n.y + o.y * pw;
+        float d = FAST ? fetch_finite(c, s, t) : fetch(c, s, t);
+        if (n.z <= d) illum = illum + 1.0f;
+        else illum += c.I;
+    }
+    return illum / (float)nf;
 }
 
 __device__ __forceinline__ float penumbra_width(const gi_vis_params& p, float avg, float z) {
@@ -249,20 +279,6 @@ __device__ float pcss_filter_grid(const gi_vis_params& p, const Ctx& c, float pw
     return illum / (float)(K * K);
 }
 
-__device__ float pcss_filter_poisson(const gi_vis_params& p, const Ctx& c, float pw, V4 n) {
-    float illum = 0.0f;
-    int K = p.kernel_size;
-    float step = 2.0f * pw / (float)K;
-    if (step <= 0.0f || step >= 1.0f) return 1.0f;
-    const int nf = p.poisson_filter_taps;
-    for (int j = 0; j < nf; ++j) {
-        float2 o = c_poisson[j];
-        float d = fetch(c, n.x + o.x * pw, n.y + o.y * pw);
-        if (n.z <= d) illum = illum + 1.0f;
-        else illum += c.I;
-    }
-    return illum / (float)nf;
-}
 
 // ---- RBSM/NonConservativeSMSR.frag and FilteredRBSM.frag -----------------------
 __device__ V4 nc_get_disc_all(const Ctx& c, V4 n) {
@@ -1072,9 +1088,14 @@ __device__ __forceinline__ float shade(const gi_vis_params& p, const Ctx& c, V4 
         }
     } else if (TECH == GI_TECH_PCSS_POISSON) {
         if (sc.w > 0.0f && shadow == 1.0f) {
-            float avg = avg_blocker_poisson(p, c, n);
+            const float bsw = blocker_search_width(p, c);
+            float avg = finite3(n.x, n.y, bsw) ? avg_blocker_poisson_t<true>(p, c, n, bsw)
+                                               : avg_blocker_poisson_t<false>(p, c, n, bsw);
             float pw = penumbra_width(p, avg, n.z);
-            shadow = pcss_filter_poisson(p, c, pw, n);
+            const float step = 2.0f * pw / (float)p.kernel_size;
+            if (step <= 0.0f || step >= 1.0f) shadow = 1.0f;
+            else if (finite3(n.x, n.y, pw)) shadow = pcss_filter_poisson_t<true>(p, c, pw, n);
+            else shadow = pcss_filter_poisson_t<false>(p, c, pw, n);
         }
     } else if (TECH == GI_TECH_SMSR_NONCONSERVATIVE) {
         if (shadow == 1.0f) shadow = nc_smsr(p, c, n);
