@@ -112,8 +112,24 @@ __device__ __forceinline__ float pretest(const gi_vis_params& p, const Ctx& c, V
     return 1.0f;
 }
 
+// Same texel as fetch() when s * W and t * H are not NaN: floor-convert
+// (out-of-range values saturate and fail the unsigned range check, -0
+// becomes 0 as floorf(-0) >= 0 does).  Callers use it only when every
+// input of the tap coordinates is finite, so no coordinate can be NaN.
+__device__ __forceinline__ float fetch_finite(const Ctx& c, float s, float t) {
+    const int ix = __float2int_rd(s * c.fW);
+    const int iy = __float2int_rd(t * c.fH);
+    if ((unsigned)ix >= (unsigned)c.W || (unsigned)iy >= (unsigned)c.H) return 0.0f;
+    return __ldg(c.map + (iy * c.W + ix));
+}
+
+__device__ __forceinline__ bool finite3(float a, float b, float d) {
+    return isfinite(a) && isfinite(b) && isfinite(d);
+}
+
 // ---- Shadow.frag -------------------------------------------------------------
-__device__ float pcf_bilinear(const gi_vis_params& p, const Ctx& c, V4 n) {
+template <bool FAST>
+__device__ float pcf_bilinear_t(const gi_vis_params& p, const Ctx& c, V4 n) {
     float incrW = 1.0f / c.fW, incrH = 1.0f / c.fH;
     float illum = 0.0f;
     float offset = (float)p.penumbra_size;
@@ -121,12 +137,19 @@ __device__ float pcf_bilinear(const gi_vis_params& p, const Ctx& c, V4 n) {
     int count = 0;
     for (float w = -offset; w < offset; w += step)
         for (float h = -offset; h < offset; h += step) {
-            float d = fetch(c, n.x + w * incrW, n.y + h * incrH);
+            const float s = n.x + w * incrW, t = n.y + h * incrH;
+            float d = FAST ? fetch_finite(c, s, t) : fetch(c, s, t);
             if (n.z <= d) illum = illum + 1.0f;
             else illum += c.I;
             count++;
         }
     return illum / (float)count;
+}
+
+__device__ float pcf_bilinear(const gi_vis_params& p, const Ctx& c, V4 n) {
+    // offsets are finite (kernel_order, penumbra_size >= 1), so finite n.x,
+    // n.y give finite tap coordinates
+    return (isfinite(n.x) && isfinite(n.y)) ? pcf_bilinear_t<true>(p, c, n) : pcf_bilinear_t<false>(p, c, n);
 }
 
 __device__ __forceinline__ void cubic(float v, float out[4]) {
@@ -211,21 +234,6 @@ __device__ float avg_blocker_grid(const gi_vis_params& p, const Ctx& c, V4 n) {
             }
         }
     return nb == 0 ? 1.0f : avg / (float)nb;
-}
-
-// Same texel as fetch() when s * W and t * H are not NaN: floor-convert
-// (out-of-range values saturate and fail the unsigned range check, -0
-// becomes 0 as floorf(-0) >= 0 does).  Callers use it only when every
-// input of the tap coordinates is finite, so no coordinate can be NaN.
-__device__ __forceinline__ float fetch_finite(const Ctx& c, float s, float t) {
-    const int ix = __float2int_rd(s * c.fW);
-    const int iy = __float2int_rd(t * c.fH);
-    if ((unsigned)ix >= (unsigned)c.W || (unsigned)iy >= (unsigned)c.H) return 0.0f;
-    return __ldg(c.map + (iy * c.W + ix));
-}
-
-__device__ __forceinline__ bool finite3(float a, float b, float d) {
-    return isfinite(a) && isfinite(b) && isfinite(d);
 }
 
 template <bool FAST>
