@@ -44,6 +44,7 @@ GI_TECH_RPCF_CONSERVATIVE = 7
 GI_TECH_RPCF_SMSR = 8
 GI_TECH_RSMSS = 9
 GI_TECH_HARD_SOFTAPP = 10
+GI_PBA_MARKER = -32768
 GI_TECH_RBSSM = 11
 GI_TECH_COUNT = 12
 GI_ACT_NONE = 0
@@ -191,6 +192,10 @@ _PROTOS = {
     "gi_shadow_volume_counts": (C.c_int, [_VP, _VP, F3, C.c_float, F16, C.c_int, C.c_int, C.c_int,
                                           _VP, _VP, _VP]),
     "gi_phong_shade": (C.c_int, [_VP, C.POINTER(VisParams), _VP, _VP, _VP, _VP, C.c_int, C.c_int, _VP, _VP]),
+    "gi_pba_voronoi": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP]),
+    "gi_edt_soft_shadows": (C.c_int, [_VP, _VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float,
+                                      C.c_float, _VP, _VP, _VP]),
+    "gi_edt_inputs": (C.c_int, [_VP, C.POINTER(VisParams), F16, _VP, _VP, _VP, C.c_int, C.c_int, _VP, _VP, _VP]),
     "gi_area_light_samples": (C.c_int, [C.POINTER(View), C.c_float, C.c_int, _VP]),
     "gi_area_light_visibility": (C.c_int, [_VP, _VP, _VP, C.c_int, C.POINTER(MapParams), F16, C.c_float, C.c_int,
                                            C.c_int, _VP, _VP]),

@@ -114,6 +114,7 @@ extern "C" void gi_context_destroy(gi_context* c) {
     cudaFree(c->d_counts);
     cudaFree(c->d_area_maps);
     cudaFree(c->d_area_acc);
+    cudaFree(c->d_pba_cols);
     for (int i = 0; i < 8; ++i) cudaFree(c->bin_buf[i]);
     for (int k = 0; k < 2; ++k)
         for (int i = 0; i < 8; ++i) cudaFree(c->tier_buf[k][i]);
@@ -609,6 +610,40 @@ extern "C" gi_status gi_phong_shade(gi_context* ctx, const gi_vis_params* vp, co
     if (st == GI_OK) st = check_image(W, H, "gi_phong_shade");
     if (st != GI_OK) return st;
     return gi::launch_phong(ctx, vp, d_pos, d_nrm, d_vis, d_color, d_out, W, H, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" gi_status gi_pba_voronoi(gi_context* ctx, const int16_t* d_sites, int W, int H, int m1, int m2, int m3,
+                                    int16_t* d_nearest, void* stream) {
+    if (!ctx || !d_sites || !d_nearest) return fail(GI_ERR_INVALID_ARG, "gi_pba_voronoi: NULL argument");
+    gi_status st = check_device(ctx);
+    if (st == GI_OK) st = gi::pba_check_shape(W, H, m1, m2, m3, "gi_pba_voronoi");
+    if (st != GI_OK) return st;
+    return gi::launch_pba(ctx, d_sites, nullptr, nullptr, W, H, m1, m2, m3, 0.0f, 0.0f, d_nearest, nullptr,
+                          static_cast<cudaStream_t>(stream));
+}
+
+extern "C" gi_status gi_edt_soft_shadows(gi_context* ctx, const float* d_image, const float* d_position, int W,
+                                         int H, int m1, int m2, int m3, float penumbra, float intensity,
+                                         float* d_out, int16_t* d_nearest, void* stream) {
+    if (!ctx || !d_image || !d_position || !d_out)
+        return fail(GI_ERR_INVALID_ARG, "gi_edt_soft_shadows: NULL argument");
+    gi_status st = check_device(ctx);
+    if (st == GI_OK) st = gi::pba_check_shape(W, H, m1, m2, m3, "gi_edt_soft_shadows");
+    if (st != GI_OK) return st;
+    return gi::launch_pba(ctx, nullptr, d_image, d_position, W, H, m1, m2, m3, penumbra, intensity, d_nearest,
+                          d_out, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" gi_status gi_edt_inputs(gi_context* ctx, const gi_vis_params* vp, const float camera_mvp[16],
+                                   const float* d_pos, const float* d_nrm, const float* d_vis, int W, int H,
+                                   float* d_image, float* d_position, void* stream) {
+    if (!ctx || !vp || !camera_mvp || !d_pos || !d_nrm || !d_vis || !d_image || !d_position)
+        return fail(GI_ERR_INVALID_ARG, "gi_edt_inputs: NULL argument");
+    gi_status st = check_device(ctx);
+    if (st == GI_OK) st = check_image(W, H, "gi_edt_inputs");
+    if (st != GI_OK) return st;
+    return gi::launch_edt_inputs(ctx, vp, camera_mvp, d_pos, d_nrm, d_vis, d_image, d_position, W, H,
+                                 static_cast<cudaStream_t>(stream));
 }
 
 extern "C" gi_status gi_surrogate_features(gi_context* ctx, const gi_scene* s, const gi_map_params* mp,

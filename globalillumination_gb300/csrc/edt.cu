@@ -1,0 +1,532 @@
+// edt.cu -- exact Euclidean distance transform and EDT-filtered hard shadows
+// for sm_103a.
+//
+// Restates on device buffers the reference's only CUDA code: the parallel
+// banding algorithm (PBA, Cao et al. 2010) of ShadowMapping/include/EDT/
+// pba2DKernel.h as ShadowMapping/src/EDT/pba2DHost.cu:121-242 sequences it,
+// together with the site detection (initializeInput, pba2DKernel.h:509-528)
+// and the normalisation (pbaNormalizeDistanceTransform, :541-569) of
+// ShadowMapping's EDTSM mode (src/main.cpp:416-422).  Which of two
+// equidistant sites a pixel receives depends on PBA's bands (m1, m2, m3), its
+// merge order and its FP32 bisector tests, so every result equals the
+// reference's for the same bands.  The kernels are organised for this GPU:
+//
+//   k_pba_columns  phase 1 in one pass.  For band height B = H / m1 >= 2
+//                  the reference's flood / propagate / update kernels give
+//                  each pixel the nearest site of its column, an equidistant
+//                  pair resolved to the site below when that site lies in the
+//                  pixel's band and to the site above otherwise.  A CTA owns 8
+//                  columns x 128 row segments (one thread each): it tests its
+//                  pixels for sites, keeps them as a 64-bit mask, and two warp
+//                  scans over the CTA's segments give every segment its
+//                  nearest sites above and below.  Output: the chosen site's
+//                  row per pixel (int16, row-major, MARKER for an empty
+//                  column) -- no transposes are needed.
+//   k_pba_rows     phases 2-3, one image row per warp, in shared memory: the
+//                  per-band proximate-point stacks and forward links (one
+//                  lane per band), the pairwise band merges level by level
+//                  (one lane per pair), then the coloring: lane 0 walks the
+//                  chain of states that the reference's groups of m3 threads
+//                  hand to each other, and every lane colors its pixels from
+//                  its group's state.  The epilogue writes the nearest-site
+//                  map and / or the normalised EDT shadow.
+//
+// Compiled like every pass with -fmad=false and IEEE division / square root,
+// so each FP32 operation rounds once in the order written (the CPU oracle
+// and the reference's kernels run on the CPU round the same way).
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cstdint>
+
+#include "internal.h"
+#include "raster.h"
+
+namespace gi {
+namespace edt {
+
+constexpr int kMarker = -32768;  // MARKER (ShadowMapping/include/EDT/pba2D.h:60)
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kColW = 8;                 // columns per CTA in the column pass
+constexpr int kSegs = 128;               // row segments per CTA
+constexpr int kColThreads = kColW * kSegs;
+constexpr int kMaxSegRows = 64;          // one 64-bit site mask per thread
+constexpr int kRowThreads = 256;         // 8 rows per CTA in the row pass
+
+enum : int { kFromSites = 0, kFromImage = 1 };
+enum : int { kOutNearest = 1, kOutNormalized = 2 };
+
+// linearize (pba2DKernel.h:499-506) with n = 1, f = 1000: 2.0 * n is a
+// double, so the reference divides in double and rounds to float.  For a
+// quotient in float's normal range that equals the IEEE float division
+// (double carries more than 2 x 24 + 2 bits, so the second rounding is
+// innocuous); tiny quotients take the double path.
+__device__ __forceinline__ float linearize(float depth) {
+    const float d = 1001.0f - depth * 999.0f;
+    float q = 2.0f / d;
+    if (!(fabsf(q) >= 2.3509887e-38f)) q = (float)(2.0 / (double)d);
+    return q;
+}
+
+// ---- phase 1 ---------------------------------------------------------------
+
+struct ColArgs {
+    const short2* sites;   // kFromSites: (x, y) at a site, x == MARKER elsewhere
+    const float4* image;   // kFromImage: (shadow, depth, preEvaluatedShadow, 1)
+    int16_t* cols;         // [H][W]: row of the chosen column site, or MARKER
+    int W, H, S, band;     // S rows per segment; band = H / m1
+    float thr;             // the largest float <= 0.0025
+};
+
+struct Px {
+    float s, L;  // shadow value, linearised depth
+    int f;       // bit 0: inside the image, bit 1: p.z == 1
+};
+
+__device__ __forceinline__ Px px_load(const ColArgs& a, int x, int y) {
+    Px p{0.0f, 0.0f, 0};
+    if (x < 0 || x >= a.W || y < 0 || y >= a.H) return p;
+    const float4 v = __ldg(a.image + (size_t)y * a.W + x);
+    p.s = v.x;
+    p.L = linearize(v.y);
+    p.f = 1 | (v.z == 1.0f ? 2 : 0);
+    return p;
+}
+
+// initializeInput's test of neighbour p against centre c (pba2DKernel.h:520)
+__device__ __forceinline__ bool triggers(const Px& c, const Px& p, float thr) {
+    return p.f == 3 && p.s != c.s && fabsf(c.L - p.L) <= thr;
+}
+
+// (x - 1, x, x + 1) of row y: the centre is loaded, its neighbours come from
+// the adjacent lanes of the 8-lane column group, the group's edge lanes load
+// their outer neighbour themselves.
+__device__ __forceinline__ void load_row(const ColArgs& a, int x, int col, int y, Px* r) {
+    const Px m = px_load(a, x, y);
+    Px l, rr;
+    l.s = __shfl_up_sync(kFull, m.s, 1, kColW);
+    l.L = __shfl_up_sync(kFull, m.L, 1, kColW);
+    l.f = __shfl_up_sync(kFull, m.f, 1, kColW);
+    rr.s = __shfl_down_sync(kFull, m.s, 1, kColW);
+    rr.L = __shfl_down_sync(kFull, m.L, 1, kColW);
+    rr.f = __shfl_down_sync(kFull, m.f, 1, kColW);
+    if (col == 0) l = px_load(a, x - 1, y);
+    if (col == kColW - 1) rr = px_load(a, x + 1, y);
+    r[0] = l;
+    r[1] = m;
+    r[2] = rr;
+}
+
+template <int kMode>
+__global__ void __launch_bounds__(kColThreads) k_pba_columns(const ColArgs a) {
+    __shared__ int s_first[kSegs][kColW], s_last[kSegs][kColW];
+    __shared__ int s_above[kSegs][kColW], s_below[kSegs][kColW];
+    const int col = threadIdx.x & (kColW - 1), seg = threadIdx.x / kColW;
+    const int x = blockIdx.x * kColW + col;
+    const int y0 = seg * a.S;
+    unsigned long long mask = 0;
+    if (kMode == kFromSites) {
+        if (x < a.W)
+            for (int i = 0; i < a.S; ++i) {
+                const int y = y0 + i;
+                if (y < a.H && a.sites[(size_t)y * a.W + x].x != kMarker) mask |= 1ull << i;
+            }
+    } else {
+        Px u[3], c[3], d[3];
+        load_row(a, x, col, y0 - 1, u);
+        load_row(a, x, col, y0, c);
+        for (int i = 0; i < a.S; ++i) {
+            load_row(a, x, col, y0 + i + 1, d);
+            if (x < a.W && y0 + i < a.H) {
+                const Px& ctr = c[1];
+                bool s = false;
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+                    s = s || triggers(ctr, u[k], a.thr) || triggers(ctr, c[k], a.thr) || triggers(ctr, d[k], a.thr);
+                if (s) mask |= 1ull << i;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                u[k] = c[k];
+                c[k] = d[k];
+            }
+        }
+    }
+    s_first[seg][col] = mask ? y0 + __ffsll((long long)mask) - 1 : INT_MAX;
+    s_last[seg][col] = mask ? y0 + 63 - __clzll((long long)mask) : -1;
+    __syncthreads();
+    // warp w < 8 scans column w: lane l holds segments 4l .. 4l + 3
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp < kColW) {
+        int lv[4], fv[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            lv[k] = s_last[4 * lane + k][warp];
+            fv[k] = s_first[4 * lane + k][warp];
+        }
+        int incl = max(max(lv[0], lv[1]), max(lv[2], lv[3]));
+        int inclf = min(min(fv[0], fv[1]), min(fv[2], fv[3]));
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(kFull, incl, o);
+            const int tf = __shfl_down_sync(kFull, inclf, o);
+            if (lane >= o) incl = max(incl, t);
+            if (lane + o < 32) inclf = min(inclf, tf);
+        }
+        int run = __shfl_up_sync(kFull, incl, 1);
+        int runf = __shfl_down_sync(kFull, inclf, 1);
+        if (lane == 0) run = -1;
+        if (lane == 31) runf = INT_MAX;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            s_above[4 * lane + k][warp] = run;
+            run = max(run, lv[k]);
+        }
+#pragma unroll
+        for (int k = 3; k >= 0; --k) {
+            s_below[4 * lane + k][warp] = runf;
+            runf = min(runf, fv[k]);
+        }
+    }
+    __syncthreads();
+    if (x >= a.W) return;
+    const int above = s_above[seg][col], below = s_below[seg][col];
+    for (int i = 0; i < a.S; ++i) {
+        const int y = y0 + i;
+        if (y >= a.H) break;
+        const unsigned long long le = mask & ((2ull << i) - 1);  // sites at rows <= y
+        const unsigned long long ge = mask >> i;                  // sites at rows >= y
+        const int up = le ? y0 + 63 - __clzll((long long)le) : above;
+        const int dn = ge ? y + __ffsll((long long)ge) - 1 : below;
+        int v;
+        if (up < 0) {
+            v = dn == INT_MAX ? kMarker : dn;
+        } else if (dn == INT_MAX) {
+            v = up;
+        } else {
+            const int da = y - up, db = dn - y;
+            v = db < da ? dn : (da < db ? up : (dn / a.band == y / a.band ? dn : up));
+        }
+        a.cols[(size_t)y * a.W + x] = (int16_t)v;
+    }
+}
+
+// ---- phases 2 and 3 ----------------------------------------------------------
+
+struct RowArgs {
+    const int16_t* cols;
+    int W, H, m2, m3, wpb, per_warp;  // per_warp: shared bytes per row
+    int out;                          // kOutNearest | kOutNormalized
+    short2* nearest;                  // (site x, site y) per pixel
+    const float4* image;              // kOutNormalized inputs
+    const float4* position;
+    float* out4;                      // channels 0-1 written
+    float penumbra, intensity, thr;   // thr: the largest float <= 0.0005
+};
+
+// One row's state: cand[p] = row of column p's phase-1 site (the reference's
+// transposed texture), lk[p] = its textures[0] line (stack value and back
+// pointer, later forward and back pointers), st[k] = the list position the
+// coloring of group k starts from.
+struct Row {
+    int16_t* cand;
+    short2* lk;
+    int* st;
+    int W, line;
+
+    // textures[0] after kernelDoubleToSingleList; tex1Dfetch reads zero
+    // outside the texture
+    __device__ __forceinline__ short2 col(int p) const {
+        if (p < 0 || p >= W) return make_short2(0, 0);
+        return make_short2(cand[p], lk[p].y);
+    }
+};
+
+// interpoint (pba2DKernel.h:227-236)
+__device__ __forceinline__ float interpoint(int x1, int y1, int x2, int y2, int x0) {
+    const float xM = (float)(x1 + x2) / 2.0f;
+    const float yM = (float)(y1 + y2) / 2.0f;
+    const float nx = (float)(x2 - x1);
+    const float ny = (float)(y2 - y1);
+    return yM + nx * (xM - (float)x0) / ny;
+}
+
+// kernelProximatePoints (pba2DKernel.h:238-268) for the band [b0, b0 + B)
+__device__ void proximate(const Row& r, int b0, int B) {
+    int lasty = -1;
+    short2 last1 = make_short2(0, -1), last2 = make_short2(0, -1);
+    for (int p = b0; p < b0 + B; ++p) {
+        const int g = r.cand[p];
+        if (g == kMarker) continue;
+        while (last2.y >= 0) {
+            const float i1 = interpoint(last1.x, last2.y, last2.x, lasty, r.line);
+            const float i2 = interpoint(last2.x, lasty, g, p, r.line);
+            if (i1 < i2) break;
+            lasty = last2.y;
+            last2 = last1;
+            if (last1.y >= 0) last1 = r.lk[last1.y];
+        }
+        last1 = last2;
+        last2 = make_short2((short)g, (short)lasty);
+        lasty = p;
+        r.lk[p] = last2;
+    }
+    if (lasty != b0 + B - 1) r.lk[b0 + B - 1] = make_short2((short)kMarker, (short)lasty);
+}
+
+// kernelCreateForwardPointers (:270-296)
+__device__ void forward(const Row& r, int b0, int B) {
+    const int ty = b0 + B - 1;
+    int lasty = -1;
+    short2 cur = r.lk[ty];
+    int nexty = cur.x == kMarker ? cur.y : ty;
+    int p = ty;
+    for (int i = 0; i < B; ++i, --p)
+        if (ty - i == nexty) {
+            cur = make_short2((short)lasty, r.lk[p].y);
+            r.lk[p] = cur;
+            lasty = nexty;
+            nexty = cur.y;
+        }
+    if (lasty != ty - B + 1) r.lk[p + 1] = make_short2((short)lasty, (short)kMarker);
+}
+
+// kernelMergeBands (:298-435) for bands band1 and band1 + 1 of size B
+__device__ void merge(const Row& r, int band1, int B) {
+    const int band2 = band1 + 1;
+    int lasty = band2 * B - 1;
+    short2 last2 = make_short2(r.cand[lasty], r.lk[lasty].y), last1 = make_short2(0, 0);
+    if (last2.x == kMarker) {
+        lasty = last2.y;
+        last2 = lasty >= 0 ? make_short2(r.cand[lasty], r.lk[lasty].y) : make_short2(kMarker, kMarker);
+    }
+    if (last2.y >= 0) last1 = make_short2(r.cand[last2.y], r.lk[last2.y].y);
+    int firsty = band2 * B;
+    short2 cur = make_short2(r.lk[firsty].x, r.cand[firsty]);
+    if (cur.y == kMarker) {
+        firsty = cur.x;
+        cur = firsty >= 0 ? make_short2(r.lk[firsty].x, r.cand[firsty]) : make_short2(kMarker, kMarker);
+    }
+    int top = 0;
+    while (top < 2 && cur.y >= 0) {
+        while (last2.y >= 0) {
+            const float i1 = interpoint(last1.x, last2.y, last2.x, lasty, r.line);
+            const float i2 = interpoint(last2.x, lasty, cur.y, firsty, r.line);
+            if (i1 < i2) break;
+            lasty = last2.y;
+            last2 = last1;
+            --top;
+            if (last1.y >= 0) last1 = make_short2(r.cand[last1.y], r.lk[last1.y].y);
+        }
+        r.lk[firsty] = make_short2(cur.x, (short)lasty);
+        if (lasty >= 0) r.lk[lasty] = make_short2((short)firsty, last2.y);
+        last1 = last2;
+        last2 = make_short2(cur.y, (short)lasty);
+        lasty = firsty;
+        firsty = cur.x;
+        top = max(1, top + 1);
+        cur = firsty >= 0 ? make_short2(r.lk[firsty].x, r.cand[firsty]) : make_short2(kMarker, kMarker);
+    }
+    // head and tail pointers of the merged band
+    firsty = band1 * B;
+    lasty = band2 * B;
+    cur = r.lk[firsty];
+    if (cur.y == kMarker && cur.x < 0) {
+        const short2 l = r.lk[lasty];
+        cur.x = l.y == kMarker ? l.x : (short)lasty;
+        r.lk[firsty] = cur;
+    }
+    firsty = band1 * B + B - 1;
+    lasty = band2 * B + B - 1;
+    cur = r.lk[lasty];
+    if (cur.x == kMarker && cur.y < 0) {
+        const short2 l = r.lk[firsty];
+        cur.y = l.x == kMarker ? l.y : (short)firsty;
+        r.lk[lasty] = cur;
+    }
+}
+
+// kernelColor's walk (:467-486) from the list position lasty for pixel ty:
+// move on towards the head while the squared distance does not grow.
+// Returns the final list position (the site's x); its row is col(x).x.
+__device__ __forceinline__ int walk(const Row& r, int lasty, int ty) {
+    short2 last2 = r.col(lasty), last1 = make_short2(0, 0);
+    if (last2.y >= 0) last1 = r.col(last2.y);
+    int dx = last2.x - r.line, dy = lasty - ty;
+    unsigned best = (unsigned)(dx * dx + dy * dy);
+    while (last2.y >= 0) {
+        dx = last1.x - r.line;
+        dy = last2.y - ty;
+        const unsigned dist = (unsigned)(dx * dx + dy * dy);
+        if (dist > best) break;
+        best = dist;
+        lasty = last2.y;
+        last2 = last1;
+        if (last2.y >= 0) last1 = r.col(last2.y);
+    }
+    return lasty;
+}
+
+__device__ __forceinline__ float plerp1(float v0, float t) { return (1.0f - t) * v0 + t * 1.0f; }
+
+template <int kOut>
+__global__ void __launch_bounds__(kRowThreads) k_pba_rows(const RowArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int line = blockIdx.x * a.wpb + warp;
+    if (line >= a.H) return;  // whole warps only; the kernel has no block barrier
+    unsigned char* base = smem + (size_t)warp * a.per_warp;
+    Row r;
+    r.W = a.W;
+    r.line = line;
+    r.cand = reinterpret_cast<int16_t*>(base);
+    r.lk = reinterpret_cast<short2*>(base + (size_t)a.W * 2);
+    r.st = reinterpret_cast<int*>(base + (size_t)a.W * 6);
+    const uint4* src = reinterpret_cast<const uint4*>(a.cols + (size_t)line * a.W);
+    for (int i = lane; i < a.W / 8; i += 32) reinterpret_cast<uint4*>(r.cand)[i] = src[i];
+    __syncwarp();
+    // pba2DPhase2: band stacks and links, then the merges
+    const int B2 = a.W / a.m2;
+    for (int b = lane; b < a.m2; b += 32) {
+        proximate(r, b * B2, B2);
+        forward(r, b * B2, B2);
+    }
+    __syncwarp();
+    for (int nb = a.m2; nb > 1; nb /= 2) {
+        const int B = a.W / nb;
+        for (int pr = lane; pr < nb / 2; pr += 32) merge(r, 2 * pr, B);
+        __syncwarp();
+    }
+    // pba2DPhase3: group k covers pixels W-1-k*m3 down to W-(k+1)*m3 and
+    // starts from the state its predecessor's last pixel reached
+    const int G = a.W / a.m3;
+    if (lane == 0) {
+        int lasty = a.W - 1;
+        const short2 tail = r.col(lasty);
+        if (tail.x == kMarker) lasty = tail.y;
+        for (int k = 0; k < G; ++k) {
+            r.st[k] = lasty;
+            lasty = walk(r, lasty, a.W - (k + 1) * a.m3);
+        }
+    }
+    __syncwarp();
+    for (int p = lane; p < a.W; p += 32) {
+        const int sx = walk(r, r.st[(a.W - 1 - p) / a.m3], p);
+        const int sy = r.col(sx).x;
+        const size_t q = (size_t)line * a.W + p;
+        if (kOut & kOutNearest) a.nearest[q] = make_short2((short)sx, (short)sy);
+        if (kOut & kOutNormalized) {
+            // pbaNormalizeDistanceTransform (pba2DKernel.h:541-569); tex2D
+            // clamps the site's coordinates
+            const int cx = min(max(sx, 0), a.W - 1), cy = min(max(sy, 0), a.H - 1);
+            const size_t qs = (size_t)cy * a.W + cx;
+            const float4 ip = __ldg(a.image + q), sp = __ldg(a.image + qs);
+            const float4 p1 = __ldg(a.position + q), p2 = __ldg(a.position + qs);
+            const float dx = p1.x - p2.x, dy = p1.y - p2.y, dz = p1.z - p2.z;
+            const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
+            float v;
+            if (sp.z != 1.0f || fabsf(linearize(sp.y) - linearize(ip.y)) > a.thr || dist > a.penumbra / 2.0f)
+                v = ip.x;
+            else if (ip.x == a.intensity)
+                v = plerp1(0.5f - dist / a.penumbra, a.intensity);
+            else
+                v = plerp1(0.5f + dist / a.penumbra, a.intensity);
+            *reinterpret_cast<float2*>(a.out4 + 4 * q) = make_float2(v, ip.y);
+        }
+    }
+}
+
+// largest float not above c
+float float_at_most(double c) {
+    float t = (float)c;
+    if ((double)t > c) t = nextafterf(t, -INFINITY);
+    return t;
+}
+
+template <class K>
+gi_status set_smem(K kernel, int bytes) {
+    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "pba rows shared memory");
+}
+
+}  // namespace edt
+
+gi_status pba_check_shape(int W, int H, int m1, int m2, int m3, const char* who) {
+    const std::string w(who);
+    if (W < 8 || H < 2 || W > 8192 || H > edt::kSegs * edt::kMaxSegRows || W % 8 != 0)
+        return fail(GI_ERR_INVALID_ARG, w + ": width must be a multiple of 8 in [8, 8192], height in [2, 8192]");
+    if (m1 < 1 || H % m1 != 0 || H / m1 < 2)
+        return fail(GI_ERR_INVALID_ARG, w + ": phase-1 bands must divide the height into bands of >= 2 rows");
+    if (m2 < 1 || (m2 & (m2 - 1)) != 0 || W % m2 != 0 || W / m2 < 2)
+        return fail(GI_ERR_INVALID_ARG,
+                    w + ": phase-2 bands must be a power of two dividing the width into bands of >= 2 pixels");
+    if (m3 < 1 || W % m3 != 0) return fail(GI_ERR_INVALID_ARG, w + ": phase-3 groups must divide the width");
+    return GI_OK;
+}
+
+gi_status launch_pba(gi_context* ctx, const int16_t* d_sites, const float* d_image, const float* d_position,
+                     int W, int H, int m1, int m2, int m3, float penumbra, float intensity, int16_t* d_nearest,
+                     float* d_out4, cudaStream_t st) {
+    using namespace edt;
+    gi_status s = ensure_buffer(reinterpret_cast<void**>(&ctx->d_pba_cols), &ctx->cap_pba_cols,
+                                (size_t)W * H * sizeof(int16_t));
+    if (s != GI_OK) return s;
+    ColArgs ca;
+    ca.sites = reinterpret_cast<const short2*>(d_sites);
+    ca.image = reinterpret_cast<const float4*>(d_image);
+    ca.cols = ctx->d_pba_cols;
+    ca.W = W;
+    ca.H = H;
+    ca.S = (H + kSegs - 1) / kSegs;
+    ca.band = H / m1;
+    ca.thr = float_at_most(0.0025);
+    const dim3 cgrid((W + kColW - 1) / kColW);
+    if (d_sites)
+        k_pba_columns<kFromSites><<<cgrid, kColThreads, 0, st>>>(ca);
+    else
+        k_pba_columns<kFromImage><<<cgrid, kColThreads, 0, st>>>(ca);
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail_cuda(e, "pba columns launch");
+
+    RowArgs ra;
+    ra.cols = ctx->d_pba_cols;
+    ra.W = W;
+    ra.H = H;
+    ra.m2 = m2;
+    ra.m3 = m3;
+    ra.per_warp = (W * 6 + (W / m3) * 4 + 15) / 16 * 16;
+    ra.wpb = max(1, min(kRowThreads / 32, (200 * 1024) / ra.per_warp));
+    ra.out = (d_nearest ? kOutNearest : 0) | (d_out4 ? kOutNormalized : 0);
+    ra.nearest = reinterpret_cast<short2*>(d_nearest);
+    ra.image = reinterpret_cast<const float4*>(d_image);
+    ra.position = reinterpret_cast<const float4*>(d_position);
+    ra.out4 = d_out4;
+    ra.penumbra = penumbra;
+    ra.intensity = intensity;
+    ra.thr = float_at_most(0.0005);
+    const int smem = ra.per_warp * ra.wpb;
+    const dim3 rgrid((H + ra.wpb - 1) / ra.wpb);
+    switch (ra.out) {
+        case kOutNearest:
+            s = set_smem(k_pba_rows<kOutNearest>, smem);
+            if (s == GI_OK) k_pba_rows<kOutNearest><<<rgrid, ra.wpb * 32, smem, st>>>(ra);
+            break;
+        case kOutNormalized:
+            s = set_smem(k_pba_rows<kOutNormalized>, smem);
+            if (s == GI_OK) k_pba_rows<kOutNormalized><<<rgrid, ra.wpb * 32, smem, st>>>(ra);
+            break;
+        case kOutNearest | kOutNormalized:
+            s = set_smem(k_pba_rows<kOutNearest | kOutNormalized>, smem);
+            if (s == GI_OK) k_pba_rows<kOutNearest | kOutNormalized><<<rgrid, ra.wpb * 32, smem, st>>>(ra);
+            break;
+        default:
+            return fail(GI_ERR_INVALID_ARG, "pba: no output requested");
+    }
+    if (s != GI_OK) return s;
+    ctx->launches++;
+    e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "pba rows launch");
+}
+
+}  // namespace gi

@@ -100,6 +100,9 @@ struct gi_context {
     size_t cap_area_maps = 0;
     float* d_area_acc = nullptr;
     size_t cap_area_acc = 0;
+    // PBA distance transform: phase-1 site row per pixel (int16)
+    int16_t* d_pba_cols = nullptr;
+    size_t cap_pba_cols = 0;
     // second stream for the camera-key pass of gi_render_frame, and the
     // fork / join events (cudaStream_t / cudaEvent_t)
     void* aux_stream = nullptr;

@@ -64,6 +64,23 @@ gi_status launch_area_accumulate(gi_context* ctx, const gi_scene* scene, const f
 gi_status launch_phong(gi_context* ctx, const gi_vis_params* p, const float* d_pos, const float* d_nrm,
                        const float* d_vis, const float* d_color, float* d_out, int W, int H, cudaStream_t st);
 
+// The SMSR shaders' EDTSM outputs (NonConservativeSMSR.frag:367-397): the
+// hard-shadow image (shadow, depth, preEvaluatedShadow, 1) and the clip
+// position MVP * vertex, float4 each; background (0, 0, 0, 1).
+gi_status launch_edt_inputs(gi_context* ctx, const gi_vis_params* p, const float camera_mvp[16], const float* d_pos,
+                            const float* d_nrm, const float* d_vis, float* d_image, float* d_position, int W, int H,
+                            cudaStream_t st);
+
+// PBA exact distance transform with PBA's bands (m1, m2, m3).  Sites come
+// from d_sites (short2 per pixel, x != MARKER at a site) or, when d_sites is
+// NULL, from initializeInput's test on d_image; d_nearest (short2, may be
+// NULL) receives each pixel's site, d_out4 (may be NULL) the normalised EDT
+// shadow in channels 0-1 (needs d_image and d_position).
+gi_status pba_check_shape(int W, int H, int m1, int m2, int m3, const char* who);
+gi_status launch_pba(gi_context* ctx, const int16_t* d_sites, const float* d_image, const float* d_position,
+                     int W, int H, int m1, int m2, int m3, float penumbra, float intensity, int16_t* d_nearest,
+                     float* d_out4, cudaStream_t st);
+
 // Progressive best-candidate Poisson-disk sequence in the unit disk
 // (poisson_table.inc); the n-tap table is its first n points.
 extern const float kPoissonDisk[64][2];

@@ -1414,6 +1414,37 @@ __global__ void __launch_bounds__(128) k_phong(const gi_vis_params p, const floa
     out[i] = make_float4(o[0], o[1], o[2], o[3]);
 }
 
+// The EDTSM branch of the SMSR shaders (NonConservativeSMSR.frag:367-397,
+// ConservativeSMSR.frag:215-245): FragData[0] = (shadow, depth,
+// preEvaluatedShadow, 1) with depth = position.z / position.w * 0.5 + 0.5,
+// FragData[1] = position = MVP * vertex; discarded background pixels keep the
+// clear colour (0, 0, 0, 1) in both.  shadow is the visibility target.
+__global__ void __launch_bounds__(128) k_edt_inputs(const gi_vis_params p, const dev::Mat4 mvp,
+                                                    const float4* __restrict__ pos, const float4* __restrict__ nrm,
+                                                    const float* __restrict__ vis, float4* __restrict__ image,
+                                                    float4* __restrict__ position, int W, int H) {
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int y = blockIdx.y * 4 + (threadIdx.x >> 5);
+    if (x >= W || y >= H) return;
+    const size_t i = (size_t)y * W + x;
+    const float4 pv = pos[i];
+    if (pv.x == 0.0f) {
+        image[i] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+        position[i] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+        return;
+    }
+    const float4 nv = nrm[i];
+    Ctx c{};
+    c.I = p.shadow_intensity;
+    const V4 vertex{pv.x, pv.y, pv.z, pv.w};
+    const float pre = pretest(p, c, vertex, V4{nv.x, nv.y, nv.z, nv.w});
+    const V4 cp = mat4_mul(mvp.m, vertex);
+    float depth = cp.z / cp.w;
+    depth = depth * 0.5f + 0.5f;
+    image[i] = make_float4(vis[i], depth, pre, 1.0f);
+    position[i] = make_float4(cp.x, cp.y, cp.z, cp.w);
+}
+
 }  // namespace vis
 
 gi_status launch_surrogate_features(gi_context* ctx, const gi_vis_params* p, const float* d_depth, int map_w,
@@ -1448,6 +1479,21 @@ gi_status launch_surrogate_finish(gi_context* ctx, const gi_vis_params* p, const
     ctx->launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "surrogate finish launch");
+}
+
+gi_status launch_edt_inputs(gi_context* ctx, const gi_vis_params* p, const float camera_mvp[16], const float* d_pos,
+                            const float* d_nrm, const float* d_vis, float* d_image, float* d_position, int W, int H,
+                            cudaStream_t st) {
+    dim3 grid((W + 31) / 32, (H + 3) / 4);
+    dev::Mat4 m;
+    for (int k = 0; k < 16; ++k) m.m[k] = camera_mvp[k];
+    vis::k_edt_inputs<<<grid, 128, 0, st>>>(*p, m, reinterpret_cast<const float4*>(d_pos),
+                                            reinterpret_cast<const float4*>(d_nrm), d_vis,
+                                            reinterpret_cast<float4*>(d_image), reinterpret_cast<float4*>(d_position),
+                                            W, H);
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "EDT inputs launch");
 }
 
 gi_status launch_phong(gi_context* ctx, const gi_vis_params* p, const float* d_pos, const float* d_nrm,

@@ -436,6 +436,62 @@ def phong_shade(ctx: Context, params: ShadowParams, frame: Frame, pos, nrm, vis,
     return out
 
 
+def _need(t, numel: int, dtype, what: str) -> None:
+    if not t.is_cuda or t.dtype != dtype or not t.is_contiguous() or t.numel() < numel:
+        raise ValueError(f"{what}: need a contiguous CUDA {dtype} tensor of >= {numel} elements")
+
+
+def pba_voronoi(ctx: Context, sites, nearest, bands=(16, 16, 16), stream=None):
+    """pba2DVoronoiDiagram: nearest site of every pixel (int16 [H, W, 2] in and out).
+
+    A site is any pixel whose x is not GI_PBA_MARKER; bands are PBA's
+    (phase1Band, phase2Band, phase3Band), (16, 16, 16) in the reference.
+    """
+    import torch
+
+    H, W = sites.shape[0], sites.shape[1]
+    _need(sites, 2 * W * H, torch.int16, "sites")
+    _need(nearest, 2 * W * H, torch.int16, "nearest")
+    check(_lib().gi_pba_voronoi(ctx.handle, _ptr(sites), W, H, int(bands[0]), int(bands[1]), int(bands[2]),
+                                _ptr(nearest), _stream_ptr(stream)), "gi_pba_voronoi")
+    return nearest
+
+
+def edt_inputs(ctx: Context, params: ShadowParams, frame: Frame, pos, nrm, vis, width: int, height: int, image,
+               position, stream=None):
+    """The SMSR shaders' EDTSM outputs: hard-shadow image and clip position (float4 each)."""
+    import torch
+
+    for t, n, what in ((pos, 4, "pos"), (nrm, 4, "nrm"), (vis, 1, "vis"), (image, 4, "image"),
+                       (position, 4, "position")):
+        _need(t, n * width * height, torch.float32, what)
+    p = params.to_c(frame)
+    check(_lib().gi_edt_inputs(ctx.handle, C.byref(p), _f16(frame.camera_mvp), _ptr(pos), _ptr(nrm), _ptr(vis),
+                               width, height, _ptr(image), _ptr(position), _stream_ptr(stream)), "gi_edt_inputs")
+    return image, position
+
+
+def edt_soft_shadows(ctx: Context, image, position, out, penumbra_size: float = 1.0, shadow_intensity: float = 0.25,
+                     bands=(16, 16, 16), nearest=None, stream=None):
+    """filterHardShadowsUsingEDT's CUDA part: sites, PBA, normalisation into out (float4, channels 0-1).
+
+    penumbra_size is shadowParams.penumbraSize; like the reference, the
+    kernels get penumbra_size / 5.
+    """
+    import torch
+
+    H, W = image.shape[0], image.shape[1]
+    for t, what in ((image, "image"), (position, "position"), (out, "out")):
+        _need(t, 4 * W * H, torch.float32, what)
+    if nearest is not None:
+        _need(nearest, 2 * W * H, torch.int16, "nearest")
+    check(_lib().gi_edt_soft_shadows(ctx.handle, _ptr(image), _ptr(position), W, H, int(bands[0]), int(bands[1]),
+                                     int(bands[2]), float(penumbra_size / 5.0), float(shadow_intensity), _ptr(out),
+                                     _ptr(nearest) if nearest is not None else None, _stream_ptr(stream)),
+          "gi_edt_soft_shadows")
+    return out
+
+
 def area_light_samples(light: ViewSpec, size: float, n_side: int = 17) -> list:
     """The reference's uniform point-light samples of an area light (n_side^2 views)."""
     n = n_side * n_side

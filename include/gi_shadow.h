@@ -349,6 +349,54 @@ gi_status gi_render_frame(gi_context* ctx, const gi_scene* scene,
  * the unit disk, interleaved x,y).  Shared with the CPU oracle. */
 gi_status gi_poisson_table(int n, float* xy_out);
 
+/* ---- EDT-filtered hard shadows (ShadowMapping's EDTSM mode) -------------
+ *
+ * filterHardShadowsUsingEDT (ShadowMapping/src/main.cpp:416-447) runs the
+ * reference's only CUDA code: an exact Euclidean distance transform by the
+ * parallel banding algorithm (PBA; src/EDT/pba2DHost.cu, include/EDT/
+ * pba2DKernel.h) over sites found in the hard-shadow image, then a
+ * normalisation that turns each pixel's distance to its nearest site into a
+ * penumbra value.  The reference reaches its images through CUDA-GL interop;
+ * here they are plain device buffers.  Results equal the reference's kernels
+ * bit for bit for the same bands, equidistant sites included. */
+
+/* MARKER of pba2D.h:60: the x (and y) of a pixel that is not a site. */
+#define GI_PBA_MARKER (-32768)
+
+/* pba2DInitializeInput(short*) + pba2DCompute(m1, m2, m3)
+ * (pba2DHost.cu:97-101, 208-221; pba2DVoronoiDiagram(16, 16, 16) in the
+ * reference): d_sites holds int16 (x, y) per pixel, a site being any pixel
+ * whose x is not GI_PBA_MARKER; d_nearest receives the (x, y) of every
+ * pixel's nearest site (all (-1, 0) when there is none, as the reference's
+ * kernels produce).  width: a multiple of 8 up to 8192; height 2..8192;
+ * phase1_band divides height into bands of >= 2 rows; phase2_band is a power
+ * of two dividing width into bands of >= 2; phase3_band divides width. */
+gi_status gi_pba_voronoi(gi_context* ctx, const int16_t* d_sites, int width, int height, int phase1_band,
+                         int phase2_band, int phase3_band, int16_t* d_nearest, void* stream);
+
+/* The CUDA half of filterHardShadowsUsingEDT (main.cpp:419-422):
+ * initializeInput over d_image (float4 per pixel: shadow, depth,
+ * preEvaluatedShadow, 1 -- the HARD_SHADOW_COLOR texture), the PBA, and
+ * pbaNormalizeEDT(out, penumbra_size, shadow_intensity) with d_position
+ * (float4 per pixel, the POSITION_MAP_COLOR texture).  Channels 0 (the
+ * filtered shadow) and 1 (depth) of d_out (float4 per pixel) are written,
+ * channels 2-3 are left as they are.  The reference passes
+ * shadowParams.penumbraSize / 5.0 as penumbra_size.  d_nearest (int16 pairs,
+ * may be NULL) receives the nearest sites. */
+gi_status gi_edt_soft_shadows(gi_context* ctx, const float* d_image, const float* d_position, int width,
+                              int height, int phase1_band, int phase2_band, int phase3_band, float penumbra_size,
+                              float shadow_intensity, float* d_out, int16_t* d_nearest, void* stream);
+
+/* The images gi_edt_soft_shadows reads, as the SMSR shaders write them in
+ * EDTSM mode (NonConservativeSMSR.frag:367-397, ConservativeSMSR.frag:
+ * 215-245) from the G-buffer (d_pos, d_nrm float4) and the visibility of
+ * GI_TECH_SMSR_CONSERVATIVE / GI_TECH_SMSR_NONCONSERVATIVE (d_vis):
+ * d_image = (shadow, depth, preEvaluatedShadow, 1) and d_position = MVP *
+ * vertex with MVP = camera_mvp; background (0, 0, 0, 1) in both. */
+gi_status gi_edt_inputs(gi_context* ctx, const gi_vis_params* vis, const float camera_mvp[16],
+                        const float* d_pos, const float* d_nrm, const float* d_vis, int width, int height,
+                        float* d_image, float* d_position, void* stream);
+
 /* shadeScene / PhongShading.frag (ShadowMapping/src/main.cpp:449-457,
  * Shaders/GBuffer/PhongShading.frag:11-46): deferred Phong shading of the
  * G-buffer (float4 position / normal per pixel) with d_vis as the shadow

@@ -29,6 +29,11 @@ def load():
         lib.or_rbssm_hits.argtypes = [vp, i]
         lib.or_phong_shade.argtypes = [vp, vp, vp, vp, vp, i, i, vp]
         lib.or_area_light_visibility.argtypes = [vp, vp, i, vp, i, vp, vp, i, i, i, f, f, f, vp, f, i, i, vp, i]
+        lib.or_pba_voronoi.argtypes = [vp, i, i, i, i, i, vp, i]
+        lib.or_edt_sites.argtypes = [vp, i, i, vp]
+        lib.or_edt_normalize.argtypes = [vp, vp, vp, i, i, f, f, vp]
+        lib.or_edt_soft_shadows.argtypes = [vp, vp, i, i, i, i, i, f, f, vp, vp, vp, i]
+        lib.or_edt_inputs.argtypes = [vp, vp, vp, vp, vp, i, i, vp, vp]
         for fn in (lib.or_shadow_map, lib.or_gbuffer, lib.or_visibility, lib.or_shadow_volume_counts):
             fn.restype = None
         _lib = lib
@@ -117,3 +122,54 @@ def phong_shade(vis_params, pos, nrm, vis, width, height, color=None):
     load().or_phong_shade(C.byref(vis_params), ps.ctypes.data, ns.ctypes.data, vs.ctypes.data,
                           cs.ctypes.data if cs is not None else None, width, height, out.ctypes.data)
     return out
+
+
+PBA_MARKER = -32768
+
+
+def pba_voronoi(sites, m=(16, 16, 16), threads=0):
+    """sites: int16 [H, W, 2] ((x, y) at a site, MARKER elsewhere) -> nearest site [H, W, 2]."""
+    s = np.ascontiguousarray(sites, dtype=np.int16)
+    H, W = s.shape[:2]
+    out = np.zeros_like(s)
+    load().or_pba_voronoi(s.ctypes.data, W, H, m[0], m[1], m[2], out.ctypes.data, threads)
+    return out
+
+
+def edt_sites(image):
+    im = _f32(image)
+    H, W = im.shape[:2]
+    out = np.empty((H, W, 2), np.int16)
+    load().or_edt_sites(im.ctypes.data, W, H, out.ctypes.data)
+    return out
+
+
+def edt_normalize(nearest, image, position, penumbra, intensity, out4=None):
+    nn = np.ascontiguousarray(nearest, dtype=np.int16)
+    im, po = _f32(image), _f32(position)
+    H, W = im.shape[:2]
+    out = np.zeros((H, W, 4), np.float32) if out4 is None else out4
+    load().or_edt_normalize(nn.ctypes.data, im.ctypes.data, po.ctypes.data, W, H, penumbra, intensity,
+                            out.ctypes.data)
+    return out
+
+
+def edt_soft_shadows(image, position, penumbra, intensity, m=(16, 16, 16), threads=0):
+    """Returns (out4 [H, W, 4] with channels 0-1 written, sites, nearest)."""
+    im, po = _f32(image), _f32(position)
+    H, W = im.shape[:2]
+    out = np.zeros((H, W, 4), np.float32)
+    sites = np.empty((H, W, 2), np.int16)
+    nearest = np.empty((H, W, 2), np.int16)
+    load().or_edt_soft_shadows(im.ctypes.data, po.ctypes.data, W, H, m[0], m[1], m[2], penumbra, intensity,
+                               sites.ctypes.data, nearest.ctypes.data, out.ctypes.data, threads)
+    return out, sites, nearest
+
+
+def edt_inputs(vis_params, camera_mvp, pos, nrm, vis, width, height):
+    ps, ns, vs, cm = _f32(pos), _f32(nrm), _f32(vis), _f32(camera_mvp).reshape(16)
+    image = np.empty((height, width, 4), np.float32)
+    position = np.empty((height, width, 4), np.float32)
+    load().or_edt_inputs(C.addressof(vis_params), cm.ctypes.data, ps.ctypes.data, ns.ctypes.data, vs.ctypes.data,
+                         width, height, image.ctypes.data, position.ctypes.data)
+    return image, position

@@ -31,9 +31,11 @@
 // border depth 0 (ShadowMapping/src/Viewers/MyGLTextureViewer.cpp:3-28).
 #include "gi_oracle.h"
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -1679,5 +1681,422 @@ extern "C" void or_rbssm_hits(unsigned long long* out4096, int reset) {
     for (int i = 0; i < 4096; ++i) {
         if (out4096) out4096[i] = g_rb_hits[i].load();
         if (reset) g_rb_hits[i].store(0);
+    }
+}
+
+// ===========================================================================
+// EDT-filtered hard shadows (ShadowMapping's EDTSM mode) and the exact
+// Euclidean distance transform it runs: the parallel banding algorithm (PBA,
+// Cao et al. 2010) as ShadowMapping/src/EDT/pba2DHost.cu:121-242 sequences
+// the kernels of ShadowMapping/include/EDT/pba2DKernel.h.  Equidistant sites
+// are resolved by the algorithm's own comparisons (flood and merge order,
+// FP32 bisector intersections, the coloring walk of each group of m3
+// threads), so the restatement keeps every band, merge and group of the
+// reference; a site image is processed column by column (phase 1) and then
+// row by row (phases 2-3), which is what the reference's transposes do.
+// ===========================================================================
+namespace {
+namespace pba {
+
+constexpr int kMarker = -32768;  // MARKER, pba2D.h:60
+
+struct P {
+    int x, y;
+};
+
+// Phase 1 on one column (pba2DPhase1, pba2DHost.cu:121-143): in[y] is the
+// row of the site at (x, y) or kMarker; out[y] the row of the site chosen
+// for (x, y) or kMarker.  Sites carry their own row as their y.
+void column(const int* in, int H, int m1, int* out) {
+    const int B = H / m1;
+    std::vector<int> down(H), up(H), links(in, in + H);
+    // kernelFloodDown (pba2DKernel.h:112-130): last site at or above, per band
+    for (int b = 0; b < m1; ++b) {
+        int cur = kMarker;
+        for (int i = 0; i < B; ++i) {
+            const int y = b * B + i;
+            if (in[y] != kMarker) cur = in[y];
+            down[y] = cur;
+        }
+    }
+    // kernelFloodUp (:132-153): from the band's last row upwards, take this
+    // row's flood value only when strictly closer than the carried one
+    for (int b = 0; b < m1; ++b) {
+        const int ty = (b + 1) * B - 1;
+        int cur = kMarker;
+        for (int i = 0; i < B; ++i) {
+            const int y = ty - i;
+            if (std::abs(down[y] - y) < std::abs(cur - y)) cur = down[y];
+            up[y] = cur;
+        }
+    }
+    // kernelPropagateInterband (:155-198): a band's first row looks at the last
+    // row of the nearest non-empty band above, its last row at the first row
+    // of the nearest non-empty band below; strictly closer sites are written
+    // over the site input, which is where the next step reads them.
+    for (int b = 0; b < m1; ++b) {
+        int ty = b * B;
+        int mine = std::abs(up[ty] - ty);
+        for (int nb = b - 1; nb >= 0; --nb) {
+            const int v = up[nb * B + B - 1];
+            if (v != kMarker) {
+                if (std::abs(v - ty) < mine) links[ty] = v;
+                break;
+            }
+        }
+        ty = b * B + B - 1;
+        mine = std::abs(up[ty] - ty);
+        for (int nb = b + 1; nb < m1; ++nb) {
+            const int v = up[nb * B];
+            if (v != kMarker) {
+                if (std::abs(v - ty) < mine) links[ty] = v;
+                break;
+            }
+        }
+    }
+    // kernelUpdateVertical (:200-225): each row compares its band value with
+    // the band's first-row and last-row links, strictly closer wins
+    for (int b = 0; b < m1; ++b) {
+        const int ty = b * B;
+        const int top = links[ty], bottom = links[ty + B - 1];
+        for (int i = 0; i < B; ++i) {
+            const int y = ty + i;
+            int v = up[y], mine = std::abs(v - y);
+            int d = std::abs(top - y);
+            if (d < mine) {
+                mine = d;
+                v = top;
+            }
+            d = std::abs(bottom - y);
+            if (d < mine) v = bottom;
+            out[y] = v;
+        }
+    }
+}
+
+// interpoint (pba2DKernel.h:227-236): where the bisector of (x1, y1) and
+// (x2, y2) crosses the line x = x0; FP32, each operation rounded once.
+float interpoint(int x1, int y1, int x2, int y2, int x0) {
+    const float xM = float(x1 + x2) / 2.0f;
+    const float yM = float(y1 + y2) / 2.0f;
+    const float nx = float(x2 - x1);
+    const float ny = float(y2 - y1);
+    return yM + nx * (xM - float(x0)) / ny;
+}
+
+// One line of phases 2-3 (pba2DPhase2 / pba2DPhase3, pba2DHost.cu:145-190).
+// cand[p] is the row of column p's phase-1 site (kMarker for none), line
+// the row being colored; out_x / out_y receive the site of every pixel.
+// lk[] plays the reference's textures[0] line: (x, y) = stack value and back
+// pointer after the proximate-points pass, (forward, back) pointers after
+// the forward pointers are created.
+struct Line {
+    const int* cand;
+    int W, line;
+    std::vector<P> lk;
+
+    P col(int p) const {  // textures[0] after kernelDoubleToSingleList; zero outside
+        if (p < 0 || p >= W) return P{0, 0};
+        return P{cand[p], lk[p].y};
+    }
+
+    // kernelProximatePoints (pba2DKernel.h:238-268)
+    void proximate(int b0, int B) {
+        int lasty = -1;
+        P last1{0, -1}, last2{0, -1};
+        for (int p = b0; p < b0 + B; ++p) {
+            if (cand[p] == kMarker) continue;
+            while (last2.y >= 0) {
+                const float i1 = interpoint(last1.x, last2.y, last2.x, lasty, line);
+                const float i2 = interpoint(last2.x, lasty, cand[p], p, line);
+                if (i1 < i2) break;
+                lasty = last2.y;
+                last2 = last1;
+                if (last1.y >= 0) last1 = lk[last1.y];
+            }
+            last1 = last2;
+            last2 = P{cand[p], lasty};
+            lasty = p;
+            lk[p] = last2;
+        }
+        if (lasty != b0 + B - 1) lk[b0 + B - 1] = P{kMarker, lasty};
+    }
+
+    // kernelCreateForwardPointers (:270-296)
+    void forward(int b0, int B) {
+        const int ty = b0 + B - 1;
+        int lasty = -1;
+        P cur = lk[ty];
+        int nexty = cur.x == kMarker ? cur.y : ty;
+        int p = ty;
+        for (int i = 0; i < B; ++i, --p)
+            if (ty - i == nexty) {
+                cur = P{lasty, lk[p].y};
+                lk[p] = cur;
+                lasty = nexty;
+                nexty = cur.y;
+            }
+        if (lasty != ty - B + 1) lk[p + 1] = P{lasty, kMarker};
+    }
+
+    // kernelMergeBands (:298-435), bands band1 and band1 + 1 of size B
+    void merge(int band1, int B) {
+        const int band2 = band1 + 1;
+        int lasty = band2 * B - 1;
+        P last2{cand[lasty], lk[lasty].y}, last1{0, 0};
+        if (last2.x == kMarker) {
+            lasty = last2.y;
+            last2 = lasty >= 0 ? P{cand[lasty], lk[lasty].y} : P{kMarker, kMarker};
+        }
+        if (last2.y >= 0) last1 = P{cand[last2.y], lk[last2.y].y};
+        int firsty = band2 * B;
+        P cur{lk[firsty].x, cand[firsty]};
+        if (cur.y == kMarker) {
+            firsty = cur.x;
+            cur = firsty >= 0 ? P{lk[firsty].x, cand[firsty]} : P{kMarker, kMarker};
+        }
+        int top = 0;
+        while (top < 2 && cur.y >= 0) {
+            while (last2.y >= 0) {
+                const float i1 = interpoint(last1.x, last2.y, last2.x, lasty, line);
+                const float i2 = interpoint(last2.x, lasty, cur.y, firsty, line);
+                if (i1 < i2) break;
+                lasty = last2.y;
+                last2 = last1;
+                --top;
+                if (last1.y >= 0) last1 = P{cand[last1.y], lk[last1.y].y};
+            }
+            lk[firsty] = P{cur.x, lasty};
+            if (lasty >= 0) lk[lasty] = P{firsty, last2.y};
+            last1 = last2;
+            last2 = P{cur.y, lasty};
+            lasty = firsty;
+            firsty = cur.x;
+            top = std::max(1, top + 1);
+            cur = firsty >= 0 ? P{lk[firsty].x, cand[firsty]} : P{kMarker, kMarker};
+        }
+        // head and tail pointers of the merged band
+        firsty = band1 * B;
+        lasty = band2 * B;
+        cur = lk[firsty];
+        if (cur.y == kMarker && cur.x < 0) {
+            const P l = lk[lasty];
+            cur.x = l.y == kMarker ? l.x : lasty;
+            lk[firsty] = cur;
+        }
+        firsty = band1 * B + B - 1;
+        lasty = band2 * B + B - 1;
+        cur = lk[lasty];
+        if (cur.x == kMarker && cur.y < 0) {
+            const P l = lk[firsty];
+            cur.y = l.x == kMarker ? l.y : firsty;
+            lk[lasty] = cur;
+        }
+    }
+
+    // kernelColor (:437-497): groups of m3 pixels from the line's end; each
+    // pixel walks the list from the state the group's last pixel left after
+    // the previous group, moving on while the squared distance does not grow.
+    void color(int m3, int16_t* out_xy) {
+        struct S {
+            P last1, last2;
+            int lasty;
+        } s;
+        s.lasty = W - 1;
+        s.last2 = col(s.lasty);
+        if (s.last2.x == kMarker) {
+            s.lasty = s.last2.y;
+            s.last2 = col(s.lasty);
+        }
+        s.last1 = P{0, 0};
+        if (s.last2.y >= 0) s.last1 = col(s.last2.y);
+        for (int g0 = W - 1; g0 >= 0; g0 -= m3) {
+            S next = s;
+            for (int t = 0; t < m3; ++t) {
+                const int ty = g0 - t;
+                S w = s;
+                int dx = w.last2.x - line, dy = w.lasty - ty;
+                uint32_t best = (uint32_t)((int64_t)dx * dx + (int64_t)dy * dy);
+                while (w.last2.y >= 0) {
+                    dx = w.last1.x - line;
+                    dy = w.last2.y - ty;
+                    const uint32_t dist = (uint32_t)((int64_t)dx * dx + (int64_t)dy * dy);
+                    if (dist > best) break;
+                    best = dist;
+                    w.lasty = w.last2.y;
+                    w.last2 = w.last1;
+                    if (w.last2.y >= 0) w.last1 = col(w.last2.y);
+                }
+                out_xy[2 * ty] = (int16_t)w.lasty;      // the final transpose swaps
+                out_xy[2 * ty + 1] = (int16_t)w.last2.x;  // (row, column) back
+                if (t == m3 - 1) next = w;
+            }
+            s = next;
+        }
+    }
+};
+
+bool shape_ok(int W, int H, int m1, int m2, int m3) {
+    return W > 0 && H > 0 && W <= 32767 && H <= 32767 && m1 > 0 && H % m1 == 0 && m2 > 0 && W % m2 == 0 &&
+           (m2 & (m2 - 1)) == 0 && m3 > 0 && W % m3 == 0;
+}
+
+// pba2DCompute on a site mask (site[y * W + x] != 0): nearest site per
+// pixel as (x, y) pairs.
+void voronoi(const uint8_t* site, int W, int H, int m1, int m2, int m3, int16_t* out, int threads) {
+    std::vector<int> cols((size_t)W * H);  // [x][y]
+#pragma omp parallel for schedule(static) num_threads(nthreads(threads))
+    for (int x = 0; x < W; ++x) {
+        std::vector<int> in(H);
+        for (int y = 0; y < H; ++y) in[y] = site[(size_t)y * W + x] ? y : kMarker;
+        column(in.data(), H, m1, &cols[(size_t)x * H]);
+    }
+#pragma omp parallel for schedule(static) num_threads(nthreads(threads))
+    for (int y = 0; y < H; ++y) {
+        std::vector<int> cand(W);
+        for (int x = 0; x < W; ++x) cand[x] = cols[(size_t)x * H + y];
+        Line L{cand.data(), W, y, std::vector<P>(W, P{0, 0})};
+        const int B2 = W / m2;
+        for (int b = 0; b < m2; ++b) L.proximate(b * B2, B2);
+        for (int b = 0; b < m2; ++b) L.forward(b * B2, B2);
+        for (int nb = m2; nb > 1; nb /= 2)
+            for (int b = 0; b < nb; b += 2) L.merge(b, W / nb);
+        L.color(m3, out + (size_t)2 * y * W);
+    }
+}
+
+// linearize (pba2DKernel.h:499-506): n = 1, f = 1000; 2.0 * n is a double,
+// so the division is a double one rounded to float.
+float linearize(float depth) {
+    const float n = 1.0f, f = 1000.0f;
+    return (float)((2.0 * n) / (f + n - depth * (f - n)));
+}
+
+// initializeInput (pba2DKernel.h:509-528): (x, y) is a site when one of its
+// 3 x 3 neighbours p in the image has p.x != x's, |linearize(depth)
+// difference| <= 0.0025 and p.z == 1.
+bool is_site(const float* img, int W, int H, int px, int py) {
+    const float* c = img + 4 * ((size_t)py * W + px);
+    for (int x = -1; x <= 1; ++x)
+        for (int y = -1; y <= 1; ++y)
+            if (px + x >= 0 && px + x < W && py + y >= 0 && py + y < H) {
+                const float* p = img + 4 * ((size_t)(py + y) * W + (px + x));
+                if (p[0] != c[0] && std::fabs(linearize(c[1]) - linearize(p[1])) <= 0.0025 && p[2] == 1.0f)
+                    return true;
+            }
+    return false;
+}
+
+// tex2D with point sampling and clamp addressing at integer coordinates
+const float* texel(const float* img, int W, int H, int x, int y) {
+    x = x < 0 ? 0 : (x >= W ? W - 1 : x);
+    y = y < 0 ? 0 : (y >= H ? H - 1 : y);
+    return img + 4 * ((size_t)y * W + x);
+}
+
+float plerp(float v0, float v1, float t) { return (1 - t) * v0 + t * v1; }
+
+}  // namespace pba
+}  // namespace
+
+extern "C" void or_pba_voronoi(const int16_t* sites, int W, int H, int m1, int m2, int m3, int16_t* out,
+                               int threads) {
+    if (!pba::shape_ok(W, H, m1, m2, m3)) return;
+    std::vector<uint8_t> site((size_t)W * H);
+    for (size_t i = 0; i < site.size(); ++i) site[i] = sites[2 * i] != pba::kMarker;
+    pba::voronoi(site.data(), W, H, m1, m2, m3, out, threads);
+}
+
+extern "C" void or_edt_sites(const float* image, int W, int H, int16_t* sites) {
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const bool s = pba::is_site(image, W, H, x, y);
+            sites[2 * ((size_t)y * W + x)] = (int16_t)(s ? x : pba::kMarker);
+            sites[2 * ((size_t)y * W + x) + 1] = (int16_t)(s ? y : pba::kMarker);
+        }
+}
+
+// pbaNormalizeDistanceTransform (pba2DKernel.h:541-569): distance between
+// the pixel's and its nearest site's positions; outside the penumbra (site
+// not lit-facing, depths apart, or farther than penumbra / 2) the hard value
+// stays, otherwise plerp(0.5 -/+ distance / penumbra, 1, intensity) for
+// umbra / lit pixels.  Channels 0 and 1 of out4 are written.
+extern "C" void or_edt_normalize(const int16_t* nearest, const float* image, const float* position, int W, int H,
+                                 float penumbra, float intensity, float* out4) {
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const size_t q = (size_t)y * W + x;
+            const int sx = nearest[2 * q], sy = nearest[2 * q + 1];
+            const float* ip = image + 4 * q;
+            const float* sp = pba::texel(image, W, H, sx, sy);
+            const float* p1 = position + 4 * q;
+            const float* p2 = pba::texel(position, W, H, sx, sy);
+            const float dist = std::sqrt((p1[0] - p2[0]) * (p1[0] - p2[0]) + (p1[1] - p2[1]) * (p1[1] - p2[1]) +
+                                         (p1[2] - p2[2]) * (p1[2] - p2[2]));
+            float r;
+            if (sp[2] != 1.0f || std::fabs(pba::linearize(sp[1]) - pba::linearize(ip[1])) > 0.0005 ||
+                dist > penumbra / 2)
+                r = ip[0];
+            else if (ip[0] == intensity)
+                r = pba::plerp((float)(0.5 - dist / penumbra), 1.0f, intensity);
+            else
+                r = pba::plerp((float)(0.5 + dist / penumbra), 1.0f, intensity);
+            out4[4 * q] = r;
+            out4[4 * q + 1] = ip[1];
+        }
+}
+
+// initializeInput + pba2DCompute(m1, m2, m3) + pbaNormalizeDistanceTransform
+// (filterHardShadowsUsingEDT's CUDA part, ShadowMapping/src/main.cpp:
+// 416-422).  sites / nearest may be NULL.
+extern "C" void or_edt_soft_shadows(const float* image, const float* position, int W, int H, int m1, int m2,
+                                    int m3, float penumbra, float intensity, int16_t* sites, int16_t* nearest,
+                                    float* out4, int threads) {
+    if (!pba::shape_ok(W, H, m1, m2, m3)) return;
+    std::vector<int16_t> s((size_t)2 * W * H), nn((size_t)2 * W * H);
+    or_edt_sites(image, W, H, s.data());
+    or_pba_voronoi(s.data(), W, H, m1, m2, m3, nn.data(), threads);
+    or_edt_normalize(nn.data(), image, position, W, H, penumbra, intensity, out4);
+    if (sites) std::memcpy(sites, s.data(), s.size() * sizeof(int16_t));
+    if (nearest) std::memcpy(nearest, nn.data(), nn.size() * sizeof(int16_t));
+}
+
+// The EDTSM output of the SMSR shaders (NonConservativeSMSR.frag:367-397,
+// ConservativeSMSR.frag:215-245): image (shadow, depth, preEvaluatedShadow,
+// 1) and position = MVP * vertex, with depth = position.z / position.w * 0.5
+// + 0.5; background pixels keep the clear colour (0, 0, 0, 1) in both.
+extern "C" void or_edt_inputs(const gi_vis_params* p, const float camera_mvp[16], const float* pos, const float* nrm,
+                              const float* vis, int W, int H, float* image, float* position) {
+    Ctx c;
+    c.p = p;
+    c.map = nullptr;
+    c.W = c.H = 0;
+    c.sx = c.sy = 0.0f;
+    c.I = p->shadow_intensity;
+    for (size_t q = 0; q < (size_t)W * H; ++q) {
+        const float* v = pos + 4 * q;
+        float* im = image + 4 * q;
+        float* po = position + 4 * q;
+        if (v[0] == 0.0f) {
+            im[0] = im[1] = im[2] = 0.0f;
+            im[3] = 1.0f;
+            po[0] = po[1] = po[2] = 0.0f;
+            po[3] = 1.0f;
+            continue;
+        }
+        const V4 vertex{v[0], v[1], v[2], v[3]};
+        const V4 normal{nrm[4 * q], nrm[4 * q + 1], nrm[4 * q + 2], nrm[4 * q + 3]};
+        const float pre = pretest(c, vertex, normal);
+        const V4 cp = mat4_mul(camera_mvp, vertex);
+        float depth = cp.z / cp.w;
+        depth = depth * 0.5f + 0.5f;
+        im[0] = vis[q];
+        im[1] = depth;
+        im[2] = pre;
+        im[3] = 1.0f;
+        po[0] = cp.x;
+        po[1] = cp.y;
+        po[2] = cp.z;
+        po[3] = cp.w;
     }
 }

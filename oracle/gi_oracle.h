@@ -69,6 +69,28 @@ void or_area_light_visibility(const float* points, const float* normals, int nv,
                               float factor, float units, const float camera_mvp[16], float I,
                               int W, int H, float* out, int threads);
 
+/* PBA exact distance transform (ShadowMapping/src/EDT/pba2DHost.cu:228-242
+ * with the kernels of include/EDT/pba2DKernel.h): sites / out are (x, y)
+ * int16 pairs per pixel, a site holding anything but x == -32768; out gets
+ * the nearest site of each pixel, equidistant sites resolved as the
+ * reference's bands (m1, m2, m3) resolve them. */
+void or_pba_voronoi(const int16_t* sites, int W, int H, int m1, int m2, int m3, int16_t* out, int threads);
+
+/* EDTSM (ShadowMapping/src/main.cpp:416-422): site detection over the
+ * hard-shadow image (float4 shadow, depth, preEvaluatedShadow, 1), PBA, and
+ * the normalisation with the position image (float4); out4 channels 0-1.
+ * or_edt_sites / or_edt_normalize are its first and last steps. */
+void or_edt_sites(const float* image, int W, int H, int16_t* sites);
+void or_edt_normalize(const int16_t* nearest, const float* image, const float* position, int W, int H,
+                      float penumbra, float intensity, float* out4);
+void or_edt_soft_shadows(const float* image, const float* position, int W, int H, int m1, int m2, int m3,
+                         float penumbra, float intensity, int16_t* sites, int16_t* nearest, float* out4,
+                         int threads);
+
+/* The SMSR shaders' EDTSM outputs from the G-buffer and visibility. */
+void or_edt_inputs(const gi_vis_params* p, const float camera_mvp[16], const float* pos, const float* nrm,
+                   const float* vis, int W, int H, float* image, float* position);
+
 /* Hit counts of the return sites of the RBSSM smoothONDS restatement,
  * indexed by source line modulo 4096 (test coverage only). */
 void or_rbssm_hits(unsigned long long* out4096, int reset);
