@@ -33,6 +33,12 @@ Extra legs in the same line (not the headline):
   area_light_ground_truth  the reference's Monte-Carlo area light (17 x 17
               point-light maps) for the 1080p frame, and the error of
               PCSS and of the surrogate against it
+  edt_soft_shadows  ShadowMapping's EDTSM mode at its 1024 x 1024 window:
+              the PBA exact distance transform over the sites of the
+              SMSR hard-shadow image plus the penumbra normalisation
+              (gi_edt_soft_shadows: one column-pass and one row-pass
+              kernel, L2 flushed before each call), the whole EDTSM frame
+              (SMSR frame, EDTSM inputs, EDT), and the CPU oracle's EDT
   surrogate   the learned PCSS surrogate (BF16 U-Net on the tcgen05
               convolution kernels) trained here on freshly rendered
               frames, then its 1080p frame time, its error against the
@@ -77,13 +83,15 @@ def parse_args():
     ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate leg")
     ap.add_argument("--no-heavy", action="store_true", help="skip the heavy 2160p leg")
     ap.add_argument("--no-area-light", action="store_true", help="skip the 289-sample area-light ground-truth leg")
+    ap.add_argument("--no-edt", action="store_true", help="skip the EDT-filtered hard shadows leg")
     ap.add_argument("--surrogate-frames", type=int, default=8000,
                     help="training frames (one 256^2 crop each, batch 16) for the surrogate leg")
     ap.add_argument("--profile", action="store_true",
                     help="render --warmup frames and exit (the command profiled with ncu)")
-    ap.add_argument("--profile-case", choices=["frame", "conv", "volumes"], default="frame",
+    ap.add_argument("--profile-case", choices=["frame", "conv", "volumes", "edt"], default="frame",
                     help="with --profile: the pcss_1080p frame, three U-Net convolutions at 1080p (d0a, d1a, "
-                         "d2a), or the heavy scene's shadow volumes of one light at 960x540")
+                         "d2a), the heavy scene's shadow volumes of one light at 960x540, or three EDTSM "
+                         "filters of the 1024^2 frame")
     return ap.parse_args()
 
 
@@ -511,6 +519,110 @@ def run_area_light(args, ctx, stream, local, w, fr, bufs, net=None):
     return out
 
 
+def edt_workload(local):
+    """ShadowMapping's EDTSM frame: the 1080p scene seen through the reference's
+    1024 x 1024 window with a 2048^2 map, non-conservative SMSR hard shadows."""
+    import globalillumination_gb300 as gi
+    from globalillumination_gb300 import _capi as api, scenes
+
+    w = scenes.pcss_1080p(width=1024, height=1024, map_size=2048)
+    fr = gi.frame_setup(w.light, w.camera)
+    p = gi.ShadowParams.defaults(api.GI_TECH_SMSR_NONCONSERVATIVE)
+    return w, fr, p
+
+
+def edt_frame_setup(ctx, local, stream):
+    import torch
+
+    import globalillumination_gb300 as gi
+
+    w, fr, p = edt_workload(local)
+    S, W, H = w.map_params.width, w.camera.width, w.camera.height
+    w.scene.upload(ctx, stream)
+    bufs = gi.allocate_frame(S, S, W, H, local)
+    image = torch.empty((H, W, 4), device="cuda")
+    position = torch.empty((H, W, 4), device="cuda")
+    out = torch.zeros((H, W, 4), device="cuda")
+
+    def hard():
+        gi.render_frame(ctx, w.scene, fr, w.map_params, p, W, H, bufs, stream, store_gbuffer=True)
+        gi.edt_inputs(ctx, p, fr, bufs.pos, bufs.nrm, bufs.vis, W, H, image, position, stream)
+
+    def edt():
+        gi.edt_soft_shadows(ctx, image, position, out, 1.0, p.shadow_intensity, (16, 16, 16), stream=stream)
+
+    return w, fr, p, bufs, image, position, out, hard, edt
+
+
+def run_edt(args, ctx, stream, local, flush):
+    """EDTSM at 1024^2: the EDT call alone, the whole EDTSM frame, the CPU oracle's EDT."""
+    import numpy as np
+    import torch
+
+    import globalillumination_gb300 as gi
+    import oracle
+
+    w, fr, p, bufs, image, position, out, hard, edt = edt_frame_setup(ctx, local, stream)
+    W, H = w.camera.width, w.camera.height
+    P = W * H
+    hard()
+    for _ in range(5):
+        edt()
+    torch.cuda.synchronize()
+
+    def timed(fn, reps):
+        ms = []
+        for r in range(reps):
+            flush.fill_(float(r))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            ms.append((e0, e1))
+        torch.cuda.synchronize()
+        return statistics.median(a.elapsed_time(b) for a, b in ms)
+
+    gi.pba_chain_rows(ctx, reset=True)
+    edt_ms = timed(edt, 100)
+    chain_rows = gi.pba_chain_rows(ctx, reset=True) / 100.0
+
+    def frame():
+        hard()
+        edt()
+
+    frame_ms = timed(frame, 50)
+    hard_ms = timed(hard, 50)
+    sites = int(((image[..., 2] == 1.0).sum()).item())  # lit-facing pixels (site candidates)
+    soft = float(((out[..., 0] != image[..., 0]) & (image[..., 0] > 0)).float().mean())
+    # algorithmic bytes per pixel: column pass reads the image (16 B) and
+    # writes a row index (2 B); row pass reads it (2 B) and writes the nearest
+    # site (4 B); normalisation reads the site (4 B), the pixel's image and
+    # position (32 B) and writes channels 0-1 (8 B)
+    alg = 68 * P
+    peak, peak_kind = measured_hbm_peak()
+    achieved = alg / (edt_ms / 1000.0) / 1e9
+    img_h, pos_h = image.cpu().numpy(), position.cpu().numpy()
+    t0 = time.perf_counter()
+    reps = 0
+    while reps < 3 and (reps == 0 or time.perf_counter() - t0 < 10.0):
+        oracle.edt_soft_shadows(img_h, pos_h, np.float32(1.0 / 5.0), p.shadow_intensity)
+        reps += 1
+    cpu_ms = (time.perf_counter() - t0) * 1000.0 / reps
+    return {
+        "workload": "ShadowMapping EDTSM window 1024x1024 (pcss_1080p scene, 2048^2 map, non-conservative SMSR), "
+                    "pba2DVoronoiDiagram(16, 16, 16) + pbaNormalizeEDT(penumbraSize 1 / 5, intensity 0.25)",
+        "edt_ms": edt_ms, "edt_per_s": 1000.0 / edt_ms,
+        "edtsm_frame_ms": frame_ms, "smsr_frame_and_inputs_ms": hard_ms,
+        "roofline": {"kernels": "k_pba_columns<kFromImage> + k_pba_rows + k_edt_normalize", "bound": "hbm",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "algorithmic_bytes_per_call": alg},
+        "lit_facing_pixels": sites, "filtered_pixel_fraction": soft,
+        "rows_colored_by_exact_chain_per_call": chain_rows,
+        "cpu_oracle_edt_ms": cpu_ms, "cpu_oracle_threads": os.cpu_count(),
+        "gpu_vs_cpu_oracle": cpu_ms / edt_ms,
+    }
+
+
 def measured_bf16_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -525,6 +637,17 @@ def run_profile_case(args, local):
 
     import globalillumination_gb300 as gi
 
+    if args.profile_case == "edt":
+        ctx = gi.Context(local)
+        stream = torch.cuda.current_stream()
+        _, _, _, _, _, _, out, hard, edt = edt_frame_setup(ctx, local, stream)
+        hard()
+        for _ in range(3):
+            edt()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "edt", "checksum": float(out[..., 0].sum())}), flush=True)
+        ctx.close()
+        return 0
     if args.profile_case == "conv":
         from globalillumination_gb300 import surrogate as sg, tc_ops
 
@@ -727,6 +850,9 @@ def run_ours(args):
     area = None
     if not args.no_area_light and rank == 0:
         area = run_area_light(args, ctx, stream, local, w, fr, bufs, net)
+    edt_leg = None
+    if not args.no_edt and rank == 0:
+        edt_leg = run_edt(args, ctx, stream, local, flush)
     heavy = None
     if not args.no_heavy and rank == 0:
         heavy = run_heavy(args, ctx, stream, local, net)
@@ -769,6 +895,8 @@ def run_ours(args):
             line["heavy"] = heavy
         if area is not None:
             line["area_light_ground_truth"] = area
+        if edt_leg is not None:
+            line["edt_soft_shadows"] = edt_leg
         if clk and any(r in clk["reasons"] for r in THROTTLE_BAD):
             line["clocks_warning"] = "throttled during the timed region"
         if world == 1 and not args.no_cpu_baseline:

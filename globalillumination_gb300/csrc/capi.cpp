@@ -115,6 +115,7 @@ extern "C" void gi_context_destroy(gi_context* c) {
     cudaFree(c->d_area_maps);
     cudaFree(c->d_area_acc);
     cudaFree(c->d_pba_cols);
+    cudaFree(c->d_pba_near);
     for (int i = 0; i < 8; ++i) cudaFree(c->bin_buf[i]);
     for (int k = 0; k < 2; ++k)
         for (int i = 0; i < 8; ++i) cudaFree(c->tier_buf[k][i]);
@@ -632,6 +633,16 @@ extern "C" gi_status gi_edt_soft_shadows(gi_context* ctx, const float* d_image, 
     if (st != GI_OK) return st;
     return gi::launch_pba(ctx, nullptr, d_image, d_position, W, H, m1, m2, m3, penumbra, intensity, d_nearest,
                           d_out, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" gi_status gi_pba_chain_rows(gi_context* ctx, uint32_t* rows, int reset) {
+    if (!ctx || !rows) return fail(GI_ERR_INVALID_ARG, "gi_pba_chain_rows: NULL argument");
+    gi_status st = check_device(ctx);
+    if (st != GI_OK) return st;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(rows, ctx->d_status + 96, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && reset) e = cudaMemset(ctx->d_status + 96, 0, sizeof(uint32_t));
+    return e == cudaSuccess ? GI_OK : gi::fail_cuda(e, "gi_pba_chain_rows");
 }
 
 extern "C" gi_status gi_edt_inputs(gi_context* ctx, const gi_vis_params* vp, const float camera_mvp[16],

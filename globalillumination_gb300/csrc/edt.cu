@@ -25,11 +25,13 @@
 //   k_pba_rows     phases 2-3, one image row per warp, in shared memory: the
 //                  per-band proximate-point stacks and forward links (one
 //                  lane per band), the pairwise band merges level by level
-//                  (one lane per pair), then the coloring: lane 0 walks the
-//                  chain of states that the reference's groups of m3 threads
-//                  hand to each other, and every lane colors its pixels from
-//                  its group's state.  The epilogue writes the nearest-site
-//                  map and / or the normalised EDT shadow.
+//                  (one lane per pair), then the coloring.  A row whose list
+//                  is a strict lower envelope is colored by a binary search
+//                  over its exact crossing points, which gives every pixel
+//                  the site the reference's group walks reach; other rows
+//                  replay the groups' chain of states.  Writes each pixel's
+//                  nearest site.
+//   k_edt_normalize  the penumbra normalisation, one thread per pixel.
 //
 // Compiled like every pass with -fmad=false and IEEE division / square root,
 // so each FP32 operation rounds once in the order written (the CPU oracle
@@ -54,7 +56,6 @@ constexpr int kMaxSegRows = 64;          // one 64-bit site mask per thread
 constexpr int kRowThreads = 256;         // 8 rows per CTA in the row pass
 
 enum : int { kFromSites = 0, kFromImage = 1 };
-enum : int { kOutNearest = 1, kOutNormalized = 2 };
 
 // linearize (pba2DKernel.h:499-506) with n = 1, f = 1000: 2.0 * n is a
 // double, so the reference divides in double and rounds to float.  For a
@@ -216,96 +217,147 @@ __global__ void __launch_bounds__(kColThreads) k_pba_columns(const ColArgs a) {
 struct RowArgs {
     const int16_t* cols;
     int W, H, m2, m3, wpb, per_warp;  // per_warp: shared bytes per row
-    int out;                          // kOutNearest | kOutNormalized
     short2* nearest;                  // (site x, site y) per pixel
-    const float4* image;              // kOutNormalized inputs
-    const float4* position;
-    float* out4;                      // channels 0-1 written
-    float penumbra, intensity, thr;   // thr: the largest float <= 0.0005
+    unsigned* status;                 // [0] += rows colored by the exact chain
 };
 
-// One row's state: cand[p] = row of column p's phase-1 site (the reference's
-// transposed texture), lk[p] = its textures[0] line (stack value and back
-// pointer, later forward and back pointers), st[k] = the list position the
-// coloring of group k starts from.
+// One row's state in shared memory.  cand[p] = row of column p's phase-1
+// site (the reference's transposed texture); lk[p] = its textures[0] line
+// (stack value and back pointer, later forward and back pointers); alive[p]
+// = p is on the list; ic[p] = interpoint(predecessor, p) of a stack entry
+// (phase 2), then site[p] = x of pixel p's site and ex[i] = i-th list
+// position (coloring); st[k] = the list position group k starts from.
+struct RowLayout {
+    int cand, lk, ic, site, ex, alive, st, bytes;
+};
+
+__host__ __device__ __forceinline__ int up16(int b) { return (b + 15) & ~15; }
+
+__host__ __device__ __forceinline__ RowLayout row_layout(int W, int m3) {
+    RowLayout l;
+    l.cand = 0;
+    l.lk = up16(2 * W);
+    l.ic = l.lk + 4 * W;
+    l.site = l.ic;  // over ic once phase 2 is done
+    l.ex = l.ic + up16(2 * W);
+    l.alive = l.ic + 4 * W;
+    l.st = l.alive + up16(W);
+    l.bytes = l.st + up16(4 * (W / m3));
+    return l;
+}
+
 struct Row {
     int16_t* cand;
     short2* lk;
+    uint8_t* alive;
+    float* ic;
+    int16_t* site;
+    int16_t* ex;
     int* st;
     int W, line;
+
+    __device__ __forceinline__ int C(int p) const { return cand[p]; }
+    __device__ __forceinline__ short2& L(int p) const { return lk[p]; }
+    __device__ __forceinline__ float& I(int p) const { return ic[p]; }
+    __device__ __forceinline__ uint8_t& A(int p) const { return alive[p]; }
+    __device__ __forceinline__ int16_t& S(int p) const { return site[p]; }
+    __device__ __forceinline__ int16_t& E(int i) const { return ex[i]; }
 
     // textures[0] after kernelDoubleToSingleList; tex1Dfetch reads zero
     // outside the texture
     __device__ __forceinline__ short2 col(int p) const {
         if (p < 0 || p >= W) return make_short2(0, 0);
-        return make_short2(cand[p], lk[p].y);
+        return make_short2((short)C(p), L(p).y);
     }
 };
 
-// interpoint (pba2DKernel.h:227-236)
+// interpoint (pba2DKernel.h:227-236).  A zero numerator (two sites in one
+// row, or the bisector's midpoint on the line) gives yM + (+-0) = yM, as yM
+// >= 0.5 here (y1 < y2 are list positions); answering it directly keeps the
+// division's special-case path out of the common case.
 __device__ __forceinline__ float interpoint(int x1, int y1, int x2, int y2, int x0) {
     const float xM = (float)(x1 + x2) / 2.0f;
     const float yM = (float)(y1 + y2) / 2.0f;
+    if (x1 == x2 || x1 + x2 == 2 * x0) return yM;
     const float nx = (float)(x2 - x1);
     const float ny = (float)(y2 - y1);
     return yM + nx * (xM - (float)x0) / ny;
 }
 
-// kernelProximatePoints (pba2DKernel.h:238-268) for the band [b0, b0 + B)
+// kernelProximatePoints (pba2DKernel.h:238-268) for the band [b0, b0 + B).
+// The reference's i1 = interpoint(last1, last2) is the intersection of the
+// top entry with the entry below it, fixed since the top was pushed, so it
+// is computed once, at the push, and read back from ic[] (same operands,
+// same float).  The nested push / pop loops run as one loop of single steps
+// -- a test that pops, or a push -- so the lanes of a warp, each on its own
+// band, do not wait for one another's pops.
 __device__ void proximate(const Row& r, int b0, int B) {
-    int lasty = -1;
+    const int end = b0 + B;
+    int lasty = -1, p = b0 - 1, g = 0;
     short2 last1 = make_short2(0, -1), last2 = make_short2(0, -1);
-    for (int p = b0; p < b0 + B; ++p) {
-        const int g = r.cand[p];
-        if (g == kMarker) continue;
-        while (last2.y >= 0) {
-            const float i1 = interpoint(last1.x, last2.y, last2.x, lasty, r.line);
+    bool placing = false;
+    for (;;) {
+        if (!placing) {
+            do {
+                ++p;
+            } while (p < end && r.C(p) == kMarker);
+            if (p >= end) break;
+            g = r.C(p);
+            placing = true;
+        }
+        if (lasty >= 0) {
             const float i2 = interpoint(last2.x, lasty, g, p, r.line);
-            if (i1 < i2) break;
-            lasty = last2.y;
-            last2 = last1;
-            if (last1.y >= 0) last1 = r.lk[last1.y];
+            if (last2.y >= 0 && !(r.I(lasty) < i2)) {  // pop the top
+                r.A(lasty) = 0;
+                lasty = last2.y;
+                last2 = last1;
+                if (last1.y >= 0) last1 = r.L(last1.y);
+                continue;
+            }
+            r.I(p) = i2;
         }
         last1 = last2;
         last2 = make_short2((short)g, (short)lasty);
         lasty = p;
-        r.lk[p] = last2;
+        r.L(p) = last2;
+        r.A(p) = 1;
+        placing = false;
     }
-    if (lasty != b0 + B - 1) r.lk[b0 + B - 1] = make_short2((short)kMarker, (short)lasty);
+    if (lasty != end - 1) r.L(end - 1) = make_short2((short)kMarker, (short)lasty);
 }
 
 // kernelCreateForwardPointers (:270-296)
 __device__ void forward(const Row& r, int b0, int B) {
     const int ty = b0 + B - 1;
     int lasty = -1;
-    short2 cur = r.lk[ty];
+    short2 cur = r.L(ty);
     int nexty = cur.x == kMarker ? cur.y : ty;
     int p = ty;
     for (int i = 0; i < B; ++i, --p)
         if (ty - i == nexty) {
-            cur = make_short2((short)lasty, r.lk[p].y);
-            r.lk[p] = cur;
+            cur = make_short2((short)lasty, r.L(p).y);
+            r.L(p) = cur;
             lasty = nexty;
             nexty = cur.y;
         }
-    if (lasty != ty - B + 1) r.lk[p + 1] = make_short2((short)lasty, (short)kMarker);
+    if (lasty != ty - B + 1) r.L(p + 1) = make_short2((short)lasty, (short)kMarker);
 }
 
 // kernelMergeBands (:298-435) for bands band1 and band1 + 1 of size B
 __device__ void merge(const Row& r, int band1, int B) {
     const int band2 = band1 + 1;
     int lasty = band2 * B - 1;
-    short2 last2 = make_short2(r.cand[lasty], r.lk[lasty].y), last1 = make_short2(0, 0);
+    short2 last2 = make_short2(r.C(lasty), r.L(lasty).y), last1 = make_short2(0, 0);
     if (last2.x == kMarker) {
         lasty = last2.y;
-        last2 = lasty >= 0 ? make_short2(r.cand[lasty], r.lk[lasty].y) : make_short2(kMarker, kMarker);
+        last2 = lasty >= 0 ? make_short2(r.C(lasty), r.L(lasty).y) : make_short2(kMarker, kMarker);
     }
-    if (last2.y >= 0) last1 = make_short2(r.cand[last2.y], r.lk[last2.y].y);
+    if (last2.y >= 0) last1 = make_short2(r.C(last2.y), r.L(last2.y).y);
     int firsty = band2 * B;
-    short2 cur = make_short2(r.lk[firsty].x, r.cand[firsty]);
+    short2 cur = make_short2(r.L(firsty).x, r.C(firsty));
     if (cur.y == kMarker) {
         firsty = cur.x;
-        cur = firsty >= 0 ? make_short2(r.lk[firsty].x, r.cand[firsty]) : make_short2(kMarker, kMarker);
+        cur = firsty >= 0 ? make_short2(r.L(firsty).x, r.C(firsty)) : make_short2(kMarker, kMarker);
     }
     int top = 0;
     while (top < 2 && cur.y >= 0) {
@@ -313,36 +365,37 @@ __device__ void merge(const Row& r, int band1, int B) {
             const float i1 = interpoint(last1.x, last2.y, last2.x, lasty, r.line);
             const float i2 = interpoint(last2.x, lasty, cur.y, firsty, r.line);
             if (i1 < i2) break;
+            r.A(lasty) = 0;
             lasty = last2.y;
             last2 = last1;
             --top;
-            if (last1.y >= 0) last1 = make_short2(r.cand[last1.y], r.lk[last1.y].y);
+            if (last1.y >= 0) last1 = make_short2(r.C(last1.y), r.L(last1.y).y);
         }
-        r.lk[firsty] = make_short2(cur.x, (short)lasty);
-        if (lasty >= 0) r.lk[lasty] = make_short2((short)firsty, last2.y);
+        r.L(firsty) = make_short2(cur.x, (short)lasty);
+        if (lasty >= 0) r.L(lasty) = make_short2((short)firsty, last2.y);
         last1 = last2;
         last2 = make_short2(cur.y, (short)lasty);
         lasty = firsty;
         firsty = cur.x;
         top = max(1, top + 1);
-        cur = firsty >= 0 ? make_short2(r.lk[firsty].x, r.cand[firsty]) : make_short2(kMarker, kMarker);
+        cur = firsty >= 0 ? make_short2(r.L(firsty).x, r.C(firsty)) : make_short2(kMarker, kMarker);
     }
     // head and tail pointers of the merged band
     firsty = band1 * B;
     lasty = band2 * B;
-    cur = r.lk[firsty];
+    cur = r.L(firsty);
     if (cur.y == kMarker && cur.x < 0) {
-        const short2 l = r.lk[lasty];
+        const short2 l = r.L(lasty);
         cur.x = l.y == kMarker ? l.x : (short)lasty;
-        r.lk[firsty] = cur;
+        r.L(firsty) = cur;
     }
     firsty = band1 * B + B - 1;
     lasty = band2 * B + B - 1;
-    cur = r.lk[lasty];
+    cur = r.L(lasty);
     if (cur.x == kMarker && cur.y < 0) {
-        const short2 l = r.lk[firsty];
+        const short2 l = r.L(firsty);
         cur.y = l.x == kMarker ? l.y : (short)firsty;
-        r.lk[lasty] = cur;
+        r.L(lasty) = cur;
     }
 }
 
@@ -367,73 +420,164 @@ __device__ __forceinline__ int walk(const Row& r, int lasty, int ty) {
     return lasty;
 }
 
+// 2 x (x_b - x_a) c, where c is the position at which list entries a < b
+// (positions) are equally far: entry a is at least as near as b for pixel
+// p exactly when 2 (x_b - x_a) p <= num(a, b).
+__device__ __forceinline__ long long crossing_num(const Row& r, int xa, int xb) {
+    const long long ha = r.C(xa) - r.line, hb = r.C(xb) - r.line;
+    return (long long)xb * xb - (long long)xa * xa + hb * hb - ha * ha;
+}
+
+// Coloring (kernelColor).  The reference's groups of m3 pixels each start
+// from the state the previous group's last pixel reached.  When the list's
+// exact crossing points increase strictly, the squared distances along the
+// list fall and then rise for every pixel, with at most two equal minima
+// next to each other, so every walk that starts on the tail side of the
+// minimum -- as each group's does -- stops at the head-most nearest entry:
+// a binary search over the crossing points finds it.  Rows whose list
+// breaks that order (entries kept by the FP32 bisector tests that are
+// nowhere strictly nearest) replay the groups' chain of states exactly.
+__device__ void color(const Row& r, int m3, int lane, unsigned* status) {
+    const int W = r.W;
+    // list entries in position order (the list's order)
+    int n = 0;
+    for (int c0 = 0; c0 < W; c0 += 32) {
+        const bool on = c0 + lane < W && r.A(c0 + lane) != 0;
+        const unsigned m = __ballot_sync(kFull, on);
+        if (on) r.E(n + __popc(m & ((1u << lane) - 1))) = (int16_t)(c0 + lane);
+        n += __popc(m);
+    }
+    __syncwarp();
+    bool ordered = true;
+    for (int i = lane; i + 2 < n; i += 32) {
+        const int x0 = r.E(i), x1 = r.E(i + 1), x2 = r.E(i + 2);
+        // num01 / (2 (x1 - x0)) < num12 / (2 (x2 - x1))
+        if (!(crossing_num(r, x0, x1) * (x2 - x1) < crossing_num(r, x1, x2) * (x1 - x0))) ordered = false;
+    }
+    ordered = __all_sync(kFull, ordered);
+    if (n == 0) {
+        // no site on the row (only when the image has none): the reference
+        // reads its list head outside the texture and colors every pixel
+        // with (x, y) = (-1, 0)
+        for (int p = lane; p < W; p += 32) r.S(p) = -1;
+    } else if (ordered) {
+        const int chunk = (W + 31) / 32;
+        const int p0 = lane * chunk, p1 = min(p0 + chunk, W);
+        // first entry i with 2 (x_{i+1} - x_i) p0 <= num(i, i+1)
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            const int xa = r.E(mid), xb = r.E(mid + 1);
+            if (2ll * (xb - xa) * p0 <= crossing_num(r, xa, xb))
+                hi = mid;
+            else
+                lo = mid + 1;
+        }
+        int i = lo;
+        for (int p = p0; p < p1; ++p) {
+            while (i < n - 1) {
+                const int xa = r.E(i), xb = r.E(i + 1);
+                if (2ll * (xb - xa) * p <= crossing_num(r, xa, xb)) break;
+                ++i;
+            }
+            r.S(p) = r.E(i);
+        }
+    } else {
+        if (lane == 0) {
+            atomicAdd(status, 1u);
+            int lasty = W - 1;
+            const short2 tail = r.col(lasty);
+            if (tail.x == kMarker) lasty = tail.y;
+            for (int k = 0; k < W / m3; ++k) {
+                r.st[k] = lasty;
+                lasty = walk(r, lasty, W - (k + 1) * m3);
+            }
+        }
+        __syncwarp();
+        for (int p = lane; p < W; p += 32) r.S(p) = (int16_t)walk(r, r.st[(W - 1 - p) / m3], p);
+    }
+    __syncwarp();
+}
+
 __device__ __forceinline__ float plerp1(float v0, float t) { return (1.0f - t) * v0 + t * 1.0f; }
 
-template <int kOut>
 __global__ void __launch_bounds__(kRowThreads) k_pba_rows(const RowArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int line = blockIdx.x * a.wpb + warp;
     if (line >= a.H) return;  // whole warps only; the kernel has no block barrier
+    const int W = a.W;
     unsigned char* base = smem + (size_t)warp * a.per_warp;
+    const RowLayout lay = row_layout(W, a.m3);
     Row r;
-    r.W = a.W;
+    r.W = W;
     r.line = line;
-    r.cand = reinterpret_cast<int16_t*>(base);
-    r.lk = reinterpret_cast<short2*>(base + (size_t)a.W * 2);
-    r.st = reinterpret_cast<int*>(base + (size_t)a.W * 6);
-    const uint4* src = reinterpret_cast<const uint4*>(a.cols + (size_t)line * a.W);
-    for (int i = lane; i < a.W / 8; i += 32) reinterpret_cast<uint4*>(r.cand)[i] = src[i];
+    r.cand = reinterpret_cast<int16_t*>(base + lay.cand);
+    r.lk = reinterpret_cast<short2*>(base + lay.lk);
+    r.ic = reinterpret_cast<float*>(base + lay.ic);
+    r.site = reinterpret_cast<int16_t*>(base + lay.site);
+    r.ex = reinterpret_cast<int16_t*>(base + lay.ex);
+    r.alive = base + lay.alive;
+    r.st = reinterpret_cast<int*>(base + lay.st);
+    const uint4* src = reinterpret_cast<const uint4*>(a.cols + (size_t)line * W);
+    for (int i = lane; i < W / 8; i += 32) reinterpret_cast<uint4*>(r.cand)[i] = src[i];
+    for (int i = lane; i < (lay.st - lay.alive) / 4; i += 32) reinterpret_cast<unsigned*>(r.alive)[i] = 0u;
     __syncwarp();
     // pba2DPhase2: band stacks and links, then the merges
-    const int B2 = a.W / a.m2;
+    const int B2 = W / a.m2;
     for (int b = lane; b < a.m2; b += 32) {
         proximate(r, b * B2, B2);
         forward(r, b * B2, B2);
     }
     __syncwarp();
     for (int nb = a.m2; nb > 1; nb /= 2) {
-        const int B = a.W / nb;
+        const int B = W / nb;
         for (int pr = lane; pr < nb / 2; pr += 32) merge(r, 2 * pr, B);
         __syncwarp();
     }
-    // pba2DPhase3: group k covers pixels W-1-k*m3 down to W-(k+1)*m3 and
-    // starts from the state its predecessor's last pixel reached
-    const int G = a.W / a.m3;
-    if (lane == 0) {
-        int lasty = a.W - 1;
-        const short2 tail = r.col(lasty);
-        if (tail.x == kMarker) lasty = tail.y;
-        for (int k = 0; k < G; ++k) {
-            r.st[k] = lasty;
-            lasty = walk(r, lasty, a.W - (k + 1) * a.m3);
-        }
+    // pba2DPhase3
+    color(r, a.m3, lane, a.status);
+    const size_t row = (size_t)line * W;
+    for (int p = lane; p < W; p += 32) {
+        const int sx = r.S(p);
+        a.nearest[row + p] = make_short2((short)sx, (short)r.col(sx).x);
     }
-    __syncwarp();
-    for (int p = lane; p < a.W; p += 32) {
-        const int sx = walk(r, r.st[(a.W - 1 - p) / a.m3], p);
-        const int sy = r.col(sx).x;
-        const size_t q = (size_t)line * a.W + p;
-        if (kOut & kOutNearest) a.nearest[q] = make_short2((short)sx, (short)sy);
-        if (kOut & kOutNormalized) {
-            // pbaNormalizeDistanceTransform (pba2DKernel.h:541-569); tex2D
-            // clamps the site's coordinates
-            const int cx = min(max(sx, 0), a.W - 1), cy = min(max(sy, 0), a.H - 1);
-            const size_t qs = (size_t)cy * a.W + cx;
-            const float4 ip = __ldg(a.image + q), sp = __ldg(a.image + qs);
-            const float4 p1 = __ldg(a.position + q), p2 = __ldg(a.position + qs);
-            const float dx = p1.x - p2.x, dy = p1.y - p2.y, dz = p1.z - p2.z;
-            const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
-            float v;
-            if (sp.z != 1.0f || fabsf(linearize(sp.y) - linearize(ip.y)) > a.thr || dist > a.penumbra / 2.0f)
-                v = ip.x;
-            else if (ip.x == a.intensity)
-                v = plerp1(0.5f - dist / a.penumbra, a.intensity);
-            else
-                v = plerp1(0.5f + dist / a.penumbra, a.intensity);
-            *reinterpret_cast<float2*>(a.out4 + 4 * q) = make_float2(v, ip.y);
-        }
-    }
+}
+
+struct NormArgs {
+    const short2* nearest;
+    const float4* image;
+    const float4* position;
+    float* out4;
+    int W, H;
+    float penumbra, intensity, thr;  // thr: the largest float <= 0.0005
+};
+
+// pbaNormalizeDistanceTransform (pba2DKernel.h:541-569), one thread per
+// pixel: the distance between the pixel's and its site's positions; outside
+// the penumbra (site not lit-facing, depths apart, farther than penumbra / 2)
+// the hard value stays, otherwise plerp(0.5 -/+ distance / penumbra, 1,
+// intensity) for umbra / lit pixels.  tex2D clamps the site's coordinates.
+__global__ void __launch_bounds__(256) k_edt_normalize(const NormArgs a) {
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= a.W || y >= a.H) return;
+    const size_t q = (size_t)y * a.W + x;
+    const short2 n = a.nearest[q];
+    const int cx = min(max((int)n.x, 0), a.W - 1), cy = min(max((int)n.y, 0), a.H - 1);
+    const size_t qs = (size_t)cy * a.W + cx;
+    const float4 ip = __ldg(a.image + q), sp = __ldg(a.image + qs);
+    const float4 p1 = __ldg(a.position + q), p2 = __ldg(a.position + qs);
+    const float dx = p1.x - p2.x, dy = p1.y - p2.y, dz = p1.z - p2.z;
+    const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
+    float v;
+    if (sp.z != 1.0f || fabsf(linearize(sp.y) - linearize(ip.y)) > a.thr || dist > a.penumbra / 2.0f)
+        v = ip.x;
+    else if (ip.x == a.intensity)
+        v = plerp1(0.5f - dist / a.penumbra, a.intensity);
+    else
+        v = plerp1(0.5f + dist / a.penumbra, a.intensity);
+    *reinterpret_cast<float2*>(a.out4 + 4 * q) = make_float2(v, ip.y);
 }
 
 // largest float not above c
@@ -489,44 +633,46 @@ gi_status launch_pba(gi_context* ctx, const int16_t* d_sites, const float* d_ima
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail_cuda(e, "pba columns launch");
 
+    short2* near = reinterpret_cast<short2*>(d_nearest);
+    if (!near) {
+        s = ensure_buffer(reinterpret_cast<void**>(&ctx->d_pba_near), &ctx->cap_pba_near,
+                          (size_t)W * H * sizeof(short2));
+        if (s != GI_OK) return s;
+        near = reinterpret_cast<short2*>(ctx->d_pba_near);
+    }
     RowArgs ra;
     ra.cols = ctx->d_pba_cols;
     ra.W = W;
     ra.H = H;
     ra.m2 = m2;
     ra.m3 = m3;
-    ra.per_warp = (W * 6 + (W / m3) * 4 + 15) / 16 * 16;
-    ra.wpb = max(1, min(kRowThreads / 32, (200 * 1024) / ra.per_warp));
-    ra.out = (d_nearest ? kOutNearest : 0) | (d_out4 ? kOutNormalized : 0);
-    ra.nearest = reinterpret_cast<short2*>(d_nearest);
-    ra.image = reinterpret_cast<const float4*>(d_image);
-    ra.position = reinterpret_cast<const float4*>(d_position);
-    ra.out4 = d_out4;
-    ra.penumbra = penumbra;
-    ra.intensity = intensity;
-    ra.thr = float_at_most(0.0005);
+    ra.per_warp = row_layout(W, m3).bytes;
+    // two rows per CTA spread the rows over every SM
+    ra.wpb = max(1, min(2, (200 * 1024) / ra.per_warp));
+    ra.nearest = near;
+    ra.status = ctx->d_status + 96;
     const int smem = ra.per_warp * ra.wpb;
-    const dim3 rgrid((H + ra.wpb - 1) / ra.wpb);
-    switch (ra.out) {
-        case kOutNearest:
-            s = set_smem(k_pba_rows<kOutNearest>, smem);
-            if (s == GI_OK) k_pba_rows<kOutNearest><<<rgrid, ra.wpb * 32, smem, st>>>(ra);
-            break;
-        case kOutNormalized:
-            s = set_smem(k_pba_rows<kOutNormalized>, smem);
-            if (s == GI_OK) k_pba_rows<kOutNormalized><<<rgrid, ra.wpb * 32, smem, st>>>(ra);
-            break;
-        case kOutNearest | kOutNormalized:
-            s = set_smem(k_pba_rows<kOutNearest | kOutNormalized>, smem);
-            if (s == GI_OK) k_pba_rows<kOutNearest | kOutNormalized><<<rgrid, ra.wpb * 32, smem, st>>>(ra);
-            break;
-        default:
-            return fail(GI_ERR_INVALID_ARG, "pba: no output requested");
-    }
+    s = set_smem(k_pba_rows, smem);
     if (s != GI_OK) return s;
+    k_pba_rows<<<dim3((H + ra.wpb - 1) / ra.wpb), ra.wpb * 32, smem, st>>>(ra);
     ctx->launches++;
     e = cudaGetLastError();
-    return e == cudaSuccess ? GI_OK : fail_cuda(e, "pba rows launch");
+    if (e != cudaSuccess) return fail_cuda(e, "pba rows launch");
+    if (!d_out4) return GI_OK;
+    NormArgs na;
+    na.nearest = near;
+    na.image = reinterpret_cast<const float4*>(d_image);
+    na.position = reinterpret_cast<const float4*>(d_position);
+    na.out4 = d_out4;
+    na.W = W;
+    na.H = H;
+    na.penumbra = penumbra;
+    na.intensity = intensity;
+    na.thr = float_at_most(0.0005);
+    k_edt_normalize<<<dim3((W + 31) / 32, (H + 7) / 8), 256, 0, st>>>(na);
+    ctx->launches++;
+    e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "EDT normalise launch");
 }
 
 }  // namespace gi

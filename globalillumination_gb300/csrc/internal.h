@@ -92,7 +92,8 @@ struct gi_context {
     // status words (128): [4..11] counters of the binned raster (records,
     // big records, spills, error bits, admitted big pairs as u64, work
     // items), [32..55] counters of the tiered light-map pass, [64..87] of
-    // the tiered camera-key pass (the two passes may run concurrently)
+    // the tiered camera-key pass (the two passes may run concurrently),
+    // [96] rows of the PBA row pass colored by the exact group chain
     unsigned int* d_status = nullptr;
     unsigned int* h_status = nullptr;  // pinned mirror
     // area-light ground truth: a wave of sample light maps, per-pixel sums
@@ -103,6 +104,9 @@ struct gi_context {
     // PBA distance transform: phase-1 site row per pixel (int16)
     int16_t* d_pba_cols = nullptr;
     size_t cap_pba_cols = 0;
+    // nearest site per pixel (short2) when the caller does not keep it
+    void* d_pba_near = nullptr;
+    size_t cap_pba_near = 0;
     // second stream for the camera-key pass of gi_render_frame, and the
     // fork / join events (cudaStream_t / cudaEvent_t)
     void* aux_stream = nullptr;

@@ -457,6 +457,13 @@ def pba_voronoi(ctx: Context, sites, nearest, bands=(16, 16, 16), stream=None):
     return nearest
 
 
+def pba_chain_rows(ctx: Context, reset: bool = False) -> int:
+    """Rows colored by replaying the reference's group chain (lists that are not strict envelopes)."""
+    n = C.c_uint32(0)
+    check(_lib().gi_pba_chain_rows(ctx.handle, C.byref(n), 1 if reset else 0), "gi_pba_chain_rows")
+    return int(n.value)
+
+
 def edt_inputs(ctx: Context, params: ShadowParams, frame: Frame, pos, nrm, vis, width: int, height: int, image,
                position, stream=None):
     """The SMSR shaders' EDTSM outputs: hard-shadow image and clip position (float4 each)."""

@@ -387,6 +387,14 @@ gi_status gi_edt_soft_shadows(gi_context* ctx, const float* d_image, const float
                               int height, int phase1_band, int phase2_band, int phase3_band, float penumbra_size,
                               float shadow_intensity, float* d_out, int16_t* d_nearest, void* stream);
 
+/* Rows (summed over calls since the last reset) whose site list was not a
+ * strict lower envelope -- the FP32 bisector tests of the reference kept an
+ * entry that is nowhere strictly nearest -- and were therefore colored by
+ * replaying the reference's chain of group states; every other row is
+ * colored by a binary search that gives the same sites.  Synchronises the
+ * context's device. */
+gi_status gi_pba_chain_rows(gi_context* ctx, uint32_t* rows, int reset);
+
 /* The images gi_edt_soft_shadows reads, as the SMSR shaders write them in
  * EDTSM mode (NonConservativeSMSR.frag:367-397, ConservativeSMSR.frag:
  * 215-245) from the G-buffer (d_pos, d_nrm float4) and the visibility of

@@ -24,6 +24,11 @@ PBA_CASES = [
     ("single_64", 64, 64, "single", 0, 9, (16, 16, 16)),
     ("pair_tie_64", 64, 64, "pair", 0, 10, (16, 16, 16)),
     ("empty_64", 64, 64, "empty", 0, 11, (16, 16, 16)),
+    # three sites whose bisectors cross row 0 at one point (35 1/3): the FP32
+    # intersections of the reference keep the middle one, so row 0's list is
+    # not a strict envelope and is colored by the exact group chain
+    ("degenerate_a_64", 64, 64, "points", ((0, 11), (3, 18), (9, 26)), 13, (16, 16, 16)),
+    ("degenerate_b_64", 64, 64, "points", ((0, 12), (3, 16), (12, 22)), 14, (16, 16, 16)),
     ("full_64", 64, 64, "full", 0, 12, (16, 16, 16)),
 ]
 
@@ -62,6 +67,9 @@ def site_mask(kind: str, W: int, H: int, param, seed: int) -> np.ndarray:
     elif kind == "pair":  # two sites symmetric about the centre
         cy, cx, d = H // 2, W // 2, 9
         m[cy - d, cx] = m[cy + d, cx] = m[cy, cx - d] = m[cy, cx + d] = True
+    elif kind == "points":
+        for x, y in param:
+            m[y, x] = True
     elif kind == "full":
         m[:] = True
     elif kind != "empty":

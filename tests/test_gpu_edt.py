@@ -54,6 +54,19 @@ def test_pba_matches_reference_golden(cuda_ctx, golden, case):
     np.testing.assert_array_equal(_pba(cuda_ctx, sites, bands), golden[f"pba/{case}/nearest"])
 
 
+def test_degenerate_lists_take_the_exact_chain(cuda_ctx, golden):
+    # rows whose list is not a strict envelope are colored by replaying the
+    # reference's group chain; the others by a binary search -- both exact
+    gi.pba_chain_rows(cuda_ctx, reset=True)
+    for case in ("degenerate_a_64", "degenerate_b_64"):
+        sites, bands = pba_case(case)
+        np.testing.assert_array_equal(_pba(cuda_ctx, sites, bands), golden[f"pba/{case}/nearest"])
+    assert gi.pba_chain_rows(cuda_ctx) >= 2
+    sites, bands = pba_case("random_sparse_64")
+    _pba(cuda_ctx, sites, bands)
+    assert gi.pba_chain_rows(cuda_ctx, reset=True) < 64 + 2
+
+
 @pytest.mark.parametrize("case", [c[0] for c in EDT_CASES])
 def test_edtsm_matches_reference_golden(cuda_ctx, golden, case):
     name, W, H, seed, pen, inten, bands = next(c for c in EDT_CASES if c[0] == case)
