@@ -228,7 +228,7 @@ struct RowArgs {
 // (phase 2), then site[p] = x of pixel p's site and ex[i] = i-th list
 // position (coloring); st[k] = the list position group k starts from.
 struct RowLayout {
-    int cand, lk, ic, site, ex, alive, st, bytes;
+    int cand, lk, ic, site, ex, alive, st, cm, bytes;
 };
 
 __host__ __device__ __forceinline__ int up16(int b) { return (b + 15) & ~15; }
@@ -242,7 +242,8 @@ __host__ __device__ __forceinline__ RowLayout row_layout(int W, int m3) {
     l.ex = l.ic + up16(2 * W);
     l.alive = l.ic + 4 * W;
     l.st = l.alive + up16(W);
-    l.bytes = l.st + up16(4 * (W / m3));
+    l.cm = l.st + up16(4 * (W / m3));
+    l.bytes = l.cm + up16(4 * ((W + 31) / 32));
     return l;
 }
 
@@ -254,6 +255,7 @@ struct Row {
     int16_t* site;
     int16_t* ex;
     int* st;
+    unsigned* cm;  // bit p & 31 of word p >> 5: column p has a site
     int W, line;
 
     __device__ __forceinline__ int C(int p) const { return cand[p]; }
@@ -284,44 +286,58 @@ __device__ __forceinline__ float interpoint(int x1, int y1, int x2, int y2, int 
     return yM + nx * (xM - (float)x0) / ny;
 }
 
+// Next position after p (before end) whose column has a site, from the
+// row's candidate bit words.
+__device__ __forceinline__ int next_cand(const unsigned* cm, int p, int end) {
+    int q = p + 1;
+    while (q < end) {
+        const unsigned w = cm[q >> 5] >> (q & 31);
+        if (w) {
+            q += __ffs(w) - 1;
+            return q < end ? q : end;
+        }
+        q = (q | 31) + 1;
+    }
+    return end;
+}
+
 // kernelProximatePoints (pba2DKernel.h:238-268) for the band [b0, b0 + B).
 // The reference's i1 = interpoint(last1, last2) is the intersection of the
 // top entry with the entry below it, fixed since the top was pushed, so it
 // is computed once, at the push, and read back from ic[] (same operands,
 // same float).  The nested push / pop loops run as one loop of single steps
-// -- a test that pops, or a push -- so the lanes of a warp, each on its own
-// band, do not wait for one another's pops.
+// -- a test that pops, or a push -- whose updates are selects, so the 16
+// lanes of a warp, each on its own band, stay converged.
 __device__ void proximate(const Row& r, int b0, int B) {
     const int end = b0 + B;
-    int lasty = -1, p = b0 - 1, g = 0;
+    int lasty = -1;
     short2 last1 = make_short2(0, -1), last2 = make_short2(0, -1);
-    bool placing = false;
-    for (;;) {
-        if (!placing) {
-            do {
-                ++p;
-            } while (p < end && r.C(p) == kMarker);
-            if (p >= end) break;
-            g = r.C(p);
-            placing = true;
-        }
+    int p = next_cand(r.cm, b0 - 1, end);
+    int g = p < end ? r.C(p) : 0;
+    while (p < end) {
+        float i2 = 0.0f;
+        bool pop = false;
         if (lasty >= 0) {
-            const float i2 = interpoint(last2.x, lasty, g, p, r.line);
-            if (last2.y >= 0 && !(r.I(lasty) < i2)) {  // pop the top
-                r.A(lasty) = 0;
-                lasty = last2.y;
-                last2 = last1;
-                if (last1.y >= 0) last1 = r.L(last1.y);
-                continue;
-            }
-            r.I(p) = i2;
+            i2 = interpoint(last2.x, lasty, g, p, r.line);
+            pop = last2.y >= 0 && !(r.I(lasty) < i2);
         }
-        last1 = last2;
-        last2 = make_short2((short)g, (short)lasty);
-        lasty = p;
-        r.L(p) = last2;
-        r.A(p) = 1;
-        placing = false;
+        const short2 below = r.L(last1.y >= 0 ? last1.y : 0);  // used only by a pop
+        if (pop) {
+            r.A(lasty) = 0;
+        } else {
+            if (lasty >= 0) r.I(p) = i2;
+            r.L(p) = make_short2((short)g, (short)lasty);
+            r.A(p) = 1;
+        }
+        const short2 n1 = pop ? (last1.y >= 0 ? below : last1) : last2;
+        const short2 n2 = pop ? last1 : make_short2((short)g, (short)lasty);
+        lasty = pop ? last2.y : p;
+        last1 = n1;
+        last2 = n2;
+        if (!pop) {
+            p = next_cand(r.cm, p, end);
+            if (p < end) g = r.C(p);
+        }
     }
     if (lasty != end - 1) r.L(end - 1) = make_short2((short)kMarker, (short)lasty);
 }
@@ -519,9 +535,15 @@ __global__ void __launch_bounds__(kRowThreads) k_pba_rows(const RowArgs a) {
     r.ex = reinterpret_cast<int16_t*>(base + lay.ex);
     r.alive = base + lay.alive;
     r.st = reinterpret_cast<int*>(base + lay.st);
+    r.cm = reinterpret_cast<unsigned*>(base + lay.cm);
     const uint4* src = reinterpret_cast<const uint4*>(a.cols + (size_t)line * W);
     for (int i = lane; i < W / 8; i += 32) reinterpret_cast<uint4*>(r.cand)[i] = src[i];
     for (int i = lane; i < (lay.st - lay.alive) / 4; i += 32) reinterpret_cast<unsigned*>(r.alive)[i] = 0u;
+    __syncwarp();
+    for (int c0 = 0; c0 < W; c0 += 32) {
+        const unsigned m = __ballot_sync(kFull, c0 + lane < W && r.C(c0 + lane) != kMarker);
+        if (lane == 0) r.cm[c0 >> 5] = m;
+    }
     __syncwarp();
     // pba2DPhase2: band stacks and links, then the merges
     const int B2 = W / a.m2;
