@@ -39,6 +39,11 @@ Extra legs in the same line (not the headline):
               (gi_edt_soft_shadows: one column-pass and one row-pass
               kernel, L2 flushed before each call), the whole EDTSM frame
               (SMSR frame, EDTSM inputs, EDT), and the CPU oracle's EDT
+  moment_shadows  ShadowMapping's filtered moment maps (VSM, ESM, EVSM,
+              MSM) at its 1024 x 1024 window over a 2048^2 map: whole
+              frames per technique (light map, moment map, box level,
+              two blur passes, G-buffer, lookups) beside the hard-shadow
+              frame, L2 flushed before each
   surrogate   the learned PCSS surrogate (BF16 U-Net on the tcgen05
               convolution kernels) trained here on freshly rendered
               frames, then its 1080p frame time, its error against the
@@ -84,6 +89,7 @@ def parse_args():
     ap.add_argument("--no-heavy", action="store_true", help="skip the heavy 2160p leg")
     ap.add_argument("--no-area-light", action="store_true", help="skip the 289-sample area-light ground-truth leg")
     ap.add_argument("--no-edt", action="store_true", help="skip the EDT-filtered hard shadows leg")
+    ap.add_argument("--no-moments", action="store_true", help="skip the moment shadow map leg")
     ap.add_argument("--surrogate-frames", type=int, default=8000,
                     help="training frames (one 256^2 crop each, batch 16) for the surrogate leg")
     ap.add_argument("--profile", action="store_true",
@@ -623,6 +629,46 @@ def run_edt(args, ctx, stream, local, flush):
     }
 
 
+def run_moments(args, ctx, stream, local, flush):
+    """VSM / ESM / EVSM / MSM frames in ShadowMapping's 1024^2-over-2048^2 setup."""
+    import torch
+
+    import globalillumination_gb300 as gi
+    from globalillumination_gb300 import _capi as api, scenes
+
+    w = scenes.pcss_1080p(width=1024, height=1024, map_size=2048)
+    fr = gi.frame_setup(w.light, w.camera)
+    S, W = w.map_params.width, w.camera.width
+    w.scene.upload(ctx, stream)
+    bufs = gi.allocate_frame(S, S, W, W, local)
+    out = {"workload": "pcss_1080p scene through ShadowMapping's 1024x1024 window, 2048^2 map; moment map, "
+                       "2x2 box level to 1024^2, 7-tap blur in x and y, bilinear lookups",
+           "ms_per_frame": {}}
+    for name, tech in (("hard", api.GI_TECH_HARD), ("vsm", api.GI_TECH_VSM), ("esm", api.GI_TECH_ESM),
+                       ("evsm", api.GI_TECH_EVSM), ("msm", api.GI_TECH_MSM)):
+        p = gi.ShadowParams.defaults(tech)
+        for _ in range(5):
+            gi.render_frame(ctx, w.scene, fr, w.map_params, p, W, W, bufs, stream)
+        torch.cuda.synchronize()
+        ms = []
+        for r in range(30):
+            flush.fill_(float(r))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            gi.render_frame(ctx, w.scene, fr, w.map_params, p, W, W, bufs, stream)
+            e1.record(stream)
+            ms.append((e0, e1))
+        torch.cuda.synchronize()
+        out["ms_per_frame"][name] = statistics.median(a.elapsed_time(b) for a, b in ms)
+        if name != "hard":
+            v = bufs.vis
+            out.setdefault("soft_pixel_fraction", {})[name] = float(((v > 0.25) & (v < 1.0)).float().mean())
+    # moment pipeline bytes: moment map write 16 S^2, box level read 16 S^2 +
+    # write 16 W^2, two blurs read + write 16 W^2 each, lookup reads ~16 W^2
+    out["moment_pipeline_algorithmic_bytes"] = 32 * S * S + 16 * W * W * 6
+    return out
+
+
 def measured_bf16_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -850,6 +896,9 @@ def run_ours(args):
     area = None
     if not args.no_area_light and rank == 0:
         area = run_area_light(args, ctx, stream, local, w, fr, bufs, net)
+    moments_leg = None
+    if not args.no_moments and rank == 0:
+        moments_leg = run_moments(args, ctx, stream, local, flush)
     edt_leg = None
     if not args.no_edt and rank == 0:
         edt_leg = run_edt(args, ctx, stream, local, flush)
@@ -897,6 +946,8 @@ def run_ours(args):
             line["area_light_ground_truth"] = area
         if edt_leg is not None:
             line["edt_soft_shadows"] = edt_leg
+        if moments_leg is not None:
+            line["moment_shadows"] = moments_leg
         if clk and any(r in clk["reasons"] for r in THROTTLE_BAD):
             line["clocks_warning"] = "throttled during the timed region"
         if world == 1 and not args.no_cpu_baseline:

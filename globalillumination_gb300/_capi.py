@@ -46,7 +46,11 @@ GI_TECH_RSMSS = 9
 GI_TECH_HARD_SOFTAPP = 10
 GI_PBA_MARKER = -32768
 GI_TECH_RBSSM = 11
-GI_TECH_COUNT = 12
+GI_TECH_VSM = 12
+GI_TECH_ESM = 13
+GI_TECH_EVSM = 14
+GI_TECH_MSM = 15
+GI_TECH_COUNT = 16
 GI_ACT_NONE = 0
 GI_ACT_RELU = 1
 

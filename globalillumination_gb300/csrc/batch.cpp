@@ -243,6 +243,11 @@ extern "C" gi_status gi_batch_add_frame(gi_batch* b, const gi_scene* scene, cons
     for (int l = 0; l < num_lights; ++l) {
         if (maps[l].width < 1 || maps[l].height < 1 || maps[l].width > 16384 || maps[l].height > 16384)
             return fail(GI_ERR_INVALID_ARG, "gi_batch_add_frame: map size must be in [1, 16384]");
+        if (gi::is_moment_technique(vis->technique)) {
+            gi_status st = gi::moment_check_shape(maps[l].width, maps[l].height, camera->width, camera->height,
+                                                  "gi_batch_add_frame");
+            if (st != GI_OK) return st;
+        }
         f.lights.push_back(lights[l]);
         f.maps.push_back(maps[l]);
         gi_frame_matrices m;

@@ -115,6 +115,8 @@ extern "C" void gi_context_destroy(gi_context* c) {
     cudaFree(c->d_area_maps);
     cudaFree(c->d_area_acc);
     cudaFree(c->d_pba_cols);
+    cudaFree(c->d_mom);
+    cudaFree(c->d_mom_blur);
     cudaFree(c->d_pba_near);
     for (int i = 0; i < 8; ++i) cudaFree(c->bin_buf[i]);
     for (int k = 0; k < 2; ++k)
@@ -468,6 +470,8 @@ extern "C" gi_status gi_visibility(gi_context* ctx, const gi_vis_params* p, cons
     gi_status st = check_image(map_w, map_h, "gi_visibility (map)");
     if (st == GI_OK) st = check_image(W, H, "gi_visibility");
     if (st == GI_OK) st = check_vis_params(p);
+    if (st == GI_OK && gi::is_moment_technique(p->technique))
+        st = gi::moment_check_shape(map_w, map_h, W, H, "gi_visibility");
     if (st == GI_OK) st = check_device(ctx);
     if (st != GI_OK) return st;
     return gi::launch_visibility(ctx, p, d_depth, map_w, map_h, d_pos, d_nrm, d_vis, W, H,
@@ -485,6 +489,8 @@ extern "C" gi_status gi_render_frame(gi_context* ctx, const gi_scene* s, const g
     st = check_image(mp->width, mp->height, "gi_render_frame (map)");
     if (st == GI_OK) st = check_image(W, H, "gi_render_frame");
     if (st == GI_OK) st = check_vis_params(vp);
+    if (st == GI_OK && gi::is_moment_technique(vp->technique))
+        st = gi::moment_check_shape(mp->width, mp->height, W, H, "gi_render_frame");
     if (st != GI_OK) return st;
     if (mp->bias_mode < GI_BIAS_NONE || mp->bias_mode > GI_BIAS_POLYGON_OFFSET)
         return fail(GI_ERR_INVALID_ARG, "gi_render_frame: bad bias_mode");

@@ -101,6 +101,12 @@ struct gi_context {
     size_t cap_area_maps = 0;
     float* d_area_acc = nullptr;
     size_t cap_area_acc = 0;
+    // moment techniques: the S x S moment map plus its first mip level, and
+    // the two W x W blur targets (float4)
+    void* d_mom = nullptr;
+    size_t cap_mom = 0;
+    void* d_mom_blur = nullptr;
+    size_t cap_mom_blur = 0;
     // PBA distance transform: phase-1 site row per pixel (int16)
     int16_t* d_pba_cols = nullptr;
     size_t cap_pba_cols = 0;

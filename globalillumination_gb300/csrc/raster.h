@@ -81,6 +81,17 @@ gi_status launch_pba(gi_context* ctx, const int16_t* d_sites, const float* d_ima
                      int W, int H, int m1, int m2, int m3, float penumbra, float intensity, int16_t* d_nearest,
                      float* d_out4, cudaStream_t st);
 
+// Filtered moment maps (GI_TECH_VSM .. GI_TECH_MSM): the moment map of the
+// S x S light map, its 2 x 2 box levels down to the W x W window, the
+// separable 7-tap blur; *filtered = the blurred map (float4, W x W).
+bool is_moment_technique(int t);
+gi_status moment_check_shape(int map_w, int map_h, int W, int H, const char* who);
+void moment_quantization(float mq[16], float mqi[16], float* tq0);
+gi_status launch_moments(gi_context* ctx, int tech, const float* d_depth, int S, int W, cudaStream_t st,
+                         const float** filtered);
+gi_status moment_prepare(gi_context* ctx, int tech, const float* d_depth, int S, int W, cudaStream_t st,
+                         const float** filtered);
+
 // Progressive best-candidate Poisson-disk sequence in the unit disk
 // (poisson_table.inc); the n-tap table is its first n points.
 extern const float kPoissonDisk[64][2];

@@ -1073,6 +1073,108 @@ __device__ float cs_rpcf(const gi_vis_params& p, const Ctx& c, V4 n) {
     return illum / (float)count;
 }
 
+// ---- filtered moment maps (Shadow.frag:118-220) -------------------------------
+// c.map holds the blurred moment map (float4 per texel, c.W x c.H); the
+// MSM inverse quantisation and its offset come from c_msm.
+__constant__ float c_msm[20];
+
+__device__ __forceinline__ float gl_linearize(float depth) { return 2.0f / (1001.0f - depth * 999.0f); }
+
+// texture2D on the blurred map: bilinear at level 0, FP32 weights, zero
+// border; coordinates that are not finite read the border.
+__device__ __forceinline__ V4 moment_fetch(const Ctx& c, float s, float t) {
+    const float4* m = reinterpret_cast<const float4*>(c.map);
+    const float u = s * c.fW - 0.5f, v = t * c.fH - 0.5f;
+    V4 r{0.0f, 0.0f, 0.0f, 0.0f};
+    if (!(u > -2.0f && u < c.fW + 1.0f && v > -2.0f && v < c.fH + 1.0f)) return r;
+    const float fu = floorf(u), fv = floorf(v);
+    const int i0 = (int)fu, j0 = (int)fv;
+    const float a = u - fu, b = v - fv;
+    const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    float4 T[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int i = i0 + (k & 1), j = j0 + (k >> 1);
+        T[k] = (i >= 0 && i < c.W && j >= 0 && j < c.H) ? __ldg(m + (size_t)j * c.W + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    r.x = ((w00 * T[0].x + w10 * T[1].x) + w01 * T[2].x) + w11 * T[3].x;
+    r.y = ((w00 * T[0].y + w10 * T[1].y) + w01 * T[2].y) + w11 * T[3].y;
+    r.z = ((w00 * T[0].z + w10 * T[1].z) + w01 * T[2].z) + w11 * T[3].z;
+    r.w = ((w00 * T[0].w + w10 * T[1].w) + w01 * T[2].w) + w11 * T[3].w;
+    return r;
+}
+
+// chebyshevUpperBound (Shadow.frag:118-131)
+__device__ __forceinline__ float chebyshev(float mx, float my, float z, float I) {
+    if (z <= mx) return 1.0f;
+    const float variance = my - mx * mx;
+    const float d = z - mx;
+    float p_max = variance / (variance + d * d);
+    const float p = z <= mx ? 1.0f : 0.0f;
+    p_max = gmax(p, p_max);
+    return gmix(p_max, 1.0f, I);
+}
+
+// varianceShadowMapping (:133-141)
+__device__ __forceinline__ float vsm(const Ctx& c, V4 n) {
+    const V4 m = moment_fetch(c, n.x, n.y);
+    return chebyshev(m.x, m.y, gl_linearize(n.z), c.I);
+}
+
+// exponentialShadowMapping (:144-157)
+__device__ __forceinline__ float esm(const Ctx& c, V4 n) {
+    const float k = 80.0f;
+    float e2 = moment_fetch(c, n.x, n.y).x;
+    e2 = expf(k * e2);
+    const float z = gl_linearize(n.z);
+    const float e1 = expf(-k * z);
+    return gclamp(e1 * e2, c.I, 1.0f);
+}
+
+// exponentialVarianceShadowMapping (:160-176)
+__device__ __forceinline__ float evsm(const Ctx& c, V4 n) {
+    const float z = gl_linearize(n.z);
+    const V4 m = moment_fetch(c, n.x, n.y);
+    const float variance = chebyshev(m.x, m.y, z, c.I);
+    const float k = 60.0f;
+    const float e1 = expf(-k * z);
+    const float e2 = expf(k * m.z);
+    const float exponential = gclamp(e1 * e2, c.I, 1.0f);
+    return gmin(variance, exponential);
+}
+
+// hamburger4MSM (:178-220)
+__device__ __forceinline__ float msm(const Ctx& c, V4 n) {
+    V4 b = moment_fetch(c, n.x, n.y);
+    b = V4{b.x - c_msm[16], b.y - c_msm[17], b.z - c_msm[18], b.w - c_msm[19]};
+    b = mat4_mul(c_msm, b);
+    const float bias = 0.00003f;
+    const float z0 = gl_linearize(n.z);
+    const float ob = 1.0f - bias, hb = bias * 0.5f;
+    b = V4{ob * b.x + hb, ob * b.y + hb, ob * b.z + hb, ob * b.w + hb};
+    const float dx = 1.0f, dy = z0, dz = z0 * z0;
+    const float L10 = b.x, L20 = b.y;
+    const float D11 = b.y - L10 * L10;
+    const float L21 = (b.z - L20 * L10) / D11;
+    const float D22 = b.w - L20 * L20 - L21 * L21 * D11;
+    const float y0 = dx;
+    float y1 = dy - L10 * y0;
+    float y2 = dz - L20 * y0 - L21 * y1;
+    y1 = y1 / D11;
+    y2 = y2 / D22;
+    const float cz = y2, cy = y1 - L21 * cz, cx = y0 - L10 * cy - L20 * cz;
+    const float p = cy / cz, q = cx / cz;
+    const float D = ((p * p) / 4.0f) - q;
+    const float r = sqrtf(D);
+    const float zy = -(p / 2.0f) - r, zz = -(p / 2.0f) + r;
+    if (z0 <= zy) return 1.0f;
+    if (z0 <= zz)
+        return gclamp(1.0f - gclamp((z0 * zz - b.x * (z0 + zz) + b.y) / ((zz - zy) * (z0 - zy)), 0.0f, 1.0f), c.I,
+                      1.0f);
+    return gclamp(1.0f - gclamp(1.0f - (zy * zz - b.x * (zy + zz) + b.y) / ((z0 - zy) * (z0 - zz)), 0.0f, 1.0f),
+                  c.I, 1.0f);
+}
+
 template <int TECH>
 __device__ __forceinline__ float shade(const gi_vis_params& p, const Ctx& c, V4 vertex, V4 normal) {
     if (vertex.x == 0.0f) return 0.0f;
@@ -1117,6 +1219,14 @@ __device__ __forceinline__ float shade(const gi_vis_params& p, const Ctx& c, V4 
         if (shadow == 1.0f) shadow = cs_rpcf(p, c, n);
     } else if (TECH == GI_TECH_RBSSM) {
         if (sc.w > 0.0f && shadow == 1.0f) shadow = rb_rbssm(p, c, n);
+    } else if (TECH == GI_TECH_VSM) {
+        if (sc.w > 0.0f && shadow == 1.0f) shadow = vsm(c, n);
+    } else if (TECH == GI_TECH_ESM) {
+        if (sc.w > 0.0f && shadow == 1.0f) shadow = esm(c, n);
+    } else if (TECH == GI_TECH_EVSM) {
+        if (sc.w > 0.0f && shadow == 1.0f) shadow = evsm(c, n);
+    } else if (TECH == GI_TECH_MSM) {
+        if (sc.w > 0.0f && shadow == 1.0f) shadow = msm(c, n);
     } else if (TECH == GI_TECH_HARD_SOFTAPP) {
         float r = shadow;
         if (sc.w > 0.0f && r == 1.0f) {
@@ -1522,10 +1632,28 @@ gi_status launch_area_accumulate(gi_context* ctx, const gi_scene* scene, const f
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "area-light accumulate launch");
 }
 
+// The moment map, its mip levels and blur for the moment techniques, then
+// the MSM constants; *filtered points at the blurred window-size map.
+gi_status moment_prepare(gi_context* ctx, int tech, const float* d_depth, int S, int W, cudaStream_t st,
+                         const float** filtered) {
+    gi_status s = launch_moments(ctx, tech, d_depth, S, W, st, filtered);
+    if (s != GI_OK || tech != GI_TECH_MSM) return s;
+    float mq[16], h[20];
+    moment_quantization(mq, h, &h[16]);
+    h[17] = h[18] = h[19] = 0.0f;
+    const cudaError_t e = cudaMemcpyToSymbolAsync(vis::c_msm, h, sizeof h, 0, cudaMemcpyHostToDevice, st);
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "MSM constants");
+}
+
 gi_status launch_visibility(gi_context* ctx, const gi_vis_params* p, const float* d_depth,
                             int map_w, int map_h, const float* d_pos, const float* d_nrm,
                             float* d_vis, int W, int H, cudaStream_t st) {
     dim3 grid((W + 31) / 32, (H + 3) / 4);
+    if (is_moment_technique(p->technique)) {
+        gi_status s = moment_prepare(ctx, p->technique, d_depth, map_w, W, st, &d_depth);
+        if (s != GI_OK) return s;
+        map_w = map_h = W;
+    }
     // shadowMapStep = (1.0 / w, 1.0 / h) in double, stored as float
     // (glUniform2f at MyGLGeometryViewer.cpp:237-238)
     const float sx = (float)(1.0 / (double)map_w), sy = (float)(1.0 / (double)map_h);
@@ -1548,6 +1676,10 @@ gi_status launch_visibility(gi_context* ctx, const gi_vis_params* p, const float
         GI_VIS_CASE(GI_TECH_RSMSS)
         GI_VIS_CASE(GI_TECH_HARD_SOFTAPP)
         GI_VIS_CASE(GI_TECH_RBSSM)
+        GI_VIS_CASE(GI_TECH_VSM)
+        GI_VIS_CASE(GI_TECH_ESM)
+        GI_VIS_CASE(GI_TECH_EVSM)
+        GI_VIS_CASE(GI_TECH_MSM)
         default:
             return fail(GI_ERR_INVALID_ARG, "gi_visibility: unknown technique");
     }
@@ -1562,6 +1694,11 @@ gi_status launch_frame_visibility(gi_context* ctx, const gi_vis_params* p, const
                                   float* d_vis, int W, int H, float* d_pos, float* d_nrm,
                                   cudaStream_t st) {
     dim3 grid((W + 31) / 32, (H + 3) / 4);
+    if (is_moment_technique(p->technique)) {
+        gi_status s = moment_prepare(ctx, p->technique, d_depth, map_w, W, st, &d_depth);
+        if (s != GI_OK) return s;
+        map_w = map_h = W;
+    }
     const float sx = (float)(1.0 / (double)map_w), sy = (float)(1.0 / (double)map_h);
     const unsigned* rec_of = static_cast<const unsigned*>(ctx->tier_buf[1][6]);
     const dev::BRec* recs = static_cast<const dev::BRec*>(ctx->tier_buf[1][0]);
@@ -1590,6 +1727,10 @@ gi_status launch_frame_visibility(gi_context* ctx, const gi_vis_params* p, const
         GI_FRAME_CASE(GI_TECH_RSMSS)
         GI_FRAME_CASE(GI_TECH_HARD_SOFTAPP)
         GI_FRAME_CASE(GI_TECH_RBSSM)
+        GI_FRAME_CASE(GI_TECH_VSM)
+        GI_FRAME_CASE(GI_TECH_ESM)
+        GI_FRAME_CASE(GI_TECH_EVSM)
+        GI_FRAME_CASE(GI_TECH_MSM)
         default:
             return fail(GI_ERR_INVALID_ARG, "gi_render_frame: unknown technique");
     }

@@ -269,6 +269,10 @@ TECHNIQUES = {
     "rsmss": api.GI_TECH_RSMSS,
     "hard_softapp": api.GI_TECH_HARD_SOFTAPP,
     "rbssm": api.GI_TECH_RBSSM,
+    "vsm": api.GI_TECH_VSM,
+    "esm": api.GI_TECH_ESM,
+    "evsm": api.GI_TECH_EVSM,
+    "msm": api.GI_TECH_MSM,
 }
 
 

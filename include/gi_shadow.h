@@ -287,7 +287,19 @@ typedef enum gi_technique {
     GI_TECH_RSMSS = 9,                /* FilteredRBSM.frag (RSMSS / RPCF v.2) */
     GI_TECH_HARD_SOFTAPP = 10,        /* SoftShadow HardShadow.frag:35-58     */
     GI_TECH_RBSSM = 11,               /* SoftShadow/RBSSM.frag:1202-1376      */
-    GI_TECH_COUNT = 12
+    /* Filtered moment maps (ShadowMapping/src/main.cpp:220-240, 374-396;
+     * Shaders/ShadowMap/{Moments,Exponential,ExponentialMoments}.frag;
+     * Shaders/Filter/{Gaussian,LogGaussian}Filter.frag; lookups
+     * Shadow.frag:118-220).  The light map becomes a moment map, is blurred
+     * by the 7-tap Gaussian (log-space for ESM) into a window-size target
+     * and read back bilinearly.  Needs a square window (width == height)
+     * and a map side equal to the window side times 2^k (k = 0..4), as the
+     * reference's 1024^2 window over its 2048^2 map. */
+    GI_TECH_VSM = 12,                 /* Shadow.frag:118-141 (Chebyshev)      */
+    GI_TECH_ESM = 13,                 /* Shadow.frag:144-157                  */
+    GI_TECH_EVSM = 14,                /* Shadow.frag:160-176                  */
+    GI_TECH_MSM = 15,                 /* Shadow.frag:178-220 (Hamburger 4MSM) */
+    GI_TECH_COUNT = 16
 } gi_technique;
 
 typedef enum gi_pretest_mode {

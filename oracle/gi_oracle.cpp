@@ -1487,6 +1487,222 @@ float cs_rpcf(const Ctx& c, V4 n) {  // computeShadowFromRPCF (conservative)
     return illum / (float)count;
 }
 
+// ---- filtered moment maps (VSM, ESM, EVSM, MSM) ------------------------------
+// ShadowMapping/src/main.cpp:220-240 (moment shaders), 374-396 (filters),
+// Shadow.frag:118-220 (lookups).  The choices GL leaves to the driver are
+// made as in the CUDA path: moments from the depth map's value; dFdx / dFdy
+// as differences inside each 2 x 2 quad (0 next to an empty texel); mip
+// levels as 2 x 2 box averages ((a + b) + (c + d)) * 0.25; the 7 Gaussian
+// taps on texel centres with a zero border, products and sums rounded
+// separately in tap order; lookups bilinear at level 0 with FP32 weights.
+const float kGauss7[7] = {1.0f / 64.0f, 6.0f / 64.0f, 15.0f / 64.0f, 20.0f / 64.0f,
+                          15.0f / 64.0f, 6.0f / 64.0f, 1.0f / 64.0f};
+
+float gl_linearize(float depth) { return 2.0f / (1001.0f - depth * 999.0f); }
+
+// MyGLGeometryViewer::configureMoments: the optimised 4MSM quantisation
+// (rows as written), column-major as the shader receives it, and its
+// inverse computed in double from the float matrix.
+void msm_quantization(float mq[16], float mqi[16]) {
+    const double Q[4][4] = {{-2.07224649, 32.2370378, -68.5710746, 39.3703274},
+                            {13.7948857, -59.4683976, 82.035975, -35.3649032},
+                            {0.105877704, -1.90774663, 9.34965551, -6.65434907},
+                            {9.79240621, -33.76521106, 47.9456097, -23.9728048}};
+    double a[4][8];
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) {
+            const float q = (float)Q[r][c];
+            mq[c * 4 + r] = q;
+            a[r][c] = (double)q;
+            a[r][c + 4] = r == c ? 1.0 : 0.0;
+        }
+    for (int c = 0; c < 4; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < 4; ++r)
+            if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+        for (int k = 0; k < 8; ++k) std::swap(a[c][k], a[piv][k]);
+        const double inv = 1.0 / a[c][c];
+        for (int k = 0; k < 8; ++k) a[c][k] *= inv;
+        for (int r = 0; r < 4; ++r)
+            if (r != c) {
+                const double f = a[r][c];
+                for (int k = 0; k < 8; ++k) a[r][k] -= f * a[c][k];
+            }
+    }
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) mqi[c * 4 + r] = (float)a[r][c + 4];
+}
+
+// The blurred window-size moment map (W x W float4) of an S x S depth map.
+std::vector<float> moment_filtered(int tech, const float* depth, int S, int W) {
+    std::vector<float> m((size_t)S * S * 4);
+    float mq[16], mqi[16];
+    msm_quantization(mq, mqi);
+    const float tq0 = 0.0359558848f;
+    auto lin_at = [&](int x, int y, bool& empty) {
+        const float d = depth[(size_t)y * S + x];
+        empty = !(d < 1.0f);
+        return gl_linearize(d);
+    };
+    for (int y = 0; y < S; ++y)
+        for (int x = 0; x < S; ++x) {
+            float* o = &m[4 * ((size_t)y * S + x)];
+            bool empty;
+            const float d = lin_at(x, y, empty);
+            if (empty) {
+                o[0] = o[1] = o[2] = 0.0f;
+                o[3] = 1.0f;
+            } else if (tech == GI_TECH_ESM) {
+                o[0] = d;
+                o[1] = o[2] = 0.0f;
+                o[3] = 1.0f;
+            } else if (tech == GI_TECH_MSM) {
+                const float d2 = d * d, d3 = d2 * d, d4 = d3 * d;
+                for (int r = 0; r < 4; ++r)
+                    o[r] = mq[r] * d + mq[4 + r] * d2 + mq[8 + r] * d3 + mq[12 + r] * d4 + (r == 0 ? tq0 : 0.0f);
+            } else {
+                bool el, er, eb, et;
+                const int xr = (x | 1) < S ? (x | 1) : x, yt = (y | 1) < S ? (y | 1) : y;
+                const float l = lin_at(x & ~1, y, el), rr = lin_at(xr, y, er);
+                const float b = lin_at(x, y & ~1, eb), t = lin_at(x, yt, et);
+                const float dx = (el || er) ? 0.0f : rr - l;
+                const float dy = (eb || et) ? 0.0f : t - b;
+                float m2 = d * d;
+                m2 = m2 + 0.25f * (dx * dx + dy * dy);
+                o[0] = d;
+                o[1] = m2;
+                o[2] = tech == GI_TECH_EVSM ? d : 0.0f;
+                o[3] = tech == GI_TECH_EVSM ? 1.0f : 0.0f;
+            }
+        }
+    for (int side = S; side > W; side /= 2) {
+        const int h = side / 2;
+        std::vector<float> n((size_t)h * h * 4);
+        for (int y = 0; y < h; ++y)
+            for (int x = 0; x < h; ++x)
+                for (int k = 0; k < 4; ++k) {
+                    const float a = m[4 * ((size_t)(2 * y) * side + 2 * x) + k];
+                    const float b = m[4 * ((size_t)(2 * y) * side + 2 * x + 1) + k];
+                    const float c = m[4 * ((size_t)(2 * y + 1) * side + 2 * x) + k];
+                    const float d = m[4 * ((size_t)(2 * y + 1) * side + 2 * x + 1) + k];
+                    n[4 * ((size_t)y * h + x) + k] = ((a + b) + (c + d)) * 0.25f;
+                }
+        m.swap(n);
+    }
+    auto blur = [&](const std::vector<float>& in, int dx, int dy) {
+        std::vector<float> out((size_t)W * W * 4);
+        for (int y = 0; y < W; ++y)
+            for (int x = 0; x < W; ++x) {
+                auto tap = [&](int k, int ch) {
+                    const int xx = x + dx * k, yy = y + dy * k;
+                    if (xx < 0 || xx >= W || yy < 0 || yy >= W) return 0.0f;
+                    return in[4 * ((size_t)yy * W + xx) + ch];
+                };
+                float* o = &out[4 * ((size_t)y * W + x)];
+                if (tech != GI_TECH_ESM) {
+                    for (int ch = 0; ch < 4; ++ch) {
+                        float r = 0.0f;
+                        for (int k = -3; k <= 3; ++k) r = r + tap(k, ch) * kGauss7[3 + k];
+                        o[ch] = r;
+                    }
+                } else {
+                    const float s0 = tap(-3, 0), s1 = tap(-2, 0);
+                    float sum = s0 + std::log(kGauss7[0] + kGauss7[1] * std::exp(s1 - s0));
+                    for (int i = 2; i < 7; ++i) sum = sum + std::log(1.0f + kGauss7[i] * std::exp(tap(i - 3, 0) - sum));
+                    o[0] = o[1] = o[2] = o[3] = sum;
+                }
+            }
+        return out;
+    };
+    return blur(blur(m, 1, 0), 0, 1);
+}
+
+V4 moment_fetch(const Ctx& c, float s, float t) {
+    const float u = s * (float)c.W - 0.5f, v = t * (float)c.H - 0.5f;
+    V4 r{0.0f, 0.0f, 0.0f, 0.0f};
+    if (!(u > -2.0f && u < (float)c.W + 1.0f && v > -2.0f && v < (float)c.H + 1.0f)) return r;
+    const float fu = std::floor(u), fv = std::floor(v);
+    const int i0 = (int)fu, j0 = (int)fv;
+    const float a = u - fu, b = v - fv;
+    const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    float T[4][4];
+    for (int k = 0; k < 4; ++k) {
+        const int i = i0 + (k & 1), j = j0 + (k >> 1);
+        for (int ch = 0; ch < 4; ++ch)
+            T[k][ch] = (i >= 0 && i < c.W && j >= 0 && j < c.H) ? c.map[4 * ((size_t)j * c.W + i) + ch] : 0.0f;
+    }
+    float* o = &r.x;
+    for (int ch = 0; ch < 4; ++ch) o[ch] = ((w00 * T[0][ch] + w10 * T[1][ch]) + w01 * T[2][ch]) + w11 * T[3][ch];
+    return r;
+}
+
+// chebyshevUpperBound (Shadow.frag:118-131)
+float chebyshev(float mx, float my, float z, float I) {
+    if (z <= mx) return 1.0f;
+    const float variance = my - mx * mx;
+    const float d = z - mx;
+    float p_max = variance / (variance + d * d);
+    const float p = z <= mx ? 1.0f : 0.0f;
+    p_max = gmax(p, p_max);
+    return gmix(p_max, 1.0f, I);
+}
+
+float moment_lookup(const Ctx& c, V4 n) {
+    const int tech = c.p->technique;
+    if (tech == GI_TECH_VSM) {  // varianceShadowMapping (:133-141)
+        const V4 m = moment_fetch(c, n.x, n.y);
+        return chebyshev(m.x, m.y, gl_linearize(n.z), c.I);
+    }
+    if (tech == GI_TECH_ESM) {  // exponentialShadowMapping (:144-157)
+        const float k = 80.0f;
+        float e2 = moment_fetch(c, n.x, n.y).x;
+        e2 = std::exp(k * e2);
+        const float z = gl_linearize(n.z);
+        const float e1 = std::exp(-k * z);
+        return gclamp(e1 * e2, c.I, 1.0f);
+    }
+    if (tech == GI_TECH_EVSM) {  // exponentialVarianceShadowMapping (:160-176)
+        const float z = gl_linearize(n.z);
+        const V4 m = moment_fetch(c, n.x, n.y);
+        const float variance = chebyshev(m.x, m.y, z, c.I);
+        const float k = 60.0f;
+        const float e1 = std::exp(-k * z);
+        const float e2 = std::exp(k * m.z);
+        return gmin(variance, gclamp(e1 * e2, c.I, 1.0f));
+    }
+    // hamburger4MSM (:178-220)
+    float mq[16], mqi[16];
+    msm_quantization(mq, mqi);
+    V4 b = moment_fetch(c, n.x, n.y);
+    b = V4{b.x - 0.0359558848f, b.y - 0.0f, b.z - 0.0f, b.w - 0.0f};
+    b = mat4_mul(mqi, b);
+    const float bias = 0.00003f;
+    const float z0 = gl_linearize(n.z);
+    const float ob = 1.0f - bias, hb = bias * 0.5f;
+    b = V4{ob * b.x + hb, ob * b.y + hb, ob * b.z + hb, ob * b.w + hb};
+    const float dx = 1.0f, dy = z0, dz = z0 * z0;
+    const float L10 = b.x, L20 = b.y;
+    const float D11 = b.y - L10 * L10;
+    const float L21 = (b.z - L20 * L10) / D11;
+    const float D22 = b.w - L20 * L20 - L21 * L21 * D11;
+    const float y0 = dx;
+    float y1 = dy - L10 * y0;
+    float y2 = dz - L20 * y0 - L21 * y1;
+    y1 = y1 / D11;
+    y2 = y2 / D22;
+    const float cz = y2, cy = y1 - L21 * cz, cx = y0 - L10 * cy - L20 * cz;
+    const float p = cy / cz, q = cx / cz;
+    const float D = ((p * p) / 4.0f) - q;
+    const float r = std::sqrt(D);
+    const float zy = -(p / 2.0f) - r, zz = -(p / 2.0f) + r;
+    if (z0 <= zy) return 1.0f;
+    if (z0 <= zz)
+        return gclamp(1.0f - gclamp((z0 * zz - b.x * (z0 + zz) + b.y) / ((zz - zy) * (z0 - zy)), 0.0f, 1.0f), c.I,
+                      1.0f);
+    return gclamp(1.0f - gclamp(1.0f - (zy * zz - b.x * (zy + zz) + b.y) / ((z0 - zy) * (z0 - zz)), 0.0f, 1.0f),
+                  c.I, 1.0f);
+}
+
 float shade_pixel(const Ctx& c, V4 vertex, V4 normal, const float* poisson) {
     if (vertex.x == 0.0f) return 0.0f;  // discard: the target keeps its clear value 0
     const gi_vis_params* p = c.p;
@@ -1538,6 +1754,12 @@ float shade_pixel(const Ctx& c, V4 vertex, V4 normal, const float* poisson) {
         case GI_TECH_RBSSM:  // RBSSM.frag:1362-1376
             if (sc.w > 0.0f && shadow == 1.0f) shadow = rb_rbssm(c, n);
             return shadow;
+        case GI_TECH_VSM:
+        case GI_TECH_ESM:
+        case GI_TECH_EVSM:
+        case GI_TECH_MSM:
+            if (sc.w > 0.0f && shadow == 1.0f) shadow = moment_lookup(c, n);
+            return shadow;
         case GI_TECH_HARD_SOFTAPP: {
             float r = shadow;
             if (sc.w > 0.0f && r == 1.0f) {
@@ -1565,6 +1787,12 @@ extern "C" void or_visibility(const gi_vis_params* p, const float* depth, int ma
     c.sx = (float)(1.0 / map_w);  // glUniform2f(1.0/w, 1.0/h): double then float
     c.sy = (float)(1.0 / map_h);
     c.I = p->shadow_intensity;
+    std::vector<float> moments;
+    if (p->technique >= GI_TECH_VSM && p->technique <= GI_TECH_MSM) {
+        moments = moment_filtered(p->technique, depth, map_w, W);
+        c.map = moments.data();
+        c.W = c.H = W;
+    }
 #pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads(threads))
     for (int y = 0; y < H; ++y)
         for (int x = 0; x < W; ++x) {

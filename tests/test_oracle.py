@@ -358,3 +358,45 @@ def test_phong_single_pixel_known_answer():
     alpha = f(f(f(1.0) + f(f(0.75) * spec)) + f(1.0))  # diffuse and ambient alpha are 1
     assert out[0].tolist() == [float(rgb)] * 3 + [float(alpha)]
     assert out[1].tolist() == [float(f(0.63)), float(f(0.82)), float(f(0.96)), 1.0]
+
+
+def _moment_probe(tech, depth_map, S, s, t, z):
+    """Like _probe, but the window is S x S (the moment techniques blur the
+    map into a window-size target): pixel 0 carries the probe, the others
+    are background."""
+    p = gi.ShadowParams.defaults(tech)
+    p.pretest = api.GI_PRETEST_OFF
+    fr = gi.Frame(IDENTITY, IDENTITY, IDENTITY, IDENTITY, np.eye(3, dtype=np.float32).reshape(-1),
+                  np.zeros(3, np.float32))
+    pos = np.zeros((S * S, 4), np.float32)
+    pos[0] = (s, t, z, 1.0)
+    nrm = np.tile(np.array([0, 0, 1, 1], np.float32), (S * S, 1))
+    return float(oracle.visibility(p.to_c(fr), depth_map, S, S, pos, nrm, S, S)[0])
+
+
+@pytest.mark.parametrize("tech", [api.GI_TECH_VSM, api.GI_TECH_ESM, api.GI_TECH_EVSM, api.GI_TECH_MSM])
+def test_moment_maps_front_lit_behind_shadowed(tech):
+    # a flat blocker at window depth 0.5 over the whole map: a receiver in
+    # front of it is lit by every moment technique, one behind it is
+    # shadowed (VSM / EVSM / MSM down to about the intensity; ESM, whose
+    # exp(80 (m - z)) acts on linearised depths near 0.004, only partly)
+    S = 32
+    m = np.full(S * S, 0.5, np.float32)
+    front = _moment_probe(tech, m, S, 0.5, 0.5, 0.4)
+    behind = _moment_probe(tech, m, S, 0.5, 0.5, 0.6)
+    assert front == 1.0
+    if tech == api.GI_TECH_ESM:
+        assert 0.25 <= behind < 0.95
+    else:
+        assert behind == pytest.approx(0.25, abs=2e-3)
+
+
+def test_vsm_variance_softens_a_depth_step():
+    # two blocker depths side by side: after the 7-tap blur the texels near
+    # the step carry variance, and a receiver between the two depths there
+    # gets a Chebyshev bound strictly between the intensity and 1
+    S = 32
+    m = np.full((S, S), 0.45, np.float32)
+    m[:, S // 2:] = 0.55
+    v = _moment_probe(api.GI_TECH_VSM, m.reshape(-1), S, (S // 2 - 1.5) / S, 0.5, 0.5)
+    assert 0.25 < v < 1.0
