@@ -663,9 +663,10 @@ def run_moments(args, ctx, stream, local, flush):
         if name != "hard":
             v = bufs.vis
             out.setdefault("soft_pixel_fraction", {})[name] = float(((v > 0.25) & (v < 1.0)).float().mean())
-    # moment pipeline bytes: moment map write 16 S^2, box level read 16 S^2 +
-    # write 16 W^2, two blurs read + write 16 W^2 each, lookup reads ~16 W^2
-    out["moment_pipeline_algorithmic_bytes"] = 32 * S * S + 16 * W * W * 6
+    # moment pipeline bytes: the depth map read (4 S^2), the first box level
+    # written straight from it (16 W^2 when S = 2 W), two blurs reading and
+    # writing 16 W^2 each, the lookups reading about 16 W^2
+    out["moment_pipeline_algorithmic_bytes"] = 4 * S * S + 96 * W * W
     return out
 
 

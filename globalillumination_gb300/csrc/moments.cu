@@ -22,7 +22,9 @@
 //
 //   k_moments       Moments.frag / Exponential.frag / ExponentialMoments.frag
 //                   per light-map texel (+ MSM's quantisation)
-//   k_mip_box       one 2 x 2 box level
+//   k_moments_box   the same fused with the first box level: one thread per
+//                   2 x 2 quad, so the full-size moment map is never stored
+//   k_mip_box       one further 2 x 2 box level
 //   k_moment_blur   GaussianFilter.frag (VSM, EVSM, MSM) or
 //                   LogGaussianFilter.frag (ESM), one direction per launch
 #include <cuda_runtime.h>
@@ -53,37 +55,63 @@ __device__ __forceinline__ float lin_at(const MomArgs& a, int x, int y, bool& em
     return gl_linearize(d);
 }
 
+// Moments.frag / Exponential.frag / ExponentialMoments.frag for texel
+// (x, y); l, r, b, t are the linearised depths of its 2 x 2 quad partners
+// (left / right of its row, bottom / top of its column).
+__device__ __forceinline__ float4 moment_of(const MomArgs& a, float d, bool empty, float l, bool el, float r, bool er,
+                                            float b, bool eb, float t, bool et) {
+    if (empty) return make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+    if (a.tech == GI_TECH_ESM) return make_float4(d, 0.0f, 0.0f, 1.0f);
+    if (a.tech == GI_TECH_MSM) {
+        const float d2 = d * d, d3 = d2 * d, d4 = d3 * d;
+        const float* q = a.mq;
+        return make_float4(q[0] * d + q[4] * d2 + q[8] * d3 + q[12] * d4 + a.tq0,
+                           q[1] * d + q[5] * d2 + q[9] * d3 + q[13] * d4 + 0.0f,
+                           q[2] * d + q[6] * d2 + q[10] * d3 + q[14] * d4 + 0.0f,
+                           q[3] * d + q[7] * d2 + q[11] * d3 + q[15] * d4 + 0.0f);
+    }
+    // VSM / EVSM: moment.y += 0.25 * (dFdx^2 + dFdy^2) over the 2 x 2 quad
+    const float dx = (el || er) ? 0.0f : r - l;
+    const float dy = (eb || et) ? 0.0f : t - b;
+    float m2 = d * d;
+    m2 = m2 + 0.25f * (dx * dx + dy * dy);
+    return a.tech == GI_TECH_EVSM ? make_float4(d, m2, d, 1.0f) : make_float4(d, m2, 0.0f, 0.0f);
+}
+
+// The moment map at the light map's own size (map side == window side).
 __global__ void __launch_bounds__(256) k_moments(const MomArgs a) {
     const int x = blockIdx.x * 32 + (threadIdx.x & 31);
     const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
     if (x >= a.S || y >= a.S) return;
-    bool empty;
-    const float d = lin_at(a, x, y, empty);
-    float4 m;
-    if (empty) {
-        m = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
-    } else if (a.tech == GI_TECH_ESM) {
-        m = make_float4(d, 0.0f, 0.0f, 1.0f);
-    } else if (a.tech == GI_TECH_MSM) {
-        const float d2 = d * d, d3 = d2 * d, d4 = d3 * d;
-        const float* q = a.mq;
-        m.x = q[0] * d + q[4] * d2 + q[8] * d3 + q[12] * d4 + a.tq0;
-        m.y = q[1] * d + q[5] * d2 + q[9] * d3 + q[13] * d4 + 0.0f;
-        m.z = q[2] * d + q[6] * d2 + q[10] * d3 + q[14] * d4 + 0.0f;
-        m.w = q[3] * d + q[7] * d2 + q[11] * d3 + q[15] * d4 + 0.0f;
-    } else {
-        // VSM / EVSM: moment.y += 0.25 * (dFdx^2 + dFdy^2) over the 2 x 2 quad
-        bool el, er, eb, et;
-        const int xr = (x | 1) < a.S ? (x | 1) : x, yt = (y | 1) < a.S ? (y | 1) : y;
-        const float l = lin_at(a, x & ~1, y, el), r = lin_at(a, xr, y, er);
-        const float b = lin_at(a, x, y & ~1, eb), t = lin_at(a, x, yt, et);
-        const float dx = (el || er) ? 0.0f : r - l;
-        const float dy = (eb || et) ? 0.0f : t - b;
-        float m2 = d * d;
-        m2 = m2 + 0.25f * (dx * dx + dy * dy);
-        m = a.tech == GI_TECH_EVSM ? make_float4(d, m2, d, 1.0f) : make_float4(d, m2, 0.0f, 0.0f);
-    }
-    a.out[(size_t)y * a.S + x] = m;
+    bool e, el, er, eb, et;
+    const int xr = (x | 1) < a.S ? (x | 1) : x, yt = (y | 1) < a.S ? (y | 1) : y;
+    const float d = lin_at(a, x, y, e);
+    const float l = lin_at(a, x & ~1, y, el), r = lin_at(a, xr, y, er);
+    const float b = lin_at(a, x, y & ~1, eb), t = lin_at(a, x, yt, et);
+    a.out[(size_t)y * a.S + x] = moment_of(a, d, e, l, el, r, er, b, eb, t, et);
+}
+
+// The moment map's first box level directly (map side == 2 x the output
+// side): each thread reads one 2 x 2 quad of depths, forms the four texels'
+// moments (the quad is also where dFdx / dFdy come from) and writes their
+// box average ((q00 + q10) + (q01 + q11)) * 0.25, so the full-size moment
+// map is never stored.
+__global__ void __launch_bounds__(256) k_moments_box(const MomArgs a) {
+    const int h = a.S / 2;
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= h || y >= h) return;
+    bool e00, e10, e01, e11;
+    const float d00 = lin_at(a, 2 * x, 2 * y, e00), d10 = lin_at(a, 2 * x + 1, 2 * y, e10);
+    const float d01 = lin_at(a, 2 * x, 2 * y + 1, e01), d11 = lin_at(a, 2 * x + 1, 2 * y + 1, e11);
+    // per texel: row partners (left, right) and column partners (bottom, top)
+    const float4 q00 = moment_of(a, d00, e00, d00, e00, d10, e10, d00, e00, d01, e01);
+    const float4 q10 = moment_of(a, d10, e10, d00, e00, d10, e10, d10, e10, d11, e11);
+    const float4 q01 = moment_of(a, d01, e01, d01, e01, d11, e11, d00, e00, d01, e01);
+    const float4 q11 = moment_of(a, d11, e11, d01, e01, d11, e11, d10, e10, d11, e11);
+    const float4 s = make_float4((q00.x + q10.x) + (q01.x + q11.x), (q00.y + q10.y) + (q01.y + q11.y),
+                                 (q00.z + q10.z) + (q01.z + q11.z), (q00.w + q10.w) + (q01.w + q11.w));
+    a.out[(size_t)y * h + x] = make_float4(s.x * 0.25f, s.y * 0.25f, s.z * 0.25f, s.w * 0.25f);
 }
 
 __device__ __forceinline__ float4 add4(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
@@ -192,7 +220,10 @@ gi_status launch_moments(gi_context* ctx, int tech, const float* d_depth, int S,
                          const float** filtered) {
     using namespace mom;
     const size_t big = (size_t)S * S * sizeof(float4), small = (size_t)W * W * sizeof(float4);
-    gi_status s = ensure_buffer(reinterpret_cast<void**>(&ctx->d_mom), &ctx->cap_mom, big + (S > W ? big / 4 : 0));
+    // the moment map at the map's size when no box level is needed, else
+    // its first box level (S^2 / 4) plus room for the next one
+    const size_t need = S > W ? big / 4 + big / 16 : big;
+    gi_status s = ensure_buffer(reinterpret_cast<void**>(&ctx->d_mom), &ctx->cap_mom, need);
     if (s == GI_OK) s = ensure_buffer(reinterpret_cast<void**>(&ctx->d_mom_blur), &ctx->cap_mom_blur, 2 * small);
     if (s != GI_OK) return s;
     MomArgs ma;
@@ -202,14 +233,20 @@ gi_status launch_moments(gi_context* ctx, int tech, const float* d_depth, int S,
     ma.tech = tech;
     float mqi[16];
     moment_quantization(ma.mq, mqi, &ma.tq0);
-    k_moments<<<dim3((S + 31) / 32, (S + 7) / 8), 256, 0, st>>>(ma);
-    ctx->launches++;
-    // mip levels down to the window size, ping-ponging between the two
-    // halves of the scratch (level 1 after the full map, then back)
     float4* lvl = ma.out;
-    float4* other = ma.out + (size_t)S * S;
-    float4* first = ma.out;
-    for (int side = S; side > W; side /= 2) {
+    int side = S;
+    if (S > W) {
+        // the first box level straight from the depths, at the scratch's start
+        k_moments_box<<<dim3((S / 2 + 31) / 32, (S / 2 + 7) / 8), 256, 0, st>>>(ma);
+        side = S / 2;
+    } else {
+        k_moments<<<dim3((S + 31) / 32, (S + 7) / 8), 256, 0, st>>>(ma);
+    }
+    ctx->launches++;
+    // further box levels, ping-ponging between the two parts of the scratch
+    float4* first = lvl;
+    float4* other = lvl + (size_t)side * side;
+    for (; side > W; side /= 2) {
         float4* dst = (lvl == first) ? other : first;
         k_mip_box<<<dim3((side / 2 + 31) / 32, (side / 2 + 7) / 8), 256, 0, st>>>(lvl, side, dst);
         ctx->launches++;
