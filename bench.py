@@ -36,9 +36,10 @@ Extra legs in the same line (not the headline):
   edt_soft_shadows  ShadowMapping's EDTSM mode at its 1024 x 1024 window:
               the PBA exact distance transform over the sites of the
               SMSR hard-shadow image plus the penumbra normalisation
-              (gi_edt_soft_shadows: one column-pass and one row-pass
-              kernel, L2 flushed before each call), the whole EDTSM frame
-              (SMSR frame, EDTSM inputs, EDT), and the CPU oracle's EDT
+              (gi_edt_soft_shadows: column pass, row pass, normalisation,
+              L2 flushed before each call), the screen-space mean filter,
+              the whole EDTSM frame (SMSR frame, EDTSM inputs, EDT, mean
+              filter), and the CPU oracle's EDT
   moment_shadows  ShadowMapping's filtered moment maps (VSM, ESM, EVSM,
               MSM) at its 1024 x 1024 window over a 2048^2 map: whole
               frames per technique (light map, moment map, box level,
@@ -549,6 +550,7 @@ def edt_frame_setup(ctx, local, stream):
     image = torch.empty((H, W, 4), device="cuda")
     position = torch.empty((H, W, 4), device="cuda")
     out = torch.zeros((H, W, 4), device="cuda")
+    final = torch.zeros((H, W, 4), device="cuda")
 
     def hard():
         gi.render_frame(ctx, w.scene, fr, w.map_params, p, W, H, bufs, stream, store_gbuffer=True)
@@ -557,7 +559,10 @@ def edt_frame_setup(ctx, local, stream):
     def edt():
         gi.edt_soft_shadows(ctx, image, position, out, 1.0, p.shadow_intensity, (16, 16, 16), stream=stream)
 
-    return w, fr, p, bufs, image, position, out, hard, edt
+    def mean():
+        gi.edt_mean_filter(ctx, p, fr, out, bufs.pos, final, W, H, 7, stream=stream)
+
+    return w, fr, p, bufs, image, position, out, hard, edt, mean
 
 
 def run_edt(args, ctx, stream, local, flush):
@@ -568,7 +573,7 @@ def run_edt(args, ctx, stream, local, flush):
     import globalillumination_gb300 as gi
     import oracle
 
-    w, fr, p, bufs, image, position, out, hard, edt = edt_frame_setup(ctx, local, stream)
+    w, fr, p, bufs, image, position, out, hard, edt, mean = edt_frame_setup(ctx, local, stream)
     W, H = w.camera.width, w.camera.height
     P = W * H
     hard()
@@ -595,8 +600,10 @@ def run_edt(args, ctx, stream, local, flush):
     def frame():
         hard()
         edt()
+        mean()
 
     frame_ms = timed(frame, 50)
+    mean_ms = timed(mean, 50)
     hard_ms = timed(hard, 50)
     sites = int(((image[..., 2] == 1.0).sum()).item())  # lit-facing pixels (site candidates)
     soft = float(((out[..., 0] != image[..., 0]) & (image[..., 0] > 0)).float().mean())
@@ -618,7 +625,7 @@ def run_edt(args, ctx, stream, local, flush):
         "workload": "ShadowMapping EDTSM window 1024x1024 (pcss_1080p scene, 2048^2 map, non-conservative SMSR), "
                     "pba2DVoronoiDiagram(16, 16, 16) + pbaNormalizeEDT(penumbraSize 1 / 5, intensity 0.25)",
         "edt_ms": edt_ms, "edt_per_s": 1000.0 / edt_ms,
-        "edtsm_frame_ms": frame_ms, "smsr_frame_and_inputs_ms": hard_ms,
+        "edtsm_frame_ms": frame_ms, "smsr_frame_and_inputs_ms": hard_ms, "mean_filter_ms": mean_ms,
         "roofline": {"kernels": "k_pba_columns<kFromImage> + k_pba_rows + k_edt_normalize", "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "algorithmic_bytes_per_call": alg},
@@ -687,7 +694,7 @@ def run_profile_case(args, local):
     if args.profile_case == "edt":
         ctx = gi.Context(local)
         stream = torch.cuda.current_stream()
-        _, _, _, _, _, _, out, hard, edt = edt_frame_setup(ctx, local, stream)
+        _, _, _, _, _, _, out, hard, edt, _ = edt_frame_setup(ctx, local, stream)
         hard()
         for _ in range(3):
             edt()

@@ -199,6 +199,7 @@ _PROTOS = {
     "gi_pba_voronoi": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP]),
     "gi_edt_soft_shadows": (C.c_int, [_VP, _VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float,
                                       C.c_float, _VP, _VP, _VP]),
+    "gi_edt_mean_filter": (C.c_int, [_VP, C.POINTER(VisParams), _VP, _VP, C.c_int, C.c_int, C.c_int, _VP, _VP]),
     "gi_pba_chain_rows": (C.c_int, [_VP, C.POINTER(C.c_uint32), C.c_int]),
     "gi_edt_inputs": (C.c_int, [_VP, C.POINTER(VisParams), F16, _VP, _VP, _VP, C.c_int, C.c_int, _VP, _VP, _VP]),
     "gi_area_light_samples": (C.c_int, [C.POINTER(View), C.c_float, C.c_int, _VP]),

@@ -118,6 +118,7 @@ extern "C" void gi_context_destroy(gi_context* c) {
     cudaFree(c->d_mom);
     cudaFree(c->d_mom_blur);
     cudaFree(c->d_pba_near);
+    cudaFree(c->d_edt_meanx);
     for (int i = 0; i < 8; ++i) cudaFree(c->bin_buf[i]);
     for (int k = 0; k < 2; ++k)
         for (int i = 0; i < 8; ++i) cudaFree(c->tier_buf[k][i]);
@@ -649,6 +650,17 @@ extern "C" gi_status gi_pba_chain_rows(gi_context* ctx, uint32_t* rows, int rese
     if (e == cudaSuccess) e = cudaMemcpy(rows, ctx->d_status + 96, sizeof(uint32_t), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && reset) e = cudaMemset(ctx->d_status + 96, 0, sizeof(uint32_t));
     return e == cudaSuccess ? GI_OK : gi::fail_cuda(e, "gi_pba_chain_rows");
+}
+
+extern "C" gi_status gi_edt_mean_filter(gi_context* ctx, const gi_vis_params* vp, const float* d_image,
+                                        const float* d_pos, int W, int H, int order, float* d_out, void* stream) {
+    if (!ctx || !vp || !d_image || !d_pos || !d_out) return fail(GI_ERR_INVALID_ARG, "gi_edt_mean_filter: NULL argument");
+    if (order < 1 || order > 33) return fail(GI_ERR_INVALID_ARG, "gi_edt_mean_filter: order must be in [1, 33]");
+    gi_status st = check_device(ctx);
+    if (st == GI_OK) st = check_image(W, H, "gi_edt_mean_filter");
+    if (st != GI_OK) return st;
+    return gi::launch_edt_mean_filter(ctx, vp->camera_mv, d_image, d_pos, W, H, order, d_out,
+                                      static_cast<cudaStream_t>(stream));
 }
 
 extern "C" gi_status gi_edt_inputs(gi_context* ctx, const gi_vis_params* vp, const float camera_mvp[16],

@@ -39,6 +39,7 @@
 #include <cuda_runtime.h>
 
 #include <climits>
+#include <cmath>
 #include <cstdint>
 
 #include "internal.h"
@@ -602,6 +603,84 @@ __global__ void __launch_bounds__(256) k_edt_normalize(const NormArgs a) {
     *reinterpret_cast<float2*>(a.out4 + 4 * q) = make_float2(v, ip.y);
 }
 
+// ---- the screen-space mean filter of filterHardShadowsUsingEDT --------------
+// MeanFilter.frag, one pass per launch (main.cpp:424-447: x into a scratch
+// target, then y).  Per geometry pixel: kernelCenter = dscreen * order * 50
+// / (deye * 2) with deye = -(MV * vertex).z and dscreen = 1 / (2 tan(fov /
+// 2)) (fov = 45 passed to GLSL's tan, i.e. 45 radians, computed once on the
+// host); samples from -kernelCenter in steps of 1 while <= kernelCenter, each
+// read at centre + dir * sample / size and replaced by the centre value when
+// it is 0 or its linearised depth differs by >= 0.0005; the mean of the
+// samples in channel 0, the centre's depth in channel 1.  Pass 1 reads the
+// EDT image GL_NEAREST (texel floor(u * size)), pass 2 reads the x pass
+// bilinearly at level 0 along the filtered axis (its GL_LINEAR_MIPMAP_LINEAR
+// level is the driver's choice), each at the pixel's own row or column on
+// the other axis; both with a zero border.  A window is cut at 2049 samples,
+// which only a vertex at eye depth < 0.16 (nearer than the camera's near
+// plane at 1) could reach.
+struct MeanArgs {
+    const float4* image;  // pass 1: the EDT image; pass 2: the x pass
+    const float4* pos;    // G-buffer vertex (x == 0: background)
+    float4* out;
+    int W, H, order;
+    float dscreen;
+    float mv[16];
+};
+
+__device__ __forceinline__ float gl_lin(float depth) { return 2.0f / (1001.0f - depth * 999.0f); }
+
+template <bool VERTICAL>
+__global__ void __launch_bounds__(256) k_edt_mean_filter(const MeanArgs a) {
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= a.W || y >= a.H) return;
+    const size_t q = (size_t)y * a.W + x;
+    const float4 v = __ldg(a.pos + q);
+    if (v.x == 0.0f) {  // discard: the target keeps its clear colour
+        a.out[q] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+        return;
+    }
+    const float4 color = __ldg(a.image + q);  // the centre texel (exact in both passes)
+    const float* m = a.mv;
+    const float ez = m[2] * v.x + m[6] * v.y + m[10] * v.z + m[14] * v.w;
+    const float deye = -ez;
+    const float kc = (a.dscreen * (float)a.order * 50.0f) / (deye * 2.0f);
+    const float step = VERTICAL ? 1.0f / (float)a.H : 1.0f / (float)a.W;
+    const float cs = ((float)(VERTICAL ? y : x) + 0.5f) / (float)(VERTICAL ? a.H : a.W);
+    const float Lc = gl_lin(color.y);
+    const float size = (float)(VERTICAL ? a.H : a.W);
+    float sum = 0.0f;
+    int count = 0;
+    const float lo = -kc;
+    for (float sample = lo; sample <= kc && count < 2049; sample = sample + 1.0f) {
+        const float u = cs + sample * step;
+        float r = 0.0f, g = 0.0f;
+        if (!VERTICAL) {
+            const float fi = floorf(u * size);
+            if (fi >= 0.0f && fi < size) {
+                const float4 t = __ldg(a.image + (size_t)y * a.W + (int)fi);
+                r = t.x;
+                g = t.y;
+            }
+        } else {
+            const float uu = u * size - 0.5f;
+            const float f0 = floorf(uu), w1 = uu - f0, w0 = 1.0f - w1;
+            const int j0 = (int)f0;
+            float4 t0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), t1 = t0;
+            if (j0 >= 0 && j0 < a.H) t0 = __ldg(a.image + (size_t)j0 * a.W + x);
+            if (j0 + 1 >= 0 && j0 + 1 < a.H) t1 = __ldg(a.image + (size_t)(j0 + 1) * a.W + x);
+            r = w0 * t0.x + w1 * t1.x;
+            g = w0 * t0.y + w1 * t1.y;
+        }
+        // adjustColor (MeanFilter.frag:27-36)
+        if (r == 0.0f || fabsf(gl_lin(g) - Lc) >= 0.0005f) r = color.x;
+        sum = sum + r;
+        ++count;
+    }
+    sum = sum / (float)count;
+    a.out[q] = make_float4(sum, color.y, 0.0f, 0.0f);
+}
+
 // largest float not above c
 float float_at_most(double c) {
     float t = (float)c;
@@ -616,6 +695,33 @@ gi_status set_smem(K kernel, int bytes) {
 }
 
 }  // namespace edt
+
+gi_status launch_edt_mean_filter(gi_context* ctx, const float camera_mv[16], const float* d_image,
+                                 const float* d_pos, int W, int H, int order, float* d_out, cudaStream_t st) {
+    using namespace edt;
+    gi_status s = ensure_buffer(reinterpret_cast<void**>(&ctx->d_edt_meanx), &ctx->cap_edt_meanx,
+                                (size_t)W * H * sizeof(float4));
+    if (s != GI_OK) return s;
+    MeanArgs a;
+    a.pos = reinterpret_cast<const float4*>(d_pos);
+    a.W = W;
+    a.H = H;
+    a.order = order;
+    // dscreen = 1 / (2 tan(fov / 2)) with the float uniform fov = 45 read by
+    // GLSL's tan as radians (MyGLGeometryViewer.cpp:6,119-120)
+    a.dscreen = 1.0f / (2.0f * (float)std::tan((double)(45.0f / 2.0f)));
+    for (int k = 0; k < 16; ++k) a.mv[k] = camera_mv[k];
+    const dim3 grid((W + 31) / 32, (H + 7) / 8);
+    a.image = reinterpret_cast<const float4*>(d_image);
+    a.out = reinterpret_cast<float4*>(ctx->d_edt_meanx);
+    k_edt_mean_filter<false><<<grid, 256, 0, st>>>(a);
+    a.image = a.out;
+    a.out = reinterpret_cast<float4*>(d_out);
+    k_edt_mean_filter<true><<<grid, 256, 0, st>>>(a);
+    ctx->launches += 2;
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "EDT mean filter launch");
+}
 
 gi_status pba_check_shape(int W, int H, int m1, int m2, int m3, const char* who) {
     const std::string w(who);

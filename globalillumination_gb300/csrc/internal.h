@@ -110,6 +110,9 @@ struct gi_context {
     // PBA distance transform: phase-1 site row per pixel (int16)
     int16_t* d_pba_cols = nullptr;
     size_t cap_pba_cols = 0;
+    // the x pass of the EDT mean filter (float4 per pixel)
+    void* d_edt_meanx = nullptr;
+    size_t cap_edt_meanx = 0;
     // nearest site per pixel (short2) when the caller does not keep it
     void* d_pba_near = nullptr;
     size_t cap_pba_near = 0;

@@ -81,6 +81,11 @@ gi_status launch_pba(gi_context* ctx, const int16_t* d_sites, const float* d_ima
                      int W, int H, int m1, int m2, int m3, float penumbra, float intensity, int16_t* d_nearest,
                      float* d_out4, cudaStream_t st);
 
+// MeanFilter.frag's two passes over an EDT image (x into context scratch,
+// then y into d_out), float4 images of W x H.
+gi_status launch_edt_mean_filter(gi_context* ctx, const float camera_mv[16], const float* d_image,
+                                 const float* d_pos, int W, int H, int order, float* d_out, cudaStream_t st);
+
 // Filtered moment maps (GI_TECH_VSM .. GI_TECH_MSM): the moment map of the
 // S x S light map, its 2 x 2 box levels down to the W x W window, the
 // separable 7-tap blur; *filtered = the blurred map (float4, W x W).

@@ -468,6 +468,19 @@ def pba_chain_rows(ctx: Context, reset: bool = False) -> int:
     return int(n.value)
 
 
+def edt_mean_filter(ctx: Context, params: ShadowParams, frame: Frame, image, pos, out, width: int, height: int,
+                    order: int = 7, stream=None):
+    """MeanFilter.frag's x and y passes over the EDT image (float4) into out (float4)."""
+    import torch
+
+    for t, what in ((image, "image"), (pos, "pos"), (out, "out")):
+        _need(t, 4 * width * height, torch.float32, what)
+    p = params.to_c(frame)
+    check(_lib().gi_edt_mean_filter(ctx.handle, C.byref(p), _ptr(image), _ptr(pos), width, height, int(order),
+                                    _ptr(out), _stream_ptr(stream)), "gi_edt_mean_filter")
+    return out
+
+
 def edt_inputs(ctx: Context, params: ShadowParams, frame: Frame, pos, nrm, vis, width: int, height: int, image,
                position, stream=None):
     """The SMSR shaders' EDTSM outputs: hard-shadow image and clip position (float4 each)."""

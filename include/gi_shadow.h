@@ -407,6 +407,19 @@ gi_status gi_edt_soft_shadows(gi_context* ctx, const float* d_image, const float
  * context's device. */
 gi_status gi_pba_chain_rows(gi_context* ctx, uint32_t* rows, int reset);
 
+/* The screen-space mean filter that ends filterHardShadowsUsingEDT
+ * (main.cpp:424-447, Shaders/Filter/MeanFilter.frag): an x pass and a y pass
+ * over d_image (the EDT output: filtered shadow in channel 0, depth in
+ * channel 1), each averaging a depth-aware window whose half-width is
+ * dscreen * order * 50 / (2 deye) for the pixel's eye depth (vis->camera_mv
+ * and the G-buffer d_pos); d_out (float4, may not alias d_image) receives
+ * (mean, depth, 0, 0), background (0, 0, 0, 1).  order is the Gaussian
+ * filter order (7 in the reference).  The first pass reads GL_NEAREST, the
+ * second bilinearly at level 0. */
+gi_status gi_edt_mean_filter(gi_context* ctx, const gi_vis_params* vis, const float* d_image,
+                             const float* d_pos, int width, int height, int order, float* d_out,
+                             void* stream);
+
 /* The images gi_edt_soft_shadows reads, as the SMSR shaders write them in
  * EDTSM mode (NonConservativeSMSR.frag:367-397, ConservativeSMSR.frag:
  * 215-245) from the G-buffer (d_pos, d_nrm float4) and the visibility of

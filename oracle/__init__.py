@@ -34,6 +34,7 @@ def load():
         lib.or_edt_normalize.argtypes = [vp, vp, vp, i, i, f, f, vp]
         lib.or_edt_soft_shadows.argtypes = [vp, vp, i, i, i, i, i, f, f, vp, vp, vp, i]
         lib.or_edt_inputs.argtypes = [vp, vp, vp, vp, vp, i, i, vp, vp]
+        lib.or_edt_mean_filter.argtypes = [vp, vp, vp, i, i, i, vp]
         for fn in (lib.or_shadow_map, lib.or_gbuffer, lib.or_visibility, lib.or_shadow_volume_counts):
             fn.restype = None
         _lib = lib
@@ -173,3 +174,11 @@ def edt_inputs(vis_params, camera_mvp, pos, nrm, vis, width, height):
     load().or_edt_inputs(C.addressof(vis_params), cm.ctypes.data, ps.ctypes.data, ns.ctypes.data, vs.ctypes.data,
                          width, height, image.ctypes.data, position.ctypes.data)
     return image, position
+
+
+def edt_mean_filter(vis_params, image, pos, width, height, order=7):
+    im, ps = _f32(image), _f32(pos)
+    out = np.empty((height, width, 4), np.float32)
+    load().or_edt_mean_filter(C.addressof(vis_params), im.ctypes.data, ps.ctypes.data, width, height, order,
+                              out.ctypes.data)
+    return out

@@ -2224,6 +2224,9 @@ const float* texel(const float* img, int W, int H, int x, int y) {
 
 float plerp(float v0, float v1, float t) { return (1 - t) * v0 + t * v1; }
 
+// MeanFilter.frag's linearize: all-float GLSL (zNear 1, zFar 1000)
+float gl_linearize_f(float depth) { return 2.0f / (1001.0f - depth * 999.0f); }
+
 }  // namespace pba
 }  // namespace
 
@@ -2326,5 +2329,78 @@ extern "C" void or_edt_inputs(const gi_vis_params* p, const float camera_mvp[16]
         po[1] = cp.y;
         po[2] = cp.z;
         po[3] = cp.w;
+    }
+}
+
+// MeanFilter.frag's x and y passes (ShadowMapping/src/main.cpp:424-447) with
+// the same choices as the CUDA path: centre = (i + 0.5) / size, pass 1
+// GL_NEAREST (texel floor(u * size)), pass 2 bilinear at level 0 along the
+// filtered axis, zero border, at most 2049 samples, dscreen from tan(22.5)
+// (GLSL's tan of the 45-degree fov uniform, taken as radians).
+extern "C" void or_edt_mean_filter(const gi_vis_params* p, const float* image, const float* pos, int W, int H,
+                                   int order, float* out) {
+    const float dscreen = 1.0f / (2.0f * (float)std::tan((double)(45.0f / 2.0f)));
+    const float* m = p->camera_mv;
+    std::vector<float> xpass((size_t)W * H * 4);
+    for (int pass = 0; pass < 2; ++pass) {
+        const bool vertical = pass == 1;
+        const float* in = vertical ? xpass.data() : image;
+        float* dst = vertical ? out : xpass.data();
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                const size_t q = (size_t)y * W + x;
+                const float* v = pos + 4 * q;
+                float* o = dst + 4 * q;
+                if (v[0] == 0.0f) {
+                    o[0] = o[1] = o[2] = 0.0f;
+                    o[3] = 1.0f;
+                    continue;
+                }
+                const float* color = in + 4 * q;
+                const float ez = m[2] * v[0] + m[6] * v[1] + m[10] * v[2] + m[14] * v[3];
+                const float deye = -ez;
+                const float kc = (dscreen * (float)order * 50.0f) / (deye * 2.0f);
+                const float step = vertical ? 1.0f / (float)H : 1.0f / (float)W;
+                const float cs = ((float)(vertical ? y : x) + 0.5f) / (float)(vertical ? H : W);
+                const float Lc = pba::gl_linearize_f(color[1]);
+                const float size = (float)(vertical ? H : W);
+                float sum = 0.0f;
+                int count = 0;
+                for (float sample = -kc; sample <= kc && count < 2049; sample = sample + 1.0f) {
+                    const float u = cs + sample * step;
+                    float r = 0.0f, g = 0.0f;
+                    if (!vertical) {
+                        const float fi = std::floor(u * size);
+                        if (fi >= 0.0f && fi < size) {
+                            const float* t = in + 4 * ((size_t)y * W + (int)fi);
+                            r = t[0];
+                            g = t[1];
+                        }
+                    } else {
+                        const float uu = u * size - 0.5f;
+                        const float f0 = std::floor(uu), w1 = uu - f0, w0 = 1.0f - w1;
+                        const int j0 = (int)f0;
+                        float t0r = 0.0f, t0g = 0.0f, t1r = 0.0f, t1g = 0.0f;
+                        if (j0 >= 0 && j0 < H) {
+                            t0r = in[4 * ((size_t)j0 * W + x)];
+                            t0g = in[4 * ((size_t)j0 * W + x) + 1];
+                        }
+                        if (j0 + 1 >= 0 && j0 + 1 < H) {
+                            t1r = in[4 * ((size_t)(j0 + 1) * W + x)];
+                            t1g = in[4 * ((size_t)(j0 + 1) * W + x) + 1];
+                        }
+                        r = w0 * t0r + w1 * t1r;
+                        g = w0 * t0g + w1 * t1g;
+                    }
+                    if (r == 0.0f || std::fabs(pba::gl_linearize_f(g) - Lc) >= 0.0005f) r = color[0];
+                    sum = sum + r;
+                    ++count;
+                }
+                sum = sum / (float)count;
+                o[0] = sum;
+                o[1] = color[1];
+                o[2] = 0.0f;
+                o[3] = 0.0f;
+            }
     }
 }

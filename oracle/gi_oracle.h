@@ -87,6 +87,10 @@ void or_edt_soft_shadows(const float* image, const float* position, int W, int H
                          float penumbra, float intensity, int16_t* sites, int16_t* nearest, float* out4,
                          int threads);
 
+/* MeanFilter.frag's x and y passes over an EDT image (float4), out float4. */
+void or_edt_mean_filter(const gi_vis_params* p, const float* image, const float* pos, int W, int H, int order,
+                        float* out);
+
 /* The SMSR shaders' EDTSM outputs from the G-buffer and visibility. */
 void or_edt_inputs(const gi_vis_params* p, const float camera_mvp[16], const float* pos, const float* nrm,
                    const float* vis, int W, int H, float* image, float* position);

@@ -159,3 +159,34 @@ def test_site_threshold_is_the_references_double_comparison():
     s_out = oracle.edt_sites(threshold_image(b_out))
     assert (s_in[:, 3:5, 0] != MARKER).all() and (s_in[:, :3, 0] == MARKER).all()
     assert (s_out[..., 0] == MARKER).all()
+
+
+def test_mean_filter_known_answers():
+    # 32 x 32 geometry at eye depth 50 (identity MV, vertex z = -50): the
+    # half-width is 50 * 7 / (2 tan(22.5) * 2 * 50) = 3.13 samples, so 7
+    # samples per pass.  A 0.25 / 1.0 step at one depth is averaged across
+    # the step, a region at another depth is left alone, background keeps
+    # (0, 0, 0, 1).
+    import globalillumination_gb300 as gi
+    from globalillumination_gb300 import _capi as api
+
+    W = H = 32
+    p = gi.ShadowParams.defaults(api.GI_TECH_SMSR_NONCONSERVATIVE)
+    fr = gi.Frame(*(np.eye(4, dtype=np.float32).reshape(-1),) * 4, np.eye(3, dtype=np.float32).reshape(-1),
+                  np.zeros(3, np.float32))
+    pos = np.zeros((H, W, 4), np.float32)
+    pos[...] = (1.0, 1.0, -50.0, 1.0)
+    pos[0, 0, 0] = 0.0  # one background pixel
+    img = np.zeros((H, W, 4), np.float32)
+    img[..., 0] = np.where(np.arange(W) < W // 2, 0.25, 1.0)[None, :]
+    img[..., 1] = 0.98
+    img[:, 28:, 1] = 0.5  # a region far in front: its own depth class
+    out = oracle.edt_mean_filter(p.to_c(fr), img, pos, W, H)
+    assert tuple(out[0, 0]) == (0.0, 0.0, 0.0, 1.0)
+    assert out[10, 5, 0] == pytest.approx(0.25) and out[10, 5, 1] == np.float32(0.98)
+    row = out[10, :, 0]
+    assert 0.25 < row[W // 2 - 1] < row[W // 2] < 1.0  # the step is smoothed over about 3 texels
+    assert row[W // 2 - 5] == pytest.approx(0.25) and row[W // 2 + 4] == pytest.approx(1.0)
+    # depth 0.5 pixels only average among themselves (away from the top and
+    # bottom rows, where the bilinear y pass blends in the zero border)
+    assert (out[5:27, 28:, 0] == 1.0).all()

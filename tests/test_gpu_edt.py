@@ -159,6 +159,13 @@ def test_edtsm_on_a_rendered_frame(cuda_ctx, tech):
     np.testing.assert_array_equal(nn, rnn)
     np.testing.assert_array_equal(out[..., :2].view(np.uint32), ref[..., :2].view(np.uint32))
     assert (sites[..., 0] != MARKER).sum() > 100, "the frame's shadow edges must produce sites"
+    # the screen-space mean filter that ends filterHardShadowsUsingEDT
+    t_out = torch.from_numpy(out).cuda()
+    mean = torch.empty_like(t_out)
+    gi.edt_mean_filter(cuda_ctx, p, fr, t_out, bufs.pos, mean, W, H)
+    torch.cuda.synchronize()
+    ref_mean = oracle.edt_mean_filter(p.to_c(fr), out, bufs.pos.cpu().numpy(), W, H)
+    np.testing.assert_array_equal(mean.cpu().numpy().view(np.uint32), ref_mean.view(np.uint32))
 
 
 def test_shape_validation(cuda_ctx):
