@@ -206,7 +206,21 @@ __device__ __forceinline__ bool inside3(const Edges& e, const int64_t E[3]) {
 // (|h| < 2^23) and 0 <= l < 2^24, both exact in FP32; h * 2^24 is exact and
 // the one addition rounds once, giving the correctly rounded v, the same
 // value as the (float) cast.
+//
+// Below 2^45 in magnitude the two halves are split at bit 23 instead and
+// converted with exponent tricks rather than conversion instructions:
+// 12582912 + h (|h| < 2^22) and 8388608 + l (0 <= l < 2^23) are exact FP32
+// integers whose bit patterns are plain integer sums, so subtracting the
+// constants recovers h and l exactly; h * 2^23 + l rounds once, to the same
+// correctly rounded v.
 __device__ __forceinline__ float i2f(int64_t v) {
+    if (v >= -(1LL << 45) && v < (1LL << 45)) {
+        const int h = (int)(v >> 23);
+        const int l = (int)(v & 0x7FFFFF);
+        const float fh = __int_as_float(0x4B400000 + h) - 12582912.0f;
+        const float fl = __int_as_float(0x4B000000 | l) - 8388608.0f;
+        return fh * 8388608.0f + fl;
+    }
     if (v >= -(1LL << 47) && v < (1LL << 47)) {
         const int h = (int)(v >> 24);
         const int l = (int)(v & 0xFFFFFF);
