@@ -1377,80 +1377,93 @@ __device__ __forceinline__ void rec_emit(const TierArgs& a, const BRec& r, int x
 
 // Tiny records: one thread each over the bounding box.
 template <int MODE>
-__global__ void __launch_bounds__(128) k_tiny(TierArgs a) {
-    const unsigned n = a.ctr[1];
-    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const BRec r = a.recs[a.tiny[i]];
-        int64_t A[3], B[3];
-        bool tl[3];
-        rec_edges(r, A, B, tl);
-        for (int y = r.y0; y <= (int)r.y1; ++y) {
-            const int64_t py = (int64_t)y * kSub + kSub / 2;
-            for (int x = r.x0; x <= (int)r.x1; ++x) {
-                const int64_t px = (int64_t)x * kSub + kSub / 2;
-                int64_t E[3];
+__device__ __forceinline__ void tiny_record(const TierArgs& a, unsigned i) {
+    const BRec r = a.recs[a.tiny[i]];
+    int64_t A[3], B[3];
+    bool tl[3];
+    rec_edges(r, A, B, tl);
+    for (int y = r.y0; y <= (int)r.y1; ++y) {
+        const int64_t py = (int64_t)y * kSub + kSub / 2;
+        for (int x = r.x0; x <= (int)r.x1; ++x) {
+            const int64_t px = (int64_t)x * kSub + kSub / 2;
+            int64_t E[3];
 #pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    const int ia = (k + 1) % 3;
-                    E[k] = A[k] * (py - r.Y[ia]) - B[k] * (px - r.X[ia]);
-                }
-                const bool in = (E[0] > 0 || (E[0] == 0 && tl[0])) && (E[1] > 0 || (E[1] == 0 && tl[1])) &&
-                                (E[2] > 0 || (E[2] == 0 && tl[2]));
-                if (in) rec_emit<MODE>(a, r, x, y, i2f(E[1]), i2f(E[2]));
+            for (int k = 0; k < 3; ++k) {
+                const int ia = (k + 1) % 3;
+                E[k] = A[k] * (py - r.Y[ia]) - B[k] * (px - r.X[ia]);
             }
+            const bool in = (E[0] > 0 || (E[0] == 0 && tl[0])) && (E[1] > 0 || (E[1] == 0 && tl[1])) &&
+                            (E[2] > 0 || (E[2] == 0 && tl[2]));
+            if (in) rec_emit<MODE>(a, r, x, y, i2f(E[1]), i2f(E[2]));
         }
     }
 }
 
 // Warp-sized records: one warp per record, lanes over the bounding box.
 template <int MODE>
-__global__ void __launch_bounds__(256) k_coop(TierArgs a) {
-    const unsigned n = a.ctr[2];
+__device__ __forceinline__ void coop_record(const TierArgs& a, unsigned i, int lane) {
+    const BRec r = a.recs[a.coop[i]];
+    const int w = r.x1 - r.x0 + 1, h = r.y1 - r.y0 + 1, npx = w * h;
+    // p / w by a reciprocal: (p + 1/2) / w stays at least 1/(2w) >= 2^-11
+    // from an integer and the product errs by under 2^-13 for p < 1024.
+    const float inv_w = 1.0f / (float)w;
+    int64_t A[3], B[3], E0[3];
+    bool tl[3];
+    rec_edges(r, A, B, tl);
+    const int64_t cx = (int64_t)r.x0 * kSub + kSub / 2, cy = (int64_t)r.y0 * kSub + kSub / 2;
+    bool fits32 = true;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int ia = (k + 1) % 3;
+        E0[k] = A[k] * (cy - r.Y[ia]) - B[k] * (cx - r.X[ia]);
+        const int64_t bound = abs(E0[k]) + abs(A[k]) * (int64_t)(h - 1) * kSub + abs(B[k]) * (int64_t)(w - 1) * kSub;
+        fits32 &= bound < (1LL << 31);
+    }
+    for (int p = lane; p < npx; p += 32) {
+        const int dy = (int)(((float)p + 0.5f) * inv_w);
+        const int dx = p - dy * w;
+        bool in;
+        float fe1, fe2;
+        if (fits32) {
+            int e[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                e[k] = (int)E0[k] + (int)A[k] * (dy << kSubBits) - (int)B[k] * (dx << kSubBits);
+            in = (e[0] > 0 || (e[0] == 0 && tl[0])) && (e[1] > 0 || (e[1] == 0 && tl[1])) &&
+                 (e[2] > 0 || (e[2] == 0 && tl[2]));
+            fe1 = (float)e[1];
+            fe2 = (float)e[2];
+        } else {
+            int64_t E[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                E[k] = E0[k] + A[k] * (int64_t)(dy << kSubBits) - B[k] * (int64_t)(dx << kSubBits);
+            in = (E[0] > 0 || (E[0] == 0 && tl[0])) && (E[1] > 0 || (E[1] == 0 && tl[1])) &&
+                 (E[2] > 0 || (E[2] == 0 && tl[2]));
+            fe1 = i2f(E[1]);
+            fe2 = i2f(E[2]);
+        }
+        if (in) rec_emit<MODE>(a, r, r.x0 + dx, r.y0 + dy, fe1, fe2);
+    }
+}
+
+// The warp-sized and tiny records in one launch, so both tiers share the
+// SMs instead of running one after the other: warps stride over a joint
+// list of units, first the warp records (one unit each, the larger and
+// more uneven work), then the tiny records in units of 32 (one per lane).
+// Their atomic updates commute, so the order does not change the result.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_tiny_coop(TierArgs a) {
+    const unsigned ncoop = a.ctr[2], ntiny = a.ctr[1];
+    const unsigned units = ncoop + (ntiny + 31) / 32;
     const int lane = threadIdx.x & 31;
     const unsigned nwarps = gridDim.x * (blockDim.x >> 5);
-    for (unsigned i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += nwarps) {
-        const BRec r = a.recs[a.coop[i]];
-        const int w = r.x1 - r.x0 + 1, h = r.y1 - r.y0 + 1, npx = w * h;
-        // p / w by a reciprocal: (p + 1/2) / w stays at least 1/(2w) >= 2^-11
-        // from an integer and the product errs by under 2^-13 for p < 1024.
-        const float inv_w = 1.0f / (float)w;
-        int64_t A[3], B[3], E0[3];
-        bool tl[3];
-        rec_edges(r, A, B, tl);
-        const int64_t cx = (int64_t)r.x0 * kSub + kSub / 2, cy = (int64_t)r.y0 * kSub + kSub / 2;
-        bool fits32 = true;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const int ia = (k + 1) % 3;
-            E0[k] = A[k] * (cy - r.Y[ia]) - B[k] * (cx - r.X[ia]);
-            const int64_t bound = abs(E0[k]) + abs(A[k]) * (int64_t)(h - 1) * kSub + abs(B[k]) * (int64_t)(w - 1) * kSub;
-            fits32 &= bound < (1LL << 31);
-        }
-        for (int p = lane; p < npx; p += 32) {
-            const int dy = (int)(((float)p + 0.5f) * inv_w);
-            const int dx = p - dy * w;
-            bool in;
-            float fe1, fe2;
-            if (fits32) {
-                int e[3];
-#pragma unroll
-                for (int k = 0; k < 3; ++k)
-                    e[k] = (int)E0[k] + (int)A[k] * (dy << kSubBits) - (int)B[k] * (dx << kSubBits);
-                in = (e[0] > 0 || (e[0] == 0 && tl[0])) && (e[1] > 0 || (e[1] == 0 && tl[1])) &&
-                     (e[2] > 0 || (e[2] == 0 && tl[2]));
-                fe1 = (float)e[1];
-                fe2 = (float)e[2];
-            } else {
-                int64_t E[3];
-#pragma unroll
-                for (int k = 0; k < 3; ++k)
-                    E[k] = E0[k] + A[k] * (int64_t)(dy << kSubBits) - B[k] * (int64_t)(dx << kSubBits);
-                in = (E[0] > 0 || (E[0] == 0 && tl[0])) && (E[1] > 0 || (E[1] == 0 && tl[1])) &&
-                     (E[2] > 0 || (E[2] == 0 && tl[2]));
-                fe1 = i2f(E[1]);
-                fe2 = i2f(E[2]);
-            }
-            if (in) rec_emit<MODE>(a, r, r.x0 + dx, r.y0 + dy, fe1, fe2);
+    for (unsigned u = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); u < units; u += nwarps) {
+        if (u < ncoop) {
+            coop_record<MODE>(a, u, lane);
+        } else {
+            const unsigned i = (u - ncoop) * 32 + lane;
+            if (i < ntiny) tiny_record<MODE>(a, i);
         }
     }
 }
@@ -1715,8 +1728,9 @@ static gi_status run_binned(gi_context* ctx, dev::RasterArgs& r, int mode, cudaS
 }
 
 // Tiered pass (light map, G-buffer keys): setup, large-record scan, base
-// layer (huge records + clear), tiny / warp / tile rasterisation with
-// atomics, spill (7 launches + 1 memset, stream-ordered).
+// layer (huge records + clear), tiny and warp records in one launch, tile
+// rasterisation, spill; atomics after the base layer (6 launches + 1
+// memset, stream-ordered).
 static gi_status run_tiered(gi_context* ctx, dev::RasterArgs& r, int mode, cudaStream_t st) {
     const size_t prims = (size_t)std::max(r.num_prims, 0);
     const size_t rec_cap = 2 * prims + 4096;
@@ -1758,20 +1772,18 @@ static gi_status run_tiered(gi_context* ctx, dev::RasterArgs& r, int mode, cudaS
         if (prims) dev::k_tier_setup<dev::MODE_DEPTH><<<gsetup, 128, 0, st>>>(a);
         dev::k_large_scan<<<1, 1024, 0, st>>>(a);
         dev::k_base<dev::MODE_DEPTH><<<gbase, 256, 0, st>>>(a);
-        dev::k_tiny<dev::MODE_DEPTH><<<sms * 8, 128, 0, st>>>(a);
-        dev::k_coop<dev::MODE_DEPTH><<<sms * 8, 256, 0, st>>>(a);
+        dev::k_tiny_coop<dev::MODE_DEPTH><<<sms * 8, 256, 0, st>>>(a);
         dev::k_large_tiles<dev::MODE_DEPTH><<<sms * 8, 256, 0, st>>>(a);
         dev::k_tier_spill<dev::MODE_DEPTH><<<sms * 2, 128, 0, st>>>(a);
     } else {
         if (prims) dev::k_tier_setup<dev::MODE_VKEY><<<gsetup, 128, 0, st>>>(a);
         dev::k_large_scan<<<1, 1024, 0, st>>>(a);
         dev::k_base<dev::MODE_VKEY><<<gbase, 256, 0, st>>>(a);
-        dev::k_tiny<dev::MODE_VKEY><<<sms * 8, 128, 0, st>>>(a);
-        dev::k_coop<dev::MODE_VKEY><<<sms * 8, 256, 0, st>>>(a);
+        dev::k_tiny_coop<dev::MODE_VKEY><<<sms * 8, 256, 0, st>>>(a);
         dev::k_large_tiles<dev::MODE_VKEY><<<sms * 8, 256, 0, st>>>(a);
         dev::k_tier_spill<dev::MODE_VKEY><<<sms * 2, 128, 0, st>>>(a);
     }
-    ctx->launches += prims ? 7 : 6;
+    ctx->launches += prims ? 6 : 5;
     e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "tiered raster launch");
 }
