@@ -45,6 +45,11 @@ Extra legs in the same line (not the headline):
               frames per technique (light map, moment map, box level,
               two blur passes, G-buffer, lookups) beside the hard-shadow
               frame, L2 flushed before each
+  soft_moment_shadows  SoftShadowMapping's moment soft shadows (SAVSM,
+              VSSM, ESSM, MSSM, each with and without the summed-area
+              table) at its 1280 x 720 window over a 1024^2 map, beside
+              the PCSS grid frame, and the moment map + SAT build alone at
+              1024^2 and 2048^2
   surrogate   the learned PCSS surrogate (BF16 U-Net on the tcgen05
               convolution kernels) trained here on freshly rendered
               frames, then its 1080p frame time, its error against the
@@ -91,6 +96,7 @@ def parse_args():
     ap.add_argument("--no-area-light", action="store_true", help="skip the 289-sample area-light ground-truth leg")
     ap.add_argument("--no-edt", action="store_true", help="skip the EDT-filtered hard shadows leg")
     ap.add_argument("--no-moments", action="store_true", help="skip the moment shadow map leg")
+    ap.add_argument("--no-soft-moments", action="store_true", help="skip the moment soft shadow leg")
     ap.add_argument("--surrogate-frames", type=int, default=8000,
                     help="training frames (one 256^2 crop each, batch 16) for the surrogate leg")
     ap.add_argument("--profile", action="store_true",
@@ -715,6 +721,71 @@ def run_moments(args, ctx, stream, local, flush):
     return out
 
 
+def run_soft_moments(args, ctx, stream, local, flush):
+    """SAVSM / VSSM / ESSM / MSSM frames in SoftShadowMapping's 1280x720-over-1024^2 setup, plus the
+    light-side map builds (moment map + summed-area table) at 1024^2 and 2048^2."""
+    import torch
+
+    import numpy as np
+
+    import globalillumination_gb300 as gi
+    from globalillumination_gb300 import _capi as api, scenes
+
+    w = scenes.pcss_1080p(width=1280, height=720, map_size=1024)
+    fr = gi.frame_setup(w.light, w.camera)
+    S, W, H = w.map_params.width, w.camera.width, w.camera.height
+    w.scene.upload(ctx, stream)
+    bufs = gi.allocate_frame(S, S, W, H, local)
+
+    def timed(fn, n=30):
+        for _ in range(5):
+            fn()
+        torch.cuda.synchronize()
+        ev = []
+        for r in range(n):
+            flush.fill_(float(r))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            ev.append((e0, e1))
+        torch.cuda.synchronize()
+        return statistics.median(a.elapsed_time(b) for a, b in ev)
+
+    out = {"workload": "pcss_1080p scene at SoftShadowMapping's 1280x720 window over a 1024^2 map (light radius "
+                       "0.25, blocker gate off), blocker 7 / kernel 7 taps; frames with and without the SAT",
+           "ms_per_frame": {}, "shadowed_fraction": {}}
+    for name, tech, sat in (("pcss_grid", api.GI_TECH_PCSS_GRID, False), ("savsm", api.GI_TECH_SAVSM, False),
+                            ("savsm_sat", api.GI_TECH_SAVSM, True), ("vssm", api.GI_TECH_VSSM, False),
+                            ("vssm_sat", api.GI_TECH_VSSM, True), ("essm", api.GI_TECH_ESSM, False),
+                            ("essm_sat", api.GI_TECH_ESSM, True), ("mssm", api.GI_TECH_MSSM, False),
+                            ("mssm_sat", api.GI_TECH_MSSM, True)):
+        p = gi.ShadowParams.defaults(tech)
+        p.summed_area_table = sat
+        p.light_radius = w.params.light_radius
+        p.pcss_min_blocker_depth = 0.0
+        out["ms_per_frame"][name] = timed(lambda: gi.render_frame(ctx, w.scene, fr, w.map_params, p, W, H, bufs,
+                                                                  stream))
+        v = bufs.vis
+        out["shadowed_fraction"][name] = float(((v > 0.0) & (v < 1.0)).float().mean())
+    # the light-side map alone: moment map + log2(S) SAT iterations, written
+    # into a caller buffer; algorithmic bytes = the depth read (4 S^2) and the
+    # table written (16 S^2)
+    peak, peak_kind = measured_hbm_peak()
+    out["sat_build"] = {}
+    for side in (1024, 2048):
+        depth = torch.rand(side * side, device="cuda", generator=torch.Generator("cuda").manual_seed(side)) * 0.1 + 0.9
+        tab = torch.empty(side * side * 4, device="cuda")
+        p = gi.ShadowParams.defaults(api.GI_TECH_SAVSM)
+        p.summed_area_table = True
+        ms = timed(lambda: gi.soft_moment_map(ctx, p, depth, side, side, tab, stream))
+        alg = 20 * side * side
+        achieved = alg / (ms / 1000.0) / 1e9
+        out["sat_build"][str(side)] = {"ms": ms, "kernels": 1 + int(np.log2(side)), "algorithmic_bytes": alg,
+                                       "achieved_gbs": achieved, "frac_of_" + peak_kind: achieved / peak}
+    return out
+
+
 def measured_bf16_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -945,6 +1016,9 @@ def run_ours(args):
     moments_leg = None
     if not args.no_moments and rank == 0:
         moments_leg = run_moments(args, ctx, stream, local, flush)
+    soft_moments_leg = None
+    if not args.no_soft_moments and rank == 0:
+        soft_moments_leg = run_soft_moments(args, ctx, stream, local, flush)
     edt_leg = None
     if not args.no_edt and rank == 0:
         edt_leg = run_edt(args, ctx, stream, local, flush)
@@ -994,6 +1068,8 @@ def run_ours(args):
             line["edt_soft_shadows"] = edt_leg
         if moments_leg is not None:
             line["moment_shadows"] = moments_leg
+        if soft_moments_leg is not None:
+            line["soft_moment_shadows"] = soft_moments_leg
         if clk and any(r in clk["reasons"] for r in THROTTLE_BAD):
             line["clocks_warning"] = "throttled during the timed region"
         if world == 1 and not args.no_cpu_baseline:

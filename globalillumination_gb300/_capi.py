@@ -50,7 +50,11 @@ GI_TECH_VSM = 12
 GI_TECH_ESM = 13
 GI_TECH_EVSM = 14
 GI_TECH_MSM = 15
-GI_TECH_COUNT = 16
+GI_TECH_SAVSM = 16
+GI_TECH_VSSM = 17
+GI_TECH_ESSM = 18
+GI_TECH_MSSM = 19
+GI_TECH_COUNT = 20
 GI_ACT_NONE = 0
 GI_ACT_RELU = 1
 
@@ -133,6 +137,9 @@ class VisParams(C.Structure):
         ("pcss_min_blocker_depth", C.c_float),
         ("poisson_blocker_taps", C.c_int),
         ("poisson_filter_taps", C.c_int),
+        ("summed_area_table", C.c_int),
+        ("hsm_alpha", C.c_float),
+        ("hsm_beta", C.c_float),
         ("light_mvp_biased", F16),
         ("camera_mv", F16),
         ("normal_matrix", F9),
@@ -193,6 +200,8 @@ _PROTOS = {
     "gi_render_frame": (C.c_int, [_VP, _VP, C.POINTER(MapParams), F16, F16, C.POINTER(VisParams), C.c_int,
                                   C.c_int, _VP, _VP, _VP, _VP, _VP]),
     "gi_poisson_table": (C.c_int, [C.c_int, _VP]),
+    "gi_soft_moment_map": (C.c_int, [_VP, C.POINTER(VisParams), _VP, C.c_int, C.c_int, _VP, _VP]),
+    "gi_hierarchical_shadow_map": (C.c_int, [_VP, C.POINTER(VisParams), _VP, C.c_int, C.c_int, C.c_int, _VP, _VP]),
     "gi_shadow_volume_counts": (C.c_int, [_VP, _VP, F3, C.c_float, F16, C.c_int, C.c_int, C.c_int,
                                           _VP, _VP, _VP]),
     "gi_phong_shade": (C.c_int, [_VP, C.POINTER(VisParams), _VP, _VP, _VP, _VP, C.c_int, C.c_int, _VP, _VP]),

@@ -248,6 +248,8 @@ extern "C" gi_status gi_batch_add_frame(gi_batch* b, const gi_scene* scene, cons
                                                   "gi_batch_add_frame");
             if (st != GI_OK) return st;
         }
+        gi_status sst = gi::soft_moment_check_shape(vis->technique, maps[l].width, maps[l].height, "gi_batch_add_frame");
+        if (sst != GI_OK) return sst;
         f.lights.push_back(lights[l]);
         f.maps.push_back(maps[l]);
         gi_frame_matrices m;

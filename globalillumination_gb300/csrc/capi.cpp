@@ -117,6 +117,7 @@ extern "C" void gi_context_destroy(gi_context* c) {
     cudaFree(c->d_pba_cols);
     cudaFree(c->d_mom);
     cudaFree(c->d_mom_blur);
+    cudaFree(c->d_hsm);
     cudaFree(c->d_pba_near);
     cudaFree(c->d_edt_meanx);
     for (int i = 0; i < 8; ++i) cudaFree(c->bin_buf[i]);
@@ -422,6 +423,10 @@ extern "C" gi_status gi_vis_params_default(int technique, gi_vis_params* p) {
     p->poisson_blocker_taps = 16;
     p->poisson_filter_taps = 32;
     if (technique == GI_TECH_RBSSM) p->kernel_size = 7;  // SoftShadowMapping/src/main.cpp:1450-1455
+    // SAVSM .. MSSM: resetShadowParameters sets kernelSize 7 (main.cpp:1341,
+    // 1433-1449); SAT starts off (:1606) and HSMAlpha / HSMBeta come from
+    // the config keys "ha" / "hb" (default 0, SceneLoader.cpp:8-9)
+    if (technique >= GI_TECH_SAVSM && technique <= GI_TECH_MSSM) p->kernel_size = 7;
     for (int i = 0; i < 4; ++i) {
         p->light_mvp_biased[i * 5] = 1.0f;
         p->camera_mv[i * 5] = 1.0f;
@@ -450,11 +455,13 @@ static gi_status check_vis_params(const gi_vis_params* p) {
         if (p->max_search < 0 || p->max_search > 4096)
             return fail(GI_ERR_INVALID_ARG, "gi_visibility: max_search must be in [0, 4096]");
     }
-    if (t == GI_TECH_PCSS_GRID || t == GI_TECH_PCSS_POISSON || t == GI_TECH_RBSSM) {
+    const bool soft_moment = gi::is_soft_moment_technique(t);
+    if (t == GI_TECH_PCSS_GRID || t == GI_TECH_PCSS_POISSON || t == GI_TECH_RBSSM || soft_moment) {
         if (p->kernel_size < 1 || p->kernel_size > 63)
             return fail(GI_ERR_INVALID_ARG, "gi_visibility: kernel_size must be in [1, 63]");
     }
-    if ((t == GI_TECH_PCSS_GRID || t == GI_TECH_RBSSM) && (p->blocker_search_size < 1 || p->blocker_search_size > 63))
+    if ((t == GI_TECH_PCSS_GRID || t == GI_TECH_RBSSM || soft_moment) &&
+        (p->blocker_search_size < 1 || p->blocker_search_size > 63))
         return fail(GI_ERR_INVALID_ARG, "gi_visibility: blocker_search_size must be in [1, 63]");
     if (t == GI_TECH_PCSS_POISSON &&
         (p->poisson_blocker_taps < 1 || p->poisson_blocker_taps > 64 ||
@@ -473,6 +480,7 @@ extern "C" gi_status gi_visibility(gi_context* ctx, const gi_vis_params* p, cons
     if (st == GI_OK) st = check_vis_params(p);
     if (st == GI_OK && gi::is_moment_technique(p->technique))
         st = gi::moment_check_shape(map_w, map_h, W, H, "gi_visibility");
+    if (st == GI_OK) st = gi::soft_moment_check_shape(p->technique, map_w, map_h, "gi_visibility");
     if (st == GI_OK) st = check_device(ctx);
     if (st != GI_OK) return st;
     return gi::launch_visibility(ctx, p, d_depth, map_w, map_h, d_pos, d_nrm, d_vis, W, H,
@@ -492,6 +500,7 @@ extern "C" gi_status gi_render_frame(gi_context* ctx, const gi_scene* s, const g
     if (st == GI_OK) st = check_vis_params(vp);
     if (st == GI_OK && gi::is_moment_technique(vp->technique))
         st = gi::moment_check_shape(mp->width, mp->height, W, H, "gi_render_frame");
+    if (st == GI_OK) st = gi::soft_moment_check_shape(vp->technique, mp->width, mp->height, "gi_render_frame");
     if (st != GI_OK) return st;
     if (mp->bias_mode < GI_BIAS_NONE || mp->bias_mode > GI_BIAS_POLYGON_OFFSET)
         return fail(GI_ERR_INVALID_ARG, "gi_render_frame: bad bias_mode");
@@ -718,6 +727,45 @@ extern "C" gi_status gi_surrogate_finish(gi_context* ctx, const gi_scene* s, int
         return fail(GI_ERR_INVALID_ARG, "gi_surrogate_finish: call gi_surrogate_features for this frame first");
     return gi::launch_surrogate_finish(ctx, vp, d_depth, map_w, map_h, s, camera_mvp, W, H, d_head, head_stride,
                                        d_feat, err_threshold, d_vis, d_fallback, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" gi_status gi_soft_moment_map(gi_context* ctx, const gi_vis_params* vis, const float* d_depth, int map_w,
+                                        int map_h, float* d_out, void* stream) {
+    if (!ctx || !vis || !d_depth || !d_out) return fail(GI_ERR_INVALID_ARG, "gi_soft_moment_map: NULL argument");
+    if (!gi::is_soft_moment_technique(vis->technique))
+        return fail(GI_ERR_INVALID_ARG, "gi_soft_moment_map: technique must be SAVSM, VSSM, ESSM or MSSM");
+    gi_status st = check_image(map_w, map_h, "gi_soft_moment_map");
+    if (st == GI_OK) st = check_device(ctx);
+    if (st != GI_OK) return st;
+    if (reinterpret_cast<uintptr_t>(d_out) % 16 != 0)
+        return fail(GI_ERR_INVALID_ARG, "gi_soft_moment_map: d_out must be 16-byte aligned");
+    const float4* m = nullptr;
+    return gi::launch_soft_moment_map(ctx, vis, d_depth, map_w, map_h, static_cast<cudaStream_t>(stream),
+                                      reinterpret_cast<float4*>(d_out), &m);
+}
+
+extern "C" gi_status gi_hierarchical_shadow_map(gi_context* ctx, const gi_vis_params* vis, const float* d_depth,
+                                                int map_w, int map_h, int level, float* d_out, void* stream) {
+    if (!ctx || !vis || !d_depth || !d_out)
+        return fail(GI_ERR_INVALID_ARG, "gi_hierarchical_shadow_map: NULL argument");
+    gi_status st = check_image(map_w, map_h, "gi_hierarchical_shadow_map");
+    if (st != GI_OK) return st;
+    int m = 0;
+    while ((1 << m) < map_w) ++m;
+    if (map_w != map_h || (1 << m) != map_w)
+        return fail(GI_ERR_UNSUPPORTED, "gi_hierarchical_shadow_map: needs a square power-of-two map");
+    // renderHSM writes levels 1 .. log2(width) - 1 after PrepareMinMax's level 0
+    if (level < 0 || (level > 0 && level >= m))
+        return fail(GI_ERR_INVALID_ARG, "gi_hierarchical_shadow_map: level must be 0 or in [1, log2(width))");
+    st = check_device(ctx);
+    if (st != GI_OK) return st;
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    const float2* lv = nullptr;
+    st = gi::launch_hsm(ctx, vis, d_depth, map_w, map_h, level, cs, &lv);
+    if (st != GI_OK) return st;
+    const size_t n = (size_t)(map_w >> level) * (map_h >> level);
+    const cudaError_t e = cudaMemcpyAsync(d_out, lv, n * sizeof(float2), cudaMemcpyDeviceToDevice, cs);
+    return e == cudaSuccess ? GI_OK : gi::fail_cuda(e, "gi_hierarchical_shadow_map: copy");
 }
 
 extern "C" gi_status gi_poisson_table(int n, float* xy) {

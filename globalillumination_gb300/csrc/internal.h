@@ -107,6 +107,8 @@ struct gi_context {
     size_t cap_mom = 0;
     void* d_mom_blur = nullptr;
     size_t cap_mom_blur = 0;
+    void* d_hsm = nullptr;  // min-max shadow map levels (float2)
+    size_t cap_hsm = 0;
     // PBA distance transform: phase-1 site row per pixel (int16)
     int16_t* d_pba_cols = nullptr;
     size_t cap_pba_cols = 0;

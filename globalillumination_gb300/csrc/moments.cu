@@ -1,4 +1,6 @@
-// moments.cu -- filtered moment shadow maps (VSM, ESM, EVSM, MSM) for sm_103a.
+// moments.cu -- moment shadow maps for sm_103a: ShadowMapping's filtered
+// maps (VSM, ESM, EVSM, MSM) and SoftShadowMapping's moment soft shadows
+// (SAVSM, VSSM, ESSM, MSSM: moment map, summed-area table, min-max levels).
 //
 // The reference renders a moment map instead of a depth map for these
 // techniques, blurs it into a window-size target and samples the blurred
@@ -27,7 +29,13 @@
 //   k_mip_box       one further 2 x 2 box level
 //   k_moment_blur   GaussianFilter.frag (VSM, EVSM, MSM) or
 //                   LogGaussianFilter.frag (ESM), one direction per launch
+//   k_soft_moments  SoftShadowMapping's Moments.frag / Exponential.frag
+//   k_sat_level     one horizontal + vertical SAT iteration
+//   k_hsm_first / k_hsm_next / k_hsm_level0
+//                   PrepareMinMax.frag and MinMax.frag levels
 #include <cuda_runtime.h>
+
+#include <cmath>
 
 #include "internal.h"
 #include "raster.h"
@@ -161,9 +169,254 @@ __global__ void __launch_bounds__(256) k_moment_blur(const float4* __restrict__ 
     out[(size_t)y * N + x] = r;
 }
 
+// ---- moment soft shadows (SoftShadowMapping) ---------------------------------
+// The light pass writes Moments.frag (SAVSM, VSSM, MSSM) or Exponential.frag
+// (ESSM) into an S x T colour target cleared to 0, read unblurred at the
+// map's size.  Same driver choices as above (moments from the light map's
+// depth, quad differences for dFdx / dFdy).
+struct SoftMomArgs {
+    const float* depth;  // S x T light map
+    float4* out;         // S x T moment map
+    int S, T, tech;
+    float mq[16], tq0;
+};
+
+__device__ __forceinline__ float soft_lin_at(const SoftMomArgs& a, int x, int y, bool& empty) {
+    const float d = __ldg(a.depth + (size_t)y * a.S + x);
+    empty = !(d < 1.0f);
+    return gl_linearize(d);
+}
+
+__global__ void __launch_bounds__(256) k_soft_moments(const SoftMomArgs a) {
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= a.S || y >= a.T) return;
+    bool e;
+    const float d = soft_lin_at(a, x, y, e);
+    float4 o = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (!e) {
+        if (a.tech == GI_TECH_ESSM) {
+            const float ex = expf(80.0f * d);
+            o = make_float4(d, ex, ex * d, 0.0f);
+        } else if (a.tech == GI_TECH_MSSM) {
+            const float d2 = d * d, d3 = d2 * d, d4 = d3 * d;
+            const float* q = a.mq;
+            o = make_float4(q[0] * d + q[4] * d2 + q[8] * d3 + q[12] * d4 + a.tq0,
+                            q[1] * d + q[5] * d2 + q[9] * d3 + q[13] * d4 + 0.0f,
+                            q[2] * d + q[6] * d2 + q[10] * d3 + q[14] * d4 + 0.0f,
+                            q[3] * d + q[7] * d2 + q[11] * d3 + q[15] * d4 + 0.0f);
+        } else {
+            bool el, er, eb, et;
+            const int xr = (x | 1) < a.S ? (x | 1) : x, yt = (y | 1) < a.T ? (y | 1) : y;
+            const float l = soft_lin_at(a, x & ~1, y, el), r = soft_lin_at(a, xr, y, er);
+            const float b = soft_lin_at(a, x, y & ~1, eb), t = soft_lin_at(a, x, yt, et);
+            const float dx = (el || er) ? 0.0f : r - l;
+            const float dy = (eb || et) ? 0.0f : t - b;
+            o = make_float4(d - 0.5f, d * d + (0.25f * (dx * dx + dy * dy) - 0.5f), 0.0f, 0.0f);
+        }
+    }
+    a.out[(size_t)y * a.S + x] = o;
+}
+
+// One iteration i of the summed-area table (SATHorizontalPass.frag then
+// SATVerticalPass.frag at offset d = 2^i, main.cpp:943-971):
+//   t(x, y) = s(x, y) + s(x - d, y),  s'(x, y) = t(x, y) + t(x, y - d),
+// i.e. s' = (s(x, y) + s(x - d, y)) + (s(x, y - d) + s(x - d, y - d)), reads
+// outside the map being 0 (CLAMP_TO_BORDER), each sum rounded as written.
+__global__ void __launch_bounds__(256) k_sat_level(const float4* __restrict__ in, int S, int T, int d,
+                                                   float4* __restrict__ out) {
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= S || y >= T) return;
+    const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const bool l = x >= d, u = y >= d;
+    const float4 a = in[(size_t)y * S + x];
+    const float4 b = l ? in[(size_t)y * S + x - d] : z;
+    const float4 c = u ? in[(size_t)(y - d) * S + x] : z;
+    const float4 e = (l && u) ? in[(size_t)(y - d) * S + x - d] : z;
+    out[(size_t)y * S + x] = add4(add4(a, b), add4(c, e));
+}
+
+// renderHSM (main.cpp:696-751).  Level 0 (PrepareMinMax.frag) is
+// ((d == 0 ? 1 : d) + alpha, d + beta) per light-map texel; level k
+// (MinMax.frag) reads level k - 1 at the output texel's centre +- one output
+// texel in x and y: two input texels, i.e. half-texel positions, so each
+// read is the 0.25-weighted bilinear average of a 2 x 2 block, and the
+// texel keeps the min of the .x and the max of the .y of the four reads.
+__device__ __forceinline__ float gmin(float x, float y) { return y < x ? y : x; }
+__device__ __forceinline__ float gmax(float x, float y) { return x < y ? y : x; }
+
+__device__ __forceinline__ float2 hsm0_texel(const float* __restrict__ depth, int S, int T, int i, int j,
+                                             float alpha, float beta) {
+    if (i < 0 || i >= S || j < 0 || j >= T) return make_float2(0.0f, 0.0f);
+    const float d = __ldg(depth + (size_t)j * S + i);
+    return make_float2((d == 0.0f ? 1.0f : d) + alpha, d + beta);
+}
+
+template <class F>
+__device__ __forceinline__ float2 hsm_quad(const F& tex, int i0, int j0) {
+    const float2 a = tex(i0, j0), b = tex(i0 + 1, j0), c = tex(i0, j0 + 1), d = tex(i0 + 1, j0 + 1);
+    return make_float2(((0.25f * a.x + 0.25f * b.x) + 0.25f * c.x) + 0.25f * d.x,
+                       ((0.25f * a.y + 0.25f * b.y) + 0.25f * c.y) + 0.25f * d.y);
+}
+
+template <class F>
+__device__ __forceinline__ float2 hsm_minmax(const F& tex, int i, int j) {
+    const int xa = 2 * i - 2, xb = 2 * i + 2, ya = 2 * j - 2, yb = 2 * j + 2;
+    const float2 v0 = hsm_quad(tex, xa, ya), v1 = hsm_quad(tex, xa, yb);
+    const float2 v2 = hsm_quad(tex, xb, ya), v3 = hsm_quad(tex, xb, yb);
+    return make_float2(gmin(v0.x, gmin(v1.x, gmin(v2.x, v3.x))), gmax(v0.y, gmax(v1.y, gmax(v2.y, v3.y))));
+}
+
+__global__ void __launch_bounds__(256) k_hsm_level0(const float* __restrict__ depth, int S, int T, float alpha,
+                                                    float beta, float2* __restrict__ out) {
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= S || y >= T) return;
+    out[(size_t)y * S + x] = hsm0_texel(depth, S, T, x, y, alpha, beta);
+}
+
+// level 1 straight from the light map (level 0 is never stored)
+__global__ void __launch_bounds__(256) k_hsm_first(const float* __restrict__ depth, int S, int T, float alpha,
+                                                   float beta, float2* __restrict__ out) {
+    const int w = S / 2, h = T / 2;
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= w || y >= h) return;
+    const auto tex = [&](int i, int j) { return hsm0_texel(depth, S, T, i, j, alpha, beta); };
+    out[(size_t)y * w + x] = hsm_minmax(tex, x, y);
+}
+
+__global__ void __launch_bounds__(256) k_hsm_next(const float2* __restrict__ in, int pw, int ph,
+                                                  float2* __restrict__ out) {
+    const int w = pw / 2, h = ph / 2;
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= w || y >= h) return;
+    const auto tex = [&](int i, int j) {
+        return (i >= 0 && i < pw && j >= 0 && j < ph) ? __ldg(in + (size_t)j * pw + i) : make_float2(0.0f, 0.0f);
+    };
+    out[(size_t)y * w + x] = hsm_minmax(tex, x, y);
+}
+
 }  // namespace mom
 
 bool is_moment_technique(int t) { return t >= GI_TECH_VSM && t <= GI_TECH_MSM; }
+
+bool is_soft_moment_technique(int t) { return t >= GI_TECH_SAVSM && t <= GI_TECH_MSSM; }
+
+static bool power_of_two(int v) { return v > 0 && (v & (v - 1)) == 0; }
+
+gi_status soft_moment_check_shape(int tech, int map_w, int map_h, const char* who) {
+    if (tech == GI_TECH_VSSM && !(map_w == map_h && power_of_two(map_w) && map_w >= 8))
+        return fail(GI_ERR_UNSUPPORTED, std::string(who) + ": VSSM needs a square power-of-two map of side >= 8");
+    return GI_OK;
+}
+
+// main.cpp:943: int m = std::logf(shadowMapWidth) / std::logf(2), in float
+static int sat_iterations(int S) { return (int)(logf((float)S) / logf(2.0f)); }
+
+gi_status launch_soft_moment_map(gi_context* ctx, const gi_vis_params* p, const float* d_depth, int S, int T,
+                                 cudaStream_t st, float4* dst, const float4** out) {
+    using namespace mom;
+    const size_t n = (size_t)S * T;
+    const bool sat = p->summed_area_table != 0;
+    const int m = sat ? sat_iterations(S) : 0;
+    // m + 1 writes (the moment map, then one per SAT iteration) alternate
+    // between two buffers so that the last lands in dst (or in the scratch)
+    const size_t scratch = dst ? (m > 0 ? 1 : 0) : (m > 0 ? 2 : 1);
+    gi_status s = GI_OK;
+    if (scratch) s = ensure_buffer(reinterpret_cast<void**>(&ctx->d_mom), &ctx->cap_mom, scratch * n * sizeof(float4));
+    if (s != GI_OK) return s;
+    float4* last = dst ? dst : reinterpret_cast<float4*>(ctx->d_mom);
+    float4* spare = dst ? reinterpret_cast<float4*>(ctx->d_mom) : last + n;
+    SoftMomArgs a;
+    a.depth = d_depth;
+    a.out = (m % 2 == 0) ? last : spare;
+    a.S = S;
+    a.T = T;
+    a.tech = p->technique;
+    float mqi[16];
+    moment_quantization(a.mq, mqi, &a.tq0);
+    const dim3 grid((S + 31) / 32, (T + 7) / 8);
+    k_soft_moments<<<grid, 256, 0, st>>>(a);
+    ctx->launches++;
+    float4* cur = a.out;
+    for (int i = 0; i < m; ++i) {
+        float4* nxt = (cur == last) ? spare : last;
+        k_sat_level<<<grid, 256, 0, st>>>(cur, S, T, 1 << i, nxt);
+        ctx->launches++;
+        cur = nxt;
+    }
+    *out = cur;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "soft moment map launch");
+}
+
+// Levels 1..L stored one after the other in ctx->d_hsm.
+static gi_status hsm_levels(gi_context* ctx, const gi_vis_params* p, const float* d_depth, int S, int T, int L,
+                            cudaStream_t st, float2** levels) {
+    using namespace mom;
+    size_t need = 0;
+    for (int k = 1; k <= L; ++k) need += (size_t)(S >> k) * (T >> k);
+    gi_status s = ensure_buffer(reinterpret_cast<void**>(&ctx->d_hsm), &ctx->cap_hsm, need * sizeof(float2));
+    if (s != GI_OK) return s;
+    float2* lv = reinterpret_cast<float2*>(ctx->d_hsm);
+    for (int k = 1; k <= L; ++k) {
+        levels[k] = lv;
+        const int w = S >> k, h = T >> k;
+        const dim3 grid((w + 31) / 32, (h + 7) / 8);
+        if (k == 1)
+            k_hsm_first<<<grid, 256, 0, st>>>(d_depth, S, T, p->hsm_alpha, p->hsm_beta, lv);
+        else
+            k_hsm_next<<<grid, 256, 0, st>>>(levels[k - 1], S >> (k - 1), T >> (k - 1), lv);
+        ctx->launches++;
+        lv += (size_t)w * h;
+    }
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "min-max shadow map launch");
+}
+
+gi_status launch_hsm(gi_context* ctx, const gi_vis_params* p, const float* d_depth, int S, int T, int level,
+                     cudaStream_t st, const float2** out) {
+    using namespace mom;
+    if (level == 0) {
+        gi_status s = ensure_buffer(reinterpret_cast<void**>(&ctx->d_hsm), &ctx->cap_hsm, (size_t)S * T * sizeof(float2));
+        if (s != GI_OK) return s;
+        float2* lv = reinterpret_cast<float2*>(ctx->d_hsm);
+        k_hsm_level0<<<dim3((S + 31) / 32, (T + 7) / 8), 256, 0, st>>>(d_depth, S, T, p->hsm_alpha, p->hsm_beta, lv);
+        ctx->launches++;
+        *out = lv;
+        cudaError_t e = cudaGetLastError();
+        return e == cudaSuccess ? GI_OK : fail_cuda(e, "min-max shadow map launch");
+    }
+    float2* levels[32] = {};
+    gi_status s = hsm_levels(ctx, p, d_depth, S, T, level, st, levels);
+    if (s == GI_OK) *out = levels[level];
+    return s;
+}
+
+gi_status soft_moment_prepare(gi_context* ctx, const gi_vis_params* p, const float* d_depth, int S, int T,
+                              cudaStream_t st, SoftMaps* out) {
+    *out = SoftMaps{};
+    gi_status s = launch_soft_moment_map(ctx, p, d_depth, S, T, st, nullptr, &out->mom);
+    if (s != GI_OK || p->technique != GI_TECH_VSSM) return s;
+    // computeVisibilityFromHSM (PlausibleSoftShadow.frag:538-539) reads at
+    // lod W / 1024 + 0.5 (1.75 above 1024): levels floor(lod) and the next
+    const float lod = S > 1024 ? 1.75f : (float)S / 1024.0f + 0.5f;
+    const int lo = (int)floorf(lod);
+    float2* levels[32] = {};
+    s = hsm_levels(ctx, p, d_depth, S, T, lo + 1, st, levels);
+    if (s != GI_OK) return s;
+    out->hsm_lo = lo == 0 ? nullptr : levels[lo];
+    out->hsm_hi = levels[lo + 1];
+    out->lo_w = S >> lo;
+    out->lo_h = T >> lo;
+    out->hi_w = S >> (lo + 1);
+    out->hi_h = T >> (lo + 1);
+    out->hsm_frac = lod - (float)lo;
+    return GI_OK;
+}
 
 gi_status moment_check_shape(int map_w, int map_h, int W, int H, const char* who) {
     const std::string w(who);

@@ -94,8 +94,29 @@ gi_status moment_check_shape(int map_w, int map_h, int W, int H, const char* who
 void moment_quantization(float mq[16], float mqi[16], float* tq0);
 gi_status launch_moments(gi_context* ctx, int tech, const float* d_depth, int S, int W, cudaStream_t st,
                          const float** filtered);
-gi_status moment_prepare(gi_context* ctx, int tech, const float* d_depth, int S, int W, cudaStream_t st,
-                         const float** filtered);
+
+// Moment soft shadows (GI_TECH_SAVSM .. GI_TECH_MSSM): the maps the lookups
+// read, built from the S x T light map.
+struct SoftMaps {
+    const float4* mom = nullptr;     // moment map or its summed-area table, S x T
+    const float2* hsm_lo = nullptr;  // VSSM: min-max level floor(lod); level 0 is
+                                     // read from the light map (nullptr here)
+    const float2* hsm_hi = nullptr;  // level floor(lod) + 1
+    int lo_w = 0, lo_h = 0, hi_w = 0, hi_h = 0;
+    float hsm_frac = 0.0f;           // lod - floor(lod)
+};
+bool is_soft_moment_technique(int t);
+gi_status soft_moment_check_shape(int tech, int map_w, int map_h, const char* who);
+// The moment map (or its SAT when p->summed_area_table) into dst, or into
+// ctx scratch when dst is NULL; *out points at the result.
+gi_status launch_soft_moment_map(gi_context* ctx, const gi_vis_params* p, const float* d_depth, int S, int T,
+                                 cudaStream_t st, float4* dst, const float4** out);
+// Min-max level `level` (>= 1) into ctx scratch; *out points at it.
+gi_status launch_hsm(gi_context* ctx, const gi_vis_params* p, const float* d_depth, int S, int T, int level,
+                     cudaStream_t st, const float2** out);
+// Everything the lookups of p->technique read.
+gi_status soft_moment_prepare(gi_context* ctx, const gi_vis_params* p, const float* d_depth, int S, int T,
+                              cudaStream_t st, SoftMaps* out);
 
 // Progressive best-candidate Poisson-disk sequence in the unit disk
 // (poisson_table.inc); the n-tap table is its first n points.

@@ -66,6 +66,7 @@ struct Ctx {
     float fW, fH;
     float sx, sy;
     float I;
+    SoftMaps sm;  // moment soft shadows only
 };
 
 __device__ __forceinline__ float fetch(const Ctx& c, float s, float t) {
@@ -1175,6 +1176,244 @@ __device__ __forceinline__ float msm(const Ctx& c, V4 n) {
                   c.I, 1.0f);
 }
 
+// ---- moment soft shadows (SoftShadowMapping PlausibleSoftShadow.frag) --------
+// c.sm.mom holds the moment map or its summed-area table (c.W x c.H float4),
+// c.sm.hsm_* the two min-max levels VSSM's lookup blends.  Every read is
+// bilinear at its level with FP32 weights and a zero border.
+template <class F>
+__device__ __forceinline__ float2 bilinear2(const F& tex, int w, int h, float s, float t) {
+    const float u = s * (float)w - 0.5f, v = t * (float)h - 0.5f;
+    if (!(u > -2.0f && u < (float)w + 1.0f && v > -2.0f && v < (float)h + 1.0f)) return make_float2(0.0f, 0.0f);
+    const float fu = floorf(u), fv = floorf(v);
+    const int i0 = (int)fu, j0 = (int)fv;
+    const float a = u - fu, b = v - fv;
+    const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    const float2 T0 = tex(i0, j0), T1 = tex(i0 + 1, j0), T2 = tex(i0, j0 + 1), T3 = tex(i0 + 1, j0 + 1);
+    return make_float2(((w00 * T0.x + w10 * T1.x) + w01 * T2.x) + w11 * T3.x,
+                       ((w00 * T0.y + w10 * T1.y) + w01 * T2.y) + w11 * T3.y);
+}
+
+__device__ __forceinline__ V4 mom_at(const Ctx& c, float s, float t) {
+    const float4* m = c.sm.mom;
+    const float u = s * c.fW - 0.5f, v = t * c.fH - 0.5f;
+    V4 r{0.0f, 0.0f, 0.0f, 0.0f};
+    if (!(u > -2.0f && u < c.fW + 1.0f && v > -2.0f && v < c.fH + 1.0f)) return r;
+    const float fu = floorf(u), fv = floorf(v);
+    const int i0 = (int)fu, j0 = (int)fv;
+    const float a = u - fu, b = v - fv;
+    const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    float4 T[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int i = i0 + (k & 1), j = j0 + (k >> 1);
+        T[k] = (i >= 0 && i < c.W && j >= 0 && j < c.H) ? __ldg(m + (size_t)j * c.W + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    r.x = ((w00 * T[0].x + w10 * T[1].x) + w01 * T[2].x) + w11 * T[3].x;
+    r.y = ((w00 * T[0].y + w10 * T[1].y) + w01 * T[2].y) + w11 * T[3].y;
+    r.z = ((w00 * T[0].z + w10 * T[1].z) + w01 * T[2].z) + w11 * T[3].z;
+    r.w = ((w00 * T[0].w + w10 * T[1].w) + w01 * T[2].w) + w11 * T[3].w;
+    return r;
+}
+
+__device__ __forceinline__ float nonlinearize(float d) { return -(2.0f - d * 1001.0f) / (d * 999.0f); }
+
+// chebyshevUpperBound (PlausibleSoftShadow.frag:78-91)
+__device__ __forceinline__ float chebyshev_soft(float mx, float my, float z) {
+    if (z <= mx) return 1.0f;
+    const float variance = my - mx * mx;
+    const float d = z - mx;
+    const float p_max = variance / (variance + d * d);
+    const float p = z <= mx ? 1.0f : 0.0f;
+    return gmax(p, p_max);
+}
+
+// the SAT branch: four corner reads, (D + A - B - C) / SATFilterSize^2
+__device__ __forceinline__ V4 sat_box(const Ctx& c, V4 n, float width, float step) {
+    const float div = 2.0f * width / step;
+    const float size = div / 2.0f;
+    const float xmax = n.x + div * step, xmin = n.x - (div + 1.0f) * step;
+    const float ymax = n.y + div * step, ymin = n.y - (div + 1.0f) * step;
+    const V4 A = mom_at(c, xmin, ymin), B = mom_at(c, xmax, ymin), C = mom_at(c, xmin, ymax), D = mom_at(c, xmax, ymax);
+    const float den = size * size;
+    return V4{(((D.x + A.x) - B.x) - C.x) / den, (((D.y + A.y) - B.y) - C.y) / den, (((D.z + A.z) - B.z) - C.z) / den,
+              (((D.w + A.w) - B.w) - C.w) / den};
+}
+
+// the tap loop: bilinear reads at n.xy + (w, h) * width / fw summed in
+// (h, w) order, then / float(count^2)
+__device__ V4 loop_box(const Ctx& c, V4 n, float width, int count) {
+    const float fw = ((float)count - 1.0f) * 0.5f;
+    V4 acc{0.0f, 0.0f, 0.0f, 0.0f};
+    for (int h = (int)(-fw); (float)h <= fw; h++)
+        for (int w = (int)(-fw); (float)w <= fw; w++) {
+            const V4 t = mom_at(c, n.x + ((float)w * width) / fw, n.y + ((float)h * width) / fw);
+            acc = V4{acc.x + t.x, acc.y + t.y, acc.z + t.z, acc.w + t.w};
+        }
+    const float den = (float)(count * count);
+    return V4{acc.x / den, acc.y / den, acc.z / den, acc.w / den};
+}
+
+__device__ __forceinline__ V4 soft_box(const gi_vis_params& p, const Ctx& c, V4 n, float width, float step,
+                                       int count) {
+    return p.summed_area_table ? sat_box(c, n, width, step) : loop_box(c, n, width, count);
+}
+
+// VSM (:400-440)
+__device__ float soft_vsm(const gi_vis_params& p, const Ctx& c, float pw, V4 n) {
+    const int K = p.kernel_size;
+    const float step = 2.0f * pw / (float)K;
+    if (step <= 0.0f || step >= 1.0f) return 1.0f;
+    const V4 m = soft_box(p, c, n, pw, step, K);
+    const float mx = m.x + 0.5f, my = m.y + 0.5f;
+    return gclamp(gmix(chebyshev_soft(mx, my, gl_linearize(n.z)), 1.0f, c.I), 0.0f, 1.0f);
+}
+
+// computeAverageBlockerDepthBasedOnVSM (:196-244)
+__device__ float vsm_blocker(const gi_vis_params& p, const Ctx& c, V4 n) {
+    const float bsw = blocker_search_width(p, c);
+    const int B = p.blocker_search_size;
+    const float step = 2.0f * bsw / (float)B;
+    const float zun = gl_linearize(n.z);
+    const V4 m = soft_box(p, c, n, bsw, step, B);
+    const float mx = m.x + 0.5f, my = m.y + 0.5f;
+    const float prob = chebyshev_soft(mx, my, zun);
+    float zocc = nonlinearize((mx - prob * zun) / (1.0f - prob));
+    if (prob > 0.99f) zocc = 1.0f;
+    return zocc;
+}
+
+// computeAverageBlockerDepthBasedOnESM (:246-301)
+__device__ float esm_blocker(const gi_vis_params& p, const Ctx& c, V4 n) {
+    const float bsw = blocker_search_width(p, c);
+    const int B = p.blocker_search_size;
+    const float step = 2.0f * bsw / (float)B;
+    const V4 s = soft_box(p, c, n, bsw, step, B);
+    const float lz = gl_linearize(n.z);
+    const float prob = expf(-80.0f * lz) * s.y;
+    if (prob > 0.91f) return 1.0f;
+    const float zocc = (s.x - expf(-80.0f * lz) * s.z) / (1.0f - prob);
+    return nonlinearize(zocc);
+}
+
+// ESM (:442-490)
+__device__ float soft_esm(const gi_vis_params& p, const Ctx& c, float pw, V4 n) {
+    const int K = p.kernel_size;
+    const float step = 2.0f * pw / (float)K;
+    if (step <= 0.0f || step >= 1.0f) return 1.0f;
+    const float avg = soft_box(p, c, n, pw, step, K).y;
+    const float dist = mom_at(c, n.x, n.y).x + 0.0001f;
+    const float lz = gl_linearize(n.z);
+    float v = expf(-80.0f * lz) * avg;
+    v = gclamp(v, c.I, 1.0f);
+    if (dist > lz && v == c.I) return 1.0f;
+    return v;
+}
+
+// computeMomentDepthsFromMSM (:93-132): b and the three depths
+struct MsmSolve {
+    V4 b;
+    float zx, zy, zz;
+};
+
+__device__ __forceinline__ MsmSolve msm_solve(V4 b, float lz) {
+    b = V4{b.x - c_msm[16], b.y - c_msm[17], b.z - c_msm[18], b.w - c_msm[19]};
+    b = mat4_mul(c_msm, b);
+    const float bias = 0.00003f;
+    const float ob = 1.0f - bias, hb = bias * 0.5f;
+    b = V4{ob * b.x + hb, ob * b.y + hb, ob * b.z + hb, ob * b.w + hb};
+    const float dx = 1.0f, dy = lz, dz = lz * lz;
+    const float L10 = b.x, L20 = b.y;
+    const float D11 = b.y - L10 * L10;
+    const float L21 = (b.z - L20 * L10) / D11;
+    const float D22 = b.w - L20 * L20 - L21 * L21 * D11;
+    const float y0 = dx;
+    float y1 = dy - L10 * y0;
+    float y2 = dz - L20 * y0 - L21 * y1;
+    y1 = y1 / D11;
+    y2 = y2 / D22;
+    const float cz = y2, cy = y1 - L21 * cz, cx = y0 - L10 * cy - L20 * cz;
+    const float pp = cy / cz, q = cx / cz;
+    const float D = ((pp * pp) / 4.0f) - q;
+    const float r = sqrtf(D);
+    return MsmSolve{b, lz, -(pp / 2.0f) - r, -(pp / 2.0f) + r};
+}
+
+// computeAverageBlockerDepthBasedOnMSM (:303-363) with computeWeightsFromMSM
+__device__ float msm_blocker(const gi_vis_params& p, const Ctx& c, V4 n) {
+    const float bias = 0.01f;
+    const float bsw = p.light_radius / c.fW;
+    const int B = p.blocker_search_size;
+    const float step = 2.0f * bsw / (float)B;
+    const MsmSolve z = msm_solve(soft_box(p, c, n, bsw, step, B), gl_linearize(n.z));
+    const V4& b = z.b;
+    const float wx = (z.zy * z.zz - b.x * (z.zy + z.zz) + b.y) / ((z.zx - z.zy) * (z.zx - z.zz));
+    const float wy = (z.zx * z.zz - b.x * (z.zx + z.zz) + b.y) / ((z.zz - z.zy) * (z.zx - z.zy));
+    const float wz = 1.0f - wx - wy;
+    const float ky = 1.0f - wy, kz = 1.0f - wz;
+    float avg = 0.0f, sum = 0.0f;
+    if (z.zx > z.zy) {
+        avg += ky * z.zy;
+        sum += ky;
+    }
+    if (z.zx > z.zz) {
+        avg += kz * z.zz;
+        sum += kz;
+    }
+    avg += bias * z.zx;
+    sum += bias;
+    if (sum > 1.0f - bias) return 1.0f;
+    return nonlinearize(avg / sum);
+}
+
+// MSM (:492-533) with computeShadowIntensityFromMSM (:149-164)
+__device__ float soft_msm(const gi_vis_params& p, const Ctx& c, float pw, V4 n) {
+    const int K = p.kernel_size;
+    const float step = 2.0f * pw / (float)K;
+    if (step <= 0.0f || step >= 1.0f) return 1.0f;
+    const MsmSolve z = msm_solve(soft_box(p, c, n, pw, step, K), gl_linearize(n.z));
+    const V4& b = z.b;
+    if (z.zx <= z.zy) return 1.0f;
+    if (z.zx <= z.zz)
+        return gclamp(1.0f - gclamp((z.zx * z.zz - b.x * (z.zx + z.zz) + b.y) / ((z.zz - z.zy) * (z.zx - z.zy)),
+                                    0.0f, 1.0f),
+                      c.I, 1.0f);
+    return gclamp(1.0f - gclamp(1.0f - (z.zy * z.zz - b.x * (z.zy + z.zz) + b.y) / ((z.zx - z.zy) * (z.zx - z.zz)),
+                                0.0f, 1.0f),
+                  c.I, 1.0f);
+}
+
+// computeVisibilityFromHSM (:535-554): levels floor(lod) and floor(lod) + 1
+// blended (1 - f) t1 + f t2; level 0 is read from the light map
+__device__ float hsm_visibility(const gi_vis_params& p, const Ctx& c, V4 n) {
+    const float2* hi = c.sm.hsm_hi;
+    const auto tex_hi = [&](int i, int j) {
+        return (i >= 0 && i < c.sm.hi_w && j >= 0 && j < c.sm.hi_h) ? __ldg(hi + (size_t)j * c.sm.hi_w + i)
+                                                                    : make_float2(0.0f, 0.0f);
+    };
+    float2 lo;
+    if (c.sm.hsm_lo) {
+        const float2* l = c.sm.hsm_lo;
+        const auto tex_lo = [&](int i, int j) {
+            return (i >= 0 && i < c.sm.lo_w && j >= 0 && j < c.sm.lo_h) ? __ldg(l + (size_t)j * c.sm.lo_w + i)
+                                                                        : make_float2(0.0f, 0.0f);
+        };
+        lo = bilinear2(tex_lo, c.sm.lo_w, c.sm.lo_h, n.x, n.y);
+    } else {
+        const auto tex0 = [&](int i, int j) {
+            if (i < 0 || i >= c.W || j < 0 || j >= c.H) return make_float2(0.0f, 0.0f);
+            const float d = __ldg(c.map + (size_t)j * c.W + i);
+            return make_float2((d == 0.0f ? 1.0f : d) + p.hsm_alpha, d + p.hsm_beta);
+        };
+        lo = bilinear2(tex0, c.W, c.H, n.x, n.y);
+    }
+    const float2 up = bilinear2(tex_hi, c.sm.hi_w, c.sm.hi_h, n.x, n.y);
+    const float f = c.sm.hsm_frac;
+    const float mn = (1.0f - f) * lo.x + f * up.x, mx = (1.0f - f) * lo.y + f * up.y;
+    if (n.z <= mn) return 1.0f;
+    if (n.z > mx) return c.I;
+    return 0.555f;
+}
+
 template <int TECH>
 __device__ __forceinline__ float shade(const gi_vis_params& p, const Ctx& c, V4 vertex, V4 normal) {
     if (vertex.x == 0.0f) return 0.0f;
@@ -1227,6 +1466,21 @@ __device__ __forceinline__ float shade(const gi_vis_params& p, const Ctx& c, V4 
         if (sc.w > 0.0f && shadow == 1.0f) shadow = evsm(c, n);
     } else if (TECH == GI_TECH_MSM) {
         if (sc.w > 0.0f && shadow == 1.0f) shadow = msm(c, n);
+    } else if (TECH == GI_TECH_SAVSM) {  // summedAreaVarianceShadowMapping (:565-572)
+        if (sc.w > 0.0f && shadow == 1.0f) {
+            const float avg = avg_blocker_grid(p, c, n);
+            shadow = soft_vsm(p, c, penumbra_width(p, avg, n.z), n);
+        }
+    } else if (TECH == GI_TECH_VSSM) {  // varianceSoftShadowMapping (:574-585)
+        if (sc.w > 0.0f && shadow == 1.0f) {
+            const float v = hsm_visibility(p, c, n);
+            if (v == c.I || v == 1.0f) shadow = v;
+            else shadow = soft_vsm(p, c, penumbra_width(p, vsm_blocker(p, c, n), n.z), n);
+        }
+    } else if (TECH == GI_TECH_ESSM) {  // exponentialSoftShadowMapping (:587-594)
+        if (sc.w > 0.0f && shadow == 1.0f) shadow = soft_esm(p, c, penumbra_width(p, esm_blocker(p, c, n), n.z), n);
+    } else if (TECH == GI_TECH_MSSM) {  // momentSoftShadowMapping (:596-603)
+        if (sc.w > 0.0f && shadow == 1.0f) shadow = soft_msm(p, c, penumbra_width(p, msm_blocker(p, c, n), n.z), n);
     } else if (TECH == GI_TECH_HARD_SOFTAPP) {
         float r = shadow;
         if (sc.w > 0.0f && r == 1.0f) {
@@ -1245,7 +1499,8 @@ __global__ void __launch_bounds__(128) k_visibility(const gi_vis_params p,
                                                     int map_h, float sx, float sy,
                                                     const float4* __restrict__ pos,
                                                     const float4* __restrict__ nrm,
-                                                    float* __restrict__ out, int W, int H) {
+                                                    float* __restrict__ out, int W, int H,
+                                                    const SoftMaps sm) {
     int x = blockIdx.x * 32 + (threadIdx.x & 31);
     int y = blockIdx.y * 4 + (threadIdx.x >> 5);
     if (x >= W || y >= H) return;
@@ -1258,6 +1513,7 @@ __global__ void __launch_bounds__(128) k_visibility(const gi_vis_params p,
     c.sx = sx;
     c.sy = sy;
     c.I = p.shadow_intensity;
+    c.sm = sm;
     size_t i = (size_t)y * W + x;
     float4 pv = __ldcs(pos + i);
     float4 nv = __ldcs(nrm + i);
@@ -1277,11 +1533,13 @@ __global__ void __launch_bounds__(128) k_frame_visibility(
     const unsigned long long* __restrict__ keys, const float* __restrict__ points,
     const float* __restrict__ normals, const int* __restrict__ indices, const dev::Mat4 mvp,
     const unsigned* __restrict__ rec_of, const dev::BRec* __restrict__ recs, const uint4* __restrict__ rres,
-    float* __restrict__ out, int W, int H, float4* __restrict__ pos_out, float4* __restrict__ nrm_out) {
+    float* __restrict__ out, int W, int H, float4* __restrict__ pos_out, float4* __restrict__ nrm_out,
+    const SoftMaps sm) {
     int x = blockIdx.x * 32 + (threadIdx.x & 31);
     int y = blockIdx.y * 4 + (threadIdx.x >> 5);
     if (x >= W || y >= H) return;
     Ctx c;
+    c.sm = sm;
     c.map = map;
     c.W = map_w;
     c.H = map_h;
@@ -1632,12 +1890,19 @@ gi_status launch_area_accumulate(gi_context* ctx, const gi_scene* scene, const f
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "area-light accumulate launch");
 }
 
-// The moment map, its mip levels and blur for the moment techniques, then
-// the MSM constants; *filtered points at the blurred window-size map.
-gi_status moment_prepare(gi_context* ctx, int tech, const float* d_depth, int S, int W, cudaStream_t st,
-                         const float** filtered) {
-    gi_status s = launch_moments(ctx, tech, d_depth, S, W, st, filtered);
-    if (s != GI_OK || tech != GI_TECH_MSM) return s;
+// The maps the moment techniques read instead of (VSM..MSM) or beside
+// (SAVSM..MSSM) the light map, and the MSM constants.
+static gi_status prepare_maps(gi_context* ctx, const gi_vis_params* p, const float** d_depth, int* map_w,
+                              int* map_h, int W, cudaStream_t st, SoftMaps* sm) {
+    const int t = p->technique;
+    gi_status s = GI_OK;
+    if (is_moment_technique(t)) {
+        s = launch_moments(ctx, t, *d_depth, *map_w, W, st, d_depth);
+        *map_w = *map_h = W;
+    } else if (is_soft_moment_technique(t)) {
+        s = soft_moment_prepare(ctx, p, *d_depth, *map_w, *map_h, st, sm);
+    }
+    if (s != GI_OK || (t != GI_TECH_MSM && t != GI_TECH_MSSM)) return s;
     float mq[16], h[20];
     moment_quantization(mq, h, &h[16]);
     h[17] = h[18] = h[19] = 0.0f;
@@ -1649,11 +1914,9 @@ gi_status launch_visibility(gi_context* ctx, const gi_vis_params* p, const float
                             int map_w, int map_h, const float* d_pos, const float* d_nrm,
                             float* d_vis, int W, int H, cudaStream_t st) {
     dim3 grid((W + 31) / 32, (H + 3) / 4);
-    if (is_moment_technique(p->technique)) {
-        gi_status s = moment_prepare(ctx, p->technique, d_depth, map_w, W, st, &d_depth);
-        if (s != GI_OK) return s;
-        map_w = map_h = W;
-    }
+    SoftMaps sm;
+    gi_status ps = prepare_maps(ctx, p, &d_depth, &map_w, &map_h, W, st, &sm);
+    if (ps != GI_OK) return ps;
     // shadowMapStep = (1.0 / w, 1.0 / h) in double, stored as float
     // (glUniform2f at MyGLGeometryViewer.cpp:237-238)
     const float sx = (float)(1.0 / (double)map_w), sy = (float)(1.0 / (double)map_h);
@@ -1661,7 +1924,7 @@ gi_status launch_visibility(gi_context* ctx, const gi_vis_params* p, const float
     const float4* nrm = reinterpret_cast<const float4*>(d_nrm);
 #define GI_VIS_CASE(T)                                                                     \
     case T:                                                                                \
-        vis::k_visibility<T><<<grid, 128, 0, st>>>(*p, d_depth, map_w, map_h, sx, sy, pos, nrm, d_vis, W, H); \
+        vis::k_visibility<T><<<grid, 128, 0, st>>>(*p, d_depth, map_w, map_h, sx, sy, pos, nrm, d_vis, W, H, sm); \
         break;
     switch (p->technique) {
         GI_VIS_CASE(GI_TECH_HARD)
@@ -1680,6 +1943,10 @@ gi_status launch_visibility(gi_context* ctx, const gi_vis_params* p, const float
         GI_VIS_CASE(GI_TECH_ESM)
         GI_VIS_CASE(GI_TECH_EVSM)
         GI_VIS_CASE(GI_TECH_MSM)
+        GI_VIS_CASE(GI_TECH_SAVSM)
+        GI_VIS_CASE(GI_TECH_VSSM)
+        GI_VIS_CASE(GI_TECH_ESSM)
+        GI_VIS_CASE(GI_TECH_MSSM)
         default:
             return fail(GI_ERR_INVALID_ARG, "gi_visibility: unknown technique");
     }
@@ -1694,11 +1961,9 @@ gi_status launch_frame_visibility(gi_context* ctx, const gi_vis_params* p, const
                                   float* d_vis, int W, int H, float* d_pos, float* d_nrm,
                                   cudaStream_t st) {
     dim3 grid((W + 31) / 32, (H + 3) / 4);
-    if (is_moment_technique(p->technique)) {
-        gi_status s = moment_prepare(ctx, p->technique, d_depth, map_w, W, st, &d_depth);
-        if (s != GI_OK) return s;
-        map_w = map_h = W;
-    }
+    SoftMaps sm;
+    gi_status ps = prepare_maps(ctx, p, &d_depth, &map_w, &map_h, W, st, &sm);
+    if (ps != GI_OK) return ps;
     const float sx = (float)(1.0 / (double)map_w), sy = (float)(1.0 / (double)map_h);
     const unsigned* rec_of = static_cast<const unsigned*>(ctx->tier_buf[1][6]);
     const dev::BRec* recs = static_cast<const dev::BRec*>(ctx->tier_buf[1][0]);
@@ -1712,7 +1977,7 @@ gi_status launch_frame_visibility(gi_context* ctx, const gi_vis_params* p, const
         vis::k_frame_visibility<T><<<grid, 128, 0, st>>>(*p, d_depth, map_w, map_h, sx, sy,         \
                                                           ctx->d_vkeys, scene->d_points,          \
                                                           scene->d_normals, scene->d_indices, m,  \
-                                                          rec_of, recs, rres, d_vis, W, H, po, no); \
+                                                          rec_of, recs, rres, d_vis, W, H, po, no, sm); \
         break;
     switch (p->technique) {
         GI_FRAME_CASE(GI_TECH_HARD)
@@ -1731,6 +1996,10 @@ gi_status launch_frame_visibility(gi_context* ctx, const gi_vis_params* p, const
         GI_FRAME_CASE(GI_TECH_ESM)
         GI_FRAME_CASE(GI_TECH_EVSM)
         GI_FRAME_CASE(GI_TECH_MSM)
+        GI_FRAME_CASE(GI_TECH_SAVSM)
+        GI_FRAME_CASE(GI_TECH_VSSM)
+        GI_FRAME_CASE(GI_TECH_ESSM)
+        GI_FRAME_CASE(GI_TECH_MSSM)
         default:
             return fail(GI_ERR_INVALID_ARG, "gi_render_frame: unknown technique");
     }

@@ -273,6 +273,10 @@ TECHNIQUES = {
     "esm": api.GI_TECH_ESM,
     "evsm": api.GI_TECH_EVSM,
     "msm": api.GI_TECH_MSM,
+    "savsm": api.GI_TECH_SAVSM,
+    "vssm": api.GI_TECH_VSSM,
+    "essm": api.GI_TECH_ESSM,
+    "mssm": api.GI_TECH_MSSM,
 }
 
 
@@ -292,6 +296,9 @@ class ShadowParams:
     pcss_min_blocker_depth: float = 0.99
     poisson_blocker_taps: int = 16
     poisson_filter_taps: int = 32
+    summed_area_table: bool = False
+    hsm_alpha: float = 0.0
+    hsm_beta: float = 0.0
     pretest: int = api.GI_PRETEST_REFERENCE
 
     @classmethod
@@ -303,6 +310,7 @@ class ShadowParams:
                    blocker_search_size=p.blocker_search_size, kernel_size=p.kernel_size,
                    light_radius=p.light_radius, znear=p.znear, pcss_min_blocker_depth=p.pcss_min_blocker_depth,
                    poisson_blocker_taps=p.poisson_blocker_taps, poisson_filter_taps=p.poisson_filter_taps,
+                   summed_area_table=bool(p.summed_area_table), hsm_alpha=p.hsm_alpha, hsm_beta=p.hsm_beta,
                    pretest=p.pretest)
 
     def to_c(self, frame: Frame) -> api.VisParams:
@@ -321,10 +329,14 @@ class ShadowParams:
         p.pcss_min_blocker_depth = self.pcss_min_blocker_depth
         p.poisson_blocker_taps = self.poisson_blocker_taps
         p.poisson_filter_taps = self.poisson_filter_taps
-        C.memmove(p.light_mvp_biased, frame.light_mvp_biased.astype(np.float32).tobytes(), 64)
-        C.memmove(p.camera_mv, frame.camera_mv.astype(np.float32).tobytes(), 64)
-        C.memmove(p.normal_matrix, frame.normal_matrix.astype(np.float32).tobytes(), 36)
-        C.memmove(p.light_position, frame.light_position.astype(np.float32).tobytes(), 12)
+        p.summed_area_table = 1 if self.summed_area_table else 0
+        p.hsm_alpha = self.hsm_alpha
+        p.hsm_beta = self.hsm_beta
+        if frame is not None:  # the light-side maps need no matrices
+            C.memmove(p.light_mvp_biased, frame.light_mvp_biased.astype(np.float32).tobytes(), 64)
+            C.memmove(p.camera_mv, frame.camera_mv.astype(np.float32).tobytes(), 64)
+            C.memmove(p.normal_matrix, frame.normal_matrix.astype(np.float32).tobytes(), 36)
+            C.memmove(p.light_position, frame.light_position.astype(np.float32).tobytes(), 12)
         return p
 
 
@@ -366,6 +378,26 @@ def compute_visibility(ctx: Context, params: ShadowParams, frame: Frame, depth, 
 
 
 compute_hard_shadows = compute_visibility
+
+
+def soft_moment_map(ctx: Context, params: ShadowParams, depth, map_w: int, map_h: int, out, stream=None):
+    """The light-side map of a moment soft-shadow technique (SAVSM..MSSM): the moment map, or its
+    summed-area table when params.summed_area_table is set; out is float32[map_h * map_w * 4]."""
+    assert out.is_cuda and out.numel() >= map_w * map_h * 4
+    p = params.to_c(None)
+    check(_lib().gi_soft_moment_map(ctx.handle, C.byref(p), _ptr(depth), map_w, map_h, _ptr(out),
+                                    _stream_ptr(stream)), "gi_soft_moment_map")
+    return out
+
+
+def hierarchical_shadow_map(ctx: Context, params: ShadowParams, depth, map_w: int, map_h: int, level: int, out,
+                            stream=None):
+    """Level `level` of renderHSM's min-max map: out is float32[(map_h >> level) * (map_w >> level) * 2]."""
+    assert out.is_cuda and out.numel() >= (map_w >> level) * (map_h >> level) * 2
+    p = params.to_c(None)
+    check(_lib().gi_hierarchical_shadow_map(ctx.handle, C.byref(p), _ptr(depth), map_w, map_h, int(level),
+                                            _ptr(out), _stream_ptr(stream)), "gi_hierarchical_shadow_map")
+    return out
 
 
 def shadow_volume_counts(ctx: Context, scene: Scene, light_pos, camera_mvp, width: int, height: int,

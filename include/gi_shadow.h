@@ -299,7 +299,20 @@ typedef enum gi_technique {
     GI_TECH_ESM = 13,                 /* Shadow.frag:144-157                  */
     GI_TECH_EVSM = 14,                /* Shadow.frag:160-176                  */
     GI_TECH_MSM = 15,                 /* Shadow.frag:178-220 (Hamburger 4MSM) */
-    GI_TECH_COUNT = 16
+    /* Moment soft shadows of SoftShadowMapping (PlausibleSoftShadow.frag;
+     * light pass Shaders/Moments/Moments.frag or Shaders/Exponential.frag;
+     * src/main.cpp:274-290, 938-973).  The light map becomes an unblurred
+     * moment map at the map's size; with summed_area_table set the lookups
+     * read its summed-area table (Shaders/Moments/SAT{Horizontal,Vertical}
+     * Pass.frag), else they loop over bilinear taps of the moment map.
+     * VSSM first classifies each pixel with the hierarchical min-max map
+     * (Shaders/Moments/{PrepareMinMax,MinMax}.frag, main.cpp:696-751) and
+     * needs a square power-of-two map of side >= 8. */
+    GI_TECH_SAVSM = 16,               /* PlausibleSoftShadow.frag:565-572     */
+    GI_TECH_VSSM = 17,                /* PlausibleSoftShadow.frag:574-585     */
+    GI_TECH_ESSM = 18,                /* PlausibleSoftShadow.frag:587-594     */
+    GI_TECH_MSSM = 19,                /* PlausibleSoftShadow.frag:596-603     */
+    GI_TECH_COUNT = 20
 } gi_technique;
 
 typedef enum gi_pretest_mode {
@@ -326,6 +339,9 @@ typedef struct gi_vis_params {
     float pcss_min_blocker_depth; /* PlausibleSoftShadow.frag:368 (0.99)    */
     int poisson_blocker_taps;   /* PCSS_POISSON: 16                         */
     int poisson_filter_taps;    /* PCSS_POISSON: 32                         */
+    int summed_area_table;      /* SAVSM..MSSM: ShadowParams.SAT (key 's')  */
+    float hsm_alpha;            /* VSSM: HSMAlpha, config key "ha"          */
+    float hsm_beta;             /* VSSM: HSMBeta, config key "hb"           */
     float light_mvp_biased[16];
     float camera_mv[16];
     float normal_matrix[9];
@@ -360,6 +376,29 @@ gi_status gi_render_frame(gi_context* ctx, const gi_scene* scene,
 /* Poisson-disk sample table used by GI_TECH_PCSS_POISSON (n <= 64 points in
  * the unit disk, interleaved x,y).  Shared with the CPU oracle. */
 gi_status gi_poisson_table(int n, float* xy_out);
+
+/* ---- moment soft shadows: the light-side maps ---------------------------
+ * The maps GI_TECH_SAVSM..MSSM sample, as the reference builds them from
+ * the light pass (SoftShadowMapping/src/main.cpp:274-290 with
+ * Shaders/Moments/Moments.frag or Shaders/Exponential.frag, and the SAT
+ * loop at :943-971).  d_out (float4 [map_width * map_height]) receives the
+ * moment map of vis->technique, or its summed-area table when
+ * vis->summed_area_table is set: log2(map_width) iterations of a horizontal
+ * pass t(x, y) = m(x, y) + m(x - 2^i, y) followed by a vertical pass
+ * m(x, y) = t(x, y) + t(x, y - 2^i), reads outside the map being 0. */
+gi_status gi_soft_moment_map(gi_context* ctx, const gi_vis_params* vis, const float* d_depth, int map_width,
+                             int map_height, float* d_out, void* stream);
+
+/* renderHSM (SoftShadowMapping/src/main.cpp:696-751): level `level` of the
+ * hierarchical min-max shadow map, float2 (min, max) per texel of the
+ * (map_width >> level) x (map_height >> level) level.  Level 0 is
+ * (depth == 0 ? 1 : depth) + vis->hsm_alpha, depth + vis->hsm_beta
+ * (PrepareMinMax.frag); level k takes min / max over the four bilinear
+ * reads of level k - 1 at the texel's diagonal neighbours (MinMax.frag).
+ * Needs a square power-of-two map, 1 <= level < log2(map_width) (level 0:
+ * 0 <= level). */
+gi_status gi_hierarchical_shadow_map(gi_context* ctx, const gi_vis_params* vis, const float* d_depth,
+                                     int map_width, int map_height, int level, float* d_out, void* stream);
 
 /* ---- EDT-filtered hard shadows (ShadowMapping's EDTSM mode) -------------
  *

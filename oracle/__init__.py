@@ -35,6 +35,8 @@ def load():
         lib.or_edt_soft_shadows.argtypes = [vp, vp, i, i, i, i, i, f, f, vp, vp, vp, i]
         lib.or_edt_inputs.argtypes = [vp, vp, vp, vp, vp, i, i, vp, vp]
         lib.or_edt_mean_filter.argtypes = [vp, vp, vp, i, i, i, vp]
+        lib.or_soft_moment_map.argtypes = [vp, vp, i, i, vp]
+        lib.or_hierarchical_shadow_map.argtypes = [vp, vp, i, i, i, vp]
         for fn in (lib.or_shadow_map, lib.or_gbuffer, lib.or_visibility, lib.or_shadow_volume_counts):
             fn.restype = None
         _lib = lib
@@ -71,6 +73,22 @@ def visibility(vis_params, depth, map_w, map_h, pos, nrm, width, height, poisson
     tab = _f32(poisson_xy) if poisson_xy is not None else None
     load().or_visibility(C.addressof(vis_params), d.ctypes.data, map_w, map_h, ps.ctypes.data, ns.ctypes.data,
                          out.ctypes.data, width, height, tab.ctypes.data if tab is not None else None, threads)
+    return out
+
+
+def soft_moment_map(vis_params, depth, S, T):
+    """Moment map (or its summed-area table) of a SoftShadowMapping moment technique, float32 [T, S, 4]."""
+    d = _f32(depth)
+    out = np.empty((T, S, 4), np.float32)
+    load().or_soft_moment_map(C.addressof(vis_params), d.ctypes.data, S, T, out.ctypes.data)
+    return out
+
+
+def hierarchical_shadow_map(vis_params, depth, S, T, level):
+    """Level `level` of the min-max shadow map, float32 [T >> level, S >> level, 2]."""
+    d = _f32(depth)
+    out = np.empty((T >> level, S >> level, 2), np.float32)
+    load().or_hierarchical_shadow_map(C.addressof(vis_params), d.ctypes.data, S, T, level, out.ctypes.data)
     return out
 
 

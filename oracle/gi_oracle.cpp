@@ -489,6 +489,13 @@ struct Ctx {
     int W, H;
     float sx, sy;  // shadowMapStep = (1/W, 1/H)
     float I;       // shadowIntensity
+    // moment soft shadows: the moment map or its summed-area table (W x H
+    // float4) and the two min-max levels VSSM's lookup blends
+    const float* mom = nullptr;
+    const float* hsm_lo = nullptr;
+    const float* hsm_hi = nullptr;
+    int lo_w = 0, lo_h = 0, hi_w = 0, hi_h = 0;
+    float hsm_frac = 0.0f;
 };
 
 float fetch(const Ctx& c, float s, float t) {
@@ -1703,6 +1710,348 @@ float moment_lookup(const Ctx& c, V4 n) {
                   c.I, 1.0f);
 }
 
+// ---- moment soft shadows (SoftShadowMapping PlausibleSoftShadow.frag) --------
+// SAVSM, VSSM, ESSM and MSSM with or without the summed-area table.  The
+// choices GL leaves to the driver are those of the filtered moment maps
+// above (moments from the depth map's value, dFdx / dFdy inside 2 x 2
+// quads, lookups bilinear at level 0 with a zero border) plus: the SAT
+// passes read exact texels (their coordinates are texel centres); the
+// min-max levels read level k - 1 at the half-texel positions MinMax.frag's
+// offsets give (each read the 0.25-weighted average of a 2 x 2 block); the
+// min-max lookup at lod L blends levels floor(L) and floor(L) + 1 as
+// (1 - f) t1 + f t2 with f = L - floor(L).
+bool is_soft_moment(int t) { return t >= GI_TECH_SAVSM && t <= GI_TECH_MSSM; }
+
+// Moments.frag (SAVSM / VSSM / MSSM) or Exponential.frag (ESSM) per texel
+// of the light map; texels no fragment reached keep the clear colour 0.
+std::vector<float> soft_moment_map(int tech, const float* depth, int S, int T) {
+    std::vector<float> m((size_t)S * T * 4, 0.0f);
+    float mq[16], mqi[16];
+    msm_quantization(mq, mqi);
+    const float tq0 = 0.0359558848f;
+    auto lin_at = [&](int x, int y, bool& empty) {
+        const float d = depth[(size_t)y * S + x];
+        empty = !(d < 1.0f);
+        return gl_linearize(d);
+    };
+    for (int y = 0; y < T; ++y)
+        for (int x = 0; x < S; ++x) {
+            float* o = &m[4 * ((size_t)y * S + x)];
+            bool empty;
+            const float d = lin_at(x, y, empty);
+            if (empty) continue;
+            if (tech == GI_TECH_ESSM) {
+                const float e = std::exp(80.0f * d);
+                o[0] = d;
+                o[1] = e;
+                o[2] = e * d;
+            } else if (tech == GI_TECH_MSSM) {
+                const float d2 = d * d, d3 = d2 * d, d4 = d3 * d;
+                for (int r = 0; r < 4; ++r)
+                    o[r] = mq[r] * d + mq[4 + r] * d2 + mq[8 + r] * d3 + mq[12 + r] * d4 + (r == 0 ? tq0 : 0.0f);
+            } else {
+                bool el, er, eb, et;
+                const int xr = (x | 1) < S ? (x | 1) : x, yt = (y | 1) < T ? (y | 1) : y;
+                const float l = lin_at(x & ~1, y, el), rr = lin_at(xr, y, er);
+                const float b = lin_at(x, y & ~1, eb), t = lin_at(x, yt, et);
+                const float dx = (el || er) ? 0.0f : rr - l;
+                const float dy = (eb || et) ? 0.0f : t - b;
+                o[0] = d - 0.5f;
+                o[1] = d * d + (0.25f * (dx * dx + dy * dy) - 0.5f);
+            }
+        }
+    return m;
+}
+
+// main.cpp:943-971: int m = logf(width) / logf(2); for i < m a horizontal
+// then a vertical pass at offset 2^i, reads outside the map giving 0.
+int sat_iterations(int S) { return (int)(std::log((float)S) / std::log(2.0f)); }
+
+void summed_area_table(std::vector<float>& s, int S, int T) {
+    std::vector<float> t(s.size());
+    const int m = sat_iterations(S);
+    for (int i = 0; i < m; ++i) {
+        const int d = 1 << i;
+        for (int y = 0; y < T; ++y)
+            for (int x = 0; x < S; ++x)
+                for (int ch = 0; ch < 4; ++ch)
+                    t[4 * ((size_t)y * S + x) + ch] =
+                        s[4 * ((size_t)y * S + x) + ch] + (x >= d ? s[4 * ((size_t)y * S + x - d) + ch] : 0.0f);
+        for (int y = 0; y < T; ++y)
+            for (int x = 0; x < S; ++x)
+                for (int ch = 0; ch < 4; ++ch)
+                    s[4 * ((size_t)y * S + x) + ch] =
+                        t[4 * ((size_t)y * S + x) + ch] + (y >= d ? t[4 * ((size_t)(y - d) * S + x) + ch] : 0.0f);
+    }
+}
+
+// renderHSM: level 0 (PrepareMinMax.frag) and levels 1..L (MinMax.frag),
+// float2 per texel; level k is (S >> k) x (T >> k).
+std::vector<std::vector<float>> hsm_levels(const float* depth, int S, int T, float alpha, float beta, int L) {
+    std::vector<std::vector<float>> lv(L + 1);
+    lv[0].resize((size_t)S * T * 2);
+    for (size_t i = 0; i < (size_t)S * T; ++i) {
+        const float d = depth[i];
+        const float mn = d == 0.0f ? 1.0f : d;
+        lv[0][2 * i] = mn + alpha;
+        lv[0][2 * i + 1] = d + beta;
+    }
+    for (int k = 1; k <= L; ++k) {
+        const int pw = S >> (k - 1), ph = T >> (k - 1), w = S >> k, h = T >> k;
+        const std::vector<float>& in = lv[k - 1];
+        lv[k].resize((size_t)w * h * 2);
+        auto tex = [&](int i, int j, int ch) {
+            return (i >= 0 && i < pw && j >= 0 && j < ph) ? in[2 * ((size_t)j * pw + i) + ch] : 0.0f;
+        };
+        // a read at a half-texel position: the 2 x 2 block from (i0, j0),
+        // bilinear weights 0.25 in moment_fetch's order
+        auto quad = [&](int i0, int j0, int ch) {
+            return ((0.25f * tex(i0, j0, ch) + 0.25f * tex(i0 + 1, j0, ch)) + 0.25f * tex(i0, j0 + 1, ch)) +
+                   0.25f * tex(i0 + 1, j0 + 1, ch);
+        };
+        for (int j = 0; j < h; ++j)
+            for (int i = 0; i < w; ++i) {
+                // shadowValues[0..3]: (-, -), (-, +), (+, -), (+, +) offsets
+                // of one output texel = two input texels
+                const int xa = 2 * i - 2, xb = 2 * i + 2, ya = 2 * j - 2, yb = 2 * j + 2;
+                const float mn = gmin(quad(xa, ya, 0), gmin(quad(xa, yb, 0), gmin(quad(xb, ya, 0), quad(xb, yb, 0))));
+                const float mx = gmax(quad(xa, ya, 1), gmax(quad(xa, yb, 1), gmax(quad(xb, ya, 1), quad(xb, yb, 1))));
+                lv[k][2 * ((size_t)j * w + i)] = mn;
+                lv[k][2 * ((size_t)j * w + i) + 1] = mx;
+            }
+    }
+    return lv;
+}
+
+// computeVisibilityFromHSM's lod (PlausibleSoftShadow.frag:538-539)
+float hsm_lod(int S) { return S > 1024 ? 1.75f : (float)S / 1024.0f + 0.5f; }
+
+// bilinear read of an n-channel level (the formula of moment_fetch)
+void bilinear(const float* tex, int W, int H, int nch, float s, float t, float* out) {
+    const float u = s * (float)W - 0.5f, v = t * (float)H - 0.5f;
+    for (int ch = 0; ch < nch; ++ch) out[ch] = 0.0f;
+    if (!(u > -2.0f && u < (float)W + 1.0f && v > -2.0f && v < (float)H + 1.0f)) return;
+    const float fu = std::floor(u), fv = std::floor(v);
+    const int i0 = (int)fu, j0 = (int)fv;
+    const float a = u - fu, b = v - fv;
+    const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    for (int ch = 0; ch < nch; ++ch) {
+        float T[4];
+        for (int k = 0; k < 4; ++k) {
+            const int i = i0 + (k & 1), j = j0 + (k >> 1);
+            T[k] = (i >= 0 && i < W && j >= 0 && j < H) ? tex[nch * ((size_t)j * W + i) + ch] : 0.0f;
+        }
+        out[ch] = ((w00 * T[0] + w10 * T[1]) + w01 * T[2]) + w11 * T[3];
+    }
+}
+
+V4 mom_at(const Ctx& c, float s, float t) {
+    V4 r;
+    bilinear(c.mom, c.W, c.H, 4, s, t, &r.x);
+    return r;
+}
+
+float nonlinearize(float d) { return -(2.0f - d * 1001.0f) / (d * 999.0f); }
+
+// chebyshevUpperBound (PlausibleSoftShadow.frag:78-91)
+float chebyshev_soft(float mx, float my, float z) {
+    if (z <= mx) return 1.0f;
+    const float variance = my - mx * mx;
+    const float d = z - mx;
+    float p_max = variance / (variance + d * d);
+    const float p = z <= mx ? 1.0f : 0.0f;
+    return gmax(p, p_max);
+}
+
+// The SAT branch shared by the filters and blocker estimates: the box from
+// the four corner reads, (D + A - B - C) / (SATFilterSize^2).
+V4 sat_box(const Ctx& c, V4 n, float width, float step) {
+    const float div = 2.0f * width / step;
+    const float size = div / 2.0f;
+    const float xmax = n.x + div * step, xmin = n.x - (div + 1.0f) * step;
+    const float ymax = n.y + div * step, ymin = n.y - (div + 1.0f) * step;
+    const V4 A = mom_at(c, xmin, ymin), B = mom_at(c, xmax, ymin), C = mom_at(c, xmin, ymax), D = mom_at(c, xmax, ymax);
+    const float den = size * size;
+    return V4{(((D.x + A.x) - B.x) - C.x) / den, (((D.y + A.y) - B.y) - C.y) / den, (((D.z + A.z) - B.z) - C.z) / den,
+              (((D.w + A.w) - B.w) - C.w) / den};
+}
+
+// The tap loop: for h, w in [-fw, fw] sum the bilinear reads at
+// n.xy + (w, h) * width / fw, then / float(count * count).
+V4 loop_box(const Ctx& c, V4 n, float width, int count) {
+    const float fw = ((float)count - 1.0f) * 0.5f;
+    V4 acc{0.0f, 0.0f, 0.0f, 0.0f};
+    for (int h = (int)(-fw); (float)h <= fw; h++)
+        for (int w = (int)(-fw); (float)w <= fw; w++) {
+            const V4 t = mom_at(c, n.x + ((float)w * width) / fw, n.y + ((float)h * width) / fw);
+            acc = V4{acc.x + t.x, acc.y + t.y, acc.z + t.z, acc.w + t.w};
+        }
+    const float den = (float)(count * count);
+    return V4{acc.x / den, acc.y / den, acc.z / den, acc.w / den};
+}
+
+V4 box(const Ctx& c, V4 n, float width, float step, int count) {
+    return c.p->summed_area_table ? sat_box(c, n, width, step) : loop_box(c, n, width, count);
+}
+
+// VSM (:400-440)
+float soft_vsm(const Ctx& c, float pw, V4 n) {
+    const int K = c.p->kernel_size;
+    const float step = 2.0f * pw / (float)K;
+    if (step <= 0.0f || step >= 1.0f) return 1.0f;
+    const V4 m = box(c, n, pw, step, K);
+    const float mx = m.x + 0.5f, my = m.y + 0.5f;
+    return gclamp(gmix(chebyshev_soft(mx, my, gl_linearize(n.z)), 1.0f, c.I), 0.0f, 1.0f);
+}
+
+// computeAverageBlockerDepthBasedOnVSM (:196-244)
+float vsm_blocker(const Ctx& c, V4 n) {
+    const float bsw = blocker_search_width(c);
+    const int B = c.p->blocker_search_size;
+    const float step = 2.0f * bsw / (float)B;
+    const float zun = gl_linearize(n.z);
+    const V4 m = box(c, n, bsw, step, B);
+    const float mx = m.x + 0.5f, my = m.y + 0.5f;
+    const float prob = chebyshev_soft(mx, my, zun);
+    float zocc = nonlinearize((mx - prob * zun) / (1.0f - prob));
+    if (prob > 0.99f) zocc = 1.0f;
+    return zocc;
+}
+
+// computeAverageBlockerDepthBasedOnESM (:246-301)
+float esm_blocker(const Ctx& c, V4 n) {
+    const float bsw = blocker_search_width(c);
+    const int B = c.p->blocker_search_size;
+    const float step = 2.0f * bsw / (float)B;
+    const V4 s = box(c, n, bsw, step, B);
+    const float lz = gl_linearize(n.z);
+    const float prob = std::exp(-80.0f * lz) * s.y;
+    if (prob > 0.91f) return 1.0f;
+    const float zocc = (s.x - std::exp(-80.0f * lz) * s.z) / (1.0f - prob);
+    return nonlinearize(zocc);
+}
+
+// ESM (:442-490)
+float soft_esm(const Ctx& c, float pw, V4 n) {
+    const int K = c.p->kernel_size;
+    const float step = 2.0f * pw / (float)K;
+    if (step <= 0.0f || step >= 1.0f) return 1.0f;
+    const float avg = box(c, n, pw, step, K).y;
+    const float dist = mom_at(c, n.x, n.y).x + 0.0001f;
+    const float lz = gl_linearize(n.z);
+    float vis = std::exp(-80.0f * lz) * avg;
+    vis = gclamp(vis, c.I, 1.0f);
+    if (dist > lz && vis == c.I) return 1.0f;
+    return vis;
+}
+
+// computeMomentDepthsFromMSM / computeWeightsFromMSM /
+// computeShadowIntensityFromMSM (:93-164): b, then the three depths
+struct Msm {
+    V4 b;
+    float zx, zy, zz;
+};
+
+Msm msm_solve(const V4& moments, float lz) {
+    float mq[16], mqi[16];
+    msm_quantization(mq, mqi);
+    V4 b = V4{moments.x - 0.0359558848f, moments.y - 0.0f, moments.z - 0.0f, moments.w - 0.0f};
+    b = mat4_mul(mqi, b);
+    const float bias = 0.00003f;
+    const float ob = 1.0f - bias, hb = bias * 0.5f;
+    b = V4{ob * b.x + hb, ob * b.y + hb, ob * b.z + hb, ob * b.w + hb};
+    const float dx = 1.0f, dy = lz, dz = lz * lz;
+    const float L10 = b.x, L20 = b.y;
+    const float D11 = b.y - L10 * L10;
+    const float L21 = (b.z - L20 * L10) / D11;
+    const float D22 = b.w - L20 * L20 - L21 * L21 * D11;
+    const float y0 = dx;
+    float y1 = dy - L10 * y0;
+    float y2 = dz - L20 * y0 - L21 * y1;
+    y1 = y1 / D11;
+    y2 = y2 / D22;
+    const float cz = y2, cy = y1 - L21 * cz, cx = y0 - L10 * cy - L20 * cz;
+    const float p = cy / cz, q = cx / cz;
+    const float D = ((p * p) / 4.0f) - q;
+    const float r = std::sqrt(D);
+    return Msm{b, lz, -(p / 2.0f) - r, -(p / 2.0f) + r};
+}
+
+// computeAverageBlockerDepthBasedOnMSM (:303-363)
+float msm_blocker(const Ctx& c, V4 n) {
+    const float bias = 0.01f;
+    const float bsw = c.p->light_radius / (float)c.W;
+    const int B = c.p->blocker_search_size;
+    const float step = 2.0f * bsw / (float)B;
+    const Msm z = msm_solve(box(c, n, bsw, step, B), gl_linearize(n.z));
+    const V4& b = z.b;
+    const float wx = (z.zy * z.zz - b.x * (z.zy + z.zz) + b.y) / ((z.zx - z.zy) * (z.zx - z.zz));
+    const float wy = (z.zx * z.zz - b.x * (z.zx + z.zz) + b.y) / ((z.zz - z.zy) * (z.zx - z.zy));
+    const float wz = 1.0f - wx - wy;
+    const float ky = 1.0f - wy, kz = 1.0f - wz;
+    float avg = 0.0f, sum = 0.0f;
+    if (z.zx > z.zy) {
+        avg += ky * z.zy;
+        sum += ky;
+    }
+    if (z.zx > z.zz) {
+        avg += kz * z.zz;
+        sum += kz;
+    }
+    avg += bias * z.zx;
+    sum += bias;
+    if (sum > 1.0f - bias) return 1.0f;
+    return nonlinearize(avg / sum);
+}
+
+// MSM (:492-533)
+float soft_msm(const Ctx& c, float pw, V4 n) {
+    const int K = c.p->kernel_size;
+    const float step = 2.0f * pw / (float)K;
+    if (step <= 0.0f || step >= 1.0f) return 1.0f;
+    const Msm z = msm_solve(box(c, n, pw, step, K), gl_linearize(n.z));
+    const V4& b = z.b;
+    if (z.zx <= z.zy) return 1.0f;
+    if (z.zx <= z.zz)
+        return gclamp(1.0f - gclamp((z.zx * z.zz - b.x * (z.zx + z.zz) + b.y) / ((z.zz - z.zy) * (z.zx - z.zy)),
+                                    0.0f, 1.0f),
+                      c.I, 1.0f);
+    return gclamp(1.0f - gclamp(1.0f - (z.zy * z.zz - b.x * (z.zy + z.zz) + b.y) / ((z.zx - z.zy) * (z.zx - z.zz)),
+                                0.0f, 1.0f),
+                  c.I, 1.0f);
+}
+
+// computeVisibilityFromHSM (:535-554)
+float hsm_visibility(const Ctx& c, V4 n) {
+    float lo[2], hi[2];
+    bilinear(c.hsm_lo, c.lo_w, c.lo_h, 2, n.x, n.y, lo);
+    bilinear(c.hsm_hi, c.hi_w, c.hi_h, 2, n.x, n.y, hi);
+    const float f = c.hsm_frac;
+    const float mn = (1.0f - f) * lo[0] + f * hi[0], mx = (1.0f - f) * lo[1] + f * hi[1];
+    if (n.z <= mn) return 1.0f;
+    if (n.z > mx) return c.I;
+    return 0.555f;
+}
+
+float soft_moment_lookup(const Ctx& c, V4 n) {
+    switch (c.p->technique) {
+        case GI_TECH_SAVSM: {  // summedAreaVarianceShadowMapping (:565-572)
+            const float avg = avg_blocker_grid(c, n);
+            return soft_vsm(c, penumbra_width(c, avg, n.z), n);
+        }
+        case GI_TECH_VSSM: {  // varianceSoftShadowMapping (:574-585)
+            const float v = hsm_visibility(c, n);
+            if (v == c.I || v == 1.0f) return v;
+            const float avg = vsm_blocker(c, n);
+            return soft_vsm(c, penumbra_width(c, avg, n.z), n);
+        }
+        case GI_TECH_ESSM:  // exponentialSoftShadowMapping (:587-594)
+            return soft_esm(c, penumbra_width(c, esm_blocker(c, n), n.z), n);
+        default:  // momentSoftShadowMapping (:596-603)
+            return soft_msm(c, penumbra_width(c, msm_blocker(c, n), n.z), n);
+    }
+}
+
 float shade_pixel(const Ctx& c, V4 vertex, V4 normal, const float* poisson) {
     if (vertex.x == 0.0f) return 0.0f;  // discard: the target keeps its clear value 0
     const gi_vis_params* p = c.p;
@@ -1760,6 +2109,12 @@ float shade_pixel(const Ctx& c, V4 vertex, V4 normal, const float* poisson) {
         case GI_TECH_MSM:
             if (sc.w > 0.0f && shadow == 1.0f) shadow = moment_lookup(c, n);
             return shadow;
+        case GI_TECH_SAVSM:
+        case GI_TECH_VSSM:
+        case GI_TECH_ESSM:
+        case GI_TECH_MSSM:
+            if (sc.w > 0.0f && shadow == 1.0f) shadow = soft_moment_lookup(c, n);
+            return shadow;
         case GI_TECH_HARD_SOFTAPP: {
             float r = shadow;
             if (sc.w > 0.0f && r == 1.0f) {
@@ -1788,10 +2143,28 @@ extern "C" void or_visibility(const gi_vis_params* p, const float* depth, int ma
     c.sy = (float)(1.0 / map_h);
     c.I = p->shadow_intensity;
     std::vector<float> moments;
+    std::vector<std::vector<float>> hsm;
     if (p->technique >= GI_TECH_VSM && p->technique <= GI_TECH_MSM) {
         moments = moment_filtered(p->technique, depth, map_w, W);
         c.map = moments.data();
         c.W = c.H = W;
+    }
+    if (is_soft_moment(p->technique)) {
+        moments = soft_moment_map(p->technique, depth, map_w, map_h);
+        if (p->summed_area_table) summed_area_table(moments, map_w, map_h);
+        c.mom = moments.data();
+        if (p->technique == GI_TECH_VSSM) {
+            const float lod = hsm_lod(map_w);
+            const int lo = (int)std::floor(lod);
+            hsm = hsm_levels(depth, map_w, map_h, p->hsm_alpha, p->hsm_beta, lo + 1);
+            c.hsm_lo = hsm[lo].data();
+            c.hsm_hi = hsm[lo + 1].data();
+            c.lo_w = map_w >> lo;
+            c.lo_h = map_h >> lo;
+            c.hi_w = map_w >> (lo + 1);
+            c.hi_h = map_h >> (lo + 1);
+            c.hsm_frac = lod - (float)lo;
+        }
     }
 #pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads(threads))
     for (int y = 0; y < H; ++y)
@@ -1801,6 +2174,20 @@ extern "C" void or_visibility(const gi_vis_params* p, const float* depth, int ma
             V4 nn = {nrm[4 * i], nrm[4 * i + 1], nrm[4 * i + 2], nrm[4 * i + 3]};
             out[i] = shade_pixel(c, v, nn, poisson_xy);
         }
+}
+
+// The light-side maps of the moment soft shadows: the moment map (or its
+// summed-area table) and one min-max level.
+extern "C" void or_soft_moment_map(const gi_vis_params* p, const float* depth, int S, int T, float* out) {
+    std::vector<float> m = soft_moment_map(p->technique, depth, S, T);
+    if (p->summed_area_table) summed_area_table(m, S, T);
+    std::memcpy(out, m.data(), m.size() * sizeof(float));
+}
+
+extern "C" void or_hierarchical_shadow_map(const gi_vis_params* p, const float* depth, int S, int T, int level,
+                                           float* out) {
+    const std::vector<std::vector<float>> lv = hsm_levels(depth, S, T, p->hsm_alpha, p->hsm_beta, level);
+    std::memcpy(out, lv[level].data(), lv[level].size() * sizeof(float));
 }
 
 // shadeScene / PhongShading.frag:11-46: shadow * fragmentColor *

@@ -49,6 +49,14 @@ void or_visibility(const gi_vis_params* p, const float* depth, int map_w,
                    int width, int height, const float* poisson_xy,
                    int threads);
 
+/* Moment soft shadows (SoftShadowMapping): the moment map of p->technique
+ * (SAVSM..MSSM) or, with p->summed_area_table, its summed-area table
+ * (float4 [S * T]); and level `level` of the hierarchical min-max map
+ * (float2 [(S >> level) * (T >> level)]). */
+void or_soft_moment_map(const gi_vis_params* p, const float* depth, int S, int T, float* out);
+void or_hierarchical_shadow_map(const gi_vis_params* p, const float* depth, int S, int T, int level,
+                                float* out);
+
 /* Shadow-volume stencil counts (uint8, wrapping). out_depth may be NULL. */
 void or_shadow_volume_counts(const float* points, const float* normals,
                              int nv, const int* indices, int nt,

@@ -39,7 +39,7 @@ def test_bindings_cover_header():
 
 def test_struct_layouts():
     # the ctypes mirrors must match the C layout (checked through sizes)
-    assert C.sizeof(api.VisParams) == 14 * 4 + 16 * 4 * 2 + 9 * 4 + 3 * 4
+    assert C.sizeof(api.VisParams) == 17 * 4 + 16 * 4 * 2 + 9 * 4 + 3 * 4
     assert C.sizeof(api.View) == 12 * 4 + 2 * 4
     assert C.sizeof(api.MapParams) == 6 * 4
 
