@@ -101,10 +101,10 @@ def parse_args():
                     help="training frames (one 256^2 crop each, batch 16) for the surrogate leg")
     ap.add_argument("--profile", action="store_true",
                     help="render --warmup frames and exit (the command profiled with ncu)")
-    ap.add_argument("--profile-case", choices=["frame", "conv", "volumes", "edt"], default="frame",
+    ap.add_argument("--profile-case", choices=["frame", "conv", "volumes", "edt", "sat"], default="frame",
                     help="with --profile: the pcss_1080p frame, three U-Net convolutions at 1080p (d0a, d1a, "
-                         "d2a), the heavy scene's shadow volumes of one light at 960x540, or three EDTSM "
-                         "filters of the 1024^2 frame")
+                         "d2a), the heavy scene's shadow volumes of one light at 960x540, three EDTSM "
+                         "filters of the 1024^2 frame, or three 1024^2 moment map + SAT builds")
     return ap.parse_args()
 
 
@@ -770,19 +770,25 @@ def run_soft_moments(args, ctx, stream, local, flush):
         out["shadowed_fraction"][name] = float(((v > 0.0) & (v < 1.0)).float().mean())
     # the light-side map alone: moment map + log2(S) SAT iterations, written
     # into a caller buffer; algorithmic bytes = the depth read (4 S^2) and the
-    # table written (16 S^2)
+    # table written (16 S^2).  SAVSM's table runs its iterations on the two
+    # non-zero channels, MSSM's on all four.
     peak, peak_kind = measured_hbm_peak()
     out["sat_build"] = {}
-    for side in (1024, 2048):
-        depth = torch.rand(side * side, device="cuda", generator=torch.Generator("cuda").manual_seed(side)) * 0.1 + 0.9
-        tab = torch.empty(side * side * 4, device="cuda")
-        p = gi.ShadowParams.defaults(api.GI_TECH_SAVSM)
-        p.summed_area_table = True
-        ms = timed(lambda: gi.soft_moment_map(ctx, p, depth, side, side, tab, stream))
-        alg = 20 * side * side
-        achieved = alg / (ms / 1000.0) / 1e9
-        out["sat_build"][str(side)] = {"ms": ms, "kernels": 1 + int(np.log2(side)), "algorithmic_bytes": alg,
-                                       "achieved_gbs": achieved, "frac_of_" + peak_kind: achieved / peak}
+    for name, tech in (("savsm", api.GI_TECH_SAVSM), ("mssm", api.GI_TECH_MSSM)):
+        for side in (1024, 2048):
+            depth = torch.rand(side * side, device="cuda",
+                               generator=torch.Generator("cuda").manual_seed(side)) * 0.1 + 0.9
+            tab = torch.empty(side * side * 4, device="cuda")
+            p = gi.ShadowParams.defaults(tech)
+            p.summed_area_table = True
+            ms = timed(lambda: gi.soft_moment_map(ctx, p, depth, side, side, tab, stream))
+            alg = 20 * side * side
+            achieved = alg / (ms / 1000.0) / 1e9
+            launches0 = ctx.launch_count
+            gi.soft_moment_map(ctx, p, depth, side, side, tab, stream)
+            out["sat_build"][f"{name}_{side}"] = {"ms": ms, "launches": ctx.launch_count - launches0,
+                                                  "algorithmic_bytes": alg, "achieved_gbs": achieved,
+                                                  "frac_of_" + peak_kind: achieved / peak}
     return out
 
 
@@ -809,6 +815,21 @@ def run_profile_case(args, local):
             edt()
         torch.cuda.synchronize()
         print(json.dumps({"profile_case": "edt", "checksum": float(out[..., 0].sum())}), flush=True)
+        ctx.close()
+        return 0
+    if args.profile_case == "sat":
+        from globalillumination_gb300 import _capi as api
+
+        ctx = gi.Context(local)
+        side = 1024
+        depth = torch.rand(side * side, device="cuda", generator=torch.Generator("cuda").manual_seed(side)) * 0.1 + 0.9
+        tab = torch.empty(side * side * 4, device="cuda")
+        p = gi.ShadowParams.defaults(api.GI_TECH_SAVSM)
+        p.summed_area_table = True
+        for _ in range(3):
+            gi.soft_moment_map(ctx, p, depth, side, side, tab)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "sat", "checksum": float(tab[-4:].sum())}), flush=True)
         ctx.close()
         return 0
     if args.profile_case == "conv":

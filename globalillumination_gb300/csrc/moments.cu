@@ -30,7 +30,8 @@
 //   k_moment_blur   GaussianFilter.frag (VSM, EVSM, MSM) or
 //                   LogGaussianFilter.frag (ESM), one direction per launch
 //   k_soft_moments  SoftShadowMapping's Moments.frag / Exponential.frag
-//   k_sat_level     one horizontal + vertical SAT iteration
+//   k_sat_level     one horizontal + vertical SAT iteration (float4, or
+//   k_sat_level2    .xy only for SAVSM / VSSM)
 //   k_hsm_first / k_hsm_next / k_hsm_level0
 //                   PrepareMinMax.frag and MinMax.frag levels
 #include <cuda_runtime.h>
@@ -177,6 +178,7 @@ __global__ void __launch_bounds__(256) k_moment_blur(const float4* __restrict__ 
 struct SoftMomArgs {
     const float* depth;  // S x T light map
     float4* out;         // S x T moment map
+    float2* out2;        // or its .xy only (SAVSM / VSSM, whose .zw are 0)
     int S, T, tech;
     float mq[16], tq0;
 };
@@ -187,6 +189,7 @@ __device__ __forceinline__ float soft_lin_at(const SoftMomArgs& a, int x, int y,
     return gl_linearize(d);
 }
 
+template <bool TWO>
 __global__ void __launch_bounds__(256) k_soft_moments(const SoftMomArgs a) {
     const int x = blockIdx.x * 32 + (threadIdx.x & 31);
     const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
@@ -215,7 +218,8 @@ __global__ void __launch_bounds__(256) k_soft_moments(const SoftMomArgs a) {
             o = make_float4(d - 0.5f, d * d + (0.25f * (dx * dx + dy * dy) - 0.5f), 0.0f, 0.0f);
         }
     }
-    a.out[(size_t)y * a.S + x] = o;
+    if (TWO) a.out2[(size_t)y * a.S + x] = make_float2(o.x, o.y);
+    else a.out[(size_t)y * a.S + x] = o;
 }
 
 // One iteration i of the summed-area table (SATHorizontalPass.frag then
@@ -235,6 +239,25 @@ __global__ void __launch_bounds__(256) k_sat_level(const float4* __restrict__ in
     const float4 c = u ? in[(size_t)(y - d) * S + x] : z;
     const float4 e = (l && u) ? in[(size_t)(y - d) * S + x - d] : z;
     out[(size_t)y * S + x] = add4(add4(a, b), add4(c, e));
+}
+
+// The same over the .xy of SAVSM / VSSM tables, whose .zw stay +0 (sums of
+// +0): half the traffic; the last iteration writes the float4 table.
+template <bool LAST>
+__global__ void __launch_bounds__(256) k_sat_level2(const float2* __restrict__ in, int S, int T, int d,
+                                                    float2* __restrict__ out2, float4* __restrict__ out4) {
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= S || y >= T) return;
+    const float2 z = make_float2(0.0f, 0.0f);
+    const bool l = x >= d, u = y >= d;
+    const float2 a = in[(size_t)y * S + x];
+    const float2 b = l ? in[(size_t)y * S + x - d] : z;
+    const float2 c = u ? in[(size_t)(y - d) * S + x] : z;
+    const float2 e = (l && u) ? in[(size_t)(y - d) * S + x - d] : z;
+    const float sx = (a.x + b.x) + (c.x + e.x), sy = (a.y + b.y) + (c.y + e.y);
+    if (LAST) out4[(size_t)y * S + x] = make_float4(sx, sy, 0.0f, 0.0f);
+    else out2[(size_t)y * S + x] = make_float2(sx, sy);
 }
 
 // renderHSM (main.cpp:696-751).  Level 0 (PrepareMinMax.frag) is
@@ -322,6 +345,40 @@ gi_status launch_soft_moment_map(gi_context* ctx, const gi_vis_params* p, const 
     const size_t n = (size_t)S * T;
     const bool sat = p->summed_area_table != 0;
     const int m = sat ? sat_iterations(S) : 0;
+    const bool two = m > 0 && (p->technique == GI_TECH_SAVSM || p->technique == GI_TECH_VSSM);
+    SoftMomArgs a;
+    a.depth = d_depth;
+    a.S = S;
+    a.T = T;
+    a.tech = p->technique;
+    float mqi[16];
+    moment_quantization(a.mq, mqi, &a.tq0);
+    const dim3 grid((S + 31) / 32, (T + 7) / 8);
+    if (two) {
+        // .xy planes ping-pong in the scratch, the last iteration writes the
+        // float4 table into dst (or the scratch's first part)
+        const size_t fin = dst ? 0 : n * sizeof(float4);
+        gi_status s = ensure_buffer(reinterpret_cast<void**>(&ctx->d_mom), &ctx->cap_mom, fin + 2 * n * sizeof(float2));
+        if (s != GI_OK) return s;
+        float4* last = dst ? dst : reinterpret_cast<float4*>(ctx->d_mom);
+        float2* pa = reinterpret_cast<float2*>(static_cast<char*>(ctx->d_mom) + fin);
+        float2* pb = pa + n;
+        a.out = nullptr;
+        a.out2 = pa;
+        k_soft_moments<true><<<grid, 256, 0, st>>>(a);
+        ctx->launches++;
+        const float2* cur = pa;
+        for (int i = 0; i < m; ++i) {
+            float2* nxt = (cur == pa) ? pb : pa;
+            if (i == m - 1) k_sat_level2<true><<<grid, 256, 0, st>>>(cur, S, T, 1 << i, nullptr, last);
+            else k_sat_level2<false><<<grid, 256, 0, st>>>(cur, S, T, 1 << i, nxt, nullptr);
+            ctx->launches++;
+            cur = nxt;
+        }
+        *out = last;
+        cudaError_t e = cudaGetLastError();
+        return e == cudaSuccess ? GI_OK : fail_cuda(e, "soft moment map launch");
+    }
     // m + 1 writes (the moment map, then one per SAT iteration) alternate
     // between two buffers so that the last lands in dst (or in the scratch)
     const size_t scratch = dst ? (m > 0 ? 1 : 0) : (m > 0 ? 2 : 1);
@@ -330,16 +387,9 @@ gi_status launch_soft_moment_map(gi_context* ctx, const gi_vis_params* p, const 
     if (s != GI_OK) return s;
     float4* last = dst ? dst : reinterpret_cast<float4*>(ctx->d_mom);
     float4* spare = dst ? reinterpret_cast<float4*>(ctx->d_mom) : last + n;
-    SoftMomArgs a;
-    a.depth = d_depth;
     a.out = (m % 2 == 0) ? last : spare;
-    a.S = S;
-    a.T = T;
-    a.tech = p->technique;
-    float mqi[16];
-    moment_quantization(a.mq, mqi, &a.tq0);
-    const dim3 grid((S + 31) / 32, (T + 7) / 8);
-    k_soft_moments<<<grid, 256, 0, st>>>(a);
+    a.out2 = nullptr;
+    k_soft_moments<false><<<grid, 256, 0, st>>>(a);
     ctx->launches++;
     float4* cur = a.out;
     for (int i = 0; i < m; ++i) {
