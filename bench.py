@@ -31,8 +31,9 @@ Extra legs in the same line (not the headline):
               as one CUDA graph, shadow-volume stencil counts, and the
               surrogate's 4K frame
   area_light_ground_truth  the reference's Monte-Carlo area light (17 x 17
-              point-light maps) for the 1080p frame, and the error of
-              PCSS and of the surrogate against it
+              point-light maps) for the 1080p frame, its adaptive
+              (quad-tree) sampling of the same light, and the error of
+              PCSS and of the surrogate against the uniform estimate
   edt_soft_shadows  ShadowMapping's EDTSM mode at its 1024 x 1024 window:
               the PBA exact distance transform over the sites of the
               SMSR hard-shadow image plus the penumbra normalisation
@@ -514,11 +515,27 @@ def run_area_light(args, ctx, stream, local, w, fr, bufs, net=None):
     ev1.record(stream)
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
+    # the reference's adaptive (quad-tree) sampling of the same light: the
+    # maps its evaluation asks for, weighted by level (one host round trip
+    # per evaluated node)
+    adapt = torch.empty(W * H, device="cuda")
+    gi.area_light_adaptive(ctx, w.scene, w.light, 2.0 * w.params.light_radius, w.map_params, fr.camera_mvp,
+                           w.params.shadow_intensity, W, H, adapt, stream=stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, a_views, a_levels = gi.area_light_adaptive(ctx, w.scene, w.light, 2.0 * w.params.light_radius, w.map_params,
+                                                  fr.camera_mvp, w.params.shadow_intensity, W, H, adapt,
+                                                  stream=stream)
+    torch.cuda.synchronize()
+    adaptive_ms = (time.perf_counter() - t0) * 1000.0
     gi.render_frame(ctx, w.scene, fr, w.map_params, w.params, W, H, bufs, stream)
     torch.cuda.synchronize()
     geo = truth > 0
     out = {"samples": len(views), "map": f"{S}x{S}", "ms": ms,
            "light_maps_per_s": len(views) * 1000.0 / ms,
+           "adaptive": {"maps": len(a_views), "ms_wall": adaptive_ms,
+                        "levels": {str(k): int((a_levels == k).sum()) for k in range(5)},
+                        "mae_vs_uniform_geometry_pixels": float((adapt - truth)[geo].abs().mean())},
            "soft_pixel_fraction": float(((truth > 0.25) & (truth < 1.0)).float().mean()),
            "pcss_poisson_mae_all_pixels": float((bufs.vis - truth).abs().mean()),
            "pcss_poisson_mae_geometry_pixels": float((bufs.vis - truth)[geo].abs().mean())}

@@ -118,6 +118,7 @@ extern "C" void gi_context_destroy(gi_context* c) {
     cudaFree(c->d_mom);
     cudaFree(c->d_mom_blur);
     cudaFree(c->d_hsm);
+    cudaFree(c->d_area_gbuf);
     cudaFree(c->d_pba_near);
     cudaFree(c->d_edt_meanx);
     for (int i = 0; i < 8; ++i) cudaFree(c->bin_buf[i]);
@@ -610,12 +611,294 @@ extern "C" gi_status gi_area_light_visibility(gi_context* ctx, const gi_scene* s
                                       mp->offset_factor, mp->offset_units, ctx->d_area_maps + (size_t)k * S * S,
                                       small_px_default(), cs);
             for (int c = 0; c < 4; ++c) wave.trans[k][c] = biased[(size_t)i * 16 + 12 + c];
+            wave.weight[k] = 1.0f;  // the uniform branch's accFactor
         }
         if (st == GI_OK)
             st = gi::launch_area_accumulate(ctx, s, camera_mvp, W, H, ctx->d_area_maps, S, nw, wave,
-                                            shadow_intensity, w0 == 0, w0 + nw == n ? n : 0, d_vis, cs);
+                                            shadow_intensity, w0 == 0, w0 + nw == n, (float)n, d_vis, cs);
     }
     return st;
+}
+
+// ---- adaptive area-light sampling -----------------------------------------
+// SoftShadowMapping's adaptiveSampling (main.cpp:440-690, 820-870) over a
+// QuadTreeLightSource (QuadTreeLightSource.cpp): the tree is evaluated
+// depth first as the reference does, so that every sample map is rendered
+// by the node that reaches its grid position first (its eye comes from that
+// node's own chain of float additions) and maps are numbered in the
+// reference's order, which is the order the final pass sums them in.
+namespace {
+
+struct QtNode {
+    int level;
+    float ref_eye[3], ref_at[3];
+    int kids[4];  // indices into QtRun::nodes, -1 without children
+};
+
+struct QtMap {
+    float eye[3], at[3];
+    float mvp[16], biased[16];
+    float level;  // accFactor[]: the level of the last leaf that used the map
+};
+
+struct QtRun {
+    gi_context* ctx;
+    const gi_scene* scene;
+    gi_view light;
+    float size;
+    int max_level;
+    const gi_map_params* mp;
+    int S, W, H;
+    cudaStream_t cs;
+    float* pos;
+    unsigned char* sums;
+    unsigned* passed;
+    int hash[17][17];
+    std::vector<QtNode> nodes;
+    std::vector<QtMap> maps;
+};
+
+// QuadTreeLightSource::computeUniformSamples (corner `index` of a node at
+// `level`) and computeReferenceSamples (the reference point of child
+// `index`): sample[0] += -step + 2 step (index % 2), sample[1] likewise with
+// index / 2, step = size / 2^(level + 1) or size / 2^(level + 2).
+void qt_offset(const float ref[3], float size, int div_pow, int index, float out[3]) {
+    const int div = (int)powf(2.0f, (float)div_pow);
+    const float step = size / (float)div;
+    out[0] = ref[0];
+    out[1] = ref[1];
+    out[2] = ref[2];
+    out[0] += -step + (2.0f * step * (float)(index % 2));
+    out[1] += -step + (2.0f * step * (float)(index / 2));
+}
+
+// computeChildIndices (main.cpp:423-436)
+void qt_children(int level, int node, int child[4]) {
+    const int div = (int)powf(2.0f, (float)level);
+    const int x = node % div, y = node / div;
+    const int base = 2 * x + (int)powf(2.0f, (float)(level + 2)) * y;
+    child[0] = base;
+    child[1] = base + 1;
+    child[2] = base + (int)powf(2.0f, (float)(level + 1));
+    child[3] = base + (int)powf(2.0f, (float)(level + 1)) + 1;
+}
+
+// The map of grid position (x, y) for corner `index` of `node`: reused if
+// rendered, else rendered now (displaySceneFromLightPOV into the next layer).
+gi_status qt_map(QtRun& r, const QtNode& node, int index, int x, int y, int* out) {
+    if (r.hash[x][y] >= 0) {
+        *out = r.hash[x][y];
+        return GI_OK;
+    }
+    QtMap m;
+    qt_offset(node.ref_eye, r.size, node.level + 1, index, m.eye);
+    qt_offset(node.ref_at, r.size, node.level + 1, index, m.at);
+    gi_view v = r.light;
+    for (int c = 0; c < 3; ++c) {
+        v.eye[c] = m.eye[c];
+        v.at[c] = m.at[c];
+    }
+    gi_frame_matrices fm;
+    gi_status st = gi_frame_setup(&v, &v, &fm);
+    if (st != GI_OK) return st;
+    std::memcpy(m.mvp, fm.light_mvp, 64);
+    std::memcpy(m.biased, fm.light_mvp_biased, 64);
+    m.level = 0.0f;
+    const int idx = (int)r.maps.size();
+    st = gi::raster_depth_map(r.ctx, r.scene, m.mvp, r.S, r.S, r.mp->bias_mode, r.mp->constant_bias,
+                              r.mp->offset_factor, r.mp->offset_units, r.ctx->d_area_maps + (size_t)idx * r.S * r.S,
+                              small_px_default(), r.cs);
+    if (st != GI_OK) return st;
+    r.maps.push_back(m);
+    r.hash[x][y] = idx;
+    *out = idx;
+    return GI_OK;
+}
+
+void qt_corner(int level, int node, int index, int* x, int* y) {
+    const int cf = (int)(16.0f / powf(2.0f, (float)level)), pf = (int)powf(2.0f, (float)level);
+    *x = (index % 2) * cf + (node % pf) * cf;
+    *y = (index / 2) * cf + (node / pf) * cf;
+}
+
+// evaluateSubAreaLightSource (main.cpp:440-570, div = 1): the node's four
+// corner maps, the reprojection and the evaluation's occlusion query.
+gi_status qt_evaluate_sub(QtRun& r, int n, int node, bool* subdivide) {
+    gi::QuadCorners q;
+    for (int index = 0; index < 4; ++index) {
+        int x, y, idx;
+        qt_corner(r.nodes[n].level, node, index, &x, &y);
+        gi_status st = qt_map(r, r.nodes[n], index, x, y, &idx);
+        if (st != GI_OK) return st;
+        q.maps[index] = r.ctx->d_area_maps + (size_t)idx * r.S * r.S;
+        std::memcpy(q.mvp[index], r.maps[idx].biased, 64);
+    }
+    cudaError_t e = cudaMemsetAsync(r.passed, 0, sizeof(unsigned), r.cs);
+    if (e != cudaSuccess) return gi::fail_cuda(e, "gi_area_light_adaptive: flag");
+    gi_status st = gi::launch_qt_evaluate(r.ctx, r.pos, r.W, r.H, q, r.S, r.sums, r.passed, r.cs);
+    if (st != GI_OK) return st;
+    unsigned h = 0;
+    e = cudaMemcpyAsync(&h, r.passed, sizeof h, cudaMemcpyDeviceToHost, r.cs);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(r.cs);
+    if (e != cudaSuccess) return gi::fail_cuda(e, "gi_area_light_adaptive: query");
+    *subdivide = h != 0;
+    return GI_OK;
+}
+
+// evaluateAreaLightSource (main.cpp:572-629, the refinement path)
+gi_status qt_evaluate(QtRun& r, int n, int node) {
+    if (r.nodes[n].level == r.max_level) return GI_OK;
+    int child[4];
+    qt_children(r.nodes[n].level, node, child);
+    bool sub = false;
+    gi_status st = qt_evaluate_sub(r, n, node, &sub);
+    if (st != GI_OK || !sub) return st;
+    // QuadTreeLightSource::subdivide
+    for (int c = 0; c < 4; ++c) {
+        QtNode k;
+        k.level = r.nodes[n].level + 1;
+        qt_offset(r.nodes[n].ref_eye, r.size, r.nodes[n].level + 2, c, k.ref_eye);
+        qt_offset(r.nodes[n].ref_at, r.size, r.nodes[n].level + 2, c, k.ref_at);
+        k.kids[0] = k.kids[1] = k.kids[2] = k.kids[3] = -1;
+        r.nodes[n].kids[c] = (int)r.nodes.size();
+        r.nodes.push_back(k);
+    }
+    for (int c = 0; c < 4 && st == GI_OK; ++c) st = qt_evaluate(r, r.nodes[n].kids[c], child[c]);
+    return st;
+}
+
+// renderAreaLightSource / renderSubAreaLightSource (main.cpp:631-690): the
+// leaves' corner maps (rendering those the evaluation did not), each map
+// taking the level of the last leaf that uses it.
+gi_status qt_render(QtRun& r, int n, int node) {
+    if (r.nodes[n].kids[0] >= 0) {
+        int child[4];
+        qt_children(r.nodes[n].level, node, child);
+        for (int c = 0; c < 4; ++c) {
+            gi_status st = qt_render(r, r.nodes[n].kids[c], child[c]);
+            if (st != GI_OK) return st;
+        }
+        return GI_OK;
+    }
+    for (int index = 0; index < 4; ++index) {
+        int x, y, idx;
+        qt_corner(r.nodes[n].level, node, index, &x, &y);
+        gi_status st = qt_map(r, r.nodes[n], index, x, y, &idx);
+        if (st != GI_OK) return st;
+        r.maps[idx].level = (float)r.nodes[n].level;
+    }
+    return GI_OK;
+}
+
+}  // namespace
+
+extern "C" gi_status gi_area_light_adaptive(gi_context* ctx, const gi_scene* s, const gi_view* light, float size,
+                                            int max_level, const gi_map_params* mp, const float camera_mvp[16],
+                                            float shadow_intensity, int W, int H, float* d_vis, gi_view* samples_out,
+                                            float* levels_out, int* num_samples, void* stream) {
+    gi_status st = check_pass(ctx, s);
+    if (st == GI_OK) st = check_view(light);
+    if (st != GI_OK) return st;
+    if (!mp || !camera_mvp || !d_vis || max_level < 0 || max_level > 4 || !(size >= 0.0f))
+        return fail(GI_ERR_INVALID_ARG, "gi_area_light_adaptive: bad arguments (0 <= max_level <= 4)");
+    if (mp->width != mp->height) return fail(GI_ERR_INVALID_ARG, "gi_area_light_adaptive: square maps only");
+    st = check_image(mp->width, mp->height, "gi_area_light_adaptive (map)");
+    if (st == GI_OK) st = check_image(W, H, "gi_area_light_adaptive");
+    if (st != GI_OK) return st;
+    if (mp->width > 4096) return fail(GI_ERR_CAPACITY, "gi_area_light_adaptive: maps up to 4096^2 (289 are kept)");
+    if ((size_t)s->dev_triangles >= ((size_t)1 << 29))
+        return fail(GI_ERR_CAPACITY, "gi_area_light_adaptive: more than 2^29 triangles");
+    QtRun r;
+    r.ctx = ctx;
+    r.scene = s;
+    r.light = *light;
+    r.size = size;
+    r.max_level = max_level;
+    r.mp = mp;
+    r.S = mp->width;
+    r.W = W;
+    r.H = H;
+    r.cs = static_cast<cudaStream_t>(stream);
+    for (auto& row : r.hash)
+        for (int& h : row) h = -1;
+    const size_t npx = (size_t)W * H;
+    const size_t map_bytes = (size_t)r.S * r.S * sizeof(float);
+    // every grid position of the 17 x 17 grid is rendered at most once
+    st = gi::ensure_buffer(reinterpret_cast<void**>(&ctx->d_area_maps), &ctx->cap_area_maps, 289 * map_bytes);
+    if (st == GI_OK)
+        st = gi::ensure_buffer(reinterpret_cast<void**>(&ctx->d_area_acc), &ctx->cap_area_acc, npx * sizeof(float));
+    if (st == GI_OK)
+        st = gi::ensure_buffer(reinterpret_cast<void**>(&ctx->d_area_gbuf), &ctx->cap_area_gbuf,
+                               npx * 8 * sizeof(float) + npx + 64);
+    if (st != GI_OK) return st;
+    r.pos = ctx->d_area_gbuf;
+    r.sums = reinterpret_cast<unsigned char*>(ctx->d_area_gbuf + npx * 8);
+    r.passed = reinterpret_cast<unsigned*>(reinterpret_cast<char*>(ctx->d_area_gbuf) +
+                                           ((npx * 8 * sizeof(float) + npx + 15) & ~(size_t)15));
+    // the G-buffer (positions for the reprojections; its keys serve the final pass)
+    st = gi::raster_gbuffer(ctx, s, camera_mvp, W, H, r.pos, r.pos + npx * 4, small_px_default(), r.cs);
+    if (st != GI_OK) return st;
+    // QuadTreeLightSource::buildFirstLevel: the root at the light
+    QtNode root;
+    root.level = 0;
+    for (int c = 0; c < 3; ++c) {
+        root.ref_eye[c] = light->eye[c];
+        root.ref_at[c] = light->at[c];
+    }
+    root.kids[0] = root.kids[1] = root.kids[2] = root.kids[3] = -1;
+    r.nodes.push_back(root);
+    st = qt_evaluate(r, 0, 0);
+    if (st == GI_OK) st = qt_render(r, 0, 0);
+    if (st != GI_OK) return st;
+    const int n = (int)r.maps.size();
+    // AccurateSoftShadow.frag's adaptive branch: configureShadow adds
+    // accFactor * 10000 to each biased translation's w (float), the shader
+    // recovers the level as int(w / 10000) (at most 4) and w - level * 10000,
+    // and weighs the map by 1 / (2^level + 1)^2; the lightMVP uniform is the
+    // last rendered map's
+    gi::AreaWave wave;
+    std::memcpy(wave.common, r.maps[n - 1].biased, 12 * sizeof(float));
+    std::vector<float> tr((size_t)n * 4), wt(n);
+    float count = 0.0f;
+    for (int i = 0; i < n; ++i) {
+        const float* b = r.maps[i].biased;
+        const float w_enc = b[15] + r.maps[i].level * 10000.0f;
+        int ql = (int)(w_enc / 10000.0f);
+        if (ql > 4) ql = 4;
+        const float wv = w_enc - (float)(ql * 10000);
+        float f = 1.0f;
+        for (int e = 1; e <= ql; ++e) f *= 2.0f;
+        f = f + 1.0f;
+        const float acc = 1.0f / (f * f);
+        tr[4 * i] = b[12];
+        tr[4 * i + 1] = b[13];
+        tr[4 * i + 2] = b[14];
+        tr[4 * i + 3] = wv;
+        wt[i] = acc;
+        count += acc;
+    }
+    for (int w0 = 0; w0 < n && st == GI_OK; w0 += 16) {
+        const int nw = std::min(16, n - w0);
+        for (int k = 0; k < nw; ++k) {
+            for (int c = 0; c < 4; ++c) wave.trans[k][c] = tr[4 * (w0 + k) + c];
+            wave.weight[k] = wt[w0 + k];
+        }
+        st = gi::launch_area_accumulate(ctx, s, camera_mvp, W, H, ctx->d_area_maps + (size_t)w0 * r.S * r.S, r.S,
+                                        nw, wave, shadow_intensity, w0 == 0, w0 + nw == n, count, d_vis, r.cs);
+    }
+    if (st != GI_OK) return st;
+    if (num_samples) *num_samples = n;
+    for (int i = 0; i < n; ++i) {
+        if (samples_out) {
+            samples_out[i] = *light;
+            for (int c = 0; c < 3; ++c) {
+                samples_out[i].eye[c] = r.maps[i].eye[c];
+                samples_out[i].at[c] = r.maps[i].at[c];
+            }
+        }
+        if (levels_out) levels_out[i] = r.maps[i].level;
+    }
+    return GI_OK;
 }
 
 extern "C" gi_status gi_phong_shade(gi_context* ctx, const gi_vis_params* vp, const float* d_pos,

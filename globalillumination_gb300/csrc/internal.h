@@ -101,6 +101,8 @@ struct gi_context {
     size_t cap_area_maps = 0;
     float* d_area_acc = nullptr;
     size_t cap_area_acc = 0;
+    float* d_area_gbuf = nullptr;  // adaptive sampling: positions, normals, counts, flag
+    size_t cap_area_gbuf = 0;
     // moment techniques: the S x S moment map plus its first mip level, and
     // the two W x W blur targets (float4)
     void* d_mom = nullptr;

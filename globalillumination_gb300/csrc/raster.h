@@ -47,17 +47,29 @@ gi_status launch_surrogate_finish(gi_context* ctx, const gi_vis_params* p, const
                                   const float* d_head, int head_stride, const void* d_feat, float thr,
                                   float* d_vis, unsigned* d_fallback, cudaStream_t st);
 
-// Area-light ground truth: adds the hard tests of `nw` sample maps (one
-// wave, maps[k] of map_s^2 texels, biased translation columns trans[k]) to
-// every pixel's running sum; `first` starts the sums at 0, and a non-zero
-// `total` finishes them into d_vis (sum / total).
+// Area-light ground truth: adds the weighted hard tests of `nw` sample maps
+// (one wave, maps[k] of map_s^2 texels, biased translation columns
+// trans[k], weights weight[k]) to every pixel's running sum; `first` starts
+// the sums at 0, and `last` finishes them into d_vis (sum / count).
 struct AreaWave {
     float trans[16][4];
+    float weight[16];
     float common[12];  // columns 0..2 of the last sample's biased light MVP
 };
 gi_status launch_area_accumulate(gi_context* ctx, const gi_scene* scene, const float camera_mvp[16], int W, int H,
                                  const float* maps, int map_s, int nw, const AreaWave& wave, float intensity,
-                                 bool first, int total, float* d_vis, cudaStream_t st);
+                                 bool first, bool last, float count, float* d_vis, cudaStream_t st);
+
+// Adaptive sampling: one quad-tree node's reprojection (per-pixel count of
+// its four corner lights that see the pixel, into d_sums) and evaluation
+// (sets *d_passed when a pixel with a count of 1-3 has eight equal
+// neighbours).
+struct QuadCorners {
+    const float* maps[4];
+    float mvp[4][16];  // biased light MVPs, column-major
+};
+gi_status launch_qt_evaluate(gi_context* ctx, const float* d_pos, int W, int H, const QuadCorners& q, int map_s,
+                             unsigned char* d_sums, unsigned* d_passed, cudaStream_t st);
 
 // Deferred Phong shading of the G-buffer with the visibility as shadow
 // term (d_color float4 per pixel or NULL for white); d_out float4.

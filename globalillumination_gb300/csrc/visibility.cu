@@ -1686,7 +1686,7 @@ __global__ void __launch_bounds__(128) k_area_accumulate(
     const unsigned long long* __restrict__ keys, const float* __restrict__ points,
     const float* __restrict__ normals, const int* __restrict__ indices, const dev::Mat4 mvp,
     const unsigned* __restrict__ rec_of, const dev::BRec* __restrict__ recs, const uint4* __restrict__ rres,
-    float* __restrict__ acc, int first, int total, float* __restrict__ out, int W, int H) {
+    float* __restrict__ acc, int first, int last, float count, float* __restrict__ out, int W, int H) {
     int x = blockIdx.x * 32 + (threadIdx.x & 31);
     int y = blockIdx.y * 4 + (threadIdx.x >> 5);
     if (x >= W || y >= H) return;
@@ -1694,7 +1694,7 @@ __global__ void __launch_bounds__(128) k_area_accumulate(
     float4 pv, nv;
     dev::resolve_pixel(__ldcs(keys + i), points, normals, indices, mvp, W, H, x, y, rec_of, recs, rres, pv, nv);
     if (pv.x == 0.0f) {
-        if (total) out[i] = 0.0f;
+        if (last) out[i] = 0.0f;
         return;
     }
     const float* m = wave.common;
@@ -1713,10 +1713,64 @@ __global__ void __launch_bounds__(128) k_area_accumulate(
         const float sz = cz + wave.trans[k][2], sw = cw + wave.trans[k][3];
         c.map = maps + (size_t)k * map_s * map_s;
         const float d = fetch(c, sx / sw, sy / sw);
-        a += ((sz / sw <= d) ? 1.0f : I) * 1.0f;
+        a += ((sz / sw <= d) ? 1.0f : I) * wave.weight[k];
     }
-    if (total) out[i] = a / (float)total;
+    if (last) out[i] = a / count;
     else acc[i] = a;
+}
+
+// ---- adaptive area-light sampling (SoftShadowMapping Shaders/QuadTree) ------
+// Reprojection.frag: how many of a quad-tree node's four corner lights see
+// the pixel (hard tests through each corner's biased MVP, GL_NEAREST with a
+// zero border); background pixels keep the target's clear colour (0.63,
+// stored as 255).
+__global__ void __launch_bounds__(128) k_qt_reproject(const float4* __restrict__ pos, int W, int H,
+                                                      const QuadCorners q, int map_s,
+                                                      unsigned char* __restrict__ sums) {
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int y = blockIdx.y * 4 + (threadIdx.x >> 5);
+    if (x >= W || y >= H) return;
+    const size_t i = (size_t)y * W + x;
+    const float4 pv = pos[i];
+    if (pv.x == 0.0f) {
+        sums[i] = 255;
+        return;
+    }
+    Ctx c;
+    c.W = map_s;
+    c.H = map_s;
+    c.fW = (float)map_s;
+    c.fH = (float)map_s;
+    const V4 v = {pv.x, pv.y, pv.z, pv.w};
+    float sum = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const V4 sc = mat4_mul(q.mvp[k], v);
+        c.map = q.maps[k];
+        const float d = fetch(c, sc.x / sc.w, sc.y / sc.w);
+        sum += (sc.z / sc.w <= d) ? 1.0f : 0.0f;
+    }
+    sums[i] = (unsigned char)sum;
+}
+
+// Evaluation.frag under an occlusion query: a pixel passes when its count
+// is 1, 2 or 3 and all eight neighbours have the same count (a neighbour
+// outside the image reads the border 0, a background one 0.63); any
+// passing pixel asks for the node to be subdivided.
+__global__ void __launch_bounds__(128) k_qt_evaluate(const unsigned char* __restrict__ sums, int W, int H,
+                                                     unsigned* __restrict__ passed) {
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int y = blockIdx.y * 4 + (threadIdx.x >> 5);
+    if (x >= W || y >= H) return;
+    const unsigned s = sums[(size_t)y * W + x];
+    if (s == 255 || s == 0 || s == 4) return;
+    for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+            const int xx = x + dx, yy = y + dy;
+            const unsigned n = (xx >= 0 && xx < W && yy >= 0 && yy < H) ? sums[(size_t)yy * W + xx] : 0u;
+            if (n != s) return;
+        }
+    atomicOr(passed, 1u);
 }
 
 // ---- deferred Phong shading (ShadowMapping/Shaders/GBuffer/PhongShading.frag:11-46)
@@ -1875,16 +1929,26 @@ gi_status launch_phong(gi_context* ctx, const gi_vis_params* p, const float* d_p
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "phong launch");
 }
 
+gi_status launch_qt_evaluate(gi_context* ctx, const float* d_pos, int W, int H, const QuadCorners& q, int map_s,
+                            unsigned char* d_sums, unsigned* d_passed, cudaStream_t st) {
+    dim3 grid((W + 31) / 32, (H + 3) / 4);
+    vis::k_qt_reproject<<<grid, 128, 0, st>>>(reinterpret_cast<const float4*>(d_pos), W, H, q, map_s, d_sums);
+    vis::k_qt_evaluate<<<grid, 128, 0, st>>>(d_sums, W, H, d_passed);
+    ctx->launches += 2;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "quad-tree evaluation launch");
+}
+
 gi_status launch_area_accumulate(gi_context* ctx, const gi_scene* scene, const float camera_mvp[16], int W, int H,
                                  const float* maps, int map_s, int nw, const AreaWave& wave, float intensity,
-                                 bool first, int total, float* d_vis, cudaStream_t st) {
+                                 bool first, bool last, float count, float* d_vis, cudaStream_t st) {
     dim3 grid((W + 31) / 32, (H + 3) / 4);
     dev::Mat4 m;
     for (int k = 0; k < 16; ++k) m.m[k] = camera_mvp[k];
     vis::k_area_accumulate<<<grid, 128, 0, st>>>(
         maps, map_s, nw, wave, intensity, ctx->d_vkeys, scene->d_points, scene->d_normals, scene->d_indices, m,
         static_cast<const unsigned*>(ctx->tier_buf[1][6]), static_cast<const dev::BRec*>(ctx->tier_buf[1][0]),
-        static_cast<const uint4*>(ctx->tier_buf[1][7]), ctx->d_area_acc, first ? 1 : 0, total, d_vis, W, H);
+        static_cast<const uint4*>(ctx->tier_buf[1][7]), ctx->d_area_acc, first ? 1 : 0, last ? 1 : 0, count, d_vis, W, H);
     ctx->launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "area-light accumulate launch");

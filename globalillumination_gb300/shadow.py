@@ -573,6 +573,26 @@ def area_light_visibility(ctx: Context, scene: Scene, samples, mp: MapParams, ca
     return vis
 
 
+def area_light_adaptive(ctx: Context, scene: Scene, light: ViewSpec, size: float, mp: MapParams, camera_mvp,
+                        intensity: float, width: int, height: int, vis, max_level: int = 4, stream=None):
+    """Adaptive (quad-tree) area-light ground truth (SoftShadowMapping adaptiveSampling).
+
+    Returns (vis, samples, levels): the sample views in the order the final pass sums them and the
+    quad-tree level each map is weighted with (1 / (2^level + 1)^2)."""
+    assert vis.is_cuda and vis.numel() >= width * height
+    lv, c = light.to_c(), mp.to_c()
+    out = (api.View * 289)()
+    levels = np.zeros(289, np.float32)
+    n = C.c_int(0)
+    check(_lib().gi_area_light_adaptive(ctx.handle, scene.handle, C.byref(lv), float(size), int(max_level),
+                                        C.byref(c), _f16(camera_mvp), float(intensity), width, height, _ptr(vis),
+                                        out, levels.ctypes.data, C.byref(n), _stream_ptr(stream)),
+          "gi_area_light_adaptive")
+    views = [ViewSpec(eye=tuple(v.eye), at=tuple(v.at), width=v.width, height=v.height, fovy_deg=v.fovy_deg,
+                      znear=v.znear, zfar=v.zfar, up=tuple(v.up)) for v in out[:n.value]]
+    return vis, views, levels[:n.value].copy()
+
+
 class Batch:
     """Many frames (scene, camera, lights) replayed as one CUDA graph (gi_batch_*).
 

@@ -508,6 +508,27 @@ gi_status gi_area_light_visibility(gi_context* ctx, const gi_scene* scene,
                                    float shadow_intensity, int width, int height,
                                    float* d_vis, void* stream);
 
+/* Adaptive area-light ground truth (SoftShadowMapping's adaptiveSampling,
+ * main.cpp:440-690 and 820-870, QuadTreeLightSource.cpp, Shaders/QuadTree/
+ * Reprojection.frag and Evaluation.frag, the adaptive branch of
+ * AccurateSoftShadow.frag:52-133).  A quad tree over the light (side
+ * `size`, corner samples on a 17 x 17 grid) is refined depth first up to
+ * `max_level` (the reference's 4): a node renders the light maps of its
+ * four corners (a grid position is rendered once, by the first node that
+ * reaches it), counts per camera pixel how many corners see it, and
+ * subdivides if a pixel with a count of 1-3 has eight equal neighbours.
+ * The leaves' corners are then rendered if missing and each map takes the
+ * level of the last leaf using it; the visibility is the 1 / (2^level + 1)^2
+ * weighted average of the maps' hard tests (1 or shadow_intensity), the
+ * level carried in the w of each biased translation as the reference's
+ * uniforms carry it.  No pre-test; background 0.  d_vis is
+ * float[width*height]; samples_out (at most 289 views), levels_out (289
+ * floats) and num_samples may be NULL.  Square maps up to 4096^2. */
+gi_status gi_area_light_adaptive(gi_context* ctx, const gi_scene* scene, const gi_view* light, float size,
+                                 int max_level, const gi_map_params* map, const float camera_mvp[16],
+                                 float shadow_intensity, int width, int height, float* d_vis,
+                                 gi_view* samples_out, float* levels_out, int* num_samples, void* stream);
+
 /* ------------------------------------------------------------------ */
 /* A13/A14: shadow volumes with stencil counts                         */
 /* ------------------------------------------------------------------ */

@@ -32,6 +32,7 @@
 #include "gi_oracle.h"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdint>
@@ -2290,6 +2291,246 @@ extern "C" void or_area_light_visibility(const float* points, const float* norma
     float count = 0.0f;
     for (int i = 0; i < n; ++i) count += 1.0f;
     for (size_t q = 0; q < (size_t)W * H; ++q) out[q] = pos[4 * q] == 0.0f ? 0.0f : acc[q] / count;
+}
+
+// Adaptive area-light sampling (SoftShadowMapping adaptiveSampling:
+// main.cpp:423-690, 820-870; QuadTreeLightSource.cpp; Shaders/QuadTree/
+// Reprojection.frag, Evaluation.frag; AccurateSoftShadow.frag adaptive
+// branch), depth first as the reference runs it.  `view_mvp` returns the
+// light MVP and biased MVP of a sample eye / at (the reference's
+// glm::perspective * lookAt, computed by the caller).
+namespace {
+
+struct OrQt {
+    const float *points, *normals;
+    const int* indices;
+    int nv, nt;
+    or_view_mvp_fn view_mvp;
+    void* user;
+    float size;
+    int max_level, S, bias_mode;
+    float cbias, factor, units;
+    int W, H, threads;
+    const float* pos;
+    int hash[17][17];
+    std::vector<std::vector<float>> maps;
+    std::vector<std::array<float, 16>> biased;
+    std::vector<std::array<float, 6>> eyes;
+    std::vector<float> level;
+};
+
+struct OrQtNode {
+    int level;
+    float eye[3], at[3];
+    std::array<int, 4> kids;
+};
+
+void or_qt_offset(const float ref[3], float size, int div_pow, int index, float out[3]) {
+    const int div = (int)std::pow(2.0f, (float)div_pow);
+    const float step = size / (float)div;
+    out[0] = ref[0];
+    out[1] = ref[1];
+    out[2] = ref[2];
+    out[0] += -step + (2.0f * step * (float)(index % 2));
+    out[1] += -step + (2.0f * step * (float)(index / 2));
+}
+
+int or_qt_map(OrQt& q, const OrQtNode& node, int index, int x, int y) {
+    if (q.hash[x][y] >= 0) return q.hash[x][y];
+    std::array<float, 6> e;
+    or_qt_offset(node.eye, q.size, node.level + 1, index, &e[0]);
+    or_qt_offset(node.at, q.size, node.level + 1, index, &e[3]);
+    float mvp[16];
+    std::array<float, 16> b;
+    q.view_mvp(&e[0], &e[3], mvp, b.data(), q.user);
+    std::vector<float> m((size_t)q.S * q.S);
+    or_shadow_map(q.points, q.nv, q.indices, q.nt, mvp, q.S, q.S, q.bias_mode, q.cbias, q.factor, q.units, m.data(),
+                  q.threads);
+    const int idx = (int)q.maps.size();
+    q.maps.push_back(std::move(m));
+    q.biased.push_back(b);
+    q.eyes.push_back(e);
+    q.level.push_back(0.0f);
+    q.hash[x][y] = idx;
+    return idx;
+}
+
+void or_qt_corner(int level, int node, int index, int* x, int* y) {
+    const int cf = (int)(16.0f / std::pow(2.0f, (float)level)), pf = (int)std::pow(2.0f, (float)level);
+    *x = (index % 2) * cf + (node % pf) * cf;
+    *y = (index / 2) * cf + (node / pf) * cf;
+}
+
+void or_qt_children(int level, int node, int child[4]) {
+    const int div = (int)std::pow(2.0f, (float)level);
+    const int x = node % div, y = node / div;
+    const int base = 2 * x + (int)std::pow(2.0f, (float)(level + 2)) * y;
+    const int row = (int)std::pow(2.0f, (float)(level + 1));
+    child[0] = base;
+    child[1] = base + 1;
+    child[2] = base + row;
+    child[3] = base + row + 1;
+}
+
+// Reprojection.frag + Evaluation.frag + the occlusion query's result
+bool or_qt_subdivide(OrQt& q, const int idx[4]) {
+    const int W = q.W, H = q.H;
+    std::vector<float> sum((size_t)W * H);
+    Ctx c;
+    c.p = nullptr;
+    c.W = q.S;
+    c.H = q.S;
+    c.sx = c.sy = 0.0f;
+    c.I = 0.0f;
+    for (size_t p = 0; p < (size_t)W * H; ++p) {
+        const float* v = &q.pos[4 * p];
+        if (v[0] == 0.0f) {
+            sum[p] = 0.63f;  // the reprojection target's clear colour
+            continue;
+        }
+        float s = 0.0f;
+        for (int k = 0; k < 4; ++k) {
+            const V4 sc = mat4_mul(q.biased[idx[k]].data(), V4{v[0], v[1], v[2], v[3]});
+            c.map = q.maps[idx[k]].data();
+            s += (sc.z / sc.w <= fetch(c, sc.x / sc.w, sc.y / sc.w)) ? 1.0f : 0.0f;
+        }
+        sum[p] = s;
+    }
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const float s = sum[(size_t)y * W + x];
+            if (s == 0.63f || s == 0.0f || s == 4.0f || s == 5.0f) continue;
+            bool pass = true;
+            for (int dy = -1; dy <= 1 && pass; ++dy)
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const int xx = x + dx, yy = y + dy;
+                    const float n = (xx >= 0 && xx < W && yy >= 0 && yy < H) ? sum[(size_t)yy * W + xx] : 0.0f;
+                    if (s != n) {
+                        pass = false;
+                        break;
+                    }
+                }
+            if (pass) return true;
+        }
+    return false;
+}
+
+void or_qt_evaluate(OrQt& q, std::vector<OrQtNode>& nodes, int n, int node) {
+    if (nodes[n].level == q.max_level) return;
+    int child[4];
+    or_qt_children(nodes[n].level, node, child);
+    int idx[4];
+    for (int index = 0; index < 4; ++index) {
+        int x, y;
+        or_qt_corner(nodes[n].level, node, index, &x, &y);
+        idx[index] = or_qt_map(q, nodes[n], index, x, y);
+    }
+    if (!or_qt_subdivide(q, idx)) return;
+    for (int c = 0; c < 4; ++c) {
+        OrQtNode k;
+        k.level = nodes[n].level + 1;
+        or_qt_offset(nodes[n].eye, q.size, nodes[n].level + 2, c, k.eye);
+        or_qt_offset(nodes[n].at, q.size, nodes[n].level + 2, c, k.at);
+        k.kids = {-1, -1, -1, -1};
+        nodes[n].kids[c] = (int)nodes.size();
+        nodes.push_back(k);
+    }
+    for (int c = 0; c < 4; ++c) or_qt_evaluate(q, nodes, nodes[n].kids[c], child[c]);
+}
+
+void or_qt_render(OrQt& q, std::vector<OrQtNode>& nodes, int n, int node) {
+    if (nodes[n].kids[0] >= 0) {
+        int child[4];
+        or_qt_children(nodes[n].level, node, child);
+        for (int c = 0; c < 4; ++c) or_qt_render(q, nodes, nodes[n].kids[c], child[c]);
+        return;
+    }
+    for (int index = 0; index < 4; ++index) {
+        int x, y;
+        or_qt_corner(nodes[n].level, node, index, &x, &y);
+        q.level[or_qt_map(q, nodes[n], index, x, y)] = (float)nodes[n].level;
+    }
+}
+
+}  // namespace
+
+extern "C" int or_area_light_adaptive(const float* points, const float* normals, int nv, const int* indices, int nt,
+                                      const float light_eye[3], const float light_at[3], float size, int max_level,
+                                      or_view_mvp_fn view_mvp, void* user, int S, int bias_mode, float cbias,
+                                      float factor, float units, const float camera_mvp[16], float I, int W, int H,
+                                      float* out, float* eyes_out, float* levels_out, int threads) {
+    std::vector<float> pos((size_t)W * H * 4), nrm((size_t)W * H * 4);
+    or_gbuffer(points, normals, nv, indices, nt, camera_mvp, W, H, pos.data(), nrm.data(), threads);
+    OrQt q;
+    q.points = points;
+    q.normals = normals;
+    q.indices = indices;
+    q.nv = nv;
+    q.nt = nt;
+    q.view_mvp = view_mvp;
+    q.user = user;
+    q.size = size;
+    q.max_level = max_level;
+    q.S = S;
+    q.bias_mode = bias_mode;
+    q.cbias = cbias;
+    q.factor = factor;
+    q.units = units;
+    q.W = W;
+    q.H = H;
+    q.threads = threads;
+    q.pos = pos.data();
+    for (auto& row : q.hash)
+        for (int& h : row) h = -1;
+    std::vector<OrQtNode> nodes(1);
+    nodes[0].level = 0;
+    for (int c = 0; c < 3; ++c) {
+        nodes[0].eye[c] = light_eye[c];
+        nodes[0].at[c] = light_at[c];
+    }
+    nodes[0].kids = {-1, -1, -1, -1};
+    or_qt_evaluate(q, nodes, 0, 0);
+    or_qt_render(q, nodes, 0, 0);
+    const int n = (int)q.maps.size();
+    // the final pass: weights from the level carried in each translation's w
+    const float* m = q.biased[n - 1].data();
+    std::vector<float> acc((size_t)W * H, 0.0f);
+    float count = 0.0f;
+    for (int i = 0; i < n; ++i) {
+        const float* b = q.biased[i].data();
+        const float w_enc = b[15] + q.level[i] * 10000.0f;
+        int ql = (int)(w_enc / 10000.0f);
+        if (ql > 4) ql = 4;
+        const float wv = w_enc - (float)(ql * 10000);
+        float f = 1.0f;
+        for (int e = 1; e <= ql; ++e) f *= 2.0f;
+        f = f + 1.0f;
+        const float wt = 1.0f / (f * f);
+        Ctx c;
+        c.p = nullptr;
+        c.map = q.maps[i].data();
+        c.W = S;
+        c.H = S;
+        c.sx = c.sy = 0.0f;
+        c.I = I;
+        for (size_t p = 0; p < (size_t)W * H; ++p) {
+            const float* v = &pos[4 * p];
+            if (v[0] == 0.0f) continue;
+            const float cx = m[0] * v[0] + m[4] * v[1] + m[8] * v[2];
+            const float cy = m[1] * v[0] + m[5] * v[1] + m[9] * v[2];
+            const float cz = m[2] * v[0] + m[6] * v[1] + m[10] * v[2];
+            const float cw = m[3] * v[0] + m[7] * v[1] + m[11] * v[2];
+            const float sx = cx + b[12], sy = cy + b[13], sz = cz + b[14], sw = cw + wv;
+            const float d = fetch(c, sx / sw, sy / sw);
+            acc[p] += ((sz / sw <= d) ? 1.0f : I) * wt;
+        }
+        count += wt;
+        if (eyes_out)
+            for (int k = 0; k < 6; ++k) eyes_out[6 * i + k] = q.eyes[i][k];
+        if (levels_out) levels_out[i] = q.level[i];
+    }
+    for (size_t p = 0; p < (size_t)W * H; ++p) out[p] = pos[4 * p] == 0.0f ? 0.0f : acc[p] / count;
+    return n;
 }
 
 extern "C" void or_rbssm_hits(unsigned long long* out4096, int reset) {

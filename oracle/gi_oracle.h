@@ -77,6 +77,18 @@ void or_area_light_visibility(const float* points, const float* normals, int nv,
                               float factor, float units, const float camera_mvp[16], float I,
                               int W, int H, float* out, int threads);
 
+/* Adaptive (quad-tree) area-light ground truth (SoftShadowMapping
+ * adaptiveSampling).  view_mvp(eye, at, mvp, biased, user) gives the light
+ * matrices of a sample; returns the number of sample maps n and writes the
+ * visibility (out), each map's eye and at (eyes_out, 6 n floats) and level
+ * (levels_out, n floats) in the order the final pass sums them. */
+typedef void (*or_view_mvp_fn)(const float* eye, const float* at, float* mvp, float* biased, void* user);
+int or_area_light_adaptive(const float* points, const float* normals, int nv, const int* indices, int nt,
+                           const float light_eye[3], const float light_at[3], float size, int max_level,
+                           or_view_mvp_fn view_mvp, void* user, int S, int bias_mode, float cbias, float factor,
+                           float units, const float camera_mvp[16], float I, int W, int H, float* out,
+                           float* eyes_out, float* levels_out, int threads);
+
 /* PBA exact distance transform (ShadowMapping/src/EDT/pba2DHost.cu:228-242
  * with the kernels of include/EDT/pba2DKernel.h): sites / out are (x, y)
  * int16 pairs per pixel, a site holding anything but x == -32768; out gets
