@@ -48,7 +48,7 @@ struct gi_batch {
     cudaEvent_t fork = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    int tiny_px = 16;
+    int tiny_px = 96;
     int coop_px = 1024;
     uint64_t launches_per_run = 0;
 };
@@ -319,10 +319,10 @@ extern "C" gi_status gi_batch_autotune(gi_batch* b, void* stream, int repeats, g
         return GI_OK;
     };
     // tier thresholds first (8 streams), then the stream count
-    const int tinies[] = {8, 16, 32, 64};
+    const int tinies[] = {16, 32, 64, 96, 128};
     const int coops[] = {256, 512, 1024};
     const int stream_counts[] = {4, 8, 16, 32};
-    int bt = 16, bc = 1024, bs = 8;
+    int bt = 96, bc = 1024, bs = 8;
     float best = 1e30f;
     gi_status s = GI_OK;
     for (int t : tinies)

@@ -87,7 +87,7 @@ struct gi_context {
     void* tier_buf[2][8] = {};
     size_t tier_cap[2][8] = {};
     // tier thresholds (bounding-box pixels): tiny <= tiny_px < warp <= coop_px
-    int tiny_px = 16;
+    int tiny_px = 96;
     int coop_px = 1024;
     // status words (128): [4..11] counters of the binned raster (records,
     // big records, spills, error bits, admitted big pairs as u64, work

@@ -1382,6 +1382,52 @@ __device__ __forceinline__ void tiny_record(const TierArgs& a, unsigned i) {
     int64_t A[3], B[3];
     bool tl[3];
     rec_edges(r, A, B, tl);
+    // When every edge value over the box fits 32 bits (the usual case: a
+    // vertex far in the guard band is what breaks it), step the edges
+    // incrementally in int32: +A kSub per row, -B kSub per column.  The
+    // values are the same integers, so the tests and conversions are too.
+    {
+        const int w = r.x1 - r.x0 + 1, h = r.y1 - r.y0 + 1;
+        const int64_t cx = (int64_t)r.x0 * kSub + kSub / 2, cy = (int64_t)r.y0 * kSub + kSub / 2;
+        int64_t E0[3];
+        bool fits32 = true;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int ia = (k + 1) % 3;
+            E0[k] = A[k] * (cy - r.Y[ia]) - B[k] * (cx - r.X[ia]);
+            const int64_t bound =
+                abs(E0[k]) + abs(A[k]) * (int64_t)(h - 1) * kSub + abs(B[k]) * (int64_t)(w - 1) * kSub;
+            fits32 &= bound < (1LL << 31);
+        }
+        if (fits32) {
+            // the steps are only added when the box has a next row / column,
+            // and then they are bounded by `bound` too
+            int er[3], sa[3], sb[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                er[k] = (int)E0[k];
+                sa[k] = h > 1 ? (int)(A[k] * kSub) : 0;
+                sb[k] = w > 1 ? (int)(B[k] * kSub) : 0;
+            }
+            for (int y = r.y0;; ++y) {
+                int e0 = er[0], e1 = er[1], e2 = er[2];
+                for (int x = r.x0;; ++x) {
+                    const bool in = (e0 > 0 || (e0 == 0 && tl[0])) && (e1 > 0 || (e1 == 0 && tl[1])) &&
+                                    (e2 > 0 || (e2 == 0 && tl[2]));
+                    if (in) rec_emit<MODE>(a, r, x, y, (float)e1, (float)e2);
+                    if (x == (int)r.x1) break;  // no step past the box: it could leave 32 bits
+                    e0 -= sb[0];
+                    e1 -= sb[1];
+                    e2 -= sb[2];
+                }
+                if (y == (int)r.y1) break;
+                er[0] += sa[0];
+                er[1] += sa[1];
+                er[2] += sa[2];
+            }
+            return;
+        }
+    }
     for (int y = r.y0; y <= (int)r.y1; ++y) {
         const int64_t py = (int64_t)y * kSub + kSub / 2;
         for (int x = r.x0; x <= (int)r.x1; ++x) {

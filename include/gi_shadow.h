@@ -75,7 +75,7 @@ uint64_t gi_context_launch_count(const gi_context* ctx);
 gi_status gi_context_set_profiling(gi_context* ctx, int enable);
 /* Rasteriser tier thresholds (bounding-box pixels): triangles up to
  * tiny_px are drawn by one thread, up to coop_px by one warp, larger ones
- * by tiles (defaults 16 / 1024; 1 <= tiny_px < coop_px <= 1024).  Results
+ * by tiles (defaults 96 / 1024; 1 <= tiny_px < coop_px <= 1024).  Results
  * do not depend on them. */
 gi_status gi_context_set_tuning(gi_context* ctx, int tiny_px, int coop_px);
 gi_status gi_context_phase_ms(gi_context* ctx, float ms[3]);
