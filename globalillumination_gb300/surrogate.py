@@ -326,19 +326,34 @@ class SurrogateFrame:
 
 # ---- training data ---------------------------------------------------------------------
 def training_scene(rng: np.random.Generator, seed: int):
-    """A pcss_1080p-style scene with random sphere count / layout, light and camera."""
+    """A random training scene: mostly pcss_1080p-style sphere fields under an overhead light, a
+    share of displaced spheres under oblique lights, 2048^2 or 4096^2 maps, 1080p or 2160p views
+    (the features measure penumbrae in map texels and screen pixels, so both resolutions are seen)."""
     s = Scene()
     s.ground(10.0, 0.0)
-    spheres = int(rng.integers(16, 96))
-    s.icosphere_field(spheres, 3, (-8.0, 0.2, -8.0), (8.0, 3.0, 8.0), 0.2, 1.0, seed)
-    lx, lz = rng.uniform(-3.0, 3.0, 2)
-    light = ViewSpec(eye=(float(lx), float(rng.uniform(10.0, 14.0)), float(lz)), at=(0.0, 0.0, 0.0),
-                     width=2048, height=2048, fovy_deg=90.0)
+    if rng.random() < 0.3:
+        grid = int(rng.choice([128, 256, 384]))
+        centre = (float(rng.uniform(-3.0, 3.0)), float(rng.uniform(1.8, 3.0)), float(rng.uniform(-3.0, 3.0)))
+        s.displaced_sphere(grid, grid, float(rng.uniform(1.0, 2.2)), float(rng.uniform(0.1, 0.4)), centre,
+                           seed ^ 0x2F5A3C1)
+    else:
+        spheres = int(rng.integers(16, 96))
+        s.icosphere_field(spheres, 3, (-8.0, 0.2, -8.0), (8.0, 3.0, 8.0), 0.2, 1.0, seed)
+    side = 4096 if rng.random() < 0.3 else 2048
+    if rng.random() < 0.3:
+        a = rng.uniform(0, 2 * math.pi)
+        rr = rng.uniform(5.0, 9.0)
+        eye = (float(rr * math.cos(a)), float(rng.uniform(6.0, 10.0)), float(rr * math.sin(a)))
+    else:
+        lx, lz = rng.uniform(-3.0, 3.0, 2)
+        eye = (float(lx), float(rng.uniform(10.0, 14.0)), float(lz))
+    light = ViewSpec(eye=eye, at=(0.0, 0.0, 0.0), width=side, height=side, fovy_deg=90.0)
     az = rng.uniform(0, 2 * math.pi)
-    r = rng.uniform(16.0, 24.0)
+    r = rng.uniform(14.0, 24.0)
+    W, H = (3840, 2160) if rng.random() < 0.25 else (1920, 1080)
     camera = ViewSpec(eye=(float(r * math.sin(az)), float(rng.uniform(8.0, 16.0)), float(-r * math.cos(az))),
-                      at=(0.0, 0.0, 0.0), width=1920, height=1080)
-    mp = MapParams(2048, 2048, bias_mode=api.GI_BIAS_POLYGON_OFFSET, offset_factor=4.0, offset_units=20.0)
+                      at=(0.0, 0.0, 0.0), width=W, height=H)
+    mp = MapParams(side, side, bias_mode=api.GI_BIAS_POLYGON_OFFSET, offset_factor=4.0, offset_units=20.0)
     p = ShadowParams.defaults(api.GI_TECH_PCSS_POISSON)
     p.light_radius = float(rng.uniform(0.1, 0.5))
     p.pcss_min_blocker_depth = 0.0
@@ -357,10 +372,15 @@ def train(ctx: Context, net: UNet, frames: int = 20000, batch: int = 16, crop: i
         s.upload(ctx)
         pool.append((s, light, camera, mp, p))
     dev = net.device
-    W, H = 1920, 1080
-    bufs = allocate_frame(2048, 2048, W, H)
-    feat = torch.empty((1, H, W, FEATURES), dtype=torch.bfloat16, device=dev)
-    depth2 = torch.empty(2048 * 2048, dtype=torch.float32, device=dev)
+    frames_by_shape = {}  # (map side, W, H) -> (frame buffers, features, depth scratch)
+
+    def buffers(side, W, H):
+        if (side, W, H) not in frames_by_shape:
+            frames_by_shape[(side, W, H)] = (allocate_frame(side, side, W, H),
+                                             torch.empty((1, H, W, FEATURES), dtype=torch.bfloat16, device=dev),
+                                             torch.empty(side * side, dtype=torch.float32, device=dev))
+        return frames_by_shape[(side, W, H)]
+
     bfeat = torch.empty((batch, crop, crop, FEATURES), dtype=torch.bfloat16, device=dev)
     btarget = torch.empty((batch, crop, crop), dtype=torch.float32, device=dev)
     head = torch.empty((batch, crop, crop, HEAD), dtype=torch.float32, device=dev)
@@ -376,6 +396,8 @@ def train(ctx: Context, net: UNet, frames: int = 20000, batch: int = 16, crop: i
             le = tuple(float(x) for x in np.asarray(light.eye) + rng.uniform(-1.0, 1.0, 3))
             lv = ViewSpec(eye=le, at=light.at, width=light.width, height=light.height, fovy_deg=light.fovy_deg)
             fr = frame_setup(lv, camera)
+            W, H = camera.width, camera.height
+            bufs, feat, depth2 = buffers(mp.width, W, H)
             render_frame(ctx, s, fr, mp, p, W, H, bufs)
             features(ctx, s, fr, mp, p, W, H, depth2, feat)
             y0 = int(rng.integers(0, H - crop + 1))
