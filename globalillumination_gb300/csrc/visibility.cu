@@ -67,6 +67,15 @@ struct Ctx {
     float sx, sy;
     float I;
     SoftMaps sm;  // moment soft shadows only
+    // PCSS_POISSON: the blocker taps' offsets c_poisson[i] * bsw, rounded as
+    // the multiplication rounds them, computed once per launch (nullptr:
+    // multiply per tap)
+    const float2* boff = nullptr;
+};
+
+// The blocker-search offsets of one launch, a kernel parameter read in place.
+struct PoissonOffsets {
+    float2 b[64];
 };
 
 __device__ __forceinline__ float fetch(const Ctx& c, float s, float t) {
@@ -241,9 +250,18 @@ template <bool FAST>
 __device__ float avg_blocker_poisson_t(const gi_vis_params& p, const Ctx& c, V4 n, float bsw) {
     float avg = 0.0f;
     int nb = 0;
+    const float2* bo = c.boff;
     for (int i = 0; i < p.poisson_blocker_taps; ++i) {
-        float2 o = c_poisson[i];
-        const float s = n.x + o.x * bsw, t = n.y + o.y * bsw;
+        float s, t;
+        if (bo) {
+            const float2 ob = bo[i];
+            s = n.x + ob.x;
+            t = n.y + ob.y;
+        } else {
+            const float2 o = c_poisson[i];
+            s = n.x + o.x * bsw;
+            t = n.y + o.y * bsw;
+        }
         float d = FAST ? fetch_finite(c, s, t) : fetch(c, s, t);
         if (n.z > d) {
             avg += d;
@@ -1500,7 +1518,8 @@ __global__ void __launch_bounds__(128) k_visibility(const gi_vis_params p,
                                                     const float4* __restrict__ pos,
                                                     const float4* __restrict__ nrm,
                                                     float* __restrict__ out, int W, int H,
-                                                    const SoftMaps sm) {
+                                                    const SoftMaps sm,
+                                                    const __grid_constant__ PoissonOffsets po) {
     int x = blockIdx.x * 32 + (threadIdx.x & 31);
     int y = blockIdx.y * 4 + (threadIdx.x >> 5);
     if (x >= W || y >= H) return;
@@ -1514,6 +1533,7 @@ __global__ void __launch_bounds__(128) k_visibility(const gi_vis_params p,
     c.sy = sy;
     c.I = p.shadow_intensity;
     c.sm = sm;
+    c.boff = TECH == GI_TECH_PCSS_POISSON ? po.b : nullptr;
     size_t i = (size_t)y * W + x;
     float4 pv = __ldcs(pos + i);
     float4 nv = __ldcs(nrm + i);
@@ -1534,12 +1554,13 @@ __global__ void __launch_bounds__(128) k_frame_visibility(
     const float* __restrict__ normals, const int* __restrict__ indices, const dev::Mat4 mvp,
     const unsigned* __restrict__ rec_of, const dev::BRec* __restrict__ recs, const uint4* __restrict__ rres,
     float* __restrict__ out, int W, int H, float4* __restrict__ pos_out, float4* __restrict__ nrm_out,
-    const SoftMaps sm) {
+    const SoftMaps sm, const __grid_constant__ PoissonOffsets po) {
     int x = blockIdx.x * 32 + (threadIdx.x & 31);
     int y = blockIdx.y * 4 + (threadIdx.x >> 5);
     if (x >= W || y >= H) return;
     Ctx c;
     c.sm = sm;
+    c.boff = TECH == GI_TECH_PCSS_POISSON ? po.b : nullptr;
     c.map = map;
     c.W = map_w;
     c.H = map_h;
@@ -1954,6 +1975,19 @@ gi_status launch_area_accumulate(gi_context* ctx, const gi_scene* scene, const f
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "area-light accumulate launch");
 }
 
+// c_poisson[i] * bsw for the PCSS_POISSON blocker taps (blocker_search_width:
+// lightSourceRadius / min(map width, 1024)), each product rounded once as
+// the kernel's multiplication would round it.
+static vis::PoissonOffsets poisson_offsets(const gi_vis_params* p, int map_w) {
+    vis::PoissonOffsets po{};
+    if (p->technique != GI_TECH_PCSS_POISSON) return po;
+    const float fw = (float)map_w;
+    const float bsw = fw <= 1024.0f ? p->light_radius / fw : p->light_radius / 1024.0f;
+    for (int i = 0; i < 64 && i < p->poisson_blocker_taps; ++i)
+        po.b[i] = make_float2(kPoissonDisk[i][0] * bsw, kPoissonDisk[i][1] * bsw);
+    return po;
+}
+
 // The maps the moment techniques read instead of (VSM..MSM) or beside
 // (SAVSM..MSSM) the light map, and the MSM constants.
 static gi_status prepare_maps(gi_context* ctx, const gi_vis_params* p, const float** d_depth, int* map_w,
@@ -1986,9 +2020,10 @@ gi_status launch_visibility(gi_context* ctx, const gi_vis_params* p, const float
     const float sx = (float)(1.0 / (double)map_w), sy = (float)(1.0 / (double)map_h);
     const float4* pos = reinterpret_cast<const float4*>(d_pos);
     const float4* nrm = reinterpret_cast<const float4*>(d_nrm);
+    const vis::PoissonOffsets po = poisson_offsets(p, map_w);
 #define GI_VIS_CASE(T)                                                                     \
     case T:                                                                                \
-        vis::k_visibility<T><<<grid, 128, 0, st>>>(*p, d_depth, map_w, map_h, sx, sy, pos, nrm, d_vis, W, H, sm); \
+        vis::k_visibility<T><<<grid, 128, 0, st>>>(*p, d_depth, map_w, map_h, sx, sy, pos, nrm, d_vis, W, H, sm, po); \
         break;
     switch (p->technique) {
         GI_VIS_CASE(GI_TECH_HARD)
@@ -2036,12 +2071,13 @@ gi_status launch_frame_visibility(gi_context* ctx, const gi_vis_params* p, const
     for (int k = 0; k < 16; ++k) m.m[k] = camera_mvp[k];
     float4* po = reinterpret_cast<float4*>(d_pos);
     float4* no = reinterpret_cast<float4*>(d_nrm);
+    const vis::PoissonOffsets boff = poisson_offsets(p, map_w);
 #define GI_FRAME_CASE(T)                                                                          \
     case T:                                                                                       \
         vis::k_frame_visibility<T><<<grid, 128, 0, st>>>(*p, d_depth, map_w, map_h, sx, sy,         \
                                                           ctx->d_vkeys, scene->d_points,          \
                                                           scene->d_normals, scene->d_indices, m,  \
-                                                          rec_of, recs, rres, d_vis, W, H, po, no, sm); \
+                                                          rec_of, recs, rres, d_vis, W, H, po, no, sm, boff); \
         break;
     switch (p->technique) {
         GI_FRAME_CASE(GI_TECH_HARD)
