@@ -214,7 +214,8 @@ _PROTOS = {
     "gi_area_light_samples": (C.c_int, [C.POINTER(View), C.c_float, C.c_int, _VP]),
     "gi_area_light_visibility": (C.c_int, [_VP, _VP, _VP, C.c_int, C.POINTER(MapParams), F16, C.c_float, C.c_int,
                                            C.c_int, _VP, _VP]),
-    "gi_area_light_adaptive": (C.c_int, [_VP, _VP, C.POINTER(View), C.c_float, C.c_int, C.POINTER(MapParams), F16,
+    "gi_area_light_adaptive": (C.c_int, [_VP, _VP, C.POINTER(View), C.c_float, C.c_int, C.c_int, C.POINTER(MapParams),
+                                         F16,
                                          C.c_float, C.c_int, C.c_int, _VP, _VP, _VP, C.POINTER(C.c_int), _VP]),
     "gi_batch_create": (C.c_int, [C.c_int, C.POINTER(_VP)]),
     "gi_batch_destroy": (None, [_VP]),

@@ -649,6 +649,7 @@ struct QtRun {
     int max_level;
     const gi_map_params* mp;
     int S, W, H;
+    int div;  // evaluation viewport divisor (4 in the lower-accuracy mode)
     cudaStream_t cs;
     float* pos;
     unsigned char* sums;
@@ -721,8 +722,9 @@ void qt_corner(int level, int node, int index, int* x, int* y) {
     *y = (index / 2) * cf + (node / pf) * cf;
 }
 
-// evaluateSubAreaLightSource (main.cpp:440-570, div = 1): the node's four
-// corner maps, the reprojection and the evaluation's occlusion query.
+// evaluateSubAreaLightSource (main.cpp:440-570; div = 1, or 4 in the
+// lower-accuracy mode, :551-555): the node's four corner maps, the
+// reprojection and the evaluation's occlusion query.
 gi_status qt_evaluate_sub(QtRun& r, int n, int node, bool* subdivide) {
     gi::QuadCorners q;
     for (int index = 0; index < 4; ++index) {
@@ -735,7 +737,7 @@ gi_status qt_evaluate_sub(QtRun& r, int n, int node, bool* subdivide) {
     }
     cudaError_t e = cudaMemsetAsync(r.passed, 0, sizeof(unsigned), r.cs);
     if (e != cudaSuccess) return gi::fail_cuda(e, "gi_area_light_adaptive: flag");
-    gi_status st = gi::launch_qt_evaluate(r.ctx, r.pos, r.W, r.H, q, r.S, r.sums, r.passed, r.cs);
+    gi_status st = gi::launch_qt_evaluate(r.ctx, r.pos, r.W, r.H, r.div, q, r.S, r.sums, r.passed, r.cs);
     if (st != GI_OK) return st;
     unsigned h = 0;
     e = cudaMemcpyAsync(&h, r.passed, sizeof h, cudaMemcpyDeviceToHost, r.cs);
@@ -793,7 +795,8 @@ gi_status qt_render(QtRun& r, int n, int node) {
 }  // namespace
 
 extern "C" gi_status gi_area_light_adaptive(gi_context* ctx, const gi_scene* s, const gi_view* light, float size,
-                                            int max_level, const gi_map_params* mp, const float camera_mvp[16],
+                                            int max_level, int lower_accuracy, const gi_map_params* mp,
+                                            const float camera_mvp[16],
                                             float shadow_intensity, int W, int H, float* d_vis, gi_view* samples_out,
                                             float* levels_out, int* num_samples, void* stream) {
     gi_status st = check_pass(ctx, s);
@@ -818,6 +821,9 @@ extern "C" gi_status gi_area_light_adaptive(gi_context* ctx, const gi_scene* s, 
     r.S = mp->width;
     r.W = W;
     r.H = H;
+    r.div = lower_accuracy ? 4 : 1;
+    if (W / r.div < 1 || H / r.div < 1)
+        return fail(GI_ERR_INVALID_ARG, "gi_area_light_adaptive: the lower-accuracy mode needs width, height >= 4");
     r.cs = static_cast<cudaStream_t>(stream);
     for (auto& row : r.hash)
         for (int& h : row) h = -1;
@@ -858,6 +864,16 @@ extern "C" gi_status gi_area_light_adaptive(gi_context* ctx, const gi_scene* s, 
     // last rendered map's
     gi::AreaWave wave;
     std::memcpy(wave.common, r.maps[n - 1].biased, 12 * sizeof(float));
+    if (lower_accuracy) {
+        // for (float w = -offset; w <= offset; w += stepSize), offset 1,
+        // stepSize 2 * offset / 3.0, in float (AccurateSoftShadow.frag:98-110)
+        const float offset = 1.0f, step = 2.0f * offset / 3.0f;
+        int k = 0;
+        for (float w = -offset; w <= offset && k < 8; w += step) wave.pcf_off[k++] = w;
+        wave.pcf_n = k;
+        wave.pcf_incr_w = 1.0f / (float)r.S;
+        wave.pcf_incr_h = 1.0f / (float)r.S;
+    }
     std::vector<float> tr((size_t)n * 4), wt(n);
     float count = 0.0f;
     for (int i = 0; i < n; ++i) {

@@ -55,6 +55,9 @@ struct AreaWave {
     float trans[16][4];
     float weight[16];
     float common[12];  // columns 0..2 of the last sample's biased light MVP
+    int pcf_n = 0;     // > 0: pcf_n x pcf_n taps per map at pcf_off[] texels
+    float pcf_off[8];
+    float pcf_incr_w, pcf_incr_h;
 };
 gi_status launch_area_accumulate(gi_context* ctx, const gi_scene* scene, const float camera_mvp[16], int W, int H,
                                  const float* maps, int map_s, int nw, const AreaWave& wave, float intensity,
@@ -62,14 +65,14 @@ gi_status launch_area_accumulate(gi_context* ctx, const gi_scene* scene, const f
 
 // Adaptive sampling: one quad-tree node's reprojection (per-pixel count of
 // its four corner lights that see the pixel, into d_sums) and evaluation
-// (sets *d_passed when a pixel with a count of 1-3 has eight equal
-// neighbours).
+// over a (W / div) x (H / div) grid of the counts (sets *d_passed when a
+// count of 1-3 has eight equal neighbours).
 struct QuadCorners {
     const float* maps[4];
     float mvp[4][16];  // biased light MVPs, column-major
 };
-gi_status launch_qt_evaluate(gi_context* ctx, const float* d_pos, int W, int H, const QuadCorners& q, int map_s,
-                             unsigned char* d_sums, unsigned* d_passed, cudaStream_t st);
+gi_status launch_qt_evaluate(gi_context* ctx, const float* d_pos, int W, int H, int div, const QuadCorners& q,
+                             int map_s, unsigned char* d_sums, unsigned* d_passed, cudaStream_t st);
 
 // Deferred Phong shading of the G-buffer with the visibility as shadow
 // term (d_color float4 per pixel or NULL for white); d_out float4.

@@ -1733,8 +1733,23 @@ __global__ void __launch_bounds__(128) k_area_accumulate(
         const float sx = cx + wave.trans[k][0], sy = cy + wave.trans[k][1];
         const float sz = cz + wave.trans[k][2], sw = cw + wave.trans[k][3];
         c.map = maps + (size_t)k * map_s * map_s;
-        const float d = fetch(c, sx / sw, sy / sw);
-        a += ((sz / sw <= d) ? 1.0f : I) * wave.weight[k];
+        if (wave.pcf_n == 0) {
+            const float d = fetch(c, sx / sw, sy / sw);
+            a += ((sz / sw <= d) ? 1.0f : I) * wave.weight[k];
+        } else {
+            // AccurateSoftShadow.frag's lower-accuracy branch: the float
+            // loops' offsets (w outer, h inner) in texels of 1 / map width
+            const float ux = sx / sw, uy = sy / sw, uz = sz / sw;
+            float illum = 0.0f;
+            for (int wi = 0; wi < wave.pcf_n; ++wi)
+                for (int hi = 0; hi < wave.pcf_n; ++hi) {
+                    const float d = fetch(c, ux + wave.pcf_off[wi] * wave.pcf_incr_w,
+                                          uy + wave.pcf_off[hi] * wave.pcf_incr_h);
+                    if (uz <= d) illum = illum + 1.0f;
+                    else illum += I;
+                }
+            a += (illum / (float)(wave.pcf_n * wave.pcf_n)) * wave.weight[k];
+        }
     }
     if (last) out[i] = a / count;
     else acc[i] = a;
@@ -1778,19 +1793,27 @@ __global__ void __launch_bounds__(128) k_qt_reproject(const float4* __restrict__
 // is 1, 2 or 3 and all eight neighbours have the same count (a neighbour
 // outside the image reads the border 0, a background one 0.63); any
 // passing pixel asks for the node to be subdivided.
-__global__ void __launch_bounds__(128) k_qt_evaluate(const unsigned char* __restrict__ sums, int W, int H,
-                                                     unsigned* __restrict__ passed) {
+// The evaluation pass runs over a Wq x Hq viewport (W / div, H / div;
+// div = 4 in the lower-accuracy mode): coarse pixel i reads the count image
+// at its centre, texel floor((2 i + 1) W / (2 Wq)), and its neighbours one
+// coarse pixel away (outside the viewport: the border).
+__device__ __forceinline__ unsigned qt_coarse(const unsigned char* sums, int W, int H, int Wq, int Hq, int i, int j) {
+    if (i < 0 || i >= Wq || j < 0 || j >= Hq) return 0u;
+    const int x = (int)(((long long)(2 * i + 1) * W) / (2LL * Wq));
+    const int y = (int)(((long long)(2 * j + 1) * H) / (2LL * Hq));
+    return sums[(size_t)y * W + x];
+}
+
+__global__ void __launch_bounds__(128) k_qt_evaluate(const unsigned char* __restrict__ sums, int W, int H, int Wq,
+                                                     int Hq, unsigned* __restrict__ passed) {
     const int x = blockIdx.x * 32 + (threadIdx.x & 31);
     const int y = blockIdx.y * 4 + (threadIdx.x >> 5);
-    if (x >= W || y >= H) return;
-    const unsigned s = sums[(size_t)y * W + x];
+    if (x >= Wq || y >= Hq) return;
+    const unsigned s = qt_coarse(sums, W, H, Wq, Hq, x, y);
     if (s == 255 || s == 0 || s == 4) return;
     for (int dy = -1; dy <= 1; ++dy)
-        for (int dx = -1; dx <= 1; ++dx) {
-            const int xx = x + dx, yy = y + dy;
-            const unsigned n = (xx >= 0 && xx < W && yy >= 0 && yy < H) ? sums[(size_t)yy * W + xx] : 0u;
-            if (n != s) return;
-        }
+        for (int dx = -1; dx <= 1; ++dx)
+            if (qt_coarse(sums, W, H, Wq, Hq, x + dx, y + dy) != s) return;
     atomicOr(passed, 1u);
 }
 
@@ -1950,11 +1973,12 @@ gi_status launch_phong(gi_context* ctx, const gi_vis_params* p, const float* d_p
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "phong launch");
 }
 
-gi_status launch_qt_evaluate(gi_context* ctx, const float* d_pos, int W, int H, const QuadCorners& q, int map_s,
-                            unsigned char* d_sums, unsigned* d_passed, cudaStream_t st) {
+gi_status launch_qt_evaluate(gi_context* ctx, const float* d_pos, int W, int H, int div, const QuadCorners& q,
+                            int map_s, unsigned char* d_sums, unsigned* d_passed, cudaStream_t st) {
     dim3 grid((W + 31) / 32, (H + 3) / 4);
     vis::k_qt_reproject<<<grid, 128, 0, st>>>(reinterpret_cast<const float4*>(d_pos), W, H, q, map_s, d_sums);
-    vis::k_qt_evaluate<<<grid, 128, 0, st>>>(d_sums, W, H, d_passed);
+    const int Wq = W / div, Hq = H / div;
+    vis::k_qt_evaluate<<<dim3((Wq + 31) / 32, (Hq + 3) / 4), 128, 0, st>>>(d_sums, W, H, Wq, Hq, d_passed);
     ctx->launches += 2;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "quad-tree evaluation launch");

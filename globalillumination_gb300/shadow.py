@@ -574,7 +574,8 @@ def area_light_visibility(ctx: Context, scene: Scene, samples, mp: MapParams, ca
 
 
 def area_light_adaptive(ctx: Context, scene: Scene, light: ViewSpec, size: float, mp: MapParams, camera_mvp,
-                        intensity: float, width: int, height: int, vis, max_level: int = 4, stream=None):
+                        intensity: float, width: int, height: int, vis, max_level: int = 4,
+                        lower_accuracy: bool = False, stream=None):
     """Adaptive (quad-tree) area-light ground truth (SoftShadowMapping adaptiveSampling).
 
     Returns (vis, samples, levels): the sample views in the order the final pass sums them and the
@@ -585,7 +586,7 @@ def area_light_adaptive(ctx: Context, scene: Scene, light: ViewSpec, size: float
     levels = np.zeros(289, np.float32)
     n = C.c_int(0)
     check(_lib().gi_area_light_adaptive(ctx.handle, scene.handle, C.byref(lv), float(size), int(max_level),
-                                        C.byref(c), _f16(camera_mvp), float(intensity), width, height, _ptr(vis),
+                                        1 if lower_accuracy else 0, C.byref(c), _f16(camera_mvp), float(intensity), width, height, _ptr(vis),
                                         out, levels.ctypes.data, C.byref(n), _stream_ptr(stream)),
           "gi_area_light_adaptive")
     views = [ViewSpec(eye=tuple(v.eye), at=tuple(v.at), width=v.width, height=v.height, fovy_deg=v.fovy_deg,

@@ -523,9 +523,15 @@ gi_status gi_area_light_visibility(gi_context* ctx, const gi_scene* scene,
  * level carried in the w of each biased translation as the reference's
  * uniforms carry it.  No pre-test; background 0.  d_vis is
  * float[width*height]; samples_out (at most 289 views), levels_out (289
- * floats) and num_samples may be NULL.  Square maps up to 4096^2. */
+ * floats) and num_samples may be NULL.  Square maps up to 4096^2.
+ * lower_accuracy != 0 is the reference's adaptiveSamplingLowerAccuracy
+ * (main.cpp:551-555, AccurateSoftShadow.frag:98-116): the evaluation reads
+ * the counts on a (width / 4) x (height / 4) grid (each coarse pixel at its
+ * centre texel) and the final pass averages 4 x 4 taps per map at offsets
+ * -1, -1/3, 1/3, 1 texels (the shader's float loop). */
 gi_status gi_area_light_adaptive(gi_context* ctx, const gi_scene* scene, const gi_view* light, float size,
-                                 int max_level, const gi_map_params* map, const float camera_mvp[16],
+                                 int max_level, int lower_accuracy, const gi_map_params* map,
+                                 const float camera_mvp[16],
                                  float shadow_intensity, int width, int height, float* d_vis,
                                  gi_view* samples_out, float* levels_out, int* num_samples, void* stream);
 

@@ -36,8 +36,8 @@ def load():
         lib.or_edt_inputs.argtypes = [vp, vp, vp, vp, vp, i, i, vp, vp]
         lib.or_edt_mean_filter.argtypes = [vp, vp, vp, i, i, i, vp]
         lib.or_soft_moment_map.argtypes = [vp, vp, i, i, vp]
-        lib.or_area_light_adaptive.argtypes = [vp, vp, i, vp, i, vp, vp, f, i, VIEW_MVP_FN, vp, i, i, f, f, f, vp,
-                                               f, i, i, vp, vp, vp, i]
+        lib.or_area_light_adaptive.argtypes = [vp, vp, i, vp, i, vp, vp, f, i, i, VIEW_MVP_FN, vp, i, i, f, f, f,
+                                               vp, f, i, i, vp, vp, vp, i]
         lib.or_area_light_adaptive.restype = i
         lib.or_hierarchical_shadow_map.argtypes = [vp, vp, i, i, i, vp]
         for fn in (lib.or_shadow_map, lib.or_gbuffer, lib.or_visibility, lib.or_shadow_volume_counts):
@@ -51,7 +51,7 @@ VIEW_MVP_FN = C.CFUNCTYPE(None, C.POINTER(C.c_float), C.POINTER(C.c_float), C.PO
 
 
 def area_light_adaptive(points, normals, indices, light_eye, light_at, size, max_level, view_mvp, S, bias_mode,
-                        cbias, factor, units, camera_mvp, intensity, width, height, threads=0):
+                        cbias, factor, units, camera_mvp, intensity, width, height, lower_accuracy=False, threads=0):
     """Adaptive (quad-tree) area-light ground truth.  view_mvp(eye, at) -> (mvp[16], biased[16]) gives a
     sample's light matrices.  Returns (vis, eyes [n, 6] (eye, at), levels [n])."""
     p, n = _f32(points), _f32(normals)
@@ -70,7 +70,8 @@ def area_light_adaptive(points, normals, indices, light_eye, light_at, size, max
     eyes = np.empty((289, 6), np.float32)
     levels = np.empty(289, np.float32)
     cnt = load().or_area_light_adaptive(p.ctypes.data, n.ctypes.data, p.size // 3, ix.ctypes.data, ix.size // 3,
-                                        le.ctypes.data, la.ctypes.data, float(size), int(max_level), fn, None, S,
+                                        le.ctypes.data, la.ctypes.data, float(size), int(max_level),
+                                        1 if lower_accuracy else 0, fn, None, S,
                                         bias_mode, cbias, factor, units, cm.ctypes.data, float(intensity), width,
                                         height, out.ctypes.data, eyes.ctypes.data, levels.ctypes.data, threads)
     return out, eyes[:cnt].copy(), levels[:cnt].copy()

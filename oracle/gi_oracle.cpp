@@ -2311,6 +2311,7 @@ struct OrQt {
     int max_level, S, bias_mode;
     float cbias, factor, units;
     int W, H, threads;
+    int div;  // evaluation viewport divisor (4: lower-accuracy mode)
     const float* pos;
     int hash[17][17];
     std::vector<std::vector<float>> maps;
@@ -2396,20 +2397,26 @@ bool or_qt_subdivide(OrQt& q, const int idx[4]) {
         }
         sum[p] = s;
     }
-    for (int y = 0; y < H; ++y)
-        for (int x = 0; x < W; ++x) {
-            const float s = sum[(size_t)y * W + x];
+    // the evaluation viewport: Wq x Hq = (W / div) x (H / div), coarse pixel
+    // i reading the count texel at its centre, floor((2 i + 1) W / (2 Wq))
+    const int Wq = W / q.div, Hq = H / q.div;
+    auto coarse = [&](int i, int j) {
+        if (i < 0 || i >= Wq || j < 0 || j >= Hq) return 0.0f;  // border
+        const int x = (int)(((long long)(2 * i + 1) * W) / (2LL * Wq));
+        const int y = (int)(((long long)(2 * j + 1) * H) / (2LL * Hq));
+        return sum[(size_t)y * W + x];
+    };
+    for (int y = 0; y < Hq; ++y)
+        for (int x = 0; x < Wq; ++x) {
+            const float s = coarse(x, y);
             if (s == 0.63f || s == 0.0f || s == 4.0f || s == 5.0f) continue;
             bool pass = true;
             for (int dy = -1; dy <= 1 && pass; ++dy)
-                for (int dx = -1; dx <= 1; ++dx) {
-                    const int xx = x + dx, yy = y + dy;
-                    const float n = (xx >= 0 && xx < W && yy >= 0 && yy < H) ? sum[(size_t)yy * W + xx] : 0.0f;
-                    if (s != n) {
+                for (int dx = -1; dx <= 1; ++dx)
+                    if (s != coarse(x + dx, y + dy)) {
                         pass = false;
                         break;
                     }
-                }
             if (pass) return true;
         }
     return false;
@@ -2456,7 +2463,8 @@ void or_qt_render(OrQt& q, std::vector<OrQtNode>& nodes, int n, int node) {
 
 extern "C" int or_area_light_adaptive(const float* points, const float* normals, int nv, const int* indices, int nt,
                                       const float light_eye[3], const float light_at[3], float size, int max_level,
-                                      or_view_mvp_fn view_mvp, void* user, int S, int bias_mode, float cbias,
+                                      int lower_accuracy, or_view_mvp_fn view_mvp, void* user, int S, int bias_mode,
+                                      float cbias,
                                       float factor, float units, const float camera_mvp[16], float I, int W, int H,
                                       float* out, float* eyes_out, float* levels_out, int threads) {
     std::vector<float> pos((size_t)W * H * 4), nrm((size_t)W * H * 4);
@@ -2479,6 +2487,7 @@ extern "C" int or_area_light_adaptive(const float* points, const float* normals,
     q.W = W;
     q.H = H;
     q.threads = threads;
+    q.div = lower_accuracy ? 4 : 1;
     q.pos = pos.data();
     for (auto& row : q.hash)
         for (int& h : row) h = -1;
@@ -2496,6 +2505,13 @@ extern "C" int or_area_light_adaptive(const float* points, const float* normals,
     const float* m = q.biased[n - 1].data();
     std::vector<float> acc((size_t)W * H, 0.0f);
     float count = 0.0f;
+    // the lower-accuracy branch's float loops (AccurateSoftShadow.frag:98-110)
+    std::vector<float> offs;
+    if (lower_accuracy) {
+        const float offset = 1.0f, step = 2.0f * offset / 3.0f;
+        for (float w = -offset; w <= offset; w += step) offs.push_back(w);
+    }
+    const float incr = 1.0f / (float)S;
     for (int i = 0; i < n; ++i) {
         const float* b = q.biased[i].data();
         const float w_enc = b[15] + q.level[i] * 10000.0f;
@@ -2521,8 +2537,19 @@ extern "C" int or_area_light_adaptive(const float* points, const float* normals,
             const float cz = m[2] * v[0] + m[6] * v[1] + m[10] * v[2];
             const float cw = m[3] * v[0] + m[7] * v[1] + m[11] * v[2];
             const float sx = cx + b[12], sy = cy + b[13], sz = cz + b[14], sw = cw + wv;
-            const float d = fetch(c, sx / sw, sy / sw);
-            acc[p] += ((sz / sw <= d) ? 1.0f : I) * wt;
+            if (!lower_accuracy) {
+                const float d = fetch(c, sx / sw, sy / sw);
+                acc[p] += ((sz / sw <= d) ? 1.0f : I) * wt;
+            } else {
+                const float ux = sx / sw, uy = sy / sw, uz = sz / sw;
+                float illum = 0.0f;
+                for (float ow : offs)
+                    for (float oh : offs) {
+                        if (uz <= fetch(c, ux + ow * incr, uy + oh * incr)) illum = illum + 1.0f;
+                        else illum += I;
+                    }
+                acc[p] += (illum / (float)(offs.size() * offs.size())) * wt;
+            }
         }
         count += wt;
         if (eyes_out)

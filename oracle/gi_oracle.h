@@ -85,7 +85,8 @@ void or_area_light_visibility(const float* points, const float* normals, int nv,
 typedef void (*or_view_mvp_fn)(const float* eye, const float* at, float* mvp, float* biased, void* user);
 int or_area_light_adaptive(const float* points, const float* normals, int nv, const int* indices, int nt,
                            const float light_eye[3], const float light_at[3], float size, int max_level,
-                           or_view_mvp_fn view_mvp, void* user, int S, int bias_mode, float cbias, float factor,
+                           int lower_accuracy, or_view_mvp_fn view_mvp, void* user, int S, int bias_mode,
+                           float cbias, float factor,
                            float units, const float camera_mvp[16], float I, int W, int H, float* out,
                            float* eyes_out, float* levels_out, int threads);
 

@@ -26,13 +26,13 @@ def view_mvp_for(light):
     return fn
 
 
-def run(w, size, max_level, W, H):
+def run(w, size, max_level, W, H, lower_accuracy=False):
     p, n, i = w.scene.arrays()
     mp = w.map_params
     cam = gi.frame_setup(w.light, w.camera).camera_mvp
     return oracle.area_light_adaptive(p, n, i, w.light.eye, w.light.at, size, max_level, view_mvp_for(w.light),
                                       mp.width, mp.bias_mode, mp.constant_bias, mp.offset_factor, mp.offset_units,
-                                      cam, 0.25, W, H)
+                                      cam, 0.25, W, H, lower_accuracy=lower_accuracy)
 
 
 def grid_positions(light, size, eyes):
@@ -97,3 +97,15 @@ def test_close_to_the_uniform_estimate(small_scene):
                                       0.25, 96, 54)
     geo = mc > 0
     assert np.abs(vis[geo] - mc[geo]).mean() < 0.05
+
+
+def test_lower_accuracy_mode(small_scene):
+    # adaptiveSamplingLowerAccuracy: the evaluation on a quarter-resolution
+    # grid needs wider uniform regions, so it refines no more than the full
+    # evaluation; the final pass's 4 x 4 taps give intermediate values
+    w, size = small_scene, 4.0
+    _, _, full = run(w, size, 4, 96, 54)
+    vis, eyes, levels = run(w, size, 4, 96, 54, lower_accuracy=True)
+    assert 4 <= len(levels) <= len(full)
+    fin = vis[vis > 0]
+    assert ((fin > 0.25) & (fin < 1.0)).sum() > 20

@@ -12,10 +12,12 @@ from test_area_adaptive_oracle import run
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("W,H,S,size,max_level,spheres",
-                         [(96, 54, 256, 4.0, 4, 8), (160, 96, 512, 8.0, 4, 16), (192, 108, 256, 2.0, 4, 8),
-                          (128, 72, 512, 6.0, 2, 16), (96, 54, 256, 4.0, 0, 8)])
-def test_adaptive_matches_oracle(cuda_ctx, W, H, S, size, max_level, spheres):
+@pytest.mark.parametrize("W,H,S,size,max_level,spheres,lower",
+                         [(96, 54, 256, 4.0, 4, 8, False), (160, 96, 512, 8.0, 4, 16, False),
+                          (192, 108, 256, 2.0, 4, 8, False), (128, 72, 512, 6.0, 2, 16, False),
+                          (96, 54, 256, 4.0, 0, 8, False), (192, 108, 256, 4.0, 4, 8, True),
+                          (150, 90, 512, 8.0, 4, 16, True)])
+def test_adaptive_matches_oracle(cuda_ctx, W, H, S, size, max_level, spheres, lower):
     import torch
 
     w = scenes.pcss_1080p(width=W, height=H, map_size=S, spheres=spheres)
@@ -23,9 +25,9 @@ def test_adaptive_matches_oracle(cuda_ctx, W, H, S, size, max_level, spheres):
     cam = gi.frame_setup(w.light, w.camera).camera_mvp
     vis = torch.full((W * H,), -1.0, device="cuda")
     _, views, levels = gi.area_light_adaptive(cuda_ctx, w.scene, w.light, size, w.map_params, cam, 0.25, W, H, vis,
-                                              max_level=max_level)
+                                              max_level=max_level, lower_accuracy=lower)
     torch.cuda.synchronize()
-    ref, eyes, ref_levels = run(w, size, max_level, W, H)
+    ref, eyes, ref_levels = run(w, size, max_level, W, H, lower_accuracy=lower)
     got_eyes = np.array([list(v.eye) + list(v.at) for v in views], np.float32)
     assert got_eyes.shape == eyes.shape
     np.testing.assert_array_equal(got_eyes.view(np.uint32), eyes.view(np.uint32))
