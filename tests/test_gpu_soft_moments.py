@@ -42,9 +42,9 @@ def _compare_maps(tech, got, ref):
 @pytest.mark.parametrize("S,T", [(64, 64), (100, 37), (300, 200), (40, 2048), (1024, 1024), (2048, 2048),
                                  (4096, 512)])
 def test_moment_map_matches_oracle(cuda_ctx, tech, sat, S, T):
-    # the SAT build runs iterations 0-4 in shared-memory tiles, the next
-    # five over residue classes mod 32 where their sub-grids are >= 8 wide,
-    # and the rest one launch each: these shapes take every branch
+    # square, non-square and non-power-of-two maps (a width that is not a
+    # power of two leaves the table short of full prefix sums, as the
+    # reference's logf-based iteration count does)
     d = blocker_scene(max(S, T), 31)[:T, :S].copy()
     p = params(tech, sat)
     got = _gpu_map(cuda_ctx, p, d, S, T)
