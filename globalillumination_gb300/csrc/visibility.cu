@@ -230,14 +230,31 @@ __device__ __forceinline__ float blocker_search_width(const gi_vis_params& p, co
     return R / 1024.0f;
 }
 
+// The tap offsets of the reference's grid loops, for (int k = (int)(-fw);
+// (float)k <= fw; k++) ... ((float)k * width) / fw: each depends on k alone,
+// so they are computed once (at most 63: grid sizes are capped at 63) and
+// both axes read them; the taps get the same numbers as when every tap
+// divided for itself.
+struct GridTaps {
+    float o[64];
+    int n;
+};
+
+__device__ __forceinline__ void grid_taps(float width, float fw, GridTaps& g) {
+    g.n = 0;
+    for (int k = (int)(-fw); (float)k <= fw && g.n < 64; k++) g.o[g.n++] = ((float)k * width) / fw;
+}
+
 __device__ float avg_blocker_grid(const gi_vis_params& p, const Ctx& c, V4 n) {
     float avg = 0.0f;
     int nb = 0;
     float bsw = blocker_search_width(p, c);
     float fw = ((float)p.blocker_search_size - 1.0f) * 0.5f;
-    for (int h = (int)(-fw); (float)h <= fw; h++)
-        for (int w = (int)(-fw); (float)w <= fw; w++) {
-            float d = fetch(c, n.x + ((float)w * bsw) / fw, n.y + ((float)h * bsw) / fw);
+    GridTaps g;
+    grid_taps(bsw, fw, g);
+    for (int hi = 0; hi < g.n; hi++)
+        for (int wi = 0; wi < g.n; wi++) {
+            float d = fetch(c, n.x + g.o[wi], n.y + g.o[hi]);
             if (n.z > d) {
                 avg += d;
                 nb++;
@@ -297,9 +314,11 @@ __device__ float pcss_filter_grid(const gi_vis_params& p, const Ctx& c, float pw
     float step = 2.0f * pw / (float)K;
     float fw = ((float)K - 1.0f) * 0.5f;
     if (step <= 0.0f || step >= 1.0f) return 1.0f;
-    for (int h = (int)(-fw); (float)h <= fw; h++)
-        for (int w = (int)(-fw); (float)w <= fw; w++) {
-            float d = fetch(c, n.x + ((float)w * pw) / fw, n.y + ((float)h * pw) / fw);
+    GridTaps g;
+    grid_taps(pw, fw, g);
+    for (int hi = 0; hi < g.n; hi++)
+        for (int wi = 0; wi < g.n; wi++) {
+            float d = fetch(c, n.x + g.o[wi], n.y + g.o[hi]);
             if (n.z <= d) illum = illum + 1.0f;
             else illum += c.I;
         }
@@ -964,9 +983,11 @@ __device__ float rb_filter(const gi_vis_params& p, const Ctx& c, float pw, V4 n)
     float illum = 0.0f;
     const int K = p.kernel_size;
     float fw = ((float)K - 1.0f) * 0.5f;
-    for (int h = (int)(-fw); (float)h <= fw; h++)
-        for (int w = (int)(-fw); (float)w <= fw; w++) {
-            V4 lc = {n.x + ((float)w * pw) / fw, n.y + ((float)h * pw) / fw, n.z, n.w};
+    GridTaps g;
+    grid_taps(pw, fw, g);
+    for (int hi = 0; hi < g.n; hi++)
+        for (int wi = 0; wi < g.n; wi++) {
+            V4 lc = {n.x + g.o[wi], n.y + g.o[hi], n.z, n.w};
             V2 sub = {gfract(lc.x * c.fW), gfract(lc.y * c.fH)};
             float d = fetch(c, lc.x, lc.y);
             V4 disc = nc_compute_disc(c, lc, d);
@@ -1262,9 +1283,11 @@ __device__ __forceinline__ V4 sat_box(const Ctx& c, V4 n, float width, float ste
 __device__ V4 loop_box(const Ctx& c, V4 n, float width, int count) {
     const float fw = ((float)count - 1.0f) * 0.5f;
     V4 acc{0.0f, 0.0f, 0.0f, 0.0f};
-    for (int h = (int)(-fw); (float)h <= fw; h++)
-        for (int w = (int)(-fw); (float)w <= fw; w++) {
-            const V4 t = mom_at(c, n.x + ((float)w * width) / fw, n.y + ((float)h * width) / fw);
+    GridTaps g;
+    grid_taps(width, fw, g);
+    for (int hi = 0; hi < g.n; hi++)
+        for (int wi = 0; wi < g.n; wi++) {
+            const V4 t = mom_at(c, n.x + g.o[wi], n.y + g.o[hi]);
             acc = V4{acc.x + t.x, acc.y + t.y, acc.z + t.z, acc.w + t.w};
         }
     const float den = (float)(count * count);
