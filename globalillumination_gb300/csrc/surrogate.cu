@@ -718,11 +718,12 @@ __global__ void k_wgrad_reduce(const float* __restrict__ scratch, int splits, in
     }
 }
 
-// db[co] += sum_p dy[p][co]
-__global__ void k_bias_grad(const uint16_t* __restrict__ dy, long long P, int cout, float* __restrict__ db) {
+// db[co] += sum_p dy[p][co] in a fixed order, so that training runs are
+// reproducible: thread row r of block b sums pixels b * rows + r, stepping by
+// gridDim.x * rows; the block's rows are added in row order into
+// partial[b][co], and k_bias_reduce adds the blocks in block order.
+__global__ void k_bias_grad(const uint16_t* __restrict__ dy, long long P, int cout, float* __restrict__ partial) {
     __shared__ float acc[256];
-    for (int c = threadIdx.x; c < cout; c += blockDim.x) acc[c] = 0.0f;
-    __syncthreads();
     const int c = threadIdx.x % cout;
     const int rows = blockDim.x / cout;
     const int r0 = threadIdx.x / cout;
@@ -730,9 +731,21 @@ __global__ void k_bias_grad(const uint16_t* __restrict__ dy, long long P, int co
     if (r0 < rows)
         for (long long p = blockIdx.x * (long long)rows + r0; p < P; p += (long long)gridDim.x * rows)
             s += bf16_to_f(dy[p * cout + c]);
-    if (r0 < rows) atomicAdd(&acc[c], s);
+    if (r0 < rows) acc[r0 * cout + c] = s;
     __syncthreads();
-    for (int k = threadIdx.x; k < cout; k += blockDim.x) atomicAdd(db + k, acc[k]);
+    if (threadIdx.x < cout) {
+        float t = 0.0f;
+        for (int r = 0; r < rows; ++r) t += acc[r * cout + threadIdx.x];
+        partial[(long long)blockIdx.x * cout + threadIdx.x] = t;
+    }
+}
+
+__global__ void k_bias_reduce(const float* __restrict__ partial, int blocks, int cout, float* __restrict__ db) {
+    const int co = blockIdx.x * blockDim.x + threadIdx.x;
+    if (co >= cout) return;
+    float t = 0.0f;
+    for (int b = 0; b < blocks; ++b) t += partial[(long long)b * cout + co];
+    db[co] += t;
 }
 
 __global__ void k_pack_weights(const float* __restrict__ w, int cout, int cin_real, int cin, int ks, int flip,
@@ -1116,7 +1129,14 @@ extern "C" gi_status gi_conv2d_wgrad_bf16(const gi_bf16* x, const gi_bf16* dy, i
     const long long red = (long long)8 * a.nkb * cout;
     tc::k_wgrad_reduce<<<tc::grid1d(red, 256), 256, 0, st>>>(scratch, pl.splits, pl.m_tiles, cout, a.nkb,
                                                             tc::nkb_pad_of(cin, ksize), dw);
-    if (db) tc::k_bias_grad<<<std::min<long long>(1216, (P + 63) / 64), 256, 0, st>>>(dy, P, cout, db);
+    if (db) {
+        // the partial sums reuse the scratch k_wgrad_reduce has finished
+        // reading (at least 128 x cout floats)
+        const long long cap = (long long)pl.splits * pl.m_tiles * 128;
+        const int blocks = (int)std::max<long long>(1, std::min<long long>(std::min<long long>(1216, (P + 63) / 64), cap));
+        tc::k_bias_grad<<<blocks, 256, 0, st>>>(dy, P, cout, scratch);
+        tc::k_bias_reduce<<<(cout + 127) / 128, 128, 0, st>>>(scratch, blocks, cout, db);
+    }
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_conv2d_wgrad_bf16 launch");
 }
