@@ -25,6 +25,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include <algorithm>
 #include <cstdint>
 
@@ -992,16 +994,26 @@ gi_status slab_map(CUtensorMap* m, const uint16_t* x, int n, int h, int w, int c
     return r == CUDA_SUCCESS ? GI_OK : fail(GI_ERR_CUDA, "cuTensorMapEncodeTiled rejected the activation map");
 }
 
+// Opt a kernel into more than 48 KB of dynamic shared memory, once per
+// device (the attribute is per device, and calls may come from several
+// threads).
+template <typename F>
+void smem_opt_in(F* fn, int bytes, std::atomic<unsigned long long>& done) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (done.load(std::memory_order_acquire) & bit) return;
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    done.fetch_or(bit, std::memory_order_acq_rel);
+}
+
 gi_status launch_slab(const tc::ConvArgs& a, cudaStream_t cs) {
     const tc::SlabGeom G = tc::persist_geom(a.cout, a.cin / 16);
     CUtensorMap m;
     gi_status st = slab_map(&m, a.x, a.n, a.h, a.w, a.cin, G.R + 2);
     if (st != GI_OK) return st;
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(tc::k_conv3_slab, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-        attr = true;
-    }
+    static std::atomic<unsigned long long> attr{0};
+    smem_opt_in(tc::k_conv3_slab, 220 * 1024, attr);
     const int tx = (a.w + 127) / 128, ty = (a.h + G.R - 1) / G.R;
     const long long tiles = (long long)tx * ty * a.n;
     if (tiles > 0x7FFFFFFFLL) return fail(GI_ERR_INVALID_ARG, "gi_conv2d_bf16: too many tiles");
@@ -1054,11 +1066,8 @@ extern "C" gi_status gi_conv2d_bf16(const gi_bf16* x, int n, int h, int w, int c
     cudaStream_t cs = static_cast<cudaStream_t>(stream);
     if (tc::slab_layout(cin, ksize)) return launch_slab(a, cs);
     const int smem = tc::kNS * (tc::kStageA + (cout / 8) * tc::kSBO);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(tc::k_conv_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * (8192 + 16384));
-        attr_set = true;
-    }
+    static std::atomic<unsigned long long> attr{0};
+    smem_opt_in(tc::k_conv_fwd, 4 * (8192 + 16384), attr);
     const long long tiles = (a.P + 127) / 128;
     if (tiles > 0x7FFFFFFFLL) return fail(GI_ERR_INVALID_ARG, "gi_conv2d_bf16: too many pixels");
     tc::k_conv_fwd<<<(unsigned)tiles, tc::kThreads, smem, cs>>>(a);
@@ -1120,11 +1129,8 @@ extern "C" gi_status gi_conv2d_wgrad_bf16(const gi_bf16* x, const gi_bf16* dy, i
     a.scratch = scratch;
     a.err = err;
     const int smem = tc::kNS * (tc::kStageA + (cout / 8) * tc::kSBO);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(tc::k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * (8192 + 16384));
-        attr_set = true;
-    }
+    static std::atomic<unsigned long long> attr{0};
+    smem_opt_in(tc::k_conv_wgrad, 4 * (8192 + 16384), attr);
     tc::k_conv_wgrad<<<dim3(pl.m_tiles, pl.splits), tc::kThreads, smem, st>>>(a);
     const long long red = (long long)8 * a.nkb * cout;
     tc::k_wgrad_reduce<<<tc::grid1d(red, 256), 256, 0, st>>>(scratch, pl.splits, pl.m_tiles, cout, a.nkb,
