@@ -39,6 +39,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <mutex>
 #include <string>
@@ -1635,16 +1636,18 @@ __global__ void __launch_bounds__(128) k_tier_spill(TierArgs a) {
 // ---------------------------------------------------------------------------
 namespace {
 
+// SM count per device, queried once; callers on several threads may race to
+// fill a slot, which is harmless since they all store the same value.
 int sm_count(int device) {
-    static int cached[64] = {0};
+    static std::atomic<int> cached[64];
     if (device < 0 || device >= 64) return 152;
-    if (!cached[device]) {
-        int v = 0;
+    int v = cached[device].load(std::memory_order_relaxed);
+    if (!v) {
         if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || v <= 0)
             v = 152;
-        cached[device] = v;
+        cached[device].store(v, std::memory_order_relaxed);
     }
-    return cached[device];
+    return v;
 }
 
 unsigned grid_for(size_t n, unsigned block) {
