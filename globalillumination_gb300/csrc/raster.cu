@@ -1316,23 +1316,25 @@ __global__ void __launch_bounds__(256) k_base(TierArgs a) {
     for (int h = 0; h < nh; ++h) {
         const BRec& r = hr[h];
         if (x < (int)r.x0 || x > (int)r.x1) continue;
+        // Edge values carry the top-left bias (-1 where the edge does not
+        // own its boundary): inside exactly when no high word is negative.
         int64_t A[3], E[3];
-        bool tl[3];
+        int bias[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             const int ia = (i + 1) % 3, ib = (i + 2) % 3;
             A[i] = (int64_t)r.X[ib] - r.X[ia];
             const int64_t B = (int64_t)r.Y[ib] - r.Y[ia];
-            tl[i] = (B < 0) || (B == 0 && A[i] < 0);
-            E[i] = A[i] * ((int64_t)yb * kSub + kSub / 2 - r.Y[ia]) - B * (px - r.X[ia]);
+            bias[i] = ((B < 0) || (B == 0 && A[i] < 0)) ? 0 : 1;
+            E[i] = A[i] * ((int64_t)yb * kSub + kSub / 2 - r.Y[ia]) - B * (px - r.X[ia]) - bias[i];
         }
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const int y = yb + k;
-            const bool in = y >= (int)r.y0 && y <= (int)r.y1 && (E[0] > 0 || (E[0] == 0 && tl[0])) &&
-                            (E[1] > 0 || (E[1] == 0 && tl[1])) && (E[2] > 0 || (E[2] == 0 && tl[2]));
+            const int hi = (int)(E[0] >> 32) | (int)(E[1] >> 32) | (int)(E[2] >> 32);
+            const bool in = y >= (int)r.y0 && y <= (int)r.y1 && hi >= 0;
             if (in) {
-                const float l1 = i2f(E[1]) * r.inv_area, l2 = i2f(E[2]) * r.inv_area;
+                const float l1 = i2f(E[1] + bias[1]) * r.inv_area, l2 = i2f(E[2] + bias[2]) * r.inv_area;
                 float z = r.z0 + (l1 * r.dz1 + l2 * r.dz2);
                 if (MODE == MODE_DEPTH) {
                     z = clamp01(z + r.zoff);
@@ -1403,19 +1405,21 @@ __device__ __forceinline__ void tiny_record(const TierArgs& a, unsigned i) {
         if (fits32) {
             // the steps are only added when the box has a next row / column,
             // and then they are bounded by `bound` too
+            // The edges carry the top-left bias (-1 on an edge that does not
+            // own its boundary), so a pixel is inside exactly when no biased
+            // value is negative: one OR of the three and a sign test.
             int er[3], sa[3], sb[3];
+            const int b1 = tl[1] ? 0 : 1, b2 = tl[2] ? 0 : 1;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                er[k] = (int)E0[k];
+                er[k] = (int)E0[k] - (tl[k] ? 0 : 1);
                 sa[k] = h > 1 ? (int)(A[k] * kSub) : 0;
                 sb[k] = w > 1 ? (int)(B[k] * kSub) : 0;
             }
             for (int y = r.y0;; ++y) {
                 int e0 = er[0], e1 = er[1], e2 = er[2];
                 for (int x = r.x0;; ++x) {
-                    const bool in = (e0 > 0 || (e0 == 0 && tl[0])) && (e1 > 0 || (e1 == 0 && tl[1])) &&
-                                    (e2 > 0 || (e2 == 0 && tl[2]));
-                    if (in) rec_emit<MODE>(a, r, x, y, (float)e1, (float)e2);
+                    if ((e0 | e1 | e2) >= 0) rec_emit<MODE>(a, r, x, y, (float)(e1 + b1), (float)(e2 + b2));
                     if (x == (int)r.x1) break;  // no step past the box: it could leave 32 bits
                     e0 -= sb[0];
                     e1 -= sb[1];
@@ -1472,14 +1476,14 @@ __device__ __forceinline__ void coop_record(const TierArgs& a, unsigned i, int l
         bool in;
         float fe1, fe2;
         if (fits32) {
+            // biased edges as in tiny_record: inside when none is negative
             int e[3];
 #pragma unroll
             for (int k = 0; k < 3; ++k)
-                e[k] = (int)E0[k] + (int)A[k] * (dy << kSubBits) - (int)B[k] * (dx << kSubBits);
-            in = (e[0] > 0 || (e[0] == 0 && tl[0])) && (e[1] > 0 || (e[1] == 0 && tl[1])) &&
-                 (e[2] > 0 || (e[2] == 0 && tl[2]));
-            fe1 = (float)e[1];
-            fe2 = (float)e[2];
+                e[k] = (int)E0[k] + (int)A[k] * (dy << kSubBits) - (int)B[k] * (dx << kSubBits) - (tl[k] ? 0 : 1);
+            in = (e[0] | e[1] | e[2]) >= 0;
+            fe1 = (float)(e[1] + (tl[1] ? 0 : 1));
+            fe2 = (float)(e[2] + (tl[2] ? 0 : 1));
         } else {
             int64_t E[3];
 #pragma unroll
