@@ -848,16 +848,16 @@ __global__ void __launch_bounds__(256) k_bin_raster(BinArgs a) {
             const int64_t B = (int64_t)r.Y[ib] - r.Y[ia];
             tl[i] = (B < 0) || (B == 0 && A[i] < 0);
             const int64_t py = (int64_t)(oy + row0) * kSub + kSub / 2;
-            E[i] = A[i] * (py - r.Y[ia]) - B * (px - r.X[ia]);
+            E[i] = A[i] * (py - r.Y[ia]) - B * (px - r.X[ia]) - tl_bias(tl[i]);
         }
         const bool colin = x >= (int)r.x0 && x <= (int)r.x1;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const int y = oy + row0 + 8 * k;
-            const bool in = colin && y >= (int)r.y0 && y <= (int)r.y1 &&
-                            (E[0] > 0 || (E[0] == 0 && tl[0])) && (E[1] > 0 || (E[1] == 0 && tl[1])) &&
-                            (E[2] > 0 || (E[2] == 0 && tl[2]));
-            if (in) bin_frag<MODE>(a, tile, dtile, (row0 + 8 * k) * kBin + col, r, i2f(E[1]), i2f(E[2]));
+            const bool in = colin && y >= (int)r.y0 && y <= (int)r.y1 && inside_biased(E);
+            if (in)
+                bin_frag<MODE>(a, tile, dtile, (row0 + 8 * k) * kBin + col, r, i2f(E[1] + tl_bias(tl[1])),
+                               i2f(E[2] + tl_bias(tl[2])));
 #pragma unroll
             for (int i = 0; i < 3; ++i) E[i] += A[i] * (8 * kSub);
         }
@@ -897,20 +897,18 @@ __global__ void __launch_bounds__(256) k_bin_raster(BinArgs a) {
                 int e[3];
 #pragma unroll
                 for (int i = 0; i < 3; ++i)
-                    e[i] = (int)E0[i] + (int)A[i] * (dy << kSubBits) - (int)B[i] * (dx << kSubBits);
-                in = (e[0] > 0 || (e[0] == 0 && tl[0])) && (e[1] > 0 || (e[1] == 0 && tl[1])) &&
-                     (e[2] > 0 || (e[2] == 0 && tl[2]));
-                fe1 = (float)e[1];
-                fe2 = (float)e[2];
+                    e[i] = (int)E0[i] + (int)A[i] * (dy << kSubBits) - (int)B[i] * (dx << kSubBits) - tl_bias(tl[i]);
+                in = (e[0] | e[1] | e[2]) >= 0;
+                fe1 = (float)(e[1] + tl_bias(tl[1]));
+                fe2 = (float)(e[2] + tl_bias(tl[2]));
             } else {
                 int64_t E[3];
 #pragma unroll
                 for (int i = 0; i < 3; ++i)
-                    E[i] = E0[i] + A[i] * (int64_t)(dy << kSubBits) - B[i] * (int64_t)(dx << kSubBits);
-                in = (E[0] > 0 || (E[0] == 0 && tl[0])) && (E[1] > 0 || (E[1] == 0 && tl[1])) &&
-                     (E[2] > 0 || (E[2] == 0 && tl[2]));
-                fe1 = i2f(E[1]);
-                fe2 = i2f(E[2]);
+                    E[i] = E0[i] + A[i] * (int64_t)(dy << kSubBits) - B[i] * (int64_t)(dx << kSubBits) - tl_bias(tl[i]);
+                in = inside_biased(E);
+                fe1 = i2f(E[1] + tl_bias(tl[1]));
+                fe2 = i2f(E[2] + tl_bias(tl[2]));
             }
             if (in) bin_frag<MODE>(a, tile, dtile, (y0 + dy - oy) * kBin + (x0 + dx - ox), r, fe1, fe2);
         }
@@ -1008,7 +1006,7 @@ __global__ void __launch_bounds__(256) k_sliver(BinArgs a) {
             const int64_t dK = A[k] * (int64_t)kSub;
             K0[k] = A[k] * (py0 - YA[k]) + B[k] * XA[k];
             if (B[k] > 0) {
-                num_b[k] = Kb - B[k] * (kSub / 2) - (tl[k] ? 0 : 1);
+                num_b[k] = Kb - B[k] * (kSub / 2) - tl_bias(tl[k]);
                 den[k] = B[k] * kSub;
                 step1[k] = dK;
             } else if (B[k] < 0) {
@@ -1074,11 +1072,9 @@ __global__ void __launch_bounds__(256) k_sliver(BinArgs a) {
                 const int64_t px = (int64_t)x * kSub + kSub / 2;
                 int64_t E[3];
 #pragma unroll
-                for (int k = 0; k < 3; ++k) E[k] = A[k] * (py - YA[k]) - B[k] * (px - XA[k]);
-                const bool in = (E[0] > 0 || (E[0] == 0 && tl[0])) && (E[1] > 0 || (E[1] == 0 && tl[1])) &&
-                                (E[2] > 0 || (E[2] == 0 && tl[2]));
-                if (!in) continue;
-                const float l1 = i2f(E[1]) * r.inv_area, l2 = i2f(E[2]) * r.inv_area;
+                for (int k = 0; k < 3; ++k) E[k] = A[k] * (py - YA[k]) - B[k] * (px - XA[k]) - tl_bias(tl[k]);
+                if (!inside_biased(E)) continue;
+                const float l1 = i2f(E[1] + tl_bias(tl[1])) * r.inv_area, l2 = i2f(E[2] + tl_bias(tl[2])) * r.inv_area;
                 const float z = clamp01(r.z0 + (l1 * r.dz1 + l2 * r.dz2));
                 const size_t idx = (size_t)y * a.r.W + x;
                 const float d = __uint_as_float(__ldg(a.r.depth + idx));
@@ -1325,14 +1321,13 @@ __global__ void __launch_bounds__(256) k_base(TierArgs a) {
             const int ia = (i + 1) % 3, ib = (i + 2) % 3;
             A[i] = (int64_t)r.X[ib] - r.X[ia];
             const int64_t B = (int64_t)r.Y[ib] - r.Y[ia];
-            bias[i] = ((B < 0) || (B == 0 && A[i] < 0)) ? 0 : 1;
+            bias[i] = tl_bias((B < 0) || (B == 0 && A[i] < 0));
             E[i] = A[i] * ((int64_t)yb * kSub + kSub / 2 - r.Y[ia]) - B * (px - r.X[ia]) - bias[i];
         }
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const int y = yb + k;
-            const int hi = (int)(E[0] >> 32) | (int)(E[1] >> 32) | (int)(E[2] >> 32);
-            const bool in = y >= (int)r.y0 && y <= (int)r.y1 && hi >= 0;
+            const bool in = y >= (int)r.y0 && y <= (int)r.y1 && inside_biased(E);
             if (in) {
                 const float l1 = i2f(E[1] + bias[1]) * r.inv_area, l2 = i2f(E[2] + bias[2]) * r.inv_area;
                 float z = r.z0 + (l1 * r.dz1 + l2 * r.dz2);
@@ -1412,7 +1407,7 @@ __device__ __forceinline__ void tiny_record(const TierArgs& a, unsigned i) {
             const int b1 = tl[1] ? 0 : 1, b2 = tl[2] ? 0 : 1;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                er[k] = (int)E0[k] - (tl[k] ? 0 : 1);
+                er[k] = (int)E0[k] - tl_bias(tl[k]);
                 sa[k] = h > 1 ? (int)(A[k] * kSub) : 0;
                 sb[k] = w > 1 ? (int)(B[k] * kSub) : 0;
             }
@@ -1480,10 +1475,10 @@ __device__ __forceinline__ void coop_record(const TierArgs& a, unsigned i, int l
             int e[3];
 #pragma unroll
             for (int k = 0; k < 3; ++k)
-                e[k] = (int)E0[k] + (int)A[k] * (dy << kSubBits) - (int)B[k] * (dx << kSubBits) - (tl[k] ? 0 : 1);
+                e[k] = (int)E0[k] + (int)A[k] * (dy << kSubBits) - (int)B[k] * (dx << kSubBits) - tl_bias(tl[k]);
             in = (e[0] | e[1] | e[2]) >= 0;
-            fe1 = (float)(e[1] + (tl[1] ? 0 : 1));
-            fe2 = (float)(e[2] + (tl[2] ? 0 : 1));
+            fe1 = (float)(e[1] + tl_bias(tl[1]));
+            fe2 = (float)(e[2] + tl_bias(tl[2]));
         } else {
             int64_t E[3];
 #pragma unroll
@@ -1578,13 +1573,12 @@ __global__ void __launch_bounds__(256) k_large_tiles(TierArgs a) {
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             const int ia = (i + 1) % 3;
-            E[i] = A[i] * (py - r.Y[ia]) - B[i] * (px - r.X[ia]);
+            E[i] = A[i] * (py - r.Y[ia]) - B[i] * (px - r.X[ia]) - tl_bias(tl[i]);
         }
 #pragma unroll 2
         for (int k = 0; k < kTile / 2; ++k, y += 2) {
-            const bool in = y >= py0 && y <= py1 && (E[0] > 0 || (E[0] == 0 && tl[0])) &&
-                            (E[1] > 0 || (E[1] == 0 && tl[1])) && (E[2] > 0 || (E[2] == 0 && tl[2]));
-            if (in) rec_emit<MODE>(a, r, x, y, i2f(E[1]), i2f(E[2]));
+            const bool in = y >= py0 && y <= py1 && inside_biased(E);
+            if (in) rec_emit<MODE>(a, r, x, y, i2f(E[1] + tl_bias(tl[1])), i2f(E[2] + tl_bias(tl[2])));
 #pragma unroll
             for (int i = 0; i < 3; ++i) E[i] += A[i] * (2 * kSub);
         }

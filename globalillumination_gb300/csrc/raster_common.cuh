@@ -229,6 +229,16 @@ __device__ __forceinline__ float i2f(int64_t v) {
     return (float)v;
 }
 
+// The top-left rule as a bias: an edge value E passes when E > 0, or
+// E == 0 on a top or left edge, that is when E - tl_bias >= 0.  With the
+// bias folded into the stepped values, a pixel is inside when none of the
+// three is negative.
+__device__ __forceinline__ int tl_bias(bool tl) { return tl ? 0 : 1; }
+
+__device__ __forceinline__ bool inside_biased(const int64_t E[3]) {
+    return ((int)(E[0] >> 32) | (int)(E[1] >> 32) | (int)(E[2] >> 32)) >= 0;
+}
+
 __device__ __forceinline__ float depth_at(const Setup& s, const int64_t E[3]) {
     float l1 = i2f(E[1]) * s.inv_area;
     float l2 = i2f(E[2]) * s.inv_area;
