@@ -969,14 +969,19 @@ struct FloorTrack {
     }
 };
 
-// One volume fragment of k_sliver: exact edge test, depth, z test, count.
-__device__ __forceinline__ void sliver_pixel(const BinArgs& a, const BRec& r, const int64_t A[3],
-                                             const int64_t B[3], const int64_t XA[3], const int64_t YA[3],
-                                             const bool tl[3], int y, int x, int inc) {
+// Biased edge values of k_sliver at pixel (x, y).
+__device__ __forceinline__ void sliver_edges(const int64_t A[3], const int64_t B[3], const int64_t XA[3],
+                                             const int64_t YA[3], const bool tl[3], int y, int x,
+                                             int64_t E[3]) {
     const int64_t py = (int64_t)y * kSub + kSub / 2, px = (int64_t)x * kSub + kSub / 2;
-    int64_t E[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) E[k] = A[k] * (py - YA[k]) - B[k] * (px - XA[k]) - tl_bias(tl[k]);
+}
+
+// One volume fragment of k_sliver from its biased edge values: exact edge
+// test, depth, z test, count.
+__device__ __forceinline__ void sliver_pixel(const BinArgs& a, const BRec& r, const int64_t E[3],
+                                             const bool tl[3], int y, int x, int inc) {
     if (!inside_biased(E)) return;
     const float l1 = i2f(E[1] + tl_bias(tl[1])) * r.inv_area, l2 = i2f(E[2] + tl_bias(tl[2])) * r.inv_area;
     const float z = clamp01(r.z0 + (l1 * r.dz1 + l2 * r.dz2));
@@ -1092,14 +1097,30 @@ __global__ void __launch_bounds__(256) k_sliver(BinArgs a) {
             const unsigned len = (y <= (int)r.y1 && hi >= lo) ? (unsigned)(hi - lo + 1) : 0u;
             const unsigned max_len = __reduce_max_sync(0xffffffffu, len);
             const unsigned row_iters = __reduce_add_sync(0xffffffffu, (len + 31u) >> 5);
+            // Along a row the edge values step by -B kSub per pixel (the
+            // same integers as evaluating each pixel afresh).
             if (max_len <= row_iters) {
-                for (int x = lo; x < lo + (int)len; ++x) sliver_pixel(a, r, A, B, XA, YA, tl, y, x, inc);
+                if (len) {
+                    int64_t E[3];
+                    sliver_edges(A, B, XA, YA, tl, y, lo, E);
+                    for (int x = lo; x < lo + (int)len; ++x) {
+                        sliver_pixel(a, r, E, tl, y, x, inc);
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) E[k] -= B[k] * kSub;
+                    }
+                }
             } else {
                 for (int rr = 0; rr < 32; ++rr) {
                     const int lo_r = __shfl_sync(0xffffffffu, lo, rr);
                     const int n_r = (int)__shfl_sync(0xffffffffu, len, rr);
-                    for (int x = lo_r + lane; x < lo_r + n_r; x += 32)
-                        sliver_pixel(a, r, A, B, XA, YA, tl, yc + rr, x, inc);
+                    if (lane >= n_r) continue;
+                    int64_t E[3];
+                    sliver_edges(A, B, XA, YA, tl, yc + rr, lo_r + lane, E);
+                    for (int x = lo_r + lane; x < lo_r + n_r; x += 32) {
+                        sliver_pixel(a, r, E, tl, yc + rr, x, inc);
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) E[k] -= B[k] * (32 * kSub);
+                    }
                 }
             }
         }
