@@ -969,28 +969,6 @@ struct FloorTrack {
     }
 };
 
-// Biased edge values of k_sliver at pixel (x, y).
-__device__ __forceinline__ void sliver_edges(const int64_t A[3], const int64_t B[3], const int64_t XA[3],
-                                             const int64_t YA[3], const bool tl[3], int y, int x,
-                                             int64_t E[3]) {
-    const int64_t py = (int64_t)y * kSub + kSub / 2, px = (int64_t)x * kSub + kSub / 2;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) E[k] = A[k] * (py - YA[k]) - B[k] * (px - XA[k]) - tl_bias(tl[k]);
-}
-
-// One volume fragment of k_sliver from its biased edge values: exact edge
-// test, depth, z test, count.
-__device__ __forceinline__ void sliver_pixel(const BinArgs& a, const BRec& r, const int64_t E[3],
-                                             const bool tl[3], int y, int x, int inc) {
-    if (!inside_biased(E)) return;
-    const float l1 = i2f(E[1] + tl_bias(tl[1])) * r.inv_area, l2 = i2f(E[2] + tl_bias(tl[2])) * r.inv_area;
-    const float z = clamp01(r.z0 + (l1 * r.dz1 + l2 * r.dz2));
-    const size_t idx = (size_t)y * a.r.W + x;
-    const float d = __uint_as_float(__ldg(a.r.depth + idx));
-    const bool pass = a.r.depth_func == GI_DEPTH_LEQUAL ? (z <= d) : (z < d);
-    if (pass) atomicAdd(a.r.counts + idx, inc);
-}
-
 __global__ void __launch_bounds__(256) k_sliver(BinArgs a) {
     const unsigned n = min(a.ctr[1], a.big_cap);
     const int lane = threadIdx.x & 31;
@@ -1009,7 +987,7 @@ __global__ void __launch_bounds__(256) k_sliver(BinArgs a) {
             YA[k] = r.Y[ia];
         }
         // every lane takes part in the shuffles below; lanes past the last
-        // row get empty intervals
+        // row simply run no row iterations
         const int y_first = (int)r.y0 + lane;
         // edge k at row y: E(x) = K - B * (x * 256 + 128), K = A * (py - Ya) + B * Xa.
         // The bound of edge k is floor(num / den) with num linear in the row;
@@ -1069,8 +1047,7 @@ __global__ void __launch_bounds__(256) k_sliver(BinArgs a) {
         }
         const float sgn_front = (r.flags & kFlagFront) ? 1.0f : -1.0f;
         const int inc = sgn_front > 0.0f ? 1 : -1;
-        for (int yc = (int)r.y0, it = 0; yc <= (int)r.y1; yc += 32, ++it) {
-            const int y = yc + lane;
+        for (int y = y_first, it = 0; y <= (int)r.y1; y += 32, ++it) {
             if (it > 0) {
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
@@ -1090,38 +1067,19 @@ __global__ void __launch_bounds__(256) k_sliver(BinArgs a) {
                     if (xm > (int64_t)lo) lo = (int)min(xm, (int64_t)hi + 1);
                 }
             }
-            // The 32 rows' intervals are walked either one row per lane
-            // (steep slivers: short rows) or row by row with the lanes over
-            // x (flat slivers: long rows, coalesced depth reads and
-            // atomics), whichever takes fewer warp iterations.
-            const unsigned len = (y <= (int)r.y1 && hi >= lo) ? (unsigned)(hi - lo + 1) : 0u;
-            const unsigned max_len = __reduce_max_sync(0xffffffffu, len);
-            const unsigned row_iters = __reduce_add_sync(0xffffffffu, (len + 31u) >> 5);
-            // Along a row the edge values step by -B kSub per pixel (the
-            // same integers as evaluating each pixel afresh).
-            if (max_len <= row_iters) {
-                if (len) {
-                    int64_t E[3];
-                    sliver_edges(A, B, XA, YA, tl, y, lo, E);
-                    for (int x = lo; x < lo + (int)len; ++x) {
-                        sliver_pixel(a, r, E, tl, y, x, inc);
+            const int64_t py = (int64_t)y * kSub + kSub / 2;
+            for (int x = lo; x <= hi; ++x) {
+                const int64_t px = (int64_t)x * kSub + kSub / 2;
+                int64_t E[3];
 #pragma unroll
-                        for (int k = 0; k < 3; ++k) E[k] -= B[k] * kSub;
-                    }
-                }
-            } else {
-                for (int rr = 0; rr < 32; ++rr) {
-                    const int lo_r = __shfl_sync(0xffffffffu, lo, rr);
-                    const int n_r = (int)__shfl_sync(0xffffffffu, len, rr);
-                    if (lane >= n_r) continue;
-                    int64_t E[3];
-                    sliver_edges(A, B, XA, YA, tl, yc + rr, lo_r + lane, E);
-                    for (int x = lo_r + lane; x < lo_r + n_r; x += 32) {
-                        sliver_pixel(a, r, E, tl, yc + rr, x, inc);
-#pragma unroll
-                        for (int k = 0; k < 3; ++k) E[k] -= B[k] * (32 * kSub);
-                    }
-                }
+                for (int k = 0; k < 3; ++k) E[k] = A[k] * (py - YA[k]) - B[k] * (px - XA[k]) - tl_bias(tl[k]);
+                if (!inside_biased(E)) continue;
+                const float l1 = i2f(E[1] + tl_bias(tl[1])) * r.inv_area, l2 = i2f(E[2] + tl_bias(tl[2])) * r.inv_area;
+                const float z = clamp01(r.z0 + (l1 * r.dz1 + l2 * r.dz2));
+                const size_t idx = (size_t)y * a.r.W + x;
+                const float d = __uint_as_float(__ldg(a.r.depth + idx));
+                const bool pass = a.r.depth_func == GI_DEPTH_LEQUAL ? (z <= d) : (z < d);
+                if (pass) atomicAdd(a.r.counts + idx, inc);
             }
         }
     }
