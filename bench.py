@@ -70,6 +70,7 @@ import re
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -139,15 +140,18 @@ class ClockSampler:
 
     def __init__(self, gpu_index: int):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else ".",
-                                 f".clocks_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"gi_clocks_{os.getpid()}.csv")
+        self.fh = None
         try:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.FIELDS}",
                  "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
-        except (OSError, FileNotFoundError):
+        except OSError:
             self.proc = None
+            if self.fh is not None:
+                self.fh.close()
+                os.unlink(self.path)
 
     def stop(self):
         if self.proc is None:
