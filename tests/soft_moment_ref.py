@@ -44,7 +44,9 @@ def linearize(d):
 
 
 def nonlinearize(d):
-    return -(f32(2.0) - d * f32(1001.0)) / (d * f32(999.0))
+    # d == 0 divides by zero and gives -inf, as the shader's IEEE division does
+    with np.errstate(divide="ignore"):
+        return -(f32(2.0) - d * f32(1001.0)) / (d * f32(999.0))
 
 
 def msm_inverse():
