@@ -1093,3 +1093,14 @@ extern "C" gi_status gi_shadow_volume_counts(gi_context* ctx, const gi_scene* s,
                                      d_stencil, d_depth, small_px_default(),
                                      static_cast<cudaStream_t>(stream));
 }
+
+extern "C" gi_status gi_shadow_volume_geometry(gi_context* ctx, const gi_scene* s,
+                                               const float light_pos[3], float infinity,
+                                               float* d_triangles, void* stream) {
+    gi_status st = check_pass(ctx, s);
+    if (st != GI_OK) return st;
+    if (!light_pos || (!d_triangles && s->dev_triangles > 0))
+        return fail(GI_ERR_INVALID_ARG, "gi_shadow_volume_geometry: NULL argument");
+    return gi::raster_volume_geometry(ctx, s, light_pos, infinity, d_triangles,
+                                      static_cast<cudaStream_t>(stream));
+}

@@ -136,6 +136,22 @@ __device__ __forceinline__ void prim_vertices(const RasterArgs& a, int prim, flo
     }
 }
 
+// The volume triangles exactly as the stencil pass draws them: entry 6t + k
+// holds side triangle k of input triangle t as three object-space vertices
+// (ShadowVolume::build, ShadowVolume.cpp:15-114, resolved through its index
+// buffer).
+__global__ void __launch_bounds__(256) k_volume_geometry(RasterArgs a, float* out) {
+    const int prim = blockIdx.x * blockDim.x + threadIdx.x;
+    if (prim >= a.num_prims) return;
+    float v[3][3];
+    prim_vertices<MODE_STENCIL>(a, prim, v);
+    float* o = out + (size_t)prim * 9;
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) o[j * 3 + ax] = v[j][ax];
+}
+
 template <int MODE>
 __device__ __forceinline__ void emit(const RasterArgs& a, int x, int y, float z, float zoff,
                                      unsigned prim, bool front) {
@@ -1902,6 +1918,26 @@ gi_status raster_gbuffer_keys(gi_context* ctx, const gi_scene* scene, const floa
     return run_tiered(ctx, a, dev::MODE_VKEY, st);
 }
 
+gi_status raster_volume_geometry(gi_context* ctx, const gi_scene* scene, const float L[3],
+                                 float infinity, float* d_out, cudaStream_t st) {
+    if ((long long)scene->dev_triangles * 6 >= (1LL << 29))
+        return fail(GI_ERR_CAPACITY, "too many volume triangles (6 T must stay below 2^29)");
+    dev::RasterArgs a = {};
+    a.points = scene->d_points;
+    a.normals = scene->d_normals;
+    a.indices = scene->d_indices;
+    a.num_prims = scene->dev_triangles * 6;
+    a.L[0] = L[0];
+    a.L[1] = L[1];
+    a.L[2] = L[2];
+    a.infinity = infinity;
+    if (a.num_prims == 0) return GI_OK;
+    dev::k_volume_geometry<<<grid_for((size_t)a.num_prims, 256), 256, 0, st>>>(a, d_out);
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "volume geometry launch");
+}
+
 gi_status raster_shadow_volumes(gi_context* ctx, const gi_scene* scene, const float L[3],
                                 float infinity, const float mvp[16], int W, int H, int depth_func,
                                 unsigned char* d_stencil, float* d_depth_out, int small_px,
@@ -1971,26 +2007,43 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
 constexpr int kNoallocMaxDevices = 64;
 std::mutex g_noalloc_mutex;
-void* g_noalloc_addr[kNoallocMaxDevices] = {};
+// Per device: the scratch address under which the pass's kernels were last
+// loaded.  A new CUDA context on the same device (after cudaDeviceReset, or
+// a caller's own driver-API context) has its own copy of the module and so
+// a different address; the kernels are then loaded again.
+void* g_noalloc_loaded[kNoallocMaxDevices] = {};
 
-// Device address of g_noalloc_scratch on the current device, resolved once
-// per device.  The array's name in host code is only a host-side handle.
-gi_status noalloc_scratch(unsigned char** out) {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return fail_cuda(e, "gi_gbuffer_noalloc: cudaGetDevice");
+// Device address of g_noalloc_scratch in the current context.  The array's
+// name in host code is only a host-side handle; the address is looked up on
+// every call (cheap once the module is loaded) and never cached across
+// contexts.  The first call in a context loads the library's module and,
+// here, every kernel the pass launches (cudaFuncGetAttributes), so that no
+// later call, whatever its triangle count, triggers lazy loading.
+gi_status noalloc_scratch(int dev, unsigned char** out) {
     if (dev < 0 || dev >= kNoallocMaxDevices)
         return fail(GI_ERR_UNSUPPORTED, "gi_gbuffer_noalloc: device index out of range");
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+        return fail_cuda(e == cudaSuccess ? cudaErrorInvalidSymbol : e,
+                         "gi_gbuffer_noalloc: cudaGetSymbolAddress");
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p)
-            return fail_cuda(e == cudaSuccess ? cudaErrorInvalidSymbol : e,
-                             "gi_gbuffer_noalloc: cudaGetSymbolAddress");
-        g_noalloc_addr[dev] = p;
+    if (g_noalloc_loaded[dev] != p) {
+        const void* kernels[] = {
+            reinterpret_cast<const void*>(&dev::k_fill_u64),
+            reinterpret_cast<const void*>(&dev::k_setup<dev::MODE_VKEY>),
+            reinterpret_cast<const void*>(&dev::k_scan),
+            reinterpret_cast<const void*>(&dev::k_tiles<dev::MODE_VKEY>),
+            reinterpret_cast<const void*>(&dev::k_gbuffer_resolve),
+        };
+        for (const void* k : kernels) {
+            cudaFuncAttributes fa;
+            e = cudaFuncGetAttributes(&fa, k);
+            if (e != cudaSuccess) return fail_cuda(e, "gi_gbuffer_noalloc: loading the pass's kernels");
+        }
+        g_noalloc_loaded[dev] = p;
     }
-    *out = static_cast<unsigned char*>(g_noalloc_addr[dev]);
+    *out = static_cast<unsigned char*>(p);
     return GI_OK;
 }
 
@@ -2014,8 +2067,11 @@ extern "C" gi_status gi_gbuffer_noalloc(const float* d_points, const float* d_no
                         " pixels exceed the allocation-free scratch (at most 1048576 = 1024 x 1024)");
     if ((size_t)num_triangles >= ((size_t)1 << 29))
         return fail(GI_ERR_CAPACITY, "gi_gbuffer_noalloc: more than 2^29 triangles");
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess) return fail_cuda(e, "gi_gbuffer_noalloc: cudaGetDevice");
     unsigned char* base = nullptr;
-    gi_status st = noalloc_scratch(&base);
+    gi_status st = noalloc_scratch(device, &base);
     if (st != GI_OK) return st;
     cudaStream_t cs = static_cast<cudaStream_t>(stream);
     unsigned long long* keys = reinterpret_cast<unsigned long long*>(base);
@@ -2023,10 +2079,8 @@ extern "C" gi_status gi_gbuffer_noalloc(const float* d_points, const float* d_no
     unsigned* status = reinterpret_cast<unsigned*>(base + kNoallocKeysBytes + kNoallocRecsBytes);
     // The array keeps the previous call's contents: reset the counters and
     // the keys before use.
-    cudaError_t e = cudaMemsetAsync(status, 0, kNoallocStatusBytes, cs);
+    e = cudaMemsetAsync(status, 0, kNoallocStatusBytes, cs);
     if (e != cudaSuccess) return fail_cuda(e, "gi_gbuffer_noalloc: cudaMemsetAsync");
-    int device = 0;
-    cudaGetDevice(&device);
     const unsigned fill_blocks = std::min<unsigned>(grid_for(npx, 256), (unsigned)sm_count(device) * 8);
     const unsigned long long clear = ((unsigned long long)0x3f800000u << 32) | 0xFFFFFFFFull;
     dev::k_fill_u64<<<fill_blocks, 256, 0, cs>>>(keys, npx, clear);

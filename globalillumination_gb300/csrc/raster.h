@@ -16,6 +16,9 @@ gi_status raster_depth_map(gi_context* ctx, const gi_scene* scene, const float m
 gi_status raster_gbuffer(gi_context* ctx, const gi_scene* scene, const float mvp[16], int W, int H,
                          float* d_pos, float* d_nrm, int small_px, cudaStream_t st);
 
+// The 6T volume triangles of the stencil pass, 9 floats each, into d_out.
+gi_status raster_volume_geometry(gi_context* ctx, const gi_scene* scene, const float L[3],
+                                 float infinity, float* d_out, cudaStream_t st);
 gi_status raster_shadow_volumes(gi_context* ctx, const gi_scene* scene, const float L[3],
                                 float infinity, const float mvp[16], int W, int H, int depth_func,
                                 unsigned char* d_stencil, float* d_depth_out, int small_px,

@@ -412,6 +412,16 @@ def shadow_volume_counts(ctx: Context, scene: Scene, light_pos, camera_mvp, widt
     return stencil
 
 
+def shadow_volume_geometry(ctx: Context, scene: Scene, light_pos, out, infinity: float = 100.0, stream=None):
+    """ShadowVolume::build's triangles as the stencil pass draws them: out is a float32
+    CUDA tensor of 6T * 9 values (entry 6t + k = side k of triangle t, three vertices)."""
+    nt = scene.info().num_triangles
+    assert out.is_cuda and out.dtype.is_floating_point and out.numel() >= 6 * nt * 9
+    check(_lib().gi_shadow_volume_geometry(ctx.handle, scene.handle, _f3(light_pos), float(infinity), _ptr(out),
+                                           _stream_ptr(stream)), "gi_shadow_volume_geometry")
+    return out
+
+
 @dataclass
 class FrameBuffers:
     depth: object

@@ -257,11 +257,15 @@ gi_status gi_gbuffer(gi_context* ctx, const gi_scene* scene,
  * result as gi_gbuffer, with the geometry passed as caller-owned device
  * arrays and no gi_context: the pass's scratch (per-pixel keys, large-
  * triangle records, counters) lives in one static device array of
- * 9,568,512 bytes that every GPU loading the library reserves until the
- * process exits.  Limit: width * height <= 1,048,576 (1024 x 1024); larger
+ * 9,568,512 bytes that each GPU holds from the library's first use on it
+ * (the module load) until the process exits.  Limit: width * height <= 1,048,576 (1024 x 1024); larger
  * images return GI_ERR_CAPACITY.  Runs on the calling thread's current
- * device; the first call on each device looks up the array's device
- * address, so make that first call before any stream capture.  Every call
+ * device and CUDA context.  The array's device address is per context and
+ * is looked up on every call.  The first call in a context loads the
+ * library's module and every kernel of the pass (CUDA loads modules lazily
+ * by default), which can itself allocate and synchronise: make that first
+ * call a warm-up outside the frame loop and before any stream capture (any
+ * triangle count, zero included, loads all of them).  Every call
  * reuses the same array: calls that overlap on the GPU (other streams,
  * other threads) race and must be serialised by the caller.  Allocates
  * nothing (no cudaMalloc / cudaFree). */
@@ -557,6 +561,18 @@ gi_status gi_shadow_volume_counts(gi_context* ctx, const gi_scene* scene,
                                   int height, int depth_func,
                                   uint8_t* d_stencil, float* d_depth,
                                   void* stream);
+
+/* ShadowVolume::build / update (ShadowVolumes/src/ShadowVolume.cpp:15-194,
+ * infinity 100 at ShadowVolumes/src/main.cpp:469-470) for callers that draw
+ * the volumes themselves: the 6T volume triangles exactly as
+ * gi_shadow_volume_counts rasterises them, resolved through the reference's
+ * index buffer.  d_triangles is float[6T * 9]: entry 6t + k is side triangle
+ * k of scene triangle t as three object-space vertices (x, y, z), the near
+ * vertices copied, the far ones (v - L) * infinity, wound by the sign of
+ * dot((n0 + n1 + n2) / 3, light_pos). */
+gi_status gi_shadow_volume_geometry(gi_context* ctx, const gi_scene* scene,
+                                    const float light_pos[3], float infinity,
+                                    float* d_triangles, void* stream);
 
 /* ------------------------------------------------------------------ */
 /* Batched frames under one CUDA graph                                 */

@@ -26,6 +26,8 @@ def load():
         lib.or_gbuffer.argtypes = [vp, vp, i, vp, i, vp, i, i, vp, vp, i]
         lib.or_visibility.argtypes = [vp, vp, i, i, vp, vp, vp, i, i, vp, i]
         lib.or_shadow_volume_counts.argtypes = [vp, vp, i, vp, i, vp, f, vp, i, i, i, vp, vp, i]
+        lib.or_shadow_volume_geometry.argtypes = [vp, vp, vp, i, vp, f, vp]
+        lib.or_shadow_volume_geometry.restype = None
         lib.or_rbssm_hits.argtypes = [vp, i]
         lib.or_phong_shade.argtypes = [vp, vp, vp, vp, vp, i, i, vp]
         lib.or_area_light_visibility.argtypes = [vp, vp, i, vp, i, vp, vp, i, i, i, f, f, f, vp, f, i, i, vp, i]
@@ -136,6 +138,84 @@ def shadow_volume_counts(points, normals, indices, light_pos, infinity, mvp, wid
                                    L.ctypes.data, infinity, m.ctypes.data, width, height, depth_func,
                                    st.ctypes.data, dp.ctypes.data, threads)
     return st, dp
+
+
+def shadow_volume_geometry(points, normals, indices, light_pos, infinity):
+    """ShadowVolume::build's triangles: float32 [6T, 3, 3] (entry 6t + k is side k of triangle t)."""
+    p, n = _f32(points), _f32(normals)
+    ix, L = np.ascontiguousarray(indices, dtype=np.int32), _f32(light_pos)
+    nt = ix.size // 3
+    out = np.empty((6 * nt, 3, 3), np.float32)
+    load().or_shadow_volume_geometry(p.ctypes.data, n.ctypes.data, ix.ctypes.data, nt, L.ctypes.data, infinity,
+                                     out.ctypes.data)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# The reference's own scene C++ (oracle/_ref/libscene_ref_<app>.so, built by
+# build_oracle.build_scene_ref where the reference tree is present).
+# ---------------------------------------------------------------------------
+class _PinScene(C.Structure):
+    _fields_ = [("num_vertices", C.c_int), ("num_triangles", C.c_int), ("points", C.POINTER(C.c_float)),
+                ("normals", C.POINTER(C.c_float)), ("indices", C.POINTER(C.c_int)), ("views", C.c_float * 13)]
+
+
+_scene_refs: dict = {}
+
+
+def scene_ref(app: str = "ShadowMapping"):
+    """The reference's scene loader of `app` ("ShadowMapping" or "ShadowVolumes"), or None if not built."""
+    from .build_oracle import scene_ref_lib
+
+    if app not in _scene_refs:
+        path = scene_ref_lib(app)
+        if not os.path.exists(path):
+            return None
+        lib = C.CDLL(path)
+        lib.pin_scene_load.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(_PinScene)]
+        lib.pin_scene_load.restype = C.c_int
+        lib.pin_scene_free.argtypes = [C.POINTER(_PinScene)]
+        lib.pin_scene_free.restype = None
+        if hasattr(lib, "pin_shadow_volume_build"):
+            vp, i = C.c_void_p, C.c_int
+            lib.pin_shadow_volume_build.argtypes = [vp, vp, i, vp, i, vp, i, vp, vp]
+            lib.pin_shadow_volume_build.restype = C.c_int
+        _scene_refs[app] = lib
+    return _scene_refs[app]
+
+
+def ref_load_config(cfg_path: str, base_dir: str, app: str = "ShadowMapping"):
+    """SceneLoader::load + Mesh of the reference itself: (points [V,3], normals [V,3], indices [T,3], views[13])."""
+    lib = scene_ref(app)
+    if lib is None:
+        raise RuntimeError(f"the reference scene pin for {app} is not built")
+    sc = _PinScene()
+    if lib.pin_scene_load(cfg_path.encode(), base_dir.encode(), C.byref(sc)) != 0:
+        raise OSError(f"reference SceneLoader could not open {cfg_path}")
+    nv, nt = sc.num_vertices, sc.num_triangles
+    p = np.ctypeslib.as_array(sc.points, (nv * 3,)).copy().reshape(nv, 3)
+    n = np.ctypeslib.as_array(sc.normals, (nv * 3,)).copy().reshape(nv, 3)
+    ix = np.ctypeslib.as_array(sc.indices, (nt * 3,)).copy().reshape(nt, 3)
+    views = np.array(sc.views[:], np.float32)
+    lib.pin_scene_free(C.byref(sc))
+    return p, n, ix, views
+
+
+def ref_shadow_volume_build(points, normals, indices, light_pos, infinity: int = 100):
+    """ShadowVolume::build of the reference itself: (quad points [6T, 3], index buffer [6T, 3])."""
+    lib = scene_ref("ShadowVolumes")
+    if lib is None:
+        raise RuntimeError("the reference ShadowVolumes pin is not built")
+    p, n = _f32(points), _f32(normals)
+    ix, L = np.ascontiguousarray(indices, dtype=np.int32), _f32(light_pos)
+    nv, nt = p.size // 3, ix.size // 3
+    out_p = np.empty((6 * nt, 3), np.float32)
+    out_i = np.empty((6 * nt, 3), np.int32)
+    rc = lib.pin_shadow_volume_build(p.ctypes.data, n.ctypes.data, nv, ix.ctypes.data, nt, L.ctypes.data,
+                                     int(infinity), out_p.ctypes.data, out_i.ctypes.data)
+    if rc != 0:
+        raise ValueError("empty mesh")
+    return out_p, out_i
 
 
 def rbssm_hits(reset=False):

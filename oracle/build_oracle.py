@@ -12,8 +12,17 @@
                           compiled for the CPU against a CUDA-emulation shim;
                           built only where the reference tree is present.
 
-Only the tests, the smoke check and the CPU-baseline leg of bench.py use
-these files; the product library never links or loads them.
+  oracle/_ref/libscene_ref_shadowmapping.so, libscene_ref_shadowvolumes.so
+                          ref_scene_pin.cpp linked with the reference's own,
+                          unmodified SceneLoader.cpp, Mesh.cpp and OBJLoader.cpp
+                          of that app (and ShadowVolume.cpp for ShadowVolumes),
+                          read where they lie, against a generated include
+                          shim under oracle/_ref/shim/; built only where the
+                          reference tree is present.
+
+Only the tests, the smoke check, the fixture generators and the CPU-baseline
+leg of bench.py use these files; the product library never links or loads
+them.
 """
 from __future__ import annotations
 
@@ -25,7 +34,8 @@ ROOT = os.path.dirname(HERE)
 ORACLE_LIB = os.path.join(HERE, "libgioracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 GLM_PIN = os.path.join(REF_DIR, "glm_pin")
-REFERENCE_ROOT = "/root/reference"
+# The reference tree (read-only); GI_REFERENCE_ROOT overrides the default.
+REFERENCE_ROOT = os.environ.get("GI_REFERENCE_ROOT", "/root/reference")
 GLM_INCLUDE = os.path.join(REFERENCE_ROOT, "ShadowMapping", "include")
 PBA_INCLUDE = os.path.join(REFERENCE_ROOT, "ShadowMapping", "include", "EDT")
 PBA_REF_LIB = os.path.join(REF_DIR, "libpba_ref.so")
@@ -76,7 +86,98 @@ def build_pba_ref() -> str | None:
     return PBA_REF_LIB
 
 
+SCENE_PIN_APPS = ("ShadowMapping", "ShadowVolumes")
+SHIM_DIR = os.path.join(REF_DIR, "shim")
+
+# What the reference's sources include but Linux does not have: GL types and
+# no-op GL calls (only glm.c's drawing functions call them; loading never
+# does), the Windows-style backslash include paths, and OpenCV (Image.h's
+# include; the pin replaces Image.cpp).
+_GLUT_SHIM = """#ifndef GI_PIN_GLUT_SHIM
+#define GI_PIN_GLUT_SHIM
+typedef float GLfloat;
+typedef unsigned int GLuint;
+typedef int GLint;
+typedef int GLsizei;
+typedef unsigned int GLenum;
+typedef unsigned char GLboolean;
+typedef unsigned char GLubyte;
+typedef void GLvoid;
+#define GL_FALSE 0
+#define GL_TRUE 1
+#define GL_TRIANGLES 0x0004
+#define GL_FRONT_AND_BACK 0x0408
+#define GL_AMBIENT 0x1200
+#define GL_DIFFUSE 0x1201
+#define GL_SPECULAR 0x1202
+#define GL_SHININESS 0x1601
+#define GL_COMPILE 0x1300
+#define GL_COLOR_MATERIAL 0x0B57
+static inline void glBegin(GLenum) {}
+static inline void glEnd(void) {}
+static inline void glEnable(GLenum) {}
+static inline void glDisable(GLenum) {}
+static inline void glNormal3fv(const GLfloat*) {}
+static inline void glVertex3fv(const GLfloat*) {}
+static inline void glTexCoord2fv(const GLfloat*) {}
+static inline void glColor3fv(const GLfloat*) {}
+static inline void glMaterialfv(GLenum, GLenum, const GLfloat*) {}
+static inline void glMaterialf(GLenum, GLenum, GLfloat) {}
+static inline GLuint glGenLists(GLsizei) { return 1; }
+static inline void glNewList(GLuint, GLenum) {}
+static inline void glEndList(void) {}
+#endif
+"""
+
+
+def _write_shim() -> None:
+    os.makedirs(os.path.join(SHIM_DIR, "GL"), exist_ok=True)
+    files = {
+        os.path.join(SHIM_DIR, "GL", "glut.h"): _GLUT_SHIM,
+        os.path.join(SHIM_DIR, "IO\\SceneLoader.h"): '#include "IO/SceneLoader.h"\n',
+        os.path.join(SHIM_DIR, "opencv2\\opencv.hpp"): "/* OpenCV is not needed to load geometry; its header brought in the C\n"
+                                                             " * library declarations the reference's files use. */\n"
+                                                             "#include <cstring>\n#include <cstdlib>\n#include <cstdio>\n",
+    }
+    for path, text in files.items():
+        if not os.path.exists(path) or open(path).read() != text:
+            with open(path, "w") as f:
+                f.write(text)
+
+
+def scene_ref_lib(app: str) -> str:
+    return os.path.join(REF_DIR, f"libscene_ref_{app.lower()}.so")
+
+
+def build_scene_ref() -> list[str]:
+    """Builds the scene / shadow-volume pins when the reference's C++ is available."""
+    built = []
+    for app in SCENE_PIN_APPS:
+        base = os.path.join(REFERENCE_ROOT, app)
+        srcs = [os.path.join(base, "src", "IO", "SceneLoader.cpp"), os.path.join(base, "src", "Mesh.cpp"),
+                os.path.join(base, "src", "IO", "OBJLoader.cpp")]
+        defs = []
+        if app == "ShadowVolumes":
+            srcs.append(os.path.join(base, "src", "ShadowVolume.cpp"))
+            defs.append("-DGI_PIN_VOLUMES")
+        if not all(os.path.exists(f) for f in srcs):
+            continue
+        os.makedirs(REF_DIR, exist_ok=True)
+        _write_shim()
+        pin = os.path.join(HERE, "ref_scene_pin.cpp")
+        lib = scene_ref_lib(app)
+        if _newer(lib, [pin, *srcs, os.path.abspath(__file__)]):
+            tmp = lib + ".tmp"
+            subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+                            "-fvisibility=hidden", "-w", *defs, "-I", SHIM_DIR, "-I", os.path.join(base, "include"),
+                            pin, *srcs, "-o", tmp], check=True)
+            os.replace(tmp, lib)
+        built.append(lib)
+    return built
+
+
 if __name__ == "__main__":
     print(build_oracle())
     print(build_ref())
     print(build_pba_ref())
+    print(build_scene_ref())

@@ -409,6 +409,43 @@ extern "C" void or_gbuffer(const float* points, const float* normals, int nv, co
         }
 }
 
+// ShadowVolume::build/update (ShadowVolumes/src/ShadowVolume.cpp:15-194):
+// the six quad vertices of triangle t (near copies, far (v - L) * infinity)
+// and the index pattern its winding rule picks (dot of the averaged vertex
+// normal with the light position, :55-61).
+namespace {
+const int kVolPatA[6][3] = {{1, 0, 3}, {1, 3, 4}, {2, 1, 4}, {2, 4, 5}, {0, 2, 5}, {0, 5, 3}};
+const int kVolPatB[6][3] = {{4, 3, 0}, {4, 0, 1}, {5, 4, 1}, {5, 1, 2}, {3, 5, 2}, {3, 2, 0}};
+
+const int (*volume_quad(const float* points, const float* normals, const int* indices, int t, const float L[3],
+                        float infinity, float q[6][3]))[3] {
+    const int* tri = indices + 3 * (size_t)t;
+    for (int k = 0; k < 3; ++k)
+        for (int a = 0; a < 3; ++a) {
+            q[k][a] = points[3 * (size_t)tri[k] + a];
+            q[k + 3][a] = (points[3 * (size_t)tri[k] + a] - L[a]) * infinity;
+        }
+    const float* n0 = normals + 3 * (size_t)tri[0];
+    const float* n1 = normals + 3 * (size_t)tri[1];
+    const float* n2 = normals + 3 * (size_t)tri[2];
+    float n[3];
+    for (int a = 0; a < 3; ++a) n[a] = ((n0[a] + n1[a]) + n2[a]) / 3.0f;
+    float d = n[0] * L[0] + n[1] * L[1] + n[2] * L[2];
+    return d >= 0.0f ? kVolPatA : kVolPatB;
+}
+}  // namespace
+
+extern "C" void or_shadow_volume_geometry(const float* points, const float* normals, const int* indices, int nt,
+                                          const float L[3], float infinity, float* out) {
+    for (int t = 0; t < nt; ++t) {
+        float q[6][3];
+        const int(*pat)[3] = volume_quad(points, normals, indices, t, L, infinity, q);
+        for (int k = 0; k < 6; ++k)
+            for (int j = 0; j < 3; ++j)
+                for (int a = 0; a < 3; ++a) out[((size_t)t * 6 + k) * 9 + j * 3 + a] = q[pat[k][j]][a];
+    }
+}
+
 extern "C" void or_shadow_volume_counts(const float* points, const float* normals, int nv,
                                         const int* indices, int nt, const float L[3],
                                         float infinity, const float mvp[16], int W, int H,
@@ -421,25 +458,10 @@ extern "C" void or_shadow_volume_counts(const float* points, const float* normal
     raster_depth(points, indices, nt, mvp, W, H, GI_BIAS_NONE, 0, 0, 0, depth.data(), threads);
     std::vector<std::atomic<int>> count(npx);
     for (auto& c : count) c.store(0, std::memory_order_relaxed);
-    // ShadowVolume::build/update (ShadowVolumes/src/ShadowVolume.cpp:15-194).
-    static const int kPatA[6][3] = {{1, 0, 3}, {1, 3, 4}, {2, 1, 4}, {2, 4, 5}, {0, 2, 5}, {0, 5, 3}};
-    static const int kPatB[6][3] = {{4, 3, 0}, {4, 0, 1}, {5, 4, 1}, {5, 1, 2}, {3, 5, 2}, {3, 2, 0}};
 #pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads(threads))
     for (int t = 0; t < nt; ++t) {
-        const int* tri = indices + 3 * (size_t)t;
         float q[6][3];
-        for (int k = 0; k < 3; ++k)
-            for (int a = 0; a < 3; ++a) {
-                q[k][a] = points[3 * (size_t)tri[k] + a];
-                q[k + 3][a] = (points[3 * (size_t)tri[k] + a] - L[a]) * infinity;
-            }
-        const float* n0 = normals + 3 * (size_t)tri[0];
-        const float* n1 = normals + 3 * (size_t)tri[1];
-        const float* n2 = normals + 3 * (size_t)tri[2];
-        float n[3];
-        for (int a = 0; a < 3; ++a) n[a] = ((n0[a] + n1[a]) + n2[a]) / 3.0f;
-        float d = n[0] * L[0] + n[1] * L[1] + n[2] * L[2];
-        const int(*pat)[3] = d >= 0.0f ? kPatA : kPatB;
+        const int(*pat)[3] = volume_quad(points, normals, indices, t, L, infinity, q);
         for (int k = 0; k < 6; ++k) {
             float c[3][4];
             for (int j = 0; j < 3; ++j) transform(mvp, q[pat[k][j]], c[j]);
@@ -2578,6 +2600,9 @@ extern "C" void or_rbssm_hits(unsigned long long* out4096, int reset) {
 // reference; a site image is processed column by column (phase 1) and then
 // row by row (phases 2-3), which is what the reference's transposes do.
 // ===========================================================================
+// PBA: Copyright (c) 2010, School of Computing, National University of
+// Singapore.  All rights reserved.  Redistribution terms: the BSD notice
+// reproduced at the top of globalillumination_gb300/csrc/edt.cu.
 namespace {
 namespace pba {
 

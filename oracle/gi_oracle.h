@@ -58,6 +58,9 @@ void or_hierarchical_shadow_map(const gi_vis_params* p, const float* depth, int 
                                 float* out);
 
 /* Shadow-volume stencil counts (uint8, wrapping). out_depth may be NULL. */
+/* The 6T volume triangles (9 floats each) of ShadowVolume::build. */
+void or_shadow_volume_geometry(const float* points, const float* normals, const int* indices, int nt,
+                               const float L[3], float infinity, float* out);
 void or_shadow_volume_counts(const float* points, const float* normals,
                              int nv, const int* indices, int nt,
                              const float light_pos[3], float infinity,

@@ -7,7 +7,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-REFERENCE = "/root/reference"
+# The reference tree, present only where the fixtures are made (GI_REFERENCE_ROOT
+# overrides the default); tests that read it skip elsewhere.
+REFERENCE = os.environ.get("GI_REFERENCE_ROOT", "/root/reference")
 
 
 def pytest_configure(config):
