@@ -14,7 +14,11 @@ one shadowed frame: light-view depth map, G-buffer, visibility.
           and reads the visibility buffer back to pinned host memory; two
           frames are in flight on two contexts and compute streams, with
           uploads and read-backs on their own streams (no L2 flush: each
-          frame's inputs arrive fresh from the host)
+          frame's inputs arrive fresh from the host).  Because two frames
+          overlap and L2 is not flushed, e2e can exceed `value`, which
+          times each frame alone between its events after an L2 flush: e2e
+          is pipelined throughput, `value` the latency-bound rate of one
+          frame at a time
   roofline  the fused G-buffer-resolve + visibility kernel: algorithmic
           bytes 12 P + 4 S^2 + scene per launch over its event-timed
           duration, against the measured HBM copy bandwidth
@@ -22,6 +26,13 @@ one shadowed frame: light-view depth map, G-buffer, visibility.
           the host cores for a bounded sample of whole frames
 
 Extra legs in the same line (not the headline):
+  batched_surrogate_1080p  the metric's own comparison: 16 pcss_1080p frames
+              of different seeded sphere fields as one autotuned CUDA graph
+              (exact PCSS) and through the learned surrogate (one U-Net
+              forward over the 16 frames, exact fallback where its error
+              head exceeds 0.02), each as frames/s and as a ratio over the
+              plain single-frame pass, with the surrogate's mean absolute
+              error against the exact frames
   batched     the 256-scene 1280 x 720 workload (1-8 spot lights per
               scene, maps 512^2-4096^2, 5 x 5 PCF) replayed as one CUDA
               graph after autotuning, against the same light-frames
@@ -56,8 +67,12 @@ Extra legs in the same line (not the headline):
               frames, then its 1080p frame time, its error against the
               exact PCSS frame, and the tensor roofline of the U-Net
 
+The last key, "summary", repeats every leg's headline numbers in a few
+hundred bytes.
+
 --impl reference times that CPU implementation alone (the reference's own
-passes need OpenGL, which this machine does not have).  For N > 1 every rank
+passes need OpenGL, which this machine does not have), on inputs read from
+oracle/pcss_1080p_inputs.npz so that it loads no product code.  For N > 1 every rank
 renders its own frames (replicas; no collective on the data path) and the
 slowest rank's time is used.
 """
@@ -117,12 +132,12 @@ def dist_env():
     return rank, world, local
 
 
-def workload_config(w, tris):
+def workload_config(S, W, H, tris):
     return {
         "workload": "pcss_1080p",
         "triangles": int(tris),
-        "light_map": f"{w.map_params.width}x{w.map_params.height} fp32, polygon offset (4, 20)",
-        "camera": f"{w.camera.width}x{w.camera.height}",
+        "light_map": f"{S}x{S} fp32, polygon offset (4, 20)",
+        "camera": f"{W}x{H}",
         "technique": "PCSS, 16 Poisson blocker taps + 32 filter taps, light radius 0.25",
         "step": "gi_render_frame: light map + G-buffer + visibility (one shadowed frame)",
         "l2": "flushed (256 MiB write) before each timed step, outside the step's events",
@@ -192,58 +207,47 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU oracle frames (cpu_baseline and the reference arm)
 # ---------------------------------------------------------------------------
-def oracle_frame(arrays, fr, w, tab, threads):
+def oracle_frame(inp, threads):
+    """One whole pcss_1080p frame of the CPU restatement (light map, G-buffer, visibility)."""
     import oracle
 
-    p, n, i = arrays
-    mp = w.map_params
-    S, W, H = mp.width, w.camera.width, w.camera.height
-    d = oracle.shadow_map(p, i, fr.light_mvp, S, S, mp.bias_mode, mp.constant_bias, mp.offset_factor,
-                          mp.offset_units, threads=threads)
-    pos, nrm = oracle.gbuffer(p, n, i, fr.camera_mvp, W, H, threads=threads)
-    return oracle.visibility(w.params.to_c(fr), d, S, S, pos, nrm, W, H, tab, threads=threads)
+    d = oracle.shadow_map(inp.points, inp.indices, inp.light_mvp, inp.S, inp.S, inp.bias_mode, inp.constant_bias,
+                          inp.offset_factor, inp.offset_units, threads=threads)
+    pos, nrm = oracle.gbuffer(inp.points, inp.normals, inp.indices, inp.camera_mvp, inp.W, inp.H, threads=threads)
+    return oracle.visibility(inp.vis_params, d, inp.S, inp.S, pos, nrm, inp.W, inp.H, inp.poisson, threads=threads)
 
 
 def cpu_frames(min_seconds: float, max_frames: int, setup):
-    arrays, fr, w, tab, threads = setup
+    inp, threads = setup
     times = []
     t_all = time.perf_counter()
     while len(times) < max_frames and (time.perf_counter() - t_all) < min_seconds:
         t0 = time.perf_counter()
-        oracle_frame(arrays, fr, w, tab, threads)
+        oracle_frame(inp, threads)
         times.append(time.perf_counter() - t0)
     return times
 
 
 def cpu_setup():
-    import numpy as np
-
+    """The CPU baseline's inputs, read from oracle/pcss_1080p_inputs.npz: no product code is loaded."""
+    from oracle.bench_inputs import Inputs
     from oracle.build_oracle import build_oracle
-    import globalillumination_gb300 as gi
-    from globalillumination_gb300 import scenes
 
     build_oracle()
-    w = scenes.pcss_1080p()
-    fr = gi.frame_setup(w.light, w.camera)
-    tab = np.concatenate([gi.poisson_table(w.params.poisson_blocker_taps).reshape(-1),
-                          gi.poisson_table(w.params.poisson_filter_taps).reshape(-1)])
-    threads = os.cpu_count() or 1
-    return (w.scene.arrays(), fr, w, tab, threads)
+    return Inputs(), os.cpu_count() or 1
 
 
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    setup = cpu_setup()
-    w = setup[2]
-    threads = setup[4]
+    inp, threads = cpu_setup()
     for _ in range(args.warmup):
-        oracle_frame(*setup[:4], threads)
+        oracle_frame(inp, threads)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        oracle_frame(*setup[:4], threads)
+        oracle_frame(inp, threads)
         times.append(time.perf_counter() - t0)
     total = sum(times)
     value = len(times) / total
@@ -251,11 +255,12 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic", "config": workload_config(w, setup[0][2].shape[0]),
+        "data": "synthetic", "config": workload_config(inp.S, inp.W, inp.H, inp.indices.shape[0]),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{len(times)} whole frames (light map, G-buffer, PCSS visibility) of "
-                                   "the CPU restatement of the reference's passes, OpenMP on all host threads; "
-                                   "the reference's own passes run only through OpenGL, unavailable on this box"},
+                                   "the CPU restatement of the reference's passes, OpenMP on all host threads, "
+                                   "inputs from oracle/pcss_1080p_inputs.npz; the reference's own passes run "
+                                   "only through OpenGL, unavailable on this box"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -416,6 +421,107 @@ def run_surrogate(args, ctx, stream, local, w, fr, bufs):
                      "flops_per_frame": flops, "ms": t_net},
     }
     return summary, net
+
+
+def run_metric_1080p(args, ctx, stream, local, net, plain_fps):
+    """The metric's own comparison at 1080p on the 16 frames of
+    pcss_1080p_batch (pcss_1080p with 16 different seeded sphere fields):
+      batched    the 16 frames as one autotuned CUDA graph (exact PCSS)
+      surrogate  the same frames through the learned surrogate: features
+                 per frame, one U-Net forward over all 16 frames (N = 16),
+                 finish with exact PCSS fallback where the predicted error
+                 exceeds 0.02
+    each as frames/s and as a ratio over the plain single-frame pass (the
+    headline value), with the surrogate's mean absolute visibility error
+    against the batched exact PCSS frames."""
+    import torch
+
+    import globalillumination_gb300 as gi
+    from globalillumination_gb300 import scenes
+    from globalillumination_gb300 import surrogate as sg
+
+    frames = scenes.pcss_1080p_batch(16)
+    F = len(frames)
+    W, H = frames[0].camera.width, frames[0].camera.height
+    S = frames[0].maps[0].width
+    for f in frames:
+        f.scene.upload(ctx, stream)
+    exact = torch.empty((F, H, W), device="cuda")
+    b = gi.Batch(local)
+    for k, f in enumerate(frames):
+        b.add_frame(f.scene, f.camera, f.lights, f.maps, f.params, exact[k:k + 1])
+    tune = b.autotune(stream, repeats=2)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(3):
+        b.run(stream)
+    torch.cuda.synchronize()
+    R = 10
+    ev0.record(stream)
+    for _ in range(R):
+        b.run(stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    batch_ms = ev0.elapsed_time(ev1) / R
+    info = b.info()
+    b.close()
+    # surrogate: one context per frame (finish reads the keys its features call left there)
+    ctxs = [gi.Context(local) for _ in range(F)]
+    for c, f in zip(ctxs, frames):
+        f.scene.upload(c, stream)
+    mats = [gi.frame_setup(f.lights[0], f.camera) for f in frames]
+    depth = torch.empty((F, S * S), device="cuda")
+    feat = torch.empty((F, H, W, sg.FEATURES), dtype=torch.bfloat16, device="cuda")
+    head = torch.empty((F, H, W, 2), device="cuda")
+    vis = torch.empty((F, H * W), device="cuda")
+    fallback = torch.zeros(1, dtype=torch.int32, device="cuda")
+
+    def surrogate_batch():
+        for k, f in enumerate(frames):
+            sg.features(ctxs[k], f.scene, mats[k], f.maps[0], f.params, W, H, depth[k], feat[k:k + 1], stream)
+        net.forward_fused(feat, head)
+        for k, f in enumerate(frames):
+            sg.finish(ctxs[k], f.scene, mats[k], f.maps[0], f.params, W, H, depth[k], head[k:k + 1], feat[k:k + 1],
+                      vis[k], fallback, sg.ERR_THRESHOLD, stream)
+
+    for _ in range(2):
+        surrogate_batch()
+    torch.cuda.synchronize()
+    fallback.zero_()
+    surrogate_batch()
+    torch.cuda.synchronize()
+    fb_frac = int(fallback.item()) / (F * W * H)
+    err = (vis.reshape(F, H, W) - exact).abs()
+    geo = feat[..., 3].float() > 0
+    mae_all = float(err.mean())
+    mae_geo = float(err[geo].mean())
+    Rs = 3
+    ev0.record(stream)
+    for _ in range(Rs):
+        surrogate_batch()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    sur_ms = ev0.elapsed_time(ev1) / Rs
+    if net.kernel_error():
+        raise RuntimeError("a tcgen05 kernel reported a timed-out wait")
+    for c in ctxs:
+        c.close()
+    batched_fps = F / (batch_ms / 1000.0)
+    sur_fps = F / (sur_ms / 1000.0)
+    return {
+        "workload": "pcss_1080p_batch: 16 pcss_1080p frames (different seeded sphere fields), 1920x1080, "
+                    "2048^2 maps, PCSS 16+32 Poisson taps",
+        "plain_single_frame_fps": plain_fps,
+        "batched_fps": batched_fps, "batched_ratio_over_plain": batched_fps / plain_fps,
+        "batched_ms_per_batch": batch_ms,
+        "batched_tuning": {k: tune[k] for k in ("tiny_px", "coop_px", "streams")},
+        "batched_kernel_launches": info["kernel_launches"],
+        "batched_surrogate_fps": sur_fps, "batched_surrogate_ratio_over_plain": sur_fps / plain_fps,
+        "batched_surrogate_ms_per_batch": sur_ms,
+        "surrogate_mae_vs_plain_pcss": mae_all, "surrogate_mae_geometry_pixels": mae_geo,
+        "surrogate_fallback_fraction": fb_frac,
+        "target": ">= 5x plain at <= 1% MAE",
+        "target_met": bool(max(batched_fps, sur_fps) / plain_fps >= 5.0 and mae_all <= 0.01),
+    }
 
 
 def run_heavy(args, ctx, stream, local, net=None):
@@ -1064,6 +1170,9 @@ def run_ours(args):
     edt_leg = None
     if not args.no_edt and rank == 0:
         edt_leg = run_edt(args, ctx, stream, local, flush)
+    metric_leg = None
+    if not args.no_surrogate and not args.no_batched and rank == 0:
+        metric_leg = run_metric_1080p(args, ctx, stream, local, net, value / world)
     heavy = None
     if not args.no_heavy and rank == 0:
         heavy = run_heavy(args, ctx, stream, local, net)
@@ -1084,7 +1193,7 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
             "warmup": args.warmup, "ms_per_step": total_ms / K, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": workload_config(w, tris),
+            "config": workload_config(S, W, H, tris),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),
@@ -1098,6 +1207,8 @@ def run_ours(args):
             "clocks": clk,
             "soft_pixel_fraction": frac_soft,
         }
+        if metric_leg is not None:
+            line["batched_surrogate_1080p"] = metric_leg
         if batched is not None:
             line["batched"] = batched
         if surrogate is not None:
@@ -1118,15 +1229,69 @@ def run_ours(args):
             setup = cpu_setup()
             times = cpu_frames(CPU_SAMPLE_SECONDS, 50, setup)
             line["cpu_baseline"] = {
-                "value": len(times) / sum(times), "unit": UNIT, "cores": setup[4], "kind": "port",
+                "value": len(times) / sum(times), "unit": UNIT, "cores": setup[1], "kind": "port",
                 "sample": f"{len(times)} whole pcss_1080p frames (light map, G-buffer, visibility) of the CPU "
                           "oracle, OpenMP on all host threads"}
+        line["summary"] = compact_summary(line)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
     ctx.close()
     return 0
+
+
+def _r(x, digits=4):
+    """Rounds to `digits` significant digits (None stays None)."""
+    if x is None:
+        return None
+    if isinstance(x, bool) or not isinstance(x, (int, float)):
+        return x
+    return float(f"{x:.{digits}g}")
+
+
+def compact_summary(line: dict) -> dict:
+    """The headline numbers of every leg in a few hundred bytes.  It is the
+    last key of the JSON line, so a consumer that keeps only the line's tail
+    still has every leg's result; the full legs precede it."""
+    def g(d, *keys):
+        for k in keys:
+            d = d.get(k) if isinstance(d, dict) else None
+        return _r(d)
+
+    out = {"frames_per_s": _r(line["value"]), "e2e_frames_per_s": _r(line["e2e"]["value"]),
+           "roofline_frac": _r(line["roofline"]["frac"], 3)}
+    m = line.get("batched_surrogate_1080p")
+    if m:
+        out["1080p_batched_x"] = _r(m["batched_ratio_over_plain"], 3)
+        out["1080p_batched_surrogate_x"] = _r(m["batched_surrogate_ratio_over_plain"], 3)
+        out["1080p_surrogate_mae"] = _r(m["surrogate_mae_vs_plain_pcss"], 3)
+        out["target_5x_met"] = m["target_met"]
+    b = line.get("batched")
+    if b:
+        out["720p_batch_light_frames_per_s"] = _r(b["light_frames_per_s"])
+        out["720p_single_calls_light_frames_per_s"] = _r(b["single_frame_calls_light_frames_per_s"])
+    sg = line.get("surrogate")
+    if sg:
+        out["surrogate_frame_ms"] = _r(sg["ms_per_frame"], 3)
+        out["unet_tflops_frac"] = _r(sg["roofline"]["frac"], 3)
+        out["surrogate_mae_fallback"] = g(sg, "accuracy_vs_plain_pcss", "with_fallback", "mae_all_pixels")
+    h = line.get("heavy")
+    if h:
+        out["heavy_pcss_ms"] = g(h, "pcss_poisson", "ms_per_frame_8_lights")
+        out["heavy_rbsm_ms"] = g(h, "rbsm_smsr", "ms_per_frame_8_lights")
+        out["heavy_volumes_ms"] = g(h, "shadow_volumes", "ms_per_frame_8_lights")
+    a = line.get("area_light_ground_truth")
+    if a:
+        out["area_289_maps_ms"] = _r(a["ms"], 3)
+        out["pcss_mae_vs_area_truth"] = _r(a["pcss_poisson_mae_all_pixels"], 3)
+    e = line.get("edt_soft_shadows")
+    if e:
+        out["edt_ms"] = _r(e["edt_ms"], 3)
+    cb = line.get("cpu_baseline")
+    if cb:
+        out["cpu_baseline_frames_per_s"] = _r(cb["value"])
+    return out
 
 
 def main():

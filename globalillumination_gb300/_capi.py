@@ -227,6 +227,9 @@ _PROTOS = {
     "gi_batch_autotune": (C.c_int, [_VP, _VP, C.c_int, C.POINTER(BatchTuning)]),
     "gi_batch_info": (C.c_int, [_VP, C.POINTER(BatchTuning)]),
     # gi_surrogate.h
+    "gi_tc_set_wait_limit": (C.c_int, [C.c_uint32]),
+    "gi_tc_wait_limit": (C.c_uint32, []),
+    "gi_tc_set_test_withhold": (C.c_int, [C.c_int]),
     "gi_conv2d_bf16": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP, C.c_int, C.c_int, C.c_int, _VP,
                                  _VP, C.c_int, C.c_int, _VP, _VP, _VP]),
     "gi_conv2d_wgrad_scratch_floats": (C.c_size_t, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),

@@ -18,8 +18,11 @@
 // pixels), applies bias / ReLU / ReLU-derivative mask and stores BF16
 // (and optionally FP32).
 //
-// Every wait on an mbarrier is bounded; on timeout the kernel sets bit 0 of
-// the caller's error word, still frees its tensor memory and returns.
+// Every wait on an mbarrier is bounded (gi_tc_set_wait_limit, default 2^20
+// polls).  When a wait runs out, the kernel stops issuing loads and MMAs,
+// skips its tensor-memory reads, waits (again bounded) for the copies and
+// MMAs it already issued, frees its tensor memory, sets bit 0 of the
+// caller's error word and returns.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -42,7 +45,7 @@ constexpr int kBKB = 4;         // K-blocks (8 elements) per stage
 constexpr int kCore = 128;      // bytes per core matrix (8 rows x 16 B)
 constexpr int kSBO = kBKB * kCore;
 constexpr int kStageA = 16 * kSBO;  // 128 rows
-constexpr unsigned kSpinLimit = 1u << 20;
+constexpr unsigned kSpinLimit = 1u << 20;  // default polls per mbarrier wait
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -69,9 +72,9 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
 
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned limit) {
     const uint32_t a = smem_u32(bar);
-    for (unsigned it = 0; it < kSpinLimit; ++it) {
+    for (unsigned it = 0; it < limit; ++it) {
         uint32_t ok;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -161,6 +164,8 @@ struct ConvArgs {
     int y_c, y_off;
     float* y32;
     uint32_t* err;
+    unsigned spin;   // polls per mbarrier wait
+    int withhold;    // test switch: the first asynchronous stage is not issued
     long long P;
     // optional fused 1x1 head on the activated BF16-rounded output:
     // hout[p][j] = hb[j] + sum_c hw[j][c] * bf16(v[c]), j < 2
@@ -229,12 +234,18 @@ __global__ void __launch_bounds__(kThreads) k_conv_fwd(ConvArgs a) {
     }
     // Iteration i: wait for chunk i's copies, issue its MMAs, then refill
     // the stage chunk i - 1 used (its MMAs overlap with those just issued).
+    // A wait that runs out stops the loop for the whole CTA at the next
+    // iteration; `issued` is the last chunk whose MMAs were committed.
+    int issued = -1;
     for (int i = 0; i < nk; ++i) {
         const int s = i % kNS;
         cp_async_wait<kNS - 2>();
         fence_proxy_async();
-        __syncthreads();
-        if (tid == 0) {
+        if (__syncthreads_or(!ok)) {
+            ok = false;
+            break;
+        }
+        if (tid == 0 && !a.withhold) {
             fence_after();
             const uint8_t* sa = smem + s * stage_bytes;
             const uint8_t* sb = sa + kStageA;
@@ -246,21 +257,31 @@ __global__ void __launch_bounds__(kThreads) k_conv_fwd(ConvArgs a) {
             }
             mma_commit(&bars[s]);
         }
+        if (!a.withhold) issued = i;
         const int j = i + kNS - 1;
         if (j < nk) {
             const int sj = j % kNS;
-            if (i >= 1) ok &= mbar_wait(&bars[sj], (unsigned)((i - 1) / kNS) & 1u);
-            load_stage(j, sj);
+            if (i >= 1) ok = mbar_wait(&bars[sj], (unsigned)((i - 1) / kNS) & 1u, a.spin);
+            if (ok) load_stage(j, sj);
         }
         cp_async_commit();
     }
-    const int last = nk - 1;
-    ok &= mbar_wait(&bars[last % kNS], (unsigned)(last / kNS) & 1u);
+    cp_async_wait<0>();
+    if (ok && nk > 0) {
+        const int last = nk - 1;
+        ok = mbar_wait(&bars[last % kNS], (unsigned)(last / kNS) & 1u, a.spin);
+    } else if (issued >= 0) {
+        // Stopped early: the committed MMAs (every chunk up to `issued`;
+        // those before issued - 1 were already waited for) must land before
+        // the tensor memory is freed.  The wait is bounded too.
+        mbar_wait(&bars[issued % kNS], (unsigned)(issued / kNS) & 1u, a.spin);
+    }
+    const bool all_ok = __syncthreads_and(ok);
     fence_after();
 
     const long long p = tile0 + warp * 32 + lane;
     const bool live = p < a.P;
-    for (int c0 = 0; c0 < N; c0 += 16) {
+    for (int c0 = 0; all_ok && c0 < N; c0 += 16) {
         float v[16];
         tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
         if (!live) continue;
@@ -298,6 +319,7 @@ __global__ void __launch_bounds__(kThreads) k_conv_fwd(ConvArgs a) {
             yp[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
         }
     }
+    ok = all_ok;
     fence_before();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, ncols);
@@ -394,6 +416,11 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
     __shared__ uint64_t full[4], empty[4], acc_full[2], acc_empty[2];
     __shared__ uint32_t tmem_slot;
+    // Stop flag (a wait ran out somewhere in the CTA) and the progress the
+    // drain after a stop needs: stages loaded by the producer, stages the
+    // MMA warp took (waited full), stages whose MMAs it committed, and
+    // commits of `empty` the producer saw land.
+    __shared__ int s_fail, s_loaded, s_taken, s_committed, s_freed;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int N = a.cout;
     const int nk = a.cin / 16;
@@ -411,13 +438,15 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
             mbar_init(&acc_full[b], 1);
             mbar_init(&acc_empty[b], 128);
         }
+        s_fail = 0;
+        s_loaded = s_taken = s_committed = s_freed = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     fence_before();
     __syncthreads();
     fence_after();
     const uint32_t tmem = tmem_slot;
-    bool ok = true;
+    volatile int* fail = &s_fail;
     const int ntiles_mine = tiles > (int)blockIdx.x ? (tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 
     auto tile_coords = [&](int t, int& x0, int& y0, int& img) {
@@ -427,18 +456,40 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
         x0 = bx * 128;
         y0 = by * R;
     };
+    // A warp-uniform bounded wait: false (and the CTA's stop flag set) when
+    // any lane's wait ran out or another warp has stopped the CTA.
+    auto warp_wait = [&](uint64_t* bar, unsigned parity) -> bool {
+        if (__shfl_sync(0xffffffffu, *fail, 0)) return false;
+        const bool w = mbar_wait(bar, parity, a.spin);
+        if (__any_sync(0xffffffffu, !w)) {
+            if (lane == 0) *fail = 1;
+            return false;
+        }
+        return true;
+    };
 
     if (warp == 0) {
         // TMA producer
         const uint32_t stage_tx = (uint32_t)(2 * G.a_box + G.b_bytes);
-        int g = 0;
-        for (int it = 0; it < ntiles_mine; ++it) {
+        int g = 0, freed = 0;
+        bool run = true;
+        for (int it = 0; run && it < ntiles_mine; ++it) {
             int x0, y0, img;
             tile_coords((int)blockIdx.x + it * (int)gridDim.x, x0, y0, img);
             for (int c = 0; c < nk; ++c, ++g) {
                 const int s = g % NS;
-                if (g >= NS) ok &= mbar_wait(&empty[s], (unsigned)((g / NS) - 1) & 1u);
-                if (lane == 0) {
+                if (g >= NS) {
+                    if (!warp_wait(&empty[s], (unsigned)((g / NS) - 1) & 1u)) {
+                        run = false;
+                        break;
+                    }
+                    freed = g - NS + 1;
+                }
+                if (__shfl_sync(0xffffffffu, *fail, 0)) {
+                    run = false;
+                    break;
+                }
+                if (lane == 0 && !a.withhold) {
                     uint8_t* sa = smem + s * G.stage_bytes;
                     mbar_expect_tx(&full[s], stage_tx);
                     tma_load_4d(sa, &xmap, c * 16, x0 - 1, y0 - 1, img, &full[s]);
@@ -448,18 +499,26 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
                 __syncwarp();
             }
         }
+        if (lane == 0) {
+            s_loaded = a.withhold ? 0 : g;
+            s_freed = freed;
+        }
     } else if (warp == 1) {
         // MMA issuer
         const uint32_t idesc = idesc_bf16(128, N);
-        int g = 0;
-        for (int it = 0; it < ntiles_mine; ++it) {
+        int g = 0, committed = 0;
+        bool run = true;
+        for (int it = 0; run && it < ntiles_mine; ++it) {
             const int b = it & 1;
-            if (it >= 2) ok &= mbar_wait(&acc_empty[b], (unsigned)((it >> 1) - 1) & 1u);
+            if (it >= 2 && !warp_wait(&acc_empty[b], (unsigned)((it >> 1) - 1) & 1u)) break;
             fence_after();
             const uint32_t acc = tmem + (uint32_t)b * set_cols;
             for (int c = 0; c < nk; ++c, ++g) {
                 const int s = g % NS;
-                ok &= mbar_wait(&full[s], (unsigned)(g / NS) & 1u);
+                if (!warp_wait(&full[s], (unsigned)(g / NS) & 1u)) {
+                    run = false;
+                    break;
+                }
                 if (lane == 0) {
                     fence_after();
                     const uint8_t* sa = smem + s * G.stage_bytes;
@@ -476,8 +535,13 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
                     mma_commit(&empty[s]);
                     if (c == nk - 1) mma_commit(&acc_full[b]);
                 }
+                committed = g + 1;
                 __syncwarp();
             }
+        }
+        if (lane == 0) {
+            s_taken = committed;  // every stage taken was also committed
+            s_committed = committed;
         }
     } else {
         // epilogue: warps 2..5 -> TMEM lane quarter warp % 4
@@ -486,7 +550,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
             const int b = it & 1;
             int x0, y0, img;
             tile_coords((int)blockIdx.x + it * (int)gridDim.x, x0, y0, img);
-            ok &= mbar_wait(&acc_full[b], (unsigned)(it >> 1) & 1u);
+            if (!warp_wait(&acc_full[b], (unsigned)(it >> 1) & 1u)) break;
             fence_after();
             const uint32_t acc = tmem + (uint32_t)b * set_cols;
             const int xo = x0 + q * 32 + lane;
@@ -548,10 +612,25 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
             asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[b])) : "memory");
         }
     }
+    // Every role has left its loop (each of its waits is bounded).  After a
+    // stop, drain what is still in flight before the tensor memory and the
+    // shared memory go away: the TMA loads the MMA warp never took (each in
+    // its own stage, waited phase by phase), and the committed MMAs whose
+    // `empty` commits nobody saw land (in commit order, so every parity
+    // wait names the barrier's next phase).  These waits are bounded too.
+    __syncthreads();
+    if (*fail && lane == 0) {
+        if (warp == 0) {
+            for (int g = s_taken; g < s_loaded; ++g) mbar_wait(&full[g % NS], (unsigned)(g / NS) & 1u, a.spin);
+        } else if (warp == 1) {
+            for (int g = s_freed; g < s_committed; ++g)
+                mbar_wait(&empty[g % NS], (unsigned)(g / NS) & 1u, a.spin);
+        }
+    }
     fence_before();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, tcols);
-    if (!ok && a.err) atomicOr(a.err, 1u);
+    if (*fail && tid == 0 && a.err) atomicOr(a.err, 1u);
 }
 
 // ---- weight gradient ---------------------------------------------------------
@@ -566,6 +645,8 @@ struct WgradArgs {
     long long P, px_per_split;
     float* scratch;
     uint32_t* err;
+    unsigned spin;
+    int withhold;
 };
 
 __device__ __forceinline__ void transpose8(const uint4 (&in)[8], uint4 (&out)[8]) {
@@ -660,11 +741,17 @@ __global__ void __launch_bounds__(kThreads) k_conv_wgrad(WgradArgs a) {
     const uint32_t idesc = idesc_bf16(128, N);
     for (int s = 0; s < kNS - 1; ++s)
         if (s < nk) load_stage(s, s);
+    // As in k_conv_fwd: a wait that runs out stops the CTA at the next
+    // iteration; `issued` is the last chunk whose MMAs were committed.
+    int issued = -1;
     for (int i = 0; i < nk; ++i) {
         const int s = i % kNS;
         fence_proxy_async();
-        __syncthreads();
-        if (tid == 0) {
+        if (__syncthreads_or(!ok)) {
+            ok = false;
+            break;
+        }
+        if (tid == 0 && !a.withhold) {
             fence_after();
             const uint8_t* sa = smem + s * stage_bytes;
             const uint8_t* sb = sa + kStageA;
@@ -676,20 +763,24 @@ __global__ void __launch_bounds__(kThreads) k_conv_wgrad(WgradArgs a) {
             }
             mma_commit(&bars[s]);
         }
+        if (!a.withhold) issued = i;
         const int j = i + kNS - 1;
         if (j < nk) {
             const int sj = j % kNS;
-            if (i >= 1) ok &= mbar_wait(&bars[sj], (unsigned)((i - 1) / kNS) & 1u);
-            load_stage(j, sj);
+            if (i >= 1) ok = mbar_wait(&bars[sj], (unsigned)((i - 1) / kNS) & 1u, a.spin);
+            if (ok) load_stage(j, sj);
         }
     }
-    if (nk > 0) {
+    if (ok && nk > 0) {
         const int last = nk - 1;
-        ok &= mbar_wait(&bars[last % kNS], (unsigned)(last / kNS) & 1u);
+        ok = mbar_wait(&bars[last % kNS], (unsigned)(last / kNS) & 1u, a.spin);
+    } else if (!ok && issued >= 0) {
+        mbar_wait(&bars[issued % kNS], (unsigned)(issued / kNS) & 1u, a.spin);  // let committed MMAs land
     }
+    const bool all_ok = __syncthreads_and(ok);
     fence_after();
     const long long row = ((long long)blockIdx.y * a.m_tiles + mt) * 128 + warp * 32 + lane;
-    for (int c0 = 0; c0 < N; c0 += 16) {
+    for (int c0 = 0; all_ok && c0 < N; c0 += 16) {
         float v[16];
         tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
         if (nk == 0) {
@@ -700,6 +791,7 @@ __global__ void __launch_bounds__(kThreads) k_conv_wgrad(WgradArgs a) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
     }
+    ok = all_ok;
     fence_before();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, ncols);
@@ -966,6 +1058,26 @@ using gi::fail_cuda;
 namespace tc = gi::tc;
 
 namespace {
+// Polls per mbarrier wait and the bounded-wait test switch, read at every
+// launch (gi_tc_set_wait_limit, gi_tc_set_test_withhold).
+std::atomic<unsigned> g_wait_limit{tc::kSpinLimit};
+std::atomic<int> g_withhold{0};
+}  // namespace
+
+extern "C" gi_status gi_tc_set_wait_limit(uint32_t polls) {
+    if (polls == 0) return gi::fail(GI_ERR_INVALID_ARG, "gi_tc_set_wait_limit: polls must be > 0");
+    g_wait_limit.store(polls);
+    return GI_OK;
+}
+
+extern "C" uint32_t gi_tc_wait_limit(void) { return g_wait_limit.load(); }
+
+extern "C" gi_status gi_tc_set_test_withhold(int enable) {
+    g_withhold.store(enable ? 1 : 0);
+    return GI_OK;
+}
+
+namespace {
 PFN_cuTensorMapEncodeTiled_v12000 g_encode_tiled = nullptr;
 
 gi_status tensor_map_fn() {
@@ -1059,6 +1171,8 @@ extern "C" gi_status gi_conv2d_bf16(const gi_bf16* x, int n, int h, int w, int c
     a.y_off = y ? y_off : 0;
     a.y32 = y32;
     a.err = err;
+    a.spin = g_wait_limit.load();
+    a.withhold = g_withhold.load();
     a.P = (long long)n * h * w;
     a.hw = nullptr;
     a.hb = nullptr;
@@ -1128,6 +1242,8 @@ extern "C" gi_status gi_conv2d_wgrad_bf16(const gi_bf16* x, const gi_bf16* dy, i
     a.px_per_split = pl.px_per_split;
     a.scratch = scratch;
     a.err = err;
+    a.spin = g_wait_limit.load();
+    a.withhold = g_withhold.load();
     const int smem = tc::kNS * (tc::kStageA + (cout / 8) * tc::kSBO);
     static std::atomic<unsigned long long> attr{0};
     smem_opt_in(tc::k_conv_wgrad, 4 * (8192 + 16384), attr);
@@ -1279,6 +1395,8 @@ extern "C" gi_status gi_conv2d_head_bf16(const gi_bf16* x, int n, int h, int w, 
     a.act = act;
     a.y_c = cout;
     a.err = err;
+    a.spin = g_wait_limit.load();
+    a.withhold = g_withhold.load();
     a.P = (long long)n * h * w;
     a.hw = head_w;
     a.hb = head_b;

@@ -24,6 +24,10 @@ visibility parameters.
                     the origin, each with a map side drawn from {512, 1024,
                     2048, 4096}; camera 1280 x 720 on a circle of radius 15,
                     height 8; 5 x 5 PCF, polygon offset (4, 20).
+  pcss_1080p_batch  16 pcss_1080p frames of different seeded sphere fields
+                    (seed base + 1 + 16 k), same light, camera and PCSS:
+                    the frames the batched and surrogate paths are measured
+                    on against the plain single-frame pass.
   heavy_2160p       1024 x 1024 UV-grid sphere (r 2) displaced by Perlin
                     noise of amplitude 0.3 + ground; 8 spot lights, 4096^2
                     maps, camera 3840 x 2160.
@@ -142,4 +146,21 @@ def batched_720p(scenes: int = 256, width: int = 1280, height: int = 720, tri_mi
         p = ShadowParams.defaults(api.GI_TECH_PCF)
         p.kernel_order = 5
         out.append(BatchFrame(s, camera, lights, maps, p, int(s.info().num_triangles)))
+    return out
+
+
+def pcss_1080p_batch(frames: int = 16, width: int = 1920, height: int = 1080, map_size: int = 2048,
+                     spheres: int = 64) -> list[BatchFrame]:
+    """pcss_1080p frames of `frames` different seeded sphere fields (one light each)."""
+    out = []
+    for k in range(frames):
+        w = pcss_1080p(width, height, map_size, spheres)
+        if k:
+            s = Scene()
+            s.ground(10.0, 0.0)
+            s.icosphere_field(spheres, 3, (-8.0, 0.2, -8.0), (8.0, 3.0, 8.0), 0.2, 1.0, SEED_BASE + 1 + 16 * k)
+            w.scene.close()
+            w.scene = s
+        out.append(BatchFrame(w.scene, w.camera, [w.light], [w.map_params], w.params,
+                              int(w.scene.info().num_triangles)))
     return out

@@ -117,6 +117,20 @@ def conv2d_wgrad(x: torch.Tensor, dy: torch.Tensor, cout: int, ksize: int, dw: t
     return scratch
 
 
+def set_wait_limit(polls: int) -> None:
+    """Polls per mbarrier wait in the tcgen05 kernels (default 2^20)."""
+    check(_lib().gi_tc_set_wait_limit(int(polls)), "gi_tc_set_wait_limit")
+
+
+def wait_limit() -> int:
+    return int(_lib().gi_tc_wait_limit())
+
+
+def set_test_withhold(enable: bool) -> None:
+    """Test switch: the kernels withhold their first asynchronous stage, so a wait runs out."""
+    check(_lib().gi_tc_set_test_withhold(1 if enable else 0), "gi_tc_set_test_withhold")
+
+
 def maxpool2(x: torch.Tensor) -> torch.Tensor:
     n, h, w, c = x.shape
     y = torch.empty((n, h // 2, w // 2, c), dtype=x.dtype, device=x.device)

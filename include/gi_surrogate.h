@@ -140,6 +140,21 @@ gi_status gi_adam_f32(float* p, const float* g, float* m, float* v, size_t n, fl
                       float beta1, float beta2, float eps, int step, float grad_scale,
                       void* stream);
 
+/* Bounded waits.  Every mbarrier wait of the tcgen05 convolution kernels
+ * polls at most `polls` times (default 1,048,576, read at each launch).
+ * When a wait runs out, the kernel stops issuing loads and MMAs, skips its
+ * tensor-memory reads, waits (bounded) for what it had already issued,
+ * frees its tensor memory, sets bit 0 of `err` and returns; the outputs of
+ * that call are undefined, the context stays usable. */
+gi_status gi_tc_set_wait_limit(uint32_t polls);
+uint32_t gi_tc_wait_limit(void);
+/* Test switch for the bounded-wait path (process-wide, off by default):
+ * while enabled, each convolution kernel withholds its first asynchronous
+ * stage (the TMA loads of the slab kernel, the MMAs of the others), so the
+ * wait on it runs out with nothing in flight.  Never enable it in
+ * production. */
+gi_status gi_tc_set_test_withhold(int enable);
+
 #ifdef __cplusplus
 }
 #endif

@@ -36,3 +36,16 @@ def test_reference_arm_line():
 
 def test_reference_arm_other_ranks_print_nothing():
     assert run_bench({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"}) == []
+
+
+def test_reference_arm_loads_no_product_code():
+    """The timed CPU restatement reads its inputs from oracle/pcss_1080p_inputs.npz:
+    libgishadow.so is never mapped into the reference arm's process."""
+    code = ("import sys, types, bench; "
+            "a = types.SimpleNamespace(gpus=1, steps=1, warmup=0); "
+            "bench.run_reference(a); "
+            "maps = open('/proc/self/maps').read(); "
+            "sys.exit(3 if 'libgishadow' in maps else 0)")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600,
+                       env=dict(os.environ, RANK="0", WORLD_SIZE="1"))
+    assert r.returncode == 0, (r.returncode, r.stderr[-2000:])
