@@ -162,6 +162,7 @@ class BatchTuning(C.Structure):
 _VP = C.c_void_p
 _PROTOS = {
     "gi_last_error_string": (C.c_char_p, []),
+    "gi_debug_fail_allocation": (C.c_int, [C.c_int]),
     "gi_version": (C.c_char_p, []),
     "gi_context_create": (C.c_int, [C.c_int, C.POINTER(_VP)]),
     "gi_context_destroy": (None, [_VP]),
@@ -205,6 +206,7 @@ _PROTOS = {
     "gi_shadow_volume_counts": (C.c_int, [_VP, _VP, F3, C.c_float, F16, C.c_int, C.c_int, C.c_int,
                                           _VP, _VP, _VP]),
     "gi_shadow_volume_geometry": (C.c_int, [_VP, _VP, F3, C.c_float, _VP, _VP]),
+    "gi_light_map_minmax": (C.c_int, [_VP, _VP, C.c_int, C.c_int, _VP, _VP]),
     "gi_phong_shade": (C.c_int, [_VP, C.POINTER(VisParams), _VP, _VP, _VP, _VP, C.c_int, C.c_int, _VP, _VP]),
     "gi_pba_voronoi": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP]),
     "gi_edt_soft_shadows": (C.c_int, [_VP, _VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float,

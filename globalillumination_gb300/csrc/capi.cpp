@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <atomic>
 #include <cstring>
 #include <vector>
 #include <string>
@@ -43,8 +44,28 @@ gi_status fail_cuda(int err, const char* what) {
     return GI_ERR_CUDA;
 }
 
+namespace {
+// countdown of allocation points until an injected failure (-1: off)
+std::atomic<long long> g_alloc_countdown{-1};
+}  // namespace
+
+bool alloc_fail_due() {
+    long long c = g_alloc_countdown.load();
+    while (c >= 0) {
+        if (g_alloc_countdown.compare_exchange_weak(c, c - 1)) return c == 0;
+    }
+    return false;
+}
+
+void alloc_point() {
+    if (alloc_fail_due()) throw std::bad_alloc();
+}
+
 gi_status ensure_buffer(void** ptr, size_t* cap, size_t bytes) {
     if (*cap >= bytes && *ptr) return GI_OK;
+    if (alloc_fail_due())
+        return fail(GI_ERR_OOM, std::string("cudaMalloc of ") + std::to_string(bytes) +
+                                    " bytes failed (injected allocation failure)");
     if (*ptr) {
         cudaFree(*ptr);
         *ptr = nullptr;
@@ -121,6 +142,7 @@ extern "C" void gi_context_destroy(gi_context* c) {
     cudaFree(c->d_area_gbuf);
     cudaFree(c->d_pba_near);
     cudaFree(c->d_edt_meanx);
+    cudaFree(c->d_pyr);
     for (int i = 0; i < 8; ++i) cudaFree(c->bin_buf[i]);
     for (int k = 0; k < 2; ++k)
         for (int i = 0; i < 8; ++i) cudaFree(c->tier_buf[k][i]);
@@ -1103,4 +1125,10 @@ extern "C" gi_status gi_shadow_volume_geometry(gi_context* ctx, const gi_scene* 
         return fail(GI_ERR_INVALID_ARG, "gi_shadow_volume_geometry: NULL argument");
     return gi::raster_volume_geometry(ctx, s, light_pos, infinity, d_triangles,
                                       static_cast<cudaStream_t>(stream));
+}
+
+extern "C" gi_status gi_debug_fail_allocation(int countdown) {
+    if (countdown < -1) return fail(GI_ERR_INVALID_ARG, "gi_debug_fail_allocation: countdown must be >= -1");
+    gi::g_alloc_countdown.store(countdown);
+    return GI_OK;
 }

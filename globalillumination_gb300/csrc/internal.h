@@ -12,6 +12,12 @@ namespace gi {
 
 // Records `msg` as the calling thread's last error and returns `st`.
 gi_status fail(gi_status st, const std::string& msg);
+// Allocation-failure injection (gi_debug_fail_allocation): true when the
+// allocation about to be made must fail.  Device allocations return
+// GI_ERR_OOM; host ones call alloc_point(), which throws std::bad_alloc,
+// and the C ABI turns that into GI_ERR_OOM.
+bool alloc_fail_due();
+void alloc_point();
 gi_status fail_cuda(int cuda_err, const char* what);
 
 struct Mesh {
@@ -93,7 +99,8 @@ struct gi_context {
     // big records, spills, error bits, admitted big pairs as u64, work
     // items), [32..55] counters of the tiered light-map pass, [64..87] of
     // the tiered camera-key pass (the two passes may run concurrently),
-    // [96] rows of the PBA row pass colored by the exact group chain
+    // [96] rows of the PBA row pass colored by the exact group chain,
+    // [100] error bits of the min-max pyramid (bit 0: a copy wait ran out)
     unsigned int* d_status = nullptr;
     unsigned int* h_status = nullptr;  // pinned mirror
     // area-light ground truth: a wave of sample light maps, per-pixel sums
@@ -120,6 +127,9 @@ struct gi_context {
     // nearest site per pixel (short2) when the caller does not keep it
     void* d_pba_near = nullptr;
     size_t cap_pba_near = 0;
+    // min-max pyramid of the light map (float2 levels 1..6), status word 100
+    void* d_pyr = nullptr;
+    size_t cap_pyr = 0;
     // second stream for the camera-key pass of gi_render_frame, and the
     // fork / join events (cudaStream_t / cudaEvent_t)
     void* aux_stream = nullptr;

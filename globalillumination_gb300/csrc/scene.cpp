@@ -29,6 +29,7 @@ namespace gi {
 // ---------------------------------------------------------------------------
 
 void compute_normals(Mesh& m) {
+    alloc_point();
     const int nv = m.num_vertices();
     if ((int)m.normals.size() != 3 * nv) m.normals.assign(3 * (size_t)nv, 0.0f);
     std::vector<int> nb_seen(nv, 0);
@@ -103,6 +104,11 @@ void mesh_rotate(Mesh& m, float x, float y, float z) {
 }
 
 void mesh_append(Mesh& dst, const Mesh& src) {
+    alloc_point();
+    // Reserve everything first: if an allocation fails, dst is unchanged.
+    dst.points.reserve(dst.points.size() + src.points.size());
+    dst.normals.reserve(dst.points.size() + src.points.size());
+    dst.indices.reserve(dst.indices.size() + src.indices.size());
     const int offset = dst.num_vertices();
     dst.points.insert(dst.points.end(), src.points.begin(), src.points.end());
     if (src.normals.size() == src.points.size())
@@ -221,6 +227,12 @@ int probe_vt(const std::string& tok) {
 gi_status read_obj(const char* path, Mesh& out) {
     std::FILE* f = std::fopen(path, "rb");
     if (!f) return fail(GI_ERR_IO, std::string("can't open OBJ file \"") + path + "\"");
+    try {
+        alloc_point();
+    } catch (...) {
+        std::fclose(f);
+        throw;
+    }
     std::string data;
     char buf[1 << 16];
     size_t got;
@@ -518,6 +530,19 @@ struct Perlin {
 // ---------------------------------------------------------------------------
 using gi::fail;
 
+// Runs an entry point's body, turning a failed host allocation into
+// GI_ERR_OOM (the reference exits instead: Mesh.cpp:336-340).  Bodies
+// change the scene only after their last allocation, so a failure leaves
+// it as it was.
+template <class F>
+static gi_status guarded(const char* who, F&& body) {
+    try {
+        return body();
+    } catch (const std::bad_alloc&) {
+        return fail(GI_ERR_OOM, std::string(who) + ": out of host memory");
+    }
+}
+
 extern "C" gi_status gi_scene_create(gi_scene** out) {
     if (!out) return fail(GI_ERR_INVALID_ARG, "gi_scene_create: out is NULL");
     try {
@@ -529,30 +554,34 @@ extern "C" gi_status gi_scene_create(gi_scene** out) {
 }
 
 extern "C" gi_status gi_scene_object_load_obj(gi_scene* s, const char* path) {
-    if (!s || !path) return fail(GI_ERR_INVALID_ARG, "gi_scene_object_load_obj: NULL argument");
-    gi::Mesh m;
-    gi_status st = gi::read_obj(path, m);
-    if (st != GI_OK) return st;
-    gi::compute_normals(m);
-    s->pending = std::move(m);
-    s->has_pending = true;
-    return GI_OK;
+    return guarded("gi_scene_object_load_obj", [&]() -> gi_status {
+        if (!s || !path) return fail(GI_ERR_INVALID_ARG, "gi_scene_object_load_obj: NULL argument");
+        gi::Mesh m;
+        gi_status st = gi::read_obj(path, m);
+        if (st != GI_OK) return st;
+        gi::compute_normals(m);
+        s->pending = std::move(m);
+        s->has_pending = true;
+        return GI_OK;
+    });
 }
 
 extern "C" gi_status gi_scene_object_from_arrays(gi_scene* s, const float* points, int nv,
                                                  const int* indices, int nt) {
-    if (!s || (nv > 0 && !points) || (nt > 0 && !indices) || nv < 0 || nt < 0)
-        return fail(GI_ERR_INVALID_ARG, "gi_scene_object_from_arrays: bad arguments");
-    gi::Mesh m;
-    m.points.assign(points, points + 3 * (size_t)nv);
-    m.indices.assign(indices, indices + 3 * (size_t)nt);
-    for (int idx : m.indices)
-        if (idx < 0 || idx >= nv)
-            return fail(GI_ERR_INVALID_ARG, "gi_scene_object_from_arrays: index out of range");
-    gi::compute_normals(m);
-    s->pending = std::move(m);
-    s->has_pending = true;
-    return GI_OK;
+    return guarded("gi_scene_object_from_arrays", [&]() -> gi_status {
+        if (!s || (nv > 0 && !points) || (nt > 0 && !indices) || nv < 0 || nt < 0)
+            return fail(GI_ERR_INVALID_ARG, "gi_scene_object_from_arrays: bad arguments");
+        gi::Mesh m;
+        m.points.assign(points, points + 3 * (size_t)nv);
+        m.indices.assign(indices, indices + 3 * (size_t)nt);
+        for (int idx : m.indices)
+            if (idx < 0 || idx >= nv)
+                return fail(GI_ERR_INVALID_ARG, "gi_scene_object_from_arrays: index out of range");
+        gi::compute_normals(m);
+        s->pending = std::move(m);
+        s->has_pending = true;
+        return GI_OK;
+    });
 }
 
 static gi_status need_pending(gi_scene* s, const char* who) {
@@ -584,15 +613,17 @@ extern "C" gi_status gi_scene_object_rotate(gi_scene* s, float x, float y, float
 }
 
 extern "C" gi_status gi_scene_object_commit(gi_scene* s) {
-    gi_status st = need_pending(s, "commit");
-    if (st != GI_OK) return st;
-    gi::mesh_append(s->mesh, s->pending);
-    if ((size_t)s->mesh.num_triangles() >= ((size_t)1 << 29))
-        return fail(GI_ERR_CAPACITY, "scene exceeds 2^29 triangles");
-    s->pending = gi::Mesh();
-    s->has_pending = false;
-    s->num_objects++;
-    return GI_OK;
+    return guarded("gi_scene_object_commit", [&]() -> gi_status {
+        gi_status st = need_pending(s, "commit");
+        if (st != GI_OK) return st;
+        gi::mesh_append(s->mesh, s->pending);
+        if ((size_t)s->mesh.num_triangles() >= ((size_t)1 << 29))
+            return fail(GI_ERR_CAPACITY, "scene exceeds 2^29 triangles");
+        s->pending = gi::Mesh();
+        s->has_pending = false;
+        s->num_objects++;
+        return GI_OK;
+    });
 }
 
 extern "C" gi_status gi_scene_set_views(gi_scene* s, const float ce[3], const float ca[3],
@@ -634,65 +665,94 @@ extern "C" gi_status gi_scene_get_arrays(const gi_scene* s, float* p, float* n, 
 }
 
 extern "C" gi_status gi_gen_ground(gi_scene* s, float h, float y) {
-    if (!s || !(h > 0)) return fail(GI_ERR_INVALID_ARG, "gi_gen_ground: bad arguments");
-    gi::gen_ground(s->pending, h, y);
-    s->has_pending = true;
-    return GI_OK;
+    return guarded("gi_gen_ground", [&]() -> gi_status {
+        if (!s || !(h > 0)) return fail(GI_ERR_INVALID_ARG, "gi_gen_ground: bad arguments");
+        gi::alloc_point();
+        gi::Mesh m;
+        gi::gen_ground(m, h, y);
+        s->pending = std::move(m);
+        s->has_pending = true;
+        return GI_OK;
+    });
 }
 
 extern "C" gi_status gi_gen_uv_sphere(gi_scene* s, int slices, int stacks, float r,
                                       const float c[3]) {
-    if (!s || !c || slices < 3 || stacks < 2 || !(r > 0))
-        return fail(GI_ERR_INVALID_ARG, "gi_gen_uv_sphere: bad arguments");
-    gi::gen_uv_grid_sphere(s->pending, slices, stacks, r, c, nullptr);
-    s->has_pending = true;
-    return GI_OK;
+    return guarded("gi_gen_uv_sphere", [&]() -> gi_status {
+        if (!s || !c || slices < 3 || stacks < 2 || !(r > 0))
+            return fail(GI_ERR_INVALID_ARG, "gi_gen_uv_sphere: bad arguments");
+        gi::alloc_point();
+        gi::Mesh m;
+        gi::gen_uv_grid_sphere(m, slices, stacks, r, c, nullptr);
+        s->pending = std::move(m);
+        s->has_pending = true;
+        return GI_OK;
+    });
 }
 
 extern "C" gi_status gi_gen_icosphere(gi_scene* s, int level, float r, const float c[3]) {
-    if (!s || !c || level < 0 || level > 8 || !(r > 0))
-        return fail(GI_ERR_INVALID_ARG, "gi_gen_icosphere: bad arguments");
-    gi::gen_icosphere(s->pending, level, r, c);
-    s->has_pending = true;
-    return GI_OK;
+    return guarded("gi_gen_icosphere", [&]() -> gi_status {
+        if (!s || !c || level < 0 || level > 8 || !(r > 0))
+            return fail(GI_ERR_INVALID_ARG, "gi_gen_icosphere: bad arguments");
+        gi::alloc_point();
+        gi::Mesh m;
+        gi::gen_icosphere(m, level, r, c);
+        s->pending = std::move(m);
+        s->has_pending = true;
+        return GI_OK;
+    });
 }
 
 extern "C" gi_status gi_gen_displaced_sphere(gi_scene* s, int slices, int stacks, float r,
                                              float amp, const float c[3], uint64_t seed) {
-    if (!s || !c || slices < 3 || stacks < 2 || !(r > 0))
-        return fail(GI_ERR_INVALID_ARG, "gi_gen_displaced_sphere: bad arguments");
-    // Radius per vertex: r + amp * noise(2 * unit direction), evaluated on
-    // the same unit directions the UV grid uses.
-    gi::Mesh unit;
-    const float zero[3] = {0, 0, 0};
-    gi::gen_uv_grid_sphere(unit, slices, stacks, 1.0f, zero, nullptr);
-    gi::Perlin noise(seed);
-    std::vector<float> radial(unit.num_vertices());
-    for (int v = 0; v < unit.num_vertices(); ++v) {
-        float x = unit.points[v * 3], y = unit.points[v * 3 + 1], z = unit.points[v * 3 + 2];
-        radial[v] = r + amp * noise.noise(2.0f * x + 17.0f, 2.0f * y + 17.0f, 2.0f * z + 17.0f);
-    }
-    gi::gen_uv_grid_sphere(s->pending, slices, stacks, r, c, &radial);
-    s->has_pending = true;
-    return GI_OK;
+    return guarded("gi_gen_displaced_sphere", [&]() -> gi_status {
+        if (!s || !c || slices < 3 || stacks < 2 || !(r > 0))
+            return fail(GI_ERR_INVALID_ARG, "gi_gen_displaced_sphere: bad arguments");
+        // Radius per vertex: r + amp * noise(2 * unit direction), evaluated on
+        // the same unit directions the UV grid uses.
+        gi::Mesh unit;
+        const float zero[3] = {0, 0, 0};
+        gi::gen_uv_grid_sphere(unit, slices, stacks, 1.0f, zero, nullptr);
+        gi::Perlin noise(seed);
+        std::vector<float> radial(unit.num_vertices());
+        for (int v = 0; v < unit.num_vertices(); ++v) {
+            float x = unit.points[v * 3], y = unit.points[v * 3 + 1], z = unit.points[v * 3 + 2];
+            radial[v] = r + amp * noise.noise(2.0f * x + 17.0f, 2.0f * y + 17.0f, 2.0f * z + 17.0f);
+        }
+        gi::alloc_point();
+        gi::Mesh m;
+        gi::gen_uv_grid_sphere(m, slices, stacks, r, c, &radial);
+        s->pending = std::move(m);
+        s->has_pending = true;
+        return GI_OK;
+    });
 }
 
 extern "C" gi_status gi_gen_icosphere_field(gi_scene* s, int count, int level, const float lo[3],
                                             const float hi[3], float rmin, float rmax,
                                             uint64_t seed) {
-    if (!s || !lo || !hi || count < 0 || level < 0 || level > 8 || !(rmin > 0) || rmax < rmin)
-        return fail(GI_ERR_INVALID_ARG, "gi_gen_icosphere_field: bad arguments");
-    gi::Pcg32 rng(seed, 54u);
-    for (int i = 0; i < count; ++i) {
-        float c[3];
-        for (int k = 0; k < 3; ++k) c[k] = rng.uniform(lo[k], hi[k]);
-        float r = rng.uniform(rmin, rmax);
-        gi::gen_icosphere(s->pending, level, r, c);
-        s->has_pending = true;
-        gi_status st = gi_scene_object_commit(s);
-        if (st != GI_OK) return st;
-    }
-    return GI_OK;
+    return guarded("gi_gen_icosphere_field", [&]() -> gi_status {
+        if (!s || !lo || !hi || count < 0 || level < 0 || level > 8 || !(rmin > 0) || rmax < rmin)
+            return fail(GI_ERR_INVALID_ARG, "gi_gen_icosphere_field: bad arguments");
+        gi::Pcg32 rng(seed, 54u);
+        // The spheres are built into one mesh first and committed together,
+        // as `count` objects: a failed allocation leaves the scene unchanged.
+        gi::Mesh field, sphere;
+        for (int i = 0; i < count; ++i) {
+            float c[3];
+            for (int k = 0; k < 3; ++k) c[k] = rng.uniform(lo[k], hi[k]);
+            float r = rng.uniform(rmin, rmax);
+            gi::gen_icosphere(sphere, level, r, c);
+            gi::mesh_append(field, sphere);
+        }
+        if ((size_t)s->mesh.num_triangles() + (size_t)field.num_triangles() >= ((size_t)1 << 29))
+            return fail(GI_ERR_CAPACITY, "scene exceeds 2^29 triangles");
+        gi::mesh_append(s->mesh, field);
+        s->num_objects += count;
+        s->pending = gi::Mesh();  // each sphere was the pending object once, then committed
+        s->has_pending = false;
+        return GI_OK;
+    });
 }
 
 // ---------------------------------------------------------------------------
@@ -711,82 +771,84 @@ static std::string join_path(const char* base, const std::string& rel) {
 
 extern "C" gi_status gi_scene_load_config(const char* cfg_path, const char* base_dir,
                                           gi_scene** out) {
-    if (!cfg_path || !out) return fail(GI_ERR_INVALID_ARG, "gi_scene_load_config: NULL");
-    std::ifstream file(cfg_path);
-    if (!file.is_open())
-        return fail(GI_ERR_IO, std::string("can't open config \"") + cfg_path + "\"");
-    gi_scene* s = nullptr;
-    gi_status st = gi_scene_create(&s);
-    if (st != GI_OK) return st;
-    // `key` and `value` live across lines as in the reference: a blank line
-    // leaves both unchanged and repeats the previous key's action with the
-    // previous value.
-    std::string line, key, value;
-    auto val = [&](std::istringstream& split) {
-        split >> value;
-        return (float)std::atof(value.c_str());
-    };
-    while (!file.eof()) {
-        std::getline(file, line);
-        std::istringstream split(line);
-        split >> key;
-        if (key.empty()) continue;
-        const char k0 = key[0];
-        const char k1 = key.size() > 1 ? key[1] : '\0';
-        st = GI_OK;
-        if (k0 == 'o') {
+    return guarded("gi_scene_load_config", [&]() -> gi_status {
+        if (!cfg_path || !out) return fail(GI_ERR_INVALID_ARG, "gi_scene_load_config: NULL");
+        std::ifstream file(cfg_path);
+        if (!file.is_open())
+            return fail(GI_ERR_IO, std::string("can't open config \"") + cfg_path + "\"");
+        gi_scene* s = nullptr;
+        gi_status st = gi_scene_create(&s);
+        if (st != GI_OK) return st;
+        // `key` and `value` live across lines as in the reference: a blank line
+        // leaves both unchanged and repeats the previous key's action with the
+        // previous value.
+        std::string line, key, value;
+        auto val = [&](std::istringstream& split) {
             split >> value;
-            st = gi_scene_object_load_obj(s, join_path(base_dir, value).c_str());
-        } else if (k0 == 'm') {
-            split >> value;  // texture image: not on the visibility path
-        } else if (k0 == 's') {
-            float v[3];
-            for (int a = 0; a < 3; ++a) v[a] = val(split);
-            st = gi_scene_object_scale(s, v[0], v[1], v[2]);
-        } else if (k0 == 't') {
-            float v[3];
-            for (int a = 0; a < 3; ++a) v[a] = val(split);
-            st = gi_scene_object_translate(s, v[0], v[1], v[2]);
-        } else if (k0 == 'r') {
-            float v[3];
-            for (int a = 0; a < 3; ++a) v[a] = val(split);
-            st = gi_scene_object_rotate(s, v[0], v[1], v[2]);
-        } else if (k0 == '+') {
-            if (line.find('+') != std::string::npos) {
-                st = gi_scene_object_commit(s);
-            } else if (!file.eof()) {
-                // A blank line after '+' makes the reference commit the object
-                // it has just deleted (use after free); refuse it.  The empty
-                // read at end of file that `while (!eof)` produces after a
-                // final "+\n" is skipped instead.
-                st = fail(GI_ERR_PARSE, "blank line after '+' repeats a commit");
-            }
-        } else if (k0 == 'v') {
-            for (int a = 0; a < 3; ++a) {
+            return (float)std::atof(value.c_str());
+        };
+        while (!file.eof()) {
+            std::getline(file, line);
+            std::istringstream split(line);
+            split >> key;
+            if (key.empty()) continue;
+            const char k0 = key[0];
+            const char k1 = key.size() > 1 ? key[1] : '\0';
+            st = GI_OK;
+            if (k0 == 'o') {
+                split >> value;
+                st = gi_scene_object_load_obj(s, join_path(base_dir, value).c_str());
+            } else if (k0 == 'm') {
+                split >> value;  // texture image: not on the visibility path
+            } else if (k0 == 's') {
+                float v[3];
+                for (int a = 0; a < 3; ++a) v[a] = val(split);
+                st = gi_scene_object_scale(s, v[0], v[1], v[2]);
+            } else if (k0 == 't') {
+                float v[3];
+                for (int a = 0; a < 3; ++a) v[a] = val(split);
+                st = gi_scene_object_translate(s, v[0], v[1], v[2]);
+            } else if (k0 == 'r') {
+                float v[3];
+                for (int a = 0; a < 3; ++a) v[a] = val(split);
+                st = gi_scene_object_rotate(s, v[0], v[1], v[2]);
+            } else if (k0 == '+') {
+                if (line.find('+') != std::string::npos) {
+                    st = gi_scene_object_commit(s);
+                } else if (!file.eof()) {
+                    // A blank line after '+' makes the reference commit the object
+                    // it has just deleted (use after free); refuse it.  The empty
+                    // read at end of file that `while (!eof)` produces after a
+                    // final "+\n" is skipped instead.
+                    st = fail(GI_ERR_PARSE, "blank line after '+' repeats a commit");
+                }
+            } else if (k0 == 'v') {
+                for (int a = 0; a < 3; ++a) {
+                    float f = val(split);
+                    if (k1 == 'e') s->camera_eye[a] = f;
+                    else s->camera_at[a] = f;
+                }
+            } else if (k0 == 'l') {
+                for (int a = 0; a < 3; ++a) {
+                    float f = val(split);
+                    if (k1 == 'e') s->light_eye[a] = f;
+                    else s->light_at[a] = f;
+                }
+            } else if (k0 == 'c') {
+                // colours (c r g b / cf obj): not on the visibility path
+            } else if (k0 == 'd') {
+                s->depth_threshold = val(split);
+            } else if (k0 == 'h') {
                 float f = val(split);
-                if (k1 == 'e') s->camera_eye[a] = f;
-                else s->camera_at[a] = f;
+                if (k1 == 'a') s->hsm_alpha = f;
+                else s->hsm_beta = f;
             }
-        } else if (k0 == 'l') {
-            for (int a = 0; a < 3; ++a) {
-                float f = val(split);
-                if (k1 == 'e') s->light_eye[a] = f;
-                else s->light_at[a] = f;
+            if (st != GI_OK) {
+                gi_scene_destroy(s);
+                return st;
             }
-        } else if (k0 == 'c') {
-            // colours (c r g b / cf obj): not on the visibility path
-        } else if (k0 == 'd') {
-            s->depth_threshold = val(split);
-        } else if (k0 == 'h') {
-            float f = val(split);
-            if (k1 == 'a') s->hsm_alpha = f;
-            else s->hsm_beta = f;
         }
-        if (st != GI_OK) {
-            gi_scene_destroy(s);
-            return st;
-        }
-    }
-    *out = s;
-    return GI_OK;
+        *out = s;
+        return GI_OK;
+    });
 }

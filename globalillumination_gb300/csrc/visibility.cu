@@ -32,6 +32,7 @@
 #include <cuda_runtime.h>
 
 #include "internal.h"
+#include "minmax.h"
 #include "raster.h"
 #include "raster_common.cuh"
 
@@ -60,6 +61,8 @@ __device__ __forceinline__ float gclamp(float x, float lo, float hi) { return gm
 __device__ __forceinline__ float gmix(float x, float y, float a) { return x * (1.0f - a) + y * a; }
 __device__ __forceinline__ float gfract(float x) { return x - floorf(x); }
 
+struct PoissonOffsets;
+
 struct Ctx {
     const float* __restrict__ map;
     int W, H;
@@ -71,11 +74,19 @@ struct Ctx {
     // the multiplication rounds them, computed once per launch (nullptr:
     // multiply per tap)
     const float2* boff = nullptr;
+    // the launch's offset table and pyramid (nullptr: run every tap)
+    const PoissonOffsets* tab = nullptr;
 };
 
-// The blocker-search offsets of one launch, a kernel parameter read in place.
+// The blocker-search offsets of one launch, a kernel parameter read in place,
+// with the extreme offsets of the blocker and filter taps (componentwise
+// minimum and maximum: the blocker offsets as rounded products, the filter's
+// Poisson points before their scale by the penumbra width) and the light
+// map's min-max pyramid (levels 0: none).
 struct PoissonOffsets {
     float2 b[64];
+    float2 bmin, bmax, fmin, fmax;
+    Pyramid pyr;
 };
 
 __device__ __forceinline__ float fetch(const Ctx& c, float s, float t) {
@@ -131,6 +142,37 @@ __device__ __forceinline__ float fetch_finite(const Ctx& c, float s, float t) {
     const int iy = __float2int_rd(t * c.fH);
     if ((unsigned)ix >= (unsigned)c.W || (unsigned)iy >= (unsigned)c.H) return 0.0f;
     return __ldg(c.map + (iy * c.W + ix));
+}
+
+// Exact tap skipping.  The taps at (sx, sy) = (n.x + o.x, n.y + o.y) for
+// offsets o in [lo, hi] (componentwise) read texels inside the box
+// [floor(sx0 W), floor(sx1 W)] x [floor(sy0 H), floor(sy1 H)], where sx0 /
+// sx1 are the coordinates of the smallest / largest offset computed with the
+// taps' own operations: float addition, multiplication by a positive scale
+// and floor are monotone, so no tap leaves the box.  Gives the minimum and
+// maximum of the map over the box from the pyramid (at the level where the
+// box spans at most 2 x 2 cells); false when the box leaves the map (border
+// texels read 0) or is wider than the pyramid's top level.
+__device__ __forceinline__ bool tap_box_minmax(const Ctx& c, float sx0, float sx1, float sy0, float sy1, float& mn,
+                                               float& mx) {
+    const int x0 = __float2int_rd(sx0 * c.fW), x1 = __float2int_rd(sx1 * c.fW);
+    const int y0 = __float2int_rd(sy0 * c.fH), y1 = __float2int_rd(sy1 * c.fH);
+    if (x0 < 0 || y0 < 0 || x1 >= c.W || y1 >= c.H) return false;
+    const int span = max(x1 - x0, y1 - y0);
+    if (span == 0) {
+        mn = mx = __ldg(c.map + (y0 * c.W + x0));
+        return true;
+    }
+    const int L = 32 - __clz(span);  // 2^L > span: at most two cells per axis
+    if (L > c.tab->pyr.levels) return false;
+    const float2* lv = c.tab->pyr.lv[L];
+    const int w = c.W >> L;
+    const int cx0 = x0 >> L, cx1 = x1 >> L, cy0 = y0 >> L, cy1 = y1 >> L;
+    const float2 a = __ldg(lv + (cy0 * w + cx0)), b = __ldg(lv + (cy0 * w + cx1));
+    const float2 d = __ldg(lv + (cy1 * w + cx0)), e = __ldg(lv + (cy1 * w + cx1));
+    mn = fminf(fminf(a.x, b.x), fminf(d.x, e.x));
+    mx = fmaxf(fmaxf(a.y, b.y), fmaxf(d.y, e.y));
+    return true;
 }
 
 __device__ __forceinline__ bool finite3(float a, float b, float d) {
@@ -265,9 +307,15 @@ __device__ float avg_blocker_grid(const gi_vis_params& p, const Ctx& c, V4 n) {
 
 template <bool FAST>
 __device__ float avg_blocker_poisson_t(const gi_vis_params& p, const Ctx& c, V4 n, float bsw) {
+    const float2* bo = c.boff;
+    if (FAST && bo && c.tab && c.tab->pyr.levels > 0) {
+        // no texel the taps can reach is below z: no tap finds a blocker
+        const float2 lo = c.tab->bmin, hi = c.tab->bmax;
+        float mn, mx;
+        if (tap_box_minmax(c, n.x + lo.x, n.x + hi.x, n.y + lo.y, n.y + hi.y, mn, mx) && n.z <= mn) return 1.0f;
+    }
     float avg = 0.0f;
     int nb = 0;
-    const float2* bo = c.boff;
     for (int i = 0; i < p.poisson_blocker_taps; ++i) {
         float s, t;
         if (bo) {
@@ -292,6 +340,18 @@ template <bool FAST>
 __device__ float pcss_filter_poisson_t(const gi_vis_params& p, const Ctx& c, float pw, V4 n) {
     float illum = 0.0f;
     const int nf = p.poisson_filter_taps;
+    if (FAST && c.tab && c.tab->pyr.levels > 0) {
+        // pw > 0 here (the caller checked the step), so o.x * pw is monotone in o.x
+        const float2 lo = c.tab->fmin, hi = c.tab->fmax;
+        float mn, mx;
+        if (tap_box_minmax(c, n.x + lo.x * pw, n.x + hi.x * pw, n.y + lo.y * pw, n.y + hi.y * pw, mn, mx)) {
+            if (n.z <= mn) return 1.0f;  // every tap lit: nf additions of 1, over nf
+            if (n.z > mx) {              // every tap shadowed: the same additions of I
+                for (int j = 0; j < nf; ++j) illum += c.I;
+                return illum / (float)nf;
+            }
+        }
+    }
     for (int j = 0; j < nf; ++j) {
         float2 o = c_poisson[j];
         const float s = n.x + o.x * pw, t = n.y + o.y * pw;
@@ -1557,6 +1617,7 @@ __global__ void __launch_bounds__(128) k_visibility(const gi_vis_params p,
     c.I = p.shadow_intensity;
     c.sm = sm;
     c.boff = TECH == GI_TECH_PCSS_POISSON ? po.b : nullptr;
+    c.tab = TECH == GI_TECH_PCSS_POISSON ? &po : nullptr;
     size_t i = (size_t)y * W + x;
     float4 pv = __ldcs(pos + i);
     float4 nv = __ldcs(nrm + i);
@@ -1588,6 +1649,7 @@ __global__ void __launch_bounds__(128, 10) k_frame_visibility(
     Ctx c;
     c.sm = sm;
     c.boff = TECH == GI_TECH_PCSS_POISSON ? po.b : nullptr;
+    c.tab = TECH == GI_TECH_PCSS_POISSON ? &po : nullptr;
     c.map = map;
     c.W = map_w;
     c.H = map_h;
@@ -2034,9 +2096,27 @@ static vis::PoissonOffsets poisson_offsets(const gi_vis_params* p, int map_w) {
     if (p->technique != GI_TECH_PCSS_POISSON) return po;
     const float fw = (float)map_w;
     const float bsw = fw <= 1024.0f ? p->light_radius / fw : p->light_radius / 1024.0f;
-    for (int i = 0; i < 64 && i < p->poisson_blocker_taps; ++i)
+    po.bmin = po.fmin = make_float2(INFINITY, INFINITY);
+    po.bmax = po.fmax = make_float2(-INFINITY, -INFINITY);
+    for (int i = 0; i < 64 && i < p->poisson_blocker_taps; ++i) {
         po.b[i] = make_float2(kPoissonDisk[i][0] * bsw, kPoissonDisk[i][1] * bsw);
+        po.bmin = make_float2(std::min(po.bmin.x, po.b[i].x), std::min(po.bmin.y, po.b[i].y));
+        po.bmax = make_float2(std::max(po.bmax.x, po.b[i].x), std::max(po.bmax.y, po.b[i].y));
+    }
+    for (int j = 0; j < 64 && j < p->poisson_filter_taps; ++j) {
+        po.fmin = make_float2(std::min(po.fmin.x, kPoissonDisk[j][0]), std::min(po.fmin.y, kPoissonDisk[j][1]));
+        po.fmax = make_float2(std::max(po.fmax.x, kPoissonDisk[j][0]), std::max(po.fmax.y, kPoissonDisk[j][1]));
+    }
     return po;
+}
+
+// PCSS_POISSON reads the light map's min-max pyramid to skip taps exactly
+// (square-tile maps only; the others run every tap).
+static gi_status prepare_pyramid(gi_context* ctx, const gi_vis_params* p, const float* d_depth, int map_w,
+                                 int map_h, cudaStream_t st, vis::PoissonOffsets* po) {
+    if (p->technique != GI_TECH_PCSS_POISSON || p->poisson_blocker_taps < 1 || p->poisson_filter_taps < 1)
+        return GI_OK;
+    return launch_minmax_pyramid(ctx, d_depth, map_w, map_h, st, &po->pyr);
 }
 
 // The maps the moment techniques read instead of (VSM..MSM) or beside
@@ -2071,7 +2151,9 @@ gi_status launch_visibility(gi_context* ctx, const gi_vis_params* p, const float
     const float sx = (float)(1.0 / (double)map_w), sy = (float)(1.0 / (double)map_h);
     const float4* pos = reinterpret_cast<const float4*>(d_pos);
     const float4* nrm = reinterpret_cast<const float4*>(d_nrm);
-    const vis::PoissonOffsets po = poisson_offsets(p, map_w);
+    vis::PoissonOffsets po = poisson_offsets(p, map_w);
+    ps = prepare_pyramid(ctx, p, d_depth, map_w, map_h, st, &po);
+    if (ps != GI_OK) return ps;
 #define GI_VIS_CASE(T)                                                                     \
     case T:                                                                                \
         vis::k_visibility<T><<<grid, 128, 0, st>>>(*p, d_depth, map_w, map_h, sx, sy, pos, nrm, d_vis, W, H, sm, po); \
@@ -2122,7 +2204,9 @@ gi_status launch_frame_visibility(gi_context* ctx, const gi_vis_params* p, const
     for (int k = 0; k < 16; ++k) m.m[k] = camera_mvp[k];
     float4* po = reinterpret_cast<float4*>(d_pos);
     float4* no = reinterpret_cast<float4*>(d_nrm);
-    const vis::PoissonOffsets boff = poisson_offsets(p, map_w);
+    vis::PoissonOffsets boff = poisson_offsets(p, map_w);
+    ps = prepare_pyramid(ctx, p, d_depth, map_w, map_h, st, &boff);
+    if (ps != GI_OK) return ps;
 #define GI_FRAME_CASE(T)                                                                          \
     case T:                                                                                       \
         vis::k_frame_visibility<T><<<grid, 128, 0, st>>>(*p, d_depth, map_w, map_h, sx, sy,         \

@@ -55,6 +55,11 @@ def _ptr(t) -> C.c_void_p:
     return C.c_void_p(int(t.data_ptr()))
 
 
+def debug_fail_allocation(countdown: int) -> None:
+    """Test hook: let `countdown` more allocations succeed and fail the next (-1: off)."""
+    check(_lib().gi_debug_fail_allocation(int(countdown)), "gi_debug_fail_allocation")
+
+
 class Context:
     """Owns the scratch memory of the passes on one CUDA device."""
 
@@ -420,6 +425,22 @@ def shadow_volume_geometry(ctx: Context, scene: Scene, light_pos, out, infinity:
     check(_lib().gi_shadow_volume_geometry(ctx.handle, scene.handle, _f3(light_pos), float(infinity), _ptr(out),
                                            _stream_ptr(stream)), "gi_shadow_volume_geometry")
     return out
+
+
+def light_map_minmax(ctx: Context, depth, width: int, height: int, stream=None) -> list:
+    """The light map's min-max pyramid (levels 1..6) as a list of float32 CUDA tensors
+    [(height >> L), (width >> L), 2] holding (min, max) per 2^L x 2^L block."""
+    import torch
+
+    sizes = [(height >> L, width >> L) for L in range(1, 7)]
+    out = torch.empty(sum(h * w for h, w in sizes) * 2, dtype=torch.float32, device=depth.device)
+    check(_lib().gi_light_map_minmax(ctx.handle, _ptr(depth), int(width), int(height), _ptr(out), _stream_ptr(stream)),
+          "gi_light_map_minmax")
+    levels, off = [], 0
+    for h, w in sizes:
+        levels.append(out[off:off + h * w * 2].view(h, w, 2))
+        off += h * w * 2
+    return levels
 
 
 @dataclass

@@ -360,63 +360,153 @@ def training_scene(rng: np.random.Generator, seed: int):
     return s, light, camera, mp, p
 
 
+# ---- checkpoints ---------------------------------------------------------------------
+CHECKPOINT_VERSION = 1
+
+
+def pack_checkpoint(net_state: dict, trainer_state: dict) -> dict:
+    """Flat numpy archive of a training run: every layer's FP32 master
+    weights and biases, their Adam moments, the optimiser step, and the
+    trainer's position (next step, data RNG state, hyperparameters)."""
+    import json
+
+    out = {k: np.asarray(v) for k, v in net_state.items()}
+    out["trainer_json"] = np.array(json.dumps(trainer_state))
+    out["checkpoint_version"] = np.array(CHECKPOINT_VERSION)
+    return out
+
+
+def unpack_checkpoint(z) -> tuple[dict, dict]:
+    import json
+
+    if int(z["checkpoint_version"]) != CHECKPOINT_VERSION:
+        raise ValueError("unsupported checkpoint version")
+    net_state = {k: np.asarray(z[k]) for k in z.keys() if k not in ("trainer_json", "checkpoint_version")}
+    return net_state, json.loads(str(z["trainer_json"]))
+
+
+def net_full_state(net: "UNet") -> dict:
+    out = {"step_count": np.array(net.step_count, np.int64)}
+    for n, L in net.layers.items():
+        out[n + ".w"] = L.w.cpu().numpy()
+        out[n + ".b"] = L.b.cpu().numpy()
+        out[n + ".mw"], out[n + ".mb"] = L.m[0].cpu().numpy(), L.m[1].cpu().numpy()
+        out[n + ".vw"], out[n + ".vb"] = L.v[0].cpu().numpy(), L.v[1].cpu().numpy()
+    return out
+
+
+def load_net_full_state(net: "UNet", st: dict) -> None:
+    for n, L in net.layers.items():
+        for t, key in ((L.w, ".w"), (L.b, ".b"), (L.m[0], ".mw"), (L.m[1], ".mb"), (L.v[0], ".vw"), (L.v[1], ".vb")):
+            t.copy_(torch.from_numpy(np.asarray(st[n + key])))
+    net.step_count = int(st["step_count"])
+    net.repack()
+
+
+class Trainer:
+    """Adam on random crops of freshly rendered PCSS frames; one crop per frame.
+
+    The run is resumable: `save(path)` writes the weights, biases, Adam
+    moments and step of every layer, the next step index and the data RNG's
+    state; a new Trainer over a fresh UNet that `load`s it continues with the
+    same crops and, the gradient reductions running in a fixed order, the
+    same losses and weights bit for bit."""
+
+    def __init__(self, ctx: Context, net: "UNet", batch: int = 16, crop: int = 256, lr: float = 1e-3,
+                 scenes_in_pool: int = 24, seed: int = 0x5EED0003):
+        self.ctx, self.net = ctx, net
+        self.batch, self.crop, self.lr = batch, crop, lr
+        self.scenes_in_pool, self.seed = scenes_in_pool, seed
+        self.rng = np.random.default_rng(seed)
+        self.pool = []
+        for k in range(scenes_in_pool):
+            s, light, camera, mp, p = training_scene(self.rng, seed + k)
+            s.upload(ctx)
+            self.pool.append((s, light, camera, mp, p))
+        self.step = 0
+        dev = net.device
+        self._frames = {}  # (map side, W, H) -> (frame buffers, features, depth scratch)
+        self.bfeat = torch.empty((batch, crop, crop, FEATURES), dtype=torch.bfloat16, device=dev)
+        self.btarget = torch.empty((batch, crop, crop), dtype=torch.float32, device=dev)
+        self.head = torch.empty((batch, crop, crop, HEAD), dtype=torch.float32, device=dev)
+        self.dhead = torch.empty((batch, crop, crop, HEAD), dtype=torch.bfloat16, device=dev)
+        self.sums = torch.zeros(3, dtype=torch.float32, device=dev)
+
+    def _buffers(self, side, W, H):
+        from .shadow import allocate_frame
+
+        if (side, W, H) not in self._frames:
+            dev = self.net.device
+            self._frames[(side, W, H)] = (allocate_frame(side, side, W, H),
+                                          torch.empty((1, H, W, FEATURES), dtype=torch.bfloat16, device=dev),
+                                          torch.empty(side * side, dtype=torch.float32, device=dev))
+        return self._frames[(side, W, H)]
+
+    def run(self, steps: int, log_every: int = 100, verbose: bool = True) -> list:
+        """Runs `steps` optimiser steps; returns [{step, mae, err_l1, seconds}] every log_every steps and at the end."""
+        from .shadow import render_frame
+
+        rng, net, ctx = self.rng, self.net, self.ctx
+        hist = []
+        t0 = time.perf_counter()
+        last = self.step + steps
+        while self.step < last:
+            for b in range(self.batch):
+                s, light, camera, mp, p = self.pool[int(rng.integers(len(self.pool)))]
+                # jitter the light within the scene's neighbourhood
+                le = tuple(float(x) for x in np.asarray(light.eye) + rng.uniform(-1.0, 1.0, 3))
+                lv = ViewSpec(eye=le, at=light.at, width=light.width, height=light.height, fovy_deg=light.fovy_deg)
+                fr = frame_setup(lv, camera)
+                W, H = camera.width, camera.height
+                bufs, feat, depth2 = self._buffers(mp.width, W, H)
+                render_frame(ctx, s, fr, mp, p, W, H, bufs)
+                features(ctx, s, fr, mp, p, W, H, depth2, feat)
+                y0 = int(rng.integers(0, H - self.crop + 1))
+                x0 = int(rng.integers(0, W - self.crop + 1))
+                self.bfeat[b].copy_(feat[0, y0:y0 + self.crop, x0:x0 + self.crop])
+                self.btarget[b].copy_(bufs.vis.view(H, W)[y0:y0 + self.crop, x0:x0 + self.crop])
+            net.forward(self.bfeat, out32=self.head, keep=True)
+            self.sums.zero_()
+            loss(self.head, self.btarget, self.bfeat, self.dhead, self.sums)
+            net.backward(self.dhead)
+            net.adam_step(self.lr)
+            self.step += 1
+            if self.step % log_every == 0 or self.step == last:
+                s_ = self.sums.cpu().numpy()
+                hist.append({"step": self.step, "mae": float(s_[0] / max(s_[1], 1.0)),
+                             "err_l1": float(s_[2] / max(s_[1], 1.0)), "seconds": time.perf_counter() - t0})
+                if verbose:
+                    print(f"step {self.step} mae {hist[-1]['mae']:.5f} err-head {hist[-1]['err_l1']:.5f} "
+                          f"{hist[-1]['seconds']:.1f}s", flush=True)
+        if net.kernel_error():
+            raise RuntimeError("a tcgen05 kernel reported a timed-out wait during training")
+        return hist
+
+    def state(self) -> dict:
+        return {"step": self.step, "rng": self.rng.bit_generator.state, "batch": self.batch, "crop": self.crop,
+                "lr": self.lr, "scenes_in_pool": self.scenes_in_pool, "seed": self.seed}
+
+    def save(self, path: str) -> None:
+        np.savez(path, **pack_checkpoint(net_full_state(self.net), self.state()))
+
+    def load(self, path: str) -> None:
+        with np.load(path) as z:
+            net_state, st = unpack_checkpoint(z)
+        for k in ("batch", "crop", "scenes_in_pool", "seed"):
+            if st[k] != getattr(self, k):
+                raise ValueError(f"checkpoint was made with {k} = {st[k]}, this trainer has {getattr(self, k)}")
+        load_net_full_state(self.net, net_state)
+        self.lr = st["lr"]
+        self.step = int(st["step"])
+        self.rng.bit_generator.state = st["rng"]
+
+
 def train(ctx: Context, net: UNet, frames: int = 20000, batch: int = 16, crop: int = 256, lr: float = 1e-3,
           scenes_in_pool: int = 24, seed: int = 0x5EED0003, log_every: int = 100, verbose: bool = True) -> dict:
-    """Adam on random crops of freshly rendered PCSS frames; one crop per frame."""
-    from .shadow import allocate_frame, render_frame
-
-    rng = np.random.default_rng(seed)
-    pool = []
-    for k in range(scenes_in_pool):
-        s, light, camera, mp, p = training_scene(rng, seed + k)
-        s.upload(ctx)
-        pool.append((s, light, camera, mp, p))
-    dev = net.device
-    frames_by_shape = {}  # (map side, W, H) -> (frame buffers, features, depth scratch)
-
-    def buffers(side, W, H):
-        if (side, W, H) not in frames_by_shape:
-            frames_by_shape[(side, W, H)] = (allocate_frame(side, side, W, H),
-                                             torch.empty((1, H, W, FEATURES), dtype=torch.bfloat16, device=dev),
-                                             torch.empty(side * side, dtype=torch.float32, device=dev))
-        return frames_by_shape[(side, W, H)]
-
-    bfeat = torch.empty((batch, crop, crop, FEATURES), dtype=torch.bfloat16, device=dev)
-    btarget = torch.empty((batch, crop, crop), dtype=torch.float32, device=dev)
-    head = torch.empty((batch, crop, crop, HEAD), dtype=torch.float32, device=dev)
-    dhead = torch.empty((batch, crop, crop, HEAD), dtype=torch.bfloat16, device=dev)
-    sums = torch.zeros(3, dtype=torch.float32, device=dev)
-    steps = max(1, frames // batch)
-    hist = []
+    """Adam on random crops of freshly rendered PCSS frames; one crop per frame (see Trainer)."""
     t0 = time.perf_counter()
-    for step in range(steps):
-        for b in range(batch):
-            s, light, camera, mp, p = pool[int(rng.integers(len(pool)))]
-            # jitter the light within the scene's neighbourhood
-            le = tuple(float(x) for x in np.asarray(light.eye) + rng.uniform(-1.0, 1.0, 3))
-            lv = ViewSpec(eye=le, at=light.at, width=light.width, height=light.height, fovy_deg=light.fovy_deg)
-            fr = frame_setup(lv, camera)
-            W, H = camera.width, camera.height
-            bufs, feat, depth2 = buffers(mp.width, W, H)
-            render_frame(ctx, s, fr, mp, p, W, H, bufs)
-            features(ctx, s, fr, mp, p, W, H, depth2, feat)
-            y0 = int(rng.integers(0, H - crop + 1))
-            x0 = int(rng.integers(0, W - crop + 1))
-            bfeat[b].copy_(feat[0, y0:y0 + crop, x0:x0 + crop])
-            btarget[b].copy_(bufs.vis.view(H, W)[y0:y0 + crop, x0:x0 + crop])
-        net.forward(bfeat, out32=head, keep=True)
-        sums.zero_()
-        loss(head, btarget, bfeat, dhead, sums)
-        net.backward(dhead)
-        net.adam_step(lr)
-        if (step + 1) % log_every == 0 or step == steps - 1:
-            s_ = sums.cpu().numpy()
-            hist.append({"step": step + 1, "mae": float(s_[0] / max(s_[1], 1.0)), "err_l1": float(s_[2] / max(s_[1], 1.0)),
-                         "seconds": time.perf_counter() - t0})
-            if verbose:
-                print(f"step {step + 1}/{steps} mae {hist[-1]['mae']:.5f} err-head {hist[-1]['err_l1']:.5f} "
-                      f"{hist[-1]['seconds']:.1f}s", flush=True)
-    if net.kernel_error():
-        raise RuntimeError("a tcgen05 kernel reported a timed-out wait during training")
+    tr = Trainer(ctx, net, batch, crop, lr, scenes_in_pool, seed)
+    steps = max(1, frames // batch)
+    hist = tr.run(steps, log_every=log_every, verbose=verbose)
     return {"steps": steps, "frames": steps * batch, "batch": batch, "crop": crop, "history": hist,
             "seconds": time.perf_counter() - t0}

@@ -53,6 +53,14 @@ typedef enum gi_status {
 
 /* Text of the last error raised on this thread ("" if none). */
 const char* gi_last_error_string(void);
+/* Allocation-failure injection, for testing the error paths (process-wide,
+ * off by default).  No counterpart in the reference, which exits on a
+ * failed load (Mesh.cpp:336-340).  With countdown n >= 0 the library lets
+ * n more allocations succeed (host: mesh and scene arrays; device: scene
+ * uploads and context scratch) and fails the next one, which the entry
+ * point that made it returns as GI_ERR_OOM, leaving its scene or context
+ * as it was; the injection then switches itself off.  -1 switches it off. */
+gi_status gi_debug_fail_allocation(int countdown);
 /* Library version string. */
 const char* gi_version(void);
 
@@ -538,6 +546,20 @@ gi_status gi_area_light_adaptive(gi_context* ctx, const gi_scene* scene, const g
                                  const float camera_mvp[16],
                                  float shadow_intensity, int width, int height, float* d_vis,
                                  gi_view* samples_out, float* levels_out, int* num_samples, void* stream);
+
+/* Min-max pyramid of a light map.  No counterpart in the reference: the
+ * PCSS pass (GI_TECH_PCSS_POISSON) builds it after the light map and skips
+ * the blocker taps of a pixel when no texel they can reach is below the
+ * receiver, and the filter taps when all of those texels lie on one side
+ * of it, which gives the same float result as running the taps.  This
+ * entry point builds it alone: d_levels receives levels 1..6 one after the
+ * other, level L as float2(min, max) of every 2^L x 2^L texel block over
+ * (width >> L) x (height >> L) cells, row-major (width * height / 3 float2
+ * in all, rounded down per level).  width and height must be multiples of
+ * 64 and d_map 16-byte aligned (the visibility pass runs every tap for
+ * maps that are not). */
+gi_status gi_light_map_minmax(gi_context* ctx, const float* d_map, int width, int height,
+                              float* d_levels, void* stream);
 
 /* ------------------------------------------------------------------ */
 /* A13/A14: shadow volumes with stencil counts                         */
