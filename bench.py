@@ -582,6 +582,31 @@ def run_heavy(args, ctx, stream, local, net=None):
     ms = timed(volumes, 2)
     out["shadow_volumes"] = {"ms_per_frame_8_lights": ms, "volume_triangles_per_light": 6 * tris,
                              "lit_fraction_last_light": float((stencil == 0).float().mean())}
+    # the opt-in silhouette mode: time for the 8 lights, triangles drawn, and
+    # the pixels whose counts (and lit / shadowed decision) differ from the
+    # exact path, per light
+    sil = torch.empty_like(stencil)
+    drawn = []
+
+    def volumes_sil():
+        drawn.clear()
+        for l in lights:
+            drawn.append(gi.shadow_volume_counts_silhouette(ctx, w.scene, l.eye, fr0.camera_mvp, W, H, sil,
+                                                            stream=stream))
+
+    volumes_sil()  # builds the edge adjacency once
+    ms_sil = timed(volumes_sil, 2)
+    differ, lit_differ = [], []
+    for l in lights:
+        gi.shadow_volume_counts(ctx, w.scene, l.eye, fr0.camera_mvp, W, H, stencil, stream=stream)
+        gi.shadow_volume_counts_silhouette(ctx, w.scene, l.eye, fr0.camera_mvp, W, H, sil, stream=stream)
+        torch.cuda.synchronize()
+        differ.append(int((stencil != sil).sum()))
+        lit_differ.append(int(((stencil == 0) != (sil == 0)).sum()))
+    out["shadow_volumes_silhouette"] = {
+        "ms_per_frame_8_lights": ms_sil, "volume_triangles_drawn_per_light": drawn,
+        "pixels_differing_from_exact_per_light": differ,
+        "pixels_lit_decision_differing_per_light": lit_differ, "pixels": W * H}
     if net is not None:
         from globalillumination_gb300 import surrogate as sg
 
@@ -1281,6 +1306,10 @@ def compact_summary(line: dict) -> dict:
         out["heavy_pcss_ms"] = g(h, "pcss_poisson", "ms_per_frame_8_lights")
         out["heavy_rbsm_ms"] = g(h, "rbsm_smsr", "ms_per_frame_8_lights")
         out["heavy_volumes_ms"] = g(h, "shadow_volumes", "ms_per_frame_8_lights")
+        out["heavy_volumes_silhouette_ms"] = g(h, "shadow_volumes_silhouette", "ms_per_frame_8_lights")
+        hs = h.get("shadow_volumes_silhouette") or {}
+        if hs.get("pixels_differing_from_exact_per_light"):
+            out["heavy_silhouette_max_differing_px"] = max(hs["pixels_differing_from_exact_per_light"])
     a = line.get("area_light_ground_truth")
     if a:
         out["area_289_maps_ms"] = _r(a["ms"], 3)

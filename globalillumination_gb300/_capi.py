@@ -206,6 +206,8 @@ _PROTOS = {
     "gi_shadow_volume_counts": (C.c_int, [_VP, _VP, F3, C.c_float, F16, C.c_int, C.c_int, C.c_int,
                                           _VP, _VP, _VP]),
     "gi_shadow_volume_geometry": (C.c_int, [_VP, _VP, F3, C.c_float, _VP, _VP]),
+    "gi_shadow_volume_counts_silhouette": (C.c_int, [_VP, _VP, F3, C.c_float, F16, C.c_int, C.c_int, C.c_int,
+                                                     _VP, _VP, C.POINTER(C.c_int), _VP]),
     "gi_light_map_minmax": (C.c_int, [_VP, _VP, C.c_int, C.c_int, _VP, _VP]),
     "gi_phong_shade": (C.c_int, [_VP, C.POINTER(VisParams), _VP, _VP, _VP, _VP, C.c_int, C.c_int, _VP, _VP]),
     "gi_pba_voronoi": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP]),

@@ -143,6 +143,7 @@ extern "C" void gi_context_destroy(gi_context* c) {
     cudaFree(c->d_pba_near);
     cudaFree(c->d_edt_meanx);
     cudaFree(c->d_pyr);
+    cudaFree(c->d_sil_list);
     for (int i = 0; i < 8; ++i) cudaFree(c->bin_buf[i]);
     for (int k = 0; k < 2; ++k)
         for (int i = 0; i < 8; ++i) cudaFree(c->tier_buf[k][i]);
@@ -200,8 +201,23 @@ extern "C" void gi_scene_destroy(gi_scene* s) {
         cudaFree(s->d_points);
         cudaFree(s->d_normals);
         cudaFree(s->d_indices);
+        cudaFree(s->d_adj);
     }
     delete s;
+}
+
+// A failed upload leaves no usable device copy: free what is left and mark
+// the scene, so that passes refuse it until it is uploaded again.
+static gi_status drop_device_copy(gi_scene* s, gi_status st) {
+    cudaFree(s->d_points);
+    cudaFree(s->d_normals);
+    cudaFree(s->d_indices);
+    s->d_points = s->d_normals = nullptr;
+    s->d_indices = nullptr;
+    s->cap_vertices = s->cap_triangles = 0;
+    s->dev_vertices = s->dev_triangles = 0;
+    s->upload_failed = true;
+    return st;
 }
 
 extern "C" gi_status gi_scene_upload(gi_scene* s, gi_context* ctx, void* stream) {
@@ -214,9 +230,13 @@ extern "C" gi_status gi_scene_upload(gi_scene* s, gi_context* ctx, void* stream)
         cudaFree(s->d_points);
         cudaFree(s->d_normals);
         cudaFree(s->d_indices);
+        cudaFree(s->d_adj);
         s->d_points = s->d_normals = nullptr;
         s->d_indices = nullptr;
+        s->d_adj = nullptr;
         s->cap_vertices = s->cap_triangles = 0;
+        s->cap_adj = 0;
+        s->adj_serial = ~0ull;
     }
     s->device = ctx->device;
     size_t capv = s->cap_vertices * 3 * sizeof(float), capn = capv;
@@ -226,7 +246,7 @@ extern "C" gi_status gi_scene_upload(gi_scene* s, gi_context* ctx, void* stream)
         st = gi::ensure_buffer(reinterpret_cast<void**>(&s->d_normals), &capn, nv * 3 * sizeof(float));
     if (st == GI_OK)
         st = gi::ensure_buffer(reinterpret_cast<void**>(&s->d_indices), &capi, nt * 3 * sizeof(int));
-    if (st != GI_OK) return st;
+    if (st != GI_OK) return drop_device_copy(s, st);
     s->cap_vertices = capv / (3 * sizeof(float));
     s->cap_triangles = capi / (3 * sizeof(int));
     cudaError_t e = cudaSuccess;
@@ -243,6 +263,8 @@ extern "C" gi_status gi_scene_upload(gi_scene* s, gi_context* ctx, void* stream)
     if (e != cudaSuccess) return gi::fail_cuda(e, "gi_scene_upload copy");
     s->dev_vertices = (int)nv;
     s->dev_triangles = (int)nt;
+    s->upload_failed = false;
+    s->upload_serial++;
     return GI_OK;
 }
 
@@ -259,9 +281,13 @@ extern "C" gi_status gi_scene_upload_from(gi_scene* s, gi_context* ctx, const fl
         cudaFree(s->d_points);
         cudaFree(s->d_normals);
         cudaFree(s->d_indices);
+        cudaFree(s->d_adj);
         s->d_points = s->d_normals = nullptr;
         s->d_indices = nullptr;
+        s->d_adj = nullptr;
         s->cap_vertices = s->cap_triangles = 0;
+        s->cap_adj = 0;
+        s->adj_serial = ~0ull;
     }
     s->device = ctx->device;
     size_t capv = s->cap_vertices * 3 * sizeof(float), capn = capv;
@@ -275,7 +301,7 @@ extern "C" gi_status gi_scene_upload_from(gi_scene* s, gi_context* ctx, const fl
     st = gi::ensure_buffer(reinterpret_cast<void**>(&s->d_points), &capv, vb);
     if (st == GI_OK) st = gi::ensure_buffer(reinterpret_cast<void**>(&s->d_normals), &capn, vb);
     if (st == GI_OK) st = gi::ensure_buffer(reinterpret_cast<void**>(&s->d_indices), &capi, ib);
-    if (st != GI_OK) return st;
+    if (st != GI_OK) return drop_device_copy(s, st);
     s->cap_vertices = capv / (3 * sizeof(float));
     s->cap_triangles = capi / (3 * sizeof(int));
     cudaError_t e = cudaSuccess;
@@ -285,6 +311,8 @@ extern "C" gi_status gi_scene_upload_from(gi_scene* s, gi_context* ctx, const fl
     if (e != cudaSuccess) return gi::fail_cuda(e, "gi_scene_upload_from copy");
     s->dev_vertices = nv;
     s->dev_triangles = nt;
+    s->upload_failed = false;
+    s->upload_serial++;
     return GI_OK;
 }
 
@@ -384,6 +412,7 @@ extern "C" gi_status gi_frame_setup(const gi_view* light, const gi_view* camera,
 static gi_status check_pass(gi_context* ctx, const gi_scene* s) {
     if (!ctx) return fail(GI_ERR_INVALID_ARG, "context is NULL");
     if (!s) return fail(GI_ERR_INVALID_ARG, "scene is NULL");
+    if (s->upload_failed) return fail(GI_ERR_INVALID_ARG, "the scene's last upload failed: upload it again");
     if (s->dev_triangles > 0 && (s->device != ctx->device || !s->d_points))
         return fail(GI_ERR_INVALID_ARG, "scene is not uploaded to the context's device");
     if (s->dev_triangles == 0 && s->mesh.num_triangles() > 0)
@@ -1131,4 +1160,22 @@ extern "C" gi_status gi_debug_fail_allocation(int countdown) {
     if (countdown < -1) return fail(GI_ERR_INVALID_ARG, "gi_debug_fail_allocation: countdown must be >= -1");
     gi::g_alloc_countdown.store(countdown);
     return GI_OK;
+}
+
+extern "C" gi_status gi_shadow_volume_counts_silhouette(gi_context* ctx, const gi_scene* s,
+                                                        const float light_pos[3], float infinity,
+                                                        const float camera_mvp[16], int W, int H,
+                                                        int depth_func, uint8_t* d_stencil, float* d_depth,
+                                                        int* volume_triangles, void* stream) {
+    gi_status st = check_pass(ctx, s);
+    if (st != GI_OK) return st;
+    if (!light_pos || !camera_mvp || !d_stencil)
+        return fail(GI_ERR_INVALID_ARG, "gi_shadow_volume_counts_silhouette: NULL argument");
+    st = check_image(W, H, "gi_shadow_volume_counts_silhouette");
+    if (st != GI_OK) return st;
+    if (depth_func != GI_DEPTH_LESS && depth_func != GI_DEPTH_LEQUAL)
+        return fail(GI_ERR_INVALID_ARG, "gi_shadow_volume_counts_silhouette: bad depth_func");
+    return gi::raster_shadow_volumes(ctx, s, light_pos, infinity, camera_mvp, W, H, depth_func, d_stencil,
+                                     d_depth, small_px_default(), static_cast<cudaStream_t>(stream), true,
+                                     volume_triangles);
 }

@@ -62,6 +62,13 @@ struct gi_scene {
     size_t cap_triangles = 0;
     int dev_vertices = 0;
     int dev_triangles = 0;
+    bool upload_failed = false;  // the last upload ran out of memory: no usable device copy
+    uint64_t upload_serial = 0;  // bumped by every upload
+    // silhouette mode of the shadow volumes: per triangle edge, the
+    // neighbouring triangle across it (see gi_shadow_volume_counts_silhouette)
+    int* d_adj = nullptr;
+    size_t cap_adj = 0;
+    uint64_t adj_serial = ~0ull;  // upload_serial the adjacency was built for
 };
 
 // Device scratch owned by a context.  Buffers only grow.
@@ -100,7 +107,8 @@ struct gi_context {
     // items), [32..55] counters of the tiered light-map pass, [64..87] of
     // the tiered camera-key pass (the two passes may run concurrently),
     // [96] rows of the PBA row pass colored by the exact group chain,
-    // [100] error bits of the min-max pyramid (bit 0: a copy wait ran out)
+    // [100] error bits of the min-max pyramid (bit 0: a copy wait ran out),
+    // [101] volume triangles kept by the silhouette mode
     unsigned int* d_status = nullptr;
     unsigned int* h_status = nullptr;  // pinned mirror
     // area-light ground truth: a wave of sample light maps, per-pixel sums
@@ -130,6 +138,10 @@ struct gi_context {
     // min-max pyramid of the light map (float2 levels 1..6), status word 100
     void* d_pyr = nullptr;
     size_t cap_pyr = 0;
+    // silhouette mode of the shadow volumes: the volume triangles to draw
+    // (count in status word 101)
+    void* d_sil_list = nullptr;
+    size_t cap_sil_list = 0;
     // second stream for the camera-key pass of gi_render_frame, and the
     // fork / join events (cudaStream_t / cudaEvent_t)
     void* aux_stream = nullptr;

@@ -87,6 +87,7 @@ struct RasterArgs {
     unsigned* counters;  // [0] records requested, [1] spilled to in-thread
     unsigned long long* tile_total;
     int small_px;
+    const int* prim_list;  // stencil: the volume triangles to draw (nullptr: all 6T)
 };
 
 __device__ __forceinline__ void load_vertex(const float* p, int idx, float out[3]) {
@@ -107,6 +108,7 @@ __device__ __forceinline__ void prim_vertices(const RasterArgs& a, int prim, flo
 #pragma unroll
         for (int j = 0; j < 3; ++j) load_vertex(a.points, __ldg(tri + j), v[j]);
     } else {
+        if (a.prim_list) prim = __ldg(a.prim_list + prim);
         int t = prim / 6, k = prim - t * 6;
         const int* tri = a.indices + 3 * (size_t)t;
         int i0 = __ldg(tri), i1 = __ldg(tri + 1), i2 = __ldg(tri + 2);
@@ -150,6 +152,68 @@ __global__ void __launch_bounds__(256) k_volume_geometry(RasterArgs a, float* ou
     for (int j = 0; j < 3; ++j)
 #pragma unroll
         for (int ax = 0; ax < 3; ++ax) o[j * 3 + ax] = v[j][ax];
+}
+
+// Winding pattern ShadowVolume::build picks for triangle t: the sign of
+// dot((n0 + n1 + n2) / 3, L) (ShadowVolume.cpp:55-61), computed as
+// prim_vertices computes it.
+__device__ __forceinline__ bool volume_pattern_a(const float* normals, const int* indices, int t, const float L[3]) {
+    const int* tri = indices + 3 * (size_t)t;
+    float n0[3], n1[3], n2[3];
+    load_vertex(normals, __ldg(tri), n0);
+    load_vertex(normals, __ldg(tri + 1), n1);
+    load_vertex(normals, __ldg(tri + 2), n2);
+    float n[3];
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) n[ax] = ((n0[ax] + n1[ax]) + n2[ax]) / 3.0f;
+    return n[0] * L[0] + n[1] * L[1] + n[2] * L[2] >= 0.0f;
+}
+
+// Silhouette extraction over the volume's quads.  Edge k of triangle t
+// owns volume triangles 6t + 2k and 6t + 2k + 1 (one quad) in either
+// pattern.  adj[3t + k] is the neighbouring triangle across that edge
+// (value >> 1) and whether it runs the edge in the same direction
+// (value & 1), or -1 for a boundary or non-manifold edge.  The two quads of
+// a shared edge span the same four points; they have opposite orientations
+// -- and would cancel -- when the triangles run the edge in opposite
+// directions and pick the same pattern, or run it in the same direction and
+// pick different ones.  Every other quad is a silhouette quad.  One thread
+// per edge; each warp compacts its silhouette quads with one ballot and one
+// atomic.
+__global__ void __launch_bounds__(256) k_silhouette_prims(const float* __restrict__ normals,
+                                                          const int* __restrict__ indices,
+                                                          const int* __restrict__ adj, int num_tris, float Lx,
+                                                          float Ly, float Lz, int* __restrict__ list,
+                                                          unsigned* __restrict__ count) {
+    const float L[3] = {Lx, Ly, Lz};
+    const int lane = threadIdx.x & 31;
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool emit_quad = false;
+    int t = 0, k = 0;
+    if (e < 3LL * num_tris) {
+        t = (int)(e / 3);
+        k = (int)(e - 3LL * t);
+        const int nb = __ldg(adj + e);
+        if (nb < 0) {
+            emit_quad = true;
+        } else {
+            const bool pa = volume_pattern_a(normals, indices, t, L);
+            const bool pb = volume_pattern_a(normals, indices, nb >> 1, L);
+            const bool cancel = (nb & 1) ? (pa != pb) : (pa == pb);
+            emit_quad = !cancel;
+        }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, emit_quad);
+    if (m == 0) return;
+    const int leader = __ffs(m) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(count, 2u * (unsigned)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (emit_quad) {
+        const unsigned off = base + 2u * (unsigned)__popc(m & ((1u << lane) - 1u));
+        list[off] = 6 * t + 2 * k;
+        list[off + 1] = 6 * t + 2 * k + 1;
+    }
 }
 
 template <int MODE>
@@ -1938,10 +2002,63 @@ gi_status raster_volume_geometry(gi_context* ctx, const gi_scene* scene, const f
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "volume geometry launch");
 }
 
+// Adjacency of the scene's triangles for the silhouette mode, built on the
+// host from the uploaded indices and cached until the next upload:
+// adj[3t + k] = (u << 1) | same for the triangle u sharing edge k of t
+// (vertices k, k + 1 mod 3), same = 1 when u runs the edge in the same
+// direction; -1 for an edge with one triangle or more than two.
+static gi_status ensure_adjacency(gi_scene* scene, cudaStream_t st) {
+    if (scene->adj_serial == scene->upload_serial && scene->d_adj) return GI_OK;
+    const int T = scene->dev_triangles;
+    std::vector<int> idx(3 * (size_t)T);
+    cudaError_t e = cudaSuccess;
+    if (T) e = cudaMemcpyAsync(idx.data(), scene->d_indices, idx.size() * sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail_cuda(e, "silhouette adjacency: index read-back");
+    struct HalfEdge {
+        unsigned long long key;  // (min vertex << 32) | max vertex
+        int slot;                // 3t + k
+    };
+    std::vector<HalfEdge> he(3 * (size_t)T);
+    for (int t = 0; t < T; ++t)
+        for (int k = 0; k < 3; ++k) {
+            const unsigned a = (unsigned)idx[3 * (size_t)t + k], b = (unsigned)idx[3 * (size_t)t + (k + 1) % 3];
+            const unsigned lo = a < b ? a : b, hi = a < b ? b : a;
+            he[3 * (size_t)t + k] = {((unsigned long long)lo << 32) | hi, 3 * t + k};
+        }
+    std::sort(he.begin(), he.end(), [](const HalfEdge& x, const HalfEdge& y) {
+        return x.key < y.key || (x.key == y.key && x.slot < y.slot);
+    });
+    std::vector<int> adj(3 * (size_t)T, -1);
+    for (size_t i = 0; i < he.size();) {
+        size_t j = i + 1;
+        while (j < he.size() && he[j].key == he[i].key) ++j;
+        if (j - i == 2 && (he[i].key >> 32) != (he[i].key & 0xffffffffull)) {
+            const int s0 = he[i].slot, s1 = he[i + 1].slot;
+            const int t0 = s0 / 3, k0 = s0 % 3, t1 = s1 / 3, k1 = s1 % 3;
+            const bool fwd0 = idx[3 * (size_t)t0 + k0] < idx[3 * (size_t)t0 + (k0 + 1) % 3];
+            const bool fwd1 = idx[3 * (size_t)t1 + k1] < idx[3 * (size_t)t1 + (k1 + 1) % 3];
+            const int same = fwd0 == fwd1 ? 1 : 0;
+            adj[s0] = (t1 << 1) | same;
+            adj[s1] = (t0 << 1) | same;
+        }
+        i = j;
+    }
+    size_t cap = scene->cap_adj;
+    gi_status s = ensure_buffer(reinterpret_cast<void**>(&scene->d_adj), &cap, std::max<size_t>(adj.size(), 1) * sizeof(int));
+    if (s != GI_OK) return s;
+    scene->cap_adj = cap;
+    if (T) e = cudaMemcpyAsync(scene->d_adj, adj.data(), adj.size() * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // adj is a local vector
+    if (e != cudaSuccess) return fail_cuda(e, "silhouette adjacency: upload");
+    scene->adj_serial = scene->upload_serial;
+    return GI_OK;
+}
+
 gi_status raster_shadow_volumes(gi_context* ctx, const gi_scene* scene, const float L[3],
                                 float infinity, const float mvp[16], int W, int H, int depth_func,
                                 unsigned char* d_stencil, float* d_depth_out, int small_px,
-                                cudaStream_t st) {
+                                cudaStream_t st, bool silhouette, int* drawn) {
     const size_t npx = (size_t)W * H;
     float* depth = d_depth_out;
     gi_status s;
@@ -1972,6 +2089,31 @@ gi_status raster_shadow_volumes(gi_context* ctx, const gi_scene* scene, const fl
     a.infinity = infinity;
     a.depth = reinterpret_cast<unsigned*>(depth);
     a.counts = ctx->d_counts;
+    if (silhouette) {
+        // Only the silhouette quads are drawn (k_silhouette_prims); their
+        // number is read back to size the binned pass.
+        s = ensure_adjacency(const_cast<gi_scene*>(scene), st);
+        if (s != GI_OK) return s;
+        s = ensure_buffer(&ctx->d_sil_list, &ctx->cap_sil_list,
+                          std::max<size_t>((size_t)a.num_prims, 1) * sizeof(int));
+        if (s != GI_OK) return s;
+        unsigned* count = ctx->d_status + 101;
+        cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned), st);
+        if (e != cudaSuccess) return fail_cuda(e, "silhouette count reset");
+        const long long edges = 3LL * scene->dev_triangles;
+        if (edges > 0) {
+            dev::k_silhouette_prims<<<grid_for((size_t)edges, 256), 256, 0, st>>>(
+                scene->d_normals, scene->d_indices, scene->d_adj, scene->dev_triangles, L[0], L[1], L[2],
+                static_cast<int*>(ctx->d_sil_list), count);
+            ctx->launches++;
+        }
+        e = cudaMemcpyAsync(ctx->h_status + 101, count, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return fail_cuda(e, "silhouette count read-back");
+        a.num_prims = (int)ctx->h_status[101];
+        a.prim_list = static_cast<const int*>(ctx->d_sil_list);
+    }
+    if (drawn) *drawn = a.num_prims;
     s = run_binned(ctx, a, dev::MODE_STENCIL, st);
     if (s != GI_OK) return s;
     dev::k_wrap_stencil<<<grid_for(npx, 256), 256, 0, st>>>(ctx->d_counts, d_stencil, npx);

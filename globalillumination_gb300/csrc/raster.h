@@ -22,7 +22,7 @@ gi_status raster_volume_geometry(gi_context* ctx, const gi_scene* scene, const f
 gi_status raster_shadow_volumes(gi_context* ctx, const gi_scene* scene, const float L[3],
                                 float infinity, const float mvp[16], int W, int H, int depth_func,
                                 unsigned char* d_stencil, float* d_depth_out, int small_px,
-                                cudaStream_t st);
+                                cudaStream_t st, bool silhouette = false, int* drawn = nullptr);
 
 // G-buffer visibility keys only (into ctx->d_vkeys), no resolve.
 gi_status raster_gbuffer_keys(gi_context* ctx, const gi_scene* scene, const float mvp[16], int W,

@@ -1007,10 +1007,18 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
     }
 }
 
+// Loss sums in fixed point: |v - t| and |e - |v - t|| scaled by 2^32 and
+// rounded per pixel, the pixel count as an integer.  Integer additions are
+// exact, so the totals do not depend on the order in which blocks finish
+// (the reported loss of a run is reproducible bit for bit).
+__device__ __forceinline__ unsigned long long to_fixed32(float v) {
+    return __float2ull_rn(fminf(v, 1.0e6f) * 4294967296.0f);
+}
+
 __global__ void k_surrogate_loss(const float* __restrict__ head, const float* __restrict__ target,
                                  const uint4* __restrict__ feat, long long P, float inv, float ew,
-                                 uint16_t* __restrict__ dhead, float* __restrict__ sums) {
-    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+                                 uint16_t* __restrict__ dhead, unsigned long long* __restrict__ sums) {
+    unsigned long long s0 = 0, s1 = 0, s2 = 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < P; i += (long long)gridDim.x * blockDim.x) {
         const float f3 = __uint_as_float(feat[2 * i].y & 0xFFFF0000u);
         float g0 = 0.0f, g1 = 0.0f;
@@ -1021,9 +1029,9 @@ __global__ void k_surrogate_loss(const float* __restrict__ head, const float* __
             g0 = (d > 0.0f ? 1.0f : d < 0.0f ? -1.0f : 0.0f) * inv;
             const float de = e - ad;
             g1 = (de > 0.0f ? ew : de < 0.0f ? -ew : 0.0f) * inv;
-            s0 += ad;
-            s1 += 1.0f;
-            s2 += fabsf(de);
+            s0 += to_fixed32(ad);
+            s1 += 1;
+            s2 += to_fixed32(fabsf(de));
         }
         uint4* o = reinterpret_cast<uint4*>(dhead + i * 16);
         o[0] = make_uint4((uint32_t)f_to_bf16(g0) | ((uint32_t)f_to_bf16(g1) << 16), 0u, 0u, 0u);
@@ -1361,12 +1369,12 @@ extern "C" gi_status gi_adam_f32(float* p, const float* g, float* m, float* v, s
 }
 
 extern "C" gi_status gi_surrogate_loss(const float* d_head, const float* d_target, const void* d_feat, size_t pixels,
-                                       float err_weight, gi_bf16* d_dhead, float* d_sums, void* stream) {
+                                       float err_weight, gi_bf16* d_dhead, uint64_t* d_sums, void* stream) {
     if (!d_head || !d_target || !d_feat || !d_dhead || !d_sums || pixels == 0)
         return fail(GI_ERR_INVALID_ARG, "gi_surrogate_loss: bad arguments");
     tc::k_surrogate_loss<<<tc::grid1d((long long)pixels, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
         d_head, d_target, static_cast<const uint4*>(d_feat), (long long)pixels, 1.0f / (float)pixels, err_weight,
-        d_dhead, d_sums);
+        d_dhead, reinterpret_cast<unsigned long long*>(d_sums));
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_surrogate_loss launch");
 }

@@ -86,6 +86,10 @@ struct Ctx {
 struct PoissonOffsets {
     float2 b[64];
     float2 bmin, bmax, fmin, fmax;
+    // PCF: the first and last offsets of the tap loop (in texels) and the
+    // number of taps (0: no skipping)
+    float pcf_lo, pcf_hi;
+    int pcf_count;
     Pyramid pyr;
 };
 
@@ -184,6 +188,19 @@ template <bool FAST>
 __device__ float pcf_bilinear_t(const gi_vis_params& p, const Ctx& c, V4 n) {
     float incrW = 1.0f / c.fW, incrH = 1.0f / c.fH;
     float illum = 0.0f;
+    if (FAST && c.tab && c.tab->pyr.levels > 0 && c.tab->pcf_count > 0) {
+        // the loop's offsets increase from pcf_lo to pcf_hi; incr > 0
+        const float lo = c.tab->pcf_lo, hi = c.tab->pcf_hi;
+        float mn, mx;
+        if (tap_box_minmax(c, n.x + lo * incrW, n.x + hi * incrW, n.y + lo * incrH, n.y + hi * incrH, mn, mx)) {
+            const int count = c.tab->pcf_count;
+            if (n.z <= mn) return 1.0f;  // every tap lit: count additions of 1, over count
+            if (n.z > mx) {              // every tap shadowed
+                for (int k = 0; k < count; ++k) illum += c.I;
+                return illum / (float)count;
+            }
+        }
+    }
     float offset = (float)p.penumbra_size;
     float step = 2.0f * offset / (float)p.kernel_order;
     int count = 0;
@@ -1617,7 +1634,7 @@ __global__ void __launch_bounds__(128) k_visibility(const gi_vis_params p,
     c.I = p.shadow_intensity;
     c.sm = sm;
     c.boff = TECH == GI_TECH_PCSS_POISSON ? po.b : nullptr;
-    c.tab = TECH == GI_TECH_PCSS_POISSON ? &po : nullptr;
+    c.tab = (TECH == GI_TECH_PCSS_POISSON || TECH == GI_TECH_PCF) ? &po : nullptr;
     size_t i = (size_t)y * W + x;
     float4 pv = __ldcs(pos + i);
     float4 nv = __ldcs(nrm + i);
@@ -1649,7 +1666,7 @@ __global__ void __launch_bounds__(128, 10) k_frame_visibility(
     Ctx c;
     c.sm = sm;
     c.boff = TECH == GI_TECH_PCSS_POISSON ? po.b : nullptr;
-    c.tab = TECH == GI_TECH_PCSS_POISSON ? &po : nullptr;
+    c.tab = (TECH == GI_TECH_PCSS_POISSON || TECH == GI_TECH_PCF) ? &po : nullptr;
     c.map = map;
     c.W = map_w;
     c.H = map_h;
@@ -2093,6 +2110,25 @@ gi_status launch_area_accumulate(gi_context* ctx, const gi_scene* scene, const f
 // the kernel's multiplication would round it.
 static vis::PoissonOffsets poisson_offsets(const gi_vis_params* p, int map_w) {
     vis::PoissonOffsets po{};
+    if (p->technique == GI_TECH_PCF) {
+        // the offsets of Shadow.frag's float loop (:86-116), as the kernel's
+        // loop produces them
+        const float offset = (float)p->penumbra_size;
+        const float step = 2.0f * offset / (float)p->kernel_order;
+        int n = 0;
+        float last = -offset;
+        if (step > 0.0f)
+            for (float w = -offset; w < offset && n <= 64; w += step) {
+                last = w;
+                ++n;
+            }
+        if (n >= 1 && n <= 64) {
+            po.pcf_lo = -offset;
+            po.pcf_hi = last;
+            po.pcf_count = n * n;
+        }
+        return po;
+    }
     if (p->technique != GI_TECH_PCSS_POISSON) return po;
     const float fw = (float)map_w;
     const float bsw = fw <= 1024.0f ? p->light_radius / fw : p->light_radius / 1024.0f;
@@ -2110,12 +2146,14 @@ static vis::PoissonOffsets poisson_offsets(const gi_vis_params* p, int map_w) {
     return po;
 }
 
-// PCSS_POISSON reads the light map's min-max pyramid to skip taps exactly
-// (square-tile maps only; the others run every tap).
+// PCSS_POISSON and PCF read the light map's min-max pyramid to skip taps
+// exactly (maps with sides that are multiples of 64; others run every tap).
 static gi_status prepare_pyramid(gi_context* ctx, const gi_vis_params* p, const float* d_depth, int map_w,
                                  int map_h, cudaStream_t st, vis::PoissonOffsets* po) {
-    if (p->technique != GI_TECH_PCSS_POISSON || p->poisson_blocker_taps < 1 || p->poisson_filter_taps < 1)
-        return GI_OK;
+    const bool pcss = p->technique == GI_TECH_PCSS_POISSON && p->poisson_blocker_taps >= 1 &&
+                      p->poisson_filter_taps >= 1;
+    const bool pcf = p->technique == GI_TECH_PCF && po->pcf_count > 0;
+    if (!pcss && !pcf) return GI_OK;
     return launch_minmax_pyramid(ctx, d_depth, map_w, map_h, st, &po->pyr);
 }
 

@@ -417,6 +417,20 @@ def shadow_volume_counts(ctx: Context, scene: Scene, light_pos, camera_mvp, widt
     return stencil
 
 
+def shadow_volume_counts_silhouette(ctx: Context, scene: Scene, light_pos, camera_mvp, width: int, height: int,
+                                    stencil, depth=None, depth_func: int = api.GI_DEPTH_LEQUAL,
+                                    infinity: float = 100.0, stream=None) -> int:
+    """The stencil passes with silhouette extraction (opt-in, see gi_shadow.h): fills stencil
+    and returns the number of volume triangles drawn."""
+    assert stencil.is_cuda and stencil.numel() >= width * height
+    drawn = C.c_int(0)
+    check(_lib().gi_shadow_volume_counts_silhouette(ctx.handle, scene.handle, _f3(light_pos), float(infinity),
+                                                    _f16(camera_mvp), width, height, int(depth_func), _ptr(stencil),
+                                                    _ptr(depth) if depth is not None else None, C.byref(drawn),
+                                                    _stream_ptr(stream)), "gi_shadow_volume_counts_silhouette")
+    return drawn.value
+
+
 def shadow_volume_geometry(ctx: Context, scene: Scene, light_pos, out, infinity: float = 100.0, stream=None):
     """ShadowVolume::build's triangles as the stencil pass draws them: out is a float32
     CUDA tensor of 6T * 9 values (entry 6t + k = side k of triangle t, three vertices)."""

@@ -296,10 +296,19 @@ def finish(ctx: Context, scene: Scene, frame: Frame, mp: MapParams, params: Shad
 
 def loss(head: torch.Tensor, target: torch.Tensor, feat: torch.Tensor, dhead: torch.Tensor, sums: torch.Tensor,
          err_weight: float = 0.5) -> None:
+    """L1 loss of the visibility head plus the error head; writes dhead and adds the fixed-point
+    totals to sums (int64 [3], see loss_totals)."""
+    assert sums.dtype == torch.int64 and sums.numel() >= 3
     pixels = target.numel()
     check(api.load().gi_surrogate_loss(_ptr(head), _ptr(target), _ptr(feat), pixels, float(err_weight), _ptr(dhead),
                                        _ptr(sums), C.c_void_p(int(torch.cuda.current_stream().cuda_stream))),
           "gi_surrogate_loss")
+
+
+def loss_totals(sums: torch.Tensor) -> np.ndarray:
+    """(sum |v - t|, pixel count, sum error-head loss) as float64 from the fixed-point sums."""
+    s = sums.cpu().numpy().astype(np.float64)
+    return np.array([s[0] / 2.0 ** 32, s[1], s[2] / 2.0 ** 32])
 
 
 class SurrogateFrame:
@@ -430,7 +439,7 @@ class Trainer:
         self.btarget = torch.empty((batch, crop, crop), dtype=torch.float32, device=dev)
         self.head = torch.empty((batch, crop, crop, HEAD), dtype=torch.float32, device=dev)
         self.dhead = torch.empty((batch, crop, crop, HEAD), dtype=torch.bfloat16, device=dev)
-        self.sums = torch.zeros(3, dtype=torch.float32, device=dev)
+        self.sums = torch.zeros(3, dtype=torch.int64, device=dev)  # fixed point, see loss()
 
     def _buffers(self, side, W, H):
         from .shadow import allocate_frame
@@ -472,7 +481,7 @@ class Trainer:
             net.adam_step(self.lr)
             self.step += 1
             if self.step % log_every == 0 or self.step == last:
-                s_ = self.sums.cpu().numpy()
+                s_ = loss_totals(self.sums)
                 hist.append({"step": self.step, "mae": float(s_[0] / max(s_[1], 1.0)),
                              "err_l1": float(s_[2] / max(s_[1], 1.0)), "seconds": time.perf_counter() - t0})
                 if verbose:

@@ -584,6 +584,30 @@ gi_status gi_shadow_volume_counts(gi_context* ctx, const gi_scene* scene,
                                   uint8_t* d_stencil, float* d_depth,
                                   void* stream);
 
+/* The same frame with silhouette extraction (opt-in; no counterpart in the
+ * reference, which extrudes every triangle).  Each edge shared by two
+ * triangles gets two coplanar volume quads over the same four points; when
+ * their orientations are opposite (the triangles pick the same winding
+ * pattern and run the edge in opposite directions, or the other way round)
+ * they cancel, and both are left out: only the silhouette quads -- boundary
+ * and non-manifold edges, and shared edges whose quads do not cancel -- are
+ * rasterised, found one thread per edge and compacted per warp with a
+ * ballot.  The counts equal gi_shadow_volume_counts' except at pixels where
+ * a cancelling pair's two triangulations (different diagonals, different
+ * near-plane clips) round the fragment depth or coverage differently, which
+ * happens along the receivers' contact with the occluders; tests and the
+ * benchmark count those pixels against the exact path.  The first call
+ * after a scene upload builds the edge adjacency on the host (cached), and
+ * every call reads the number of silhouette triangles back (a stream
+ * synchronisation).  *volume_triangles (may be NULL) receives the number of
+ * volume triangles drawn (6T for the exact path). */
+gi_status gi_shadow_volume_counts_silhouette(gi_context* ctx, const gi_scene* scene,
+                                             const float light_pos[3], float infinity,
+                                             const float camera_mvp[16], int width,
+                                             int height, int depth_func,
+                                             uint8_t* d_stencil, float* d_depth,
+                                             int* volume_triangles, void* stream);
+
 /* ShadowVolume::build / update (ShadowVolumes/src/ShadowVolume.cpp:15-194,
  * infinity 100 at ShadowVolumes/src/main.cpp:469-470) for callers that draw
  * the volumes themselves: the 6T volume triangles exactly as

@@ -130,9 +130,12 @@ gi_status gi_surrogate_finish(gi_context* ctx, const gi_scene* scene, int map_wi
  * is 1, plus L1 of the error head (channel 1) against the current
  * |visibility - target|.  Writes dhead (BF16 [pixels][16], gradient of
  * the mean loss, other channels 0) and adds {sum |v - t|, pixel count,
- * sum error-head loss} to sums[0..2]. */
+ * sum error-head loss} to sums[0..2] in fixed point: sums[0] and sums[2]
+ * in units of 2^-32 (each pixel's term rounded once, terms above 1e6
+ * clamped), sums[1] an integer count.  The additions are exact integer
+ * ones, so the totals do not depend on the order of the GPU's blocks. */
 gi_status gi_surrogate_loss(const float* d_head, const float* d_target, const void* d_feat, size_t pixels,
-                            float err_weight, gi_bf16* d_dhead, float* d_sums, void* stream);
+                            float err_weight, gi_bf16* d_dhead, uint64_t* d_sums, void* stream);
 
 /* Adam step on FP32 master weights p with gradient g (both n floats), then
  * the BF16 copy is refreshed by the caller with gi_pack_conv_weights. */

@@ -68,7 +68,7 @@ def test_unet_gradients_match_torch():
     target = torch.rand(n, H, W, generator=g) * 0.75 + 0.25
     head = net.forward(f.cuda(), keep=True)
     dhead = torch.empty((n, H, W, sg.HEAD), dtype=torch.bfloat16, device="cuda")
-    sums = torch.zeros(3, device="cuda")
+    sums = torch.zeros(3, dtype=torch.int64, device="cuda")
     sg.loss(head, target.cuda(), f.cuda(), dhead, sums, err_weight=0.5)
     net.backward(dhead)
     torch.cuda.synchronize()
