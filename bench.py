@@ -344,6 +344,38 @@ def run_batched(args, ctx, stream, local, rank=0, world=1, dist=None):
     torch.cuda.synchronize()
     single_ms = replicas.max_over_ranks(e0.elapsed_time(e1), dist, torch.device("cuda", local))
     info = b.info()
+    # persistent mode: every map and G-buffer resident, one persistent
+    # visibility launch over all (light-frame, tile) items; the tile size is
+    # swept with the tier thresholds and stream count the graph mode chose
+    pers = {}
+    for tw, th in ((32, 4), (64, 4), (64, 8), (128, 8), (256, 8), (128, 16)):
+        b.build_persistent(tune["streams"], tw, th)
+        b.run(stream)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(R):
+            b.run(stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        pers[f"{tw}x{th}"] = replicas.max_over_ranks(e0.elapsed_time(e1) / R, dist, torch.device("cuda", local))
+    best_tile = min(pers, key=pers.get)
+    tw, th = (int(v) for v in best_tile.split("x"))
+    b.build_persistent(tune["streams"], tw, th)
+    pinfo = b.info()
+    pers_ms = pers[best_tile]
+    # algorithmic bytes of one persistent batch: per frame the camera raster
+    # (vertices, indices) and the G-buffer write (32 B/px); per light-frame
+    # the map raster (vertices, indices, clear + write 8 B/texel), one read
+    # of the map (4 B/texel), the G-buffer read (32 B/px) and the visibility
+    # write (4 B/px)
+    alg = 0
+    for f in frames:
+        P = f.camera.width * f.camera.height
+        geo = 24 * f.triangles  # float3 vertices (about T / 2 of them, x2 arrays) + int3 indices, bounded by 24 T
+        alg += geo + 32 * P
+        for m in f.maps:
+            alg += geo + 12 * m.width * m.height + 36 * P
+    peak, peak_kind = measured_hbm_peak()
     b.close()
     del outs
     return {
@@ -356,6 +388,12 @@ def run_batched(args, ctx, stream, local, rank=0, world=1, dist=None):
         "tuning": {k: tune[k] for k in ("tiny_px", "coop_px", "streams")},
         "kernel_launches_per_batch": info["kernel_launches"],
         "single_frame_calls_light_frames_per_s": total_light_frames / (single_ms / 1000.0),
+        "persistent": {"light_frames_per_s": light_frames / (pers_ms / 1000.0), "ms_per_batch": pers_ms,
+                       "tile": best_tile, "ms_per_tile_size": pers, "work_items": pinfo["work_items"],
+                       "kernel_launches_per_batch": pinfo["kernel_launches"],
+                       "roofline": {"bound": "hbm", "achieved": alg / (pers_ms / 1000.0) / 1e9, "peak": peak,
+                                    "unit": "GB/s", "frac": alg / (pers_ms / 1000.0) / 1e9 / peak,
+                                    "peak_source": peak_kind, "algorithmic_bytes_per_batch": int(alg)}},
         "setup_and_autotune_s": setup_s,
         "l2": "working set (4+ GB of outputs, up to 64 MiB maps) larger than L2",
     }
@@ -1296,6 +1334,8 @@ def compact_summary(line: dict) -> dict:
     if b:
         out["720p_batch_light_frames_per_s"] = _r(b["light_frames_per_s"])
         out["720p_single_calls_light_frames_per_s"] = _r(b["single_frame_calls_light_frames_per_s"])
+        if b.get("persistent"):
+            out["720p_persistent_light_frames_per_s"] = _r(b["persistent"]["light_frames_per_s"])
     sg = line.get("surrogate")
     if sg:
         out["surrogate_frame_ms"] = _r(sg["ms_per_frame"], 3)

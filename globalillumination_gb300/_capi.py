@@ -155,6 +155,10 @@ class BatchTuning(C.Structure):
         ("frames", C.c_int),
         ("kernel_launches", C.c_uint64),
         ("best_ms", C.c_float),
+        ("persistent", C.c_int),
+        ("tile_w", C.c_int),
+        ("tile_h", C.c_int),
+        ("work_items", C.c_uint32),
     ]
 
 
@@ -229,6 +233,8 @@ _PROTOS = {
     "gi_batch_build": (C.c_int, [_VP, C.c_int]),
     "gi_batch_run": (C.c_int, [_VP, _VP]),
     "gi_batch_autotune": (C.c_int, [_VP, _VP, C.c_int, C.POINTER(BatchTuning)]),
+    "gi_batch_build_persistent": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int]),
+    "gi_batch_autotune_persistent": (C.c_int, [_VP, _VP, C.c_int, C.POINTER(BatchTuning)]),
     "gi_batch_info": (C.c_int, [_VP, C.POINTER(BatchTuning)]),
     # gi_surrogate.h
     "gi_tc_set_wait_limit": (C.c_int, [C.c_uint32]),

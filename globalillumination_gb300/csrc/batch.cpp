@@ -14,6 +14,15 @@
 // bounding boxes) and stream counts on the real batch and keeps the
 // fastest.  The reference renders one scene and one light per frame
 // (ShadowMapping/src/main.cpp:459-472); batching is new.
+//
+// Persistent mode (gi_batch_build_persistent): the graph rasterises, per
+// frame, its G-buffer into the batch's own per-frame buffers and, per
+// light, its light map into a per-light-frame buffer (every map of the
+// batch stays resident: about 27 GB for the 256-scene workload), over the
+// same streams; then one persistent launch of k_batch_visibility shades
+// every (light-frame, tile) work item of the batch from a global counter.
+// Its tile size is tuned with the tier thresholds and stream count
+// (gi_batch_autotune_persistent).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -51,12 +60,38 @@ struct gi_batch {
     int tiny_px = 96;
     int coop_px = 1024;
     uint64_t launches_per_run = 0;
+    // persistent mode
+    bool persistent = false;
+    int tile_w = 64, tile_h = 8;
+    std::vector<float*> lf_map;        // one light map per light-frame
+    std::vector<size_t> lf_map_cap;
+    std::vector<float*> fr_gbuf;       // per frame: position then normal, float4 each
+    std::vector<size_t> fr_gbuf_cap;
+    gi::BatchLightFrame* d_lf = nullptr;
+    size_t cap_lf = 0;
+    unsigned* d_queue = nullptr;
+    unsigned total_tiles = 0;
+    int n_lf = 0;
 };
 
 using gi::fail;
 using gi::fail_cuda;
 
 namespace {
+
+void release_persistent(gi_batch* b) {
+    for (auto* p : b->lf_map) cudaFree(p);
+    for (auto* p : b->fr_gbuf) cudaFree(p);
+    b->lf_map.clear();
+    b->lf_map_cap.clear();
+    b->fr_gbuf.clear();
+    b->fr_gbuf_cap.clear();
+    cudaFree(b->d_lf);
+    cudaFree(b->d_queue);
+    b->d_lf = nullptr;
+    b->d_queue = nullptr;
+    b->cap_lf = 0;
+}
 
 void release_streams(gi_batch* b) {
     for (auto* c : b->ctxs) gi_context_destroy(c);
@@ -131,6 +166,114 @@ gi_status enqueue_frame(gi_batch* b, const gi_batch_frame& f, int k) {
     return GI_OK;
 }
 
+// Persistent mode, phase A for frame i on stream slot k: its G-buffer and
+// every light's map into the batch's buffers (lf: index of its first
+// light-frame).
+gi_status enqueue_frame_persistent(gi_batch* b, size_t i, int k, int lf) {
+    const gi_batch_frame& f = b->frames[i];
+    gi_context* ctx = b->ctxs[k];
+    cudaStream_t st = b->streams[k];
+    const int W = f.camera.width, H = f.camera.height;
+    float* pos = b->fr_gbuf[i];
+    float* nrm = pos + 4 * (size_t)W * H;
+    gi_status s = gi::raster_gbuffer(ctx, f.scene, f.fm[0].camera_mvp, W, H, pos, nrm, ctx->tiny_px, st);
+    if (s != GI_OK) return s;
+    for (size_t l = 0; l < f.lights.size(); ++l) {
+        const gi_map_params& mp = f.maps[l];
+        const gi_frame_matrices& m = f.fm[l];
+        s = gi::raster_depth_map(ctx, f.scene, m.light_mvp, mp.width, mp.height, mp.bias_mode, mp.constant_bias,
+                                 mp.offset_factor, mp.offset_units, b->lf_map[lf + l], 0, st);
+        if (s != GI_OK) return s;
+    }
+    return GI_OK;
+}
+
+// Phase B on the origin stream: reset the work counter, one persistent launch.
+gi_status enqueue_visibility_persistent(gi_batch* b, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(b->d_queue, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return fail_cuda(e, "gi_batch: queue reset");
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+    const int grid = std::max(1, sms) * 8;
+    gi_status s = gi::launch_batch_visibility(b->frames[0].vis.technique, b->d_lf, b->n_lf, b->total_tiles,
+                                              b->d_queue, b->tile_w, b->tile_h, grid, st);
+    if (s == GI_OK) b->ctxs[0]->launches++;
+    return s;
+}
+
+// Sizes the per-frame G-buffers and per-light-frame maps and uploads the
+// light-frame table for the current tile size.
+gi_status prepare_persistent(gi_batch* b) {
+    const int tech = b->frames[0].vis.technique;
+    for (const auto& f : b->frames)
+        if (f.vis.technique != tech)
+            return fail(GI_ERR_UNSUPPORTED, "gi_batch_build_persistent: the frames must share one technique");
+    if (!gi::batch_visibility_supported(tech))
+        return fail(GI_ERR_UNSUPPORTED, "gi_batch_build_persistent: technique not supported (moment maps)");
+    size_t n_lf = 0;
+    for (const auto& f : b->frames) n_lf += f.lights.size();
+    b->lf_map.resize(n_lf, nullptr);
+    b->lf_map_cap.resize(n_lf, 0);
+    b->fr_gbuf.resize(b->frames.size(), nullptr);
+    b->fr_gbuf_cap.resize(b->frames.size(), 0);
+    std::vector<gi::BatchLightFrame> table;
+    table.reserve(n_lf);
+    unsigned tiles = 0;
+    size_t j = 0;
+    for (size_t i = 0; i < b->frames.size(); ++i) {
+        const gi_batch_frame& f = b->frames[i];
+        const int W = f.camera.width, H = f.camera.height;
+        gi_status s = gi::ensure_buffer(reinterpret_cast<void**>(&b->fr_gbuf[i]), &b->fr_gbuf_cap[i],
+                                        8 * sizeof(float) * (size_t)W * H);
+        if (s != GI_OK) return s;
+        for (size_t l = 0; l < f.lights.size(); ++l, ++j) {
+            const gi_map_params& mp = f.maps[l];
+            const gi_frame_matrices& m = f.fm[l];
+            s = gi::ensure_buffer(reinterpret_cast<void**>(&b->lf_map[j]), &b->lf_map_cap[j],
+                                  sizeof(float) * (size_t)mp.width * mp.height);
+            if (s != GI_OK) return s;
+            gi::BatchLightFrame e{};
+            e.p = f.vis;
+            std::memcpy(e.p.light_mvp_biased, m.light_mvp_biased, sizeof e.p.light_mvp_biased);
+            std::memcpy(e.p.camera_mv, m.camera_mv, sizeof e.p.camera_mv);
+            std::memcpy(e.p.normal_matrix, m.normal_matrix, sizeof e.p.normal_matrix);
+            std::memcpy(e.p.light_position, m.light_position, sizeof e.p.light_position);
+            e.map = b->lf_map[j];
+            e.pos = reinterpret_cast<const float4*>(b->fr_gbuf[i]);
+            e.nrm = reinterpret_cast<const float4*>(b->fr_gbuf[i] + 4 * (size_t)W * H);
+            e.out = f.d_vis + l * (size_t)W * H;
+            e.map_w = mp.width;
+            e.map_h = mp.height;
+            // shadowMapStep = (1.0 / w, 1.0 / h) in double, stored as float
+            e.sx = (float)(1.0 / (double)mp.width);
+            e.sy = (float)(1.0 / (double)mp.height);
+            e.W = W;
+            e.H = H;
+            e.tiles_x = (W + b->tile_w - 1) / b->tile_w;
+            e.tiles_y = (H + b->tile_h - 1) / b->tile_h;
+            e.tile_begin = tiles;
+            const unsigned long long nt = (unsigned long long)e.tiles_x * e.tiles_y;
+            if (tiles + nt >= (1ull << 32) - 1) return fail(GI_ERR_CAPACITY, "gi_batch_build_persistent: too many tiles");
+            tiles += (unsigned)nt;
+            table.push_back(e);
+        }
+    }
+    gi_status s = gi::ensure_buffer(reinterpret_cast<void**>(&b->d_lf), &b->cap_lf,
+                                    std::max<size_t>(table.size(), 1) * sizeof(gi::BatchLightFrame));
+    if (s != GI_OK) return s;
+    if (!b->d_queue) {
+        size_t cap = 0;
+        s = gi::ensure_buffer(reinterpret_cast<void**>(&b->d_queue), &cap, sizeof(unsigned));
+        if (s != GI_OK) return s;
+    }
+    cudaError_t e = cudaMemcpy(b->d_lf, table.data(), table.size() * sizeof(gi::BatchLightFrame),
+                               cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail_cuda(e, "gi_batch_build_persistent: light-frame table");
+    b->n_lf = (int)table.size();
+    b->total_tiles = tiles;
+    return GI_OK;
+}
+
 gi_status size_depth(gi_batch* b) {
     size_t need = 0;
     for (const auto& f : b->frames)
@@ -144,9 +287,24 @@ gi_status size_depth(gi_batch* b) {
 
 // Runs every frame once outside capture so each context's scratch reaches
 // its working size (capture must not allocate).
-gi_status dry_run(gi_batch* b) {
+gi_status enqueue_all(gi_batch* b) {
+    int lf = 0;
     for (size_t i = 0; i < b->frames.size(); ++i) {
-        gi_status s = enqueue_frame(b, b->frames[i], (int)(i % b->num_streams));
+        const int k = (int)(i % b->num_streams);
+        gi_status s = b->persistent ? enqueue_frame_persistent(b, i, k, lf) : enqueue_frame(b, b->frames[i], k);
+        if (s != GI_OK) return s;
+        lf += (int)b->frames[i].lights.size();
+    }
+    return GI_OK;
+}
+
+gi_status dry_run(gi_batch* b) {
+    gi_status s = enqueue_all(b);
+    if (s != GI_OK) return s;
+    if (b->persistent) {
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) return fail_cuda(e, "gi_batch dry run");
+        s = enqueue_visibility_persistent(b, b->streams[0]);
         if (s != GI_OK) return s;
     }
     cudaError_t e = cudaDeviceSynchronize();
@@ -163,12 +321,12 @@ gi_status capture(gi_batch* b) {
     for (int k = 1; k < b->num_streams && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(b->streams[k], b->fork, 0);
     uint64_t before = 0;
     for (auto* c : b->ctxs) before += c->launches;
-    for (size_t i = 0; i < b->frames.size() && s == GI_OK && e == cudaSuccess; ++i)
-        s = enqueue_frame(b, b->frames[i], (int)(i % b->num_streams));
+    if (e == cudaSuccess) s = enqueue_all(b);
     for (int k = 1; k < b->num_streams && e == cudaSuccess; ++k) {
         e = cudaEventRecord(b->join[k], b->streams[k]);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(origin, b->join[k], 0);
     }
+    if (b->persistent && s == GI_OK && e == cudaSuccess) s = enqueue_visibility_persistent(b, origin);
     cudaGraph_t g = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(origin, &g);
     if (s != GI_OK) {
@@ -189,7 +347,7 @@ gi_status capture(gi_batch* b) {
 
 gi_status build(gi_batch* b, int streams) {
     gi_status s = make_streams(b, streams);
-    if (s == GI_OK) s = size_depth(b);
+    if (s == GI_OK) s = b->persistent ? prepare_persistent(b) : size_depth(b);
     if (s == GI_OK) s = dry_run(b);
     if (s == GI_OK) s = capture(b);
     return s;
@@ -224,6 +382,7 @@ extern "C" void gi_batch_destroy(gi_batch* b) {
     cudaDeviceSynchronize();
     release_graph(b);
     release_streams(b);
+    release_persistent(b);
     if (b->fork) cudaEventDestroy(b->fork);
     delete b;
 }
@@ -269,6 +428,28 @@ extern "C" gi_status gi_batch_build(gi_batch* b, int streams) {
     if (b->frames.empty()) return fail(GI_ERR_INVALID_ARG, "gi_batch_build: empty batch");
     cudaError_t e = cudaSetDevice(b->device);
     if (e != cudaSuccess) return fail_cuda(e, "gi_batch_build: cudaSetDevice");
+    b->persistent = false;
+    return build(b, streams);
+}
+
+static gi_status check_tile(int tile_w, int tile_h) {
+    if (tile_w < 32 || tile_w > 1024 || tile_w % 32 != 0 || tile_h < 1 || tile_h > 256 || tile_w * tile_h > 65536)
+        return fail(GI_ERR_INVALID_ARG, "gi_batch_build_persistent: tile_w a multiple of 32 in [32, 1024], "
+                                        "tile_h in [1, 256], at most 65536 pixels");
+    return GI_OK;
+}
+
+extern "C" gi_status gi_batch_build_persistent(gi_batch* b, int streams, int tile_w, int tile_h) {
+    if (!b || streams < 1 || streams > 64)
+        return fail(GI_ERR_INVALID_ARG, "gi_batch_build_persistent: streams in [1, 64]");
+    if (b->frames.empty()) return fail(GI_ERR_INVALID_ARG, "gi_batch_build_persistent: empty batch");
+    gi_status s = check_tile(tile_w, tile_h);
+    if (s != GI_OK) return s;
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e != cudaSuccess) return fail_cuda(e, "gi_batch_build_persistent: cudaSetDevice");
+    b->persistent = true;
+    b->tile_w = tile_w;
+    b->tile_h = tile_h;
     return build(b, streams);
 }
 
@@ -286,10 +467,17 @@ extern "C" gi_status gi_batch_info(const gi_batch* b, gi_batch_tuning* out) {
     out->frames = (int)b->frames.size();
     out->kernel_launches = b->launches_per_run;
     out->best_ms = 0.0f;
+    out->persistent = b->persistent ? 1 : 0;
+    out->tile_w = b->persistent ? b->tile_w : 0;
+    out->tile_h = b->persistent ? b->tile_h : 0;
+    out->work_items = b->persistent ? b->total_tiles : 0;
     return GI_OK;
 }
 
-extern "C" gi_status gi_batch_autotune(gi_batch* b, void* stream, int repeats, gi_batch_tuning* out) {
+// Times candidate settings on the real batch and keeps the fastest: tier
+// thresholds (tiny / warp-sized bounding boxes) at 8 streams, then the
+// stream count, and in persistent mode the work-item tile size.
+static gi_status autotune(gi_batch* b, void* stream, int repeats, bool persistent, gi_batch_tuning* out) {
     if (!b || b->frames.empty()) return fail(GI_ERR_INVALID_ARG, "gi_batch_autotune: empty batch");
     if (repeats < 1) repeats = 1;
     cudaError_t e = cudaSetDevice(b->device);
@@ -298,9 +486,12 @@ extern "C" gi_status gi_batch_autotune(gi_batch* b, void* stream, int repeats, g
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);
     cudaEventCreate(&t1);
-    auto time_config = [&](int tiny, int coop, int streams, float* ms) -> gi_status {
+    b->persistent = persistent;
+    auto time_config = [&](int tiny, int coop, int streams, int tw, int th, float* ms) -> gi_status {
         b->tiny_px = tiny;
         b->coop_px = coop;
+        b->tile_w = tw;
+        b->tile_h = th;
         gi_status s = build(b, streams);
         if (s != GI_OK) return s;
         cudaGraphLaunch(b->exec, st);  // warm
@@ -318,20 +509,19 @@ extern "C" gi_status gi_batch_autotune(gi_batch* b, void* stream, int repeats, g
         *ms = best;
         return GI_OK;
     };
-    // tier thresholds first (8 streams), then the stream count
     const int tinies[] = {16, 32, 64, 96, 128};
     const int coops[] = {256, 512, 1024};
     const int stream_counts[] = {4, 8, 16, 32};
-    int bt = 96, bc = 1024, bs = 8;
+    const int tiles[][2] = {{32, 4}, {64, 4}, {64, 8}, {128, 8}, {256, 8}, {128, 16}};
+    int bt = 96, bc = 1024, bs = 8, btw = 64, bth = 8;
     float best = 1e30f;
     gi_status s = GI_OK;
     for (int t : tinies)
         for (int c : coops) {
-            if (c <= t) continue;
+            if (c <= t || s != GI_OK) continue;
             float ms = 0;
-            s = time_config(t, c, 8, &ms);
-            if (s != GI_OK) break;
-            if (ms < best) {
+            s = time_config(t, c, 8, btw, bth, &ms);
+            if (s == GI_OK && ms < best) {
                 best = ms;
                 bt = t;
                 bc = c;
@@ -340,18 +530,30 @@ extern "C" gi_status gi_batch_autotune(gi_batch* b, void* stream, int repeats, g
     for (int n : stream_counts) {
         if (s != GI_OK) break;
         float ms = 0;
-        s = time_config(bt, bc, n, &ms);
-        if (s != GI_OK) break;
-        if (ms < best) {
+        s = time_config(bt, bc, n, btw, bth, &ms);
+        if (s == GI_OK && ms < best) {
             best = ms;
             bs = n;
         }
     }
+    if (persistent)
+        for (const auto& tl : tiles) {
+            if (s != GI_OK) break;
+            float ms = 0;
+            s = time_config(bt, bc, bs, tl[0], tl[1], &ms);
+            if (s == GI_OK && ms < best) {
+                best = ms;
+                btw = tl[0];
+                bth = tl[1];
+            }
+        }
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
     if (s != GI_OK) return s;
     b->tiny_px = bt;
     b->coop_px = bc;
+    b->tile_w = btw;
+    b->tile_h = bth;
     s = build(b, bs);
     if (s != GI_OK) return s;
     if (out) {
@@ -359,4 +561,20 @@ extern "C" gi_status gi_batch_autotune(gi_batch* b, void* stream, int repeats, g
         out->best_ms = best;
     }
     return GI_OK;
+}
+
+extern "C" gi_status gi_batch_autotune(gi_batch* b, void* stream, int repeats, gi_batch_tuning* out) {
+    return autotune(b, stream, repeats, false, out);
+}
+
+extern "C" gi_status gi_batch_autotune_persistent(gi_batch* b, void* stream, int repeats, gi_batch_tuning* out) {
+    if (b && !b->frames.empty()) {
+        const int tech = b->frames[0].vis.technique;
+        for (const auto& f : b->frames)
+            if (f.vis.technique != tech)
+                return fail(GI_ERR_UNSUPPORTED, "gi_batch_autotune_persistent: the frames must share one technique");
+        if (!gi::batch_visibility_supported(tech))
+            return fail(GI_ERR_UNSUPPORTED, "gi_batch_autotune_persistent: technique not supported (moment maps)");
+    }
+    return autotune(b, stream, repeats, true, out);
 }

@@ -115,6 +115,27 @@ gi_status launch_moments(gi_context* ctx, int tech, const float* d_depth, int S,
 
 // Moment soft shadows (GI_TECH_SAVSM .. GI_TECH_MSSM): the maps the lookups
 // read, built from the S x T light map.
+// One light-frame of a batch for the persistent visibility pass (device
+// table entry): the visibility parameters with the light's matrices, the
+// light map, the frame's G-buffer and the output image, and the light-
+// frame's first tile in the batch's tile numbering.
+struct BatchLightFrame {
+    gi_vis_params p;
+    const float* map;
+    const float4* pos;
+    const float4* nrm;
+    float* out;
+    int map_w, map_h;
+    float sx, sy;
+    int W, H;
+    int tiles_x, tiles_y;
+    unsigned tile_begin;
+    unsigned pad_;
+};
+bool batch_visibility_supported(int technique);
+gi_status launch_batch_visibility(int technique, const BatchLightFrame* d_lf, int n_lf, unsigned total_tiles,
+                                  unsigned* d_queue, int tile_w, int tile_h, int grid, cudaStream_t st);
+
 struct SoftMaps {
     const float4* mom = nullptr;     // moment map or its summed-area table, S x T
     const float2* hsm_lo = nullptr;  // VSSM: min-max level floor(lod); level 0 is

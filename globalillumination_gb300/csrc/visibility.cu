@@ -1643,6 +1643,73 @@ __global__ void __launch_bounds__(128) k_visibility(const gi_vis_params p,
     __stcs(out + i, shade<TECH>(p, c, vertex, normal));
 }
 
+// Persistent visibility pass of a batch: one launch shades every tile of
+// every light-frame.  The light maps and the frames' G-buffers are complete
+// when it starts (stream order), so nothing waits on another kernel: each
+// CTA takes the next tile from a global counter (one atomic per tile), finds
+// its light-frame by binary search over the tiles' prefix sums, stages that
+// light-frame's parameters in shared memory, and shades the tile's pixels
+// with the same shade<TECH> as the per-frame kernels.  Tiles of tile_w x
+// tile_h pixels (tile_w a multiple of 32) are walked row by row, 128
+// pixels per step.
+template <int TECH>
+__global__ void __launch_bounds__(128) k_batch_visibility(const BatchLightFrame* __restrict__ lf, int n_lf,
+                                                          unsigned total_tiles, unsigned* __restrict__ queue,
+                                                          int tile_w, int tile_h) {
+    __shared__ BatchLightFrame s_lf;
+    __shared__ unsigned s_tile;
+    __shared__ int s_idx;
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (tid == 0) {
+            const unsigned t = atomicAdd(queue, 1u);
+            s_tile = t;
+            int lo = 0, hi = n_lf - 1;  // last light-frame whose first tile <= t
+            if (t < total_tiles) {
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (lf[mid].tile_begin <= t) lo = mid;
+                    else hi = mid - 1;
+                }
+            }
+            s_idx = lo;
+        }
+        __syncthreads();
+        const unsigned t = s_tile;
+        if (t >= total_tiles) break;
+        {
+            const int* src = reinterpret_cast<const int*>(lf + s_idx);
+            int* dst = reinterpret_cast<int*>(&s_lf);
+            for (int k = tid; k < (int)(sizeof(BatchLightFrame) / sizeof(int)); k += blockDim.x) dst[k] = src[k];
+        }
+        __syncthreads();
+        const BatchLightFrame& f = s_lf;
+        const unsigned local = t - f.tile_begin;
+        const int x0 = (int)(local % (unsigned)f.tiles_x) * tile_w;
+        const int y0 = (int)(local / (unsigned)f.tiles_x) * tile_h;
+        Ctx c;
+        c.map = f.map;
+        c.W = f.map_w;
+        c.H = f.map_h;
+        c.fW = (float)f.map_w;
+        c.fH = (float)f.map_h;
+        c.sx = f.sx;
+        c.sy = f.sy;
+        c.I = f.p.shadow_intensity;
+        for (int k = tid; k < tile_w * tile_h; k += blockDim.x) {
+            const int x = x0 + k % tile_w, y = y0 + k / tile_w;
+            if (x >= f.W || y >= f.H) continue;
+            const size_t i = (size_t)y * f.W + x;
+            const float4 pv = __ldcs(f.pos + i);
+            const float4 nv = __ldcs(f.nrm + i);
+            V4 vertex = {pv.x, pv.y, pv.z, pv.w};
+            V4 normal = {nv.x, nv.y, nv.z, nv.w};
+            __stcs(f.out + i, shade<TECH>(f.p, c, vertex, normal));
+        }
+        __syncthreads();  // s_lf and s_tile are rewritten by the next take
+    }
+}
+
 // Fused G-buffer resolve and visibility: the G-buffer texel of each pixel
 // is interpolated from the visibility key in registers and shaded at once,
 // so the frame never writes / reads the 32-byte-per-pixel G-buffer (it is
@@ -2280,6 +2347,53 @@ gi_status launch_frame_visibility(gi_context* ctx, const gi_vis_params* p, const
     ctx->launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "frame visibility kernel launch");
+}
+
+bool batch_visibility_supported(int technique) {
+    switch (technique) {
+        case GI_TECH_HARD:
+        case GI_TECH_PCF:
+        case GI_TECH_PCF_TRICUBIC:
+        case GI_TECH_PCSS_GRID:
+        case GI_TECH_PCSS_POISSON:
+        case GI_TECH_SMSR_CONSERVATIVE:
+        case GI_TECH_SMSR_NONCONSERVATIVE:
+        case GI_TECH_RPCF_CONSERVATIVE:
+        case GI_TECH_RPCF_SMSR:
+        case GI_TECH_RSMSS:
+        case GI_TECH_HARD_SOFTAPP:
+        case GI_TECH_RBSSM:
+            return true;
+        default:
+            return false;  // the moment techniques need per-light prepared maps
+    }
+}
+
+gi_status launch_batch_visibility(int technique, const BatchLightFrame* d_lf, int n_lf, unsigned total_tiles,
+                                  unsigned* d_queue, int tile_w, int tile_h, int grid, cudaStream_t st) {
+#define GI_BATCH_CASE(T)                                                                                 \
+    case T:                                                                                              \
+        vis::k_batch_visibility<T><<<grid, 128, 0, st>>>(d_lf, n_lf, total_tiles, d_queue, tile_w, tile_h); \
+        break;
+    switch (technique) {
+        GI_BATCH_CASE(GI_TECH_HARD)
+        GI_BATCH_CASE(GI_TECH_PCF)
+        GI_BATCH_CASE(GI_TECH_PCF_TRICUBIC)
+        GI_BATCH_CASE(GI_TECH_PCSS_GRID)
+        GI_BATCH_CASE(GI_TECH_PCSS_POISSON)
+        GI_BATCH_CASE(GI_TECH_SMSR_CONSERVATIVE)
+        GI_BATCH_CASE(GI_TECH_SMSR_NONCONSERVATIVE)
+        GI_BATCH_CASE(GI_TECH_RPCF_CONSERVATIVE)
+        GI_BATCH_CASE(GI_TECH_RPCF_SMSR)
+        GI_BATCH_CASE(GI_TECH_RSMSS)
+        GI_BATCH_CASE(GI_TECH_HARD_SOFTAPP)
+        GI_BATCH_CASE(GI_TECH_RBSSM)
+        default:
+            return fail(GI_ERR_UNSUPPORTED, "persistent batch visibility: technique needs prepared maps");
+    }
+#undef GI_BATCH_CASE
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "persistent batch visibility launch");
 }
 
 }  // namespace gi

@@ -672,6 +672,16 @@ class Batch:
     def build(self, streams: int = 8) -> None:
         check(_lib().gi_batch_build(self.handle, streams), "gi_batch_build")
 
+    def build_persistent(self, streams: int = 8, tile_w: int = 64, tile_h: int = 8) -> None:
+        """Persistent mode: all maps and G-buffers resident, one persistent visibility launch."""
+        check(_lib().gi_batch_build_persistent(self.handle, streams, tile_w, tile_h), "gi_batch_build_persistent")
+
+    def autotune_persistent(self, stream=None, repeats: int = 3) -> dict:
+        t = api.BatchTuning()
+        check(_lib().gi_batch_autotune_persistent(self.handle, _stream_ptr(stream), repeats, C.byref(t)),
+              "gi_batch_autotune_persistent")
+        return self._tuning(t)
+
     def run(self, stream=None) -> None:
         check(_lib().gi_batch_run(self.handle, _stream_ptr(stream)), "gi_batch_run")
 
@@ -688,7 +698,9 @@ class Batch:
     @staticmethod
     def _tuning(t) -> dict:
         return {"tiny_px": t.tiny_px, "coop_px": t.coop_px, "streams": t.streams, "frames": t.frames,
-                "kernel_launches": int(t.kernel_launches), "best_ms": float(t.best_ms)}
+                "kernel_launches": int(t.kernel_launches), "best_ms": float(t.best_ms),
+                "persistent": bool(t.persistent), "tile_w": t.tile_w, "tile_h": t.tile_h,
+                "work_items": int(t.work_items)}
 
     def close(self) -> None:
         if self.handle:

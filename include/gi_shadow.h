@@ -638,6 +638,9 @@ typedef struct gi_batch_tuning {
     int frames;
     uint64_t kernel_launches; /* kernel nodes in one gi_batch_run           */
     float best_ms;            /* autotune: time of the chosen setting       */
+    int persistent;           /* 1: built by gi_batch_build_persistent      */
+    int tile_w, tile_h;       /* persistent: pixels per work item           */
+    uint32_t work_items;      /* persistent: (light-frame, tile) items      */
 } gi_batch_tuning;
 
 gi_status gi_batch_create(int device, gi_batch** out);
@@ -655,6 +658,15 @@ gi_status gi_batch_add_frame(gi_batch* batch, const gi_scene* scene,
 gi_status gi_batch_build(gi_batch* batch, int streams);
 /* Launches the captured graph on `stream`. */
 gi_status gi_batch_run(gi_batch* batch, void* stream);
+/* Persistent mode.  The graph rasterises every frame's G-buffer and every
+ * light's map into buffers the batch owns (all of them stay resident),
+ * then ONE persistent kernel shades every (light-frame, tile_w x tile_h
+ * tile) work item of the batch, taken from a device counter.  The frames
+ * must share one technique, and not a moment technique.  Results equal
+ * gi_batch_build's (and gi_render_frame's) bit for bit. */
+gi_status gi_batch_build_persistent(gi_batch* batch, int streams, int tile_w, int tile_h);
+/* gi_batch_autotune for the persistent mode: also picks the tile size. */
+gi_status gi_batch_autotune_persistent(gi_batch* batch, void* stream, int repeats, gi_batch_tuning* out);
 /* Times tier thresholds and stream counts on this batch (each candidate
  * rebuilt and replayed `repeats` times on `stream`), keeps the fastest
  * and rebuilds with it.  *out (may be NULL) receives the choice. */

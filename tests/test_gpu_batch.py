@@ -133,3 +133,79 @@ def test_batch_rejects_bad_input(cuda_ctx):
     with pytest.raises(gi.GIError):
         b.add_frame(f.scene, f.camera, f.lights, bad, f.params, o)
     b.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tech", [api.GI_TECH_PCF, api.GI_TECH_PCSS_POISSON, api.GI_TECH_SMSR_NONCONSERVATIVE])
+@pytest.mark.parametrize("tile", [(32, 4), (64, 8), (256, 16)])
+def test_persistent_batch_equals_graph_batch(cuda_ctx, tech, tile):
+    """One persistent visibility launch over every (light-frame, tile) item
+    gives the graph mode's images bit for bit (which equal gi_render_frame)."""
+    import torch
+
+    frames = _small_batch(n=7, W=200, H=110)
+    for f in frames:
+        p = gi.ShadowParams.defaults(tech)
+        p.light_radius = 0.5
+        p.pcss_min_blocker_depth = 0.0
+        p.kernel_order = 5
+        f.params = p
+    _upload(cuda_ctx, frames)
+    graph_outs, pers_outs = _outputs(frames), _outputs(frames)
+    bg, bp = gi.Batch(0), gi.Batch(0)
+    for f, og, op in zip(frames, graph_outs, pers_outs):
+        bg.add_frame(f.scene, f.camera, f.lights, f.maps, f.params, og)
+        bp.add_frame(f.scene, f.camera, f.lights, f.maps, f.params, op)
+    bg.build(3)
+    bp.build_persistent(3, tile[0], tile[1])
+    info = bp.info()
+    n_lf = sum(len(f.lights) for f in frames)
+    assert info["persistent"] and (info["tile_w"], info["tile_h"]) == tile
+    assert info["work_items"] == n_lf * ((200 + tile[0] - 1) // tile[0]) * ((110 + tile[1] - 1) // tile[1])
+    for _ in range(2):
+        bg.run()
+        bp.run()
+    torch.cuda.synchronize()
+    for og, op in zip(graph_outs, pers_outs):
+        assert torch.equal(og.view(torch.int32), op.view(torch.int32))
+    assert float((pers_outs[0] < 1.0).float().mean()) > 0.0
+    bg.close()
+    bp.close()
+
+
+@pytest.mark.gpu
+def test_persistent_autotune_and_rejections(cuda_ctx):
+    import torch
+
+    frames = _small_batch(n=3)
+    _upload(cuda_ctx, frames)
+    outs = _outputs(frames)
+    b = gi.Batch(0)
+    for f, o in zip(frames, outs):
+        b.add_frame(f.scene, f.camera, f.lights, f.maps, f.params, o)
+    b.build(2)
+    b.run()
+    torch.cuda.synchronize()
+    ref = [o.clone() for o in outs]
+    t = b.autotune_persistent(repeats=1)
+    assert t["persistent"] and t["tile_w"] % 32 == 0 and t["work_items"] > 0 and t["best_ms"] > 0
+    for o in outs:
+        o.fill_(-3.0)
+    b.run()
+    torch.cuda.synchronize()
+    for o, r in zip(outs, ref):
+        assert torch.equal(o, r)
+    with pytest.raises(gi.GIError):
+        b.build_persistent(2, 48, 8)  # tile width not a multiple of 32
+    b.close()
+    # a moment technique needs per-light prepared maps: refused
+    vsm = gi.Batch(0)
+    f = frames[0]
+    p = gi.ShadowParams.defaults(api.GI_TECH_VSM)
+    cam = gi.ViewSpec(eye=f.camera.eye, at=f.camera.at, width=128, height=128)
+    maps = [gi.MapParams(256, 256)] * len(f.lights)
+    o = torch.zeros((len(f.lights), 128, 128), device="cuda")
+    vsm.add_frame(f.scene, cam, f.lights, maps, p, o)
+    with pytest.raises(gi.GIError):
+        vsm.build_persistent(1, 64, 8)
+    vsm.close()
