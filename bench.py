@@ -1150,6 +1150,18 @@ def run_ours(args):
         "keys_after_light_map": statistics.mean(p[1] for p in phases),
         "resolve_and_visibility": statistics.mean(p[2] for p in phases),
     }
+    # the same phase with the min-max pyramid built for larger tap boxes
+    # (gi_context_set_tap_pyramid): one more launch, larger boxes skipped
+    ctx.set_tap_pyramid(True)
+    ctx.set_profiling(True)
+    phases_pyr = []
+    for r in range(R):
+        flush.fill_(float(r))
+        frame()
+        phases_pyr.append(ctx.phase_ms())
+    ctx.set_profiling(False)
+    ctx.set_tap_pyramid(False)
+    pass_ms["resolve_and_visibility_with_pyramid"] = statistics.mean(p[2] for p in phases_pyr)
 
     # ---- end to end through the C ABI with host buffers ---------------------
     h_pts = torch.from_numpy(pts.reshape(-1).copy()).pin_memory()

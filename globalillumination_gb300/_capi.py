@@ -213,6 +213,7 @@ _PROTOS = {
     "gi_shadow_volume_counts_silhouette": (C.c_int, [_VP, _VP, F3, C.c_float, F16, C.c_int, C.c_int, C.c_int,
                                                      _VP, _VP, C.POINTER(C.c_int), _VP]),
     "gi_light_map_minmax": (C.c_int, [_VP, _VP, C.c_int, C.c_int, _VP, _VP]),
+    "gi_context_set_tap_pyramid": (C.c_int, [_VP, C.c_int]),
     "gi_phong_shade": (C.c_int, [_VP, C.POINTER(VisParams), _VP, _VP, _VP, _VP, C.c_int, C.c_int, _VP, _VP]),
     "gi_pba_voronoi": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP]),
     "gi_edt_soft_shadows": (C.c_int, [_VP, _VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float,

@@ -159,6 +159,12 @@ extern "C" void gi_context_destroy(gi_context* c) {
 
 extern "C" uint64_t gi_context_launch_count(const gi_context* c) { return c ? c->launches : 0; }
 
+extern "C" gi_status gi_context_set_tap_pyramid(gi_context* c, int enable) {
+    if (!c) return fail(GI_ERR_INVALID_ARG, "gi_context_set_tap_pyramid: NULL context");
+    c->tap_pyramid = enable != 0;
+    return GI_OK;
+}
+
 extern "C" gi_status gi_context_set_tuning(gi_context* c, int tiny_px, int coop_px) {
     if (!c) return fail(GI_ERR_INVALID_ARG, "gi_context_set_tuning: NULL context");
     if (tiny_px < 1 || coop_px <= tiny_px || coop_px > 1024)

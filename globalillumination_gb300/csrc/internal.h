@@ -135,9 +135,11 @@ struct gi_context {
     // nearest site per pixel (short2) when the caller does not keep it
     void* d_pba_near = nullptr;
     size_t cap_pba_near = 0;
-    // min-max pyramid of the light map (float2 levels 1..6), status word 100
+    // min-max pyramid of the light map (float2 levels 1..6), status word 100;
+    // built for PCSS / PCF only when tap_pyramid is set
     void* d_pyr = nullptr;
     size_t cap_pyr = 0;
+    bool tap_pyramid = false;
     // silhouette mode of the shadow volumes: the volume triangles to draw
     // (count in status word 101)
     void* d_sil_list = nullptr;

@@ -156,17 +156,27 @@ __device__ __forceinline__ float fetch_finite(const Ctx& c, float s, float t) {
 // and floor are monotone, so no tap leaves the box.  Gives the minimum and
 // maximum of the map over the box from the pyramid (at the level where the
 // box spans at most 2 x 2 cells); false when the box leaves the map (border
-// texels read 0) or is wider than the pyramid's top level.
+// texels read 0) or is wider than the pyramid's top level.  Boxes of at
+// most 3 x 3 texels are read from the map itself, so they need no pyramid.
 __device__ __forceinline__ bool tap_box_minmax(const Ctx& c, float sx0, float sx1, float sy0, float sy1, float& mn,
                                                float& mx) {
     const int x0 = __float2int_rd(sx0 * c.fW), x1 = __float2int_rd(sx1 * c.fW);
     const int y0 = __float2int_rd(sy0 * c.fH), y1 = __float2int_rd(sy1 * c.fH);
     if (x0 < 0 || y0 < 0 || x1 >= c.W || y1 >= c.H) return false;
-    const int span = max(x1 - x0, y1 - y0);
-    if (span == 0) {
-        mn = mx = __ldg(c.map + (y0 * c.W + x0));
+    if (x1 - x0 <= 2 && y1 - y0 <= 2) {
+        // at most 3 x 3 texels (the blocker box of PCSS up to 2048^2 maps,
+        // 5 x 5 PCF): read them from the map
+        mn = __int_as_float(0x7f800000);
+        mx = -mn;
+        for (int y = y0; y <= y1; ++y)
+            for (int x = x0; x <= x1; ++x) {
+                const float v = __ldg(c.map + (y * c.W + x));
+                mn = fminf(mn, v);
+                mx = fmaxf(mx, v);
+            }
         return true;
     }
+    const int span = max(x1 - x0, y1 - y0);
     const int L = 32 - __clz(span);  // 2^L > span: at most two cells per axis
     if (L > c.tab->pyr.levels) return false;
     const float2* lv = c.tab->pyr.lv[L];
@@ -188,7 +198,7 @@ template <bool FAST>
 __device__ float pcf_bilinear_t(const gi_vis_params& p, const Ctx& c, V4 n) {
     float incrW = 1.0f / c.fW, incrH = 1.0f / c.fH;
     float illum = 0.0f;
-    if (FAST && c.tab && c.tab->pyr.levels > 0 && c.tab->pcf_count > 0) {
+    if (FAST && c.tab && c.tab->pcf_count > 0) {
         // the loop's offsets increase from pcf_lo to pcf_hi; incr > 0
         const float lo = c.tab->pcf_lo, hi = c.tab->pcf_hi;
         float mn, mx;
@@ -325,7 +335,7 @@ __device__ float avg_blocker_grid(const gi_vis_params& p, const Ctx& c, V4 n) {
 template <bool FAST>
 __device__ float avg_blocker_poisson_t(const gi_vis_params& p, const Ctx& c, V4 n, float bsw) {
     const float2* bo = c.boff;
-    if (FAST && bo && c.tab && c.tab->pyr.levels > 0) {
+    if (FAST && bo && c.tab) {
         // no texel the taps can reach is below z: no tap finds a blocker
         const float2 lo = c.tab->bmin, hi = c.tab->bmax;
         float mn, mx;
@@ -357,7 +367,7 @@ template <bool FAST>
 __device__ float pcss_filter_poisson_t(const gi_vis_params& p, const Ctx& c, float pw, V4 n) {
     float illum = 0.0f;
     const int nf = p.poisson_filter_taps;
-    if (FAST && c.tab && c.tab->pyr.levels > 0) {
+    if (FAST && c.tab) {
         // pw > 0 here (the caller checked the step), so o.x * pw is monotone in o.x
         const float2 lo = c.tab->fmin, hi = c.tab->fmax;
         float mn, mx;
@@ -2217,6 +2227,7 @@ static vis::PoissonOffsets poisson_offsets(const gi_vis_params* p, int map_w) {
 // exactly (maps with sides that are multiples of 64; others run every tap).
 static gi_status prepare_pyramid(gi_context* ctx, const gi_vis_params* p, const float* d_depth, int map_w,
                                  int map_h, cudaStream_t st, vis::PoissonOffsets* po) {
+    if (!ctx->tap_pyramid) return GI_OK;  // boxes of up to 3 x 3 texels are still skipped
     const bool pcss = p->technique == GI_TECH_PCSS_POISSON && p->poisson_blocker_taps >= 1 &&
                       p->poisson_filter_taps >= 1;
     const bool pcf = p->technique == GI_TECH_PCF && po->pcf_count > 0;

@@ -77,6 +77,10 @@ class Context:
         """Rasteriser tier thresholds (results do not depend on them)."""
         check(_lib().gi_context_set_tuning(self.handle, int(tiny_px), int(coop_px)), "gi_context_set_tuning")
 
+    def set_tap_pyramid(self, enable: bool) -> None:
+        """Build the light map's min-max pyramid for exact tap skipping of larger boxes."""
+        check(_lib().gi_context_set_tap_pyramid(self.handle, 1 if enable else 0), "gi_context_set_tap_pyramid")
+
     def set_profiling(self, enable: bool) -> None:
         check(_lib().gi_context_set_profiling(self.handle, int(bool(enable))), "gi_context_set_profiling")
 

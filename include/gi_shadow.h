@@ -87,6 +87,14 @@ gi_status gi_context_set_profiling(gi_context* ctx, int enable);
  * do not depend on them. */
 gi_status gi_context_set_tuning(gi_context* ctx, int tiny_px, int coop_px);
 gi_status gi_context_phase_ms(gi_context* ctx, float ms[3]);
+/* Exact tap skipping of PCSS (GI_TECH_PCSS_POISSON) and PCF: a pixel whose
+ * taps can only reach texels on one side of its depth gets the taps' result
+ * without running them.  Boxes of up to 3 x 3 texels are always tested from
+ * the map itself; with enable != 0 the visibility pass also builds the
+ * light map's min-max pyramid (gi_light_map_minmax) to test larger boxes
+ * (one more launch per pass).  Off by default.  Results do not depend on
+ * it. */
+gi_status gi_context_set_tap_pyramid(gi_context* ctx, int enable);
 
 /* ------------------------------------------------------------------ */
 /* Scene (host geometry + optional device copy)                        */
@@ -547,12 +555,12 @@ gi_status gi_area_light_adaptive(gi_context* ctx, const gi_scene* scene, const g
                                  float shadow_intensity, int width, int height, float* d_vis,
                                  gi_view* samples_out, float* levels_out, int* num_samples, void* stream);
 
-/* Min-max pyramid of a light map.  No counterpart in the reference: the
- * PCSS pass (GI_TECH_PCSS_POISSON) builds it after the light map and skips
- * the blocker taps of a pixel when no texel they can reach is below the
- * receiver, and the filter taps when all of those texels lie on one side
- * of it, which gives the same float result as running the taps.  This
- * entry point builds it alone: d_levels receives levels 1..6 one after the
+/* Min-max pyramid of a light map.  No counterpart in the reference: with
+ * gi_context_set_tap_pyramid the PCSS and PCF passes build it after the
+ * light map and skip a pixel's blocker taps when no texel they can reach is
+ * below the receiver, and its filter taps when all of those texels lie on
+ * one side of it, which gives the same float result as running the taps.
+ * This entry point builds it alone: d_levels receives levels 1..6 one after the
  * other, level L as float2(min, max) of every 2^L x 2^L texel block over
  * (width >> L) x (height >> L) cells, row-major (width * height / 3 float2
  * in all, rounded down per level).  width and height must be multiples of

@@ -257,9 +257,25 @@ void raster_clipped(const float c0[4], const float c1[4], const float c2[4], int
         int64_t x1 = std::min<int64_t>(W - 1, floor_div(maxX - kSub / 2, kSub));
         int64_t y0 = std::max<int64_t>(0, -floor_div(-(minY - kSub / 2), kSub));
         int64_t y1 = std::min<int64_t>(H - 1, floor_div(maxY - kSub / 2, kSub));
-        for (int64_t y = y0; y <= y1; ++y)
-            for (int64_t x = x0; x <= x1; ++x) {
-                int64_t px = x * kSub + kSub / 2, py = y * kSub + kSub / 2;
+        for (int64_t y = y0; y <= y1; ++y) {
+            // Scan only the row's span: each edge with B != 0 bounds px on
+            // one side at A (py - Ya) / B + Xa, found in double and widened
+            // by two pixels, so that no covered pixel is skipped; the exact
+            // test below still decides every pixel of the span.
+            int64_t xl = x0, xr = x1;
+            const int64_t pyc = y * kSub + kSub / 2;
+            for (int k = 0; k < 3; ++k) {
+                const int a = (k + 1) % 3, b = (k + 2) % 3;
+                const int64_t A = s.X[b] - s.X[a], B = s.Y[b] - s.Y[a];
+                if (B == 0) continue;
+                const double lim = (double)A * (double)(pyc - s.Y[a]) / (double)B + (double)s.X[a];
+                const double xb = (lim - kSub / 2) / kSub;
+                if (!(std::fabs(xb) < 1e15)) continue;
+                if (B > 0) xr = std::min<int64_t>(xr, (int64_t)std::floor(xb) + 2);
+                else xl = std::max<int64_t>(xl, (int64_t)std::ceil(xb) - 2);
+            }
+            for (int64_t x = xl; x <= xr; ++x) {
+                int64_t px = x * kSub + kSub / 2, py = pyc;
                 int64_t e[3];
                 bool inside = true;
                 for (int k = 0; k < 3 && inside; ++k) {
@@ -268,6 +284,7 @@ void raster_clipped(const float c0[4], const float c1[4], const float c2[4], int
                 }
                 if (inside) fn(i - 1, s, (int)x, (int)y, e);
             }
+        }
     }
 }
 

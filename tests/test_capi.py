@@ -107,4 +107,4 @@ def test_batch_argument_checks():
     assert lib.gi_batch_run(None, None) == api.GI_ERR_INVALID_ARG
     assert lib.gi_batch_add_frame(None, None, None, None, None, 1, None, None) == api.GI_ERR_INVALID_ARG
     assert lib.gi_batch_info(None, None) == api.GI_ERR_INVALID_ARG
-    assert C.sizeof(api.BatchTuning) == 4 * 4 + 8 + 8
+    assert C.sizeof(api.BatchTuning) == 4 * 4 + 8 + 4 + 3 * 4 + 4 + 4  # + padding to 8

@@ -1,5 +1,9 @@
 """The light map's min-max pyramid and the exact tap skipping built on it.
 
+Tap skipping tests small texel boxes (up to 3 x 3) from the map itself and
+larger ones from the pyramid when the context builds it; both settings are
+run.
+
 gi_light_map_minmax against numpy block minima / maxima on random maps and
 on a rendered light map; and PCSS (Poisson) visibility that reads the
 pyramid against the oracle, which runs every tap, bit for bit: on maps with
@@ -54,9 +58,11 @@ def _frame(spheres, S, W, H, radius):
 
 
 @pytest.mark.parametrize("S,spheres,radius", [(1024, 40, 0.25), (960, 40, 0.25), (2048, 64, 1.5)])
-def test_pcss_with_pyramid_equals_oracle(cuda_ctx, S, spheres, radius):
+@pytest.mark.parametrize("pyramid", [False, True])
+def test_pcss_with_pyramid_equals_oracle(cuda_ctx, S, spheres, radius, pyramid):
     import torch
 
+    cuda_ctx.set_tap_pyramid(pyramid)
     W, H = 640, 360
     w = _frame(spheres, S, W, H, radius)
     fr = gi.frame_setup(w.light, w.camera)
@@ -84,3 +90,26 @@ def test_pcss_with_pyramid_equals_oracle(cuda_ctx, S, spheres, radius):
     assert torch.equal(out2.view(torch.int32), bufs.vis.view(torch.int32))
     lit = float((bufs.vis == 1.0).float().mean())
     assert 0.05 < lit < 0.99  # the frame has lit pixels to skip and others to filter
+    cuda_ctx.set_tap_pyramid(False)
+
+
+@pytest.mark.parametrize("pyramid", [False, True])
+@pytest.mark.parametrize("order", [3, 5])
+def test_pcf_tap_skipping_equals_oracle(cuda_ctx, pyramid, order):
+    import torch
+
+    cuda_ctx.set_tap_pyramid(pyramid)
+    W, H, S = 512, 300, 1024
+    w = scenes.hard_pcf_1024(width=W, height=H, map_size=S)
+    w.params.kernel_order = order
+    fr = gi.frame_setup(w.light, w.camera)
+    w.scene.upload(cuda_ctx)
+    bufs = gi.allocate_frame(S, S, W, H)
+    gi.render_frame(cuda_ctx, w.scene, fr, w.map_params, w.params, W, H, bufs, store_gbuffer=True)
+    torch.cuda.synchronize()
+    want = oracle.visibility(w.params.to_c(fr), bufs.depth.cpu().numpy(), S, S, bufs.pos.cpu().numpy(),
+                             bufs.nrm.cpu().numpy(), W, H)
+    got = bufs.vis.cpu().numpy()
+    cuda_ctx.set_tap_pyramid(False)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), f"{int((got != want).sum())} pixels differ"
+    assert ((got > 0.25) & (got < 1.0)).sum() > 100
