@@ -118,7 +118,8 @@ def parse_args():
                     help="training frames (one 256^2 crop each, batch 16) for the surrogate leg")
     ap.add_argument("--profile", action="store_true",
                     help="render --warmup frames and exit (the command profiled with ncu)")
-    ap.add_argument("--profile-case", choices=["frame", "conv", "volumes", "edt", "sat"], default="frame",
+    ap.add_argument("--profile-case", choices=["frame", "conv", "volumes", "silhouette", "edt", "sat", "pyramid",
+                                               "persistent"], default="frame",
                     help="with --profile: the pcss_1080p frame, three U-Net convolutions at 1080p (d0a, d1a, "
                          "d2a), the heavy scene's shadow volumes of one light at 960x540, three EDTSM "
                          "filters of the 1024^2 frame, or three 1024^2 moment map + SAT builds")
@@ -1055,6 +1056,39 @@ def run_profile_case(args, local):
         return 0
     from globalillumination_gb300 import scenes
 
+    if args.profile_case == "pyramid":
+        # the min-max pyramid of the pcss_1080p light map (2048^2), three builds
+        w = scenes.pcss_1080p()
+        ctx = gi.Context(local)
+        w.scene.upload(ctx)
+        fr = gi.frame_setup(w.light, w.camera)
+        S = w.map_params.width
+        depth = torch.empty(S * S, device="cuda")
+        gi.render_shadow_map(ctx, w.scene, w.map_params, fr.light_mvp, depth)
+        for _ in range(3):
+            lv = gi.light_map_minmax(ctx, depth, S, S)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "pyramid", "top_min": float(lv[-1][..., 0].min())}), flush=True)
+        ctx.close()
+        return 0
+    if args.profile_case == "persistent":
+        # a 12-scene slice of the batched workload in persistent mode, replayed twice
+        frames = scenes.batched_720p(scenes=12)
+        ctx = gi.Context(local)
+        for f in frames:
+            f.scene.upload(ctx)
+        outs = [torch.empty((len(f.lights), f.camera.height, f.camera.width), device="cuda") for f in frames]
+        b = gi.Batch(local)
+        for f, o in zip(frames, outs):
+            b.add_frame(f.scene, f.camera, f.lights, f.maps, f.params, o)
+        b.build_persistent(8, 256, 8)
+        for _ in range(2):
+            b.run()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "persistent", "work_items": b.info()["work_items"]}), flush=True)
+        b.close()
+        ctx.close()
+        return 0
     w = scenes.heavy_2160p()
     ctx = gi.Context(local)
     w.scene.upload(ctx)
@@ -1062,6 +1096,14 @@ def run_profile_case(args, local):
     light = gi.ViewSpec(eye=w.lights[0], at=(0.0, 0.0, 0.0), width=4096, height=4096, fovy_deg=90.0)
     fr = gi.frame_setup(light, cam)
     st = torch.empty(960 * 540, dtype=torch.uint8, device="cuda")
+    if args.profile_case == "silhouette":
+        drawn = gi.shadow_volume_counts_silhouette(ctx, w.scene, light.eye, fr.camera_mvp, 960, 540, st)
+        drawn = gi.shadow_volume_counts_silhouette(ctx, w.scene, light.eye, fr.camera_mvp, 960, 540, st)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "silhouette", "drawn": drawn,
+                          "lit_fraction": float((st == 0).float().mean())}), flush=True)
+        ctx.close()
+        return 0
     gi.shadow_volume_counts(ctx, w.scene, light.eye, fr.camera_mvp, 960, 540, st)
     torch.cuda.synchronize()
     print(json.dumps({"profile_case": "volumes", "lit_fraction": float((st == 0).float().mean())}), flush=True)
