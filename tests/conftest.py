@@ -16,10 +16,11 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA device (runs on the GB300 box)")
     # Build (incrementally) the library and the oracle before any test imports them.
     from globalillumination_gb300.build import build_library
-    from oracle.build_oracle import build_oracle
+    from oracle.build_oracle import build_oracle, build_scene_ref
 
     build_library()
     build_oracle()
+    build_scene_ref()  # the reference's own scene C++, where its tree is present
 
 
 def has_reference() -> bool:
