@@ -328,39 +328,38 @@ __global__ void __launch_bounds__(kThreads) k_conv_fwd(ConvArgs a) {
 
 // ---- 3x3 convolution from halo slabs (cin % 16 == 0) ---------------------------
 // A CTA computes R output rows x 128 pixels (R accumulators of 128 x N in
-// TMEM).  A stage holds two channel groups (16 channels) of the R + 2 input
-// rows y0-1 .. y0+R over x0-1 .. x0+128 ("slab": 130 pixels x 16 B per
-// row and group), fetched by one 4-D TMA box load per group (the halo
-// outside the image is zero-filled by TMA), and the weights of all 9 taps
-// for those channels, fetched by one bulk copy from the stage-ordered
-// packing [chunk][tap][group][cout][8].  The MMA of tap (dy, dx) for output
-// row r reads A at slab row r + dy, shifted by dx pixels (16 B): the
-// 8-pixel core matrices stay contiguous (SBO 128 B) and the second channel
-// group is one slab further (LBO).  Each input pixel is loaded (R + 2) / R
-// times instead of 9.  Warp 0 runs the main loop (lane 0 issues the TMA
-// loads and the MMAs; full / empty mbarriers per stage); all four warps
-// then drain the accumulators.
+// TMEM).  A stage holds 16 channels of the R + 2 input rows y0-1 .. y0+R
+// over x0-1 .. x0+128 ("slab": 130 pixels x 32 B per row), fetched by one
+// 4-D TMA box load in the 32-byte swizzled layout (the halo outside the
+// image is zero-filled by TMA), and the weights of all 9 taps for those
+// channels, fetched by one bulk copy from the stage-ordered packing
+// [chunk][tap][group][cout][8].  The MMA of tap (dy, dx) for output row r
+// reads A at slab row r + dy, shifted by dx pixels (32 B): each pixel's 16
+// channels are one 32-byte row of the K-major swizzled layout (8-pixel
+// groups 256 B apart), and the swizzle is a function of the shared-memory
+// address, which TMA and the MMA compute alike, so any pixel can start the
+// operand.  Each input pixel is loaded (R + 2) / R times instead of 9, in
+// boxes whose rows are 32 bytes (a 16-byte box row costs the TMA engine
+// as much as a 32-byte one).
 constexpr int kSlabPx = 130;
-constexpr int kSlabRow = kSlabPx * 16;  // 2080 B
+constexpr int kSlabRow = kSlabPx * 32;  // 4160 B
 
 struct SlabGeom {
-    int R, NS, ncols, slab, a_box, a_bytes, b_bytes, stage_bytes;
+    int R, NS, ncols, a_box, a_bytes, b_bytes, stage_bytes;
 };
 
-// Rows per CTA R and stage count NS: 32-wide outputs keep R = 4 so that
-// two or three CTAs fit an SM; 64-wide ones use R = 8 (weights reused over
-// more pixels, TMEM full); layers with at most two K-stages use two stages.
-__host__ __device__ inline SlabGeom slab_geom(int N, int nk) {
-    SlabGeom g;
-    g.ncols = N <= 32 ? 32 : N <= 64 ? 64 : N <= 128 ? 128 : 256;
-    g.R = N <= 32 ? 4 : N <= 64 ? 8 : N <= 128 ? 4 : 2;
-    g.a_box = (g.R + 2) * kSlabRow;
-    g.slab = (g.a_box + 127) / 128 * 128;  // TMA destinations are 128-byte aligned
-    g.a_bytes = 2 * g.slab;
-    g.b_bytes = 9 * 2 * N * 16;
-    g.stage_bytes = g.a_bytes + g.b_bytes;
-    g.NS = (nk > 2 && 3 * g.stage_bytes <= 200 * 1024) ? 3 : 2;
-    return g;
+// tcgen05 shared-memory descriptor of a K-major operand in the 32-byte
+// swizzled layout that TMA writes with CU_TENSOR_MAP_SWIZZLE_32B: rows of
+// 32 B (16 BF16 = one MMA's K), 8-row groups 256 B apart (SBO), layout
+// type 6; the leading-dimension offset is unused because K fits the
+// swizzle width.
+__device__ __forceinline__ uint64_t smem_desc_sw32(uint32_t addr) {
+    uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(256u >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)6 << 61;
+    return d;
 }
 
 __host__ __device__ inline bool slab_layout(int kin, int ks) { return ks == 3 && kin % 16 == 0; }
@@ -400,10 +399,9 @@ __host__ __device__ inline SlabGeom persist_geom(int N, int nk) {
     g.R = 256 / g.ncols;  // two accumulator sets of R x ncols columns
     if (g.R > 8) g.R = 8;
     g.a_box = (g.R + 2) * kSlabRow;
-    g.slab = (g.a_box + 127) / 128 * 128;
-    g.a_bytes = 2 * g.slab;
+    g.a_bytes = (g.a_box + 1023) / 1024 * 1024;  // swizzled TMA destinations: 1024-byte aligned
     g.b_bytes = 9 * 2 * N * 16;
-    g.stage_bytes = g.a_bytes + g.b_bytes;
+    g.stage_bytes = (g.a_bytes + g.b_bytes + 1023) / 1024 * 1024;
     g.NS = 4;
     while (g.NS > 2 && g.NS * g.stage_bytes > 200 * 1024) --g.NS;
     (void)nk;
@@ -413,7 +411,7 @@ __host__ __device__ inline SlabGeom persist_geom(int N, int nk) {
 __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, const __grid_constant__ CUtensorMap xmap,
                                                                 int tiles_x, int tiles_y, int tiles) {
     extern __shared__ uint8_t smem_raw[];
-    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     __shared__ uint64_t full[4], empty[4], acc_full[2], acc_empty[2];
     __shared__ uint32_t tmem_slot;
     // Stop flag (a wait ran out somewhere in the CTA) and the progress the
@@ -470,7 +468,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
 
     if (warp == 0) {
         // TMA producer
-        const uint32_t stage_tx = (uint32_t)(2 * G.a_box + G.b_bytes);
+        const uint32_t stage_tx = (uint32_t)(G.a_box + G.b_bytes);
         int g = 0, freed = 0;
         bool run = true;
         for (int it = 0; run && it < ntiles_mine; ++it) {
@@ -493,7 +491,6 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
                     uint8_t* sa = smem + s * G.stage_bytes;
                     mbar_expect_tx(&full[s], stage_tx);
                     tma_load_4d(sa, &xmap, c * 16, x0 - 1, y0 - 1, img, &full[s]);
-                    tma_load_4d(sa + G.slab, &xmap, c * 16 + 8, x0 - 1, y0 - 1, img, &full[s]);
                     bulk_load(sa + G.a_bytes, a.wt + (size_t)c * (G.b_bytes / 2), (uint32_t)G.b_bytes, &full[s]);
                 }
                 __syncwarp();
@@ -527,8 +524,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
                         const int dy = t / 3, dx = t % 3;
                         const uint64_t bd = smem_desc(smem_u32(sb + t * 2 * N * 16), (uint32_t)N * 16u, 128u);
                         for (int r = 0; r < R; ++r) {
-                            const uint64_t ad = smem_desc(smem_u32(sa + (r + dy) * kSlabRow + dx * 16),
-                                                          (uint32_t)G.slab, 128u);
+                            const uint64_t ad = smem_desc_sw32(smem_u32(sa + (r + dy) * kSlabRow + dx * 32));
                             mma_bf16(acc + (uint32_t)(r * G.ncols), ad, bd, idesc, (c > 0 || t > 0) ? 1u : 0u);
                         }
                     }
@@ -1099,17 +1095,18 @@ gi_status tensor_map_fn() {
     return GI_OK;
 }
 
-// 4-D map (c, w, h, n) of an NHWC BF16 tensor with boxes of 8 channels x
-// 130 pixels x `rows` rows x 1 image (the halo slab of one channel group).
+// 4-D map (c, w, h, n) of an NHWC BF16 tensor with boxes of 16 channels x
+// 130 pixels x `rows` rows x 1 image (the halo slab of one stage), written
+// to shared memory in the 32-byte swizzled layout.
 gi_status slab_map(CUtensorMap* m, const uint16_t* x, int n, int h, int w, int c, int rows) {
     gi_status st = tensor_map_fn();
     if (st != GI_OK) return st;
     const cuuint64_t dims[4] = {(cuuint64_t)c, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
     const cuuint64_t strides[3] = {(cuuint64_t)c * 2, (cuuint64_t)w * c * 2, (cuuint64_t)h * w * c * 2};
-    const cuuint32_t box[4] = {8, (cuuint32_t)tc::kSlabPx, (cuuint32_t)rows, 1};
+    const cuuint32_t box[4] = {16, (cuuint32_t)tc::kSlabPx, (cuuint32_t)rows, 1};
     const cuuint32_t es[4] = {1, 1, 1, 1};
     CUresult r = g_encode_tiled(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<uint16_t*>(x), dims, strides,
-                                box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B,
                                 CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? GI_OK : fail(GI_ERR_CUDA, "cuTensorMapEncodeTiled rejected the activation map");
 }
@@ -1141,7 +1138,7 @@ gi_status launch_slab(const tc::ConvArgs& a, cudaStream_t cs) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int grid = (int)std::min<long long>(tiles, sms);
-    tc::k_conv3_slab<<<grid, tc::kPersistThreads, G.NS * G.stage_bytes + 128, cs>>>(a, m, tx, ty, (int)tiles);
+    tc::k_conv3_slab<<<grid, tc::kPersistThreads, G.NS * G.stage_bytes + 1024, cs>>>(a, m, tx, ty, (int)tiles);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_conv2d_bf16 launch");
 }
