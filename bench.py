@@ -370,12 +370,18 @@ def run_batched(args, ctx, stream, local, rank=0, world=1, dist=None):
     # of the map (4 B/texel), the G-buffer read (32 B/px) and the visibility
     # write (4 B/px)
     alg = 0
+    # the graph mode resolves the G-buffer from the camera keys in registers:
+    # per frame the key write (8 B/px), per light-frame the key read and the
+    # visibility write (12 B/px) instead of the G-buffer's 32 B each way
+    alg_graph = 0
     for f in frames:
         P = f.camera.width * f.camera.height
         geo = 24 * f.triangles  # float3 vertices (about T / 2 of them, x2 arrays) + int3 indices, bounded by 24 T
         alg += geo + 32 * P
+        alg_graph += geo + 8 * P
         for m in f.maps:
             alg += geo + 12 * m.width * m.height + 36 * P
+            alg_graph += geo + 12 * m.width * m.height + 12 * P
     peak, peak_kind = measured_hbm_peak()
     b.close()
     del outs
@@ -389,6 +395,9 @@ def run_batched(args, ctx, stream, local, rank=0, world=1, dist=None):
         "tuning": {k: tune[k] for k in ("tiny_px", "coop_px", "streams")},
         "kernel_launches_per_batch": info["kernel_launches"],
         "single_frame_calls_light_frames_per_s": total_light_frames / (single_ms / 1000.0),
+        "roofline": {"bound": "hbm", "achieved": alg_graph / (batch_ms / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": alg_graph / (batch_ms / 1000.0) / 1e9 / peak, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_batch": int(alg_graph)},
         "persistent": {"light_frames_per_s": light_frames / (pers_ms / 1000.0), "ms_per_batch": pers_ms,
                        "tile": best_tile, "ms_per_tile_size": pers, "work_items": pinfo["work_items"],
                        "kernel_launches_per_batch": pinfo["kernel_launches"],
