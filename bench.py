@@ -11,14 +11,15 @@ one shadowed frame: light-view depth map, G-buffer, visibility.
           before every timed step, outside the step's events
   e2e     frames/s through the C ABI with host buffers: every step uploads
           the scene from pinned host memory (gi_scene_upload_from), renders,
-          and reads the visibility buffer back to pinned host memory; two
-          frames are in flight on two contexts and compute streams, with
+          and reads the visibility buffer back to pinned host memory; several
+          frames are in flight on their own contexts and compute streams, with
           uploads and read-backs on their own streams (no L2 flush: each
-          frame's inputs arrive fresh from the host).  Because two frames
-          overlap and L2 is not flushed, e2e can exceed `value`, which
-          times each frame alone between its events after an L2 flush: e2e
-          is pipelined throughput, `value` the latency-bound rate of one
-          frame at a time
+          frame's inputs arrive fresh from the host).  Four frames are in
+          flight on four contexts (the line also gives the rate with two).
+          Because frames overlap and L2 is not flushed, e2e can exceed
+          `value`, which times each frame alone between its events after an
+          L2 flush: e2e is pipelined throughput, `value` the latency-bound
+          rate of one frame at a time
   roofline  the fused G-buffer-resolve + visibility kernel: algorithmic
           bytes 12 P + 4 S^2 + scene per launch over its event-timed
           duration, against the measured HBM copy bandwidth
@@ -1235,56 +1236,65 @@ def run_ours(args):
     h_pts = torch.from_numpy(pts.reshape(-1).copy()).pin_memory()
     h_nrm = torch.from_numpy(nrm.reshape(-1).copy()).pin_memory()
     h_idx = torch.from_numpy(idx.reshape(-1).copy()).pin_memory()
-    # Two frames in flight on two contexts and two compute streams: frame k's
-    # scene upload and visibility read-back (their own streams) and its
-    # rendering overlap frame k+1's; every step still uploads the whole scene
-    # from pinned host memory and reads the whole visibility image back.
-    h_vis = [torch.empty(P, dtype=torch.float32).pin_memory() for _ in range(2)]
-    e2e_scenes = [gi.Scene(), gi.Scene()]
-    e2e_bufs = [bufs, gi.allocate_frame(S, S, W, H, local)]
-    e2e_ctx = [ctx, gi.Context(local)]
-    e2e_streams = [stream, torch.cuda.Stream()]
-    up_stream, down_stream = torch.cuda.Stream(), torch.cuda.Stream()
-    up_done = [torch.cuda.Event() for _ in range(2)]
-    render_done = [torch.cuda.Event() for _ in range(2)]
-    copy_done = [torch.cuda.Event() for _ in range(2)]
-    for ev in render_done + copy_done:
-        ev.record(stream)
-    step_no = [0]
+    # D frames in flight on D contexts and compute streams: frame k's scene
+    # upload and visibility read-back (their own streams) and its rendering
+    # overlap the other in-flight frames'; every step still uploads the
+    # whole scene from pinned host memory and reads the whole visibility
+    # image back.
+    def run_e2e(D):
+        h_vis = [torch.empty(P, dtype=torch.float32).pin_memory() for _ in range(D)]
+        e2e_scenes = [gi.Scene() for _ in range(D)]
+        e2e_bufs = [bufs] + [gi.allocate_frame(S, S, W, H, local) for _ in range(D - 1)]
+        e2e_ctx = [ctx] + [gi.Context(local) for _ in range(D - 1)]
+        e2e_streams = [stream] + [torch.cuda.Stream() for _ in range(D - 1)]
+        up_stream, down_stream = torch.cuda.Stream(), torch.cuda.Stream()
+        up_done = [torch.cuda.Event() for _ in range(D)]
+        render_done = [torch.cuda.Event() for _ in range(D)]
+        copy_done = [torch.cuda.Event() for _ in range(D)]
+        for ev in render_done + copy_done:
+            ev.record(stream)
+        step_no = [0]
 
-    def e2e_step():
-        k = step_no[0] % 2
-        step_no[0] += 1
-        sc, fb, cx, cs = e2e_scenes[k], e2e_bufs[k], e2e_ctx[k], e2e_streams[k]
-        up_stream.wait_event(render_done[k])  # frame k-2 finished with this scene
-        sc.upload_from(cx, h_pts.data_ptr(), h_nrm.data_ptr(), pts.shape[0], h_idx.data_ptr(), tris, up_stream)
-        up_done[k].record(up_stream)
-        cs.wait_event(up_done[k])
-        cs.wait_event(copy_done[k])  # frame k-2's read-back finished with these buffers
-        gi.render_frame(cx, sc, fr, w.map_params, w.params, W, H, fb, cs)
-        render_done[k].record(cs)
-        down_stream.wait_event(render_done[k])
-        with torch.cuda.stream(down_stream):
-            h_vis[k].copy_(fb.vis, non_blocking=True)
-        copy_done[k].record(down_stream)
+        def e2e_step():
+            k = step_no[0] % D
+            step_no[0] += 1
+            sc, fb, cx, cs = e2e_scenes[k], e2e_bufs[k], e2e_ctx[k], e2e_streams[k]
+            up_stream.wait_event(render_done[k])  # frame k-D finished with this scene
+            sc.upload_from(cx, h_pts.data_ptr(), h_nrm.data_ptr(), pts.shape[0], h_idx.data_ptr(), tris, up_stream)
+            up_done[k].record(up_stream)
+            cs.wait_event(up_done[k])
+            cs.wait_event(copy_done[k])  # frame k-D's read-back finished with these buffers
+            gi.render_frame(cx, sc, fr, w.map_params, w.params, W, H, fb, cs)
+            render_done[k].record(cs)
+            down_stream.wait_event(render_done[k])
+            with torch.cuda.stream(down_stream):
+                h_vis[k].copy_(fb.vis, non_blocking=True)
+            copy_done[k].record(down_stream)
 
-    for _ in range(4):
-        e2e_step()
-    barrier()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    start = torch.cuda.Event()
-    start.record(stream)
-    for st_ in (e2e_streams[1], up_stream, down_stream):
-        st_.wait_event(start)  # nothing of the timed frames runs before e0
-    for _ in range(K):
-        e2e_step()
-    stream.wait_event(copy_done[0])
-    stream.wait_event(copy_done[1])
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1)
+        for _ in range(2 * D):
+            e2e_step()
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        start = torch.cuda.Event()
+        start.record(stream)
+        for st_ in e2e_streams[1:] + [up_stream, down_stream]:
+            st_.wait_event(start)  # nothing of the timed frames runs before e0
+        for _ in range(K):
+            e2e_step()
+        for ev in copy_done:
+            stream.wait_event(ev)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        for c in e2e_ctx[1:]:
+            c.close()
+        return ms
+
+    e2e_depth = 4
+    e2e_ms_by_depth = {d: run_e2e(d) for d in (2, e2e_depth)}
+    e2e_ms = e2e_ms_by_depth[e2e_depth]
     if dist is not None:
         t = torch.tensor([e2e_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -1338,7 +1348,9 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": workload_config(S, W, H, tris),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h)},
+                    "d2h_bytes_per_step": int(d2h), "frames_in_flight": e2e_depth,
+                    "frames_per_s_by_frames_in_flight": {str(d): world * K / (ms / 1000.0)
+                                                         for d, ms in e2e_ms_by_depth.items()}},
             "gpu_launches": int(launches),
             "roofline": {"kernel": "k_frame_visibility<PCSS_POISSON> (G-buffer resolve + visibility)",
                          "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
