@@ -260,6 +260,8 @@ _PROTOS = {
                                       _VP, C.c_int, _VP, C.c_float, _VP, _VP, _VP]),
     "gi_conv2d_head_bf16": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP, C.c_int, C.c_int, _VP, _VP,
                                       _VP, _VP, _VP]),
+    "gi_conv2d_fused_bf16": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP, C.c_int, C.c_int, _VP,
+                                       C.c_int, C.c_int, _VP, C.c_int, _VP, _VP]),
     "gi_surrogate_loss": (C.c_int, [_VP, _VP, _VP, C.c_size_t, C.c_float, _VP, _VP, _VP]),
     "gi_adam_f32": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
                               C.c_float, _VP]),

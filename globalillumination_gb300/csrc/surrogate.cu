@@ -121,6 +121,18 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
                  : "memory");
 }
 
+// 16 consecutive FP32 columns of this thread's TMEM lane, without the
+// wait: the registers are valid after tmem_wait_ld().
+__device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
 // 16 consecutive FP32 columns of this thread's TMEM lane.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     uint32_t r[16];
@@ -172,6 +184,11 @@ struct ConvArgs {
     const float* hw;
     const float* hb;
     float* hout;
+    // slab kernel only: pool (BF16, [n][h / 2][w / 2][cout]) also receives
+    // the 2 x 2 max-pooled output; up2 writes y upsampled 2x (nearest) into
+    // a [n][2 h][2 w][y_c] tensor
+    uint16_t* pool;
+    int up2;
 };
 
 __global__ void __launch_bounds__(kThreads) k_conv_fwd(ConvArgs a) {
@@ -386,12 +403,15 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
         : "memory");
 }
 
-// Persistent CTAs (one per SM) of six warps: warp 0 issues the TMA loads,
-// warp 1 the MMAs, warps 2-5 drain the accumulators (warp w reads TMEM
-// lanes 32 (w % 4) ..).  Two TMEM accumulator sets alternate between tiles,
-// so the epilogue of tile t overlaps the MMAs of tile t + 1.  Barriers:
-// full / empty per smem stage, acc_full / acc_empty per accumulator set.
-constexpr int kPersistThreads = 192;
+// Persistent CTAs (one per SM) of ten warps: warp 0 issues the TMA loads,
+// warp 1 the MMAs, warps 2-9 drain the accumulators (warp w reads TMEM
+// lanes 32 (w % 4) ..; the two warps of a lane quarter take alternate rows,
+// or alternate row pairs when pooling).  Two TMEM accumulator sets
+// alternate between tiles, so the epilogue of tile t overlaps the MMAs of
+// tile t + 1.  Barriers: full / empty per smem stage, acc_full / acc_empty
+// per accumulator set.
+constexpr int kPersistThreads = 320;
+constexpr int kEpilogueThreads = kPersistThreads - 64;
 
 __host__ __device__ inline SlabGeom persist_geom(int N, int nk) {
     SlabGeom g;
@@ -408,6 +428,10 @@ __host__ __device__ inline SlabGeom persist_geom(int N, int nk) {
     return g;
 }
 
+// R (output rows per tile, 256 / accumulator columns) is a template
+// parameter so that the MMA warp's issue loop is fully unrolled: one
+// 64-bit add per descriptor and the MMA itself per instruction.
+template <int R>
 __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, const __grid_constant__ CUtensorMap xmap,
                                                                 int tiles_x, int tiles_y, int tiles) {
     extern __shared__ uint8_t smem_raw[];
@@ -423,8 +447,9 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
     const int N = a.cout;
     const int nk = a.cin / 16;
     const SlabGeom G = persist_geom(N, nk);
-    const int R = G.R, NS = G.NS;
-    const uint32_t set_cols = (uint32_t)(R * G.ncols);
+    const int NS = G.NS;
+    constexpr int kCols = 256 / R;  // accumulator columns of one output row
+    const uint32_t set_cols = (uint32_t)(R * kCols);
     const uint32_t tcols = 2 * set_cols;
     if (warp == 0) tmem_alloc(&tmem_slot, tcols);
     if (tid == 0) {
@@ -434,7 +459,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&acc_full[b], 1);
-            mbar_init(&acc_empty[b], 128);
+            mbar_init(&acc_empty[b], kEpilogueThreads);
         }
         s_fail = 0;
         s_loaded = s_taken = s_committed = s_freed = 0;
@@ -503,6 +528,11 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
     } else if (warp == 1) {
         // MMA issuer
         const uint32_t idesc = idesc_bf16(128, N);
+        // taps stacked along N: one, two or three dy taps of N columns each
+        // (R >= 4 and N equal to the row stride kCols, so 3 N <= 192)
+        const bool stacked = R >= 4 && N == kCols;
+        const uint32_t idesc2 = stacked ? idesc_bf16(128, 2 * N) : idesc;
+        const uint32_t idesc3 = stacked ? idesc_bf16(128, 3 * N) : idesc;
         int g = 0, committed = 0;
         bool run = true;
         for (int it = 0; run && it < ntiles_mine; ++it) {
@@ -510,6 +540,8 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
             if (it >= 2 && !warp_wait(&acc_empty[b], (unsigned)((it >> 1) - 1) & 1u)) break;
             fence_after();
             const uint32_t acc = tmem + (uint32_t)b * set_cols;
+            // output row r's accumulator: rows in reverse order, kCols apart
+            auto acc_col = [&](int r) { return acc + (uint32_t)((R - 1 - r) * kCols); };
             for (int c = 0; c < nk; ++c, ++g) {
                 const int s = g % NS;
                 if (!warp_wait(&full[s], (unsigned)(g / NS) & 1u)) {
@@ -518,14 +550,55 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
                 }
                 if (lane == 0) {
                     fence_after();
-                    const uint8_t* sa = smem + s * G.stage_bytes;
-                    const uint8_t* sb = sa + G.a_bytes;
-                    for (int t = 0; t < 9; ++t) {
-                        const int dy = t / 3, dx = t % 3;
-                        const uint64_t bd = smem_desc(smem_u32(sb + t * 2 * N * 16), (uint32_t)N * 16u, 128u);
-                        for (int r = 0; r < R; ++r) {
-                            const uint64_t ad = smem_desc_sw32(smem_u32(sa + (r + dy) * kSlabRow + dx * 32));
-                            mma_bf16(acc + (uint32_t)(r * G.ncols), ad, bd, idesc, (c > 0 || t > 0) ? 1u : 0u);
+                    // Descriptors of the stage's first A and B matrices; the
+                    // others differ only in the start-address field (bits
+                    // 0-13, in 16-byte units), and every start stays below
+                    // 256 KB, so adding the offset there never carries.
+                    // B: tap (dx, dy) at (3 dx + dy) x N x 32 bytes, 8-row
+                    // groups 256 B apart, the two K halves 128 B apart.
+                    const uint32_t sa = smem_u32(smem + s * G.stage_bytes);
+                    const uint64_t ad0 = smem_desc_sw32(sa);
+                    const uint64_t bd0 = smem_desc(sa + (uint32_t)G.a_bytes, 128u, 256u);
+                    const uint32_t tap_step = (uint32_t)N * 2u;  // N x 32 B / 16
+                    if (stacked) {
+                        // Slab row ri (input row y0 - 1 + ri) feeds output
+                        // row ri - dy through tap dy; the accumulators run
+                        // in reverse row order kCols apart, so one MMA with
+                        // the taps dlo..dhi stacked along N writes rows
+                        // ri - dlo, ri - dlo - 1, ...  On the first stage,
+                        // tap (dx 0, dy 0) starts every row's accumulator
+                        // (accumulate off) before any stacked MMA adds to it.
+                        const bool init = c == 0;
+#pragma unroll
+                        for (int dx = 0; dx < 3; ++dx) {
+                            if (dx == 0 && init) {
+#pragma unroll
+                                for (int r = 0; r < R; ++r)
+                                    mma_bf16(acc_col(r), ad0 + (uint64_t)((r * kSlabRow) >> 4), bd0, idesc, 0u);
+                            }
+#pragma unroll
+                            for (int ri = 0; ri < R + 2; ++ri) {
+                                int dlo = ri - R + 1 > 0 ? ri - R + 1 : 0;
+                                const int dhi = ri < 2 ? ri : 2;
+                                if (dx == 0 && init && dlo == 0) dlo = 1;
+                                if (dlo > dhi) continue;
+                                const uint64_t ad = ad0 + (uint64_t)((ri * kSlabRow + dx * 32) >> 4);
+                                const uint64_t bd = bd0 + (uint64_t)((dx * 3 + dlo) * tap_step);
+                                const int nd = dhi - dlo;
+                                mma_bf16(acc_col(ri - dlo), ad, bd, nd == 0 ? idesc : nd == 1 ? idesc2 : idesc3, 1u);
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int t = 0; t < 9; ++t) {
+                            const int dy = t / 3, dx = t % 3;
+                            const uint64_t bd = bd0 + (uint64_t)((dx * 3 + dy) * tap_step);
+                            const uint32_t first = (c > 0 || t > 0) ? 1u : 0u;
+#pragma unroll
+                            for (int r = 0; r < R; ++r) {
+                                const uint64_t ad = ad0 + (uint64_t)(((r + dy) * kSlabRow + dx * 32) >> 4);
+                                mma_bf16(acc_col(r), ad, bd, idesc, first);
+                            }
                         }
                     }
                     mma_commit(&empty[s]);
@@ -540,8 +613,9 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
             s_committed = committed;
         }
     } else {
-        // epilogue: warps 2..5 -> TMEM lane quarter warp % 4
+        // epilogue: warps 2..9 -> TMEM lane quarter warp % 4, row half
         const int q = warp & 3;
+        const int half = (warp - 2) >> 2;
         for (int it = 0; it < ntiles_mine; ++it) {
             const int b = it & 1;
             int x0, y0, img;
@@ -550,59 +624,137 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
             fence_after();
             const uint32_t acc = tmem + (uint32_t)b * set_cols;
             const int xo = x0 + q * 32 + lane;
-            for (int r = 0; r < R; ++r) {
+            const uint32_t lane_acc = acc + ((uint32_t)(q * 32) << 16);
+            // Bias, activation, mask and the stores of one 16-channel chunk
+            // (c0..c0 + 15) of output row r at this lane's pixel; the head
+            // sums h0 / h1 take the chunk's BF16-rounded values.
+            auto finish = [&](int r, int c0, float (&v)[16], float& h0, float& h1) {
                 const int yo = y0 + r;
-                const bool live = xo < a.w && yo < a.h;
                 const long long p = ((long long)img * a.h + yo) * a.w + xo;
-                float h0 = a.hw ? __ldg(a.hb) : 0.0f, h1 = a.hw ? __ldg(a.hb + 1) : 0.0f;
-                for (int c0 = 0; c0 < N; c0 += 16) {
-                    float v[16];
-                    tmem_ld16(acc + ((uint32_t)(q * 32) << 16) + (uint32_t)(r * G.ncols + c0), v);
-                    if (!live) continue;
-                    if (a.bias) {
+                if (a.bias) {
 #pragma unroll
-                        for (int k = 0; k < 16; ++k) v[k] += __ldg(a.bias + c0 + k);
-                    }
-                    if (a.act == GI_ACT_RELU) {
+                    for (int k = 0; k < 16; ++k) v[k] += __ldg(a.bias + c0 + k);
+                }
+                if (a.act == GI_ACT_RELU) {
 #pragma unroll
-                        for (int k = 0; k < 16; ++k) v[k] = fmaxf(v[k], 0.0f);
-                    }
-                    const long long o = p * a.y_c + a.y_off + c0;
-                    if (a.mask) {
-                        const uint4* mp = reinterpret_cast<const uint4*>(a.mask + o);
-                        uint4 m0 = __ldg(mp), m1 = __ldg(mp + 1);
-                        const uint32_t mw[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
+                    for (int k = 0; k < 16; ++k) v[k] = fmaxf(v[k], 0.0f);
+                }
+                const long long o = p * a.y_c + a.y_off + c0;
+                if (a.mask) {
+                    const uint4* mp = reinterpret_cast<const uint4*>(a.mask + o);
+                    uint4 m0 = __ldg(mp), m1 = __ldg(mp + 1);
+                    const uint32_t mw[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
 #pragma unroll
-                        for (int k = 0; k < 16; ++k) {
-                            const uint16_t mv = (uint16_t)(mw[k >> 1] >> ((k & 1) * 16));
-                            if (!(bf16_to_f(mv) > 0.0f)) v[k] = 0.0f;
-                        }
-                    }
-                    if (a.y32) {
-                        float4* yp = reinterpret_cast<float4*>(a.y32 + p * N + c0);
-#pragma unroll
-                        for (int k = 0; k < 4; ++k)
-                            yp[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
-                    }
-                    if (a.hw) {
-#pragma unroll
-                        for (int k = 0; k < 16; ++k) {
-                            const float vb = bf16_to_f(f_to_bf16(v[k]));
-                            h0 += __ldg(a.hw + c0 + k) * vb;
-                            h1 += __ldg(a.hw + N + c0 + k) * vb;
-                        }
-                    }
-                    if (a.y) {
-                        uint32_t pk[8];
-#pragma unroll
-                        for (int k = 0; k < 8; ++k)
-                            pk[k] = (uint32_t)f_to_bf16(v[2 * k]) | ((uint32_t)f_to_bf16(v[2 * k + 1]) << 16);
-                        uint4* yp = reinterpret_cast<uint4*>(a.y + o);
-                        yp[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-                        yp[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                    for (int k = 0; k < 16; ++k) {
+                        const uint16_t mv = (uint16_t)(mw[k >> 1] >> ((k & 1) * 16));
+                        if (!(bf16_to_f(mv) > 0.0f)) v[k] = 0.0f;
                     }
                 }
-                if (a.hout && live) *reinterpret_cast<float2*>(a.hout + p * 2) = make_float2(h0, h1);
+                if (a.y32) {
+                    float4* yp = reinterpret_cast<float4*>(a.y32 + p * N + c0);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) yp[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+                }
+                if (a.hw) {
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) {
+                        const float vb = bf16_to_f(f_to_bf16(v[k]));
+                        h0 += __ldg(a.hw + c0 + k) * vb;
+                        h1 += __ldg(a.hw + N + c0 + k) * vb;
+                    }
+                }
+                if (a.y) {
+                    uint32_t pk[8];
+#pragma unroll
+                    for (int k = 0; k < 8; ++k)
+                        pk[k] = (uint32_t)f_to_bf16(v[2 * k]) | ((uint32_t)f_to_bf16(v[2 * k + 1]) << 16);
+                    const uint4 lo = make_uint4(pk[0], pk[1], pk[2], pk[3]), hi = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                    if (a.up2) {
+                        // nearest 2x upsampling: the pixel's 2 x 2 block of
+                        // the (2 h) x (2 w) output
+                        const long long W2 = 2LL * a.w;
+                        const long long p2 = ((long long)img * 2 * a.h + 2 * yo) * W2 + 2 * xo;
+#pragma unroll
+                        for (int d = 0; d < 4; ++d) {
+                            uint4* yp = reinterpret_cast<uint4*>(a.y + (p2 + (d >> 1) * W2 + (d & 1)) * a.y_c + a.y_off + c0);
+                            yp[0] = lo;
+                            yp[1] = hi;
+                        }
+                    } else {
+                        uint4* yp = reinterpret_cast<uint4*>(a.y + o);
+                        yp[0] = lo;
+                        yp[1] = hi;
+                    }
+                }
+            };
+            if (a.pool) {
+                // Rows in pairs (y0 and R are even): the 2 x 2 maximum of the
+                // finished values, the partner pixel from the neighbouring
+                // lane; even lanes store the pooled chunk.  Rounding to BF16
+                // is monotone, so this equals pooling the stored output.
+                const int wo = a.w / 2, ho = a.h / 2;
+                for (int r = 2 * half; r < R; r += 4) {
+                    const int yo = y0 + r;
+                    const bool live = xo < a.w && yo < a.h;  // w, h even: the 2 x 2 window is live as a whole
+                    for (int c0 = 0; c0 < N; c0 += 16) {
+                        float v0[16], v1[16], hu = 0.0f;
+                        uint32_t u0[16], u1[16];
+                        tmem_ld16_async(lane_acc + (uint32_t)((R - 1 - r) * kCols + c0), u0);
+                        tmem_ld16_async(lane_acc + (uint32_t)((R - 2 - r) * kCols + c0), u1);
+                        tmem_wait_ld();
+#pragma unroll
+                        for (int k = 0; k < 16; ++k) {
+                            v0[k] = __uint_as_float(u0[k]);
+                            v1[k] = __uint_as_float(u1[k]);
+                        }
+                        if (live) {
+                            finish(r, c0, v0, hu, hu);
+                            finish(r + 1, c0, v1, hu, hu);
+                        }
+                        uint32_t pk[8];
+#pragma unroll
+                        for (int k = 0; k < 16; k += 2) {
+                            float m0 = fmaxf(v0[k], v1[k]), m1 = fmaxf(v0[k + 1], v1[k + 1]);
+                            m0 = fmaxf(m0, __shfl_xor_sync(0xffffffffu, m0, 1));
+                            m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, 1));
+                            pk[k >> 1] = (uint32_t)f_to_bf16(m0) | ((uint32_t)f_to_bf16(m1) << 16);
+                        }
+                        if (live && !(lane & 1)) {
+                            const long long pp = ((long long)img * ho + yo / 2) * wo + xo / 2;
+                            uint4* yp = reinterpret_cast<uint4*>(a.pool + pp * N + c0);
+                            yp[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                            yp[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                        }
+                    }
+                }
+            } else {
+                for (int r = half; r < R; r += 2) {
+                    const int yo = y0 + r;
+                    const bool live = xo < a.w && yo < a.h;
+                    float h0 = a.hw ? __ldg(a.hb) : 0.0f, h1 = a.hw ? __ldg(a.hb + 1) : 0.0f;
+                    // two 16-column chunks in flight per wait
+                    for (int c0 = 0; c0 < N; c0 += 32) {
+                        const uint32_t col = lane_acc + (uint32_t)((R - 1 - r) * kCols + c0);
+                        const bool two = c0 + 16 < N;
+                        uint32_t u0[16], u1[16];
+                        tmem_ld16_async(col, u0);
+                        if (two) tmem_ld16_async(col + 16, u1);
+                        tmem_wait_ld();
+                        float v[16];
+#pragma unroll
+                        for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(u0[k]);
+                        if (live) finish(r, c0, v, h0, h1);
+                        if (two) {
+#pragma unroll
+                            for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(u1[k]);
+                            if (live) finish(r, c0 + 16, v, h0, h1);
+                        }
+                    }
+                    if (a.hout && live) {
+                        const long long p = ((long long)img * a.h + yo) * a.w + xo;
+                        *reinterpret_cast<float2*>(a.hout + p * 2) = make_float2(h0, h1);
+                    }
+                }
             }
             fence_before();
             asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[b])) : "memory");
@@ -846,7 +998,9 @@ __global__ void k_pack_weights(const float* __restrict__ w, int cout, int cin_re
     const long long total = (long long)rows * nkb_pad * 8;
     const int cgk = kin / 8;
     const int taps = ks * ks;
-    // the slab kernel reads stage-ordered weights [kin/16][tap][2][rows][8]
+    // the slab kernel reads stage-ordered weights [kin/16][tap'][rows/8][2][8][8]
+    // with the taps dx-major (tap' = 3 dx + dy), so that the three dy taps
+    // of one dx are one contiguous B operand of 3 x rows rows
     const bool slab = slab_layout(kin, ks);
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
          i += (long long)gridDim.x * blockDim.x) {
@@ -866,7 +1020,10 @@ __global__ void k_pack_weights(const float* __restrict__ w, int cout, int cin_re
                 const int src_tap = taps - 1 - tap;
                 if (r < cin_real) v = w[(((long long)k * cin_real + r) * ks + src_tap / ks) * ks + src_tap % ks];
             }
-            if (slab) dst = ((((long long)(g >> 1) * 9 + tap) * 2 + (g & 1)) * rows + r) * 8 + j;
+            if (slab) {
+                const int tap_dx = (tap % 3) * 3 + tap / 3;
+                dst = (((((long long)(g >> 1) * 9 + tap_dx) * (rows / 8) + (r >> 3)) * 2 + (g & 1)) * 8 + (r & 7)) * 8 + j;
+            }
         } else if (slab) {
             continue;
         }
@@ -1129,8 +1286,10 @@ gi_status launch_slab(const tc::ConvArgs& a, cudaStream_t cs) {
     CUtensorMap m;
     gi_status st = slab_map(&m, a.x, a.n, a.h, a.w, a.cin, G.R + 2);
     if (st != GI_OK) return st;
-    static std::atomic<unsigned long long> attr{0};
-    smem_opt_in(tc::k_conv3_slab, 220 * 1024, attr);
+    static std::atomic<unsigned long long> attr[4];
+    auto* kern = G.R == 8 ? tc::k_conv3_slab<8> : G.R == 4 ? tc::k_conv3_slab<4>
+               : G.R == 2 ? tc::k_conv3_slab<2> : tc::k_conv3_slab<1>;
+    smem_opt_in(kern, 220 * 1024, attr[G.R == 8 ? 3 : G.R == 4 ? 2 : G.R == 2 ? 1 : 0]);
     const int tx = (a.w + 127) / 128, ty = (a.h + G.R - 1) / G.R;
     const long long tiles = (long long)tx * ty * a.n;
     if (tiles > 0x7FFFFFFFLL) return fail(GI_ERR_INVALID_ARG, "gi_conv2d_bf16: too many tiles");
@@ -1138,7 +1297,7 @@ gi_status launch_slab(const tc::ConvArgs& a, cudaStream_t cs) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int grid = (int)std::min<long long>(tiles, sms);
-    tc::k_conv3_slab<<<grid, tc::kPersistThreads, G.NS * G.stage_bytes + 1024, cs>>>(a, m, tx, ty, (int)tiles);
+    kern<<<grid, tc::kPersistThreads, G.NS * G.stage_bytes + 1024, cs>>>(a, m, tx, ty, (int)tiles);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_conv2d_bf16 launch");
 }
@@ -1157,7 +1316,7 @@ extern "C" gi_status gi_conv2d_bf16(const gi_bf16* x, int n, int h, int w, int c
     if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(wt) | reinterpret_cast<uintptr_t>(y) |
          reinterpret_cast<uintptr_t>(mask) | reinterpret_cast<uintptr_t>(y32)) % 16)
         return fail(GI_ERR_INVALID_ARG, "gi_conv2d_bf16: tensors must be 16-byte aligned");
-    tc::ConvArgs a;
+    tc::ConvArgs a = {};
     a.x = x;
     a.n = n;
     a.h = h;
@@ -1374,6 +1533,49 @@ extern "C" gi_status gi_surrogate_loss(const float* d_head, const float* d_targe
         d_dhead, reinterpret_cast<unsigned long long*>(d_sums));
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_surrogate_loss launch");
+}
+
+extern "C" gi_status gi_conv2d_fused_bf16(const gi_bf16* x, int n, int h, int w, int cin, const gi_bf16* wt,
+                                          const float* bias, int cout, int act, gi_bf16* y, int y_stride, int y_off,
+                                          gi_bf16* pool, int upsample, uint32_t* err, void* stream) {
+    if (!x || !wt || (!y && !pool)) return fail(GI_ERR_INVALID_ARG, "gi_conv2d_fused_bf16: NULL argument");
+    if (n < 1 || h < 1 || w < 1 || cin < 16 || cin % 16 || cout < 16 || cout > 256 || cout % 16 ||
+        (act != GI_ACT_NONE && act != GI_ACT_RELU))
+        return fail(GI_ERR_INVALID_ARG, "gi_conv2d_fused_bf16: bad shape (cin % 16, cout % 16 in [16, 256])");
+    if (y && (y_stride % 8 || y_off % 8 || y_off < 0 || y_off + cout > y_stride))
+        return fail(GI_ERR_INVALID_ARG, "gi_conv2d_fused_bf16: y_stride / y_off must be multiples of 8 and fit cout");
+    if (pool && (h % 2 || w % 2 || cout > 128))
+        return fail(GI_ERR_INVALID_ARG, "gi_conv2d_fused_bf16: pooling needs even h, w and cout <= 128");
+    if (upsample && !y) return fail(GI_ERR_INVALID_ARG, "gi_conv2d_fused_bf16: upsample needs y");
+    if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(wt) | reinterpret_cast<uintptr_t>(y) |
+         reinterpret_cast<uintptr_t>(pool)) % 16)
+        return fail(GI_ERR_INVALID_ARG, "gi_conv2d_fused_bf16: tensors must be 16-byte aligned");
+    tc::ConvArgs a = {};
+    a.x = x;
+    a.n = n;
+    a.h = h;
+    a.w = w;
+    a.cin = cin;
+    a.wt = wt;
+    a.cout = cout;
+    a.nkb = tc::nkb_of(cin, 3);
+    a.nkb_pad = tc::nkb_pad_of(cin, 3);
+    a.ksize = 3;
+    a.bias = bias;
+    a.act = act;
+    a.y = y;
+    a.y_c = y ? y_stride : cout;
+    a.y_off = y ? y_off : 0;
+    a.err = err;
+    a.spin = g_wait_limit.load();
+    a.withhold = g_withhold.load();
+    a.P = (long long)n * h * w;
+    a.pool = pool;
+    a.up2 = upsample ? 1 : 0;
+    gi_status st = launch_slab(a, static_cast<cudaStream_t>(stream));
+    if (st != GI_OK) return st;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_conv2d_fused_bf16 launch");
 }
 
 extern "C" gi_status gi_conv2d_head_bf16(const gi_bf16* x, int n, int h, int w, int cin, const gi_bf16* wt,

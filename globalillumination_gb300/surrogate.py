@@ -131,6 +131,11 @@ class UNet:
         return ops.conv2d(x, L.wp, L.cout, L.k, bias=L.b, relu=relu, out=out, out_off=out_off, out32=out32,
                           err=self.err)
 
+    def _conv_fused(self, name, x, out, out_off, pool=None, upsample=False):
+        L = self.layers[name]
+        ops.conv2d_fused(x, L.wp, L.cout, bias=L.b, relu=True, out=out, out_off=out_off, pool=pool,
+                         upsample=upsample, err=self.err)
+
     def forward(self, feat: torch.Tensor, out32: torch.Tensor | None = None, keep: bool = False) -> torch.Tensor:
         n, H, W, _ = feat.shape
         assert H % 8 == 0 and W % 8 == 0, "the U-Net needs height and width divisible by 8"
@@ -172,7 +177,10 @@ class UNet:
         """Inference: forward with the 1x1 head fused into the last 3x3
         convolution's epilogue; head2 (FP32, [n, H, W, 2]) receives the
         visibility and the predicted error, the last activation is never
-        stored."""
+        stored.  The max-pools and upsamplings run in the epilogues of the
+        convolutions that produce their inputs (gi_conv2d_fused_bf16), so
+        the pooled and concatenated tensors are the same bits as forward()'s
+        without its slice, pool and upsample passes."""
         n, H, W, _ = feat.shape
         assert H % 8 == 0 and W % 8 == 0, "the U-Net needs height and width divisible by 8"
         if getattr(self, "_hw_ver", -1) != self.step_count or not hasattr(self, "_hw"):
@@ -181,24 +189,25 @@ class UNet:
             self._hb = L.b[:2].contiguous()
             self._hw_ver = self.step_count
         bf = dict(dtype=torch.bfloat16, device=feat.device)
+        # the encoders' 3x3 convolutions also write their pooled output, the
+        # decoders' second convolutions write upsampled into the next
+        # level's concatenation buffer (both fused into the epilogue)
+        fused = self._conv_fused
         t0 = self._conv("e0a", feat)
         cat0 = torch.empty((n, H, W, 96), **bf)
-        self._conv("e0b", t0, out=cat0, out_off=0)
-        p0 = ops.maxpool2(ops.channel_slice(cat0, 0, 32))
+        p0 = torch.empty((n, H // 2, W // 2, 32), **bf)
+        fused("e0b", t0, cat0, 0, pool=p0)
         t1 = self._conv("e1a", p0)
         cat1 = torch.empty((n, H // 2, W // 2, 160), **bf)
-        self._conv("e1b", t1, out=cat1, out_off=0)
-        p1 = ops.maxpool2(ops.channel_slice(cat1, 0, 64))
+        p1 = torch.empty((n, H // 4, W // 4, 64), **bf)
+        fused("e1b", t1, cat1, 0, pool=p1)
         t2 = self._conv("e2a", p1)
         cat2 = torch.empty((n, H // 4, W // 4, 224), **bf)
-        self._conv("e2b", t2, out=cat2, out_off=0)
-        p2 = ops.maxpool2(ops.channel_slice(cat2, 0, 96))
-        b3 = self._conv("e3b", self._conv("e3a", p2))
-        ops.upsample2(b3, cat2, 96)
-        u2 = self._conv("d2b", self._conv("d2a", cat2))
-        ops.upsample2(u2, cat1, 64)
-        u1 = self._conv("d1b", self._conv("d1a", cat1))
-        ops.upsample2(u1, cat0, 32)
+        p2 = torch.empty((n, H // 8, W // 8, 96), **bf)
+        fused("e2b", t2, cat2, 0, pool=p2)
+        fused("e3b", self._conv("e3a", p2), cat2, 96, upsample=True)
+        fused("d2b", self._conv("d2a", cat2), cat1, 64, upsample=True)
+        fused("d1b", self._conv("d1a", cat1), cat0, 32, upsample=True)
         u0a = self._conv("d0a", cat0)
         L = self.layers["d0b"]
         ops.conv2d_head(u0a, L.wp, L.cout, L.b, self._hw, self._hb, head2, relu=True, err=self.err)

@@ -84,6 +84,31 @@ def conv2d(x: torch.Tensor, wp: torch.Tensor, cout: int, ksize: int, bias: torch
     return out if out is not None else out32
 
 
+def conv2d_fused(x: torch.Tensor, wp: torch.Tensor, cout: int, bias: torch.Tensor | None = None, relu: bool = True,
+                 out: torch.Tensor | None = None, out_off: int = 0, pool: torch.Tensor | None = None,
+                 upsample: bool = False, err: torch.Tensor | None = None) -> None:
+    """3x3 convolution (cin % 16 == 0) with the max-pool and / or the 2x
+    nearest upsampling of its output fused into the epilogue: `pool`
+    ([n, h/2, w/2, cout]) receives maxpool2(output); with `upsample`, `out`
+    is [n, 2h, 2w, C] and receives upsample2(output) at channel out_off."""
+    n, h, w, cin = x.shape
+    _need(x, n * h * w * cin, torch.bfloat16, "x")
+    _need(wp, wp.shape[0] * nkb_pad(cin, 3) * 8, torch.bfloat16, "packed weights")
+    stride = out.shape[-1] if out is not None else cout
+    scale = 4 if upsample else 1
+    if out is not None:
+        _need(out, n * h * w * scale * stride, torch.bfloat16, "out")
+        if out_off + cout > stride:
+            raise ValueError("out_off + cout exceeds the channels of out")
+    if pool is not None:
+        _need(pool, n * (h // 2) * (w // 2) * cout, torch.bfloat16, "pool")
+    if bias is not None:
+        _need(bias, cout, torch.float32, "bias")
+    check(_lib().gi_conv2d_fused_bf16(_p(x), n, h, w, cin, _p(wp), _p(bias), cout,
+                                      api.GI_ACT_RELU if relu else api.GI_ACT_NONE, _p(out), stride, out_off,
+                                      _p(pool), 1 if upsample else 0, _p(err), _s()), "gi_conv2d_fused_bf16")
+
+
 def conv2d_head(x: torch.Tensor, wp: torch.Tensor, cout: int, bias: torch.Tensor, head_w: torch.Tensor,
                 head_b: torch.Tensor, out: torch.Tensor, relu: bool = True, err: torch.Tensor | None = None):
     """3x3 convolution with a fused two-output 1x1 head: out (FP32, [.., 2]) only."""

@@ -23,8 +23,11 @@
  * Conventions: tensors are NHWC, channel counts multiples of 8 (16 bytes),
  * row 0 at the bottom as in gi_shadow.h.  Weights are packed as
  * [cout][kblocks][8] BF16 where K-block kb = tap * (cin / 8) + channel
- * group, taps in row-major (dy, dx) order from (-1, -1); gi_pack_conv_weights
- * builds that layout from [cout][cin][kh][kw] FP32.  Every call is
+ * group, taps in row-major (dy, dx) order from (-1, -1); 3x3 kernels with
+ * cin % 16 == 0 use the same size in the order the persistent slab kernel
+ * loads them: per 16 input channels, the nine taps column-major (dx, then
+ * dy), each as [cout / 8][2][8][8].  gi_pack_conv_weights builds the right
+ * layout from [cout][cin][kh][kw] FP32.  Every call is
  * stream-ordered; `err` (device uint32, may be NULL) collects kernel error
  * bits (1 = a wait on an mbarrier ran out of its iteration limit).
  */
@@ -56,6 +59,23 @@ gi_status gi_conv2d_bf16(const gi_bf16* x, int n, int h, int w, int cin,
                          const gi_bf16* wt, const float* bias, int cout, int ksize,
                          int act, const gi_bf16* mask, gi_bf16* y, int y_stride,
                          int y_off, float* y32, uint32_t* err, void* stream);
+
+/* 3x3 convolution (cin % 16 == 0) as gi_conv2d_bf16 (no mask, no FP32
+ * output) with two optional fusions in its epilogue, both bit-identical to
+ * running the separate kernels on the stored output:
+ *   - pool (may be NULL): also writes the 2x2 max-pooled result,
+ *     pool[n][h / 2][w / 2][cout] (BF16; h and w even, cout <= 128), what
+ *     gi_maxpool2_bf16 of the output gives;
+ *   - upsample != 0: y is [n][2 h][2 w][y_stride] and receives the output
+ *     upsampled 2x (nearest) at channel y_off, what gi_upsample2_bf16 of
+ *     the output writes.
+ * y may be NULL when pool is not (only the pooled result is stored).  The
+ * U-Net's encoder layers feed its pooling this way, and its decoder layers
+ * their concatenation buffers, without the intermediate tensors. */
+gi_status gi_conv2d_fused_bf16(const gi_bf16* x, int n, int h, int w, int cin,
+                               const gi_bf16* wt, const float* bias, int cout, int act,
+                               gi_bf16* y, int y_stride, int y_off, gi_bf16* pool,
+                               int upsample, uint32_t* err, void* stream);
 
 /* 3x3 convolution (cin % 16 == 0) whose epilogue also applies a 1x1 head
  * with two outputs to the activated, BF16-rounded result and writes only

@@ -44,7 +44,15 @@ def test_gemm_as_1x1_conv(P, K, N):
 
 
 @pytest.mark.parametrize("n,h,w,cin,cin_real,cout", [(2, 13, 17, 24, 24, 32), (1, 32, 40, 8, 4, 32),
-                                                     (1, 9, 130, 96, 96, 64), (3, 16, 16, 160, 160, 128)])
+                                                     (1, 9, 130, 96, 96, 64), (3, 16, 16, 160, 160, 128),
+                                                     # slab kernel, taps stacked along N (cout 32 / 64), one
+                                                     # stage (cin 16) and ragged row / column tiles
+                                                     (2, 13, 131, 32, 32, 32), (1, 21, 40, 16, 16, 64),
+                                                     (1, 3, 200, 16, 4, 32), (1, 19, 33, 64, 64, 64),
+                                                     # slab kernel, not stacked: cout 16 and 48 (row stride
+                                                     # wider than cout), cout 96 and 256
+                                                     (1, 11, 20, 48, 48, 16), (1, 10, 150, 32, 32, 48),
+                                                     (2, 7, 30, 32, 32, 96), (1, 5, 140, 16, 16, 256)])
 def test_conv3x3_forward(n, h, w, cin, cin_real, cout):
     x = _bf(_rand(n, h, w, cin, seed=3))
     x[..., cin_real:] = 0
@@ -78,7 +86,48 @@ def test_conv_output_slice_and_mask():
     assert bool((full[..., 48:] == 0).all())
 
 
-@pytest.mark.parametrize("n,h,w,cin,cout", [(2, 12, 20, 32, 32), (1, 16, 24, 64, 96), (2, 8, 8, 96, 16)])
+@pytest.mark.parametrize("n,h,w,cin,cout,pool,up", [(1, 16, 40, 32, 32, True, False),
+                                                    (2, 10, 260, 64, 64, True, False),
+                                                    (1, 6, 10, 96, 96, True, False),
+                                                    (1, 8, 12, 128, 128, False, True),
+                                                    (1, 9, 130, 96, 64, False, True),
+                                                    (2, 14, 34, 16, 32, True, True)])
+def test_conv_fused_pool_upsample_equal_separate_kernels(n, h, w, cin, cout, pool, up):
+    """gi_conv2d_fused_bf16's pooled / upsampled outputs are bit-identical to
+    gi_maxpool2_bf16 / gi_upsample2_bf16 of gi_conv2d_bf16's output, and
+    channels outside the written slice stay untouched."""
+    x = _bf(_rand(n, h, w, cin, seed=21)).to(torch.bfloat16).cuda()
+    wp = tc_ops.pack_weights(_bf(_rand(cout, cin, 3, 3, seed=22) * 0.2).cuda(), cin)
+    b = _rand(cout, seed=23).cuda()
+    plain = tc_ops.conv2d(x, wp, cout, 3, bias=b, relu=True)
+    C, off = cout + 16, 8
+    scale = 2 if up else 1
+    out = torch.full((n, h * scale, w * scale, C), 3.0, dtype=torch.bfloat16, device="cuda")
+    pooled = torch.empty((n, h // 2, w // 2, cout), dtype=torch.bfloat16, device="cuda") if pool else None
+    tc_ops.conv2d_fused(x, wp, cout, bias=b, relu=True, out=out, out_off=off, pool=pooled, upsample=up)
+    torch.cuda.synchronize()
+    if up:
+        ref = torch.full_like(out, 3.0)
+        tc_ops.upsample2(plain, ref, off)
+        assert torch.equal(out, ref)
+    else:
+        assert torch.equal(out[..., off:off + cout], plain)
+        assert bool((out[..., :off] == 3.0).all()) and bool((out[..., off + cout:] == 3.0).all())
+    if pool:
+        assert torch.equal(pooled, tc_ops.maxpool2(plain))
+
+
+def test_conv_fused_rejects_bad_shapes():
+    from globalillumination_gb300._capi import GIError
+
+    x = torch.zeros((1, 5, 8, 32), dtype=torch.bfloat16, device="cuda")
+    wp = tc_ops.pack_weights(torch.zeros(32, 32, 3, 3, device="cuda"), 32)
+    with pytest.raises(GIError):  # odd height with pooling
+        tc_ops.conv2d_fused(x, wp, 32, pool=torch.empty((1, 2, 4, 32), dtype=torch.bfloat16, device="cuda"))
+
+
+@pytest.mark.parametrize("n,h,w,cin,cout", [(2, 12, 20, 32, 32), (1, 16, 24, 64, 96), (2, 8, 8, 96, 16),
+                                            (1, 17, 140, 64, 32)])
 def test_conv3x3_data_gradient(n, h, w, cin, cout):
     x = _bf(_rand(n, cin, h, w, seed=8)).requires_grad_(True)
     wt = _bf(_rand(cout, cin, 3, 3, seed=9) * 0.2)
