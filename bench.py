@@ -121,8 +121,8 @@ def parse_args():
                     help="render --warmup frames and exit (the command profiled with ncu)")
     ap.add_argument("--profile-case", choices=["frame", "conv", "volumes", "silhouette", "edt", "sat", "pyramid",
                                                "persistent"], default="frame",
-                    help="with --profile: the pcss_1080p frame, three U-Net convolutions at 1080p (d0a, d1a, "
-                         "d2a), the heavy scene's shadow volumes of one light at 960x540, three EDTSM "
+                    help="with --profile: the pcss_1080p frame, four U-Net convolutions at 1080p (e0a, e0b "
+                         "with its fused pool, d0a, d1a), the heavy scene's shadow volumes of one light at 960x540, three EDTSM "
                          "filters of the 1024^2 frame, or three 1024^2 moment map + SAT builds")
     return ap.parse_args()
 
@@ -1054,11 +1054,16 @@ def run_profile_case(args, local):
         from globalillumination_gb300 import surrogate as sg, tc_ops
 
         net = sg.UNet(local, seed=1)
-        for name in ("d0a", "d1a", "d2a"):
+        for name in ("e0a", "e0b", "d0a", "d1a"):
             L = net.layers[name]
             sc = sg.LEVEL_SCALE[name[:2]]
             h, w = 1080 // sc, 1920 // sc
             x = torch.randn((1, h, w, L.cin), device="cuda").to(torch.bfloat16)
+            if name == "e0b":  # as in the inference forward: into the concatenation buffer, pooled too
+                y = torch.empty((1, h, w, 96), dtype=torch.bfloat16, device="cuda")
+                p = torch.empty((1, h // 2, w // 2, L.cout), dtype=torch.bfloat16, device="cuda")
+                tc_ops.conv2d_fused(x, L.wp, L.cout, bias=L.b, relu=True, out=y, pool=p, err=net.err)
+                continue
             y = torch.empty((1, h, w, L.cout), dtype=torch.bfloat16, device="cuda")
             tc_ops.conv2d(x, L.wp, L.cout, 3, bias=L.b, relu=True, out=y, err=net.err)
         torch.cuda.synchronize()

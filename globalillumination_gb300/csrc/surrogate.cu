@@ -121,6 +121,13 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
                  : "memory");
 }
 
+// One 32-byte store (the address 32-byte aligned): a whole sector per lane.
+__device__ __forceinline__ void st_global_v8(void* ptr, const uint32_t (&v)[8]) {
+    asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(ptr), "r"(v[0]), "r"(v[1]),
+                 "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+                 : "memory");
+}
+
 // 16 consecutive FP32 columns of this thread's TMEM lane, without the
 // wait: the registers are valid after tmem_wait_ld().
 __device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t (&r)[16]) {
@@ -443,10 +450,17 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
     // MMA warp took (waited full), stages whose MMAs it committed, and
     // commits of `empty` the producer saw land.
     __shared__ int s_fail, s_loaded, s_taken, s_committed, s_freed;
+    // the epilogue's per-channel constants, read once per CTA: bias and the
+    // fused head's weights (the L1 cache is small next to the slab ring)
+    __shared__ __align__(16) float s_bias[256];
+    __shared__ __align__(16) float s_hw[512];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int N = a.cout;
     const int nk = a.cin / 16;
     const SlabGeom G = persist_geom(N, nk);
+    for (int i = tid; i < N; i += kPersistThreads) s_bias[i] = a.bias ? __ldg(a.bias + i) : 0.0f;
+    if (a.hw)
+        for (int i = tid; i < 2 * N; i += kPersistThreads) s_hw[i] = __ldg(a.hw + i);
     const int NS = G.NS;
     constexpr int kCols = 256 / R;  // accumulator columns of one output row
     const uint32_t set_cols = (uint32_t)(R * kCols);
@@ -625,6 +639,20 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
             const uint32_t acc = tmem + (uint32_t)b * set_cols;
             const int xo = x0 + q * 32 + lane;
             const uint32_t lane_acc = acc + ((uint32_t)(q * 32) << 16);
+            // 32-byte stores where every chunk of the outputs starts on a
+            // 32-byte boundary (BF16 chunks of 16 channels)
+            const bool v8_y = a.y && (reinterpret_cast<uintptr_t>(a.y) & 31) == 0 && a.y_c % 16 == 0 &&
+                              a.y_off % 16 == 0;
+            const bool v8_pool = a.pool && (reinterpret_cast<uintptr_t>(a.pool) & 31) == 0;
+            auto store_bf16 = [](uint16_t* dst, const uint32_t (&pk)[8], bool v8) {
+                if (v8) {
+                    st_global_v8(dst, pk);
+                } else {
+                    uint4* yp = reinterpret_cast<uint4*>(dst);
+                    yp[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                    yp[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                }
+            };
             // Bias, activation, mask and the stores of one 16-channel chunk
             // (c0..c0 + 15) of output row r at this lane's pixel; the head
             // sums h0 / h1 take the chunk's BF16-rounded values.
@@ -632,8 +660,15 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
                 const int yo = y0 + r;
                 const long long p = ((long long)img * a.h + yo) * a.w + xo;
                 if (a.bias) {
+                    const float4* bb = reinterpret_cast<const float4*>(s_bias + c0);
 #pragma unroll
-                    for (int k = 0; k < 16; ++k) v[k] += __ldg(a.bias + c0 + k);
+                    for (int j = 0; j < 4; ++j) {
+                        const float4 t = bb[j];
+                        v[4 * j] += t.x;
+                        v[4 * j + 1] += t.y;
+                        v[4 * j + 2] += t.z;
+                        v[4 * j + 3] += t.w;
+                    }
                 }
                 if (a.act == GI_ACT_RELU) {
 #pragma unroll
@@ -659,8 +694,8 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
 #pragma unroll
                     for (int k = 0; k < 16; ++k) {
                         const float vb = bf16_to_f(f_to_bf16(v[k]));
-                        h0 += __ldg(a.hw + c0 + k) * vb;
-                        h1 += __ldg(a.hw + N + c0 + k) * vb;
+                        h0 += s_hw[c0 + k] * vb;
+                        h1 += s_hw[N + c0 + k] * vb;
                     }
                 }
                 if (a.y) {
@@ -668,22 +703,16 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
 #pragma unroll
                     for (int k = 0; k < 8; ++k)
                         pk[k] = (uint32_t)f_to_bf16(v[2 * k]) | ((uint32_t)f_to_bf16(v[2 * k + 1]) << 16);
-                    const uint4 lo = make_uint4(pk[0], pk[1], pk[2], pk[3]), hi = make_uint4(pk[4], pk[5], pk[6], pk[7]);
                     if (a.up2) {
                         // nearest 2x upsampling: the pixel's 2 x 2 block of
                         // the (2 h) x (2 w) output
                         const long long W2 = 2LL * a.w;
                         const long long p2 = ((long long)img * 2 * a.h + 2 * yo) * W2 + 2 * xo;
 #pragma unroll
-                        for (int d = 0; d < 4; ++d) {
-                            uint4* yp = reinterpret_cast<uint4*>(a.y + (p2 + (d >> 1) * W2 + (d & 1)) * a.y_c + a.y_off + c0);
-                            yp[0] = lo;
-                            yp[1] = hi;
-                        }
+                        for (int d = 0; d < 4; ++d)
+                            store_bf16(a.y + (p2 + (d >> 1) * W2 + (d & 1)) * a.y_c + a.y_off + c0, pk, v8_y);
                     } else {
-                        uint4* yp = reinterpret_cast<uint4*>(a.y + o);
-                        yp[0] = lo;
-                        yp[1] = hi;
+                        store_bf16(a.y + o, pk, v8_y);
                     }
                 }
             };
@@ -721,9 +750,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
                         }
                         if (live && !(lane & 1)) {
                             const long long pp = ((long long)img * ho + yo / 2) * wo + xo / 2;
-                            uint4* yp = reinterpret_cast<uint4*>(a.pool + pp * N + c0);
-                            yp[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-                            yp[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                            store_bf16(a.pool + pp * N + c0, pk, v8_pool);
                         }
                     }
                 }
