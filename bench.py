@@ -119,10 +119,11 @@ def parse_args():
                     help="training frames (one 256^2 crop each, batch 16) for the surrogate leg")
     ap.add_argument("--profile", action="store_true",
                     help="render --warmup frames and exit (the command profiled with ncu)")
-    ap.add_argument("--profile-case", choices=["frame", "conv", "volumes", "silhouette", "edt", "sat", "pyramid",
-                                               "persistent"], default="frame",
+    ap.add_argument("--profile-case", choices=["frame", "conv", "wgrad", "volumes", "silhouette", "edt", "sat",
+                                               "pyramid", "persistent"], default="frame",
                     help="with --profile: the pcss_1080p frame, four U-Net convolutions at 1080p (e0a, e0b "
-                         "with its fused pool, d0a, d1a), the heavy scene's shadow volumes of one light at 960x540, three EDTSM "
+                         "with its fused pool, d0a, d1a), the weight gradients of e0b and d0a at the training size "
+                         "(16 crops of 256^2), the heavy scene's shadow volumes of one light at 960x540, three EDTSM "
                          "filters of the 1024^2 frame, or three 1024^2 moment map + SAT builds")
     return ap.parse_args()
 
@@ -1068,6 +1069,18 @@ def run_profile_case(args, local):
             tc_ops.conv2d(x, L.wp, L.cout, 3, bias=L.b, relu=True, out=y, err=net.err)
         torch.cuda.synchronize()
         print(json.dumps({"profile_case": "conv", "kernel_error": net.kernel_error()}), flush=True)
+        return 0
+    if args.profile_case == "wgrad":
+        from globalillumination_gb300 import surrogate as sg, tc_ops
+
+        net = sg.UNet(local, seed=1)
+        for name in ("e0b", "d0a"):
+            L = net.layers[name]
+            x = torch.randn((16, 256, 256, L.cin), device="cuda").to(torch.bfloat16)
+            dy = torch.randn((16, 256, 256, L.cout), device="cuda").to(torch.bfloat16)
+            tc_ops.conv2d_wgrad(x, dy, L.cout, 3, L.dwp, L.db, err=net.err)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "wgrad", "kernel_error": net.kernel_error()}), flush=True)
         return 0
     from globalillumination_gb300 import scenes
 

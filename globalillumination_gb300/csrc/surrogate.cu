@@ -973,24 +973,40 @@ __global__ void __launch_bounds__(kThreads) k_conv_wgrad(WgradArgs a) {
     if (!ok && tid == 0 && a.err) atomicOr(a.err, 1u);
 }
 
-// dw[co][r] += sum over splits of scratch[split][r][co], r < 8 * nkb.
-__global__ void k_wgrad_reduce(const float* __restrict__ scratch, int splits, int m_tiles, int cout, int nkb,
-                               int nkb_pad, float* __restrict__ dw) {
-    const long long total = (long long)8 * nkb * cout;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int co = (int)(i % cout);
-        const long long r = i / cout;
-        float s = 0.0f;
-        for (int k = 0; k < splits; ++k) s += scratch[((long long)k * m_tiles * 128 + r) * cout + co];
-        dw[(long long)co * nkb_pad * 8 + r] += s;
+// dw[co][r] += sum over splits of scratch[split][r][co], r < 8 * nkb, in a
+// fixed order: block (r, 32-channel group) of kReducePhases warps; warp t
+// sums the splits t, t + kReducePhases, ... in order, then thread 0 of each
+// lane adds the warps' sums in warp order.
+constexpr int kReducePhases = 8;
+__global__ void __launch_bounds__(32 * kReducePhases) k_wgrad_reduce(const float* __restrict__ scratch, int splits,
+                                                                      int m_tiles, int cout, int nkb, int nkb_pad,
+                                                                      float* __restrict__ dw) {
+    __shared__ float part[kReducePhases][32];
+    const int lane = threadIdx.x & 31, t = threadIdx.x >> 5;
+    const long long r = blockIdx.x;
+    const int co = blockIdx.y * 32 + lane;
+    float s = 0.0f;
+    if (co < cout) {
+        const long long stride = (long long)m_tiles * 128 * cout;
+        const float* src = scratch + r * cout + co;
+#pragma unroll 4
+        for (int k = t; k < splits; k += kReducePhases) s += __ldg(src + (long long)k * stride);
     }
+    part[t][lane] = s;
+    __syncthreads();
+    if (t == 0 && co < cout) {
+        float v = 0.0f;
+#pragma unroll
+        for (int q = 0; q < kReducePhases; ++q) v += part[q][lane];
+        dw[(long long)co * nkb_pad * 8 + r] += v;
+    }
+    (void)nkb;
 }
 
 // db[co] += sum_p dy[p][co] in a fixed order, so that training runs are
 // reproducible: thread row r of block b sums pixels b * rows + r, stepping by
 // gridDim.x * rows; the block's rows are added in row order into
-// partial[b][co], and k_bias_reduce adds the blocks in block order.
+// partial[b][co], and k_bias_reduce adds the blocks in a fixed order.
 __global__ void k_bias_grad(const uint16_t* __restrict__ dy, long long P, int cout, float* __restrict__ partial) {
     __shared__ float acc[256];
     const int c = threadIdx.x % cout;
@@ -1009,12 +1025,24 @@ __global__ void k_bias_grad(const uint16_t* __restrict__ dy, long long P, int co
     }
 }
 
-__global__ void k_bias_reduce(const float* __restrict__ partial, int blocks, int cout, float* __restrict__ db) {
-    const int co = blockIdx.x * blockDim.x + threadIdx.x;
-    if (co >= cout) return;
-    float t = 0.0f;
-    for (int b = 0; b < blocks; ++b) t += partial[(long long)b * cout + co];
-    db[co] += t;
+// db[co] += the blocks' partial sums in a fixed order: warp t of the
+// 32-channel group sums blocks t, t + 32, ... in order, then the warps'
+// sums are added in warp order.
+__global__ void __launch_bounds__(1024) k_bias_reduce(const float* __restrict__ partial, int blocks, int cout,
+                                                      float* __restrict__ db) {
+    __shared__ float part[32][33];
+    const int lane = threadIdx.x & 31, t = threadIdx.x >> 5;
+    const int co = blockIdx.x * 32 + lane;
+    float s = 0.0f;
+    if (co < cout)
+        for (int b = t; b < blocks; b += 32) s += __ldg(partial + (long long)b * cout + co);
+    part[t][lane] = s;
+    __syncthreads();
+    if (t == 0 && co < cout) {
+        float v = 0.0f;
+        for (int q = 0; q < 32; ++q) v += part[q][lane];
+        db[co] += v;
+    }
 }
 
 __global__ void k_pack_weights(const float* __restrict__ w, int cout, int cin_real, int cin, int ks, int flip,
@@ -1230,6 +1258,203 @@ __global__ void k_surrogate_loss(const float* __restrict__ head, const float* __
     }
 }
 
+// ---- weight gradient from TMA-staged, MN-major operands --------------------
+// dW[co][tap][ci] = sum over pixels p of dy[p][co] * x[p + tap][ci], with
+// K = pixels.  Both operands come straight from the NHWC tensors: a TMA box
+// of AW channels x pixels of one image row lands in shared memory as an
+// MN-major swizzled operand (channels contiguous, one 2 * AW-byte row per
+// pixel), which the MMA reads with the transpose bits set, so nothing is
+// transposed.  A unit is one (dy, AW-channel chunk): its box covers the
+// chunk's kpx + 2 pixels of input row y + dy - 1 from x0 - 1, and the
+// MMA's M = 128 rows are 128 / AW atoms of that one box at successive
+// one-pixel offsets (the atoms' stride is one row), so atom dx is tap
+// (dy, dx) and the box serves all three dx taps; atoms past dx = 2 fall in
+// TMEM lanes that are not read.  N = cout from dy boxes at the same
+// pixels.  A CTA owns a group of units (one TMEM accumulator each) and a
+// range of pixel chunks (split K); its partial sums go to scratch rows
+// tap * cin + ci, added in a fixed order by k_wgrad_reduce.
+constexpr int kWgThreads = 128;  // warp 0 TMA, warp 1 MMA; all four warps drain TMEM
+constexpr int kWgMaxStages = 6;
+constexpr int kWgMaxUnits = 16;
+
+struct WgradTmaArgs {
+    int n, h, w, cin, cout;
+    int aw, bw;                   // channels per box of x (16 or 32) / of dy (16, 32 or 64)
+    int units, units_per_cta;     // (dy, channel chunk) units in all; per CTA
+    int m_tiles, chunks_x;        // scratch rows / 128; pixel chunks per image row
+    long long chunks, per_split;  // pixel chunks in all; per CTA
+    int kpx;                      // pixels (K) per stage: 64 or 128
+    int ns, unit_bytes, a_bytes, b_bytes;
+    float* scratch;
+    uint32_t* err;
+    unsigned spin;
+    int withhold;
+};
+
+// Layout-type code of the tcgen05 shared-memory descriptor for a swizzle
+// span of 2 * channels bytes (32, 64 or 128).
+__host__ __device__ constexpr uint32_t swizzle_code(int channels) {
+    return channels == 64 ? 2u : channels == 32 ? 4u : 6u;
+}
+
+// Descriptor of an MN-major swizzled operand: `lbo` bytes between atoms of
+// `channels` MN elements, `sbo` bytes between groups of 8 K rows.
+__device__ __forceinline__ uint64_t smem_desc_mn(uint32_t addr, uint32_t lbo, uint32_t sbo, int channels) {
+    uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)swizzle_code(channels) << 61;
+    return d;
+}
+
+__global__ void __launch_bounds__(kWgThreads) k_conv_wgrad_tma(WgradTmaArgs a, const __grid_constant__ CUtensorMap xmap,
+                                                              const __grid_constant__ CUtensorMap dmap) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    __shared__ uint64_t full[kWgMaxStages], empty[kWgMaxStages], done;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int s_fail, s_loaded, s_taken, s_committed, s_freed;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int N = a.cout, NS = a.ns;
+    const int u0 = blockIdx.x * a.units_per_cta;
+    const int nu = a.units - u0 < a.units_per_cta ? a.units - u0 : a.units_per_cta;
+    const long long c_begin = (long long)blockIdx.y * a.per_split;
+    const long long c_end = c_begin + a.per_split < a.chunks ? c_begin + a.per_split : a.chunks;
+    const int nk = c_end > c_begin ? (int)(c_end - c_begin) : 0;
+    uint32_t ncols = 32;  // a power of two covering the units' accumulators (at most 512)
+    while (ncols < (uint32_t)(a.units_per_cta * N)) ncols *= 2;
+    const int stage_bytes = a.a_bytes + a.b_bytes;
+    const int chunks_c = a.cin / a.aw;
+    const int box_a = (a.kpx + 2) * a.aw * 2, box_b = a.kpx * a.bw * 2;
+    const int nb = N / a.bw;
+    if (warp == 0) tmem_alloc(&tmem_slot, ncols);
+    if (tid == 0) {
+        for (int s = 0; s < NS; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(&done, 1);
+        s_fail = 0;
+        s_loaded = s_taken = s_committed = s_freed = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_slot;
+    volatile int* fail = &s_fail;
+    auto warp_wait = [&](uint64_t* bar, unsigned parity) -> bool {
+        if (__shfl_sync(0xffffffffu, *fail, 0)) return false;
+        const bool w = mbar_wait(bar, parity, a.spin);
+        if (__any_sync(0xffffffffu, !w)) {
+            if (lane == 0) *fail = 1;
+            return false;
+        }
+        return true;
+    };
+
+    if (warp == 0) {
+        // TMA producer: per stage one x box per unit, cout / BW dy boxes
+        const uint32_t tx = (uint32_t)(nu * box_a + nb * box_b);
+        int g = 0, freed = 0;
+        for (; g < nk; ++g) {
+            const int s = g % NS;
+            if (g >= NS) {
+                if (!warp_wait(&empty[s], (unsigned)((g / NS) - 1) & 1u)) break;
+                freed = g - NS + 1;
+            }
+            if (__shfl_sync(0xffffffffu, *fail, 0)) break;
+            if (lane == 0 && !a.withhold) {
+                const long long c = c_begin + g;
+                const int x0 = (int)(c % a.chunks_x) * a.kpx;
+                const long long row = c / a.chunks_x;
+                const int y = (int)(row % a.h), img = (int)(row / a.h);
+                uint8_t* sa = smem + s * stage_bytes;
+                mbar_expect_tx(&full[s], tx);
+                for (int j = 0; j < nu; ++j) {
+                    const int u = u0 + j, dy = u / chunks_c, cc = u - dy * chunks_c;
+                    tma_load_4d(sa + j * a.unit_bytes, &xmap, cc * a.aw, x0 - 1, y + dy - 1, img, &full[s]);
+                }
+                for (int j = 0; j < nb; ++j) tma_load_4d(sa + a.a_bytes + j * box_b, &dmap, j * a.bw, x0, y, img, &full[s]);
+            }
+            __syncwarp();
+        }
+        if (lane == 0) {
+            s_loaded = a.withhold ? 0 : g;
+            s_freed = freed;
+        }
+    } else if (warp == 1) {
+        // MMA issuer: both operands MN-major (transpose bits 15 and 16);
+        // A's atoms one pixel row (2 * AW bytes) apart
+        const uint32_t idesc = idesc_bf16(128, N) | (1u << 15) | (1u << 16);
+        const uint32_t row_a = 2u * (uint32_t)a.aw, sbo_a = 8u * row_a, sbo_b = 16u * (uint32_t)a.bw;
+        int committed = 0;
+        for (int g = 0; g < nk; ++g) {
+            const int s = g % NS;
+            if (!warp_wait(&full[s], (unsigned)(g / NS) & 1u)) break;
+            if (lane == 0) {
+                fence_after();
+                const uint32_t sa = smem_u32(smem + s * stage_bytes), sb = sa + (uint32_t)a.a_bytes;
+                for (int k = 0; k < a.kpx / 16; ++k) {
+                    const uint64_t bd = smem_desc_mn(sb + (uint32_t)k * 2u * sbo_b, (uint32_t)box_b, sbo_b, a.bw);
+                    for (int j = 0; j < nu; ++j) {
+                        const uint64_t ad = smem_desc_mn(sa + (uint32_t)(j * a.unit_bytes) + (uint32_t)k * 16u * row_a,
+                                                         row_a, sbo_a, a.aw);
+                        mma_bf16(tmem + (uint32_t)(j * N), ad, bd, idesc, (g > 0 || k > 0) ? 1u : 0u);
+                    }
+                }
+                mma_commit(&empty[s]);
+                if (g == nk - 1) mma_commit(&done);
+            }
+            committed = g + 1;
+            __syncwarp();
+        }
+        if (lane == 0) {
+            s_taken = committed;
+            s_committed = committed;
+        }
+    }
+    __syncthreads();
+    // every MMA landed (the last commit), or a wait ran out: then drain the
+    // loads nobody took and the commits nobody saw (bounded waits) first
+    bool ok = !*fail;
+    if (ok && nk > 0 && !mbar_wait(&done, 0u, a.spin)) ok = false;
+    const bool all_ok = __syncthreads_and(ok);
+    if (!all_ok && lane == 0) {
+        if (warp == 0) {
+            for (int g = s_taken; g < s_loaded; ++g) mbar_wait(&full[g % NS], (unsigned)(g / NS) & 1u, a.spin);
+        } else if (warp == 1) {
+            for (int g = s_freed; g < s_committed; ++g) mbar_wait(&empty[g % NS], (unsigned)(g / NS) & 1u, a.spin);
+        }
+    }
+    fence_after();
+    // lane m of unit (dy, cc): tap (dy, m / AW), channel cc * AW + m % AW
+    const int m = warp * 32 + lane;
+    const int dx = m / a.aw;
+    const long long split_row = (long long)blockIdx.y * a.m_tiles * 128;
+    for (int j = 0; all_ok && j < nu; ++j) {
+        const int u = u0 + j, dy = u / chunks_c, cc = u - dy * chunks_c;
+        const long long r = (long long)(dy * 3 + dx) * a.cin + cc * a.aw + m % a.aw;
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(j * N + c0), v);
+            if (dx > 2) continue;
+            if (nk == 0) {
+#pragma unroll
+                for (int q = 0; q < 16; ++q) v[q] = 0.0f;
+            }
+            float4* o = reinterpret_cast<float4*>(a.scratch + (split_row + r) * N + c0);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, ncols);
+    if (!all_ok && tid == 0 && a.err) atomicOr(a.err, 1u);
+}
+
 unsigned grid1d(long long n, int threads) {
     long long b = (n + threads - 1) / threads;
     return (unsigned)std::max<long long>(1, std::min<long long>(b, 152LL * 16));
@@ -1293,6 +1518,75 @@ gi_status slab_map(CUtensorMap* m, const uint16_t* x, int n, int h, int w, int c
                                 box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B,
                                 CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? GI_OK : fail(GI_ERR_CUDA, "cuTensorMapEncodeTiled rejected the activation map");
+}
+
+// The TMA weight-gradient kernel serves 3x3 convolutions with cin % 16 == 0
+// (every 3x3 layer of the U-Net); 1x1 and other shapes keep the gather kernel.
+bool wgrad_uses_tma(int cin, int ks) { return ks == 3 && cin % 16 == 0; }
+
+int box_channels(int c) { return c % 64 == 0 ? 64 : c % 32 == 0 ? 32 : 16; }
+
+tc::WgradTmaArgs wgrad_tma_plan(int n, int h, int w, int cin, int cout) {
+    tc::WgradTmaArgs a = {};
+    a.n = n;
+    a.h = h;
+    a.w = w;
+    a.cin = cin;
+    a.cout = cout;
+    a.aw = cin % 32 == 0 ? 32 : 16;  // 128 / AW atoms per MMA, at least the three dx taps
+    a.bw = box_channels(cout);
+    a.units = 3 * (cin / a.aw);
+    a.m_tiles = (9 * cin + 127) / 128;
+    // The loads are latency-bound (a TMA round trip takes several thousand
+    // cycles), so a stage should carry as many bytes as the ring allows:
+    // 128 pixels per stage where every unit of a CTA still fits four
+    // stages, else 64 pixels and at least three.  A unit's box region holds
+    // kpx + 2 loaded rows plus the rows the atoms past dx = 2 read,
+    // 1024-byte aligned for the swizzle; units per CTA are also bounded by
+    // TMEM (one cout-wide accumulator each, 512 columns).
+    const int want = std::min(std::min(a.units, tc::kWgMaxUnits), 512 / cout);
+    for (int kpx : {128, 64}) {
+        const int min_stages = kpx == 128 ? 4 : 3;
+        a.kpx = kpx;
+        a.unit_bytes = ((kpx + 128 / a.aw) * a.aw * 2 + 1023) / 1024 * 1024;
+        a.b_bytes = cout * kpx * 2;
+        int per = want;
+        while (per > 1 && min_stages * (per * a.unit_bytes + a.b_bytes) > 200 * 1024) --per;
+        a.units_per_cta = per;
+        if (per == want) break;
+    }
+    a.a_bytes = a.units_per_cta * a.unit_bytes;
+    a.ns = std::min(tc::kWgMaxStages, (200 * 1024) / (a.a_bytes + a.b_bytes));
+    a.chunks_x = (w + a.kpx - 1) / a.kpx;
+    a.chunks = (long long)n * h * a.chunks_x;
+    // one wave: a CTA per SM over all unit groups, at least 4 chunks each
+    const int groups = (a.units + a.units_per_cta - 1) / a.units_per_cta;
+    long long splits = std::max<long long>(1, 152 / groups);
+    splits = std::min<long long>(splits, std::max<long long>(1, a.chunks / 4));
+    a.per_split = (a.chunks + splits - 1) / splits;
+    return a;
+}
+
+int wgrad_tma_groups(const tc::WgradTmaArgs& a) { return (a.units + a.units_per_cta - 1) / a.units_per_cta; }
+
+long long wgrad_tma_splits(const tc::WgradTmaArgs& a) { return (a.chunks + a.per_split - 1) / a.per_split; }
+
+// 4-D map (c, w, h, n) of an NHWC BF16 tensor with boxes of `box_c`
+// channels x `box_px` pixels of one row, swizzled over 2 * box_c bytes:
+// the MN-major operands of the weight-gradient kernel.
+gi_status wgrad_map(CUtensorMap* m, const uint16_t* t, int n, int h, int w, int c, int box_c, int box_px) {
+    gi_status st = tensor_map_fn();
+    if (st != GI_OK) return st;
+    const cuuint64_t dims[4] = {(cuuint64_t)c, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
+    const cuuint64_t strides[3] = {(cuuint64_t)c * 2, (cuuint64_t)w * c * 2, (cuuint64_t)h * w * c * 2};
+    const cuuint32_t box[4] = {(cuuint32_t)box_c, (cuuint32_t)box_px, 1, 1};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    const CUtensorMapSwizzle sw = box_c == 64 ? CU_TENSOR_MAP_SWIZZLE_128B
+                                 : box_c == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B;
+    CUresult r = g_encode_tiled(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<uint16_t*>(t), dims, strides, box,
+                                es, CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? GI_OK : fail(GI_ERR_CUDA, "cuTensorMapEncodeTiled rejected a weight-gradient map");
 }
 
 // Opt a kernel into more than 48 KB of dynamic shared memory, once per
@@ -1402,6 +1696,10 @@ WgradPlan wgrad_plan(long long P, int cin, int ks) {
 
 extern "C" size_t gi_conv2d_wgrad_scratch_floats(int n, int h, int w, int cin, int cout, int ksize) {
     if (n < 1 || h < 1 || w < 1 || cin < 8 || cout < 16) return 0;
+    if (wgrad_uses_tma(cin, ksize)) {
+        const tc::WgradTmaArgs a = wgrad_tma_plan(n, h, w, cin, cout);
+        return (size_t)wgrad_tma_splits(a) * a.m_tiles * 128 * cout;
+    }
     WgradPlan pl = wgrad_plan((long long)n * h * w, cin, ksize);
     return (size_t)pl.splits * pl.m_tiles * 128 * cout;
 }
@@ -1418,37 +1716,57 @@ extern "C" gi_status gi_conv2d_wgrad_bf16(const gi_bf16* x, const gi_bf16* dy, i
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const long long P = (long long)n * h * w;
     WgradPlan pl = wgrad_plan(P, cin, ksize);
-    tc::WgradArgs a;
-    a.x = x;
-    a.dy = dy;
-    a.n = n;
-    a.h = h;
-    a.w = w;
-    a.cin = cin;
-    a.cout = cout;
-    a.ksize = ksize;
-    a.nkb = tc::nkb_of(cin, ksize);
-    a.m_tiles = pl.m_tiles;
-    a.P = P;
-    a.px_per_split = pl.px_per_split;
-    a.scratch = scratch;
-    a.err = err;
-    a.spin = g_wait_limit.load();
-    a.withhold = g_withhold.load();
-    const int smem = tc::kNS * (tc::kStageA + (cout / 8) * tc::kSBO);
-    static std::atomic<unsigned long long> attr{0};
-    smem_opt_in(tc::k_conv_wgrad, 4 * (8192 + 16384), attr);
-    tc::k_conv_wgrad<<<dim3(pl.m_tiles, pl.splits), tc::kThreads, smem, st>>>(a);
-    const long long red = (long long)8 * a.nkb * cout;
-    tc::k_wgrad_reduce<<<tc::grid1d(red, 256), 256, 0, st>>>(scratch, pl.splits, pl.m_tiles, cout, a.nkb,
-                                                            tc::nkb_pad_of(cin, ksize), dw);
+    if (wgrad_uses_tma(cin, ksize)) {
+        tc::WgradTmaArgs t = wgrad_tma_plan(n, h, w, cin, cout);
+        const long long splits = wgrad_tma_splits(t);
+        if (splits > 65535) return fail(GI_ERR_INVALID_ARG, "gi_conv2d_wgrad_bf16: too many pixel splits");
+        t.scratch = scratch;
+        t.err = err;
+        t.spin = g_wait_limit.load();
+        t.withhold = g_withhold.load();
+        CUtensorMap xm, dm;
+        gi_status gs = wgrad_map(&xm, x, n, h, w, cin, t.aw, t.kpx + 2);
+        if (gs == GI_OK) gs = wgrad_map(&dm, dy, n, h, w, cout, t.bw, t.kpx);
+        if (gs != GI_OK) return gs;
+        static std::atomic<unsigned long long> attr_tma{0};
+        smem_opt_in(tc::k_conv_wgrad_tma, 220 * 1024, attr_tma);
+        const int smem = t.ns * (t.a_bytes + t.b_bytes) + 1024;
+        tc::k_conv_wgrad_tma<<<dim3(wgrad_tma_groups(t), (unsigned)splits), tc::kWgThreads, smem, st>>>(t, xm, dm);
+        pl.m_tiles = t.m_tiles;  // the reduction below reads this kernel's partial sums
+        pl.splits = (int)splits;
+    } else {
+        tc::WgradArgs a;
+        a.x = x;
+        a.dy = dy;
+        a.n = n;
+        a.h = h;
+        a.w = w;
+        a.cin = cin;
+        a.cout = cout;
+        a.ksize = ksize;
+        a.nkb = tc::nkb_of(cin, ksize);
+        a.m_tiles = pl.m_tiles;
+        a.P = P;
+        a.px_per_split = pl.px_per_split;
+        a.scratch = scratch;
+        a.err = err;
+        a.spin = g_wait_limit.load();
+        a.withhold = g_withhold.load();
+        const int smem = tc::kNS * (tc::kStageA + (cout / 8) * tc::kSBO);
+        static std::atomic<unsigned long long> attr{0};
+        smem_opt_in(tc::k_conv_wgrad, 4 * (8192 + 16384), attr);
+        tc::k_conv_wgrad<<<dim3(pl.m_tiles, pl.splits), tc::kThreads, smem, st>>>(a);
+    }
+    const int nkb = tc::nkb_of(cin, ksize);
+    tc::k_wgrad_reduce<<<dim3((unsigned)(8 * nkb), (unsigned)((cout + 31) / 32)), 32 * tc::kReducePhases, 0, st>>>(
+        scratch, pl.splits, pl.m_tiles, cout, nkb, tc::nkb_pad_of(cin, ksize), dw);
     if (db) {
         // the partial sums reuse the scratch k_wgrad_reduce has finished
         // reading (at least 128 x cout floats)
         const long long cap = (long long)pl.splits * pl.m_tiles * 128;
         const int blocks = (int)std::max<long long>(1, std::min<long long>(std::min<long long>(1216, (P + 63) / 64), cap));
         tc::k_bias_grad<<<blocks, 256, 0, st>>>(dy, P, cout, scratch);
-        tc::k_bias_reduce<<<(cout + 127) / 128, 128, 0, st>>>(scratch, blocks, cout, db);
+        tc::k_bias_reduce<<<(cout + 31) / 32, 1024, 0, st>>>(scratch, blocks, cout, db);
     }
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_conv2d_wgrad_bf16 launch");

@@ -1,8 +1,9 @@
 """Bounded mbarrier waits of the tcgen05 kernels: a wait that runs out ends the kernel cleanly.
 
 With the test switch on, every convolution kernel withholds its first
-asynchronous stage (the TMA loads of the persistent slab kernel, the MMAs of
-the gather and weight-gradient kernels), so its first wait on that stage
+asynchronous stage (the TMA loads of the persistent slab kernel and of the
+3x3 weight-gradient kernel, the MMAs of the gather kernels), so its first
+wait on that stage
 can never complete.  With a short wait limit each kernel must then stop
 issuing work, skip its tensor-memory reads, free its tensor memory, set bit
 0 of the error word and return: the stream synchronises, and the next
@@ -68,6 +69,20 @@ def _cases():
 
     xf, df = xg.reshape(-1, 16), dyg.reshape(-1, 32)
     out.append(("wgrad", wgrad, df.t() @ xf, df.abs().t() @ xf.abs()))
+    # weight gradient (3x3, TMA-fed kernel)
+    x3 = _bf(_rand(1, 32, 6, 70, seed=17))
+    d3 = _bf(_rand(1, 32, 6, 70, seed=18))
+    x3c = x3.permute(0, 2, 3, 1).contiguous().to(torch.bfloat16).cuda()
+    d3c = d3.permute(0, 2, 3, 1).contiguous().to(torch.bfloat16).cuda()
+
+    def wgrad3(err):
+        dw = torch.zeros(32 * tc_ops.nkb_pad(32, 3) * 8, device="cuda")
+        tc_ops.conv2d_wgrad(x3c, d3c, 32, 3, dw, err=err)
+        return tc_ops.unpack_grad(dw.reshape(32, -1, 8), 32, 32, 32, 3)
+
+    ref3 = torch.nn.grad.conv2d_weight(x3, (32, 32, 3, 3), d3, padding=1)
+    abs3 = torch.nn.grad.conv2d_weight(x3.abs(), (32, 32, 3, 3), d3.abs(), padding=1)
+    out.append(("wgrad3x3", wgrad3, ref3, abs3))
     return out
 
 

@@ -144,7 +144,11 @@ def test_conv3x3_data_gradient(n, h, w, cin, cout):
 
 
 @pytest.mark.parametrize("n,h,w,cin,cout", [(2, 12, 20, 32, 32), (1, 33, 47, 8, 32), (4, 16, 16, 64, 128),
-                                            (1, 40, 64, 224, 96)])
+                                            (1, 40, 64, 224, 96),
+                                            # TMA kernel: 16- / 32- / 64-channel boxes, rows longer
+                                            # than one 64-pixel chunk, several images, cout 256
+                                            (1, 9, 70, 16, 32), (1, 10, 130, 96, 32), (1, 6, 65, 160, 64),
+                                            (1, 5, 20, 32, 256), (3, 7, 9, 48, 16)])
 def test_conv3x3_weight_gradient(n, h, w, cin, cout):
     x = _bf(_rand(n, cin, h, w, seed=11))
     wt = _bf(_rand(cout, cin, 3, 3, seed=12)).requires_grad_(True)
