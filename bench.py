@@ -8,7 +8,11 @@ one shadowed frame: light-view depth map, G-buffer, visibility.
 
   value   frames/s with the scene resident in HBM, timed per step with CUDA
           events on the launching stream; L2 is flushed (256 MiB write)
-          before every timed step, outside the step's events
+          before every timed step, outside the step's events.  Each step is
+          one gi_render_frame call on a context with its frame graph on
+          (gi_context_set_frame_graph): the repeated frame replays one
+          captured CUDA graph of its 13 kernels.  `direct_launch` gives the
+          same frames (and e2e) with the 13 kernels launched from the host
   e2e     frames/s through the C ABI with host buffers: every step uploads
           the scene from pinned host memory (gi_scene_upload_from), renders,
           and reads the visibility buffer back to pinned host memory; several
@@ -1188,6 +1192,11 @@ def run_ours(args):
         print(json.dumps({"profile_frames": max(args.warmup, 1), "launches": ctx.launch_count}), flush=True)
         ctx.close()
         return 0
+    # The headline runs gi_render_frame with the context's frame graph on
+    # (gi_context_set_frame_graph): the repeated frame replays one captured
+    # CUDA graph of its 13 kernels.  The same frames launched directly are
+    # timed below and reported beside it.
+    ctx.set_frame_graph(True)
     for _ in range(max(args.warmup, 3)):
         frame()
     torch.cuda.synchronize()
@@ -1259,11 +1268,13 @@ def run_ours(args):
     # overlap the other in-flight frames'; every step still uploads the
     # whole scene from pinned host memory and reads the whole visibility
     # image back.
-    def run_e2e(D):
+    def run_e2e(D, graph=False):
         h_vis = [torch.empty(P, dtype=torch.float32).pin_memory() for _ in range(D)]
         e2e_scenes = [gi.Scene() for _ in range(D)]
         e2e_bufs = [bufs] + [gi.allocate_frame(S, S, W, H, local) for _ in range(D - 1)]
         e2e_ctx = [ctx] + [gi.Context(local) for _ in range(D - 1)]
+        for c in e2e_ctx:
+            c.set_frame_graph(graph)
         e2e_streams = [stream] + [torch.cuda.Stream() for _ in range(D - 1)]
         up_stream, down_stream = torch.cuda.Stream(), torch.cuda.Stream()
         up_done = [torch.cuda.Event() for _ in range(D)]
@@ -1308,16 +1319,40 @@ def run_ours(args):
         ms = e0.elapsed_time(e1)
         for c in e2e_ctx[1:]:
             c.close()
+        ctx.set_frame_graph(False)
         return ms
 
     e2e_depth = 4
-    e2e_ms_by_depth = {d: run_e2e(d) for d in (2, e2e_depth)}
+    e2e_ms_by_depth = {d: run_e2e(d, graph=True) for d in (2, e2e_depth)}
     e2e_ms = e2e_ms_by_depth[e2e_depth]
     if dist is not None:
         t = torch.tensor([e2e_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
     e2e_value = world * K / (e2e_ms / 1000.0)
+
+    # ---- the same frames launched directly (frame graph off) ---------------
+    ctx.set_frame_graph(False)
+    for _ in range(3):
+        frame()
+    barrier()
+    d_starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    d_ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    for k in range(K):
+        flush.fill_(float(k))
+        d_starts[k].record(stream)
+        frame()
+        d_ends[k].record(stream)
+    barrier()
+    direct_ms = sum(a.elapsed_time(b) for a, b in zip(d_starts, d_ends))
+    direct_e2e_ms = run_e2e(e2e_depth, graph=False)
+    if dist is not None:
+        t = torch.tensor([direct_ms, direct_e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        direct_ms, direct_e2e_ms = float(t[0].item()), float(t[1].item())
+    direct = {"frames_per_s": world * K / (direct_ms / 1000.0), "ms_per_step": direct_ms / K,
+              "e2e_frames_per_s": world * K / (direct_e2e_ms / 1000.0),
+              "note": "gi_render_frame with the frame graph off: 13 kernel launches per frame from the host"}
     h2d = pts.nbytes + nrm.nbytes + idx.nbytes
     d2h = P * 4
     clk = clocks.stop()
@@ -1375,6 +1410,8 @@ def run_ours(args):
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic_from_profiles(),
                          "algorithmic_bytes_per_launch": int(alg_bytes)},
             "pass_ms": pass_ms,
+            "frame_graph": True,
+            "direct_launch": direct,
             "step_ms_median": statistics.median(step_ms),
             "wall_s_timed_region": wall,
             "clocks": clk,
@@ -1434,6 +1471,10 @@ def compact_summary(line: dict) -> dict:
 
     out = {"frames_per_s": _r(line["value"]), "e2e_frames_per_s": _r(line["e2e"]["value"]),
            "roofline_frac": _r(line["roofline"]["frac"], 3)}
+    dl = line.get("direct_launch")
+    if dl:
+        out["direct_launch_frames_per_s"] = _r(dl["frames_per_s"])
+        out["direct_launch_e2e_frames_per_s"] = _r(dl["e2e_frames_per_s"])
     m = line.get("batched_surrogate_1080p")
     if m:
         out["1080p_batched_x"] = _r(m["batched_ratio_over_plain"], 3)

@@ -214,6 +214,7 @@ _PROTOS = {
                                                      _VP, _VP, C.POINTER(C.c_int), _VP]),
     "gi_light_map_minmax": (C.c_int, [_VP, _VP, C.c_int, C.c_int, _VP, _VP]),
     "gi_context_set_tap_pyramid": (C.c_int, [_VP, C.c_int]),
+    "gi_context_set_frame_graph": (C.c_int, [_VP, C.c_int]),
     "gi_phong_shade": (C.c_int, [_VP, C.POINTER(VisParams), _VP, _VP, _VP, _VP, C.c_int, C.c_int, _VP, _VP]),
     "gi_pba_voronoi": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP]),
     "gi_edt_soft_shadows": (C.c_int, [_VP, _VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float,

@@ -61,8 +61,15 @@ void alloc_point() {
     if (alloc_fail_due()) throw std::bad_alloc();
 }
 
+namespace {
+std::atomic<uint64_t> g_buffer_epoch{0};
+}
+uint64_t buffer_epoch() { return g_buffer_epoch.load(std::memory_order_acquire); }
+void bump_buffer_epoch() { g_buffer_epoch.fetch_add(1, std::memory_order_acq_rel); }
+
 gi_status ensure_buffer(void** ptr, size_t* cap, size_t bytes) {
     if (*cap >= bytes && *ptr) return GI_OK;
+    bump_buffer_epoch();
     if (alloc_fail_due())
         return fail(GI_ERR_OOM, std::string("cudaMalloc of ") + std::to_string(bytes) +
                                     " bytes failed (injected allocation failure)");
@@ -149,6 +156,8 @@ extern "C" void gi_context_destroy(gi_context* c) {
         for (int i = 0; i < 8; ++i) cudaFree(c->tier_buf[k][i]);
     for (int i = 0; i < 4; ++i)
         if (c->phase_ev[i]) cudaEventDestroy(static_cast<cudaEvent_t>(c->phase_ev[i]));
+    if (c->fg_exec) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(c->fg_exec));
+    if (c->fg_stream) cudaStreamDestroy(static_cast<cudaStream_t>(c->fg_stream));
     if (c->aux_stream) cudaStreamDestroy(static_cast<cudaStream_t>(c->aux_stream));
     if (c->fork_ev) cudaEventDestroy(static_cast<cudaEvent_t>(c->fork_ev));
     if (c->join_ev) cudaEventDestroy(static_cast<cudaEvent_t>(c->join_ev));
@@ -162,6 +171,18 @@ extern "C" uint64_t gi_context_launch_count(const gi_context* c) { return c ? c-
 extern "C" gi_status gi_context_set_tap_pyramid(gi_context* c, int enable) {
     if (!c) return fail(GI_ERR_INVALID_ARG, "gi_context_set_tap_pyramid: NULL context");
     c->tap_pyramid = enable != 0;
+    return GI_OK;
+}
+
+extern "C" gi_status gi_context_set_frame_graph(gi_context* c, int enable) {
+    if (!c) return fail(GI_ERR_INVALID_ARG, "gi_context_set_frame_graph: NULL context");
+    c->frame_graph = enable != 0;
+    if (!c->frame_graph && c->fg_exec) {
+        cudaSetDevice(c->device);
+        cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(c->fg_exec));
+        c->fg_exec = nullptr;
+    }
+    c->fg_seen = false;
     return GI_OK;
 }
 
@@ -204,6 +225,7 @@ extern "C" void gi_scene_destroy(gi_scene* s) {
     if (!s) return;
     if (s->device >= 0) {
         cudaSetDevice(s->device);
+        gi::bump_buffer_epoch();
         cudaFree(s->d_points);
         cudaFree(s->d_normals);
         cudaFree(s->d_indices);
@@ -215,6 +237,7 @@ extern "C" void gi_scene_destroy(gi_scene* s) {
 // A failed upload leaves no usable device copy: free what is left and mark
 // the scene, so that passes refuse it until it is uploaded again.
 static gi_status drop_device_copy(gi_scene* s, gi_status st) {
+    gi::bump_buffer_epoch();
     cudaFree(s->d_points);
     cudaFree(s->d_normals);
     cudaFree(s->d_indices);
@@ -545,6 +568,38 @@ extern "C" gi_status gi_visibility(gi_context* ctx, const gi_vis_params* p, cons
                                  static_cast<cudaStream_t>(stream));
 }
 
+// The launch sequence of one frame on stream cs: the camera-key pass on the
+// context's second stream, concurrently with the light map, then the fused
+// resolve + visibility kernel once both are done.
+static gi_status enqueue_frame(gi_context* ctx, const gi_scene* s, const gi_map_params* mp,
+                               const float light_mvp[16], const float camera_mvp[16], const gi_vis_params* vp,
+                               int W, int H, float* d_depth, float* d_vis, float* d_pos, float* d_nrm,
+                               cudaStream_t cs) {
+    cudaStream_t aux = static_cast<cudaStream_t>(ctx->aux_stream);
+    auto mark = [&](int i) {
+        if (ctx->profiling) cudaEventRecord(static_cast<cudaEvent_t>(ctx->phase_ev[i]), cs);
+    };
+    mark(0);
+    cudaError_t e = cudaEventRecord(static_cast<cudaEvent_t>(ctx->fork_ev), cs);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, static_cast<cudaEvent_t>(ctx->fork_ev), 0);
+    if (e != cudaSuccess) return gi::fail_cuda(e, "gi_render_frame: fork");
+    gi_status st = gi::raster_gbuffer_keys(ctx, s, camera_mvp, W, H, aux);
+    e = cudaEventRecord(static_cast<cudaEvent_t>(ctx->join_ev), aux);
+    if (st == GI_OK)
+        st = gi::raster_depth_map(ctx, s, light_mvp, mp->width, mp->height, mp->bias_mode,
+                                  mp->constant_bias, mp->offset_factor, mp->offset_units, d_depth,
+                                  small_px_default(), cs);
+    mark(1);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, static_cast<cudaEvent_t>(ctx->join_ev), 0);
+    if (e != cudaSuccess) return gi::fail_cuda(e, "gi_render_frame: join");
+    mark(2);
+    if (st == GI_OK)
+        st = gi::launch_frame_visibility(ctx, vp, d_depth, mp->width, mp->height, s, camera_mvp, d_vis,
+                                         W, H, d_pos, d_nrm, cs);
+    mark(3);
+    return st;
+}
+
 extern "C" gi_status gi_render_frame(gi_context* ctx, const gi_scene* s, const gi_map_params* mp,
                                      const float light_mvp[16], const float camera_mvp[16],
                                      const gi_vis_params* vp, int W, int H, float* d_depth,
@@ -565,31 +620,88 @@ extern "C" gi_status gi_render_frame(gi_context* ctx, const gi_scene* s, const g
     if ((size_t)s->dev_triangles >= ((size_t)1 << 29))
         return fail(GI_ERR_CAPACITY, "gi_render_frame: more than 2^29 triangles");
     cudaStream_t cs = static_cast<cudaStream_t>(stream);
-    cudaStream_t aux = static_cast<cudaStream_t>(ctx->aux_stream);
-    auto mark = [&](int i) {
-        if (ctx->profiling) cudaEventRecord(static_cast<cudaEvent_t>(ctx->phase_ev[i]), cs);
-    };
-    // the camera-key pass runs on the context's second stream, concurrently
-    // with the light map; the visibility kernel waits for both
-    mark(0);
-    cudaError_t e = cudaEventRecord(static_cast<cudaEvent_t>(ctx->fork_ev), cs);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, static_cast<cudaEvent_t>(ctx->fork_ev), 0);
-    if (e != cudaSuccess) return gi::fail_cuda(e, "gi_render_frame: fork");
-    st = gi::raster_gbuffer_keys(ctx, s, camera_mvp, W, H, aux);
-    e = cudaEventRecord(static_cast<cudaEvent_t>(ctx->join_ev), aux);
-    if (st == GI_OK)
-        st = gi::raster_depth_map(ctx, s, light_mvp, mp->width, mp->height, mp->bias_mode,
-                                  mp->constant_bias, mp->offset_factor, mp->offset_units, d_depth,
-                                  small_px_default(), cs);
-    mark(1);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, static_cast<cudaEvent_t>(ctx->join_ev), 0);
-    if (e != cudaSuccess) return gi::fail_cuda(e, "gi_render_frame: join");
-    mark(2);
-    if (st == GI_OK)
-        st = gi::launch_frame_visibility(ctx, vp, d_depth, mp->width, mp->height, s, camera_mvp, d_vis,
-                                         W, H, d_pos, d_nrm, cs);
-    mark(3);
-    return st;
+    if (!ctx->frame_graph || ctx->profiling)
+        return enqueue_frame(ctx, s, mp, light_mvp, camera_mvp, vp, W, H, d_depth, d_vis, d_pos, d_nrm, cs);
+    // Frame graph: a new argument signature runs eagerly once (allocating
+    // what the frame needs); the next call with the same signature captures
+    // the launch sequence into a graph on the context's capture stream;
+    // later ones replay it with one launch.
+    gi::FrameSig sig;
+    std::memset(&sig, 0, sizeof(sig));
+    sig.scene = s;
+    sig.points = s->d_points;
+    sig.normals = s->d_normals;
+    sig.indices = s->d_indices;
+    sig.triangles = s->dev_triangles;
+    sig.mp = *mp;
+    std::memcpy(sig.light_mvp, light_mvp, sizeof(sig.light_mvp));
+    std::memcpy(sig.camera_mvp, camera_mvp, sizeof(sig.camera_mvp));
+    sig.vp = *vp;
+    sig.W = W;
+    sig.H = H;
+    sig.depth = d_depth;
+    sig.vis = d_vis;
+    sig.pos = d_pos;
+    sig.nrm = d_nrm;
+    sig.tiny_px = ctx->tiny_px;
+    sig.coop_px = ctx->coop_px;
+    sig.tap_pyramid = ctx->tap_pyramid ? 1 : 0;
+    sig.epoch = gi::buffer_epoch();
+    const bool same = ctx->fg_seen && std::memcmp(&sig, &ctx->fg_sig, sizeof(sig)) == 0;
+    if (same && ctx->fg_exec) {
+        cudaError_t e = cudaGraphLaunch(static_cast<cudaGraphExec_t>(ctx->fg_exec), cs);
+        if (e != cudaSuccess) return gi::fail_cuda(e, "gi_render_frame: graph launch");
+        ctx->launches += ctx->fg_launches;
+        return GI_OK;
+    }
+    if (!same) {
+        ctx->fg_seen = false;
+        st = enqueue_frame(ctx, s, mp, light_mvp, camera_mvp, vp, W, H, d_depth, d_vis, d_pos, d_nrm, cs);
+        if (st != GI_OK) return st;
+        ctx->fg_sig = sig;
+        ctx->fg_sig.epoch = gi::buffer_epoch();  // what this run allocated belongs to the frame
+        ctx->fg_seen = true;
+        if (ctx->fg_exec) {  // the graph of an older signature is of no further use
+            cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(ctx->fg_exec));
+            ctx->fg_exec = nullptr;
+        }
+        return GI_OK;
+    }
+    cudaError_t e = cudaSuccess;
+    if (!ctx->fg_stream) {
+        cudaStream_t fs = nullptr;
+        e = cudaStreamCreateWithFlags(&fs, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return gi::fail_cuda(e, "gi_render_frame: capture stream");
+        ctx->fg_stream = fs;
+    }
+    cudaStream_t fs = static_cast<cudaStream_t>(ctx->fg_stream);
+    e = cudaStreamBeginCapture(fs, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return gi::fail_cuda(e, "gi_render_frame: begin capture");
+    const uint64_t launches0 = ctx->launches;
+    st = enqueue_frame(ctx, s, mp, light_mvp, camera_mvp, vp, W, H, d_depth, d_vis, d_pos, d_nrm, fs);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(fs, &graph);
+    const uint64_t held = ctx->launches - launches0;
+    ctx->launches = launches0;
+    if (st != GI_OK || e != cudaSuccess || !graph) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        ctx->fg_seen = false;
+        return st != GI_OK ? st : gi::fail_cuda(e == cudaSuccess ? cudaErrorUnknown : e, "gi_render_frame: capture");
+    }
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        ctx->fg_seen = false;
+        return gi::fail_cuda(e, "gi_render_frame: graph instantiate");
+    }
+    ctx->fg_exec = exec;
+    ctx->fg_launches = held;
+    e = cudaGraphLaunch(exec, cs);
+    if (e != cudaSuccess) return gi::fail_cuda(e, "gi_render_frame: graph launch");
+    ctx->launches += held;
+    return GI_OK;
 }
 
 // UniformSampledLightSource::computeUniformSampling

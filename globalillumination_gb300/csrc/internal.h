@@ -72,6 +72,32 @@ struct gi_scene {
 };
 
 // Device scratch owned by a context.  Buffers only grow.
+namespace gi {
+// Everything a gi_render_frame launch sequence depends on besides device
+// memory contents: the scene's device copy, the call's arguments, the
+// context's raster tuning and tap-pyramid switch, and the buffer epoch.
+// Compared bytewise (filled after a memset).
+struct FrameSig {
+    const void* scene;
+    const void* points;
+    const void* normals;
+    const void* indices;
+    int triangles;
+    gi_map_params mp;
+    float light_mvp[16];
+    float camera_mvp[16];
+    gi_vis_params vp;
+    int W, H;
+    const void* depth;
+    const void* vis;
+    const void* pos;
+    const void* nrm;
+    int tiny_px, coop_px;
+    int tap_pyramid;
+    uint64_t epoch;
+};
+}  // namespace gi
+
 struct gi_context {
     int device = 0;
     uint64_t launches = 0;
@@ -152,9 +178,24 @@ struct gi_context {
     // phase timing (cudaEvent_t handles) for gi_render_frame
     bool profiling = false;
     void* phase_ev[4] = {};
+    // frame graph (gi_context_set_frame_graph): the arguments of the last
+    // gi_render_frame call, whether they have run once eagerly, the graph
+    // captured from them (cudaGraphExec_t), the kernels it holds, and the
+    // stream it was captured on (cudaStream_t)
+    bool frame_graph = false;
+    gi::FrameSig fg_sig = {};
+    bool fg_seen = false;
+    void* fg_exec = nullptr;
+    uint64_t fg_launches = 0;
+    void* fg_stream = nullptr;
 };
 
 namespace gi {
 // Grows a device buffer to at least `bytes` (cudaMalloc). Returns GI_OK or an error.
 gi_status ensure_buffer(void** ptr, size_t* cap, size_t bytes);
+// Bumped by every device allocation of ensure_buffer and every free of a
+// scene's device copy: a captured frame graph whose epoch differs may hold
+// stale pointers and is captured again.
+uint64_t buffer_epoch();
+void bump_buffer_epoch();
 }

@@ -81,6 +81,10 @@ class Context:
         """Build the light map's min-max pyramid for exact tap skipping of larger boxes."""
         check(_lib().gi_context_set_tap_pyramid(self.handle, 1 if enable else 0), "gi_context_set_tap_pyramid")
 
+    def set_frame_graph(self, enable: bool) -> None:
+        """Replay repeated render_frame calls (same arguments) as one captured CUDA graph."""
+        check(_lib().gi_context_set_frame_graph(self.handle, 1 if enable else 0), "gi_context_set_frame_graph")
+
     def set_profiling(self, enable: bool) -> None:
         check(_lib().gi_context_set_profiling(self.handle, int(bool(enable))), "gi_context_set_profiling")
 

@@ -95,6 +95,18 @@ gi_status gi_context_phase_ms(gi_context* ctx, float ms[3]);
  * (one more launch per pass).  Off by default.  Results do not depend on
  * it. */
 gi_status gi_context_set_tap_pyramid(gi_context* ctx, int enable);
+/* Frame graph of gi_render_frame (no counterpart in the reference, whose
+ * frame is a sequence of GL draws): with enable != 0 the context keeps the
+ * launch sequence of the last gi_render_frame call as a CUDA graph.  A call
+ * whose arguments, scene device copy and context settings all equal the
+ * previous call's replays it with one graph launch (the first repeat
+ * captures it; a new argument set runs the launches directly once).  Any
+ * device buffer (re)allocation by the library, or freeing of a scene's
+ * device copy, invalidates it.  The graph reads device memory when it
+ * runs, so new scene contents uploaded into the same buffers are used.
+ * Results do not depend on it; timing events (gi_context_set_profiling)
+ * bypass it.  Off by default. */
+gi_status gi_context_set_frame_graph(gi_context* ctx, int enable);
 
 /* ------------------------------------------------------------------ */
 /* Scene (host geometry + optional device copy)                        */
