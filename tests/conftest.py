@@ -7,9 +7,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-# The reference tree, present only where the fixtures are made (GI_REFERENCE_ROOT
-# overrides the default); tests that read it skip elsewhere.
-REFERENCE = os.environ.get("GI_REFERENCE_ROOT", "/root/reference")
+# The reference tree, present only where the fixtures are made; its location
+# is the oracle build recipe's (GI_REFERENCE_ROOT overrides it).  Tests that
+# read it skip elsewhere.
+from oracle.build_oracle import REFERENCE_ROOT as REFERENCE  # noqa: E402
 
 
 def pytest_configure(config):
