@@ -72,6 +72,10 @@ def test_pass_argument_checks_before_device_work():
     assert lib.gi_visibility(None, C.byref(p), None, 4, 4, None, None, None, 4, 4, None) == api.GI_ERR_INVALID_ARG
     assert lib.gi_shadow_map(None, None, None, api.F16(), None, None) == api.GI_ERR_INVALID_ARG
     assert lib.gi_gbuffer(None, None, api.F16(), 4, 4, None, None, None) == api.GI_ERR_INVALID_ARG
+    # context switches reject a NULL context
+    assert lib.gi_context_set_frame_graph(None, 1) == api.GI_ERR_INVALID_ARG
+    assert lib.gi_context_set_tap_pyramid(None, 1) == api.GI_ERR_INVALID_ARG
+    assert lib.gi_context_set_tuning(None, 96, 1024) == api.GI_ERR_INVALID_ARG
 
 
 def test_poisson_table():
