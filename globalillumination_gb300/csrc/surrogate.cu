@@ -458,9 +458,6 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
     const int N = a.cout;
     const int nk = a.cin / 16;
     const SlabGeom G = persist_geom(N, nk);
-    for (int i = tid; i < N; i += kPersistThreads) s_bias[i] = a.bias ? __ldg(a.bias + i) : 0.0f;
-    if (a.hw)
-        for (int i = tid; i < 2 * N; i += kPersistThreads) s_hw[i] = __ldg(a.hw + i);
     const int NS = G.NS;
     constexpr int kCols = 256 / R;  // accumulator columns of one output row
     const uint32_t set_cols = (uint32_t)(R * kCols);
@@ -479,6 +476,17 @@ __global__ void __launch_bounds__(kPersistThreads) k_conv3_slab(ConvArgs a, cons
         s_loaded = s_taken = s_committed = s_freed = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    // Launched as a programmatic dependent of the previous kernel in the
+    // stream: everything above touches only shared and tensor memory, so it
+    // overlaps that kernel's tail; no global memory is read or written
+    // before the previous grid has completed and its writes are visible.
+    // The next kernel may then be scheduled onto SMs as this grid's CTAs
+    // finish.  (Both are no-ops for an ordinary launch.)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    for (int i = tid; i < N; i += kPersistThreads) s_bias[i] = a.bias ? __ldg(a.bias + i) : 0.0f;
+    if (a.hw)
+        for (int i = tid; i < 2 * N; i += kPersistThreads) s_hw[i] = __ldg(a.hw + i);
     fence_before();
     __syncthreads();
     fence_after();
@@ -1618,8 +1626,20 @@ gi_status launch_slab(const tc::ConvArgs& a, cudaStream_t cs) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int grid = (int)std::min<long long>(tiles, sms);
-    kern<<<grid, tc::kPersistThreads, G.NS * G.stage_bytes + 1024, cs>>>(a, m, tx, ty, (int)tiles);
-    cudaError_t e = cudaGetLastError();
+    // programmatic dependent launch: the prologue overlaps the previous
+    // kernel's tail (the kernel waits for it before any global access)
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(tc::kPersistThreads);
+    cfg.dynamicSmemBytes = (size_t)(G.NS * G.stage_bytes + 1024);
+    cfg.stream = cs;
+    cudaLaunchAttribute attr_pdl[1];
+    attr_pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr_pdl[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr_pdl;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, a, m, tx, ty, (int)tiles);
+    if (e == cudaSuccess) e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_conv2d_bf16 launch");
 }
 }  // namespace
