@@ -1305,6 +1305,7 @@ __device__ void tier_sub(const TierArgs& a, const float* c0, const float* c1, co
 
 template <int MODE>
 __global__ void __launch_bounds__(128) k_tier_setup(TierArgs a) {
+    pdl_enter();
     int prim = blockIdx.x * blockDim.x + threadIdx.x;
     if (prim >= a.r.num_prims) return;
     float v[3][3];
@@ -1341,6 +1342,7 @@ __device__ __forceinline__ unsigned long long rec_tiles(const BRec& r) {
 __global__ void __launch_bounds__(1024) k_large_scan(TierArgs a) {
     __shared__ unsigned long long warp_sums[32];
     __shared__ int nhuge;
+    pdl_enter();
     const unsigned n = a.ctr[3];
     if (threadIdx.x == 0) nhuge = 0;
     __syncthreads();
@@ -1379,6 +1381,7 @@ template <int MODE>
 __global__ void __launch_bounds__(256) k_base(TierArgs a) {
     typedef typename BinVal<MODE>::T V;
     __shared__ BRec hr[kHugeMax];
+    pdl_enter();
     const int nh = (int)a.ctr[6];
     if (threadIdx.x < nh) hr[threadIdx.x] = a.recs[a.ctr[16 + threadIdx.x]];
     __syncthreads();
@@ -1580,6 +1583,7 @@ __device__ __forceinline__ void coop_record(const TierArgs& a, unsigned i, int l
 // Their atomic updates commute, so the order does not change the result.
 template <int MODE>
 __global__ void __launch_bounds__(256) k_tiny_coop(TierArgs a) {
+    pdl_enter();
     const unsigned ncoop = a.ctr[2], ntiny = a.ctr[1];
     const unsigned units = ncoop + (ntiny + 31) / 32;
     const int lane = threadIdx.x & 31;
@@ -1598,6 +1602,7 @@ __global__ void __launch_bounds__(256) k_tiny_coop(TierArgs a) {
 // 16 x 16 tile list, reject tiles the triangle misses, 8 pixels per lane.
 template <int MODE>
 __global__ void __launch_bounds__(256) k_large_tiles(TierArgs a) {
+    pdl_enter();
     const unsigned n = a.ctr[3];
     const unsigned long long total = *reinterpret_cast<const unsigned long long*>(a.ctr + 8);
     if (n == 0 || total == 0) return;
@@ -1668,6 +1673,7 @@ __global__ void __launch_bounds__(256) k_large_tiles(TierArgs a) {
 // Spilled sub-triangles of the tiered passes (one thread each, atomics).
 template <int MODE>
 __global__ void __launch_bounds__(128) k_tier_spill(TierArgs a) {
+    pdl_enter();
     const unsigned n = min(a.ctr[4], a.spill_cap);
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const unsigned id = a.spill[i];
@@ -1895,22 +1901,49 @@ static gi_status run_tiered(gi_context* ctx, dev::RasterArgs& r, int mode, cudaS
     const unsigned sms = (unsigned)sm_count(ctx->device);
     const unsigned gsetup = grid_for(prims ? prims : 1, 128);
     const dim3 gbase((r.W + 31) / 32, (r.H + 31) / 32);
+    // Launched directly, each kernel after the first is a programmatic
+    // dependent of the one before it (pdl_enter): it is scheduled while that
+    // one drains and waits for it before touching global memory (pcss_1080p
+    // frame 8,700 -> 9,360 frames/s).  Under stream capture (frame graphs,
+    // batches) the kernels are ordinary nodes: with several frames in flight
+    // the waiting CTAs held SM slots the other frames could use (graph-mode
+    // end to end 11,100 -> 10,600 frames/s).
+    cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &capturing) != cudaSuccess) {
+        cudaGetLastError();
+        capturing = cudaStreamCaptureStatusActive;  // unknown: launch ordinarily
+    }
+    const bool pdl = capturing == cudaStreamCaptureStatusNone;
+    auto chain = [&](auto kernel, dim3 grid, int threads) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = grid;
+        cfg.blockDim = dim3((unsigned)threads);
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = pdl ? 1 : 0;
+        cudaError_t le = cudaLaunchKernelEx(&cfg, kernel, a);
+        if (le != cudaSuccess && e == cudaSuccess) e = le;
+    };
     if (mode == dev::MODE_DEPTH) {
         if (prims) dev::k_tier_setup<dev::MODE_DEPTH><<<gsetup, 128, 0, st>>>(a);
-        dev::k_large_scan<<<1, 1024, 0, st>>>(a);
-        dev::k_base<dev::MODE_DEPTH><<<gbase, 256, 0, st>>>(a);
-        dev::k_tiny_coop<dev::MODE_DEPTH><<<sms * 8, 256, 0, st>>>(a);
-        dev::k_large_tiles<dev::MODE_DEPTH><<<sms * 8, 256, 0, st>>>(a);
-        dev::k_tier_spill<dev::MODE_DEPTH><<<sms * 2, 128, 0, st>>>(a);
+        chain(dev::k_large_scan, dim3(1), 1024);
+        chain(dev::k_base<dev::MODE_DEPTH>, gbase, 256);
+        chain(dev::k_tiny_coop<dev::MODE_DEPTH>, dim3(sms * 8), 256);
+        chain(dev::k_large_tiles<dev::MODE_DEPTH>, dim3(sms * 8), 256);
+        chain(dev::k_tier_spill<dev::MODE_DEPTH>, dim3(sms * 2), 128);
     } else {
         if (prims) dev::k_tier_setup<dev::MODE_VKEY><<<gsetup, 128, 0, st>>>(a);
-        dev::k_large_scan<<<1, 1024, 0, st>>>(a);
-        dev::k_base<dev::MODE_VKEY><<<gbase, 256, 0, st>>>(a);
-        dev::k_tiny_coop<dev::MODE_VKEY><<<sms * 8, 256, 0, st>>>(a);
-        dev::k_large_tiles<dev::MODE_VKEY><<<sms * 8, 256, 0, st>>>(a);
-        dev::k_tier_spill<dev::MODE_VKEY><<<sms * 2, 128, 0, st>>>(a);
+        chain(dev::k_large_scan, dim3(1), 1024);
+        chain(dev::k_base<dev::MODE_VKEY>, gbase, 256);
+        chain(dev::k_tiny_coop<dev::MODE_VKEY>, dim3(sms * 8), 256);
+        chain(dev::k_large_tiles<dev::MODE_VKEY>, dim3(sms * 8), 256);
+        chain(dev::k_tier_spill<dev::MODE_VKEY>, dim3(sms * 2), 128);
     }
     ctx->launches += prims ? 6 : 5;
+    if (e != cudaSuccess) return fail_cuda(e, "tiered raster launch");
     e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "tiered raster launch");
 }
