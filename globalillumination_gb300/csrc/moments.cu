@@ -40,6 +40,7 @@
 
 #include "internal.h"
 #include "raster.h"
+#include "launch.cuh"
 
 namespace gi {
 namespace mom {
@@ -89,6 +90,7 @@ __device__ __forceinline__ float4 moment_of(const MomArgs& a, float d, bool empt
 
 // The moment map at the light map's own size (map side == window side).
 __global__ void __launch_bounds__(256) k_moments(const MomArgs a) {
+    pdl_enter();
     const int x = blockIdx.x * 32 + (threadIdx.x & 31);
     const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
     if (x >= a.S || y >= a.S) return;
@@ -106,6 +108,7 @@ __global__ void __launch_bounds__(256) k_moments(const MomArgs a) {
 // box average ((q00 + q10) + (q01 + q11)) * 0.25, so the full-size moment
 // map is never stored.
 __global__ void __launch_bounds__(256) k_moments_box(const MomArgs a) {
+    pdl_enter();
     const int h = a.S / 2;
     const int x = blockIdx.x * 32 + (threadIdx.x & 31);
     const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
@@ -127,6 +130,7 @@ __device__ __forceinline__ float4 add4(float4 a, float4 b) { return make_float4(
 
 // One mip level of glGenerateMipmap as a 2 x 2 box: ((a + b) + (c + d)) * 0.25.
 __global__ void __launch_bounds__(256) k_mip_box(const float4* __restrict__ in, int S, float4* __restrict__ out) {
+    pdl_enter();
     const int h = S / 2;
     const int x = blockIdx.x * 32 + (threadIdx.x & 31);
     const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
@@ -143,6 +147,7 @@ __global__ void __launch_bounds__(256) k_mip_box(const float4* __restrict__ in, 
 template <bool LOG>
 __global__ void __launch_bounds__(256) k_moment_blur(const float4* __restrict__ in, int N, int dx, int dy,
                                                      float4* __restrict__ out) {
+    pdl_enter();
     const int x = blockIdx.x * 32 + (threadIdx.x & 31);
     const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
     if (x >= N || y >= N) return;
@@ -189,8 +194,9 @@ __device__ __forceinline__ float soft_lin_at(const SoftMomArgs& a, int x, int y,
     return gl_linearize(d);
 }
 
-template <bool TWO>
+template <bool TWO, bool DEP>
 __global__ void __launch_bounds__(256) k_soft_moments(const SoftMomArgs a) {
+    if (DEP) pdl_enter();
     const int x = blockIdx.x * 32 + (threadIdx.x & 31);
     const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
     if (x >= a.S || y >= a.T) return;
@@ -227,8 +233,10 @@ __global__ void __launch_bounds__(256) k_soft_moments(const SoftMomArgs a) {
 //   t(x, y) = s(x, y) + s(x - d, y),  s'(x, y) = t(x, y) + t(x, y - d),
 // i.e. s' = (s(x, y) + s(x - d, y)) + (s(x, y - d) + s(x - d, y - d)), reads
 // outside the map being 0 (CLAMP_TO_BORDER), each sum rounded as written.
+template <bool DEP>  // DEP: launched as a programmatic dependent (launch_dependent_if)
 __global__ void __launch_bounds__(256) k_sat_level(const float4* __restrict__ in, int S, int T, int d,
                                                    float4* __restrict__ out) {
+    if (DEP) pdl_enter();
     const int x = blockIdx.x * 32 + (threadIdx.x & 31);
     const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
     if (x >= S || y >= T) return;
@@ -243,9 +251,10 @@ __global__ void __launch_bounds__(256) k_sat_level(const float4* __restrict__ in
 
 // The same over the .xy of SAVSM / VSSM tables, whose .zw stay +0 (sums of
 // +0): half the traffic; the last iteration writes the float4 table.
-template <bool LAST>
+template <bool LAST, bool DEP>
 __global__ void __launch_bounds__(256) k_sat_level2(const float2* __restrict__ in, int S, int T, int d,
                                                     float2* __restrict__ out2, float4* __restrict__ out4) {
+    if (DEP) pdl_enter();
     const int x = blockIdx.x * 32 + (threadIdx.x & 31);
     const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
     if (x >= S || y >= T) return;
@@ -293,6 +302,7 @@ __device__ __forceinline__ float2 hsm_minmax(const F& tex, int i, int j) {
 
 __global__ void __launch_bounds__(256) k_hsm_level0(const float* __restrict__ depth, int S, int T, float alpha,
                                                     float beta, float2* __restrict__ out) {
+    pdl_enter();
     const int x = blockIdx.x * 32 + (threadIdx.x & 31);
     const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
     if (x >= S || y >= T) return;
@@ -302,6 +312,7 @@ __global__ void __launch_bounds__(256) k_hsm_level0(const float* __restrict__ de
 // level 1 straight from the light map (level 0 is never stored)
 __global__ void __launch_bounds__(256) k_hsm_first(const float* __restrict__ depth, int S, int T, float alpha,
                                                    float beta, float2* __restrict__ out) {
+    pdl_enter();
     const int w = S / 2, h = T / 2;
     const int x = blockIdx.x * 32 + (threadIdx.x & 31);
     const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
@@ -312,6 +323,7 @@ __global__ void __launch_bounds__(256) k_hsm_first(const float* __restrict__ dep
 
 __global__ void __launch_bounds__(256) k_hsm_next(const float2* __restrict__ in, int pw, int ph,
                                                   float2* __restrict__ out) {
+    pdl_enter();
     const int w = pw / 2, h = ph / 2;
     const int x = blockIdx.x * 32 + (threadIdx.x & 31);
     const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
@@ -354,6 +366,10 @@ gi_status launch_soft_moment_map(gi_context* ctx, const gi_vis_params* p, const 
     float mqi[16];
     moment_quantization(a.mq, mqi, &a.tq0);
     const dim3 grid((S + 31) / 32, (T + 7) / 8);
+    // the chain of log2(S) dependent passes as programmatic dependent
+    // launches up to 1024^2 (SAVSM 0.073 -> 0.062 ms, MSSM 0.083 -> 0.062
+    // ms); ordinary launches above (the 2048^2 two-channel table lost 18 %)
+    const bool small = (size_t)S * T <= (size_t)1024 * 1024;
     if (two) {
         // .xy planes ping-pong in the scratch, the last iteration writes the
         // float4 table into dst (or the scratch's first part)
@@ -365,13 +381,21 @@ gi_status launch_soft_moment_map(gi_context* ctx, const gi_vis_params* p, const 
         float2* pb = pa + n;
         a.out = nullptr;
         a.out2 = pa;
-        k_soft_moments<true><<<grid, 256, 0, st>>>(a);
+        if (small) launch_dependent_if(true, k_soft_moments<true, true>, grid, dim3(256), 0, st, a);
+        else k_soft_moments<true, false><<<grid, 256, 0, st>>>(a);
         ctx->launches++;
         const float2* cur = pa;
         for (int i = 0; i < m; ++i) {
             float2* nxt = (cur == pa) ? pb : pa;
-            if (i == m - 1) k_sat_level2<true><<<grid, 256, 0, st>>>(cur, S, T, 1 << i, nullptr, last);
-            else k_sat_level2<false><<<grid, 256, 0, st>>>(cur, S, T, 1 << i, nxt, nullptr);
+            float2* o2 = i == m - 1 ? nullptr : nxt;
+            float4* o4 = i == m - 1 ? last : nullptr;
+            if (small) {
+                if (i == m - 1) launch_dependent_if(true, k_sat_level2<true, true>, grid, dim3(256), 0, st, cur, S, T, 1 << i, o2, o4);
+                else launch_dependent_if(true, k_sat_level2<false, true>, grid, dim3(256), 0, st, cur, S, T, 1 << i, o2, o4);
+            } else {
+                if (i == m - 1) k_sat_level2<true, false><<<grid, 256, 0, st>>>(cur, S, T, 1 << i, o2, o4);
+                else k_sat_level2<false, false><<<grid, 256, 0, st>>>(cur, S, T, 1 << i, o2, o4);
+            }
             ctx->launches++;
             cur = nxt;
         }
@@ -389,12 +413,14 @@ gi_status launch_soft_moment_map(gi_context* ctx, const gi_vis_params* p, const 
     float4* spare = dst ? reinterpret_cast<float4*>(ctx->d_mom) : last + n;
     a.out = (m % 2 == 0) ? last : spare;
     a.out2 = nullptr;
-    k_soft_moments<false><<<grid, 256, 0, st>>>(a);
+    if (small) launch_dependent_if(true, k_soft_moments<false, true>, grid, dim3(256), 0, st, a);
+    else k_soft_moments<false, false><<<grid, 256, 0, st>>>(a);
     ctx->launches++;
     float4* cur = a.out;
     for (int i = 0; i < m; ++i) {
         float4* nxt = (cur == last) ? spare : last;
-        k_sat_level<<<grid, 256, 0, st>>>(cur, S, T, 1 << i, nxt);
+        if (small) launch_dependent_if(true, k_sat_level<true>, grid, dim3(256), 0, st, cur, S, T, 1 << i, nxt);
+        else k_sat_level<false><<<grid, 256, 0, st>>>(cur, S, T, 1 << i, nxt);
         ctx->launches++;
         cur = nxt;
     }
@@ -417,9 +443,9 @@ static gi_status hsm_levels(gi_context* ctx, const gi_vis_params* p, const float
         const int w = S >> k, h = T >> k;
         const dim3 grid((w + 31) / 32, (h + 7) / 8);
         if (k == 1)
-            k_hsm_first<<<grid, 256, 0, st>>>(d_depth, S, T, p->hsm_alpha, p->hsm_beta, lv);
+            launch_dependent(k_hsm_first, grid, dim3(256), 0, st, d_depth, S, T, p->hsm_alpha, p->hsm_beta, lv);
         else
-            k_hsm_next<<<grid, 256, 0, st>>>(levels[k - 1], S >> (k - 1), T >> (k - 1), lv);
+            launch_dependent(k_hsm_next, grid, dim3(256), 0, st, (const float2*)levels[k - 1], S >> (k - 1), T >> (k - 1), lv);
         ctx->launches++;
         lv += (size_t)w * h;
     }
@@ -434,7 +460,7 @@ gi_status launch_hsm(gi_context* ctx, const gi_vis_params* p, const float* d_dep
         gi_status s = ensure_buffer(reinterpret_cast<void**>(&ctx->d_hsm), &ctx->cap_hsm, (size_t)S * T * sizeof(float2));
         if (s != GI_OK) return s;
         float2* lv = reinterpret_cast<float2*>(ctx->d_hsm);
-        k_hsm_level0<<<dim3((S + 31) / 32, (T + 7) / 8), 256, 0, st>>>(d_depth, S, T, p->hsm_alpha, p->hsm_beta, lv);
+        launch_dependent(k_hsm_level0, dim3((S + 31) / 32, (T + 7) / 8), dim3(256), 0, st, d_depth, S, T, p->hsm_alpha, p->hsm_beta, lv);
         ctx->launches++;
         *out = lv;
         cudaError_t e = cudaGetLastError();
@@ -540,10 +566,10 @@ gi_status launch_moments(gi_context* ctx, int tech, const float* d_depth, int S,
     int side = S;
     if (S > W) {
         // the first box level straight from the depths, at the scratch's start
-        k_moments_box<<<dim3((S / 2 + 31) / 32, (S / 2 + 7) / 8), 256, 0, st>>>(ma);
+        launch_dependent(k_moments_box, dim3((S / 2 + 31) / 32, (S / 2 + 7) / 8), dim3(256), 0, st, ma);
         side = S / 2;
     } else {
-        k_moments<<<dim3((S + 31) / 32, (S + 7) / 8), 256, 0, st>>>(ma);
+        launch_dependent(k_moments, dim3((S + 31) / 32, (S + 7) / 8), dim3(256), 0, st, ma);
     }
     ctx->launches++;
     // further box levels, ping-ponging between the two parts of the scratch
@@ -551,7 +577,7 @@ gi_status launch_moments(gi_context* ctx, int tech, const float* d_depth, int S,
     float4* other = lvl + (size_t)side * side;
     for (; side > W; side /= 2) {
         float4* dst = (lvl == first) ? other : first;
-        k_mip_box<<<dim3((side / 2 + 31) / 32, (side / 2 + 7) / 8), 256, 0, st>>>(lvl, side, dst);
+        launch_dependent(k_mip_box, dim3((side / 2 + 31) / 32, (side / 2 + 7) / 8), dim3(256), 0, st, (const float4*)lvl, side, dst);
         ctx->launches++;
         lvl = dst;
     }
@@ -559,11 +585,11 @@ gi_status launch_moments(gi_context* ctx, int tech, const float* d_depth, int S,
     float4* by = bx + (size_t)W * W;
     const dim3 grid((W + 31) / 32, (W + 7) / 8);
     if (tech == GI_TECH_ESM) {
-        k_moment_blur<true><<<grid, 256, 0, st>>>(lvl, W, 1, 0, bx);
-        k_moment_blur<true><<<grid, 256, 0, st>>>(bx, W, 0, 1, by);
+        launch_dependent(k_moment_blur<true>, grid, dim3(256), 0, st, (const float4*)lvl, W, 1, 0, bx);
+        launch_dependent(k_moment_blur<true>, grid, dim3(256), 0, st, (const float4*)bx, W, 0, 1, by);
     } else {
-        k_moment_blur<false><<<grid, 256, 0, st>>>(lvl, W, 1, 0, bx);
-        k_moment_blur<false><<<grid, 256, 0, st>>>(bx, W, 0, 1, by);
+        launch_dependent(k_moment_blur<false>, grid, dim3(256), 0, st, (const float4*)lvl, W, 1, 0, bx);
+        launch_dependent(k_moment_blur<false>, grid, dim3(256), 0, st, (const float4*)bx, W, 0, 1, by);
     }
     ctx->launches += 2;
     *filtered = reinterpret_cast<const float*>(by);

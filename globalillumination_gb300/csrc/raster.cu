@@ -1901,30 +1901,13 @@ static gi_status run_tiered(gi_context* ctx, dev::RasterArgs& r, int mode, cudaS
     const unsigned sms = (unsigned)sm_count(ctx->device);
     const unsigned gsetup = grid_for(prims ? prims : 1, 128);
     const dim3 gbase((r.W + 31) / 32, (r.H + 31) / 32);
-    // Launched directly, each kernel after the first is a programmatic
-    // dependent of the one before it (pdl_enter): it is scheduled while that
-    // one drains and waits for it before touching global memory (pcss_1080p
-    // frame 8,700 -> 9,360 frames/s).  Under stream capture (frame graphs,
-    // batches) the kernels are ordinary nodes: with several frames in flight
-    // the waiting CTAs held SM slots the other frames could use (graph-mode
-    // end to end 11,100 -> 10,600 frames/s).
-    cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
-    if (cudaStreamIsCapturing(st, &capturing) != cudaSuccess) {
-        cudaGetLastError();
-        capturing = cudaStreamCaptureStatusActive;  // unknown: launch ordinarily
-    }
-    const bool pdl = capturing == cudaStreamCaptureStatusNone;
+    // Each kernel after the first is a programmatic dependent of the one
+    // before it (launch_dependent, pdl_enter): launched directly, the
+    // pcss_1080p frame went 8,700 -> 9,400 frames/s; under stream capture
+    // (frame graphs, batches) the launches are ordinary (with the dependents
+    // inside frame graphs, graph-mode end to end fell 11,100 -> 10,600).
     auto chain = [&](auto kernel, dim3 grid, int threads) {
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = grid;
-        cfg.blockDim = dim3((unsigned)threads);
-        cfg.stream = st;
-        cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-        at[0].val.programmaticStreamSerializationAllowed = 1;
-        cfg.attrs = at;
-        cfg.numAttrs = pdl ? 1 : 0;
-        cudaError_t le = cudaLaunchKernelEx(&cfg, kernel, a);
+        cudaError_t le = launch_dependent(kernel, grid, dim3((unsigned)threads), 0, st, a);
         if (le != cudaSuccess && e == cudaSuccess) e = le;
     };
     if (mode == dev::MODE_DEPTH) {

@@ -9,6 +9,7 @@
 #pragma once
 
 #include <cstdint>
+#include "launch.cuh"
 
 namespace gi {
 namespace dev {
@@ -235,15 +236,6 @@ __device__ __forceinline__ float i2f(int64_t v) {
 // three is negative.
 __device__ __forceinline__ int tl_bias(bool tl) { return tl ? 0 : 1; }
 
-// First statement of a kernel launched as a programmatic dependent of the
-// previous kernel in its stream: wait until that grid has completed and its
-// writes are visible (nothing global is touched before), then let the next
-// kernel be scheduled as this grid's CTAs finish.  No-ops for an ordinary
-// launch.
-__device__ __forceinline__ void pdl_enter() {
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
 
 __device__ __forceinline__ bool inside_biased(const int64_t E[3]) {
     return ((int)(E[0] >> 32) | (int)(E[1] >> 32) | (int)(E[2] >> 32)) >= 0;
