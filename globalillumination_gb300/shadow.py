@@ -40,8 +40,10 @@ def _f3(v) -> api.F3:
 
 
 def _f16(m) -> api.F16:
-    a = np.asarray(m, dtype=np.float32).reshape(-1)
-    return api.F16(*[float(x) for x in a])
+    a = np.ascontiguousarray(m, dtype=np.float32).reshape(-1)
+    if a.size != 16:
+        raise ValueError("a 4x4 matrix needs 16 values")
+    return api.F16.from_buffer_copy(a)
 
 
 def _stream_ptr(stream) -> C.c_void_p:
@@ -327,6 +329,28 @@ class ShadowParams:
                    pretest=p.pretest)
 
     def to_c(self, frame: Frame) -> api.VisParams:
+        # The scalar part is built once per set of field values (fields may
+        # change between calls) and copied; the frame's matrices are copied
+        # straight from their float32 buffers.
+        key = (self.technique, self.pretest, self.shadow_intensity, self.kernel_order, self.penumbra_size,
+               self.max_search, self.depth_threshold, self.blocker_search_size, self.kernel_size,
+               self.light_radius, self.znear, self.pcss_min_blocker_depth, self.poisson_blocker_taps,
+               self.poisson_filter_taps, self.summed_area_table, self.hsm_alpha, self.hsm_beta)
+        cached = self.__dict__.get("_c_scalars")
+        if cached is None or cached[0] != key:
+            cached = (key, bytes(self._scalars_to_c()))
+            self.__dict__["_c_scalars"] = cached
+        p = api.VisParams.from_buffer_copy(cached[1])
+        if frame is not None:  # the light-side maps need no matrices
+            for dst, src, n in ((p.light_mvp_biased, frame.light_mvp_biased, 64), (p.camera_mv, frame.camera_mv, 64),
+                                (p.normal_matrix, frame.normal_matrix, 36), (p.light_position, frame.light_position, 12)):
+                b = (src if src.dtype == np.float32 else src.astype(np.float32)).tobytes()
+                if len(b) != n:
+                    raise ValueError("frame matrix of the wrong size")
+                C.memmove(dst, b, n)
+        return p
+
+    def _scalars_to_c(self) -> api.VisParams:
         p = api.VisParams()
         p.technique = int(self.technique)
         p.pretest = int(self.pretest)
@@ -345,11 +369,6 @@ class ShadowParams:
         p.summed_area_table = 1 if self.summed_area_table else 0
         p.hsm_alpha = self.hsm_alpha
         p.hsm_beta = self.hsm_beta
-        if frame is not None:  # the light-side maps need no matrices
-            C.memmove(p.light_mvp_biased, frame.light_mvp_biased.astype(np.float32).tobytes(), 64)
-            C.memmove(p.camera_mv, frame.camera_mv.astype(np.float32).tobytes(), 64)
-            C.memmove(p.normal_matrix, frame.normal_matrix.astype(np.float32).tobytes(), 36)
-            C.memmove(p.light_position, frame.light_position.astype(np.float32).tobytes(), 12)
         return p
 
 
