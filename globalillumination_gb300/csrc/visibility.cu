@@ -1725,12 +1725,14 @@ __global__ void __launch_bounds__(128) k_batch_visibility(const BatchLightFrame*
 // so the frame never writes / reads the 32-byte-per-pixel G-buffer (it is
 // stored only when the caller asks for it).  Same values as
 // k_gbuffer_resolve followed by k_visibility.
-// (128, 10): 48 registers instead of 60, 40 resident warps per SM instead
-// of 32; the kernel waits on memory (the key's record and vertices, the
-// map taps) more than it computes, so the extra warps pay for the few
-// spilled words (measured: resolve + visibility 40.0 -> 38.5 us).
+// Occupancy: the kernel waits on memory (the key's record and vertices,
+// the map taps) more than it computes, so extra resident warps pay for a
+// few spilled words.  PCSS-Poisson: (128, 12), 40 registers, 48 warps per
+// SM (resolve + visibility on pcss_1080p: (128, 8) 40.1 us, (128, 10)
+// 37.0 us, (128, 12) 36.7 us, (128, 14) 39.6 us); the other techniques
+// keep (128, 10), 48 registers.
 template <int TECH>
-__global__ void __launch_bounds__(128, 10) k_frame_visibility(
+__global__ void __launch_bounds__(128, TECH == GI_TECH_PCSS_POISSON ? 12 : 10) k_frame_visibility(
     const gi_vis_params p, const float* __restrict__ map, int map_w, int map_h, float sx, float sy,
     const unsigned long long* __restrict__ keys, const float* __restrict__ points,
     const float* __restrict__ normals, const int* __restrict__ indices, const dev::Mat4 mvp,
