@@ -1129,6 +1129,127 @@ __global__ void k_maxpool2(const uint16_t* __restrict__ x, int n, int h, int w, 
     }
 }
 
+// 8-channel variants of the pooling / upsampling / slice helpers (one
+// 16-byte vector per thread), used when channel counts, strides and offsets
+// are multiples of 8 and the tensors 16-byte aligned.  Each keeps its
+// scalar counterpart's per-element arithmetic and order, so the results
+// are the same bits.
+__device__ __forceinline__ void unpack8(const uint4& v, float (&f)[8]) {
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) f[k] = bf16_to_f((uint16_t)(w[k >> 1] >> ((k & 1) * 16)));
+}
+__device__ __forceinline__ uint4 pack8(const float (&f)[8]) {
+    uint32_t w[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) w[k] = (uint32_t)f_to_bf16(f[2 * k]) | ((uint32_t)f_to_bf16(f[2 * k + 1]) << 16);
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+__device__ __forceinline__ uint16_t lane16(const uint4& v, int k) {
+    const uint32_t ws[4] = {v.x, v.y, v.z, v.w};
+    return (uint16_t)(ws[k >> 1] >> ((k & 1) * 16));
+}
+
+__global__ void k_maxpool2_v8(const uint16_t* __restrict__ x, int n, int h, int w, int c, uint16_t* __restrict__ y) {
+    const int ho = h / 2, wo = w / 2, g8 = c / 8;
+    const long long total = (long long)n * ho * wo * g8;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int g = (int)(i % g8);
+        const long long pix = i / g8;
+        const int xo = (int)(pix % wo);
+        const int yo = (int)((pix / wo) % ho);
+        const long long img = pix / ((long long)wo * ho);
+        const long long b = ((img * h + 2 * yo) * w + 2 * xo) * c + g * 8;
+        float a0[8], a1[8], a2[8], a3[8], m[8];
+        unpack8(__ldg(reinterpret_cast<const uint4*>(x + b)), a0);
+        unpack8(__ldg(reinterpret_cast<const uint4*>(x + b + c)), a1);
+        unpack8(__ldg(reinterpret_cast<const uint4*>(x + b + (long long)w * c)), a2);
+        unpack8(__ldg(reinterpret_cast<const uint4*>(x + b + (long long)w * c + c)), a3);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) m[k] = fmaxf(fmaxf(fmaxf(a0[k], a1[k]), a2[k]), a3[k]);
+        *reinterpret_cast<uint4*>(y + pix * c + g * 8) = pack8(m);
+    }
+}
+
+__global__ void k_maxpool2_bwd_v8(const uint16_t* __restrict__ x, const uint16_t* __restrict__ y,
+                                  const uint16_t* __restrict__ dy, int n, int h, int w, int c,
+                                  uint16_t* __restrict__ dx) {
+    const int ho = h / 2, wo = w / 2, g8 = c / 8;
+    const long long total = (long long)n * ho * wo * g8;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int g = (int)(i % g8);
+        const long long pix = i / g8;
+        const int xo = (int)(pix % wo);
+        const int yo = (int)((pix / wo) % ho);
+        const long long img = pix / ((long long)wo * ho);
+        const long long b = ((img * h + 2 * yo) * w + 2 * xo) * c + g * 8;
+        const long long off[4] = {0, c, (long long)w * c, (long long)w * c + c};
+        const uint4 ym = __ldg(reinterpret_cast<const uint4*>(y + pix * c + g * 8));
+        const uint4 gr = __ldg(reinterpret_cast<const uint4*>(dy + pix * c + g * 8));
+        uint4 xv[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) xv[q] = __ldg(reinterpret_cast<const uint4*>(x + b + off[q]));
+        uint32_t out[4][4] = {};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const uint16_t yk = lane16(ym, k), gk = lane16(gr, k);
+            bool taken = false;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const bool hit = !taken && lane16(xv[q], k) == yk;
+                if (hit) out[q][k >> 1] |= (uint32_t)gk << ((k & 1) * 16);
+                taken |= hit;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            *reinterpret_cast<uint4*>(dx + b + off[q]) = make_uint4(out[q][0], out[q][1], out[q][2], out[q][3]);
+    }
+}
+
+__global__ void k_upsample2_bwd_v8(const uint16_t* __restrict__ dy, int n, int h, int w, int c, int ds, int doff,
+                                   uint16_t* __restrict__ dx) {
+    const int W = 2 * w, g8 = c / 8;
+    const long long total = (long long)n * h * w * g8;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int g = (int)(i % g8);
+        const long long pix = i / g8;
+        const int xx = (int)(pix % w);
+        const int yy = (int)((pix / w) % h);
+        const long long img = pix / ((long long)w * h);
+        const long long b = ((img * 2 * h + 2 * yy) * W + 2 * xx);
+        float a[8], bb[8], cc[8], d[8], sum[8];
+        unpack8(__ldg(reinterpret_cast<const uint4*>(dy + b * ds + doff + g * 8)), a);
+        unpack8(__ldg(reinterpret_cast<const uint4*>(dy + (b + 1) * ds + doff + g * 8)), bb);
+        unpack8(__ldg(reinterpret_cast<const uint4*>(dy + (b + W) * ds + doff + g * 8)), cc);
+        unpack8(__ldg(reinterpret_cast<const uint4*>(dy + (b + W + 1) * ds + doff + g * 8)), d);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) sum[k] = a[k] + bb[k] + cc[k] + d[k];
+        *reinterpret_cast<uint4*>(dx + pix * c + g * 8) = pack8(sum);
+    }
+}
+
+__global__ void k_slice_add_v8(const uint16_t* __restrict__ x, long long pixels, int c, uint16_t* __restrict__ y,
+                               int stride, int off) {
+    const int g8 = c / 8;
+    const long long total = pixels * g8;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int g = (int)(i % g8);
+        const long long p = i / g8;
+        uint4* d = reinterpret_cast<uint4*>(y + p * stride + off + g * 8);
+        float a[8], b[8], r[8];
+        unpack8(*d, a);
+        unpack8(__ldg(reinterpret_cast<const uint4*>(x + p * c + g * 8)), b);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) r[k] = a[k] + b[k];
+        *d = pack8(r);
+    }
+}
+
 __global__ void k_maxpool2_bwd(const uint16_t* __restrict__ x, const uint16_t* __restrict__ y,
                                const uint16_t* __restrict__ dy, int n, int h, int w, int c, uint16_t* __restrict__ dx) {
     const int ho = h / 2, wo = w / 2;
@@ -1478,6 +1599,8 @@ using gi::fail;
 using gi::fail_cuda;
 namespace tc = gi::tc;
 
+static inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
 namespace {
 // Polls per mbarrier wait and the bounded-wait test switch, read at every
 // launch (gi_tc_set_wait_limit, gi_tc_set_test_withhold).
@@ -1821,7 +1944,10 @@ extern "C" gi_status gi_unpack_conv_grad(const float* dw_packed, int cout, int c
 extern "C" gi_status gi_maxpool2_bf16(const gi_bf16* x, int n, int h, int w, int c, gi_bf16* y, void* stream) {
     if (!x || !y || h % 2 || w % 2 || c < 1) return fail(GI_ERR_INVALID_ARG, "gi_maxpool2_bf16: bad arguments");
     const long long total = (long long)n * (h / 2) * (w / 2) * c;
-    tc::k_maxpool2<<<tc::grid1d(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, n, h, w, c, y);
+    if (c % 8 == 0 && aligned16(x) && aligned16(y))
+        tc::k_maxpool2_v8<<<tc::grid1d(total / 8, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, n, h, w, c, y);
+    else
+        tc::k_maxpool2<<<tc::grid1d(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, n, h, w, c, y);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_maxpool2_bf16 launch");
 }
@@ -1830,8 +1956,12 @@ extern "C" gi_status gi_maxpool2_bwd_bf16(const gi_bf16* x, const gi_bf16* y, co
                                           int w, int c, gi_bf16* dx, void* stream) {
     if (!x || !y || !dy || !dx || h % 2 || w % 2) return fail(GI_ERR_INVALID_ARG, "gi_maxpool2_bwd_bf16: bad arguments");
     const long long total = (long long)n * (h / 2) * (w / 2) * c;
-    tc::k_maxpool2_bwd<<<tc::grid1d(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, y, dy, n, h, w, c,
-                                                                                            dx);
+    if (c % 8 == 0 && aligned16(x) && aligned16(y) && aligned16(dy) && aligned16(dx))
+        tc::k_maxpool2_bwd_v8<<<tc::grid1d(total / 8, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            x, y, dy, n, h, w, c, dx);
+    else
+        tc::k_maxpool2_bwd<<<tc::grid1d(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, y, dy, n, h, w,
+                                                                                                c, dx);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_maxpool2_bwd_bf16 launch");
 }
@@ -1851,8 +1981,12 @@ extern "C" gi_status gi_upsample2_bwd_bf16(const gi_bf16* dy, int n, int h, int 
                                            int dy_off, gi_bf16* dx, void* stream) {
     if (!dy || !dx || dy_off + c > dy_stride) return fail(GI_ERR_INVALID_ARG, "gi_upsample2_bwd_bf16: bad arguments");
     const long long total = (long long)n * h * w * c;
-    tc::k_upsample2_bwd<<<tc::grid1d(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(dy, n, h, w, c,
-                                                                                             dy_stride, dy_off, dx);
+    if (c % 8 == 0 && dy_stride % 8 == 0 && dy_off % 8 == 0 && aligned16(dy) && aligned16(dx))
+        tc::k_upsample2_bwd_v8<<<tc::grid1d(total / 8, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            dy, n, h, w, c, dy_stride, dy_off, dx);
+    else
+        tc::k_upsample2_bwd<<<tc::grid1d(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            dy, n, h, w, c, dy_stride, dy_off, dx);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_upsample2_bwd_bf16 launch");
 }
@@ -1872,8 +2006,12 @@ extern "C" gi_status gi_channel_slice_add_bf16(const gi_bf16* x, size_t pixels, 
                                                int off, void* stream) {
     if (!x || !y || off + c > stride) return fail(GI_ERR_INVALID_ARG, "gi_channel_slice_add_bf16: bad arguments");
     const long long total = (long long)pixels * c;
-    tc::k_slice_add<<<tc::grid1d(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, (long long)pixels, c,
-                                                                                          y, stride, off);
+    if (c % 8 == 0 && stride % 8 == 0 && off % 8 == 0 && aligned16(x) && aligned16(y))
+        tc::k_slice_add_v8<<<tc::grid1d(total / 8, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            x, (long long)pixels, c, y, stride, off);
+    else
+        tc::k_slice_add<<<tc::grid1d(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            x, (long long)pixels, c, y, stride, off);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GI_OK : fail_cuda(e, "gi_channel_slice_add_bf16 launch");
 }

@@ -167,6 +167,43 @@ def test_conv3x3_weight_gradient(n, h, w, cin, cout):
     _close(db.cpu(), b.grad, gy.abs().sum((0, 2, 3)), rtol=1e-3)
 
 
+@pytest.mark.parametrize("c", [16, 12])  # 16: the 8-channel kernels; 12: the per-element ones
+def test_pool_upsample_helpers_bitwise(c):
+    """The training helpers against a PyTorch restatement of their per-element
+    rules (same operation order, BF16 rounding of FP32 results): max-pool,
+    its gradient to the first maximum of each window, the upsampling
+    gradient ((a + b) + c) + d, and the slice add."""
+    g = torch.Generator().manual_seed(31)
+    # coarse values so that windows hold ties
+    x = (torch.randint(0, 6, (2, 8, 10, c), generator=g).float() * 0.25).to(torch.bfloat16).cuda()
+    y = tc_ops.maxpool2(x)
+    xf = x.float()
+    win = torch.stack([xf[:, 0::2, 0::2], xf[:, 0::2, 1::2], xf[:, 1::2, 0::2], xf[:, 1::2, 1::2]])
+    ref_y = torch.maximum(torch.maximum(torch.maximum(win[0], win[1]), win[2]), win[3]).to(torch.bfloat16)
+    assert torch.equal(y, ref_y)
+    dy = (torch.randn((2, 4, 5, c), generator=g)).to(torch.bfloat16).cuda()
+    dx = tc_ops.maxpool2_bwd(x, y, dy)
+    ref_dx = torch.zeros_like(xf)
+    taken = torch.zeros_like(y.float(), dtype=torch.bool)
+    for q, (oy, ox) in enumerate(((0, 0), (0, 1), (1, 0), (1, 1))):
+        hit = (~taken) & (x[:, oy::2, ox::2] == y)
+        ref_dx[:, oy::2, ox::2] = torch.where(hit, dy.float(), torch.zeros_like(dy.float()))
+        taken |= hit
+    assert torch.equal(dx.float(), ref_dx)
+    stride, off = c + 16, 8
+    up = (torch.randn((2, 8, 10, stride), generator=g)).to(torch.bfloat16).cuda()
+    d = tc_ops.upsample2_bwd(up, c, off)
+    uf = up.float()[..., off:off + c]
+    ref_d = (((uf[:, 0::2, 0::2] + uf[:, 0::2, 1::2]) + uf[:, 1::2, 0::2]) + uf[:, 1::2, 1::2]).to(torch.bfloat16)
+    assert torch.equal(d, ref_d)
+    base = (torch.randn((2, 8, 10, stride), generator=g)).to(torch.bfloat16).cuda()
+    add = (torch.randn((2, 8, 10, c), generator=g)).to(torch.bfloat16).cuda()
+    ref_s = base.clone()
+    ref_s[..., off:off + c] = (base.float()[..., off:off + c] + add.float()).to(torch.bfloat16)
+    tc_ops.channel_slice_add(add, base, off)
+    assert torch.equal(base, ref_s)
+
+
 def test_pool_upsample_roundtrip():
     x = _bf(_rand(2, 8, 12, 16, seed=14)).to(torch.bfloat16).cuda()
     y = tc_ops.maxpool2(x)
