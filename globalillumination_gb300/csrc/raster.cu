@@ -1376,7 +1376,16 @@ __global__ void __launch_bounds__(1024) k_large_scan(TierArgs a) {
     }
 }
 
-// Huge records at every pixel; writes the target (and so clears it).
+// Huge records at every pixel; writes the target (and so clears it).  A
+// thread owns base_rows(MODE) rows of one column, so a record's 64-bit edge
+// set-up is shared by that many texels; the rows after the first step the
+// edges by exact integer adds.  Measured on the pcss_1080p frame (2048^2
+// map, 1920 x 1080 keys; depth / key rows per thread): 4 / 4 -> 8 / 8 took
+// the light-map pass 0.071 -> 0.066 ms; 16 / 8, 16 / 16 and 32 / 8 were
+// slower (more registers, fewer resident blocks).
+constexpr int kBaseRowsDepth = 8, kBaseRowsKeys = 8;
+__host__ __device__ constexpr int base_rows(int mode) { return mode == MODE_DEPTH ? kBaseRowsDepth : kBaseRowsKeys; }
+
 template <int MODE>
 __global__ void __launch_bounds__(256) k_base(TierArgs a) {
     typedef typename BinVal<MODE>::T V;
@@ -1386,11 +1395,14 @@ __global__ void __launch_bounds__(256) k_base(TierArgs a) {
     if (threadIdx.x < nh) hr[threadIdx.x] = a.recs[a.ctr[16 + threadIdx.x]];
     __syncthreads();
     const int x = blockIdx.x * 32 + (threadIdx.x & 31);
-    const int yb = blockIdx.y * 32 + (threadIdx.x >> 5) * 4;  // 4 rows per thread
+    constexpr int kBaseRows = base_rows(MODE);
+    const int yb = (blockIdx.y * 8 + (threadIdx.x >> 5)) * kBaseRows;
     if (x >= a.r.W) return;
     const V clearv = MODE == MODE_DEPTH ? (V)0x3f800000u
                                         : (V)(((unsigned long long)0x3f800000u << 32) | 0xFFFFFFFFull);
-    V val[4] = {clearv, clearv, clearv, clearv};
+    V val[kBaseRows];
+#pragma unroll
+    for (int k = 0; k < kBaseRows; ++k) val[k] = clearv;
     const int64_t px = (int64_t)x * kSub + kSub / 2;
     for (int h = 0; h < nh; ++h) {
         const BRec& r = hr[h];
@@ -1408,7 +1420,7 @@ __global__ void __launch_bounds__(256) k_base(TierArgs a) {
             E[i] = A[i] * ((int64_t)yb * kSub + kSub / 2 - r.Y[ia]) - B * (px - r.X[ia]) - bias[i];
         }
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < kBaseRows; ++k) {
             const int y = yb + k;
             const bool in = y >= (int)r.y0 && y <= (int)r.y1 && inside_biased(E);
             if (in) {
@@ -1430,7 +1442,7 @@ __global__ void __launch_bounds__(256) k_base(TierArgs a) {
         }
     }
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < kBaseRows; ++k) {
         const int y = yb + k;
         if (y >= a.r.H) break;
         const size_t idx = (size_t)y * a.r.W + x;
@@ -1900,7 +1912,8 @@ static gi_status run_tiered(gi_context* ctx, dev::RasterArgs& r, int mode, cudaS
     if (e != cudaSuccess) return fail_cuda(e, "tiered raster memset");
     const unsigned sms = (unsigned)sm_count(ctx->device);
     const unsigned gsetup = grid_for(prims ? prims : 1, 128);
-    const dim3 gbase((r.W + 31) / 32, (r.H + 31) / 32);
+    const int base_rows = 8 * dev::base_rows(mode);  // rows per block of k_base
+    const dim3 gbase((r.W + 31) / 32, (r.H + base_rows - 1) / base_rows);
     // Each kernel after the first is a programmatic dependent of the one
     // before it (launch_dependent, pdl_enter): launched directly, the
     // pcss_1080p frame went 8,700 -> 9,400 frames/s; under stream capture
