@@ -1739,8 +1739,14 @@ __global__ void __launch_bounds__(128, TECH == GI_TECH_PCSS_POISSON ? 12 : 10) k
     const unsigned* __restrict__ rec_of, const dev::BRec* __restrict__ recs, const uint4* __restrict__ rres,
     float* __restrict__ out, int W, int H, float4* __restrict__ pos_out, float4* __restrict__ nrm_out,
     const SoftMaps sm, const __grid_constant__ PoissonOffsets po) {
-    int x = blockIdx.x * 32 + (threadIdx.x & 31);
-    int y = blockIdx.y * 4 + (threadIdx.x >> 5);
+    // A warp shades an 8 x 4 patch of the block's 32 x 4 pixels, so its
+    // lanes more often share a triangle, a lit / shadowed state and map
+    // texels (pcss_1080p resolve + visibility: 36.6 us as 32 x 1 rows,
+    // 36.3 as 16 x 2, 36.0 as 8 x 4).
+    constexpr int kWarpW = 8;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = blockIdx.x * 32 + (warp * kWarpW) % 32 + lane % kWarpW;
+    int y = blockIdx.y * 4 + (warp * kWarpW) / 32 * (32 / kWarpW) + lane / kWarpW;
     if (x >= W || y >= H) return;
     Ctx c;
     c.sm = sm;
