@@ -1932,7 +1932,7 @@ extern "C" gi_status gi_pack_conv_weights(const float* w, int cout, int cin_real
 
 extern "C" gi_status gi_unpack_conv_grad(const float* dw_packed, int cout, int cin_real, int cin, int ksize,
                                          float* out, void* stream) {
-    if (!dw_packed || !out || cin % 8 || cin_real > cin || (ksize != 1 && ksize != 3))
+    if (!dw_packed || !out || cout < 1 || cin_real < 1 || cin % 8 || cin_real > cin || (ksize != 1 && ksize != 3))
         return fail(GI_ERR_INVALID_ARG, "gi_unpack_conv_grad: bad arguments");
     const long long total = (long long)cout * cin_real * ksize * ksize;
     tc::k_unpack_grad<<<tc::grid1d(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
@@ -1942,7 +1942,8 @@ extern "C" gi_status gi_unpack_conv_grad(const float* dw_packed, int cout, int c
 }
 
 extern "C" gi_status gi_maxpool2_bf16(const gi_bf16* x, int n, int h, int w, int c, gi_bf16* y, void* stream) {
-    if (!x || !y || h % 2 || w % 2 || c < 1) return fail(GI_ERR_INVALID_ARG, "gi_maxpool2_bf16: bad arguments");
+    if (!x || !y || n < 1 || h < 2 || w < 2 || h % 2 || w % 2 || c < 1)
+        return fail(GI_ERR_INVALID_ARG, "gi_maxpool2_bf16: bad arguments");
     const long long total = (long long)n * (h / 2) * (w / 2) * c;
     if (c % 8 == 0 && aligned16(x) && aligned16(y))
         tc::k_maxpool2_v8<<<tc::grid1d(total / 8, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, n, h, w, c, y);
@@ -1954,7 +1955,8 @@ extern "C" gi_status gi_maxpool2_bf16(const gi_bf16* x, int n, int h, int w, int
 
 extern "C" gi_status gi_maxpool2_bwd_bf16(const gi_bf16* x, const gi_bf16* y, const gi_bf16* dy, int n, int h,
                                           int w, int c, gi_bf16* dx, void* stream) {
-    if (!x || !y || !dy || !dx || h % 2 || w % 2) return fail(GI_ERR_INVALID_ARG, "gi_maxpool2_bwd_bf16: bad arguments");
+    if (!x || !y || !dy || !dx || n < 1 || h < 2 || w < 2 || h % 2 || w % 2 || c < 1)
+        return fail(GI_ERR_INVALID_ARG, "gi_maxpool2_bwd_bf16: bad arguments");
     const long long total = (long long)n * (h / 2) * (w / 2) * c;
     if (c % 8 == 0 && aligned16(x) && aligned16(y) && aligned16(dy) && aligned16(dx))
         tc::k_maxpool2_bwd_v8<<<tc::grid1d(total / 8, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
@@ -1968,7 +1970,8 @@ extern "C" gi_status gi_maxpool2_bwd_bf16(const gi_bf16* x, const gi_bf16* y, co
 
 extern "C" gi_status gi_upsample2_bf16(const gi_bf16* x, int n, int h, int w, int c, gi_bf16* y, int y_stride,
                                        int y_off, void* stream) {
-    if (!x || !y || c % 8 || y_stride % 8 || y_off % 8 || y_off + c > y_stride)
+    if (!x || !y || n < 1 || h < 1 || w < 1 || c < 8 || c % 8 || y_stride % 8 || y_off < 0 || y_off % 8 ||
+        y_off + c > y_stride)
         return fail(GI_ERR_INVALID_ARG, "gi_upsample2_bf16: bad arguments");
     const long long total = (long long)n * 4 * h * w * (c / 8);
     tc::k_upsample2<<<tc::grid1d(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, n, h, w, c, y,
@@ -1979,7 +1982,8 @@ extern "C" gi_status gi_upsample2_bf16(const gi_bf16* x, int n, int h, int w, in
 
 extern "C" gi_status gi_upsample2_bwd_bf16(const gi_bf16* dy, int n, int h, int w, int c, int dy_stride,
                                            int dy_off, gi_bf16* dx, void* stream) {
-    if (!dy || !dx || dy_off + c > dy_stride) return fail(GI_ERR_INVALID_ARG, "gi_upsample2_bwd_bf16: bad arguments");
+    if (!dy || !dx || n < 1 || h < 1 || w < 1 || c < 1 || dy_off < 0 || dy_off + c > dy_stride)
+        return fail(GI_ERR_INVALID_ARG, "gi_upsample2_bwd_bf16: bad arguments");
     const long long total = (long long)n * h * w * c;
     if (c % 8 == 0 && dy_stride % 8 == 0 && dy_off % 8 == 0 && aligned16(dy) && aligned16(dx))
         tc::k_upsample2_bwd_v8<<<tc::grid1d(total / 8, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
@@ -1993,7 +1997,7 @@ extern "C" gi_status gi_upsample2_bwd_bf16(const gi_bf16* dy, int n, int h, int 
 
 extern "C" gi_status gi_channel_slice_bf16(const gi_bf16* x, size_t pixels, int stride, int off, int c, gi_bf16* y,
                                            void* stream) {
-    if (!x || !y || c % 8 || stride % 8 || off % 8 || off + c > stride)
+    if (!x || !y || c < 8 || c % 8 || stride % 8 || off < 0 || off % 8 || off + c > stride)
         return fail(GI_ERR_INVALID_ARG, "gi_channel_slice_bf16: bad arguments");
     const long long total = (long long)pixels * (c / 8);
     tc::k_slice<<<tc::grid1d(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, (long long)pixels, stride,
@@ -2004,7 +2008,8 @@ extern "C" gi_status gi_channel_slice_bf16(const gi_bf16* x, size_t pixels, int 
 
 extern "C" gi_status gi_channel_slice_add_bf16(const gi_bf16* x, size_t pixels, int c, gi_bf16* y, int stride,
                                                int off, void* stream) {
-    if (!x || !y || off + c > stride) return fail(GI_ERR_INVALID_ARG, "gi_channel_slice_add_bf16: bad arguments");
+    if (!x || !y || c < 1 || off < 0 || off + c > stride)
+        return fail(GI_ERR_INVALID_ARG, "gi_channel_slice_add_bf16: bad arguments");
     const long long total = (long long)pixels * c;
     if (c % 8 == 0 && stride % 8 == 0 && off % 8 == 0 && aligned16(x) && aligned16(y))
         tc::k_slice_add_v8<<<tc::grid1d(total / 8, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(

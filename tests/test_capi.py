@@ -112,3 +112,33 @@ def test_batch_argument_checks():
     assert lib.gi_batch_add_frame(None, None, None, None, None, 1, None, None) == api.GI_ERR_INVALID_ARG
     assert lib.gi_batch_info(None, None) == api.GI_ERR_INVALID_ARG
     assert C.sizeof(api.BatchTuning) == 4 * 4 + 8 + 4 + 3 * 4 + 4 + 4  # + padding to 8
+
+
+def test_training_helpers_reject_bad_shapes_before_device_work():
+    """Every call below breaks a host-side shape check, so none launches a
+    kernel (the dummy pointers are never dereferenced)."""
+    lib = api.load()
+    P = C.c_void_p(256)
+    bad = api.GI_ERR_INVALID_ARG
+    # max-pool: negative or empty batch / image, odd sizes, no channels
+    assert lib.gi_maxpool2_bf16(P, -1, -2, 4, 8, P, None) == bad
+    assert lib.gi_maxpool2_bf16(P, 1, 0, 4, 8, P, None) == bad
+    assert lib.gi_maxpool2_bf16(P, 1, 3, 4, 8, P, None) == bad
+    assert lib.gi_maxpool2_bf16(P, 1, 4, 4, 0, P, None) == bad
+    assert lib.gi_maxpool2_bwd_bf16(P, P, P, -1, -2, 4, 8, P, None) == bad
+    assert lib.gi_maxpool2_bwd_bf16(P, P, P, 1, 4, 4, -8, P, None) == bad
+    # upsampling and its gradient: negative sizes, offsets outside the stride
+    assert lib.gi_upsample2_bf16(P, -1, -4, 4, 8, P, 8, 0, None) == bad
+    assert lib.gi_upsample2_bf16(P, 1, 4, 4, 0, P, 8, 0, None) == bad
+    assert lib.gi_upsample2_bf16(P, 1, 4, 4, 8, P, 16, -8, None) == bad
+    assert lib.gi_upsample2_bwd_bf16(P, -1, -4, 4, 8, 8, 0, P, None) == bad
+    assert lib.gi_upsample2_bwd_bf16(P, 1, 4, 4, 8, 16, -8, P, None) == bad
+    assert lib.gi_upsample2_bwd_bf16(P, 1, 4, 4, 0, 16, 0, P, None) == bad
+    # channel slices
+    assert lib.gi_channel_slice_bf16(P, 16, 16, -8, 8, P, None) == bad
+    assert lib.gi_channel_slice_bf16(P, 16, 16, 0, 0, P, None) == bad
+    assert lib.gi_channel_slice_add_bf16(P, 16, 8, P, 16, -8, None) == bad
+    assert lib.gi_channel_slice_add_bf16(P, 16, 0, P, 16, 0, None) == bad
+    # weight (un)packing with negative sizes
+    assert lib.gi_unpack_conv_grad(P, -1, -1, 8, 3, P, None) == bad
+    assert lib.gi_pack_conv_weights(P, -1, 1, 8, 3, 0, P, None) == bad
