@@ -620,7 +620,14 @@ extern "C" gi_status gi_render_frame(gi_context* ctx, const gi_scene* s, const g
     if ((size_t)s->dev_triangles >= ((size_t)1 << 29))
         return fail(GI_ERR_CAPACITY, "gi_render_frame: more than 2^29 triangles");
     cudaStream_t cs = static_cast<cudaStream_t>(stream);
-    if (!ctx->frame_graph || ctx->profiling)
+    // A caller that captures its own stream gets the launches themselves in
+    // its graph: the frame graph is neither replayed nor captured inside it.
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    if (ctx->frame_graph && cudaStreamIsCapturing(cs, &capture) != cudaSuccess) {
+        cudaGetLastError();
+        capture = cudaStreamCaptureStatusNone;
+    }
+    if (!ctx->frame_graph || ctx->profiling || capture != cudaStreamCaptureStatusNone)
         return enqueue_frame(ctx, s, mp, light_mvp, camera_mvp, vp, W, H, d_depth, d_vis, d_pos, d_nrm, cs);
     // Frame graph: a new argument signature runs eagerly once (allocating
     // what the frame needs); the next call with the same signature captures

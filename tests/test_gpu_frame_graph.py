@@ -128,3 +128,35 @@ def test_profiling_bypasses_the_graph(pair):
     g.set_profiling(False)
     assert torch.equal(vis, ref)
     assert all(np.isfinite(ms)) and ms[2] > 0
+
+
+def test_caller_capture_gets_the_launches(pair):
+    """With the frame graph on, a call made while the caller captures its own
+    stream enqueues the launches themselves (no graph inside the capture);
+    replaying the caller's graph gives the direct frame's bits."""
+    g, d = pair
+    w = _world()
+    fr = gi.frame_setup(w.light, w.camera)
+    stream = torch.cuda.current_stream()
+    w.scene.upload(g, stream)
+    S, W, H = w.map_params.width, w.camera.width, w.camera.height
+    bg = gi.allocate_frame(S, S, W, H)
+    bd = gi.allocate_frame(S, S, W, H)
+    ref_vis, ref_depth = _render(d, w, fr, bd, stream)
+    for _ in range(3):  # allocations done, the context's own graph built
+        _render(g, w, fr, bg, stream)
+    bg.vis.zero_()
+    bg.depth.zero_()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    side.wait_stream(stream)
+    with torch.cuda.graph(graph, stream=side):
+        gi.render_frame(g, w.scene, fr, w.map_params, w.params, W, H, bg, torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(bg.vis, ref_vis)
+    assert torch.equal(bg.depth, ref_depth)
+    # the context's own frame graph still replays afterwards
+    assert torch.equal(_render(g, w, fr, bg, stream)[0], ref_vis)
