@@ -105,7 +105,8 @@ gi_status gi_context_set_tap_pyramid(gi_context* ctx, int enable);
  * device copy, invalidates it.  The graph reads device memory when it
  * runs, so new scene contents uploaded into the same buffers are used.
  * Results do not depend on it; timing events (gi_context_set_profiling)
- * bypass it.  Off by default. */
+ * bypass it, and so does a call on a stream the caller is capturing (the
+ * launches themselves go into the caller's graph).  Off by default. */
 gi_status gi_context_set_frame_graph(gi_context* ctx, int enable);
 
 /* ------------------------------------------------------------------ */
