@@ -1377,14 +1377,13 @@ __global__ void __launch_bounds__(1024) k_large_scan(TierArgs a) {
 }
 
 // Huge records at every pixel; writes the target (and so clears it).  A
-// thread owns base_rows(MODE) rows of one column, so a record's 64-bit edge
-// set-up is shared by that many texels; the rows after the first step the
-// edges by exact integer adds.  Measured on the pcss_1080p frame (2048^2
-// map, 1920 x 1080 keys; depth / key rows per thread): 4 / 4 -> 8 / 8 took
-// the light-map pass 0.071 -> 0.066 ms; 16 / 8, 16 / 16 and 32 / 8 were
-// slower (more registers, fewer resident blocks).
-constexpr int kBaseRowsDepth = 8, kBaseRowsKeys = 8;
-__host__ __device__ constexpr int base_rows(int mode) { return mode == MODE_DEPTH ? kBaseRowsDepth : kBaseRowsKeys; }
+// thread owns kBaseRows rows of one column, so a record's 64-bit edge set-up
+// is shared by that many texels; the rows after the first step the edges by
+// exact integer adds.  Measured on the pcss_1080p frame (2048^2 map, 1920 x
+// 1080 keys; depth / key rows per thread): 4 / 4 -> 8 / 8 took the light-map
+// pass 0.071 -> 0.066 ms; 16 / 8, 16 / 16 and 32 / 8 were slower (more
+// registers, fewer resident blocks).
+constexpr int kBaseRows = 8;
 
 template <int MODE>
 __global__ void __launch_bounds__(256) k_base(TierArgs a) {
@@ -1395,7 +1394,6 @@ __global__ void __launch_bounds__(256) k_base(TierArgs a) {
     if (threadIdx.x < nh) hr[threadIdx.x] = a.recs[a.ctr[16 + threadIdx.x]];
     __syncthreads();
     const int x = blockIdx.x * 32 + (threadIdx.x & 31);
-    constexpr int kBaseRows = base_rows(MODE);
     const int yb = (blockIdx.y * 8 + (threadIdx.x >> 5)) * kBaseRows;
     if (x >= a.r.W) return;
     const V clearv = MODE == MODE_DEPTH ? (V)0x3f800000u
@@ -1912,7 +1910,7 @@ static gi_status run_tiered(gi_context* ctx, dev::RasterArgs& r, int mode, cudaS
     if (e != cudaSuccess) return fail_cuda(e, "tiered raster memset");
     const unsigned sms = (unsigned)sm_count(ctx->device);
     const unsigned gsetup = grid_for(prims ? prims : 1, 128);
-    const int base_rows = 8 * dev::base_rows(mode);  // rows per block of k_base
+    const int base_rows = 8 * dev::kBaseRows;  // rows per block of k_base (8 warps)
     const dim3 gbase((r.W + 31) / 32, (r.H + base_rows - 1) / base_rows);
     // Each kernel after the first is a programmatic dependent of the one
     // before it (launch_dependent, pdl_enter): launched directly, the
