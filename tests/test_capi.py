@@ -142,3 +142,31 @@ def test_training_helpers_reject_bad_shapes_before_device_work():
     # weight (un)packing with negative sizes
     assert lib.gi_unpack_conv_grad(P, -1, -1, 8, 3, P, None) == bad
     assert lib.gi_pack_conv_weights(P, -1, 1, 8, 3, 0, P, None) == bad
+
+
+def test_shadow_params_to_c_follows_field_changes():
+    """ShadowParams.to_c caches the scalar part of the C struct per set of
+    field values: every change, down to a zero's sign, reaches the struct."""
+    import math
+
+    import numpy as np
+
+    from globalillumination_gb300.shadow import Frame, ShadowParams
+
+    p = ShadowParams.defaults(api.GI_TECH_PCSS_POISSON)
+    first = bytes(p.to_c(None))
+    assert bytes(p.to_c(None)) == first
+    p.light_radius = 0.25
+    assert p.to_c(None).light_radius == 0.25 and bytes(p.to_c(None)) != first
+    p.depth_threshold = 0.0
+    plus = bytes(p.to_c(None))
+    p.depth_threshold = -0.0
+    assert bytes(p.to_c(None)) != plus
+    assert math.copysign(1.0, p.to_c(None).depth_threshold) == -1.0
+    p.technique = api.GI_TECH_PCF
+    assert p.to_c(None).technique == api.GI_TECH_PCF
+    m = np.arange(16, dtype=np.float32)
+    fr = Frame(m, m + 1, m + 2, m + 3, m[:9] + 4, m[:3] + 5)
+    c = p.to_c(fr)
+    assert list(c.light_mvp_biased) == list(m + 1) and list(c.light_position) == list(m[:3] + 5)
+    assert list(c.normal_matrix) == list(m[:9] + 4) and list(c.camera_mv) == list(m + 3)
