@@ -23,7 +23,7 @@ GIError on failure; nothing falls back to a CPU path.
 from __future__ import annotations
 
 import ctypes as C
-import math
+import struct
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -296,6 +296,11 @@ TECHNIQUES = {
 }
 
 
+# ShadowParams.to_c's cache key: the scalar fields in declaration order
+# (integers as int64, reals as float64, the SAT switch as a bool).
+_SCALAR_KEY = struct.Struct("<qqdqqqdqqdddqq?dd")
+
+
 @dataclass
 class ShadowParams:
     """ShadowParams of the reference with the technique as one enum value."""
@@ -333,13 +338,13 @@ class ShadowParams:
         # The scalar part is built once per set of field values (fields may
         # change between calls) and copied; the frame's matrices are copied
         # straight from their float32 buffers.
-        # (A float's sign goes into the key too: -0.0 == 0.0 in Python, but
-        # they are different bits in the C struct.)
-        key = tuple((v, math.copysign(1.0, v)) if isinstance(v, float) else v for v in (
+        # The key is the fields' bytes, so values that compare equal in
+        # Python but differ in bits (-0.0 and 0.0) get their own struct.
+        key = _SCALAR_KEY.pack(
             self.technique, self.pretest, self.shadow_intensity, self.kernel_order, self.penumbra_size,
             self.max_search, self.depth_threshold, self.blocker_search_size, self.kernel_size,
             self.light_radius, self.znear, self.pcss_min_blocker_depth, self.poisson_blocker_taps,
-            self.poisson_filter_taps, self.summed_area_table, self.hsm_alpha, self.hsm_beta))
+            self.poisson_filter_taps, self.summed_area_table, self.hsm_alpha, self.hsm_beta)
         cached = self.__dict__.get("_c_scalars")
         if cached is None or cached[0] != key:
             cached = (key, bytes(self._scalars_to_c()))
