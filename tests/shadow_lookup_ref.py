@@ -1,0 +1,175 @@
+"""A second, numpy restatement of the per-pixel shadow lookups (test helper).
+
+The hard test, PCF and PCSS of the reference's visibility shaders written
+again with numpy float32 scalars (every operation rounds to float32, in the
+order the shader text writes it), independently of the C++ oracle, so the
+CPU tests can hold the oracle to it bit for bit:
+
+* main() of ShadowMapping/Shaders/Shadow.frag:240-272 and of
+  SoftShadowMapping/Shaders/SoftShadow/PlausibleSoftShadow.frag:605-632:
+  background where vertex.x == 0, shadowCoord = lightMVP * vertex divided by
+  its w, the pre-test, and the lookup only where w > 0 and the pre-test
+  passed;
+* computePreEvaluationBasedOnNormalOrientation (Shadow.frag:222-238), with
+  normalize(v) fixed as v * (1 / sqrt(dot(v, v))) and dot / matrix products
+  summed left to right;
+* the naive hard test (Shadow.frag:253-256) and PCF's float loop
+  (Shadow.frag:86-116) over a NEAREST, CLAMP_TO_BORDER (border 0) map: the
+  texel of (s, t) is (floor(s * W), floor(t * H));
+* PCSS (PlausibleSoftShadow.frag:166-194 blocker search, 365-374 penumbra
+  width, 376-398 filter, 556-563), with the light radius a float and the
+  0.99 average-blocker cut-off a parameter;
+* the Poisson-disk PCSS of this library (no reference counterpart): the
+  same blocker search and filter with the grid offsets replaced by the
+  Poisson points times the blocker search width / the penumbra width, the
+  filter averaging over its own tap count.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+f32 = np.float32
+
+TECH_HARD, TECH_PCF, TECH_PCSS_GRID, TECH_PCSS_POISSON = 0, 1, 3, 4
+PRETEST_REFERENCE, PRETEST_OFF = 0, 1
+
+
+def mat4_mul(m, v):
+    """Column-major mat4 times vec4, each row summed left to right."""
+    return [((m[r] * v[0] + m[4 + r] * v[1]) + m[8 + r] * v[2]) + m[12 + r] * v[3] for r in range(4)]
+
+
+def fetch(depth, W, H, s, t):
+    """texture2D(shadowMap, (s, t)).z with NEAREST filtering and a border of 0."""
+    fi = np.floor(s * f32(W))
+    fj = np.floor(t * f32(H))
+    if not (fi >= 0 and fi < f32(W) and fj >= 0 and fj < f32(H)):
+        return f32(0.0)
+    return depth[int(fj) * W + int(fi)]
+
+
+def pretest(p, vertex, normal):
+    if p["pretest"] == PRETEST_OFF:
+        return f32(1.0)
+    ev = mat4_mul(p["camera_mv"], vertex)
+    nm = p["normal_matrix"]
+    nx = (nm[0] * normal[0] + nm[3] * normal[1]) + nm[6] * normal[2]
+    ny = (nm[1] * normal[0] + nm[4] * normal[1]) + nm[7] * normal[2]
+    nz = (nm[2] * normal[0] + nm[5] * normal[1]) + nm[8] * normal[2]
+    inv = f32(1.0) / np.sqrt((nx * nx + ny * ny) + nz * nz)
+    nx, ny, nz = nx * inv, ny * inv, nz * inv
+    lp = p["light_position"]
+    lx, ly, lz = lp[0] - ev[0], lp[1] - ev[1], lp[2] - ev[2]
+    linv = f32(1.0) / np.sqrt((lx * lx + ly * ly) + lz * lz)
+    lx, ly, lz = lx * linv, ly * linv, lz * linv
+    if not normal[3] != 0:  # !bool(normal.w)
+        nx, ny, nz = nx * f32(-1.0), ny * f32(-1.0), nz * f32(-1.0)
+    d = (nx * lx + ny * ly) + nz * lz
+    return p["intensity"] if max(d, f32(0.0)) == 0 else f32(1.0)
+
+
+def pcf(p, depth, W, H, n):
+    incr_w, incr_h = f32(1.0) / f32(W), f32(1.0) / f32(H)
+    illum = f32(0.0)
+    offset = f32(p["penumbra_size"])
+    step = (f32(2.0) * offset) / f32(p["kernel_order"])
+    count = 0
+    w = -offset
+    while w < offset:
+        h = -offset
+        while h < offset:
+            d = fetch(depth, W, H, n[0] + w * incr_w, n[1] + h * incr_h)
+            illum = illum + (f32(1.0) if n[2] <= d else p["intensity"])
+            count += 1
+            h = h + step
+        w = w + step
+    return illum / f32(count)
+
+
+def blocker_search_width(p, W):
+    R = p["light_radius"]
+    return R / f32(W) if f32(W) <= f32(1024.0) else R / f32(1024.0)
+
+
+def grid_range(fw):
+    """for (int h = -filterWidth; h <= filterWidth; h++) with a float filterWidth."""
+    h = int(-fw)  # float to int conversion truncates
+    while f32(h) <= fw:
+        yield h
+        h += 1
+
+
+def avg_blocker(p, depth, W, H, n, taps=None):
+    avg, nb = f32(0.0), 0
+    bsw = blocker_search_width(p, W)
+    if taps is None:
+        fw = (f32(p["blocker_search_size"]) - f32(1.0)) * f32(0.5)
+        offs = [((f32(w) * bsw) / fw, (f32(h) * bsw) / fw) for h in grid_range(fw) for w in grid_range(fw)]
+    else:
+        offs = [(x * bsw, y * bsw) for x, y in taps]
+    for ox, oy in offs:
+        d = fetch(depth, W, H, n[0] + ox, n[1] + oy)
+        if n[2] > d:
+            avg = avg + d
+            nb += 1
+    return f32(1.0) if nb == 0 else avg / f32(nb)
+
+
+def penumbra_width(p, avg, z):
+    if avg < p["min_blocker_depth"]:
+        return f32(0.0)
+    pw = ((z - avg) / avg) * p["light_radius"]
+    return (p["znear"] * pw) / z
+
+
+def pcss_filter(p, depth, W, H, n, pw, taps=None):
+    K = p["kernel_size"]
+    step = (f32(2.0) * pw) / f32(K)
+    if step <= 0 or step >= 1:
+        return f32(1.0)
+    illum = f32(0.0)
+    if taps is None:
+        fw = (f32(K) - f32(1.0)) * f32(0.5)
+        offs = [((f32(w) * pw) / fw, (f32(h) * pw) / fw) for h in grid_range(fw) for w in grid_range(fw)]
+        count = f32(K * K)
+    else:
+        offs = [(x * pw, y * pw) for x, y in taps]
+        count = f32(len(taps))
+    for ox, oy in offs:
+        d = fetch(depth, W, H, n[0] + ox, n[1] + oy)
+        illum = illum + (f32(1.0) if n[2] <= d else p["intensity"])
+    return illum / count
+
+
+def shade(p, depth, W, H, vertex, normal, blocker_taps=None, filter_taps=None):
+    """Visibility of one G-buffer pixel (vertex, normal: 4 float32 each)."""
+    if vertex[0] == 0:
+        return f32(0.0)
+    sc = mat4_mul(p["light_mvp_biased"], vertex)
+    n = [sc[0] / sc[3], sc[1] / sc[3], sc[2] / sc[3], sc[3] / sc[3]]
+    shadow = pretest(p, vertex, normal)
+    if not (sc[3] > 0 and shadow == 1):
+        return shadow
+    tech = p["technique"]
+    if tech == TECH_HARD:
+        return f32(1.0) if n[2] <= fetch(depth, W, H, n[0], n[1]) else p["intensity"]
+    if tech == TECH_PCF:
+        return pcf(p, depth, W, H, n)
+    if tech == TECH_PCSS_GRID:
+        return pcss_filter(p, depth, W, H, n, penumbra_width(p, avg_blocker(p, depth, W, H, n), n[2]))
+    if tech == TECH_PCSS_POISSON:
+        avg = avg_blocker(p, depth, W, H, n, blocker_taps)
+        return pcss_filter(p, depth, W, H, n, penumbra_width(p, avg, n[2]), filter_taps)
+    raise ValueError(f"technique {tech} is not restated here")
+
+
+def params_of(c):
+    """The fields of a gi_vis_params (ctypes) this restatement reads, as float32 / int."""
+    return {
+        "technique": int(c.technique), "pretest": int(c.pretest), "intensity": f32(c.shadow_intensity),
+        "kernel_order": int(c.kernel_order), "penumbra_size": int(c.penumbra_size),
+        "blocker_search_size": int(c.blocker_search_size), "kernel_size": int(c.kernel_size),
+        "light_radius": f32(c.light_radius), "znear": f32(c.znear), "min_blocker_depth": f32(c.pcss_min_blocker_depth),
+        "light_mvp_biased": [f32(x) for x in c.light_mvp_biased], "camera_mv": [f32(x) for x in c.camera_mv],
+        "normal_matrix": [f32(x) for x in c.normal_matrix], "light_position": [f32(x) for x in c.light_position],
+    }

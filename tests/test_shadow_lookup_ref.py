@@ -1,0 +1,106 @@
+"""The C++ oracle's hard test, PCF and PCSS (grid and Poisson) against a
+second restatement of the same shader text in numpy float32
+(tests/shadow_lookup_ref.py), bit for bit, on G-buffer pixels and a light
+map that the oracle rasterises from a sphere-field scene."""
+import numpy as np
+import pytest
+
+import oracle
+import globalillumination_gb300 as gi
+from globalillumination_gb300 import _capi as api
+from globalillumination_gb300 import scenes
+
+import shadow_lookup_ref as ref
+
+W, H, S = 96, 54, 128
+
+
+@pytest.fixture(scope="module")
+def world():
+    w = scenes.pcss_1080p(width=W, height=H, map_size=S, spheres=24)
+    fr = gi.frame_setup(w.light, w.camera)
+    p, n, i = w.scene.arrays()
+    mp = w.map_params
+    depth = oracle.shadow_map(p, i, fr.light_mvp, S, S, mp.bias_mode, mp.constant_bias, mp.offset_factor,
+                              mp.offset_units)
+    pos, nrm = oracle.gbuffer(p, n, i, fr.camera_mvp, W, H)
+    pos, nrm = pos.reshape(-1, 4), nrm.reshape(-1, 4)
+    rng = np.random.default_rng(0x5EED)
+    fg = np.flatnonzero(pos[:, 0] != 0)
+    bg = np.flatnonzero(pos[:, 0] == 0)
+    pick = np.concatenate([rng.choice(fg, 400, replace=False), rng.choice(bg, 4, replace=False)])
+    w.scene.close()
+    return fr, depth, pos[pick].copy(), nrm[pick].copy()
+
+
+CASES = [
+    ("hard", api.GI_TECH_HARD, {}),
+    ("hard, no pre-test", api.GI_TECH_HARD, {"pretest": api.GI_PRETEST_OFF}),
+    ("pcf 7 / 1", api.GI_TECH_PCF, {"kernel_order": 7, "penumbra_size": 1}),
+    ("pcf 3 / 2", api.GI_TECH_PCF, {"kernel_order": 3, "penumbra_size": 2}),
+    ("pcss grid 7 / 15", api.GI_TECH_PCSS_GRID,
+     {"blocker_search_size": 7, "kernel_size": 15, "light_radius": 4.0, "pcss_min_blocker_depth": 0.0}),
+    ("pcss grid 4 / 6, cut-off", api.GI_TECH_PCSS_GRID,
+     {"blocker_search_size": 4, "kernel_size": 6, "light_radius": 2.5, "pcss_min_blocker_depth": 0.99}),
+    ("pcss poisson 16 / 32", api.GI_TECH_PCSS_POISSON,
+     {"poisson_blocker_taps": 16, "poisson_filter_taps": 32, "kernel_size": 15, "light_radius": 4.0,
+      "pcss_min_blocker_depth": 0.0}),
+    ("pcss poisson 8 / 12, no pre-test", api.GI_TECH_PCSS_POISSON,
+     {"poisson_blocker_taps": 8, "poisson_filter_taps": 12, "kernel_size": 9, "light_radius": 6.0,
+      "pcss_min_blocker_depth": 0.0, "pretest": api.GI_PRETEST_OFF}),
+]
+
+
+@pytest.mark.parametrize("name,tech,fields", CASES, ids=[c[0] for c in CASES])
+def test_oracle_lookups_equal_the_second_restatement(world, name, tech, fields):
+    fr, depth, pos, nrm = world
+    p = gi.ShadowParams.defaults(tech)
+    for k, v in fields.items():
+        setattr(p, k, v)
+    c = p.to_c(fr)
+    bt = gi.poisson_table(p.poisson_blocker_taps)
+    ft = gi.poisson_table(p.poisson_filter_taps)
+    tab = np.concatenate([bt.reshape(-1), ft.reshape(-1)])
+    got = oracle.visibility(c, depth, S, S, pos.reshape(-1), nrm.reshape(-1), len(pos), 1, tab)
+    rp = ref.params_of(c)
+    taps_b = [(np.float32(x), np.float32(y)) for x, y in bt]
+    taps_f = [(np.float32(x), np.float32(y)) for x, y in ft]
+    want = np.array([ref.shade(rp, depth, S, S, [np.float32(v) for v in pos[k]], [np.float32(v) for v in nrm[k]],
+                               taps_b, taps_f) for k in range(len(pos))], np.float32)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), \
+        f"{name}: {int((got != want).sum())} of {len(pos)} pixels differ"
+    fgv = want[pos[:, 0] != 0]
+    if "cut-off" in name:
+        # every blocker of this scene lies below the reference's 0.99 cut-off,
+        # so PCSS returns fully lit wherever the pre-test passes
+        assert set(np.unique(fgv).tolist()) <= {1.0, float(np.float32(p.shadow_intensity))}
+        return
+    # the probes cover lit, shadowed and (for the soft techniques) partly lit pixels
+    assert (fgv == 1.0).any() and (fgv < 1.0).any()
+    if tech in (api.GI_TECH_PCF, api.GI_TECH_PCSS_GRID, api.GI_TECH_PCSS_POISSON):
+        assert ((fgv > p.shadow_intensity) & (fgv < 1.0)).any(), "no partly lit pixel among the probes"
+
+
+def test_receiver_on_the_stored_depth_is_lit(world):
+    """Shadow.frag's test is z <= depth: a receiver whose texel holds exactly
+    its own depth is lit, in the oracle and in the restatement."""
+    fr, depth, pos, nrm = world
+    p = gi.ShadowParams.defaults(api.GI_TECH_HARD)
+    p.pretest = api.GI_PRETEST_OFF
+    c = p.to_c(fr)
+    rp = ref.params_of(c)
+    on_surface = depth.copy()
+    fg = [k for k in range(len(pos)) if pos[k, 0] != 0]
+    for k in fg:
+        v = [np.float32(x) for x in pos[k]]
+        sc = ref.mat4_mul(rp["light_mvp_biased"], v)
+        s, t, z = sc[0] / sc[3], sc[1] / sc[3], sc[2] / sc[3]
+        i, j = int(np.floor(s * np.float32(S))), int(np.floor(t * np.float32(S)))
+        if 0 <= i < S and 0 <= j < S:
+            on_surface[j * S + i] = z
+    got = oracle.visibility(c, on_surface, S, S, pos.reshape(-1), nrm.reshape(-1), len(pos), 1)
+    want = np.array([ref.shade(rp, on_surface, S, S, [np.float32(x) for x in pos[k]],
+                               [np.float32(x) for x in nrm[k]]) for k in range(len(pos))], np.float32)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    # two probes may share a texel; the one written last is lit for sure
+    assert (got[fg] == 1.0).mean() > 0.9
