@@ -13,12 +13,18 @@ import raster_ref as ref
 
 
 @pytest.fixture(scope="module")
-def mesh():
+def scene_arrays():
     s = gi.Scene()
     s.ground(10.0, 0.0)
     s.icosphere_field(8, 2, (-8.0, 0.2, -8.0), (8.0, 3.0, 8.0), 0.4, 1.6, 0x5EED0007)
-    p, _, i = s.arrays()
+    arrays = s.arrays()
     s.close()
+    return arrays
+
+
+@pytest.fixture(scope="module")
+def mesh(scene_arrays):
+    p, _, i = scene_arrays
     return p, i
 
 
@@ -86,3 +92,27 @@ def test_edges_through_pixel_centres_follow_the_top_left_rule():
     za, zb = d[4, 3], d[11, 10]  # inside the first / the second triangle only
     diag = [(y, x) for y in range(3, 13) for x in range(2, 12) if x + y == 14 and not (5 <= x <= 9 and 5 <= y <= 9)]
     assert za != zb and all(d[y, x] in (za, zb) for y, x in diag)
+
+
+@pytest.mark.parametrize("eye,W,H", [((0.0, 14.0, -20.0), 96, 54), ((0.0, 0.6, -9.5), 72, 40),
+                                     ((-9.0, 3.0, 6.0), 64, 64), ((2.0, -6.0, -9.0), 64, 48)],
+                         ids=["camera over the field", "low eye (near-plane clipping)", "oblique",
+                              "below the ground (back faces)"])
+def test_oracle_gbuffer_equals_brute_force_restatement(scene_arrays, eye, W, H):
+    """The G-buffer: nearest fragment, first in draw order among equal depths,
+    position and normal interpolated perspective-correct (through the
+    clipped sub-triangle's source weights), front-facing flag in nrm.w."""
+    p, n, i = scene_arrays
+    v = gi.ViewSpec(eye=eye, at=(0.0, 0.0, 0.0), width=W, height=H)
+    mvp = gi.frame_setup(v, v).camera_mvp
+    got_p, got_n = oracle.gbuffer(p, n, i, mvp, W, H)
+    want_p, want_n = ref.gbuffer(p, n, i, mvp, W, H)
+    assert np.array_equal(got_p.view(np.uint32), want_p.view(np.uint32))
+    assert np.array_equal(got_n.view(np.uint32), want_n.view(np.uint32))
+    fg = want_p.reshape(-1, 4)[:, 0] != 0
+    assert fg.mean() > 0.3
+    w = want_n.reshape(-1, 4)[fg, 3]
+    if eye[1] < 0:  # the ground seen from below shows its back face
+        assert (w == 0.0).any() and (w == 1.0).any()
+    else:
+        assert (w == 1.0).any()
