@@ -218,3 +218,22 @@ def gbuffer(points, normals, indices, mvp, W, H):
             out_n[p, j] = (B[0] * N[0][j] + B[1] * N[1][j]) + B[2] * N[2][j]
         out_n[p, 3] = 1.0 if s["front"] else 0.0
     return pos.reshape(-1), out_n.reshape(-1)
+
+
+def stencil_counts(points, indices, volume_triangles, mvp, W, H, less_equal):
+    """ShadowVolumes' stencil pass (ShadowVolumes/src/main.cpp:150-172): the
+    depth prepass (no bias), then every volume triangle drawn against it with
+    LESS (or LEQUAL), +1 for a front-facing and -1 for a back-facing
+    fragment that passes, the sum wrapped to 8 bits.  volume_triangles:
+    float32 [n, 3, 3] world-space triangles."""
+    depth = shadow_map(points, indices, mvp, W, H)
+    count = np.zeros(H * W, np.int64)
+    vt = np.asarray(volume_triangles, np.float32).reshape(-1, 3)
+    tri = np.arange(len(vt), dtype=np.int64).reshape(-1, 3)
+    for _, _, s, ys, xs, _, z in fragments(vt, tri, mvp, W, H):
+        z = clamp01(z)
+        idx = ys * W + xs
+        d = depth[idx]
+        passed = (z <= d) if less_equal else (z < d)
+        np.add.at(count, idx[passed], 1 if s["front"] else -1)
+    return (count & 0xFF).astype(np.uint8), depth

@@ -116,3 +116,21 @@ def test_oracle_gbuffer_equals_brute_force_restatement(scene_arrays, eye, W, H):
         assert (w == 0.0).any() and (w == 1.0).any()
     else:
         assert (w == 1.0).any()
+
+
+@pytest.mark.parametrize("func", [api.GI_DEPTH_LESS, api.GI_DEPTH_LEQUAL], ids=["LESS", "LEQUAL"])
+def test_oracle_stencil_counts_equal_brute_force_restatement(scene_arrays, func):
+    """Shadow-volume stencil counts: the volume triangles are ShadowVolume::
+    build's (the oracle's geometry, itself pinned to the reference's own
+    code), drawn by the brute-force rasteriser against its own prepass."""
+    p, n, i = scene_arrays
+    W, H = 80, 48
+    v = gi.ViewSpec(eye=(0.0, 9.0, -14.0), at=(0.0, 0.5, 0.0), width=W, height=H)
+    mvp = gi.frame_setup(v, v).camera_mvp
+    L = np.array([3.0, 12.0, -2.0], np.float32)
+    got_st, got_d = oracle.shadow_volume_counts(p, n, i, L, 100.0, mvp, W, H, func)
+    vols = oracle.shadow_volume_geometry(p, n, i, L, 100.0)
+    want_st, want_d = ref.stencil_counts(p, i, vols, mvp, W, H, func == api.GI_DEPTH_LEQUAL)
+    assert np.array_equal(got_d.view(np.uint32), want_d.view(np.uint32))
+    assert np.array_equal(got_st, want_st), f"{int((got_st != want_st).sum())} pixels differ"
+    assert (want_st != 0).any() and (want_st == 0).any()  # shadowed and lit pixels
