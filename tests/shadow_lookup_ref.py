@@ -22,7 +22,9 @@ CPU tests can hold the oracle to it bit for bit:
 * the Poisson-disk PCSS of this library (no reference counterpart): the
   same blocker search and filter with the grid offsets replaced by the
   Poisson points times the blocker search width / the penumbra width, the
-  filter averaging over its own tap count.
+  filter averaging over its own tap count;
+* deferred Phong shading (ShadowMapping/Shaders/GBuffer/PhongShading.frag:
+  11-46, shadeScene).
 """
 from __future__ import annotations
 
@@ -173,3 +175,42 @@ def params_of(c):
         "light_mvp_biased": [f32(x) for x in c.light_mvp_biased], "camera_mv": [f32(x) for x in c.camera_mv],
         "normal_matrix": [f32(x) for x in c.normal_matrix], "light_position": [f32(x) for x in c.light_position],
     }
+
+
+def phong(p, vertex, normal, shadow, color=(1.0, 1.0, 1.0, 1.0)):
+    """shadeScene's PhongShading.frag:11-46 for one pixel (RGBA float32):
+    shadow * fragmentColor * (Idiff + Ispec + Iamb), with reflect(I, N) =
+    I - 2 dot(N, I) N, E = normalize(-vertex) over the 4-component eye-space
+    vertex, pow(x, 0.3 * 10) as x * x * x; background keeps the clear colour."""
+    if vertex[0] == 0:
+        return [f32(0.63), f32(0.82), f32(0.96), f32(1.0)]
+    spec_shadow = shadow - p["intensity"]
+    v = mat4_mul(p["camera_mv"], vertex)
+    nm = p["normal_matrix"]
+    nx = (nm[0] * normal[0] + nm[3] * normal[1]) + nm[6] * normal[2]
+    ny = (nm[1] * normal[0] + nm[4] * normal[1]) + nm[7] * normal[2]
+    nz = (nm[2] * normal[0] + nm[5] * normal[1]) + nm[8] * normal[2]
+    inv = f32(1.0) / np.sqrt((nx * nx + ny * ny) + nz * nz)
+    nx, ny, nz = nx * inv, ny * inv, nz * inv
+    lp = p["light_position"]
+    lx, ly, lz = lp[0] - v[0], lp[1] - v[1], lp[2] - v[2]
+    inv = f32(1.0) / np.sqrt((lx * lx + ly * ly) + lz * lz)
+    lx, ly, lz = lx * inv, ly * inv, lz * inv
+    e = [-v[0], -v[1], -v[2], -v[3]]
+    inv = f32(1.0) / np.sqrt(((e[0] * e[0] + e[1] * e[1]) + e[2] * e[2]) + e[3] * e[3])
+    ex, ey, ez = e[0] * inv, e[1] * inv, e[2] * inv
+    ndl = (nx * lx + ny * ly) + nz * lz
+    two = f32(2.0)
+    rx, ry, rz = -(lx - (two * ndl) * nx), -(ly - (two * ndl) * ny), -(lz - (two * ndl) * nz)
+    inv = f32(1.0) / np.sqrt((rx * rx + ry * ry) + rz * rz)
+    rx, ry, rz = rx * inv, ry * inv, rz * inv
+    diff = max(ndl, f32(0.0))
+    re = max((rx * ex + ry * ey) + rz * ez, f32(0.0))
+    spec = (re * re) * re
+    amb, dif, spc = (0.4, 0.4, 0.4, 1.0), (0.5, 0.5, 0.5, 1.0), (0.25, 0.25, 0.25, 1.0)
+    out = []
+    for k in range(4):
+        idiff = f32(dif[k]) * diff
+        ispec = (spec_shadow * f32(spc[k])) * spec
+        out.append((shadow * f32(color[k])) * ((idiff + ispec) + f32(amb[k])))
+    return out

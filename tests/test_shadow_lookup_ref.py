@@ -104,3 +104,19 @@ def test_receiver_on_the_stored_depth_is_lit(world):
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
     # two probes may share a texel; the one written last is lit for sure
     assert (got[fg] == 1.0).mean() > 0.9
+
+
+def test_oracle_phong_equals_the_second_restatement(world):
+    """Deferred Phong (shadeScene) of the probes, with visibility values of
+    every kind (0, the intensity, 1 and fractions) and per-pixel colours."""
+    fr, depth, pos, nrm = world
+    p = gi.ShadowParams.defaults(api.GI_TECH_HARD)
+    c = p.to_c(fr)
+    rng = np.random.default_rng(7)
+    vis = rng.choice(np.array([0.0, 0.25, 1.0, 0.6, 0.93], np.float32), len(pos)).astype(np.float32)
+    color = rng.random((len(pos), 4), dtype=np.float32)
+    got = oracle.phong_shade(c, pos.reshape(-1), nrm.reshape(-1), vis, len(pos), 1, color.reshape(-1))
+    rp = ref.params_of(c)
+    want = np.array([ref.phong(rp, [np.float32(v) for v in pos[k]], [np.float32(v) for v in nrm[k]], vis[k], color[k])
+                     for k in range(len(pos))], np.float32).reshape(-1)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
