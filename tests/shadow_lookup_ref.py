@@ -24,7 +24,9 @@ CPU tests can hold the oracle to it bit for bit:
   Poisson points times the blocker search width / the penumbra width, the
   filter averaging over its own tap count;
 * deferred Phong shading (ShadowMapping/Shaders/GBuffer/PhongShading.frag:
-  11-46, shadeScene).
+  11-46, shadeScene);
+* the uniform area-light ground truth (AccurateSoftShadow.frag:52-133), its
+  maps and G-buffer drawn by raster_ref's brute-force rasteriser.
 """
 from __future__ import annotations
 
@@ -213,4 +215,37 @@ def phong(p, vertex, normal, shadow, color=(1.0, 1.0, 1.0, 1.0)):
         idiff = f32(dif[k]) * diff
         ispec = (spec_shadow * f32(spc[k])) * spec
         out.append((shadow * f32(color[k])) * ((idiff + ispec) + f32(amb[k])))
+    return out
+
+
+def area_light_visibility(points, normals, indices, mvps, biased, S, bias_mode, cbias, factor, units, camera_mvp,
+                          intensity, W, H):
+    """renderMonteCarlo's uniform branch (SoftShadowMapping/src/main.cpp:756-811,
+    AccurateSoftShadow.frag:52-133) with the light maps and the G-buffer drawn
+    by the brute-force rasteriser of raster_ref: per pixel the common
+    coordinate from columns 0-2 of the LAST sample's biased MVP, plus each
+    sample's translation column, divided by w, one NEAREST fetch from that
+    sample's map, accShadow += (z <= d ? 1 : intensity) * 1, shadow =
+    accShadow / count; no pre-test, background 0."""
+    import raster_ref
+
+    pos, _ = raster_ref.gbuffer(points, normals, indices, camera_mvp, W, H)
+    pos = pos.reshape(-1, 4)
+    I = f32(intensity)
+    m = [f32(v) for v in np.asarray(biased[-1], np.float32).reshape(16)]
+    acc = np.zeros(W * H, np.float32)
+    fg = np.flatnonzero(pos[:, 0] != 0)
+    for k in range(len(mvps)):
+        depth = raster_ref.shadow_map(points, indices, mvps[k], S, S, bias_mode, cbias, factor, units)
+        t = [f32(v) for v in np.asarray(biased[k], np.float32).reshape(16)[12:]]
+        for q in fg:
+            x, y, z = pos[q, 0], pos[q, 1], pos[q, 2]
+            c = [((m[r] * x + m[4 + r] * y) + m[8 + r] * z) + t[r] for r in range(4)]
+            d = fetch(depth, S, S, c[0] / c[3], c[1] / c[3])
+            acc[q] = acc[q] + (f32(1.0) if c[2] / c[3] <= d else I) * f32(1.0)
+    count = f32(0.0)
+    for _ in range(len(mvps)):
+        count = count + f32(1.0)
+    out = np.zeros(W * H, np.float32)
+    out[fg] = acc[fg] / count
     return out

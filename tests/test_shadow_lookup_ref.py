@@ -120,3 +120,23 @@ def test_oracle_phong_equals_the_second_restatement(world):
     want = np.array([ref.phong(rp, [np.float32(v) for v in pos[k]], [np.float32(v) for v in nrm[k]], vis[k], color[k])
                      for k in range(len(pos))], np.float32).reshape(-1)
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_oracle_area_light_truth_equals_the_second_restatement():
+    """The uniform area-light ground truth of a 3 x 3 sample grid, every map
+    and the G-buffer drawn by the brute-force rasteriser."""
+    Wc, Hc, Sm = 48, 28, 64
+    w = scenes.pcss_1080p(width=Wc, height=Hc, map_size=Sm, spheres=6)
+    views = gi.area_light_samples(w.light, 1.5, 3)
+    frames = [gi.frame_setup(v, w.camera) for v in views]
+    p, n, i = w.scene.arrays()
+    w.scene.close()
+    mp = w.map_params
+    mvps = np.stack([f.light_mvp for f in frames])
+    biased = np.stack([f.light_mvp_biased for f in frames])
+    args = (p, n, i, mvps, biased, Sm, mp.bias_mode, mp.constant_bias, mp.offset_factor, mp.offset_units,
+            frames[0].camera_mvp, 0.25, Wc, Hc)
+    got = oracle.area_light_visibility(*args)
+    want = ref.area_light_visibility(*args)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), f"{int((got != want).sum())} pixels differ"
+    assert ((want > 0.25) & (want < 1.0)).any()  # penumbrae present
