@@ -140,3 +140,45 @@ def test_oracle_area_light_truth_equals_the_second_restatement():
     want = ref.area_light_visibility(*args)
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), f"{int((got != want).sum())} pixels differ"
     assert ((want > 0.25) & (want < 1.0)).any()  # penumbrae present
+
+
+SMSR_CASES = [
+    ("smsr", api.GI_TECH_SMSR_NONCONSERVATIVE, {"max_search": 16, "depth_threshold": 0.0}),
+    ("smsr, depth threshold", api.GI_TECH_SMSR_NONCONSERVATIVE, {"max_search": 8, "depth_threshold": 1e-2}),
+    ("rpcf + smsr 3 / 1", api.GI_TECH_RPCF_SMSR, {"max_search": 16, "kernel_order": 3, "penumbra_size": 1}),
+    ("rpcf + smsr 2 / 2, threshold", api.GI_TECH_RPCF_SMSR,
+     {"max_search": 12, "kernel_order": 2, "penumbra_size": 2, "depth_threshold": 1e-2}),
+]
+
+
+@pytest.mark.parametrize("name,tech,fields", SMSR_CASES, ids=[c[0] for c in SMSR_CASES])
+def test_oracle_smsr_equals_the_second_restatement(world, name, tech, fields):
+    """NonConservativeSMSR.frag (SMSR and RPCF + SMSR) on the probes, bit for
+    bit, with enough probes on shadow edges to exercise the revectorisation."""
+    import smsr_ref
+
+    fr, depth, pos, nrm = world
+    p = gi.ShadowParams.defaults(tech)
+    for k, v in fields.items():
+        setattr(p, k, v)
+    c = p.to_c(fr)
+    got = oracle.visibility(c, depth, S, S, pos.reshape(-1), nrm.reshape(-1), len(pos), 1)
+    rp = ref.params_of(c)
+    sm = smsr_ref.Smsr(depth, S, S, p.shadow_intensity, p.depth_threshold, p.max_search, p.kernel_order,
+                       p.penumbra_size)
+    want = []
+    for k in range(len(pos)):
+        v, nv = [np.float32(x) for x in pos[k]], [np.float32(x) for x in nrm[k]]
+        if v[0] == 0:
+            want.append(np.float32(0.0))
+            continue
+        sc = ref.mat4_mul(rp["light_mvp_biased"], v)
+        n = [sc[0] / sc[3], sc[1] / sc[3], sc[2] / sc[3], sc[3] / sc[3]]
+        shadow = ref.pretest(rp, v, nv)
+        if shadow == 1:
+            shadow = sm.smsr(n) if tech == api.GI_TECH_SMSR_NONCONSERVATIVE else sm.rpcf(n)
+        want.append(shadow)
+    want = np.array(want, np.float32)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), \
+        f"{name}: {int((got != want).sum())} of {len(pos)} pixels differ"
+    assert sm.discontinuities >= 10, "too few probes on a shadow edge"
