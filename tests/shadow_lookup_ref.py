@@ -14,8 +14,9 @@ CPU tests can hold the oracle to it bit for bit:
   normalize(v) fixed as v * (1 / sqrt(dot(v, v))) and dot / matrix products
   summed left to right;
 * the naive hard test (Shadow.frag:253-256) and PCF's float loop
-  (Shadow.frag:86-116) over a NEAREST, CLAMP_TO_BORDER (border 0) map: the
-  texel of (s, t) is (floor(s * W), floor(t * H));
+  (Shadow.frag:86-116), bilinear (one texture2D) or tricubic
+  (textureBicubic, :41-84), over a NEAREST, CLAMP_TO_BORDER (border 0) map:
+  the texel of (s, t) is (floor(s * W), floor(t * H));
 * PCSS (PlausibleSoftShadow.frag:166-194 blocker search, 365-374 penumbra
   width, 376-398 filter, 556-563), with the light radius a float and the
   0.99 average-blocker cut-off a parameter;
@@ -34,7 +35,7 @@ import numpy as np
 
 f32 = np.float32
 
-TECH_HARD, TECH_PCF, TECH_PCSS_GRID, TECH_PCSS_POISSON = 0, 1, 3, 4
+TECH_HARD, TECH_PCF, TECH_PCF_TRICUBIC, TECH_PCSS_GRID, TECH_PCSS_POISSON = 0, 1, 2, 3, 4
 PRETEST_REFERENCE, PRETEST_OFF = 0, 1
 
 
@@ -72,7 +73,42 @@ def pretest(p, vertex, normal):
     return p["intensity"] if max(d, f32(0.0)) == 0 else f32(1.0)
 
 
-def pcf(p, depth, W, H, n):
+def cubic(v):
+    """cubic() of Shadow.frag:41-52."""
+    n = [f32(1.0) - v, f32(2.0) - v, f32(3.0) - v, f32(4.0) - v]
+    s = [(k * k) * k for k in n]
+    x = s[0]
+    y = s[1] - f32(4.0) * s[0]
+    z = (s[2] - f32(4.0) * s[1]) + f32(6.0) * s[0]
+    w = ((f32(6.0) - x) - y) - z
+    k = f32(1.0 / 6.0)
+    return [x * k, y * k, z * k, w * k]
+
+
+def texture_bicubic(depth, W, H, u, v):
+    """textureBicubic (Shadow.frag:54-84): four NEAREST fetches blended."""
+    inv_w, inv_h = f32(1.0) / f32(W), f32(1.0) / f32(H)
+    tx, ty = u * f32(W) - f32(0.5), v * f32(H) - f32(0.5)
+    fx, fy = tx - np.floor(tx), ty - np.floor(ty)
+    tx, ty = tx - fx, ty - fy
+    xc, yc = cubic(fx), cubic(fy)
+    c = [tx + f32(-0.5), tx + f32(1.5), ty + f32(-0.5), ty + f32(1.5)]
+    s = [xc[0] + xc[1], xc[2] + xc[3], yc[0] + yc[1], yc[2] + yc[3]]
+    num = [xc[1], xc[3], yc[1], yc[3]]
+    off = [c[i] + num[i] / s[i] for i in range(4)]
+    off = [off[0] * inv_w, off[1] * inv_w, off[2] * inv_h, off[3] * inv_h]
+    s0, s1 = fetch(depth, W, H, off[0], off[2]), fetch(depth, W, H, off[1], off[2])
+    s2, s3 = fetch(depth, W, H, off[0], off[3]), fetch(depth, W, H, off[1], off[3])
+    sx = s[0] / (s[0] + s[1])
+    sy = s[2] / (s[2] + s[3])
+
+    def mix(a, b, t):
+        return a * (f32(1.0) - t) + b * t
+
+    return mix(mix(s3, s2, sx), mix(s1, s0, sx), sy)
+
+
+def pcf(p, depth, W, H, n, tricubic=False):
     incr_w, incr_h = f32(1.0) / f32(W), f32(1.0) / f32(H)
     illum = f32(0.0)
     offset = f32(p["penumbra_size"])
@@ -82,7 +118,8 @@ def pcf(p, depth, W, H, n):
     while w < offset:
         h = -offset
         while h < offset:
-            d = fetch(depth, W, H, n[0] + w * incr_w, n[1] + h * incr_h)
+            u, v = n[0] + w * incr_w, n[1] + h * incr_h
+            d = texture_bicubic(depth, W, H, u, v) if tricubic else fetch(depth, W, H, u, v)
             illum = illum + (f32(1.0) if n[2] <= d else p["intensity"])
             count += 1
             h = h + step
@@ -159,6 +196,8 @@ def shade(p, depth, W, H, vertex, normal, blocker_taps=None, filter_taps=None):
         return f32(1.0) if n[2] <= fetch(depth, W, H, n[0], n[1]) else p["intensity"]
     if tech == TECH_PCF:
         return pcf(p, depth, W, H, n)
+    if tech == TECH_PCF_TRICUBIC:
+        return pcf(p, depth, W, H, n, tricubic=True)
     if tech == TECH_PCSS_GRID:
         return pcss_filter(p, depth, W, H, n, penumbra_width(p, avg_blocker(p, depth, W, H, n), n[2]))
     if tech == TECH_PCSS_POISSON:

@@ -38,6 +38,7 @@ CASES = [
     ("hard, no pre-test", api.GI_TECH_HARD, {"pretest": api.GI_PRETEST_OFF}),
     ("pcf 7 / 1", api.GI_TECH_PCF, {"kernel_order": 7, "penumbra_size": 1}),
     ("pcf 3 / 2", api.GI_TECH_PCF, {"kernel_order": 3, "penumbra_size": 2}),
+    ("pcf tricubic 5 / 1", api.GI_TECH_PCF_TRICUBIC, {"kernel_order": 5, "penumbra_size": 1}),
     ("pcss grid 7 / 15", api.GI_TECH_PCSS_GRID,
      {"blocker_search_size": 7, "kernel_size": 15, "light_radius": 4.0, "pcss_min_blocker_depth": 0.0}),
     ("pcss grid 4 / 6, cut-off", api.GI_TECH_PCSS_GRID,
@@ -77,7 +78,7 @@ def test_oracle_lookups_equal_the_second_restatement(world, name, tech, fields):
         return
     # the probes cover lit, shadowed and (for the soft techniques) partly lit pixels
     assert (fgv == 1.0).any() and (fgv < 1.0).any()
-    if tech in (api.GI_TECH_PCF, api.GI_TECH_PCSS_GRID, api.GI_TECH_PCSS_POISSON):
+    if tech in (api.GI_TECH_PCF, api.GI_TECH_PCF_TRICUBIC, api.GI_TECH_PCSS_GRID, api.GI_TECH_PCSS_POISSON):
         assert ((fgv > p.shadow_intensity) & (fgv < 1.0)).any(), "no partly lit pixel among the probes"
 
 
