@@ -13,7 +13,8 @@ CPU tests can hold the oracle to it bit for bit:
 * computePreEvaluationBasedOnNormalOrientation (Shadow.frag:222-238), with
   normalize(v) fixed as v * (1 / sqrt(dot(v, v))) and dot / matrix products
   summed left to right;
-* the naive hard test (Shadow.frag:253-256) and PCF's float loop
+* the naive hard test (Shadow.frag:253-256; the soft app's
+  HardShadow.frag:36-58, background for failed pre-tests) and PCF's float loop
   (Shadow.frag:86-116), bilinear (one texture2D) or tricubic
   (textureBicubic, :41-84), over a NEAREST, CLAMP_TO_BORDER (border 0) map:
   the texel of (s, t) is (floor(s * W), floor(t * H));
@@ -36,6 +37,7 @@ import numpy as np
 f32 = np.float32
 
 TECH_HARD, TECH_PCF, TECH_PCF_TRICUBIC, TECH_PCSS_GRID, TECH_PCSS_POISSON = 0, 1, 2, 3, 4
+TECH_HARD_SOFTAPP = 10
 PRETEST_REFERENCE, PRETEST_OFF = 0, 1
 
 
@@ -189,9 +191,14 @@ def shade(p, depth, W, H, vertex, normal, blocker_taps=None, filter_taps=None):
     sc = mat4_mul(p["light_mvp_biased"], vertex)
     n = [sc[0] / sc[3], sc[1] / sc[3], sc[2] / sc[3], sc[3] / sc[3]]
     shadow = pretest(p, vertex, normal)
+    tech = p["technique"]
+    if tech == TECH_HARD_SOFTAPP:  # SoftShadowMapping HardShadow.frag:36-58
+        r = shadow
+        if sc[3] > 0 and r == 1:
+            r = f32(1.0) if n[2] <= fetch(depth, W, H, n[0], n[1]) else p["intensity"]
+        return f32(0.0) if pretest(p, vertex, normal) == p["intensity"] else r
     if not (sc[3] > 0 and shadow == 1):
         return shadow
-    tech = p["technique"]
     if tech == TECH_HARD:
         return f32(1.0) if n[2] <= fetch(depth, W, H, n[0], n[1]) else p["intensity"]
     if tech == TECH_PCF:

@@ -36,6 +36,7 @@ def world():
 CASES = [
     ("hard", api.GI_TECH_HARD, {}),
     ("hard, no pre-test", api.GI_TECH_HARD, {"pretest": api.GI_PRETEST_OFF}),
+    ("hard, soft app", api.GI_TECH_HARD_SOFTAPP, {}),
     ("pcf 7 / 1", api.GI_TECH_PCF, {"kernel_order": 7, "penumbra_size": 1}),
     ("pcf 3 / 2", api.GI_TECH_PCF, {"kernel_order": 3, "penumbra_size": 2}),
     ("pcf tricubic 5 / 1", api.GI_TECH_PCF_TRICUBIC, {"kernel_order": 5, "penumbra_size": 1}),
