@@ -210,3 +210,113 @@ class Smsr:
                 h = h + step
             w = w + step
         return illum / f32(count)
+
+
+class ConservativeSmsr:
+    """ShadowMapping/Shaders/RBSM/ConservativeSMSR.frag: computeShadowFromSMSR
+    (:127-144, the conservative SMSR technique) and computeShadowFromRPCF
+    (:146-198, conservative RPCF), with computeDiscontinuity (:23-47: 1 for a
+    shadowed neighbour), computeRelativeDistance (:49-94), its normalisation
+    (:96-115) and revectorizeShadow (:117-125)."""
+
+    def __init__(self, depth, W, H, intensity, depth_threshold, max_search, kernel_order=3, penumbra_size=1):
+        self.depth, self.W, self.H = depth, W, H
+        self.sx, self.sy = f32(1.0 / W), f32(1.0 / H)
+        self.I = f32(intensity)
+        self.thr = f32(depth_threshold)
+        self.max_search = int(max_search)
+        self.kernel_order, self.penumbra_size = int(kernel_order), int(penumbra_size)
+        self.discontinuities = 0
+
+    def tex(self, x, y):
+        return fetch(self.depth, self.W, self.H, x, y)
+
+    def disc(self, c):
+        x, y, z = c[0], c[1], c[2]
+        out = []
+        x = x - self.sx
+        out.append(ONE if z <= self.tex(x, y) else ZERO)
+        x = x + TWO * self.sx
+        out.append(ONE if z <= self.tex(x, y) else ZERO)
+        x = x - self.sx
+        y = y + self.sy
+        out.append(ONE if z <= self.tex(x, y) else ZERO)
+        y = y - TWO * self.sy
+        out.append(ONE if z <= self.tex(x, y) else ZERO)
+        return [abs(v - ONE) for v in out]
+
+    def distance(self, c, dir_, sub):
+        x, y, z = c[0], c[1], c[2]
+        found = ZERO
+        dist = ZERO
+        stx, sty = f32(dir_[0]) * self.sx, f32(dir_[1]) * self.sy
+        x, y = x + stx, y + sty
+        for _ in range(self.max_search):
+            d = self.tex(x, y)
+            if abs(z - d) < self.thr:
+                z = z - self.thr
+            if not (z <= d):  # the centre is in umbra: the silhouette ends here
+                found = ONE
+                break
+            dd = self.disc((x, y, z))
+            if ((dd[0] + dd[1]) + dd[2]) + dd[3] == 0:
+                break
+            dist = dist + ONE
+            x, y = x + stx, y + sty
+        dist = dist + (ONE - sub)
+        return mix(-dist, dist, found)
+
+    def normalise(self, dx, dy):
+        T = ONE
+        if dx < 0 and dy < 0:
+            T = ZERO
+        if dx > 0 and dy > 0:
+            T = f32(-2.0)
+        length = min(abs(dx) + abs(dy), f32(self.max_search))
+        return abs(max(T * dx, T * dy)) / length
+
+    def revectorized(self, c):
+        self.discontinuities += 1
+        sub = (fract(c[0] * f32(self.W)), fract(c[1] * f32(self.H)))
+        ds = [self.distance(c, (-1.0, 0.0), ONE - sub[0]), self.distance(c, (1.0, 0.0), sub[0]),
+              self.distance(c, (0.0, -1.0), ONE - sub[1]), self.distance(c, (0.0, 1.0), sub[1])]
+        r = (self.normalise(ds[0], ds[1]), self.normalise(ds[2], ds[3]))
+        if (r[0] * r[1] > 0) and (ONE - r[0] > r[1]):
+            return self.I
+        return ONE
+
+    def smsr(self, c):
+        d = self.tex(c[0], c[1])
+        if not (c[2] <= d):
+            return self.I
+        dd = self.disc(c)
+        if ((dd[0] + dd[1]) + dd[2]) + dd[3] == 0:
+            return ONE
+        if dd[0] + dd[1] == TWO or dd[2] + dd[3] == TWO:
+            return self.I
+        return self.revectorized(c)
+
+    def rpcf(self, c):
+        incr_w, incr_h = ONE / f32(self.W), ONE / f32(self.H)
+        illum = ZERO
+        offset = f32(self.penumbra_size)
+        step = (TWO * offset) / f32(self.kernel_order)
+        count = 0
+        w = -offset
+        while w <= offset:
+            h = -offset
+            while h <= offset:
+                d = self.tex(c[0] + w * incr_w, c[1] + h * incr_h)
+                if c[2] <= d:
+                    s = (c[0] + w * incr_w, c[1] + h * incr_h, c[2], c[3])
+                    dd = self.disc(s)
+                    if dd[0] == 0 and dd[1] == 0:
+                        illum = illum + ONE
+                    else:
+                        illum = illum + self.revectorized(s)
+                else:
+                    illum = illum + self.I
+                count += 1
+                h = h + step
+            w = w + step
+        return illum / f32(count)

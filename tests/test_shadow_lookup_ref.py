@@ -30,7 +30,12 @@ def world():
     bg = np.flatnonzero(pos[:, 0] == 0)
     pick = np.concatenate([rng.choice(fg, 400, replace=False), rng.choice(bg, 4, replace=False)])
     w.scene.close()
-    return fr, depth, pos[pick].copy(), nrm[pick].copy()
+    return fr, depth, pos[pick].copy(), nrm[pick].copy(), pos, nrm
+
+
+@pytest.fixture(scope="module")
+def world_probes(world):
+    return world[:4]
 
 
 CASES = [
@@ -54,8 +59,8 @@ CASES = [
 
 
 @pytest.mark.parametrize("name,tech,fields", CASES, ids=[c[0] for c in CASES])
-def test_oracle_lookups_equal_the_second_restatement(world, name, tech, fields):
-    fr, depth, pos, nrm = world
+def test_oracle_lookups_equal_the_second_restatement(world_probes, name, tech, fields):
+    fr, depth, pos, nrm = world_probes
     p = gi.ShadowParams.defaults(tech)
     for k, v in fields.items():
         setattr(p, k, v)
@@ -83,10 +88,10 @@ def test_oracle_lookups_equal_the_second_restatement(world, name, tech, fields):
         assert ((fgv > p.shadow_intensity) & (fgv < 1.0)).any(), "no partly lit pixel among the probes"
 
 
-def test_receiver_on_the_stored_depth_is_lit(world):
+def test_receiver_on_the_stored_depth_is_lit(world_probes):
     """Shadow.frag's test is z <= depth: a receiver whose texel holds exactly
     its own depth is lit, in the oracle and in the restatement."""
-    fr, depth, pos, nrm = world
+    fr, depth, pos, nrm = world_probes
     p = gi.ShadowParams.defaults(api.GI_TECH_HARD)
     p.pretest = api.GI_PRETEST_OFF
     c = p.to_c(fr)
@@ -108,10 +113,10 @@ def test_receiver_on_the_stored_depth_is_lit(world):
     assert (got[fg] == 1.0).mean() > 0.9
 
 
-def test_oracle_phong_equals_the_second_restatement(world):
+def test_oracle_phong_equals_the_second_restatement(world_probes):
     """Deferred Phong (shadeScene) of the probes, with visibility values of
     every kind (0, the intensity, 1 and fractions) and per-pixel colours."""
-    fr, depth, pos, nrm = world
+    fr, depth, pos, nrm = world_probes
     p = gi.ShadowParams.defaults(api.GI_TECH_HARD)
     c = p.to_c(fr)
     rng = np.random.default_rng(7)
@@ -150,24 +155,32 @@ SMSR_CASES = [
     ("rpcf + smsr 3 / 1", api.GI_TECH_RPCF_SMSR, {"max_search": 16, "kernel_order": 3, "penumbra_size": 1}),
     ("rpcf + smsr 2 / 2, threshold", api.GI_TECH_RPCF_SMSR,
      {"max_search": 12, "kernel_order": 2, "penumbra_size": 2, "depth_threshold": 1e-2}),
+    ("conservative smsr", api.GI_TECH_SMSR_CONSERVATIVE, {"max_search": 16, "depth_threshold": 0.0}),
+    ("conservative smsr, threshold", api.GI_TECH_SMSR_CONSERVATIVE, {"max_search": 6, "depth_threshold": 1e-2}),
+    ("conservative rpcf 3 / 1", api.GI_TECH_RPCF_CONSERVATIVE,
+     {"max_search": 16, "kernel_order": 3, "penumbra_size": 1, "depth_threshold": 0.0}),
+    ("conservative rpcf 4 / 2, threshold", api.GI_TECH_RPCF_CONSERVATIVE,
+     {"max_search": 10, "kernel_order": 4, "penumbra_size": 2, "depth_threshold": 1e-2}),
 ]
 
 
 @pytest.mark.parametrize("name,tech,fields", SMSR_CASES, ids=[c[0] for c in SMSR_CASES])
 def test_oracle_smsr_equals_the_second_restatement(world, name, tech, fields):
-    """NonConservativeSMSR.frag (SMSR and RPCF + SMSR) on the probes, bit for
-    bit, with enough probes on shadow edges to exercise the revectorisation."""
+    """NonConservativeSMSR.frag (SMSR and RPCF + SMSR) and ConservativeSMSR.frag
+    (SMSR and RPCF) on the probes, bit for bit, with enough probes on shadow
+    edges to exercise the revectorisation."""
     import smsr_ref
 
-    fr, depth, pos, nrm = world
+    fr, depth, _, _, pos, nrm = world  # every pixel of the frame
     p = gi.ShadowParams.defaults(tech)
     for k, v in fields.items():
         setattr(p, k, v)
     c = p.to_c(fr)
     got = oracle.visibility(c, depth, S, S, pos.reshape(-1), nrm.reshape(-1), len(pos), 1)
     rp = ref.params_of(c)
-    sm = smsr_ref.Smsr(depth, S, S, p.shadow_intensity, p.depth_threshold, p.max_search, p.kernel_order,
-                       p.penumbra_size)
+    conservative = tech in (api.GI_TECH_SMSR_CONSERVATIVE, api.GI_TECH_RPCF_CONSERVATIVE)
+    cls = smsr_ref.ConservativeSmsr if conservative else smsr_ref.Smsr
+    sm = cls(depth, S, S, p.shadow_intensity, p.depth_threshold, p.max_search, p.kernel_order, p.penumbra_size)
     want = []
     for k in range(len(pos)):
         v, nv = [np.float32(x) for x in pos[k]], [np.float32(x) for x in nrm[k]]
@@ -178,7 +191,8 @@ def test_oracle_smsr_equals_the_second_restatement(world, name, tech, fields):
         n = [sc[0] / sc[3], sc[1] / sc[3], sc[2] / sc[3], sc[3] / sc[3]]
         shadow = ref.pretest(rp, v, nv)
         if shadow == 1:
-            shadow = sm.smsr(n) if tech == api.GI_TECH_SMSR_NONCONSERVATIVE else sm.rpcf(n)
+            smsr = tech in (api.GI_TECH_SMSR_NONCONSERVATIVE, api.GI_TECH_SMSR_CONSERVATIVE)
+            shadow = sm.smsr(n) if smsr else sm.rpcf(n)
         want.append(shadow)
     want = np.array(want, np.float32)
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), \
