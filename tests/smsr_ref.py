@@ -4,7 +4,8 @@ silhouette revectorisation (test helper).
 ShadowMapping/Shaders/RBSM/NonConservativeSMSR.frag written again with
 numpy float32 scalars, independently of the C++ oracle, in the shader's
 operation order: computeShadowFromSMSR (:279-303, the SMSR technique) and
-computeShadowFromAccurateRPCF (:305-348, RPCF + SMSR), with getDisc's three
+computeShadowFromAccurateRPCF (:305-348, RPCF + SMSR; with FilteredRBSM.frag's
+relative position and revectorisation, RSMSS), with getDisc's three
 overloads (:23-174), computeDiscontinuityLength (:176-225, including the
 shader's global newDepth), estimateRelativePosition (:227-236, 249-256),
 orientateDS (:238-247), revectorizeShadow (:258-266) and
@@ -32,7 +33,13 @@ def fract(x):
 
 
 class Smsr:
-    def __init__(self, depth, W, H, intensity, depth_threshold, max_search, kernel_order=3, penumbra_size=1):
+    """NonConservativeSMSR.frag; with filtered=True FilteredRBSM.frag (RSMSS),
+    whose relative position drops the shadow factor (:241) and whose
+    revectorisation returns a fractional fill (:268-272)."""
+
+    def __init__(self, depth, W, H, intensity, depth_threshold, max_search, kernel_order=3, penumbra_size=1,
+                 filtered=False):
+        self.filtered = filtered
         self.depth, self.W, self.H = depth, W, H
         self.sx, self.sy = f32(1.0 / W), f32(1.0 / H)
         self.I = f32(intensity)
@@ -154,9 +161,18 @@ class Smsr:
         if dx > 0 and dy > 0:
             T = f32(-2.0)
         edge_length = min(abs(dx) + abs(dy), f32(self.max_search))
+        if self.filtered:
+            return (T * abs(max(T * dx, T * dy))) / edge_length
         return (max(T, TWO * shadow - ONE) * abs(max(T * dx, T * dy))) / edge_length
 
     def revectorize(self, r, shadow):
+        if self.filtered:
+            if r[0] * r[1] < 0:
+                return (ONE - shadow) + (TWO * shadow - ONE) * max(r[0], r[1])
+            if r[0] * r[1] == 0:
+                return shadow
+            v = (ONE - shadow) + (TWO * shadow - ONE) * (r[0] + r[1])
+            return min(max(v, ZERO), ONE)
         if (r[0] * r[1] == TWO * shadow) or (
                 (abs(r[0]) * abs(r[1]) > 0) and ((ONE - shadow) + (TWO * shadow - ONE) * (abs(r[0]) + abs(r[1])) < f32(0.5))):
             return ZERO

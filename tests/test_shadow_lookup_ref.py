@@ -155,6 +155,10 @@ SMSR_CASES = [
     ("rpcf + smsr 3 / 1", api.GI_TECH_RPCF_SMSR, {"max_search": 16, "kernel_order": 3, "penumbra_size": 1}),
     ("rpcf + smsr 2 / 2, threshold", api.GI_TECH_RPCF_SMSR,
      {"max_search": 12, "kernel_order": 2, "penumbra_size": 2, "depth_threshold": 1e-2}),
+    ("rsmss 3 / 1", api.GI_TECH_RSMSS, {"max_search": 16, "kernel_order": 3, "penumbra_size": 1,
+                                         "depth_threshold": 0.0}),
+    ("rsmss 5 / 2, threshold", api.GI_TECH_RSMSS,
+     {"max_search": 12, "kernel_order": 5, "penumbra_size": 2, "depth_threshold": 1e-2}),
     ("conservative smsr", api.GI_TECH_SMSR_CONSERVATIVE, {"max_search": 16, "depth_threshold": 0.0}),
     ("conservative smsr, threshold", api.GI_TECH_SMSR_CONSERVATIVE, {"max_search": 6, "depth_threshold": 1e-2}),
     ("conservative rpcf 3 / 1", api.GI_TECH_RPCF_CONSERVATIVE,
@@ -166,8 +170,8 @@ SMSR_CASES = [
 
 @pytest.mark.parametrize("name,tech,fields", SMSR_CASES, ids=[c[0] for c in SMSR_CASES])
 def test_oracle_smsr_equals_the_second_restatement(world, name, tech, fields):
-    """NonConservativeSMSR.frag (SMSR and RPCF + SMSR) and ConservativeSMSR.frag
-    (SMSR and RPCF) on the probes, bit for bit, with enough probes on shadow
+    """NonConservativeSMSR.frag (SMSR and RPCF + SMSR), FilteredRBSM.frag
+    (RSMSS) and ConservativeSMSR.frag (SMSR and RPCF) on the probes, bit for bit, with enough probes on shadow
     edges to exercise the revectorisation."""
     import smsr_ref
 
@@ -179,8 +183,11 @@ def test_oracle_smsr_equals_the_second_restatement(world, name, tech, fields):
     got = oracle.visibility(c, depth, S, S, pos.reshape(-1), nrm.reshape(-1), len(pos), 1)
     rp = ref.params_of(c)
     conservative = tech in (api.GI_TECH_SMSR_CONSERVATIVE, api.GI_TECH_RPCF_CONSERVATIVE)
-    cls = smsr_ref.ConservativeSmsr if conservative else smsr_ref.Smsr
-    sm = cls(depth, S, S, p.shadow_intensity, p.depth_threshold, p.max_search, p.kernel_order, p.penumbra_size)
+    args = (depth, S, S, p.shadow_intensity, p.depth_threshold, p.max_search, p.kernel_order, p.penumbra_size)
+    if conservative:
+        sm = smsr_ref.ConservativeSmsr(*args)
+    else:
+        sm = smsr_ref.Smsr(*args, filtered=tech == api.GI_TECH_RSMSS)
     want = []
     for k in range(len(pos)):
         v, nv = [np.float32(x) for x in pos[k]], [np.float32(x) for x in nrm[k]]
