@@ -27,8 +27,10 @@ CPU tests can hold the oracle to it bit for bit:
   filter averaging over its own tap count;
 * deferred Phong shading (ShadowMapping/Shaders/GBuffer/PhongShading.frag:
   11-46, shadeScene);
-* the uniform area-light ground truth (AccurateSoftShadow.frag:52-133), its
-  maps and G-buffer drawn by raster_ref's brute-force rasteriser.
+* the uniform area-light ground truth (AccurateSoftShadow.frag:52-133) and
+  the adaptive quad-tree one (SoftShadowMapping/src/main.cpp:423-690,
+  Shaders/QuadTree/{Reprojection,Evaluation}.frag, QuadTreeLightSource.cpp),
+  their maps and G-buffer drawn by raster_ref's brute-force rasteriser.
 """
 from __future__ import annotations
 
@@ -295,3 +297,152 @@ def area_light_visibility(points, normals, indices, mvps, biased, S, bias_mode, 
     out = np.zeros(W * H, np.float32)
     out[fg] = acc[fg] / count
     return out
+
+
+def area_light_adaptive(points, normals, indices, light_eye, light_at, size, max_level, view_mvp, S, bias_mode,
+                        cbias, factor, units, camera_mvp, intensity, W, H, lower_accuracy=False):
+    """SoftShadowMapping's adaptive light-source sampling without temporal
+    coherency (src/main.cpp:423-690, 820-870): evaluateAreaLightSource
+    depth first from the root node, each node rendering its four corner
+    samples (QuadTreeLightSource::getEye / getAt, the light's 17 x 17 grid,
+    one map per grid position), the reprojection pass
+    (Shaders/QuadTree/Reprojection.frag: the four corners' hard tests summed,
+    background the clear red 0.63), the evaluation pass
+    (Shaders/QuadTree/Evaluation.frag over a (W / div) x (H / div) viewport,
+    div 4 in the lower-accuracy mode, each coarse pixel reading the count
+    texel at its centre, the border 0) whose occlusion query decides the
+    subdivision (children's reference samples: computeReferenceSamples), then
+    renderAreaLightSource setting each leaf corner's level and the final
+    AccurateSoftShadow.frag pass with weights 1 / (2^level + 1)^2 carried in
+    the translation's w.  Maps and G-buffer come from raster_ref's
+    rasteriser.  Returns (vis, eyes [n, 6], levels [n])."""
+    import raster_ref
+
+    pos, _ = raster_ref.gbuffer(points, normals, indices, camera_mvp, W, H)
+    pos = pos.reshape(-1, 4)
+    fg = np.flatnonzero(pos[:, 0] != 0)
+    I = f32(intensity)
+    fsize = f32(size)
+    grid = {}  # quadTreeHash: grid position -> sample index
+    maps, biased, eyes, level = [], [], [], []
+
+    def offset(ref_, div_pow, index):
+        div = int(np.float32(2.0) ** np.float32(div_pow))
+        step = fsize / f32(div)
+        out = list(ref_)
+        out[0] = out[0] + (-step + (f32(2.0) * step) * f32(index % 2))
+        out[1] = out[1] + (-step + (f32(2.0) * step) * f32(index // 2))
+        return out
+
+    def corner(lvl, node, index):
+        cf, pf = int(16.0 / 2.0 ** lvl), int(2.0 ** lvl)
+        return (index % 2) * cf + (node % pf) * cf, (index // 2) * cf + (node // pf) * cf
+
+    def children(lvl, node):
+        div = int(2.0 ** lvl)
+        x, y = node % div, node // div
+        base = 2 * x + int(2.0 ** (lvl + 2)) * y
+        row = int(2.0 ** (lvl + 1))
+        return [base, base + 1, base + row, base + row + 1]
+
+    def sample(nd, index, x, y):
+        if (x, y) in grid:
+            return grid[(x, y)]
+        e = offset(nd["eye"], nd["level"] + 1, index) + offset(nd["at"], nd["level"] + 1, index)
+        mvp, b = view_mvp(tuple(e[:3]), tuple(e[3:]))
+        maps.append(raster_ref.shadow_map(points, indices, mvp, S, S, bias_mode, cbias, factor, units))
+        biased.append([f32(v) for v in np.asarray(b, np.float32).reshape(16)])
+        eyes.append(e)
+        level.append(f32(0.0))
+        grid[(x, y)] = len(maps) - 1
+        return grid[(x, y)]
+
+    def needs_subdivision(idx):
+        count = np.full(W * H, f32(0.63), np.float32)
+        for p in fg:
+            v = [f32(c) for c in pos[p]]
+            s = f32(0.0)
+            for k in range(4):
+                c = mat4_mul(biased[idx[k]], v)
+                lit = c[2] / c[3] <= fetch(maps[idx[k]], S, S, c[0] / c[3], c[1] / c[3])
+                s = s + (f32(1.0) if lit else f32(0.0))
+            count[p] = s
+        div = 4 if lower_accuracy else 1
+        Wq, Hq = W // div, H // div
+
+        def coarse(i, j):
+            if not (0 <= i < Wq and 0 <= j < Hq):
+                return f32(0.0)
+            return count[((2 * j + 1) * H // (2 * Hq)) * W + (2 * i + 1) * W // (2 * Wq)]
+
+        for y in range(Hq):
+            for x in range(Wq):
+                s = coarse(x, y)
+                if s in (f32(0.63), f32(0.0), f32(4.0), f32(5.0)):
+                    continue
+                if all(coarse(x + dx, y + dy) == s for dy in (-1, 0, 1) for dx in (-1, 0, 1)):
+                    return True
+        return False
+
+    def evaluate(nd, node):
+        if nd["level"] == max_level:
+            return
+        kids = children(nd["level"], node)
+        idx = [sample(nd, k, *corner(nd["level"], node, k)) for k in range(4)]
+        if not needs_subdivision(idx):
+            return
+        nd["kids"] = [{"level": nd["level"] + 1, "eye": offset(nd["eye"], nd["level"] + 2, c),
+                       "at": offset(nd["at"], nd["level"] + 2, c), "kids": None} for c in range(4)]
+        for c in range(4):
+            evaluate(nd["kids"][c], kids[c])
+
+    def render(nd, node):
+        if nd["kids"] is not None:
+            for c, k in enumerate(children(nd["level"], node)):
+                render(nd["kids"][c], k)
+            return
+        for k in range(4):
+            level[sample(nd, k, *corner(nd["level"], node, k))] = f32(nd["level"])
+
+    root = {"level": 0, "eye": [f32(v) for v in light_eye], "at": [f32(v) for v in light_at], "kids": None}
+    evaluate(root, 0)
+    render(root, 0)
+    m = biased[-1]
+    acc = np.zeros(W * H, np.float32)
+    count = f32(0.0)
+    offs = []
+    if lower_accuracy:
+        o, st = f32(1.0), (f32(2.0) * f32(1.0)) / f32(3.0)
+        w = -o
+        while w <= o:
+            offs.append(w)
+            w = w + st
+    incr = f32(1.0) / f32(S)
+    for i in range(len(maps)):
+        b = biased[i]
+        w_enc = b[15] + level[i] * f32(10000.0)
+        ql = min(int(w_enc / f32(10000.0)), 4)
+        wv = w_enc - f32(ql * 10000)
+        f = f32(1.0)
+        for _ in range(ql):
+            f = f * f32(2.0)
+        f = f + f32(1.0)
+        wt = f32(1.0) / (f * f)
+        for p in fg:
+            v = [f32(c) for c in pos[p]]
+            c = [(m[r] * v[0] + m[4 + r] * v[1]) + m[8 + r] * v[2] for r in range(4)]
+            sx, sy, sz, sw = c[0] + b[12], c[1] + b[13], c[2] + b[14], c[3] + wv
+            if not lower_accuracy:
+                d = fetch(maps[i], S, S, sx / sw, sy / sw)
+                acc[p] = acc[p] + (f32(1.0) if sz / sw <= d else I) * wt
+            else:
+                ux, uy, uz = sx / sw, sy / sw, sz / sw
+                illum = f32(0.0)
+                for ow in offs:
+                    for oh in offs:
+                        illum = illum + (f32(1.0) if uz <= fetch(maps[i], S, S, ux + ow * incr, uy + oh * incr) else I)
+                acc[p] = acc[p] + (illum / f32(len(offs) * len(offs))) * wt
+        count = count + wt
+    out = np.zeros(W * H, np.float32)
+    out[fg] = acc[fg] / count
+    return out, np.array(eyes, np.float32), np.array(level, np.float32)

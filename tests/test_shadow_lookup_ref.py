@@ -205,3 +205,40 @@ def test_oracle_smsr_equals_the_second_restatement(world, name, tech, fields):
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), \
         f"{name}: {int((got != want).sum())} of {len(pos)} pixels differ"
     assert sm.discontinuities >= 10, "too few probes on a shadow edge"
+
+
+@pytest.mark.parametrize("lower_accuracy", [False, True], ids=["full", "lower accuracy"])
+def test_oracle_adaptive_area_light_equals_the_second_restatement(lower_accuracy):
+    """The adaptive (quad-tree) area-light ground truth: the same samples in
+    the same order, the same levels and the same image, every map and the
+    G-buffer drawn by the brute-force rasteriser.  The full-accuracy case
+    refines to level 3 in several quadrants; the lower-accuracy evaluation
+    looks at a quarter-size viewport, so it gets a larger window."""
+    import dataclasses
+
+    Wc, Hc, Sm, size, depth = (96, 56, 64, 6.0, 2) if lower_accuracy else (64, 40, 64, 8.0, 3)
+    w = scenes.pcss_1080p(width=Wc, height=Hc, map_size=Sm, spheres=1)
+    w.scene.close()
+    s = gi.Scene()
+    s.ground(10.0, 0.0)
+    s.icosphere_field(8, 2, (-8.0, 0.2, -8.0), (8.0, 3.0, 8.0), 0.2, 1.0, 0x5EED0001)
+    p, n, i = s.arrays()
+    s.close()
+    mp = w.map_params
+    cam = gi.frame_setup(w.light, w.camera).camera_mvp
+
+    def view_mvp(eye, at):
+        v = dataclasses.replace(w.light, eye=tuple(eye), at=tuple(at))
+        f = gi.frame_setup(v, v)
+        return f.light_mvp, f.light_mvp_biased
+
+    args = (p, n, i, w.light.eye, w.light.at, size, depth, view_mvp, Sm, mp.bias_mode, mp.constant_bias,
+            mp.offset_factor, mp.offset_units, cam, 0.25, Wc, Hc)
+    vis, eyes, levels = oracle.area_light_adaptive(*args, lower_accuracy=lower_accuracy)
+    r_vis, r_eyes, r_levels = ref.area_light_adaptive(*args, lower_accuracy=lower_accuracy)
+    assert np.array_equal(eyes.view(np.uint32), r_eyes.view(np.uint32))
+    assert np.array_equal(levels, r_levels)
+    assert np.array_equal(vis.view(np.uint32), r_vis.view(np.uint32)), f"{int((vis != r_vis).sum())} pixels differ"
+    assert len(levels) > 4, "the light was refined at least once"
+    if not lower_accuracy:
+        assert levels.max() == 3.0 and len(levels) > 40
