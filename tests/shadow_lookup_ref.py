@@ -30,7 +30,8 @@ CPU tests can hold the oracle to it bit for bit:
 * the uniform area-light ground truth (AccurateSoftShadow.frag:52-133) and
   the adaptive quad-tree one (SoftShadowMapping/src/main.cpp:423-690,
   Shaders/QuadTree/{Reprojection,Evaluation}.frag, QuadTreeLightSource.cpp),
-  their maps and G-buffer drawn by raster_ref's brute-force rasteriser.
+  their maps and G-buffer drawn by raster_ref's brute-force rasteriser;
+* EDTSM's screen-space mean filter (Shaders/Filter/MeanFilter.frag).
 """
 from __future__ import annotations
 
@@ -446,3 +447,62 @@ def area_light_adaptive(points, normals, indices, light_eye, light_at, size, max
     out = np.zeros(W * H, np.float32)
     out[fg] = acc[fg] / count
     return out, np.array(eyes, np.float32), np.array(level, np.float32)
+
+
+def edt_mean_filter(p, image, pos, W, H, order=7):
+    """filterHardShadowsUsingEDT's two MeanFilter.frag passes
+    (ShadowMapping/src/main.cpp:424-447; Shaders/Filter/MeanFilter.frag) with
+    the library's sampling choices: the centre of pixel i at (i + 0.5) /
+    size; the x pass NEAREST (texel floor(u size)), the y pass bilinear along
+    y at level 0; a zero border; at most 2049 samples; dscreen = 1 / (2
+    tan(45 / 2)) with the 45-degree fov uniform taken as radians, tan in
+    double.  image, pos: float32 [H, W, 4]; returns float32 [H, W, 4]."""
+    import math
+
+    dscreen = f32(1.0) / (f32(2.0) * f32(math.tan(float(f32(45.0) / f32(2.0)))))
+    m = p["camera_mv"]
+    thr = f32(0.0005)
+
+    def lin(d):
+        return f32(2.0) / (f32(1001.0) - d * f32(999.0))
+
+    src = image.astype(np.float32)
+    for vertical in (False, True):
+        dst = np.zeros((H, W, 4), np.float32)
+        size = f32(H if vertical else W)
+        step = f32(1.0) / size
+        for y in range(H):
+            for x in range(W):
+                v = pos[y, x]
+                if v[0] == 0:
+                    dst[y, x] = (0.0, 0.0, 0.0, 1.0)
+                    continue
+                color = src[y, x]
+                ez = ((m[2] * v[0] + m[6] * v[1]) + m[10] * v[2]) + m[14] * v[3]
+                kc = ((dscreen * f32(order)) * f32(50.0)) / (-ez * f32(2.0))
+                cs = (f32(y if vertical else x) + f32(0.5)) / size
+                Lc = lin(color[1])
+                total, count = f32(0.0), 0
+                s = -kc
+                while s <= kc and count < 2049:
+                    u = cs + s * step
+                    if not vertical:
+                        fi = np.floor(u * size)
+                        r, g = (src[y, int(fi), 0], src[y, int(fi), 1]) if 0 <= fi < size else (f32(0.0), f32(0.0))
+                    else:
+                        uu = u * size - f32(0.5)
+                        f0 = np.floor(uu)
+                        w1 = uu - f0
+                        w0 = f32(1.0) - w1
+                        j0 = int(f0)
+                        t0 = src[j0, x, :2] if 0 <= j0 < H else np.zeros(2, np.float32)
+                        t1 = src[j0 + 1, x, :2] if 0 <= j0 + 1 < H else np.zeros(2, np.float32)
+                        r, g = w0 * t0[0] + w1 * t1[0], w0 * t0[1] + w1 * t1[1]
+                    if r == 0 or abs(lin(g) - Lc) >= thr:
+                        r = color[0]
+                    total = total + r
+                    count += 1
+                    s = s + f32(1.0)
+                dst[y, x] = (total / f32(count), color[1], 0.0, 0.0)
+        src = dst
+    return src

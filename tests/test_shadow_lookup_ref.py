@@ -242,3 +242,29 @@ def test_oracle_adaptive_area_light_equals_the_second_restatement(lower_accuracy
     assert len(levels) > 4, "the light was refined at least once"
     if not lower_accuracy:
         assert levels.max() == 3.0 and len(levels) > 40
+
+
+def test_oracle_edt_mean_filter_equals_the_second_restatement():
+    """EDTSM's screen-space mean filter on a rendered G-buffer, with shadow
+    values of every kind and the pixels' own window depths in channel 1."""
+    Wc, Hc = 64, 40
+    w = scenes.pcss_1080p(width=Wc, height=Hc, map_size=64, spheres=6)
+    fr = gi.frame_setup(w.light, w.camera)
+    p, n, i = w.scene.arrays()
+    w.scene.close()
+    pos, _ = oracle.gbuffer(p, n, i, fr.camera_mvp, Wc, Hc)
+    pos = pos.reshape(Hc, Wc, 4)
+    rng = np.random.default_rng(11)
+    img = np.zeros((Hc, Wc, 4), np.float32)
+    img[..., 0] = rng.choice(np.array([0.25, 1.0, 1.0, 0.6], np.float32), (Hc, Wc))
+    m = fr.camera_mvp.reshape(4, 4).T  # column-major -> rows
+    clip = pos.reshape(-1, 4) @ m.T.astype(np.float64)
+    img[..., 1] = (clip[:, 2] / clip[:, 3] * 0.5 + 0.5).reshape(Hc, Wc).astype(np.float32)
+    img[pos[..., 0] == 0] = (0.0, 0.0, 0.0, 1.0)
+    prm = gi.ShadowParams.defaults(api.GI_TECH_SMSR_NONCONSERVATIVE)
+    c = prm.to_c(fr)
+    got = oracle.edt_mean_filter(c, img, pos, Wc, Hc)
+    want = ref.edt_mean_filter(ref.params_of(c), img, pos, Wc, Hc)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), f"{int((got != want).sum())} values differ"
+    fg = pos[..., 0] != 0
+    assert ((got[..., 0] > 0.25) & (got[..., 0] < 1.0) & fg).any()
