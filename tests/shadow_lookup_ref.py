@@ -31,7 +31,8 @@ CPU tests can hold the oracle to it bit for bit:
   the adaptive quad-tree one (SoftShadowMapping/src/main.cpp:423-690,
   Shaders/QuadTree/{Reprojection,Evaluation}.frag, QuadTreeLightSource.cpp),
   their maps and G-buffer drawn by raster_ref's brute-force rasteriser;
-* EDTSM's screen-space mean filter (Shaders/Filter/MeanFilter.frag).
+* EDTSM's inputs written by the SMSR shaders and its screen-space mean
+  filter (Shaders/Filter/MeanFilter.frag).
 """
 from __future__ import annotations
 
@@ -506,3 +507,18 @@ def edt_mean_filter(p, image, pos, W, H, order=7):
                 dst[y, x] = (total / f32(count), color[1], 0.0, 0.0)
         src = dst
     return src
+
+
+def edt_inputs(p, camera_mvp, vertex, normal, shadow):
+    """The EDTSM outputs of NonConservativeSMSR.frag:367-397 (and
+    ConservativeSMSR.frag's) for one pixel: image (shadow, depth,
+    preEvaluatedShadow, 1) with depth = position.z / position.w * 0.5 + 0.5,
+    and position = MVP * vertex; background keeps (0, 0, 0, 1) in both."""
+    if vertex[0] == 0:
+        bg = [f32(0.0), f32(0.0), f32(0.0), f32(1.0)]
+        return bg, list(bg)
+    pre = pretest(p, vertex, normal)
+    cp = mat4_mul([f32(v) for v in np.asarray(camera_mvp, np.float32).reshape(16)], vertex)
+    depth = cp[2] / cp[3]
+    depth = depth * f32(0.5) + f32(0.5)
+    return [shadow, depth, pre, f32(1.0)], cp

@@ -268,3 +268,20 @@ def test_oracle_edt_mean_filter_equals_the_second_restatement():
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), f"{int((got != want).sum())} values differ"
     fg = pos[..., 0] != 0
     assert ((got[..., 0] > 0.25) & (got[..., 0] < 1.0) & fg).any()
+
+
+def test_oracle_edt_inputs_equal_the_second_restatement(world):
+    """The image and position targets the SMSR shaders write for EDTSM."""
+    fr, depth, _, _, pos, nrm = world
+    prm = gi.ShadowParams.defaults(api.GI_TECH_SMSR_NONCONSERVATIVE)
+    c = prm.to_c(fr)
+    rng = np.random.default_rng(5)
+    vis = rng.choice(np.array([0.25, 1.0, 0.0], np.float32), len(pos)).astype(np.float32)
+    image, position = oracle.edt_inputs(c, fr.camera_mvp, pos.reshape(-1), nrm.reshape(-1), vis, W, H)
+    rp = ref.params_of(c)
+    for k in range(len(pos)):
+        im, po = ref.edt_inputs(rp, fr.camera_mvp, [np.float32(x) for x in pos[k]], [np.float32(x) for x in nrm[k]],
+                                vis[k])
+        y, x = divmod(k, W)
+        assert np.array_equal(image[y, x].view(np.uint32), np.array(im, np.float32).view(np.uint32)), k
+        assert np.array_equal(position[y, x].view(np.uint32), np.array(po, np.float32).view(np.uint32)), k
