@@ -20,6 +20,12 @@
                           shim under oracle/_ref/shim/; built only where the
                           reference tree is present.
 
+  oracle/_ref/libshader_ref.so
+                          ref_shader_pin.cpp: the reference's own fragment
+                          shaders (PlausibleSoftShadow.frag, ...) included
+                          unmodified as C++ on top of glsl_shim.h; built only
+                          where the reference tree is present.
+
 Only the tests, the smoke check, the fixture generators and the CPU-baseline
 leg of bench.py use these files; the product library never links or loads
 them.
@@ -176,8 +182,36 @@ def build_scene_ref() -> list[str]:
     return built
 
 
+SHADER_PIN_LIB = os.path.join(REF_DIR, "libshader_ref.so")
+# The reference's fragment shaders compiled by oracle/ref_shader_pin.cpp.
+SHADER_PIN_SOURCES = {
+    "GI_SHADER_PCSS": os.path.join(REFERENCE_ROOT, "SoftShadowMapping", "Shaders", "SoftShadow",
+                                   "PlausibleSoftShadow.frag"),
+}
+
+
+def build_shader_ref() -> str | None:
+    """Builds oracle/_ref/libshader_ref.so when the reference's shaders are present:
+    ref_shader_pin.cpp includes each one unmodified on top of glsl_shim.h
+    (-fsingle-precision-constant so GLSL's float literals stay float)."""
+    shaders = list(SHADER_PIN_SOURCES.values())
+    if not all(os.path.exists(f) for f in shaders):
+        return None
+    pin = os.path.join(HERE, "ref_shader_pin.cpp")
+    deps = [pin, os.path.join(HERE, "glsl_shim.h"), *shaders, os.path.abspath(__file__)]
+    if _newer(SHADER_PIN_LIB, deps):
+        os.makedirs(REF_DIR, exist_ok=True)
+        tmp = SHADER_PIN_LIB + ".tmp"
+        defs = [f'-D{k}="{v}"' for k, v in SHADER_PIN_SOURCES.items()]
+        subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+                        "-fsingle-precision-constant", "-w", "-I", HERE, *defs, pin, "-o", tmp], check=True)
+        os.replace(tmp, SHADER_PIN_LIB)
+    return SHADER_PIN_LIB
+
+
 if __name__ == "__main__":
     print(build_oracle())
     print(build_ref())
     print(build_pba_ref())
     print(build_scene_ref())
+    print(build_shader_ref())
