@@ -187,6 +187,11 @@ SHADER_PIN_LIB = os.path.join(REF_DIR, "libshader_ref.so")
 SHADER_PIN_SOURCES = {
     "GI_SHADER_PCSS": os.path.join(REFERENCE_ROOT, "SoftShadowMapping", "Shaders", "SoftShadow",
                                    "PlausibleSoftShadow.frag"),
+    "GI_SHADER_SHADOW": os.path.join(REFERENCE_ROOT, "ShadowMapping", "Shaders", "Shadow.frag"),
+    "GI_SHADER_NCSMSR": os.path.join(REFERENCE_ROOT, "ShadowMapping", "Shaders", "RBSM", "NonConservativeSMSR.frag"),
+    "GI_SHADER_CSMSR": os.path.join(REFERENCE_ROOT, "ShadowMapping", "Shaders", "RBSM", "ConservativeSMSR.frag"),
+    "GI_SHADER_FRBSM": os.path.join(REFERENCE_ROOT, "ShadowMapping", "Shaders", "RBSM", "FilteredRBSM.frag"),
+    "GI_SHADER_RBSSM": os.path.join(REFERENCE_ROOT, "SoftShadowMapping", "Shaders", "SoftShadow", "RBSSM.frag"),
 }
 
 

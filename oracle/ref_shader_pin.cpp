@@ -31,6 +31,42 @@ GI_SHADER_GLOBALS
 #include GI_SHADER_PCSS
 }  // namespace pin_pcss
 
+namespace pin_shadow {
+GI_SHADER_GLOBALS
+#include GI_SHADER_SHADOW
+}  // namespace pin_shadow
+
+namespace pin_ncsmsr {
+GI_SHADER_GLOBALS
+#include GI_SHADER_NCSMSR
+}  // namespace pin_ncsmsr
+
+namespace pin_csmsr {
+GI_SHADER_GLOBALS
+#include GI_SHADER_CSMSR
+}  // namespace pin_csmsr
+
+namespace pin_frbsm {
+GI_SHADER_GLOBALS
+#include GI_SHADER_FRBSM
+}  // namespace pin_frbsm
+
+namespace pin_rbssm {
+GI_SHADER_GLOBALS
+// RBSSM.frag returns a float from a vec4 function and stores that vec4 in a
+// float, which the reference's GL driver accepts (a splat, then the first
+// component); in this namespace its vec4 does the same.
+struct lenient_vec4 : glsl::vec4 {
+    using glsl::vec4::vec4;
+    lenient_vec4(float f) : glsl::vec4(f) {}
+    lenient_vec4(const glsl::vec4& v) : glsl::vec4(v) {}
+    operator float() const { return x; }
+};
+#define vec4 lenient_vec4
+#include GI_SHADER_RBSSM
+#undef vec4
+}  // namespace pin_rbssm
+
 namespace {
 
 glsl::mat4 mat4_of(const float* m) {
@@ -101,6 +137,133 @@ void ref_pcss(const float* depth, int S, const float* pos, const float* nrm, int
     lightSourceRadius = light_source_radius;
     PCSS = 1;
     SAVSM = VSSM = ESSM = MSSM = SAT = 0;
+    per_pixel(f, out, [](const glsl::vec2& tc) {
+        f_texcoord = tc;
+        gl_discarded = false;
+        gl_FragColor = glsl::vec4(0.0f);
+        shader_main();
+        return gl_discarded ? 0.0f : gl_FragColor.x;
+    });
+}
+
+// ShadowMapping/Shaders/Shadow.frag (computeHardShadows, ShadowMapping/src/
+// main.cpp:400-414): mode 0 the naive hard test, 1 bilinear PCF, 2 tricubic
+// PCF.
+void ref_shadow(int mode, const float* depth, int S, const float* pos, const float* nrm, int W, int H,
+                const float* light_mvp, const float* camera_mv, const float* normal_matrix,
+                const float* light_position, float intensity, int kernel_order, int penumbra_size, float* out) {
+    using namespace pin_shadow;
+    const Frame f{depth, S, pos, nrm, W, H, light_mvp, camera_mv, normal_matrix, light_position, intensity};
+    shadowMap = glsl::sampler2D{depth, S, S, 1};
+    vertexMap = glsl::sampler2D{pos, W, H, 4};
+    normalMap = glsl::sampler2D{nrm, W, H, 4};
+    lightMVP = mat4_of(light_mvp);
+    MV = mat4_of(camera_mv);
+    normalMatrix = mat3_of(normal_matrix);
+    lightPosition = glsl::vec3(light_position[0], light_position[1], light_position[2]);
+    shadowIntensity = intensity;
+    shadowMapWidth = S;
+    shadowMapHeight = S;
+    kernelOrder = kernel_order;
+    penumbraSize = penumbra_size;
+    zNear = 1;
+    zFar = 1000;
+    naive = mode == 0;
+    bilinearPCF = mode == 1;
+    tricubicPCF = mode == 2;
+    VSM = ESM = EVSM = MSM = 0;
+    per_pixel(f, out, [](const glsl::vec2& tc) {
+        f_texcoord = tc;
+        gl_discarded = false;
+        gl_FragColor = glsl::vec4(0.0f);
+        shader_main();
+        return gl_discarded ? 0.0f : gl_FragColor.x;
+    });
+}
+
+// The RBSM shaders (computeHardShadows with the RBSM techniques): shader 0
+// NonConservativeSMSR.frag, 1 ConservativeSMSR.frag, 2 FilteredRBSM.frag;
+// mode 0 SMSR, 1 RPCF (+ SMSR), 2 EDTSM.  out4 receives gl_FragData[0] and,
+// when given, out_pos4 gl_FragData[1]; a discarded pixel keeps the clear
+// colour (0, 0, 0, 1).
+#define GI_RBSM_RUN(NS)                                                                              \
+    do {                                                                                             \
+        using namespace NS;                                                                          \
+        shadowMap = glsl::sampler2D{depth, S, S, 1};                                                 \
+        vertexMap = glsl::sampler2D{pos, W, H, 4};                                                   \
+        normalMap = glsl::sampler2D{nrm, W, H, 4};                                                   \
+        lightMVP = mat4_of(light_mvp);                                                               \
+        MV = mat4_of(camera_mv);                                                                     \
+        MVP = mat4_of(camera_mvp);                                                                   \
+        normalMatrix = mat3_of(normal_matrix);                                                       \
+        lightPosition = glsl::vec3(light_position[0], light_position[1], light_position[2]);         \
+        shadowMapStep = glsl::vec2((float)(1.0 / S), (float)(1.0 / S));                              \
+        shadowIntensity = intensity;                                                                 \
+        depthThreshold = depth_threshold;                                                            \
+        shadowMapWidth = S;                                                                          \
+        shadowMapHeight = S;                                                                         \
+        maxSearch = max_search;                                                                      \
+        kernelOrder = kernel_order;                                                                  \
+        penumbraSize = penumbra_size;                                                                \
+        SMSR = mode == 0;                                                                            \
+        RPCFPlusSMSR = mode == 1;                                                                    \
+        EDTSM = mode == 2;                                                                           \
+        for (int y = 0; y < H; ++y)                                                                  \
+            for (int x = 0; x < W; ++x) {                                                            \
+                const size_t q = (size_t)y * W + x;                                                  \
+                f_texcoord = glsl::vec2(((float)x + 0.5f) / (float)W, ((float)y + 0.5f) / (float)H); \
+                gl_discarded = false;                                                                \
+                gl_FragData[0] = glsl::vec4(0.0f, 0.0f, 0.0f, 1.0f);                                 \
+                gl_FragData[1] = glsl::vec4(0.0f, 0.0f, 0.0f, 1.0f);                                 \
+                shader_main();                                                                       \
+                if (gl_discarded) {                                                                  \
+                    gl_FragData[0] = glsl::vec4(0.0f, 0.0f, 0.0f, 1.0f);                             \
+                    gl_FragData[1] = glsl::vec4(0.0f, 0.0f, 0.0f, 1.0f);                             \
+                }                                                                                    \
+                for (int k = 0; k < 4; ++k) {                                                        \
+                    out4[4 * q + k] = gl_FragData[0].e[k];                                           \
+                    if (out_pos4) out_pos4[4 * q + k] = gl_FragData[1].e[k];                         \
+                }                                                                                    \
+            }                                                                                        \
+    } while (0)
+
+void ref_rbsm(int shader, int mode, const float* depth, int S, const float* pos, const float* nrm, int W, int H,
+              const float* light_mvp, const float* camera_mv, const float* camera_mvp, const float* normal_matrix,
+              const float* light_position, float intensity, float depth_threshold, int max_search, int kernel_order,
+              int penumbra_size, float* out4, float* out_pos4) {
+    if (shader == 0) GI_RBSM_RUN(pin_ncsmsr);
+    else if (shader == 1) GI_RBSM_RUN(pin_csmsr);
+    else GI_RBSM_RUN(pin_frbsm);
+}
+
+// SoftShadowMapping/Shaders/SoftShadow/RBSSM.frag (renderSoftShadows with
+// RBSSM).
+void ref_rbssm(const float* depth, int S, const float* pos, const float* nrm, int W, int H, const float* light_mvp,
+               const float* camera_mv, const float* normal_matrix, const float* light_position, float intensity,
+               float depth_threshold, int max_search, int blocker_search_size, int kernel_size,
+               int light_source_radius, int z_near, int z_far, float* out) {
+    using namespace pin_rbssm;
+    const Frame f{depth, S, pos, nrm, W, H, light_mvp, camera_mv, normal_matrix, light_position, intensity};
+    shadowMap = glsl::sampler2D{depth, S, S, 1};
+    hierarchicalShadowMap = shadowMap;
+    vertexMap = glsl::sampler2D{pos, W, H, 4};
+    normalMap = glsl::sampler2D{nrm, W, H, 4};
+    lightMVP = mat4_of(light_mvp);
+    MV = mat4_of(camera_mv);
+    normalMatrix = mat3_of(normal_matrix);
+    lightPosition = glsl::vec3(light_position[0], light_position[1], light_position[2]);
+    shadowMapStep = glsl::vec2((float)(1.0 / S), (float)(1.0 / S));
+    shadowIntensity = intensity;
+    depthThreshold = depth_threshold;
+    zNear = z_near;
+    zFar = z_far;
+    shadowMapWidth = S;
+    shadowMapHeight = S;
+    maxSearch = max_search;
+    blockerSearchSize = blocker_search_size;
+    kernelSize = kernel_size;
+    lightSourceRadius = light_source_radius;
+    useTextureForColoring = useMeshColor = 0;
     per_pixel(f, out, [](const glsl::vec2& tc) {
         f_texcoord = tc;
         gl_discarded = false;

@@ -70,3 +70,96 @@ def test_pcss_equals_the_reference_shader(lib, frame, blocker, kernel, radius):
     assert not diff.any(), f"{int(diff.sum())} of {W * H} pixels differ"
     fg = want[pos.reshape(-1, 4)[:, 0] != 0]
     assert ((fg > p.shadow_intensity) & (fg < 1.0)).sum() >= 10, "few penumbrae: the cut-off or the light placement"
+
+
+def _mats(fr):
+    return [np.ascontiguousarray(x, np.float32) for x in (fr.light_mvp_biased, fr.camera_mv, fr.normal_matrix,
+                                                          fr.light_position)]
+
+
+@pytest.fixture(scope="module")
+def lib_all(lib):
+    P, I, F = C.c_void_p, C.c_int, C.c_float
+    lib.ref_shadow.argtypes = [I, P, I, P, P, I, I, P, P, P, P, F, I, I, P]
+    lib.ref_rbsm.argtypes = [I, I, P, I, P, P, I, I, P, P, P, P, P, F, F, I, I, I, P, P]
+    lib.ref_rbssm.argtypes = [P, I, P, P, I, I, P, P, P, P, F, F, I, I, I, I, I, I, P]
+    for f in (lib.ref_shadow, lib.ref_rbsm, lib.ref_rbssm):
+        f.restype = None
+    return lib
+
+
+@pytest.mark.parametrize("tech,mode,kernel_order,penumbra", [
+    (api.GI_TECH_HARD, 0, 7, 1), (api.GI_TECH_PCF, 1, 7, 1), (api.GI_TECH_PCF, 1, 3, 2),
+    (api.GI_TECH_PCF_TRICUBIC, 2, 5, 1)], ids=["hard", "pcf 7/1", "pcf 3/2", "tricubic 5/1"])
+def test_hard_and_pcf_equal_the_reference_shader(lib_all, frame, tech, mode, kernel_order, penumbra):
+    """ShadowMapping's Shadow.frag: the naive hard test and PCF's float loop,
+    bilinear and tricubic (textureBicubic), pre-test included."""
+    fr, depth, pos, nrm = frame
+    p = gi.ShadowParams.defaults(tech)
+    p.kernel_order, p.penumbra_size = kernel_order, penumbra
+    got = oracle.visibility(p.to_c(fr), depth, S, S, pos, nrm, W, H)
+    want = np.empty(W * H, np.float32)
+    lib_all.ref_shadow(mode, _ptr(depth), S, _ptr(pos), _ptr(nrm), W, H, *(_ptr(x) for x in _mats(fr)),
+                       p.shadow_intensity, kernel_order, penumbra, _ptr(want))
+    diff = got.view(np.uint32) != want.view(np.uint32)
+    assert not diff.any(), f"{int(diff.sum())} of {W * H} pixels differ"
+
+
+RBSM = [  # technique, shader (0 non-conservative, 1 conservative, 2 filtered), mode (0 SMSR, 1 RPCF)
+    (api.GI_TECH_SMSR_NONCONSERVATIVE, 0, 0), (api.GI_TECH_RPCF_SMSR, 0, 1), (api.GI_TECH_RSMSS, 2, 1),
+    (api.GI_TECH_SMSR_CONSERVATIVE, 1, 0), (api.GI_TECH_RPCF_CONSERVATIVE, 1, 1)]
+
+
+@pytest.mark.parametrize("tech,shader,mode", RBSM,
+                         ids=["smsr", "rpcf+smsr", "rsmss", "conservative smsr", "conservative rpcf"])
+@pytest.mark.parametrize("threshold", [0.0, 1e-2])
+def test_rbsm_equals_the_reference_shaders(lib_all, frame, tech, shader, mode, threshold):
+    """NonConservativeSMSR.frag, ConservativeSMSR.frag and FilteredRBSM.frag."""
+    fr, depth, pos, nrm = frame
+    p = gi.ShadowParams.defaults(tech)
+    p.max_search, p.depth_threshold, p.kernel_order, p.penumbra_size = 16, threshold, 3, 1
+    got = oracle.visibility(p.to_c(fr), depth, S, S, pos, nrm, W, H)
+    out4 = np.empty(W * H * 4, np.float32)
+    cmvp = np.ascontiguousarray(fr.camera_mvp, np.float32)
+    lf, mv, nm, lp = _mats(fr)
+    lib_all.ref_rbsm(shader, mode, _ptr(depth), S, _ptr(pos), _ptr(nrm), W, H, _ptr(lf), _ptr(mv), _ptr(cmvp),
+                     _ptr(nm), _ptr(lp), p.shadow_intensity, threshold, 16, 3, 1, _ptr(out4), None)
+    want = out4.reshape(-1, 4)[:, 0].copy()
+    want[pos.reshape(-1, 4)[:, 0] == 0] = 0.0  # background: the visibility target's clear value
+    diff = got.view(np.uint32) != want.view(np.uint32)
+    assert not diff.any(), f"{int(diff.sum())} of {W * H} pixels differ"
+
+
+def test_edtsm_inputs_equal_the_reference_shader(lib_all, frame):
+    """The EDTSM outputs of NonConservativeSMSR.frag: (shadow, depth,
+    pre-test, 1) and the clip position."""
+    fr, depth, pos, nrm = frame
+    p = gi.ShadowParams.defaults(api.GI_TECH_SMSR_NONCONSERVATIVE)
+    c = p.to_c(fr)
+    vis = oracle.visibility(c, depth, S, S, pos, nrm, W, H)
+    image, position = oracle.edt_inputs(c, fr.camera_mvp, pos, nrm, vis, W, H)
+    out4, pos4 = np.empty(W * H * 4, np.float32), np.empty(W * H * 4, np.float32)
+    cmvp = np.ascontiguousarray(fr.camera_mvp, np.float32)
+    lf, mv, nm, lp = _mats(fr)
+    lib_all.ref_rbsm(0, 2, _ptr(depth), S, _ptr(pos), _ptr(nrm), W, H, _ptr(lf), _ptr(mv), _ptr(cmvp), _ptr(nm),
+                     _ptr(lp), p.shadow_intensity, p.depth_threshold, p.max_search, p.kernel_order, p.penumbra_size,
+                     _ptr(out4), _ptr(pos4))
+    assert np.array_equal(image.reshape(-1).view(np.uint32), out4.view(np.uint32))
+    assert np.array_equal(position.reshape(-1).view(np.uint32), pos4.view(np.uint32))
+
+
+@pytest.mark.parametrize("blocker,kernel,radius,threshold", [(7, 15, 4, 0.0), (5, 9, 12, 0.0), (3, 5, 20, 1e-2)])
+def test_rbssm_equals_the_reference_shader(lib_all, frame, blocker, kernel, radius, threshold):
+    """SoftShadowMapping's RBSSM.frag (1,378 lines) whole."""
+    fr, depth, pos, nrm = frame
+    p = gi.ShadowParams.defaults(api.GI_TECH_RBSSM)
+    p.blocker_search_size, p.kernel_size, p.light_radius = blocker, kernel, float(radius)
+    p.pcss_min_blocker_depth, p.znear, p.depth_threshold = 0.99, 1.0, threshold
+    got = oracle.visibility(p.to_c(fr), depth, S, S, pos, nrm, W, H)
+    want = np.empty(W * H, np.float32)
+    lib_all.ref_rbssm(_ptr(depth), S, _ptr(pos), _ptr(nrm), W, H, *(_ptr(x) for x in _mats(fr)), p.shadow_intensity,
+                      threshold, p.max_search, blocker, kernel, radius, 1, 1000, _ptr(want))
+    diff = got.view(np.uint32) != want.view(np.uint32)
+    assert not diff.any(), f"{int(diff.sum())} of {W * H} pixels differ"
+    fg = want[pos.reshape(-1, 4)[:, 0] != 0]
+    assert ((fg > p.shadow_intensity) & (fg < 1.0)).sum() >= 10
