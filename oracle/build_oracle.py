@@ -192,6 +192,7 @@ SHADER_PIN_SOURCES = {
     "GI_SHADER_CSMSR": os.path.join(REFERENCE_ROOT, "ShadowMapping", "Shaders", "RBSM", "ConservativeSMSR.frag"),
     "GI_SHADER_FRBSM": os.path.join(REFERENCE_ROOT, "ShadowMapping", "Shaders", "RBSM", "FilteredRBSM.frag"),
     "GI_SHADER_RBSSM": os.path.join(REFERENCE_ROOT, "SoftShadowMapping", "Shaders", "SoftShadow", "RBSSM.frag"),
+    "GI_SHADER_PHONG": os.path.join(REFERENCE_ROOT, "ShadowMapping", "Shaders", "GBuffer", "PhongShading.frag"),
 }
 
 

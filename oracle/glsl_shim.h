@@ -11,7 +11,7 @@
 // to right; normalize(v) = v * (1 / sqrt(dot(v, v))); mix(x, y, a) =
 // x (1 - a) + y a; max(x, y) = x < y ? y : x; min(x, y) = y < x ? y : x;
 // clamp(x, a, b) = min(max(x, a), b); step(e, x) = x < e ? 0 : 1; fract(x) =
-// x - floor(x); mod(x, y) = x - y floor(x / y); texture lookups NEAREST at
+// x - floor(x); mod(x, y) = x - y floor(x / y); pow(x, 3) = x x x; texture lookups NEAREST at
 // level 0 (texel floor(u * size)) with a zero border, a one-channel (depth)
 // texture reading as (d, d, d, 1).
 #pragma once
@@ -285,7 +285,8 @@ inline float clamp(float x, float lo, float hi) { return min(max(x, lo), hi); }
 inline float mix(float x, float y, float a) { return x * (1.0f - a) + y * a; }
 inline float step(float edge, float x) { return x < edge ? 0.0f : 1.0f; }
 inline float mod(float x, float y) { return x - y * std::floor(x / y); }
-inline float pow(float x, float y) { return std::pow(x, y); }
+// pow(x, 3) as x * x * x (PhongShading.frag's 0.3 * shininess), else the C library's
+inline float pow(float x, float y) { return y == 3.0f ? (x * x) * x : std::pow(x, y); }
 
 #define GLSL_VEC_FUNCS(V, N)                                                               \
     inline V abs(const V& a) {                                                             \

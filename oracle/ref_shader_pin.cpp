@@ -51,6 +51,11 @@ GI_SHADER_GLOBALS
 #include GI_SHADER_FRBSM
 }  // namespace pin_frbsm
 
+namespace pin_phong {
+GI_SHADER_GLOBALS
+#include GI_SHADER_PHONG
+}  // namespace pin_phong
+
 namespace pin_rbssm {
 GI_SHADER_GLOBALS
 // RBSSM.frag returns a float from a vec4 function and stores that vec4 in a
@@ -271,6 +276,33 @@ void ref_rbssm(const float* depth, int S, const float* pos, const float* nrm, in
         shader_main();
         return gl_discarded ? 0.0f : gl_FragColor.x;
     });
+}
+
+// ShadowMapping/Shaders/GBuffer/PhongShading.frag (shadeScene): RGBA per
+// pixel; a discarded (background) pixel keeps the shading target's clear
+// colour (0.63, 0.82, 0.96, 1).
+void ref_phong(const float* pos, const float* nrm, const float* vis, const float* color, int W, int H,
+               const float* camera_mv, const float* normal_matrix, const float* light_position, float intensity,
+               float* out4) {
+    using namespace pin_phong;
+    hardShadowMap = glsl::sampler2D{vis, W, H, 1};
+    colorMap = glsl::sampler2D{color, W, H, 4};
+    vertexMap = glsl::sampler2D{pos, W, H, 4};
+    normalMap = glsl::sampler2D{nrm, W, H, 4};
+    MV = mat4_of(camera_mv);
+    normalMatrix = mat3_of(normal_matrix);
+    lightPosition = glsl::vec3(light_position[0], light_position[1], light_position[2]);
+    shadowIntensity = intensity;
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const size_t q = (size_t)y * W + x;
+            f_texcoord = glsl::vec2(((float)x + 0.5f) / (float)W, ((float)y + 0.5f) / (float)H);
+            gl_discarded = false;
+            gl_FragColor = glsl::vec4(0.0f);
+            shader_main();
+            const glsl::vec4 c = gl_discarded ? glsl::vec4(0.63f, 0.82f, 0.96f, 1.0f) : gl_FragColor;
+            for (int k = 0; k < 4; ++k) out4[4 * q + k] = c.e[k];
+        }
 }
 
 }  // extern "C"

@@ -163,3 +163,23 @@ def test_rbssm_equals_the_reference_shader(lib_all, frame, blocker, kernel, radi
     assert not diff.any(), f"{int(diff.sum())} of {W * H} pixels differ"
     fg = want[pos.reshape(-1, 4)[:, 0] != 0]
     assert ((fg > p.shadow_intensity) & (fg < 1.0)).sum() >= 10
+
+
+def test_phong_equals_the_reference_shader(lib_all, frame):
+    """ShadowMapping's PhongShading.frag (shadeScene) over the G-buffer, with
+    visibility values of every kind and per-pixel colours."""
+    fr, depth, pos, nrm = frame
+    lib_all.ref_phong.argtypes = [C.c_void_p] * 4 + [C.c_int, C.c_int] + [C.c_void_p] * 3 + [C.c_float, C.c_void_p]
+    lib_all.ref_phong.restype = None
+    p = gi.ShadowParams.defaults(api.GI_TECH_HARD)
+    c = p.to_c(fr)
+    rng = np.random.default_rng(3)
+    vis = rng.choice(np.array([0.0, 0.25, 1.0, 0.55], np.float32), W * H).astype(np.float32)
+    color = rng.random(W * H * 4, dtype=np.float32)
+    got = oracle.phong_shade(c, pos, nrm, vis, W, H, color)
+    want = np.empty(W * H * 4, np.float32)
+    _, mv, nm, lp = _mats(fr)
+    lib_all.ref_phong(_ptr(pos), _ptr(nrm), _ptr(vis), _ptr(color), W, H, _ptr(mv), _ptr(nm), _ptr(lp),
+                      p.shadow_intensity, _ptr(want))
+    diff = got.view(np.uint32) != want.view(np.uint32)
+    assert not diff.any(), f"{int(diff.sum())} of {W * H * 4} values differ"
