@@ -13,7 +13,8 @@
 // clamp(x, a, b) = min(max(x, a), b); step(e, x) = x < e ? 0 : 1; fract(x) =
 // x - floor(x); mod(x, y) = x - y floor(x / y); pow(x, 3) = x x x; texture lookups NEAREST at
 // level 0 (texel floor(u * size)) with a zero border, a one-channel (depth)
-// texture reading as (d, d, d, 1).
+// texture reading as (d, d, d, 1); the moment maps bilinear at level 0 with
+// float32 weights and a zero border.
 #pragma once
 
 #include <cmath>
@@ -344,9 +345,30 @@ inline vec3 reflect(const vec3& i, const vec3& n) { return i - (2.0f * dot(n, i)
 struct sampler2D {
     const float* data = nullptr;
     int w = 0, h = 0, channels = 1;
+    bool linear = false;  // bilinear at level 0 (the moment maps), else NEAREST
 };
 
+inline vec4 texel(const sampler2D& s, int i, int j) {
+    if (i < 0 || i >= s.w || j < 0 || j >= s.h) return vec4(0.0f);
+    const float* t = s.data + ((size_t)j * s.w + i) * s.channels;
+    if (s.channels == 1) return vec4(t[0], t[0], t[0], 1.0f);
+    return vec4(t[0], t[1], t[2], t[3]);
+}
+
 inline vec4 texture2D(const sampler2D& s, const vec2& uv) {
+    if (s.linear) {  // float32 weights, zero border
+        const float u = uv.e[0] * (float)s.w - 0.5f, v = uv.e[1] * (float)s.h - 0.5f;
+        if (!(u > -2.0f && u < (float)s.w + 1.0f && v > -2.0f && v < (float)s.h + 1.0f)) return vec4(0.0f);
+        const float fu = std::floor(u), fv = std::floor(v);
+        const int i0 = (int)fu, j0 = (int)fv;
+        const float a = u - fu, b = v - fv;
+        const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+        const vec4 t0 = texel(s, i0, j0), t1 = texel(s, i0 + 1, j0), t2 = texel(s, i0, j0 + 1),
+                   t3 = texel(s, i0 + 1, j0 + 1);
+        vec4 r;
+        for (int k = 0; k < 4; ++k) r.e[k] = ((w00 * t0.e[k] + w10 * t1.e[k]) + w01 * t2.e[k]) + w11 * t3.e[k];
+        return r;
+    }
     const float fi = std::floor(uv.e[0] * (float)s.w), fj = std::floor(uv.e[1] * (float)s.h);
     if (!(fi >= 0.0f && fi < (float)s.w && fj >= 0.0f && fj < (float)s.h)) return vec4(0.0f);
     const float* t = s.data + ((size_t)(int)fj * s.w + (int)fi) * s.channels;

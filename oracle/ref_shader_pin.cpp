@@ -186,6 +186,43 @@ void ref_shadow(int mode, const float* depth, int S, const float* pos, const flo
     });
 }
 
+// Shadow.frag's moment lookups (VSM, ESM, EVSM, MSM: mode 3..6) over the
+// blurred window-size moment target `moments` (float4, side M, read
+// bilinearly), with MSM's quantisation uniforms.
+void ref_shadow_moments(int tech_mode, const float* moments, int M, const float* pos, const float* nrm, int W, int H,
+                        const float* light_mvp, const float* camera_mv, const float* normal_matrix,
+                        const float* light_position, float intensity, const float* mq_inverse, float tq0,
+                        float* out) {
+    using namespace pin_shadow;
+    const Frame f{moments, M, pos, nrm, W, H, light_mvp, camera_mv, normal_matrix, light_position, intensity};
+    shadowMap = glsl::sampler2D{moments, M, M, 4, true};
+    vertexMap = glsl::sampler2D{pos, W, H, 4};
+    normalMap = glsl::sampler2D{nrm, W, H, 4};
+    lightMVP = mat4_of(light_mvp);
+    MV = mat4_of(camera_mv);
+    normalMatrix = mat3_of(normal_matrix);
+    lightPosition = glsl::vec3(light_position[0], light_position[1], light_position[2]);
+    mQuantizationInverse = mat4_of(mq_inverse);
+    tQuantization = glsl::vec4(tq0, 0.0f, 0.0f, 0.0f);
+    shadowIntensity = intensity;
+    shadowMapWidth = M;
+    shadowMapHeight = M;
+    zNear = 1;
+    zFar = 1000;
+    naive = bilinearPCF = tricubicPCF = 0;
+    VSM = tech_mode == 3;
+    ESM = tech_mode == 4;
+    EVSM = tech_mode == 5;
+    MSM = tech_mode == 6;
+    per_pixel(f, out, [](const glsl::vec2& tc) {
+        f_texcoord = tc;
+        gl_discarded = false;
+        gl_FragColor = glsl::vec4(0.0f);
+        shader_main();
+        return gl_discarded ? 0.0f : gl_FragColor.x;
+    });
+}
+
 // The RBSM shaders (computeHardShadows with the RBSM techniques): shader 0
 // NonConservativeSMSR.frag, 1 ConservativeSMSR.frag, 2 FilteredRBSM.frag;
 // mode 0 SMSR, 1 RPCF (+ SMSR), 2 EDTSM.  out4 receives gl_FragData[0] and,

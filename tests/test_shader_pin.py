@@ -183,3 +183,40 @@ def test_phong_equals_the_reference_shader(lib_all, frame):
                       p.shadow_intensity, _ptr(want))
     diff = got.view(np.uint32) != want.view(np.uint32)
     assert not diff.any(), f"{int(diff.sum())} of {W * H * 4} values differ"
+
+
+@pytest.mark.parametrize("tech,mode", [(api.GI_TECH_VSM, 3), (api.GI_TECH_ESM, 4), (api.GI_TECH_EVSM, 5),
+                                       (api.GI_TECH_MSM, 6)], ids=["VSM", "ESM", "EVSM", "MSM"])
+def test_moment_lookups_equal_the_reference_shader(lib_all, tech, mode):
+    """Shadow.frag's varianceShadowMapping, exponentialShadowMapping,
+    exponentialVarianceShadowMapping and hamburger4MSM over the blurred
+    moment target (made by tests/moment_ref.py, which equals the oracle's
+    own, texel for texel), read bilinearly."""
+    import moment_ref
+    from globalillumination_gb300 import scenes
+
+    Wm, Sm = 48, 96
+    w = scenes.pcss_1080p(width=Wm, height=Wm, map_size=Sm, spheres=10)
+    fr = gi.frame_setup(w.light, w.camera)
+    p, n, i = w.scene.arrays()
+    w.scene.close()
+    mp = w.map_params
+    depth = oracle.shadow_map(p, i, fr.light_mvp, Sm, Sm, mp.bias_mode, mp.constant_bias, mp.offset_factor,
+                              mp.offset_units)
+    pos, nrm = oracle.gbuffer(p, n, i, fr.camera_mvp, Wm, Wm)
+    prm = gi.ShadowParams.defaults(tech)
+    got = oracle.visibility(prm.to_c(fr), depth, Sm, Sm, pos, nrm, Wm, Wm)
+    moments = np.ascontiguousarray(moment_ref.filtered(tech, depth, Sm, Wm), np.float32)
+    _, mqi = moment_ref.quantization()
+    mqi = np.array(mqi, np.float32)
+    lib_all.ref_shadow_moments.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p,
+                                           C.c_float, C.c_void_p]
+    lib_all.ref_shadow_moments.restype = None
+    want = np.empty(Wm * Wm, np.float32)
+    lib_all.ref_shadow_moments(mode, _ptr(moments), Wm, _ptr(pos), _ptr(nrm), Wm, Wm, *(_ptr(x) for x in _mats(fr)),
+                               prm.shadow_intensity, _ptr(mqi), float(moment_ref.TQ0), _ptr(want))
+    diff = got.view(np.uint32) != want.view(np.uint32)
+    assert not diff.any(), f"{int(diff.sum())} of {Wm * Wm} pixels differ"
+    fg = want[pos.reshape(-1, 4)[:, 0] != 0]
+    assert ((fg > prm.shadow_intensity) & (fg < 1.0)).any()
