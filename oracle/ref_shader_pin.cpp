@@ -151,6 +151,47 @@ void ref_pcss(const float* depth, int S, const float* pos, const float* nrm, int
     });
 }
 
+// PlausibleSoftShadow.frag's SAVSM (mode 0) and ESSM (mode 1), with or
+// without the summed-area table: `moments` is the soft app's moment map or
+// its SAT (float4, S x S, read bilinearly), `depth` the light map the blocker
+// search reads.
+void ref_soft_moments(int mode, int sat, const float* depth, const float* moments, int S, const float* pos,
+                      const float* nrm, int W, int H, const float* light_mvp, const float* camera_mv,
+                      const float* normal_matrix, const float* light_position, float intensity,
+                      int blocker_search_size, int kernel_size, int light_source_radius, float* out) {
+    using namespace pin_pcss;
+    const Frame f{depth, S, pos, nrm, W, H, light_mvp, camera_mv, normal_matrix, light_position, intensity};
+    shadowMap = glsl::sampler2D{depth, S, S, 1};
+    SATShadowMap = glsl::sampler2D{moments, S, S, 4, true};
+    vertexMap = glsl::sampler2D{pos, W, H, 4};
+    normalMap = glsl::sampler2D{nrm, W, H, 4};
+    lightMVP = mat4_of(light_mvp);
+    MV = mat4_of(camera_mv);
+    normalMatrix = mat3_of(normal_matrix);
+    lightPosition = glsl::vec3(light_position[0], light_position[1], light_position[2]);
+    shadowIntensity = intensity;
+    zNear = 1;
+    zFar = 1000;
+    windowWidth = W;
+    windowHeight = H;
+    shadowMapWidth = S;
+    shadowMapHeight = S;
+    blockerSearchSize = blocker_search_size;
+    kernelSize = kernel_size;
+    lightSourceRadius = light_source_radius;
+    PCSS = VSSM = MSSM = 0;
+    SAVSM = mode == 0;
+    ESSM = mode == 1;
+    SAT = sat;
+    per_pixel(f, out, [](const glsl::vec2& tc) {
+        f_texcoord = tc;
+        gl_discarded = false;
+        gl_FragColor = glsl::vec4(0.0f);
+        shader_main();
+        return gl_discarded ? 0.0f : gl_FragColor.x;
+    });
+}
+
 // ShadowMapping/Shaders/Shadow.frag (computeHardShadows, ShadowMapping/src/
 // main.cpp:400-414): mode 0 the naive hard test, 1 bilinear PCF, 2 tricubic
 // PCF.

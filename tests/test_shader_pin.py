@@ -220,3 +220,27 @@ def test_moment_lookups_equal_the_reference_shader(lib_all, tech, mode):
     assert not diff.any(), f"{int(diff.sum())} of {Wm * Wm} pixels differ"
     fg = want[pos.reshape(-1, 4)[:, 0] != 0]
     assert ((fg > prm.shadow_intensity) & (fg < 1.0)).any()
+
+
+@pytest.mark.parametrize("tech,mode", [(api.GI_TECH_SAVSM, 0), (api.GI_TECH_ESSM, 1)], ids=["SAVSM", "ESSM"])
+@pytest.mark.parametrize("sat", [False, True], ids=["moment map", "SAT"])
+def test_soft_moments_equal_the_reference_shader(lib_all, frame, tech, mode, sat):
+    """PlausibleSoftShadow.frag's summedAreaVarianceShadowMapping and
+    exponentialSoftShadowMapping over the oracle's moment map or its SAT
+    (which tests/soft_moment_ref.py pins texel for texel), read bilinearly."""
+    fr, depth, pos, nrm = frame
+    prm = gi.ShadowParams.defaults(tech)
+    prm.blocker_search_size, prm.kernel_size, prm.light_radius = 7, 7, 4.0
+    prm.pcss_min_blocker_depth, prm.znear, prm.summed_area_table = 0.99, 1.0, sat
+    c = prm.to_c(fr)
+    got = oracle.visibility(c, depth, S, S, pos, nrm, W, H)
+    moments = np.ascontiguousarray(oracle.soft_moment_map(c, depth, S, S), np.float32)
+    lib_all.ref_soft_moments.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                         C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
+                                         C.c_int, C.c_int, C.c_int, C.c_void_p]
+    lib_all.ref_soft_moments.restype = None
+    want = np.empty(W * H, np.float32)
+    lib_all.ref_soft_moments(mode, int(sat), _ptr(depth), _ptr(moments), S, _ptr(pos), _ptr(nrm), W, H,
+                             *(_ptr(x) for x in _mats(fr)), prm.shadow_intensity, 7, 7, 4, _ptr(want))
+    diff = got.view(np.uint32) != want.view(np.uint32)
+    assert not diff.any(), f"{int(diff.sum())} of {W * H} pixels differ"
